@@ -1,0 +1,128 @@
+/*
+ * rcg — GB300 (sm_103a) implementation of rust-compress's JPEG `--target-ssimulacra2` quality search.
+ *
+ * C ABI. Plain pointers and sizes only; every call returns an rcg_status and never aborts the process. Buffers
+ * passed in are owned by the caller and never freed here. Device memory is owned by an opaque rcg_ctx. A context
+ * holds its own CUDA stream and workspace and is not thread-safe: use one context per calling thread (the
+ * reference runs one search per rayon worker, cli/src/main.rs:57-60). There is no global mutable state.
+ *
+ * Image data: 8-bit samples, interleaved, row-major, no row padding (rc_core::image::Image, core/src/image.rs:103-113).
+ * `channels` is 1 (Gray) or 3 (Rgb) for the encoder and the search (the reference encodes flattened 8-bit Gray/Rgb
+ * images, jpeg/src/encode.rs:424-426); the scorer also takes 2 (GrayAlpha) and 4 (Rgba) and 16-bit samples
+ * (big-endian), as core/src/ssimulacra2.rs:177-221 does.
+ *
+ * Coefficients: the flat form of jpeg::encode::CoefImage (jpeg/src/encode.rs:56-83). Components are stored back to
+ * back (Y, then Cb, then Cr); each holds blocks_w*blocks_h blocks in raster order over the MCU-padded grid, 64
+ * zigzag-ordered int16 per block. Quantization tables are natural order, slot 0 luma, slot 1 chroma.
+ */
+#ifndef RCG_H
+#define RCG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. The reference's rc_core::error::Error::{Invalid, Unsupported} (core/src/error.rs:4-20) map to
+ * RCG_INVALID and RCG_UNSUPPORTED; rcg_last_error() gives the message. */
+typedef enum {
+  RCG_OK = 0,
+  RCG_INVALID = 1,      /* bad sizes, mismatched images, <8x8 for the scorer, null pointers, short buffers */
+  RCG_UNSUPPORTED = 2,  /* a format the path does not handle (e.g. >65535 pixels for JPEG) */
+  RCG_CUDA_ERROR = 3,   /* a CUDA runtime error; the context stays usable if the device does */
+  RCG_TIMEOUT = 4,      /* a bounded device-side wait gave up */
+  RCG_NO_MEMORY = 5     /* device allocation failed */
+} rcg_status;
+
+/* jpeg::encode::Subsampling (jpeg/src/encode.rs:12-20). AUTO is 4:2:0 below quality 90, else 4:4:4. */
+typedef enum { RCG_SUB_AUTO = 0, RCG_SUB_444 = 1, RCG_SUB_422 = 2, RCG_SUB_420 = 3 } rcg_subsampling;
+
+/* jpeg::encode::EncodeOptions (jpeg/src/encode.rs:22-37), minus `background`: the caller flattens alpha first, as
+ * cli/src/pipeline.rs:236 does before the search. */
+typedef struct {
+  int32_t quality;     /* 1..=100 */
+  int32_t subsampling; /* rcg_subsampling */
+  int32_t trellis;     /* nonzero: rate-distortion optimized AC quantization (default on in the reference) */
+} rcg_encode_options;
+
+/* Block-grid layout of the CoefImage that build_coefs produces (jpeg/src/encode.rs:440-443, :511-513). */
+typedef struct {
+  int32_t ncomp;       /* 1 (Gray) or 3 (YCbCr) */
+  int32_t h[3], v[3];  /* sampling factors per component */
+  int32_t blocks_w[3]; /* block-grid width, padded to whole MCUs */
+  int32_t blocks_h[3];
+  int64_t ncoefs;      /* total int16 coefficients over all components (= 64 * total blocks) */
+} rcg_coef_layout;
+
+/* jpeg::target::Found (jpeg/src/target.rs:12-18) plus the trace of evaluated candidates. */
+typedef struct {
+  int32_t quality;
+  double score;
+  int32_t nsteps;         /* candidates evaluated (max quality first, then the bisection steps) */
+  int32_t trace_q[16];    /* quality of each evaluated candidate, in order */
+  double trace_score[16]; /* its SSIMULACRA2 score (-DBL_MAX when it could not be scored) */
+} rcg_found;
+
+typedef struct rcg_ctx rcg_ctx;
+
+/* Context lifetime. `device` is a CUDA device ordinal. */
+int rcg_ctx_create(int device, rcg_ctx** out);
+void rcg_ctx_destroy(rcg_ctx* ctx);
+/* Message of the last failed call on this context ("" if none). Valid until the next call on it. */
+const char* rcg_last_error(const rcg_ctx* ctx);
+/* Run the context's work on a caller stream (a cudaStream_t; NULL restores the context's own stream). */
+int rcg_ctx_set_stream(rcg_ctx* ctx, void* stream);
+void* rcg_ctx_stream(const rcg_ctx* ctx);
+int rcg_ctx_synchronize(rcg_ctx* ctx);
+/* Kernels this context has launched so far (each kernel launch counts once). */
+uint64_t rcg_ctx_launch_count(const rcg_ctx* ctx);
+/* Per-kernel timing with CUDA events around every launch, for profiling: 1 on, 0 off. Off by default. */
+int rcg_ctx_set_profiling(rcg_ctx* ctx, int on);
+/* Accumulated event time of kernel `name` since profiling was switched on. Synchronizes the context. */
+int rcg_ctx_kernel_time(rcg_ctx* ctx, const char* name, uint64_t* launches, double* total_ms);
+
+/* Coefficient layout for an image and options. Replaces nothing in the reference: it sizes the caller-allocated
+ * output buffers that a Rust `Vec<i16>` would otherwise grow (jpeg/src/encode.rs:440-517). */
+int rcg_coef_layout_for(uint32_t width, uint32_t height, int channels, const rcg_encode_options* opts,
+                        rcg_coef_layout* out);
+
+/* rc_core::ssimulacra2::ssimulacra2(reference, distorted) -> Result<f64> (core/src/ssimulacra2.rs:471).
+ * Host buffers of width*height*channels*(depth/8) bytes. Errors as the reference: RCG_INVALID for a size mismatch
+ * (here: impossible, one size is passed), sides < 8, or a non-finite score. */
+int rcg_ssimulacra2(rcg_ctx* ctx, const uint8_t* reference, const uint8_t* distorted, uint32_t width,
+                    uint32_t height, int channels, int depth, double* score);
+/* The same on device buffers (8-bit Gray/Rgb only); no host<->device copies besides the 8-byte score. */
+int rcg_ssimulacra2_device(rcg_ctx* ctx, const uint8_t* d_reference, const uint8_t* d_distorted, uint32_t width,
+                           uint32_t height, int channels, double* score);
+
+/* jpeg::encode::build_coefs(src, opts) -> CoefImage (jpeg/src/encode.rs:426). `src` is 8-bit Gray/Rgb on the host.
+ * `coefs` receives layout.ncoefs int16 (capacity `coefs_len`), `qtables` (nullable) 2*64 bytes. */
+int rcg_build_coefs(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
+                    const rcg_encode_options* opts, int16_t* coefs, size_t coefs_len, uint8_t* qtables);
+
+/* jpeg::decode::reconstruct(ci) -> Result<Image> (jpeg/src/decode.rs:334) for a CoefImage with this library's
+ * layout. `out` receives width*height*ncomp bytes (Gray for 1 component, Rgb for 3). */
+int rcg_reconstruct(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                    const uint8_t* qtables, const int16_t* coefs, uint8_t* out, size_t out_len);
+
+/* The whole `--target-ssimulacra2` search: jpeg::target::find_quality_with(reference, target, max_quality, make,
+ * metric) (jpeg/src/target.rs:29) with make = build_coefs at each quality (cli/src/pipeline.rs:238) and metric =
+ * ssimulacra2(..).unwrap_or(f64::MIN) (cli/src/pipeline.rs:218). Every step (encode, decode, score, bisection
+ * decision) runs on the device; the host only copies the image in and the chosen coefficients out.
+ * `opts->quality` is ignored. `coefs`/`qtables` (nullable) receive the chosen candidate's CoefImage, sized by
+ * rcg_coef_layout_for at the found quality (the layout depends on quality only with RCG_SUB_AUTO). */
+int rcg_search(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels, double target,
+               int max_quality, const rcg_encode_options* opts, rcg_found* found, int16_t* coefs, size_t coefs_len,
+               uint8_t* qtables);
+/* The same with the image already on the device; coefs/qtables (nullable) are device pointers. */
+int rcg_search_device(rcg_ctx* ctx, const uint8_t* d_src, uint32_t width, uint32_t height, int channels,
+                      double target, int max_quality, const rcg_encode_options* opts, rcg_found* found,
+                      int16_t* d_coefs, size_t coefs_len, uint8_t* d_qtables);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RCG_H */

@@ -1,0 +1,177 @@
+"""ctypes binding of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs, where it is
+the checker (or the timed CPU restatement of the reference), never the measured product.
+"""
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+
+def build():
+    r = subprocess.run(["make", "-s", "-C", HERE], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        P, i32 = ctypes.c_void_p, ctypes.c_int
+        pd = ctypes.POINTER(ctypes.c_double)
+        pi = ctypes.POINTER(ctypes.c_int)
+        L.orc_ssimulacra2.argtypes = [P, P, i32, i32, i32, i32, pd, P, pi]
+        L.orc_ssimulacra2_fp64.argtypes = [P, P, i32, i32, i32, i32, pd, P, pi]
+        L.orc_build_coefs.argtypes = [P, i32, i32, i32, i32, i32, i32, P, P]
+        L.orc_coef_layout.argtypes = [i32, i32, i32, i32, i32, pi, P, P, P, P]
+        L.orc_reconstruct.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, pi]
+        L.orc_ac_code_lengths.argtypes = [i32, i32, i32, P, P, P, P, P, P, P]
+        L.orc_search.argtypes = [P, i32, i32, i32, ctypes.c_double, i32, i32, i32, pi, pd, P, P, P, P, pi]
+        L.orc_write_best.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, ctypes.c_long, pi]
+        L.orc_write_best.restype = ctypes.c_long
+        L.orc_round_f32.argtypes = [ctypes.c_float]
+        L.orc_round_f32.restype = ctypes.c_int32
+        L.orc_fdct.argtypes = [P]
+        L.orc_idct.argtypes = [P]
+        L.orc_aan.restype = ctypes.POINTER(ctypes.c_float)
+        L.orc_scale_table.argtypes = [i32, P]
+        L.orc_rdo_quantize_ac.argtypes = [P, ctypes.c_float, P, P, P]
+        L.orc_build_lengths.argtypes = [P, i32, i32, P]
+        L.orc_optimal_sizes.argtypes = [P, P]
+        L.orc_set_threads.argtypes = [i32]
+        L.orc_max_threads.restype = i32
+        _lib = L
+    return _lib
+
+
+def set_threads(n):
+    lib().orc_set_threads(int(n))
+
+
+def max_threads():
+    return int(lib().orc_max_threads())
+
+
+def _img(a):
+    a = np.ascontiguousarray(a)
+    if a.ndim == 2:
+        a = a[:, :, None]
+    h, w, c = a.shape
+    depth = 8
+    if a.dtype == np.uint16:
+        depth = 16
+        a = np.ascontiguousarray(a.astype(">u2"))
+    return a, w, h, c, depth
+
+
+def ssimulacra2(ref, dist, fp64=False, per_scale=False):
+    a, w, h, c, d = _img(ref)
+    b, _, _, _, _ = _img(dist)
+    out = ctypes.c_double()
+    ps = np.zeros((6, 3, 6), dtype=np.float64)
+    ns = ctypes.c_int()
+    f = lib().orc_ssimulacra2_fp64 if fp64 else lib().orc_ssimulacra2
+    rc = f(a.ctypes.data, b.ctypes.data, w, h, c, d, ctypes.byref(out), ps.ctypes.data, ctypes.byref(ns))
+    if rc != 0:
+        raise ValueError("invalid input for SSIMULACRA 2")
+    if per_scale:
+        return out.value, ps[: ns.value]
+    return out.value
+
+
+def layout(w, h, channels, quality, subsampling):
+    nc = ctypes.c_int()
+    hs, vs, bws, bhs = (np.zeros(3, dtype=np.int32) for _ in range(4))
+    rc = lib().orc_coef_layout(w, h, channels, quality, int(subsampling), ctypes.byref(nc), hs.ctypes.data,
+                               vs.ctypes.data, bws.ctypes.data, bhs.ctypes.data)
+    if rc != 0:
+        raise ValueError("bad layout")
+    n = nc.value
+    return dict(ncomp=n, h=hs[:n].copy(), v=vs[:n].copy(), blocks_w=bws[:n].copy(), blocks_h=bhs[:n].copy(),
+                ncoefs=int(sum(bws[i] * bhs[i] for i in range(n)) * 64))
+
+
+def build_coefs(src, quality, subsampling, trellis=True):
+    a, w, h, c, _ = _img(src)
+    lay = layout(w, h, c, quality, subsampling)
+    coefs = np.zeros(lay["ncoefs"], dtype=np.int16)
+    qt = np.zeros((2, 64), dtype=np.uint8)
+    rc = lib().orc_build_coefs(a.ctypes.data, w, h, c, quality, int(subsampling), 1 if trellis else 0,
+                               coefs.ctypes.data, qt.ctypes.data)
+    if rc != 0:
+        raise ValueError("bad input")
+    return coefs, qt, lay
+
+
+def _lay_arrays(lay):
+    n = lay["ncomp"]
+    pad = lambda x: np.ascontiguousarray(np.pad(np.asarray(x, dtype=np.int32), (0, 3 - n)))
+    return n, pad(lay["h"]), pad(lay["v"]), pad(lay["blocks_w"]), pad(lay["blocks_h"])
+
+
+def reconstruct(w, h, lay, qt, coefs):
+    n, hs, vs, bws, bhs = _lay_arrays(lay)
+    qt = np.ascontiguousarray(qt, dtype=np.uint8)
+    coefs = np.ascontiguousarray(coefs, dtype=np.int16)
+    out = np.zeros((h, w, n), dtype=np.uint8)
+    oc = ctypes.c_int()
+    lib().orc_reconstruct(w, h, n, hs.ctypes.data, vs.ctypes.data, bws.ctypes.data, bhs.ctypes.data, qt.ctypes.data,
+                          coefs.ctypes.data, out.ctypes.data, ctypes.byref(oc))
+    return out[:, :, 0] if n == 1 else out
+
+
+def ac_code_lengths(w, h, lay, qt, coefs):
+    n, hs, vs, bws, bhs = _lay_arrays(lay)
+    out = np.zeros((2, 256), dtype=np.uint8)
+    qt = np.ascontiguousarray(qt, dtype=np.uint8)
+    coefs = np.ascontiguousarray(coefs, dtype=np.int16)
+    lib().orc_ac_code_lengths(w, h, n, hs.ctypes.data, vs.ctypes.data, bws.ctypes.data, bhs.ctypes.data,
+                              qt.ctypes.data, coefs.ctypes.data, out.ctypes.data)
+    return out
+
+
+def search(src, target, max_quality=100, subsampling=0, trellis=True):
+    a, w, h, c, _ = _img(src)
+    q = ctypes.c_int()
+    s = ctypes.c_double()
+    tq = np.zeros(16, dtype=np.int32)
+    ts = np.zeros(16, dtype=np.float64)
+    nt = ctypes.c_int()
+    # layout depends on the found quality under Auto: size for the largest
+    cap = max(layout(w, h, c, qq, subsampling)["ncoefs"] for qq in (1, 89, 90, 100))
+    coefs = np.zeros(cap, dtype=np.int16)
+    qt = np.zeros((2, 64), dtype=np.uint8)
+    rc = lib().orc_search(a.ctypes.data, w, h, c, float(target), int(max_quality), int(subsampling),
+                          1 if trellis else 0, ctypes.byref(q), ctypes.byref(s), coefs.ctypes.data, qt.ctypes.data,
+                          tq.ctypes.data, ts.ctypes.data, ctypes.byref(nt))
+    if rc != 0:
+        raise ValueError("bad input")
+    lay = layout(w, h, c, q.value, subsampling)
+    trace = [(int(tq[i]), float(ts[i])) for i in range(nt.value)]
+    return q.value, s.value, coefs[: lay["ncoefs"]].copy(), qt, lay, trace
+
+
+def write_best(w, h, lay, qt, coefs):
+    n, hs, vs, bws, bhs = _lay_arrays(lay)
+    qt = np.ascontiguousarray(qt, dtype=np.uint8)
+    coefs = np.ascontiguousarray(coefs, dtype=np.int16)
+    prog = ctypes.c_int()
+    size = lib().orc_write_best(w, h, n, hs.ctypes.data, vs.ctypes.data, bws.ctypes.data, bhs.ctypes.data,
+                                qt.ctypes.data, coefs.ctypes.data, None, 0, ctypes.byref(prog))
+    out = np.zeros(size, dtype=np.uint8)
+    lib().orc_write_best(w, h, n, hs.ctypes.data, vs.ctypes.data, bws.ctypes.data, bhs.ctypes.data, qt.ctypes.data,
+                         coefs.ctypes.data, out.ctypes.data, size, ctypes.byref(prog))
+    return out.tobytes(), bool(prog.value)

@@ -1,0 +1,620 @@
+// C ABI of rcg (include/rcg.h): contexts, workspace, the host-driven single calls (build_coefs, reconstruct,
+// ssimulacra2) and the device-driven quality search.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "rcg_internal.cuh"
+
+namespace rcg {
+
+// ------------------------------------------------------------------------------------------------ errors, workspace
+
+int fail(rcg_ctx* ctx, int status, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+  return status;
+}
+
+int cuda_fail(rcg_ctx* ctx, cudaError_t e, const char* what) {
+  if (ctx) ctx->last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? RCG_NO_MEMORY : RCG_CUDA_ERROR;
+}
+
+void* workspace(rcg_ctx* ctx, const char* name, size_t bytes) {
+  DeviceBuffer& b = ctx->bufs[name];
+  if (b.ptr && b.bytes >= bytes) return b.ptr;
+  if (b.ptr) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+  }
+  size_t sz = std::max<size_t>(bytes, 256);
+  if (cudaMalloc(&b.ptr, sz) != cudaSuccess) {
+    cudaGetLastError();
+    b.ptr = nullptr;
+    fail(ctx, RCG_NO_MEMORY, std::string("device allocation of ") + std::to_string(sz) + " bytes for " + name);
+    return nullptr;
+  }
+  cudaMemsetAsync(b.ptr, 0, sz, ctx->stream);
+  b.bytes = sz;
+  return b.ptr;
+}
+
+void launch_begin(rcg_ctx* ctx, const char* name, cudaEvent_t* a, cudaEvent_t* b) {
+  (void)name;
+  ctx->launches++;
+  if (!ctx->profiling) return;
+  auto take = [&]() {
+    cudaEvent_t e;
+    if (!ctx->event_pool.empty()) {
+      e = ctx->event_pool.back();
+      ctx->event_pool.pop_back();
+    } else {
+      cudaEventCreate(&e);
+    }
+    return e;
+  };
+  *a = take();
+  *b = take();
+  cudaEventRecord(*a, ctx->stream);
+}
+
+void launch_end(rcg_ctx* ctx, const char* name, cudaEvent_t a, cudaEvent_t b) {
+  if (!ctx->profiling || !a) return;
+  cudaEventRecord(b, ctx->stream);
+  ctx->pending.push_back({name, a, b});
+}
+
+void collect_times(rcg_ctx* ctx) {
+  if (ctx->pending.empty()) return;
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& p : ctx->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      KernelTimes& kt = ctx->ktimes[p.name];
+      kt.launches++;
+      kt.ms += ms;
+    }
+    ctx->event_pool.push_back(p.a);
+    ctx->event_pool.push_back(p.b);
+  }
+  ctx->pending.clear();
+}
+
+// ------------------------------------------------------------------------------------------------ sRGB tables
+
+// core/src/ssimulacra2.rs:172-175 in f64, rounded to f32 as :192 does.
+static double srgb_to_linear(double v) { return v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4); }
+
+void srgb_lut8(float out[256]) {
+  for (int v = 0; v < 256; v++) out[v] = (float)srgb_to_linear((double)v / 255.0);
+}
+
+const float* srgb_lut16_device(rcg_ctx* ctx) {
+  if (ctx->lut16) return ctx->lut16;
+  std::vector<float> lut(65536);
+  for (int v = 0; v < 65536; v++) lut[v] = (float)srgb_to_linear((double)v / 65535.0);
+  float* d = nullptr;
+  if (cudaMalloc(&d, 65536 * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    fail(ctx, RCG_NO_MEMORY, "device allocation of the 16-bit sRGB table");
+    return nullptr;
+  }
+  cudaMemcpy(d, lut.data(), 65536 * sizeof(float), cudaMemcpyHostToDevice);
+  ctx->lut16 = d;
+  return d;
+}
+
+// ------------------------------------------------------------------------------------------------ helpers
+
+static std::mutex g_init_mu;
+
+static int ensure_init(rcg_ctx* ctx) {
+  std::lock_guard<std::mutex> lk(g_init_mu);
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+  return scorer_init(ctx);
+}
+
+static int finish(rcg_ctx* ctx, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, what);
+  e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, what);
+  if (ctx->profiling) collect_times(ctx);
+  ctx->last_error.clear();
+  return RCG_OK;
+}
+
+static void layout_of(int w, int h, int channels, int quality, int subsampling, rcg_coef_layout* out) {
+  StepDesc* st = new StepDesc;
+  host_step_tables(st, quality, subsampling, channels, 0, w, h);
+  std::memset(out, 0, sizeof *out);
+  out->ncomp = st->ncomp;
+  for (int c = 0; c < st->ncomp; c++) {
+    out->h[c] = st->comp[c].h;
+    out->v[c] = st->comp[c].v;
+    out->blocks_w[c] = st->comp[c].bw;
+    out->blocks_h[c] = st->comp[c].bh;
+  }
+  out->ncoefs = st->nblocks * 64;
+  delete st;
+}
+
+// Encoder front half shared by build_coefs and the search: colour planes and the FDCT caches of every sampling
+// layout the options can produce (two for Subsampling::Auto, whose layout depends on the quality).
+struct EncoderSetup {
+  const float* caches[9] = {nullptr};
+  long long max_blocks = 0;
+  long long max_coefs = 0;
+  long long max_plane_bytes = 0;
+};
+
+static int setup_encoder(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, int subsampling,
+                         EncoderSetup* es) {
+  bool kinds[3] = {false, false, false};
+  if (channels == 1) {
+    kinds[2] = true;
+  } else {
+    switch (subsampling) {
+      case RCG_SUB_420: kinds[0] = true; break;
+      case RCG_SUB_422: kinds[1] = true; break;
+      case RCG_SUB_444: kinds[2] = true; break;
+      default: kinds[0] = kinds[2] = true;
+    }
+  }
+  const int hv[3][2] = {{2, 2}, {2, 1}, {1, 1}};
+  int pw_max = 0, ph_max = 0;
+  for (int k = 0; k < 3; k++) {
+    if (!kinds[k]) continue;
+    int hm = channels == 1 ? 1 : hv[k][0], vm = channels == 1 ? 1 : hv[k][1];
+    pw_max = std::max(pw_max, (w + 8 * hm - 1) / (8 * hm) * 8 * hm);
+    ph_max = std::max(ph_max, (h + 8 * vm - 1) / (8 * vm) * 8 * vm);
+  }
+  size_t plane = (size_t)pw_max * ph_max;
+  uint8_t* yp = (uint8_t*)workspace(ctx, "plane_y", plane);
+  uint8_t* cbp = channels == 1 ? nullptr : (uint8_t*)workspace(ctx, "plane_cb", plane);
+  uint8_t* crp = channels == 1 ? nullptr : (uint8_t*)workspace(ctx, "plane_cr", plane);
+  if (!yp || (channels == 3 && (!cbp || !crp))) return RCG_NO_MEMORY;
+  color_pad(ctx, d_src, w, h, channels, pw_max, ph_max, yp, cbp, crp);
+  for (int k = 0; k < 3; k++) {
+    if (!kinds[k]) continue;
+    int hm = channels == 1 ? 1 : hv[k][0], vm = channels == 1 ? 1 : hv[k][1];
+    int pw = (w + 8 * hm - 1) / (8 * hm) * 8 * hm, ph = (h + 8 * vm - 1) / (8 * vm) * 8 * vm;
+    long long blocks = 0, pbytes = 0;
+    for (int c = 0; c < (channels == 1 ? 1 : 3); c++) {
+      int cw = c == 0 ? pw : pw / hm, chh = c == 0 ? ph : ph / vm;
+      int bw = cw / 8, bh = chh / 8;
+      std::string name = "fdct_cache_" + std::to_string(k * 3 + c);
+      float* cache = (float*)workspace(ctx, name.c_str(), (size_t)bw * bh * 64 * sizeof(float));
+      if (!cache) return RCG_NO_MEMORY;
+      const uint8_t* src = c == 0 ? yp : (c == 1 ? cbp : crp);
+      int stride = pw_max;
+      if (c > 0 && hm * vm > 1) {
+        std::string dn = "plane_sub_" + std::to_string(k * 3 + c);
+        uint8_t* sub = (uint8_t*)workspace(ctx, dn.c_str(), (size_t)cw * chh);
+        if (!sub) return RCG_NO_MEMORY;
+        chroma_down(ctx, src, pw_max, pw, ph, hm, vm, sub);
+        src = sub;
+        stride = cw;
+      }
+      fdct_cache(ctx, src, stride, bw, bh, cache);
+      es->caches[k * 3 + c] = cache;
+      blocks += (long long)bw * bh;
+      pbytes += (long long)cw * chh;
+    }
+    es->max_blocks = std::max(es->max_blocks, blocks);
+    es->max_coefs = std::max(es->max_coefs, blocks * 64);
+    es->max_plane_bytes = std::max(es->max_plane_bytes, pbytes);
+  }
+  return RCG_OK;
+}
+
+static int check_image(rcg_ctx* ctx, uint32_t w, uint32_t h, int channels) {
+  if (w == 0 || h == 0) return fail(ctx, RCG_INVALID, "empty image");
+  if (channels != 1 && channels != 3) return fail(ctx, RCG_INVALID, "the JPEG path takes 8-bit Gray or Rgb pixels");
+  if (w > 65535 || h > 65535) return fail(ctx, RCG_UNSUPPORTED, "JPEG dimensions are limited to 65535 pixels");
+  return RCG_OK;
+}
+
+static int check_opts(rcg_ctx* ctx, const rcg_encode_options* o, bool need_quality) {
+  if (!o) return fail(ctx, RCG_INVALID, "null options");
+  if (need_quality && (o->quality < 1 || o->quality > 100)) return fail(ctx, RCG_INVALID, "quality must be 1..=100");
+  if (o->subsampling < RCG_SUB_AUTO || o->subsampling > RCG_SUB_420)
+    return fail(ctx, RCG_INVALID, "unknown subsampling");
+  return RCG_OK;
+}
+
+}  // namespace rcg
+
+using namespace rcg;
+
+extern "C" {
+
+int rcg_ctx_create(int device, rcg_ctx** out) {
+  if (!out) return RCG_INVALID;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || device < 0 || device >= n) {
+    cudaGetLastError();
+    return RCG_CUDA_ERROR;
+  }
+  rcg_ctx* ctx = new (std::nothrow) rcg_ctx;
+  if (!ctx) return RCG_NO_MEMORY;
+  ctx->device = device;
+  if ((e = cudaSetDevice(device)) != cudaSuccess || (e = cudaStreamCreateWithFlags(&ctx->own_stream,
+                                                                                   cudaStreamNonBlocking)) !=
+                                                        cudaSuccess) {
+    cudaGetLastError();
+    delete ctx;
+    return RCG_CUDA_ERROR;
+  }
+  ctx->stream = ctx->own_stream;
+  int rc = ensure_init(ctx);
+  if (rc != RCG_OK) {
+    cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return rc;
+  }
+  *out = ctx;
+  return RCG_OK;
+}
+
+void rcg_ctx_destroy(rcg_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& kv : ctx->bufs)
+    if (kv.second.ptr) cudaFree(kv.second.ptr);
+  if (ctx->lut16) cudaFree(ctx->lut16);
+  for (auto& p : ctx->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (auto e : ctx->event_pool) cudaEventDestroy(e);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+}
+
+const char* rcg_last_error(const rcg_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+int rcg_ctx_set_stream(rcg_ctx* ctx, void* stream) {
+  if (!ctx) return RCG_INVALID;
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+  return RCG_OK;
+}
+
+void* rcg_ctx_stream(const rcg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int rcg_ctx_synchronize(rcg_ctx* ctx) {
+  if (!ctx) return RCG_INVALID;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
+  return RCG_OK;
+}
+
+uint64_t rcg_ctx_launch_count(const rcg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int rcg_ctx_set_profiling(rcg_ctx* ctx, int on) {
+  if (!ctx) return RCG_INVALID;
+  collect_times(ctx);
+  ctx->profiling = on != 0;
+  if (on) ctx->ktimes.clear();
+  return RCG_OK;
+}
+
+int rcg_ctx_kernel_time(rcg_ctx* ctx, const char* name, uint64_t* launches, double* total_ms) {
+  if (!ctx || !name) return RCG_INVALID;
+  collect_times(ctx);
+  auto it = ctx->ktimes.find(name);
+  if (launches) *launches = it == ctx->ktimes.end() ? 0 : it->second.launches;
+  if (total_ms) *total_ms = it == ctx->ktimes.end() ? 0.0 : it->second.ms;
+  return RCG_OK;
+}
+
+int rcg_coef_layout_for(uint32_t width, uint32_t height, int channels, const rcg_encode_options* opts,
+                        rcg_coef_layout* out) {
+  if (!opts || !out || width == 0 || height == 0 || (channels != 1 && channels != 3)) return RCG_INVALID;
+  int q = opts->quality < 1 ? 1 : (opts->quality > 100 ? 100 : opts->quality);
+  layout_of((int)width, (int)height, channels, q, opts->subsampling, out);
+  return RCG_OK;
+}
+
+// ---- scorer
+
+static int score_device_images(rcg_ctx* ctx, const uint8_t* d_ref, const uint8_t* d_dist, int w, int h, int channels,
+                               int depth, double* score) {
+  PyramidDesc pd = make_pyramid(w, h);
+  float* ref_pyr = (float*)workspace(ctx, "ref_pyr", (size_t)pd.floats * sizeof(float));
+  float* dist_pyr = (float*)workspace(ctx, "dist_pyr", (size_t)pd.floats * sizeof(float));
+  double* d_score = (double*)workspace(ctx, "score", sizeof(double));
+  if (!ref_pyr || !dist_pyr || !d_score) return RCG_NO_MEMORY;
+  int rc;
+  if ((rc = to_linear(ctx, d_ref, w, h, channels, depth, ref_pyr)) != RCG_OK) return rc;
+  if ((rc = to_linear(ctx, d_dist, w, h, channels, depth, dist_pyr)) != RCG_OK) return rc;
+  build_pyramid(ctx, pd, ref_pyr);
+  build_pyramid(ctx, pd, dist_pyr);
+  score_pyramids(ctx, pd, ref_pyr, dist_pyr, d_score, nullptr, nullptr);
+  double s = 0.0;
+  cudaMemcpyAsync(&s, d_score, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if ((rc = finish(ctx, "ssimulacra2")) != RCG_OK) return rc;
+  if (!std::isfinite(s)) return fail(ctx, RCG_INVALID, "SSIMULACRA 2 produced a non-finite score");
+  *score = s;
+  return RCG_OK;
+}
+
+int rcg_ssimulacra2(rcg_ctx* ctx, const uint8_t* reference, const uint8_t* distorted, uint32_t width,
+                    uint32_t height, int channels, int depth, double* score) {
+  if (!ctx) return RCG_INVALID;
+  if (!reference || !distorted || !score) return fail(ctx, RCG_INVALID, "null pointer");
+  if (channels < 1 || channels > 4 || (depth != 8 && depth != 16))
+    return fail(ctx, RCG_INVALID, "channels must be 1..4 and depth 8 or 16");
+  if (width < (uint32_t)kMinSide || height < (uint32_t)kMinSide)
+    return fail(ctx, RCG_INVALID, "SSIMULACRA 2 needs at least 8x8 pixels");
+  cudaSetDevice(ctx->device);
+  size_t bytes = (size_t)width * height * channels * (depth / 8);
+  uint8_t* d_a = (uint8_t*)workspace(ctx, "img_a", bytes);
+  uint8_t* d_b = (uint8_t*)workspace(ctx, "img_b", bytes);
+  if (!d_a || !d_b) return RCG_NO_MEMORY;
+  cudaMemcpyAsync(d_a, reference, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(d_b, distorted, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  return score_device_images(ctx, d_a, d_b, (int)width, (int)height, channels, depth, score);
+}
+
+int rcg_ssimulacra2_device(rcg_ctx* ctx, const uint8_t* d_reference, const uint8_t* d_distorted, uint32_t width,
+                           uint32_t height, int channels, double* score) {
+  if (!ctx) return RCG_INVALID;
+  if (!d_reference || !d_distorted || !score) return fail(ctx, RCG_INVALID, "null pointer");
+  if (channels != 1 && channels != 3) return fail(ctx, RCG_INVALID, "device scorer takes 8-bit Gray or Rgb");
+  if (width < (uint32_t)kMinSide || height < (uint32_t)kMinSide)
+    return fail(ctx, RCG_INVALID, "SSIMULACRA 2 needs at least 8x8 pixels");
+  cudaSetDevice(ctx->device);
+  return score_device_images(ctx, d_reference, d_distorted, (int)width, (int)height, channels, 8, score);
+}
+
+// ---- encoder
+
+int rcg_build_coefs(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
+                    const rcg_encode_options* opts, int16_t* coefs, size_t coefs_len, uint8_t* qtables) {
+  if (!ctx) return RCG_INVALID;
+  int rc;
+  if ((rc = check_image(ctx, width, height, channels)) != RCG_OK) return rc;
+  if ((rc = check_opts(ctx, opts, true)) != RCG_OK) return rc;
+  if (!src || !coefs) return fail(ctx, RCG_INVALID, "null pointer");
+  int w = (int)width, h = (int)height;
+  StepDesc* st = new StepDesc;
+  host_step_tables(st, opts->quality, opts->subsampling, channels, opts->trellis, w, h);
+  long long ncoefs = st->nblocks * 64;
+  if ((long long)coefs_len < ncoefs) {
+    delete st;
+    return fail(ctx, RCG_INVALID, "coefficient buffer too short");
+  }
+  cudaSetDevice(ctx->device);
+  size_t bytes = (size_t)w * h * channels;
+  uint8_t* d_src = (uint8_t*)workspace(ctx, "img_a", bytes);
+  int16_t* d_coefs = (int16_t*)workspace(ctx, "coefs_single", (size_t)ncoefs * 2);
+  StepDesc* d_st = (StepDesc*)workspace(ctx, "step_single", sizeof(StepDesc));
+  if (!d_src || !d_coefs || !d_st) {
+    delete st;
+    return RCG_NO_MEMORY;
+  }
+  st->coefs = d_coefs;
+  cudaMemcpyAsync(d_src, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(d_st, st, sizeof(StepDesc), cudaMemcpyHostToDevice, ctx->stream);
+  EncoderSetup es;
+  // Only this quality's layout is needed: pin Auto to what it resolves to.
+  int sub = opts->subsampling;
+  if (channels == 3 && sub == RCG_SUB_AUTO) sub = opts->quality < 90 ? RCG_SUB_420 : RCG_SUB_444;
+  if ((rc = setup_encoder(ctx, d_src, w, h, channels, sub, &es)) != RCG_OK) {
+    delete st;
+    return rc;
+  }
+  quantize(ctx, d_st, es.caches, st->nblocks);
+  rate_tables(ctx, d_st);
+  trellis(ctx, d_st, es.caches, st->nblocks);
+  cudaMemcpyAsync(coefs, d_coefs, (size_t)ncoefs * 2, cudaMemcpyDeviceToHost, ctx->stream);
+  if (qtables) {
+    std::memcpy(qtables, st->qt[0], 64);
+    std::memcpy(qtables + 64, st->qt[1], 64);
+  }
+  cudaStreamSynchronize(ctx->stream);  // the host StepDesc must outlive the async upload
+  delete st;
+  return finish(ctx, "build_coefs");
+}
+
+// ---- decoder
+
+int rcg_reconstruct(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                    const uint8_t* qtables, const int16_t* coefs, uint8_t* out, size_t out_len) {
+  if (!ctx) return RCG_INVALID;
+  if (!layout || !qtables || !coefs || !out) return fail(ctx, RCG_INVALID, "null pointer");
+  if (width == 0 || height == 0) return fail(ctx, RCG_INVALID, "empty image");
+  int nc = layout->ncomp;
+  if (nc != 1 && nc != 3) return fail(ctx, RCG_UNSUPPORTED, "reconstruct takes 1 or 3 components");
+  int w = (int)width, h = (int)height;
+  StepDesc* st = new StepDesc;
+  std::memset(st, 0, sizeof *st);
+  st->active = 1;
+  st->ncomp = nc;
+  int hmax = 1, vmax = 1;
+  for (int c = 0; c < nc; c++) {
+    hmax = std::max(hmax, (int)layout->h[c]);
+    vmax = std::max(vmax, (int)layout->v[c]);
+  }
+  st->hmax = hmax;
+  st->vmax = vmax;
+  long long blk = 0, poff = 0;
+  int mcus_x = (w + 8 * hmax - 1) / (8 * hmax), mcus_y = (h + 8 * vmax - 1) / (8 * vmax);
+  for (int c = 0; c < nc; c++) {
+    CompDesc& cd = st->comp[c];
+    cd.h = layout->h[c];
+    cd.v = layout->v[c];
+    cd.bw = layout->blocks_w[c];
+    cd.bh = layout->blocks_h[c];
+    cd.cls = c == 0 ? 0 : 1;
+    if (cd.h < 1 || cd.v < 1 || hmax % cd.h || vmax % cd.v) {
+      delete st;
+      return fail(ctx, RCG_UNSUPPORTED, "non-integral chroma subsampling ratio");
+    }
+    if (cd.bw < mcus_x * cd.h || cd.bh < mcus_y * cd.v) {
+      delete st;
+      return fail(ctx, RCG_INVALID, "block grid smaller than the MCU grid");
+    }
+    cd.blk0 = blk;
+    cd.plane_off = poff;
+    blk += (long long)cd.bw * cd.bh;
+    poff += (long long)cd.bw * 8 * cd.bh * 8;
+  }
+  st->nblocks = blk;
+  if (layout->ncoefs != blk * 64) {
+    delete st;
+    return fail(ctx, RCG_INVALID, "layout.ncoefs does not match the block grids");
+  }
+  if (out_len < (size_t)w * h * nc) {
+    delete st;
+    return fail(ctx, RCG_INVALID, "output buffer too short");
+  }
+  // idct_planes multipliers from the given tables (jpeg/src/decode.rs:1316-1321)
+  fill_mult(st, qtables, nc == 1 ? 1 : 2);
+  cudaSetDevice(ctx->device);
+  int16_t* d_coefs = (int16_t*)workspace(ctx, "coefs_single", (size_t)blk * 64 * 2);
+  uint8_t* d_planes = (uint8_t*)workspace(ctx, "dec_planes_single", (size_t)poff);
+  uint8_t* d_out = (uint8_t*)workspace(ctx, "img_b", (size_t)w * h * nc);
+  StepDesc* d_st = (StepDesc*)workspace(ctx, "step_single", sizeof(StepDesc));
+  if (!d_coefs || !d_planes || !d_out || !d_st) {
+    delete st;
+    return RCG_NO_MEMORY;
+  }
+  cudaMemcpyAsync(d_coefs, coefs, (size_t)blk * 64 * 2, cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(d_st, st, sizeof(StepDesc), cudaMemcpyHostToDevice, ctx->stream);
+  dequant_idct(ctx, d_st, d_coefs, d_planes, blk);
+  upsample_color(ctx, d_st, d_planes, w, h, d_out, nullptr);
+  cudaMemcpyAsync(out, d_out, (size_t)w * h * nc, cudaMemcpyDeviceToHost, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  delete st;
+  return finish(ctx, "reconstruct");
+}
+
+// ---- search
+
+static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, double target, int max_q,
+                       int subsampling, int trellis_on, rcg_found* found, int16_t* d_coefs_out, size_t coefs_len,
+                       uint8_t* d_qt_out, int16_t* h_coefs_out, uint8_t* h_qt_out) {
+  int rc;
+  PyramidDesc pd = make_pyramid(w, h);
+  float* ref_pyr = (float*)workspace(ctx, "ref_pyr", (size_t)pd.floats * sizeof(float));
+  float* dist_pyr = (float*)workspace(ctx, "dist_pyr", (size_t)pd.floats * sizeof(float));
+  double* d_score = (double*)workspace(ctx, "score", sizeof(double));
+  SearchState* d_ss = (SearchState*)workspace(ctx, "search_state", sizeof(SearchState));
+  StepDesc* d_st = (StepDesc*)workspace(ctx, "step_search", sizeof(StepDesc));
+  if (!ref_pyr || !dist_pyr || !d_score || !d_ss || !d_st) return RCG_NO_MEMORY;
+  // Quality-independent work, once per search: the reference image's linear pyramid, colour planes, FDCTs.
+  if ((rc = to_linear(ctx, d_src, w, h, channels, 8, ref_pyr)) != RCG_OK) return rc;
+  build_pyramid(ctx, pd, ref_pyr);
+  EncoderSetup es;
+  if ((rc = setup_encoder(ctx, d_src, w, h, channels, subsampling, &es)) != RCG_OK) return rc;
+  int max_steps = 1;
+  for (int span = max_q; span > 1; span = (span + 1) / 2) max_steps++;
+  max_steps = std::min(max_steps, kMaxSteps);
+  int16_t* slots = (int16_t*)workspace(ctx, "coef_slots", (size_t)es.max_coefs * 2 * max_steps);
+  uint8_t* planes = (uint8_t*)workspace(ctx, "dec_planes", (size_t)es.max_plane_bytes);
+  if (!slots || !planes) return RCG_NO_MEMORY;
+  SearchState hs;
+  std::memset(&hs, 0, sizeof hs);
+  hs.lo = 1;
+  hs.hi = max_q;
+  hs.step = 0;
+  hs.qs[0] = max_q;
+  hs.target = target;
+  hs.max_q = max_q;
+  hs.subsampling = subsampling;
+  hs.trellis = trellis_on;
+  hs.channels = channels;
+  hs.best_q = max_q;
+  cudaMemcpyAsync(d_ss, &hs, sizeof hs, cudaMemcpyHostToDevice, ctx->stream);
+  for (int s = 0; s < max_steps; s++) {
+    step_tables(ctx, d_ss, d_st, w, h, slots, es.max_coefs);
+    quantize(ctx, d_st, es.caches, es.max_blocks);
+    rate_tables(ctx, d_st);
+    trellis(ctx, d_st, es.caches, es.max_blocks);
+    dequant_idct(ctx, d_st, nullptr, planes, es.max_blocks);
+    upsample_color(ctx, d_st, planes, w, h, nullptr, dist_pyr);
+    build_pyramid_gated(ctx, pd, dist_pyr, d_st);
+    score_pyramids(ctx, pd, ref_pyr, dist_pyr, d_score, d_ss, d_st);
+  }
+  cudaMemcpyAsync(&hs, d_ss, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream);
+  if ((rc = finish(ctx, "search")) != RCG_OK) return rc;
+  if (!hs.done) return fail(ctx, RCG_TIMEOUT, "bisection did not finish within the step budget");
+  found->quality = hs.best_q;
+  found->score = hs.best_score;
+  found->nsteps = 0;
+  for (int s = 0; s < kMaxSteps && s <= hs.step; s++) {
+    found->trace_q[s] = hs.qs[s];
+    found->trace_score[s] = hs.scores[s];
+    found->nsteps = s + 1;
+  }
+  rcg_coef_layout lay;
+  layout_of(w, h, channels, hs.best_q, subsampling, &lay);
+  const int16_t* best = slots + (size_t)hs.best_step * es.max_coefs;
+  if (d_coefs_out || h_coefs_out) {
+    if ((long long)coefs_len < lay.ncoefs) return fail(ctx, RCG_INVALID, "coefficient buffer too short");
+    if (d_coefs_out)
+      cudaMemcpyAsync(d_coefs_out, best, (size_t)lay.ncoefs * 2, cudaMemcpyDeviceToDevice, ctx->stream);
+    else
+      cudaMemcpyAsync(h_coefs_out, best, (size_t)lay.ncoefs * 2, cudaMemcpyDeviceToHost, ctx->stream);
+  }
+  uint8_t qt[128];
+  qtables_for(hs.best_q, qt);
+  if (h_qt_out) std::memcpy(h_qt_out, qt, 128);
+  if (d_qt_out) cudaMemcpyAsync(d_qt_out, qt, 128, cudaMemcpyHostToDevice, ctx->stream);
+  return finish(ctx, "search output");
+}
+
+int rcg_search(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels, double target,
+               int max_quality, const rcg_encode_options* opts, rcg_found* found, int16_t* coefs, size_t coefs_len,
+               uint8_t* qtables) {
+  if (!ctx) return RCG_INVALID;
+  int rc;
+  if ((rc = check_image(ctx, width, height, channels)) != RCG_OK) return rc;
+  if ((rc = check_opts(ctx, opts, false)) != RCG_OK) return rc;
+  if (!src || !found) return fail(ctx, RCG_INVALID, "null pointer");
+  if (width < (uint32_t)kMinSide || height < (uint32_t)kMinSide)
+    return fail(ctx, RCG_UNSUPPORTED, "--target-ssimulacra2 needs an image of at least 8x8 pixels");
+  if (!(target == target)) return fail(ctx, RCG_INVALID, "target is NaN");
+  int max_q = std::max(1, std::min(max_quality, 100));
+  cudaSetDevice(ctx->device);
+  size_t bytes = (size_t)width * height * channels;
+  uint8_t* d_src = (uint8_t*)workspace(ctx, "img_src", bytes);
+  if (!d_src) return RCG_NO_MEMORY;
+  cudaMemcpyAsync(d_src, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  return search_impl(ctx, d_src, (int)width, (int)height, channels, target, max_q, opts->subsampling,
+                     opts->trellis, found, nullptr, coefs_len, nullptr, coefs, qtables);
+}
+
+int rcg_search_device(rcg_ctx* ctx, const uint8_t* d_src, uint32_t width, uint32_t height, int channels,
+                      double target, int max_quality, const rcg_encode_options* opts, rcg_found* found,
+                      int16_t* d_coefs, size_t coefs_len, uint8_t* d_qtables) {
+  if (!ctx) return RCG_INVALID;
+  int rc;
+  if ((rc = check_image(ctx, width, height, channels)) != RCG_OK) return rc;
+  if ((rc = check_opts(ctx, opts, false)) != RCG_OK) return rc;
+  if (!d_src || !found) return fail(ctx, RCG_INVALID, "null pointer");
+  if (width < (uint32_t)kMinSide || height < (uint32_t)kMinSide)
+    return fail(ctx, RCG_UNSUPPORTED, "--target-ssimulacra2 needs an image of at least 8x8 pixels");
+  if (!(target == target)) return fail(ctx, RCG_INVALID, "target is NaN");
+  int max_q = std::max(1, std::min(max_quality, 100));
+  cudaSetDevice(ctx->device);
+  return search_impl(ctx, d_src, (int)width, (int)height, channels, target, max_q, opts->subsampling, opts->trellis,
+                     found, d_coefs, coefs_len, d_qtables, nullptr, nullptr);
+}
+
+}  // extern "C"

@@ -1,0 +1,863 @@
+// JPEG encoder and decoder kernels of the quality search (K1-K7).
+//
+// Bit-exactness: every f32 operation the reference performs is written as an explicit round-to-nearest intrinsic
+// (__fadd_rn, __fsub_rn, __fmul_rn, __fdiv_rn) in the reference's order, so no FMA contraction can change a result
+// (rustc never contracts). The translation unit is also compiled with -fmad=false as a second guard. Integer steps
+// (colour conversion, subsampling, upsampling, histograms) are exact by construction.
+//
+// Layouts in HBM:
+//   padded planes      u8, row-major, stride = padded width (the MCU-padded grid of jpeg/src/encode.rs:440-443)
+//   FDCT cache         f32, [64][nblocks] per component: zigzag coefficient k of block b at k*nblocks + b, so a
+//                      thread-per-block kernel reads one coalesced row per coefficient. Quality-independent: the
+//                      reference recomputes it for every candidate (jpeg/src/encode.rs:189-196).
+//   coefficients       i16, the flat CoefImage: components back to back, 64 zigzag values per block.
+//   decoded planes     u8, one per component, stride blocks_w*8 (jpeg/src/decode.rs:1322-1323).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "rcg_internal.cuh"
+
+namespace rcg {
+
+// ------------------------------------------------------------------------------------------------ tables
+
+// jpeg/src/lib.rs:14-19
+__host__ __device__ inline int zigzag(int k) {
+  constexpr int Z[64] = {0,  1,  8,  16, 9,  2,  3,  10, 17, 24, 32, 25, 18, 11, 4,  5,  12, 19, 26, 33, 40, 48,
+                         41, 34, 27, 20, 13, 6,  7,  14, 21, 28, 35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23,
+                         30, 37, 44, 51, 58, 59, 52, 45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63};
+  return Z[k];
+}
+
+// jpeg/src/dct.rs:8 (AAN scale factors)
+__host__ __device__ inline float aan(int i) {
+  constexpr float A[8] = {1.0f, 1.3870398f, 1.306563f, 1.1758756f, 1.0f, 0.78569495f, 0.5411961f, 0.27589938f};
+  return A[i];
+}
+
+// jpeg/src/quality.rs:26-35
+__host__ __device__ inline uint8_t perceptual_q(int i) {
+  constexpr uint8_t P[64] = {16, 16, 16,  18,  25,  37,  56,  85,  16, 17, 20,  27,  34,  40,  53,  75,
+                             16, 20, 24,  31,  43,  62,  91,  135, 18, 27, 31,  40,  53,  74,  106, 156,
+                             25, 34, 43,  53,  69,  94,  131, 189, 37, 40, 62,  74,  94,  124, 169, 238,
+                             56, 53, 91,  106, 131, 169, 226, 255, 85, 75, 135, 156, 189, 238, 255, 255};
+  return P[i];
+}
+
+// Exact f32 arithmetic on host and device: round-to-nearest, never contracted.
+__host__ __device__ inline float fadd(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fadd_rn(a, b);
+#else
+  volatile float r = a + b;
+  return r;
+#endif
+}
+__host__ __device__ inline float fsub(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fsub_rn(a, b);
+#else
+  volatile float r = a - b;
+  return r;
+#endif
+}
+__host__ __device__ inline float fmul(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fmul_rn(a, b);
+#else
+  volatile float r = a * b;
+  return r;
+#endif
+}
+__host__ __device__ inline float fdiv(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fdiv_rn(a, b);
+#else
+  volatile float r = a / b;
+  return r;
+#endif
+}
+
+// jpeg/src/dct.rs:125-129: round half to even for |x| < 2^22; wrapping integer arithmetic beyond, as the reference.
+__device__ __forceinline__ int round_f32(float x) {
+  return (int)((unsigned)__float_as_int(__fadd_rn(x, 12582912.0f)) - 0x4B400000u);
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
+
+// jpeg/src/quality.rs:6-15 (scale_table over PERCEPTUAL_Q; luma_table == chroma_table, :37-43)
+__host__ __device__ inline void scale_table(int quality, uint8_t* out) {
+  unsigned q = (unsigned)(quality < 1 ? 1 : (quality > 100 ? 100 : quality));
+  unsigned scale = q < 50 ? 5000 / q : 200 - 2 * q;
+  for (int i = 0; i < 64; i++) {
+    unsigned v = ((unsigned)perceptual_q(i) * scale + 50) / 100;
+    out[i] = (uint8_t)(v < 1 ? 1 : (v > 255 ? 255 : v));
+  }
+}
+
+// Sampling factors build_coefs chooses (jpeg/src/encode.rs:428-439).
+__host__ __device__ inline void sampling(int channels, int subsampling, int quality, int* hmax, int* vmax) {
+  if (channels == 1) {
+    *hmax = 1;
+    *vmax = 1;
+    return;
+  }
+  switch (subsampling) {
+    case RCG_SUB_420: *hmax = 2; *vmax = 2; break;
+    case RCG_SUB_422: *hmax = 2; *vmax = 1; break;
+    case RCG_SUB_444: *hmax = 1; *vmax = 1; break;
+    default:
+      if (quality < 90) { *hmax = 2; *vmax = 2; } else { *hmax = 1; *vmax = 1; }
+  }
+}
+
+// FDCT cache slot of a component for a sampling layout: 3 caches (Y, Cb, Cr) per layout kind.
+__host__ __device__ inline int layout_kind(int hmax, int vmax) { return hmax == 2 ? (vmax == 2 ? 0 : 1) : 2; }
+
+// The per-quality tables of one candidate: quantization tables (jpeg/src/quality.rs), fdct divisors
+// (jpeg/src/encode.rs:174-183), dequantization multipliers (jpeg/src/decode.rs:1316-1321), the Rdo parameters that
+// do not depend on the rate model (jpeg/src/rdo.rs:28-45), and the block layout (jpeg/src/encode.rs:440-517).
+// Shared by the host (single calls) and the device (search steps) so both produce identical bits.
+__host__ __device__ inline void fill_step(StepDesc* st, int quality, int subsampling, int channels, int trellis, int w,
+                                          int h) {
+  const float kappa = 0.02f;  // TRELLIS_KAPPA, jpeg/src/encode.rs:42
+  st->quality = quality;
+  st->use_trellis = (trellis && quality < 100) ? 1 : 0;
+  int hmax, vmax;
+  sampling(channels, subsampling, quality, &hmax, &vmax);
+  st->hmax = hmax;
+  st->vmax = vmax;
+  int pw = (w + 8 * hmax - 1) / (8 * hmax) * 8 * hmax;
+  int ph = (h + 8 * vmax - 1) / (8 * vmax) * 8 * vmax;
+  st->ncomp = channels == 1 ? 1 : 3;
+  long long blk = 0, poff = 0;
+  int kind = layout_kind(hmax, vmax);
+  for (int c = 0; c < st->ncomp; c++) {
+    CompDesc& cd = st->comp[c];
+    cd.h = c == 0 ? hmax : 1;
+    cd.v = c == 0 ? vmax : 1;
+    cd.bw = c == 0 ? pw / 8 : pw / hmax / 8;
+    cd.bh = c == 0 ? ph / 8 : ph / vmax / 8;
+    cd.cls = c == 0 ? 0 : 1;
+    cd.cache = kind * 3 + c;
+    cd.blk0 = blk;
+    cd.plane_off = poff;
+    blk += (long long)cd.bw * cd.bh;
+    poff += (long long)cd.bw * 8 * cd.bh * 8;
+  }
+  st->nblocks = blk;
+  for (int cls = 0; cls < 2; cls++) {
+    uint8_t* qt = st->qt[cls];
+    scale_table(quality, qt);
+    // fdct_divisors: d[u*8+v] = 1 / (q[v*8+u] * AAN[u] * AAN[v] * 8), stored here per zigzag position.
+    float div[64];
+    for (int v = 0; v < 8; v++)
+      for (int u = 0; u < 8; u++)
+        div[u * 8 + v] = fdiv(1.0f, fmul(fmul(fmul((float)qt[v * 8 + u], aan(u)), aan(v)), 8.0f));
+    for (int k = 0; k < 64; k++) {
+      int n = zigzag(k);
+      st->divz[cls][k] = div[(n % 8) * 8 + n / 8];
+    }
+    // idct_planes: mult[v][u] = q[v*8+u] * AAN[u] * AAN[v]
+    for (int v = 0; v < 8; v++)
+      for (int u = 0; u < 8; u++) st->mult[cls][v * 8 + u] = fmul(fmul((float)qt[v * 8 + u], aan(u)), aan(v));
+    // Rdo::new: q per zigzag position, median of q[1..] (sorted, index 31), w = (median/q)^1, lambda.
+    float sorted[63];
+    for (int k = 0; k < 64; k++) st->rq[cls][k] = (float)qt[zigzag(k)];
+    for (int k = 1; k < 64; k++) sorted[k - 1] = st->rq[cls][k];
+    for (int i = 1; i < 63; i++) {
+      float x = sorted[i];
+      int j = i - 1;
+      while (j >= 0 && sorted[j] > x) {
+        sorted[j + 1] = sorted[j];
+        j--;
+      }
+      sorted[j + 1] = x;
+    }
+    float median = sorted[31];
+    st->rw[cls][0] = 1.0f;
+    // FREQ_WEIGHT_GAMMA is 1.0 (jpeg/src/rdo.rs:12) and pow(x, 1) == x, so w = median / q exactly.
+    for (int k = 1; k < 64; k++) st->rw[cls][k] = fdiv(median, st->rq[cls][k]);
+    st->lambda[cls] = fmul(fmul(kappa, median), median);
+  }
+}
+
+void fill_mult(StepDesc* st, const uint8_t* qtables, int ntables) {
+  for (int cls = 0; cls < 2; cls++) {
+    const uint8_t* qt = qtables + 64 * (cls < ntables ? cls : 0);
+    std::memcpy(st->qt[cls], qt, 64);
+    for (int v = 0; v < 8; v++)
+      for (int u = 0; u < 8; u++) st->mult[cls][v * 8 + u] = fmul(fmul((float)qt[v * 8 + u], aan(u)), aan(v));
+  }
+}
+
+void qtables_for(int quality, uint8_t* out128) {
+  scale_table(quality, out128);
+  scale_table(quality, out128 + 64);
+}
+
+void host_step_tables(StepDesc* st, int quality, int subsampling, int channels, int trellis, int w, int h) {
+  std::memset(st, 0, sizeof *st);
+  st->active = 1;
+  fill_step(st, quality, subsampling, channels, trellis, w, h);
+}
+
+struct CacheSet {
+  const float* p[9];
+};
+
+// Locate the component of a global block index.
+__device__ __forceinline__ int comp_of(const StepDesc* st, long long gb) {
+  int c = 0;
+  if (st->ncomp > 1 && gb >= st->comp[1].blk0) c = gb >= st->comp[2].blk0 ? 2 : 1;
+  return c;
+}
+
+// ------------------------------------------------------------------------------------------------ K1 colour + pad
+
+// jpeg/src/encode.rs:451-477: edge-replicated Y/Cb/Cr planes over the padded grid (Gray: Y only).
+__global__ void k_color_pad(const uint8_t* __restrict__ src, int w, int h, int channels, int pw, int ph,
+                            uint8_t* __restrict__ yp, uint8_t* __restrict__ cbp, uint8_t* __restrict__ crp) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= pw) return;
+  for (int r = blockIdx.y; r < ph; r += gridDim.y) {
+    int sr = min(r, h - 1), sx = min(x, w - 1);
+    size_t o = (size_t)r * pw + x;
+    if (channels == 1) {
+      yp[o] = src[(size_t)sr * w + sx];
+      continue;
+    }
+    size_t i = ((size_t)sr * w + sx) * 3;
+    int rr = src[i], gg = src[i + 1], bb = src[i + 2];
+    yp[o] = (uint8_t)((19595 * rr + 38470 * gg + 7471 * bb + 32768) >> 16);
+    cbp[o] = (uint8_t)((-11059 * rr - 21709 * gg + 32768 * bb + (128 << 16) + 32767) >> 16);
+    crp[o] = (uint8_t)((32768 * rr - 27439 * gg - 5329 * bb + (128 << 16) + 32767) >> 16);
+  }
+}
+
+int color_pad(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, int pw, int ph, uint8_t* d_y,
+              uint8_t* d_cb, uint8_t* d_cr) {
+  dim3 grid((pw + 255) / 256, std::min(ph, 65535));
+  RCG_LAUNCH(ctx, "color_pad", k_color_pad, grid, 256, 0, d_src, w, h, channels, pw, ph, d_y, d_cb, d_cr);
+  return RCG_OK;
+}
+
+// jpeg/src/encode.rs:478-499 (down): (sum + n/2) / n over fx*fy samples. Source stride pw, output (pw/fx)x(ph/fy).
+__global__ void k_chroma_down(const uint8_t* __restrict__ p, int stride, int pw, int ph, int fx, int fy,
+                              uint8_t* __restrict__ o) {
+  int cw = pw / fx, ch = ph / fy;
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= cw) return;
+  for (int r = blockIdx.y; r < ch; r += gridDim.y) {
+    unsigned s = 0;
+    for (int dy = 0; dy < fy; dy++)
+      for (int dx = 0; dx < fx; dx++) s += p[(size_t)(fy * r + dy) * stride + fx * x + dx];
+    unsigned n = (unsigned)(fx * fy);
+    o[(size_t)r * cw + x] = (uint8_t)((s + n / 2) / n);
+  }
+}
+
+int chroma_down(rcg_ctx* ctx, const uint8_t* d_src, int src_stride, int pw, int ph, int fx, int fy, uint8_t* d_dst) {
+  dim3 grid((pw / fx + 255) / 256, std::min(ph / fy, 65535));
+  RCG_LAUNCH(ctx, "chroma_down", k_chroma_down, grid, 256, 0, d_src, src_stride, pw, ph, fx, fy, d_dst);
+  return RCG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------ K2 FDCT cache
+
+// jpeg/src/dct.rs:20-57 (fdct_pass) on column j of a row-major 8x8 block held in registers.
+__device__ __forceinline__ void fdct_pass(float (&d)[64]) {
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    float d0 = d[0 * 8 + j], d1 = d[1 * 8 + j], d2 = d[2 * 8 + j], d3 = d[3 * 8 + j];
+    float d4 = d[4 * 8 + j], d5 = d[5 * 8 + j], d6 = d[6 * 8 + j], d7 = d[7 * 8 + j];
+    float tmp0 = fadd(d0, d7), tmp7 = fsub(d0, d7), tmp1 = fadd(d1, d6), tmp6 = fsub(d1, d6);
+    float tmp2 = fadd(d2, d5), tmp5 = fsub(d2, d5), tmp3 = fadd(d3, d4), tmp4 = fsub(d3, d4);
+    float tmp10 = fadd(tmp0, tmp3), tmp13 = fsub(tmp0, tmp3), tmp11 = fadd(tmp1, tmp2), tmp12 = fsub(tmp1, tmp2);
+    d[0 * 8 + j] = fadd(tmp10, tmp11);
+    d[4 * 8 + j] = fsub(tmp10, tmp11);
+    float z1 = fmul(fadd(tmp12, tmp13), 0.70710677f);
+    d[2 * 8 + j] = fadd(tmp13, z1);
+    d[6 * 8 + j] = fsub(tmp13, z1);
+    float t10 = fadd(tmp4, tmp5), t11 = fadd(tmp5, tmp6), t12 = fadd(tmp6, tmp7);
+    float z5 = fmul(fsub(t10, t12), 0.38268343f);
+    float z2 = fadd(fmul(0.5411961f, t10), z5);
+    float z4 = fadd(fmul(1.306563f, t12), z5);
+    float z3 = fmul(t11, 0.70710677f);
+    float z11 = fadd(tmp7, z3), z13 = fsub(tmp7, z3);
+    d[5 * 8 + j] = fadd(z13, z2);
+    d[3 * 8 + j] = fsub(z13, z2);
+    d[1 * 8 + j] = fadd(z11, z4);
+    d[7 * 8 + j] = fsub(z11, z4);
+  }
+}
+
+__device__ __forceinline__ void transpose8(float (&b)[64]) {
+#pragma unroll
+  for (int i = 0; i < 8; i++)
+#pragma unroll
+    for (int j = i + 1; j < 8; j++) {
+      float t = b[i * 8 + j];
+      b[i * 8 + j] = b[j * 8 + i];
+      b[j * 8 + i] = t;
+    }
+}
+
+// One thread per block: level shift (x - 128), FDCT (jpeg/src/dct.rs:59-65), store in zigzag order
+// (flat[ZZ_T[k]], jpeg/src/encode.rs:201-211) as cache[k*nb + b].
+__global__ void k_fdct_cache(const uint8_t* __restrict__ plane, int stride, int bw, int bh, float* __restrict__ cache) {
+  long long nb = (long long)bw * bh;
+  long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  int by = (int)(b / bw), bx = (int)(b % bw);
+  float blk[64];
+#pragma unroll
+  for (int y = 0; y < 8; y++) {
+    const uint8_t* src = plane + (size_t)(by * 8 + y) * stride + bx * 8;
+    uint2 v = *reinterpret_cast<const uint2*>(src);
+#pragma unroll
+    for (int x = 0; x < 8; x++) {
+      unsigned word = x < 4 ? v.x : v.y;
+      unsigned byte = (word >> (8 * (x & 3))) & 0xFF;
+      blk[y * 8 + x] = fsub((float)byte, 128.0f);
+    }
+  }
+  fdct_pass(blk);
+  transpose8(blk);
+  fdct_pass(blk);
+#pragma unroll
+  for (int k = 0; k < 64; k++) {
+    constexpr int ZT[64] = {0,  8,  1,  2,  9,  16, 24, 17, 10, 3,  4,  11, 18, 25, 32, 40, 33, 26, 19, 12, 5,  6,
+                            13, 20, 27, 34, 41, 48, 56, 49, 42, 35, 28, 21, 14, 7,  15, 22, 29, 36, 43, 50, 57, 58,
+                            51, 44, 37, 30, 23, 31, 38, 45, 52, 59, 60, 53, 46, 39, 47, 54, 61, 62, 55, 63};
+    cache[(long long)k * nb + b] = blk[ZT[k]];
+  }
+}
+
+int fdct_cache(rcg_ctx* ctx, const uint8_t* d_plane, int stride, int bw, int bh, float* d_cache) {
+  long long nb = (long long)bw * bh;
+  int grid = (int)((nb + 127) / 128);
+  RCG_LAUNCH(ctx, "fdct_cache", k_fdct_cache, grid, 128, 0, d_plane, stride, bw, bh, d_cache);
+  return RCG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------ K3 quantize
+
+__device__ __forceinline__ int bitlen(unsigned v) { return 32 - __clz(v); }
+
+// Plain quantization (jpeg/src/encode.rs:200-205): round_f32(flat*div) clamped to +-2047. When the candidate uses
+// the trellis, the plain coefficients only feed the AC symbol histogram of the rate model (jpeg/src/encode.rs:
+// 221-228, :343-374: (run<<4)|size symbols, ZRL 0xF0, EOB 0x00; luma = component 0, chroma = components 1-2);
+// otherwise they are the candidate's output.
+__global__ void __launch_bounds__(128) k_quantize(StepDesc* __restrict__ st, CacheSet cs) {
+  __shared__ unsigned int sh[2][256];
+  if (!st->active) return;
+  const bool hist = st->use_trellis != 0;
+  if (hist) {
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) (&sh[0][0])[i] = 0;
+    __syncthreads();
+  }
+  long long gb = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gb < st->nblocks) {
+    int c = comp_of(st, gb);
+    const CompDesc& cd = st->comp[c];
+    long long nb = (long long)cd.bw * cd.bh;
+    long long lb = gb - cd.blk0;
+    const float* cache = cs.p[cd.cache] + lb;
+    const float* divz = st->divz[cd.cls];
+    if (!hist) {
+      int16_t* out = st->coefs + gb * 64;
+#pragma unroll
+      for (int g = 0; g < 8; g++) {
+        int v[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          int k = g * 8 + j;
+          v[j] = clampi(round_f32(fmul(cache[(long long)k * nb], divz[k])), -2047, 2047);
+        }
+        int4 pk;
+        pk.x = (v[0] & 0xFFFF) | (v[1] << 16);
+        pk.y = (v[2] & 0xFFFF) | (v[3] << 16);
+        pk.z = (v[4] & 0xFFFF) | (v[5] << 16);
+        pk.w = (v[6] & 0xFFFF) | (v[7] << 16);
+        reinterpret_cast<int4*>(out)[g] = pk;
+      }
+    } else {
+      unsigned* hs = sh[cd.cls];
+      unsigned run = 0;
+      for (int k = 1; k < 64; k++) {
+        int v = clampi(round_f32(fmul(cache[(long long)k * nb], divz[k])), -2047, 2047);
+        if (v == 0) {
+          run++;
+          continue;
+        }
+        while (run >= 16) {
+          atomicAdd(&hs[0xF0], 1u);
+          run -= 16;
+        }
+        unsigned size = (unsigned)bitlen((unsigned)abs(v));
+        atomicAdd(&hs[(run << 4) | size], 1u);
+        run = 0;
+      }
+      if (run > 0) atomicAdd(&hs[0], 1u);
+    }
+  }
+  if (hist) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) {
+      unsigned v = (&sh[0][0])[i];
+      if (v) atomicAdd(&(&st->hist[0][0])[i], v);
+    }
+  }
+}
+
+int quantize(rcg_ctx* ctx, StepDesc* d_step, const float* const* d_caches, long long max_blocks) {
+  CacheSet cs;
+  for (int i = 0; i < 9; i++) cs.p[i] = d_caches[i];
+  int grid = (int)((max_blocks + 127) / 128);
+  RCG_LAUNCH(ctx, "quantize", k_quantize, grid, 128, 0, d_step, cs);
+  return RCG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------ K4 rate model
+
+// core/src/util/huffman.rs:10-86 (build_lengths, max_len 16) over 257 symbols (the 256 AC symbols plus the dummy
+// symbol of frequency 1 that optimal_table adds, jpeg/src/encode.rs:241-244), then optimal_table's sizes
+// (jpeg/src/encode.rs:245-262), Rdo's code-length table (jpeg/src/rdo.rs:36-39) and the lambda*rate table
+// (jpeg/src/rdo.rs:47-52). One CTA per class. The sort is a parallel rank sort on the unique keys
+// (freq, reverse symbol); the two-queue merge and the depth pass are sequential, as in the reference.
+__global__ void __launch_bounds__(288) k_rate_tables(StepDesc* __restrict__ st) {
+  constexpr int NS = 257;
+  __shared__ unsigned freq[NS];
+  __shared__ int order[NS];        // sorted position -> symbol
+  __shared__ unsigned long long weight[2 * NS];
+  __shared__ int parent[2 * NS];
+  __shared__ unsigned char depth[2 * NS];
+  __shared__ int count[17];
+  __shared__ unsigned char lens[NS];
+  __shared__ float len[256];
+  __shared__ int n_used;
+  if (!st->active || !st->use_trellis) return;
+  const int cls = blockIdx.x;
+  const int t = threadIdx.x;
+  if (t < NS) {
+    freq[t] = t < 256 ? st->hist[cls][t] : 1u;
+    lens[t] = 0;
+  }
+  if (t == 0) n_used = 0;
+  __syncthreads();
+  if (t < NS && freq[t] > 0) {
+    // rank of (freq[t], -t) among used symbols
+    unsigned f = freq[t];
+    int r = 0;
+    for (int j = 0; j < NS; j++) {
+      unsigned g = freq[j];
+      if (g > 0 && (g < f || (g == f && j > t))) r++;
+    }
+    order[r] = t;
+    atomicAdd(&n_used, 1);
+  }
+  __syncthreads();
+  const int n = n_used;
+  if (t == 0) {
+    if (n == 1) {
+      lens[order[0]] = 1;
+    } else if (n > 1) {
+      for (int i = 0; i < n; i++) weight[i] = freq[order[i]];
+      int leaf = 0, node = n, next = n;
+      while (next < 2 * n - 1) {
+        int ab[2];
+        for (int p = 0; p < 2; p++) {
+          if (leaf < n && (node >= next || weight[leaf] <= weight[node]))
+            ab[p] = leaf++;
+          else
+            ab[p] = node++;
+        }
+        weight[next] = weight[ab[0]] + weight[ab[1]];
+        parent[ab[0]] = next;
+        parent[ab[1]] = next;
+        next++;
+      }
+      depth[2 * n - 2] = 0;
+      for (int i = 2 * n - 3; i >= 0; i--) depth[i] = (unsigned char)(depth[parent[i]] + 1);
+      for (int l = 0; l <= 16; l++) count[l] = 0;
+      for (int i = 0; i < n; i++) count[min((int)depth[i], 16)] += 1;
+      unsigned long long total = 0;
+      for (int l = 1; l <= 16; l++) total += (unsigned long long)count[l] << (16 - l);
+      while (total > (1ull << 16)) {
+        count[16] -= 1;
+        for (int l = 15; l >= 1; l--) {
+          if (count[l] > 0) {
+            count[l] -= 1;
+            count[l + 1] += 2;
+            break;
+          }
+        }
+        total -= 1;
+      }
+      int idx = 0;
+      for (int l = 16; l >= 1; l--)
+        for (int c = 0; c < count[l]; c++) lens[order[idx++]] = (unsigned char)l;
+    }
+  }
+  __syncthreads();
+  // optimal_table sizes of the 256 real symbols; an empty table gets symbol 0 at length 1. Rdo: 0 -> 18 bits.
+  if (t < 256) {
+    bool any = false;
+    for (int s = 0; s < 256; s++) any |= lens[s] > 0;
+    unsigned size = lens[t];
+    if (!any && t == 0) size = 1;
+    len[t] = size == 0 ? 18.0f : (float)size;
+  }
+  __syncthreads();
+  const float lambda = st->lambda[cls];
+  // rate(run, v) = zrl * len[0xF0] + len[((run % 16) << 4) | size] + size, for size = bit length of v.
+  for (int i = t; i < 64 * 16; i += blockDim.x) {
+    int run = i / 16, size = i % 16;
+    float rate = fadd(fadd(fmul((float)(run / 16), len[0xF0]), len[((run % 16) << 4) | size]), (float)size);
+    st->lr[cls][i] = fmul(lambda, rate);
+  }
+  if (t == 0) st->eob[cls] = fmul(lambda, len[0]);
+}
+
+int rate_tables(rcg_ctx* ctx, StepDesc* d_step) {
+  RCG_LAUNCH(ctx, "rate_tables", k_rate_tables, 2, 288, 0, d_step);
+  return RCG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------ K5 trellis
+
+// Rdo::quantize_ac (jpeg/src/rdo.rs:54-119) for one block per thread, plus the DC rounding of the trellis pass
+// (jpeg/src/encode.rs:206-214). Same candidates, costs, evaluation order and strict `<` tie rule as the reference;
+// both candidate values of a position scan the earlier nodes in one pass (neither sees the other: the reference
+// skips nodes at the same position, :86-88). zd[i-1] is carried as a running sum, and each node keeps zd at its
+// own position, so no 64-entry zd table is needed.
+__global__ void __launch_bounds__(128) k_trellis(StepDesc* __restrict__ st, CacheSet cs) {
+  __shared__ float lr[2][64 * 16];
+  if (!st->active || !st->use_trellis) return;
+  for (int i = threadIdx.x; i < 2 * 64 * 16; i += blockDim.x) (&lr[0][0])[i] = (&st->lr[0][0])[i];
+  __syncthreads();
+  long long gb = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gb >= st->nblocks) return;
+  int c = comp_of(st, gb);
+  const CompDesc& cd = st->comp[c];
+  const int cls = cd.cls;
+  long long nb = (long long)cd.bw * cd.bh;
+  const float* cache = cs.p[cd.cache] + (gb - cd.blk0);
+  const float* divz = st->divz[cls];
+  const float* rq = st->rq[cls];
+  const float* rw = st->rw[cls];
+  const float* lrc = lr[cls];
+
+  float ncost[128], nzd[128];
+  unsigned char npos[128];
+  short nv[128];
+  signed char nprev[128];
+  int nn = 0;
+  unsigned long long negmask = 0;
+
+  float a0 = fmul(cache[0], divz[0]);
+  int dc = clampi(round_f32(a0), -2047, 2047);
+  float zprev = 0.0f;  // zd[i-1]
+  for (int i = 1; i < 64; i++) {
+    float a = fmul(cache[(long long)i * nb], divz[i]);
+    float q = rq[i], w = rw[i];
+    if (a < 0.0f) negmask |= 1ull << i;
+    float m = fabsf(a);
+    unsigned v0 = (unsigned)fadd(m, 0.5f);
+    if (v0 != 0) {
+      unsigned lo = v0 > 1 ? v0 - 1 : v0;
+      bool two = lo != v0;
+      // candidate lo (first) and v0 (second, if distinct)
+      float e_lo = fmul(fsub(m, (float)lo), q);
+      float dnz_lo = fmul(fmul(e_lo, e_lo), w);
+      float e_hi = fmul(fsub(m, (float)v0), q);
+      float dnz_hi = fmul(fmul(e_hi, e_hi), w);
+      int s_lo = bitlen(lo), s_hi = bitlen(v0);
+      float best_lo = fadd(fadd(zprev, lrc[(i - 1) * 16 + s_lo]), dnz_lo);
+      float best_hi = fadd(fadd(zprev, lrc[(i - 1) * 16 + s_hi]), dnz_hi);
+      int prev_lo = -1, prev_hi = -1;
+      for (int ni = 0; ni < nn; ni++) {
+        float base = fadd(ncost[ni], fsub(zprev, nzd[ni]));
+        int ridx = (i - npos[ni] - 1) * 16;
+        float c_lo = fadd(fadd(base, lrc[ridx + s_lo]), dnz_lo);
+        float c_hi = fadd(fadd(base, lrc[ridx + s_hi]), dnz_hi);
+        if (c_lo < best_lo) {
+          best_lo = c_lo;
+          prev_lo = ni;
+        }
+        if (c_hi < best_hi) {
+          best_hi = c_hi;
+          prev_hi = ni;
+        }
+      }
+      ncost[nn] = best_lo;
+      nzd[nn] = zprev;
+      npos[nn] = (unsigned char)i;
+      nv[nn] = (short)lo;
+      nprev[nn] = (signed char)prev_lo;
+      nn++;
+      if (two) {
+        ncost[nn] = best_hi;
+        nzd[nn] = zprev;
+        npos[nn] = (unsigned char)i;
+        nv[nn] = (short)v0;
+        nprev[nn] = (signed char)prev_hi;
+        nn++;
+      }
+    }
+    // zd[i] = zd[i-1] + (a*q)^2 * w
+    float e = fmul(a, q);
+    float zcur = fadd(zprev, fmul(fmul(e, e), w));
+    // A node at position i stores zd[i] (the reference reads zd[n.pos]).
+    for (int ni = nn - 1; ni >= 0 && npos[ni] == i; ni--) nzd[ni] = zcur;
+    zprev = zcur;
+  }
+  // End of block (jpeg/src/rdo.rs:98-108): zprev is zd[63].
+  const float eob = st->eob[cls];
+  float best_cost = fadd(zprev, eob);
+  int best_end = -1;
+  for (int ni = 0; ni < nn; ni++) {
+    float cst = fadd(fadd(ncost[ni], fsub(zprev, nzd[ni])), npos[ni] < 63 ? eob : 0.0f);
+    if (cst < best_cost) {
+      best_cost = cst;
+      best_end = ni;
+    }
+  }
+  int16_t* out = st->coefs + gb * 64;
+  int4 z = make_int4(0, 0, 0, 0);
+  int4 first = z;
+  first.x = dc & 0xFFFF;
+  reinterpret_cast<int4*>(out)[0] = first;
+#pragma unroll
+  for (int g = 1; g < 8; g++) reinterpret_cast<int4*>(out)[g] = z;
+  int cur = best_end;
+  while (cur >= 0) {
+    int p = npos[cur];
+    short v = nv[cur];
+    out[p] = ((negmask >> p) & 1) ? (int16_t)(-v) : (int16_t)v;
+    cur = nprev[cur];
+  }
+}
+
+int trellis(rcg_ctx* ctx, StepDesc* d_step, const float* const* d_caches, long long max_blocks) {
+  CacheSet cs;
+  for (int i = 0; i < 9; i++) cs.p[i] = d_caches[i];
+  int grid = (int)((max_blocks + 127) / 128);
+  RCG_LAUNCH(ctx, "trellis", k_trellis, grid, 128, 0, d_step, cs);
+  return RCG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------ K6 IDCT
+
+// jpeg/src/dct.rs:67-109 (idct_pass)
+__device__ __forceinline__ void idct_pass(float (&d)[64]) {
+  const float SQRT_2 = 1.41421356237309504880f;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    float tmp0 = d[0 * 8 + j], tmp1 = d[2 * 8 + j], tmp2 = d[4 * 8 + j], tmp3 = d[6 * 8 + j];
+    float tmp10 = fadd(tmp0, tmp2), tmp11 = fsub(tmp0, tmp2), tmp13 = fadd(tmp1, tmp3);
+    float tmp12 = fsub(fmul(fsub(tmp1, tmp3), SQRT_2), tmp13);
+    float e0 = fadd(tmp10, tmp13), e3 = fsub(tmp10, tmp13), e1 = fadd(tmp11, tmp12), e2 = fsub(tmp11, tmp12);
+    float tmp4 = d[1 * 8 + j], tmp5 = d[3 * 8 + j], tmp6 = d[5 * 8 + j], tmp7 = d[7 * 8 + j];
+    float z13 = fadd(tmp6, tmp5), z10 = fsub(tmp6, tmp5), z11 = fadd(tmp4, tmp7), z12 = fsub(tmp4, tmp7);
+    float o7 = fadd(z11, z13);
+    float o11 = fmul(fsub(z11, z13), SQRT_2);
+    float z5 = fmul(fadd(z10, z12), 1.8477591f);
+    float o10 = fsub(fmul(1.0823922f, z12), z5);
+    float o12 = fadd(fmul(-2.613126f, z10), z5);
+    float o6 = fsub(o12, o7);
+    float o5 = fsub(o11, o6);
+    float o4 = fadd(o10, o5);
+    d[0 * 8 + j] = fadd(e0, o7);
+    d[7 * 8 + j] = fsub(e0, o7);
+    d[1 * 8 + j] = fadd(e1, o6);
+    d[6 * 8 + j] = fsub(e1, o6);
+    d[2 * 8 + j] = fadd(e2, o5);
+    d[5 * 8 + j] = fsub(e2, o5);
+    d[4 * 8 + j] = fadd(e3, o4);
+    d[3 * 8 + j] = fsub(e3, o4);
+  }
+}
+
+// idct_planes (jpeg/src/decode.rs:1310-1343): dequantize into natural order, IDCT (jpeg/src/dct.rs:111-123),
+// round_f32 + 128 clamped to 0..255. One thread per block.
+__global__ void __launch_bounds__(128) k_dequant_idct(const StepDesc* __restrict__ st,
+                                                     const int16_t* __restrict__ coefs, uint8_t* __restrict__ planes) {
+  if (!st->active) return;
+  long long gb = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gb >= st->nblocks) return;
+  int c = comp_of(st, gb);
+  const CompDesc& cd = st->comp[c];
+  long long lb = gb - cd.blk0;
+  int by = (int)(lb / cd.bw), bx = (int)(lb % cd.bw);
+  const float* mult = st->mult[cd.cls];
+  float blk[64];
+  const int16_t* base = coefs ? coefs : st->coefs;
+  const int4* src = reinterpret_cast<const int4*>(base + gb * 64);
+#pragma unroll
+  for (int g = 0; g < 8; g++) {
+    int4 pk = src[g];
+    int w4[4] = {pk.x, pk.y, pk.z, pk.w};
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      int k = g * 8 + j;
+      int v = (int)(short)((w4[j >> 1] >> (16 * (j & 1))) & 0xFFFF);
+      int n = zigzag(k);
+      blk[n] = fmul((float)v, mult[n]);
+    }
+  }
+  idct_pass(blk);
+  transpose8(blk);
+  idct_pass(blk);
+  transpose8(blk);
+  int stride = cd.bw * 8;
+  uint8_t* dst = planes + cd.plane_off + (size_t)(by * 8) * stride + bx * 8;
+#pragma unroll
+  for (int y = 0; y < 8; y++) {
+    unsigned lo = 0, hi = 0;
+#pragma unroll
+    for (int x = 0; x < 8; x++) {
+      unsigned p = (unsigned)clampi(round_f32(fmul(blk[y * 8 + x], 0.125f)) + 128, 0, 255);
+      if (x < 4)
+        lo |= p << (8 * x);
+      else
+        hi |= p << (8 * (x - 4));
+    }
+    *reinterpret_cast<uint2*>(dst + (size_t)y * stride) = make_uint2(lo, hi);
+  }
+}
+
+int dequant_idct(rcg_ctx* ctx, StepDesc* d_step, const int16_t* d_coefs, uint8_t* d_planes, long long max_blocks) {
+  int grid = (int)((max_blocks + 127) / 128);
+  RCG_LAUNCH(ctx, "dequant_idct", k_dequant_idct, grid, 128, 0, d_step, d_coefs, d_planes);
+  return RCG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------ K7 upsample+colour
+
+__constant__ float c_lut8[256];
+
+// upsample (jpeg/src/decode.rs:1768-1828) of one component sample at full-resolution (x, y).
+__device__ __forceinline__ int up_sample(const uint8_t* p, int stride, int cw, int ch, int fx, int fy, int x, int y) {
+  auto px = [&](int xx, int yy) -> int { return p[(size_t)yy * stride + xx]; };
+  if (fx == 1 && fy == 1) return px(x, y);
+  if (fx == 2 && fy == 1) {
+    int i = x / 2;
+    int nr = px(i, y);
+    int fr = (x % 2 == 0) ? px(max(i - 1, 0), y) : px(min(i + 1, cw - 1), y);
+    return (3 * nr + fr + ((x % 2 == 0) ? 1 : 2)) >> 2;
+  }
+  if (fx == 1 && fy == 2) {
+    int j = y / 2;
+    int fy_ = (y % 2 == 0) ? max(j - 1, 0) : min(j + 1, ch - 1);
+    return (3 * px(x, j) + px(x, fy_) + ((y % 2 == 0) ? 1 : 2)) >> 2;
+  }
+  if (fx == 2 && fy == 2) {
+    int j = y / 2;
+    int fy_ = (y % 2 == 0) ? max(j - 1, 0) : min(j + 1, ch - 1);
+    int i = x / 2;
+    int fi = (x % 2 == 0) ? max(i - 1, 0) : min(i + 1, cw - 1);
+    int nr = 3 * px(i, j) + px(i, fy_);
+    int fr = 3 * px(fi, j) + px(fi, fy_);
+    return (3 * nr + fr + ((x % 2 == 0) ? 8 : 7)) >> 4;
+  }
+  return px(x / fx, y / fy);
+}
+
+__device__ __forceinline__ void upsample_color_px(const StepDesc* __restrict__ st, const uint8_t* __restrict__ planes,
+                                                  int w, int h, uint8_t* __restrict__ rgb, float* __restrict__ lin,
+                                                  int x, int y);
+
+// Decoder::finish for an 8-bit YCbCr or Gray CoefImage (jpeg/src/decode.rs:1404-1444): upsample every component to
+// full resolution, then the fixed-point YCbCr->RGB of :1438-1441. Writes interleaved pixels and/or the linear-light
+// planes the scorer starts from (core/src/ssimulacra2.rs:192-203: Gray is replicated to three channels).
+__global__ void k_upsample_color(const StepDesc* __restrict__ st, const uint8_t* __restrict__ planes, int w, int h,
+                                 uint8_t* __restrict__ rgb, float* __restrict__ lin) {
+  if (!st->active) return;
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= w) return;
+  for (int y = blockIdx.y; y < h; y += gridDim.y) upsample_color_px(st, planes, w, h, rgb, lin, x, y);
+}
+
+__device__ __forceinline__ void upsample_color_px(const StepDesc* __restrict__ st, const uint8_t* __restrict__ planes,
+                                                  int w, int h, uint8_t* __restrict__ rgb, float* __restrict__ lin,
+                                                  int x, int y) {
+  size_t plane_px = (size_t)w * h;
+  size_t i = (size_t)y * w + x;
+  const CompDesc& c0 = st->comp[0];
+  int yv = up_sample(planes + c0.plane_off, c0.bw * 8, (w * c0.h + st->hmax - 1) / st->hmax,
+                     (h * c0.v + st->vmax - 1) / st->vmax, st->hmax / c0.h, st->vmax / c0.v, x, y);
+  if (st->ncomp == 1) {
+    if (rgb) rgb[i] = (uint8_t)yv;
+    if (lin) {
+      float l = c_lut8[yv];
+      lin[i] = l;
+      lin[plane_px + i] = l;
+      lin[2 * plane_px + i] = l;
+    }
+    return;
+  }
+  int s[2];
+#pragma unroll
+  for (int c = 1; c < 3; c++) {
+    const CompDesc& cd = st->comp[c];
+    s[c - 1] = up_sample(planes + cd.plane_off, cd.bw * 8, (w * cd.h + st->hmax - 1) / st->hmax,
+                         (h * cd.v + st->vmax - 1) / st->vmax, st->hmax / cd.h, st->vmax / cd.v, x, y);
+  }
+  int cb = s[0] - 128, cr = s[1] - 128;
+  int r = clampi(yv + ((91881 * cr + 32768) >> 16), 0, 255);
+  int g = clampi(yv - ((22554 * cb + 46802 * cr + 32768) >> 16), 0, 255);
+  int b = clampi(yv + ((116130 * cb + 32768) >> 16), 0, 255);
+  if (rgb) {
+    rgb[i * 3] = (uint8_t)r;
+    rgb[i * 3 + 1] = (uint8_t)g;
+    rgb[i * 3 + 2] = (uint8_t)b;
+  }
+  if (lin) {
+    lin[i] = c_lut8[r];
+    lin[plane_px + i] = c_lut8[g];
+    lin[2 * plane_px + i] = c_lut8[b];
+  }
+}
+
+int upsample_color(rcg_ctx* ctx, StepDesc* d_step, const uint8_t* d_planes, int w, int h, uint8_t* d_rgb,
+                   float* d_lin) {
+  dim3 grid((w + 255) / 256, std::min(h, 65535));
+  RCG_LAUNCH(ctx, "upsample_color", k_upsample_color, grid, 256, 0, d_step, d_planes, w, h, d_rgb, d_lin);
+  return RCG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------ step tables
+
+// First kernel of every search step: the bisection state names the quality; fill the candidate's tables.
+__global__ void k_step_tables(const SearchState* __restrict__ ss, StepDesc* __restrict__ st, int w, int h,
+                              int16_t* slots, long long slot_stride) {
+  if (threadIdx.x != 0) return;
+  if (ss->done) {
+    st->active = 0;
+    return;
+  }
+  int step = ss->step;
+  int q = ss->qs[step];
+  st->active = 1;
+  fill_step(st, q, ss->subsampling, ss->channels, ss->trellis, w, h);
+  for (int i = 0; i < 512; i++) (&st->hist[0][0])[i] = 0;
+  st->coefs = slots + (long long)step * slot_stride;
+}
+
+int step_tables(rcg_ctx* ctx, SearchState* d_search, StepDesc* d_step, int w, int h, int16_t* d_coef_slots,
+                long long slot_stride) {
+  RCG_LAUNCH(ctx, "step_tables", k_step_tables, 1, 32, 0, d_search, d_step, w, h, d_coef_slots, slot_stride);
+  return RCG_OK;
+}
+
+int codec_upload_lut(const float* lut8) {
+  cudaError_t e = cudaMemcpyToSymbol(c_lut8, lut8, 256 * sizeof(float));
+  return e == cudaSuccess ? 0 : (int)e;
+}
+
+}  // namespace rcg

@@ -1,0 +1,201 @@
+// Internal declarations shared by the rcg translation units (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/rcg.h"
+
+namespace rcg {
+
+// ------------------------------------------------------------------------------------------------ constants
+
+constexpr int kMaxScales = 6;     // core/src/ssimulacra2.rs:27 (NUM_SCALES)
+constexpr int kMinSide = 8;       // core/src/ssimulacra2.rs:25 (MIN_SIDE)
+constexpr int kMaxSteps = 16;     // candidates per search (8 suffice for max_quality <= 100)
+constexpr int kScoreSums = 18;    // 3 channels x 6 sums (core/src/ssimulacra2.rs:323-326)
+
+// Scorer tile: TW x TH output pixels per CTA, with a 5-pixel halo (11-tap blur, core/src/ssimulacra2.rs:31).
+constexpr int kRadius = 5;
+constexpr int kTileW = 32;
+constexpr int kTileH = 32;
+constexpr int kTileThreads = 256;
+
+// ------------------------------------------------------------------------------------------------ descriptors
+
+// One scale of the scorer's pyramid: planes are channel-planar f32, [3][h][w], at `off` (floats) in a pyramid buffer.
+struct ScaleDesc {
+  int w, h;
+  int tiles_x, tiles_y;
+  int tile0;        // first CTA of this scale in the multi-scale launch
+  long long off;    // float offset of channel 0 of this scale
+};
+
+struct PyramidDesc {
+  int nscales;
+  int total_tiles;
+  ScaleDesc s[kMaxScales];
+  long long floats;  // total floats of one image's pyramid
+};
+
+// One JPEG component of the current candidate, as the device kernels see it.
+struct CompDesc {
+  int bw, bh;            // block grid (blocks_w, blocks_h)
+  int h, v;              // sampling factors
+  int cls;               // quantization / Huffman class: 0 luma, 1 chroma (component index min 1)
+  int cache;             // which FDCT cache plane set holds this component (index into StepDesc-independent caches)
+  long long blk0;        // first block of this component in the concatenated block space
+  long long plane_off;   // byte offset of the decoded component plane (stride bw*8) in the plane buffer
+};
+
+// Everything the per-candidate kernels need; lives in device memory. Written by the host for single calls and by
+// the device-side search for each bisection step.
+struct StepDesc {
+  int active;            // 0: nothing to do (the search has finished)
+  int quality;
+  int use_trellis;       // trellis && quality < 100 (jpeg/src/encode.rs:527)
+  int ncomp;
+  int hmax, vmax;
+  long long nblocks;     // total blocks of all components
+  CompDesc comp[3];
+  uint8_t qt[2][64];     // quantization tables, natural order (slot 0 luma, slot 1 chroma)
+  float divz[2][64];     // fdct divisors per zigzag position: div[ZZ_T[k]] (jpeg/src/encode.rs:174-183, :202)
+  float mult[2][64];     // dequantization multipliers, natural order (jpeg/src/decode.rs:1316-1321)
+  // Trellis (jpeg/src/rdo.rs:14-52)
+  float rq[2][64];       // step per zigzag position
+  float rw[2][64];       // distortion weight per zigzag position
+  float lambda[2];
+  float eob[2];          // lambda * len[0x00]
+  float lr[2][64 * 16];  // lambda * rate(run, v) for run 0..63, size 0..15 (index run*16 + size)
+  unsigned int hist[2][256];  // AC symbol histogram of the plain pass (jpeg/src/encode.rs:223-227)
+  int16_t* coefs;        // where this candidate's coefficients go
+};
+
+// The device-side bisection (jpeg/src/target.rs:29-56).
+struct SearchState {
+  int lo, hi;
+  int step;              // index of the candidate being evaluated
+  int done;
+  int best_q;
+  int best_step;
+  double best_score;
+  double target;
+  int max_q;
+  int subsampling;
+  int trellis;
+  int channels;
+  int qs[kMaxSteps];
+  double scores[kMaxSteps];
+  int status;            // nonzero: a device-side check failed
+};
+
+// ------------------------------------------------------------------------------------------------ context
+
+struct KernelTimes {
+  uint64_t launches = 0;
+  double ms = 0.0;
+};
+
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace rcg
+
+struct rcg_ctx {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  uint64_t launches = 0;
+  bool profiling = false;
+  std::map<std::string, rcg::KernelTimes> ktimes;
+  struct PendingEvent {
+    std::string name;
+    cudaEvent_t a, b;
+  };
+  std::vector<PendingEvent> pending;
+  std::vector<cudaEvent_t> event_pool;
+  std::map<std::string, rcg::DeviceBuffer> bufs;
+  float* lut16 = nullptr;  // 65536-entry sRGB->linear table for 16-bit samples (allocated on first use)
+};
+
+namespace rcg {
+
+// Error helpers: every entry point returns a status and stores a message; nothing aborts.
+int fail(rcg_ctx* ctx, int status, const std::string& msg);
+int cuda_fail(rcg_ctx* ctx, cudaError_t e, const char* what);
+
+// Grow-only named device workspace. Returns nullptr (and sets the error) on allocation failure.
+void* workspace(rcg_ctx* ctx, const char* name, size_t bytes);
+
+// Kernel launch bookkeeping: counts launches and, when profiling, brackets them with events.
+void launch_begin(rcg_ctx* ctx, const char* name, cudaEvent_t* a, cudaEvent_t* b);
+void launch_end(rcg_ctx* ctx, const char* name, cudaEvent_t a, cudaEvent_t b);
+void collect_times(rcg_ctx* ctx);
+
+#define RCG_LAUNCH(ctx, name, kernel, grid, block, smem, ...)                     \
+  do {                                                                            \
+    cudaEvent_t _ea = nullptr, _eb = nullptr;                                     \
+    ::rcg::launch_begin((ctx), (name), &_ea, &_eb);                               \
+    kernel<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);              \
+    ::rcg::launch_end((ctx), (name), _ea, _eb);                                   \
+  } while (0)
+
+// Host-side sRGB -> linear tables (core/src/ssimulacra2.rs:172-175, :192, :207).
+void srgb_lut8(float out[256]);
+const float* srgb_lut16_device(rcg_ctx* ctx);
+
+// Pyramid geometry of the scorer for a w x h image (core/src/ssimulacra2.rs:480-490).
+PyramidDesc make_pyramid(int w, int h);
+
+// ---- scorer (ssim2.cu)
+// Upload the 8-bit LUT to constant memory once per device.
+int scorer_init(rcg_ctx* ctx);
+// Interleaved 8-bit Gray/Rgb (or GrayAlpha/Rgba, or 16-bit) image -> linear planes at scale 0 of `pyr`.
+int to_linear(rcg_ctx* ctx, const uint8_t* d_img, int w, int h, int channels, int depth, float* d_pyr);
+// Fill scales 1.. of a pyramid from scale 0 (core/src/ssimulacra2.rs:225-247).
+int build_pyramid(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr);
+// The same, skipped on the device when the search step is inactive.
+int build_pyramid_gated(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, const StepDesc* st);
+// Score: per-tile sums of every scale, then the final mapping. `d_score` receives the score (f64); when
+// `search` is non-null the final kernel also advances the device-side bisection.
+int score_pyramids(rcg_ctx* ctx, const PyramidDesc& pd, const float* d_ref, const float* d_dist, double* d_score,
+                   SearchState* search, StepDesc* step);
+
+// ---- codec (codec.cu)
+// Colour conversion + edge padding (jpeg/src/encode.rs:463-477): full-resolution padded Y/Cb/Cr planes.
+int color_pad(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, int pw, int ph, uint8_t* d_y,
+              uint8_t* d_cb, uint8_t* d_cr);
+// 2-D box downsample of a padded chroma plane (jpeg/src/encode.rs:478-499).
+int chroma_down(rcg_ctx* ctx, const uint8_t* d_src, int src_stride, int pw, int ph, int fx, int fy, uint8_t* d_dst);
+// FDCT of every block of a plane into the zigzag [k][block] cache (quality-independent; jpeg/src/encode.rs:189-196).
+int fdct_cache(rcg_ctx* ctx, const uint8_t* d_plane, int stride, int bw, int bh, float* d_cache);
+// Per-candidate pipeline pieces, all driven by a device StepDesc.
+int quantize(rcg_ctx* ctx, StepDesc* d_step, const float* const* d_caches, long long max_blocks);
+int rate_tables(rcg_ctx* ctx, StepDesc* d_step);
+int trellis(rcg_ctx* ctx, StepDesc* d_step, const float* const* d_caches, long long max_blocks);
+// d_coefs null: decode the candidate's own coefficients (d_step->coefs).
+int dequant_idct(rcg_ctx* ctx, StepDesc* d_step, const int16_t* d_coefs, uint8_t* d_planes, long long max_blocks);
+// Upsample + YCbCr->RGB (jpeg/src/decode.rs:1404-1444). Writes interleaved 8-bit pixels to d_rgb (nullable)
+// and/or linear planes to d_lin (nullable).
+int upsample_color(rcg_ctx* ctx, StepDesc* d_step, const uint8_t* d_planes, int w, int h, uint8_t* d_rgb,
+                   float* d_lin);
+// Host-side table setup of one quality into a host StepDesc (no device work).
+void host_step_tables(StepDesc* st, int quality, int subsampling, int channels, int trellis, int w, int h);
+// Dequantization multipliers from caller-given tables (ntables 1 or 2; natural order).
+void fill_mult(StepDesc* st, const uint8_t* qtables, int ntables);
+// Quantization tables of a quality, slot 0 then slot 1 (jpeg/src/quality.rs:37-43).
+void qtables_for(int quality, uint8_t* out128);
+// Copy the 8-bit sRGB table to the codec's constant memory (current device).
+int codec_upload_lut(const float* lut8);
+// Device-side: fill the step tables from the quality the search state holds.
+int step_tables(rcg_ctx* ctx, SearchState* d_search, StepDesc* d_step, int w, int h, int16_t* d_coef_slots,
+                long long slot_stride);
+
+}  // namespace rcg

@@ -1,0 +1,605 @@
+// SSIMULACRA2 scorer kernels (K8-K10): the reference's core/src/ssimulacra2.rs on one GPU.
+//
+// Pipeline per score: linear-light planes (f32, channel-planar) -> 2x2 pyramid (scales 1..5) -> one launch that
+// covers every tile of every scale (XYB, five moments, 11-tap blur, error maps, six partial sums per channel) ->
+// a deterministic f64 reduction and the final 108-weight mapping.
+//
+// Arithmetic. The reference holds the planes in f32 and computes XYB, the blur, the maps and the sums in f64
+// (:18, :345-346, :361). GB300's FP64 rate is a small fraction of its FP32 rate, so here:
+//   * planes: f32 exactly as the reference (LUT values; the 2x2 average is a compensated sum that rounds like the
+//     reference's f64 sum nearly always);
+//   * XYB, blur and maps: f32, arranged so that nothing cancels catastrophically. Each pixel carries the reference
+//     image's XYB and the XYB *difference* of the two images, both computed from cube-root difference identities
+//     (see pix()); both are offset by their value at the tile centre, so the five blurred moments (mu_a, mu_(a-b),
+//     E[a^2], E[b^2], E[(a-b)^2]) are small where the image is smooth. The variances and mu1 - mu2 are recovered
+//     exactly from them (the offsets cancel wherever the blur taps sum to 1 and are corrected with the in-image tap
+//     sum within 5 columns of the zero left/right border, :34-40). The SSIM term is evaluated as
+//     (sigma_(a-b)^2 + (mu1-mu2)^2 num_s) / denom_s and the edge term from r1 = a - mu1 and its difference, forms
+//     that equal the reference's expressions algebraically but keep full relative precision for similar images;
+//   * sums: f32 over the 4 pixels of a thread, f32 across a warp, f64 from there on, in a fixed order
+//     (bit-reproducible from run to run, as the reference's test :630 requires).
+// Identical images give exactly 100: every difference term is exactly 0, so every map value is exactly 0.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "rcg_internal.cuh"
+
+namespace rcg {
+
+__constant__ float c_gauss[2 * kRadius + 1];
+__constant__ float c_lut8s[256];
+__constant__ double c_weights[108];
+
+// core/src/ssimulacra2.rs:42-52 (opsin absorbance matrix and bias), as f32
+constexpr double kM02 = 0.078, kM00 = 0.30, kM01 = 1.0 - kM02 - kM00;
+constexpr double kM12 = 0.078, kM10 = 0.23, kM11 = 1.0 - kM12 - kM10;
+constexpr double kM20 = 0.2434226892454782, kM21 = 0.2047674442449682, kM22 = 1.0 - kM20 - kM21;
+constexpr double kBias = 0.0037930732552754493;
+
+// x^2 + x*y + y^2: cbrt(u) - cbrt(v) = (u - v) / D(cbrt(u), cbrt(v)).
+__device__ __forceinline__ float dsq(float x, float y) { return fmaf(x, x, fmaf(x, y, y * y)); }
+
+// q_a/D_a - q_b/D_b without cancellation: (dq*D_b - q_b*dD) / (D_a*D_b), dq = q_a - q_b and dD = D_a - D_b given.
+__device__ __forceinline__ float qdiff(float qb, float dq, float Da, float Db, float dD) {
+  return __fdividef(fmaf(dq, Db, -qb * dD), Da * Db);
+}
+
+// One pixel of the tile: the reference image's XYB minus the tile offsets (`a`, core/src/ssimulacra2.rs:249-258)
+// and XYB(reference) - XYB(distorted) minus the tile's difference offsets (`d`). Every quantity that is a small
+// difference of nearly equal cube roots is formed from the identity above, so it keeps its relative precision in
+// f32: X - 0.42 = 7 (c0 - c1), B - 0.55 = ((c2 - c0) + (c2 - c1)) / 2, each c_i - c_j from the difference of two
+// opsin-matrix rows applied to (r, g, b); and the per-pixel differences between the two images from the linear
+// differences (r_a - r_b, ...).
+struct Pix {
+  float a[3], d[3];
+};
+
+__device__ __forceinline__ Pix pix(float ra, float ga, float ba, float rb, float gb, float bb, const float* oa,
+                                   const float* od, float cbrt_bias) {
+  const float bias = (float)kBias;
+  // opsin rows (f32) and the exact differences of rows, rounded once
+  const float M00 = (float)kM00, M01 = (float)kM01, M02 = (float)kM02;
+  const float M10 = (float)kM10, M11 = (float)kM11, M12 = (float)kM12;
+  const float M20 = (float)kM20, M21 = (float)kM21, M22 = (float)kM22;
+  const float L20r = (float)(kM20 - kM00), L20g = (float)(kM21 - kM01), L20b = (float)(kM22 - kM02);
+  const float L21r = (float)(kM20 - kM10), L21g = (float)(kM21 - kM11), L21b = (float)(kM22 - kM12);
+  float ca[3], cb[3];
+  ca[0] = cbrtf(fmaxf(fmaf(M00, ra, fmaf(M01, ga, fmaf(M02, ba, bias))), 0.0f));
+  ca[1] = cbrtf(fmaxf(fmaf(M10, ra, fmaf(M11, ga, fmaf(M12, ba, bias))), 0.0f));
+  ca[2] = cbrtf(fmaxf(fmaf(M20, ra, fmaf(M21, ga, fmaf(M22, ba, bias))), 0.0f));
+  cb[0] = cbrtf(fmaxf(fmaf(M00, rb, fmaf(M01, gb, fmaf(M02, bb, bias))), 0.0f));
+  cb[1] = cbrtf(fmaxf(fmaf(M10, rb, fmaf(M11, gb, fmaf(M12, bb, bias))), 0.0f));
+  cb[2] = cbrtf(fmaxf(fmaf(M20, rb, fmaf(M21, gb, fmaf(M22, bb, bias))), 0.0f));
+  float q01a = 0.07f * (ra - ga), q01b = 0.07f * (rb - gb);
+  float q20a = fmaf(L20r, ra, fmaf(L20g, ga, L20b * ba)), q20b = fmaf(L20r, rb, fmaf(L20g, gb, L20b * bb));
+  float q21a = fmaf(L21r, ra, fmaf(L21g, ga, L21b * ba)), q21b = fmaf(L21r, rb, fmaf(L21g, gb, L21b * bb));
+  float D01a = dsq(ca[0], ca[1]), D20a = dsq(ca[2], ca[0]), D21a = dsq(ca[2], ca[1]);
+  float D01b = dsq(cb[0], cb[1]), D20b = dsq(cb[2], cb[0]), D21b = dsq(cb[2], cb[1]);
+  Pix o;
+  float ya = 0.5f * (ca[0] + ca[1]);
+  o.a[0] = fmaf(7.0f, __fdividef(q01a, D01a), 0.42f - oa[0]);
+  o.a[1] = (ya - cbrt_bias) + (0.01f - oa[1]);
+  o.a[2] = 0.5f * (__fdividef(q20a, D20a) + __fdividef(q21a, D21a)) + (0.55f - oa[2]);
+  float dr = ra - rb, dg = ga - gb, db = ba - bb;
+  float dc0 = __fdividef(fmaf(M00, dr, fmaf(M01, dg, M02 * db)), dsq(ca[0], cb[0]));
+  float dc1 = __fdividef(fmaf(M10, dr, fmaf(M11, dg, M12 * db)), dsq(ca[1], cb[1]));
+  float dc2 = __fdividef(fmaf(M20, dr, fmaf(M21, dg, M22 * db)), dsq(ca[2], cb[2]));
+  // D(x, y) of image a minus of image b: dx (xa + xb) + dx ya + xb dy + dy (ya + yb)
+  float dD01 = fmaf(dc0, ca[0] + cb[0], fmaf(dc0, ca[1], fmaf(cb[0], dc1, dc1 * (ca[1] + cb[1]))));
+  float dD20 = fmaf(dc2, ca[2] + cb[2], fmaf(dc2, ca[0], fmaf(cb[2], dc0, dc0 * (ca[0] + cb[0]))));
+  float dD21 = fmaf(dc2, ca[2] + cb[2], fmaf(dc2, ca[1], fmaf(cb[2], dc1, dc1 * (ca[1] + cb[1]))));
+  float dq01 = 0.07f * (dr - dg);
+  float dq20 = fmaf(L20r, dr, fmaf(L20g, dg, L20b * db));
+  float dq21 = fmaf(L21r, dr, fmaf(L21g, dg, L21b * db));
+  o.d[0] = 7.0f * qdiff(q01b, dq01, D01a, D01b, dD01) - od[0];
+  o.d[1] = 0.5f * (dc0 + dc1) - od[1];
+  o.d[2] = 0.5f * (qdiff(q20b, dq20, D20a, D20b, dD20) + qdiff(q21b, dq21, D21a, D21b, dD21)) - od[2];
+  return o;
+}
+
+// Row index under the top/bottom mirror rule (core/src/ssimulacra2.rs:385-397); -1 for rows no valid output reads.
+__device__ __forceinline__ int mirror_row(int yy, int h) {
+  if (yy < -kRadius || yy > h - 1 + kRadius) return -1;
+  if (yy < 0) return -yy - 1;
+  if (yy >= h) return 2 * h - 1 - yy;
+  return yy;
+}
+
+constexpr int kIW = kTileW + 2 * kRadius;  // 42
+constexpr int kIH = kTileH + 2 * kRadius;  // 42
+constexpr size_t kTileSmem = (size_t)(6 * kIH * kIW + 5 * kIH * kTileW) * sizeof(float);
+
+// One CTA = one 32x32 output tile of one scale. Shared memory: XYB (offset) of both images for the tile plus its
+// 5-pixel halo, 3 channels each; then per channel the horizontally blurred five moments of the 42 halo rows.
+__global__ void __launch_bounds__(kTileThreads, 3)
+    k_ssim2_tiles(PyramidDesc pd, const float* __restrict__ ref, const float* __restrict__ dist,
+                  double* __restrict__ partials, const StepDesc* __restrict__ st) {
+  if (st && !st->active) return;
+  extern __shared__ float smem[];
+  float* xs = smem;                      // [6][kIH][kIW]: ref X,Y,B then dist X,Y,B
+  float* hb = smem + 6 * kIH * kIW;      // [5][kIH][kTileW]
+  __shared__ float s_red[kTileThreads / 32][kScoreSums];
+
+  int blk = blockIdx.x;
+  int s = 0;
+  while (s + 1 < pd.nscales && blk >= pd.s[s + 1].tile0) s++;
+  const ScaleDesc sd = pd.s[s];
+  const int local = blk - sd.tile0;
+  const int tx = local % sd.tiles_x, ty = local / sd.tiles_x;
+  const int x0 = tx * kTileW, y0 = ty * kTileH;
+  const int w = sd.w, h = sd.h;
+  const size_t np = (size_t)w * h;
+  const float* ra = ref + sd.off;
+  const float* rb = dist + sd.off;
+  const float cb_bias = cbrtf((float)kBias);
+  const int tid = threadIdx.x;
+
+  // Per-tile offsets: the reference's XYB and the XYB difference at the tile centre. Stored values are
+  // a' = a - oa and d' = (a - b) - od inside the image and 0 outside (the zero border). Every moment the maps need
+  // is recovered exactly from the blurred primed values and the in-image tap sum K of the column (K = 1 away from
+  // the left/right edges, where the offsets cancel outright).
+  __shared__ float s_oa[3], s_od[3];
+  if (tid == 0) {
+    int cx = min(x0 + kTileW / 2, w - 1), cy = min(y0 + kTileH / 2, h - 1);
+    size_t i = (size_t)cy * w + cx;
+    const float z[3] = {0.f, 0.f, 0.f};
+    Pix c = pix(ra[i], ra[np + i], ra[2 * np + i], rb[i], rb[np + i], rb[2 * np + i], z, z, cb_bias);
+    for (int k = 0; k < 3; k++) {
+      s_oa[k] = c.a[k];
+      s_od[k] = c.d[k];
+    }
+  }
+  __syncthreads();
+  float oa[3] = {s_oa[0], s_oa[1], s_oa[2]}, od[3] = {s_od[0], s_od[1], s_od[2]};
+
+  for (int idx = tid; idx < kIH * kIW; idx += kTileThreads) {
+    int r = idx / kIW, c = idx - r * kIW;
+    int gy = mirror_row(y0 - kRadius + r, h);
+    int gx = x0 - kRadius + c;
+    float v[6] = {0, 0, 0, 0, 0, 0};
+    if (gy >= 0 && gx >= 0 && gx < w) {
+      size_t i = (size_t)gy * w + gx;
+      Pix p = pix(__ldg(ra + i), __ldg(ra + np + i), __ldg(ra + 2 * np + i), __ldg(rb + i), __ldg(rb + np + i),
+                  __ldg(rb + 2 * np + i), oa, od, cb_bias);
+      v[0] = p.a[0]; v[1] = p.a[1]; v[2] = p.a[2];
+      v[3] = p.d[0]; v[4] = p.d[1]; v[5] = p.d[2];
+    }
+#pragma unroll
+    for (int k = 0; k < 6; k++) xs[k * kIH * kIW + idx] = v[k];
+  }
+
+  float sums[kScoreSums];
+#pragma unroll
+  for (int i = 0; i < kScoreSums; i++) sums[i] = 0.0f;
+
+  const int col = tid & 31, rg = tid >> 5;  // vertical pass: column, group of 4 output rows
+  const int gx = x0 + col;
+  // In-image tap sum of this column (1 except within kRadius of the left/right edge).
+  const bool edge = gx < kRadius || gx >= w - kRadius;
+  float K = 1.0f;
+  if (edge) {
+    K = 0.0f;
+#pragma unroll
+    for (int t = 0; t < 2 * kRadius + 1; t++) {
+      int xx = gx + t - kRadius;
+      if (xx >= 0 && xx < w) K += c_gauss[t];
+    }
+  }
+  const float omk = 1.0f - K;
+#pragma unroll 1
+  for (int ch = 0; ch < 3; ch++) {
+    __syncthreads();  // xs complete (ch 0) / previous channel's vertical pass done with hb
+    const float* A = xs + ch * kIH * kIW;
+    const float* D = xs + (3 + ch) * kIH * kIW;
+    // Horizontal pass: 2 adjacent outputs per item; moments a', d', a'^2, b'^2 (b' = a' - d'), d'^2.
+    for (int item = tid; item < kIH * (kTileW / 2); item += kTileThreads) {
+      int r = item / (kTileW / 2), p = item - r * (kTileW / 2);
+      const float* ar = A + r * kIW + 2 * p;
+      const float* dr = D + r * kIW + 2 * p;
+      float va[12], vd[12];
+#pragma unroll
+      for (int t = 0; t < 12; t++) {
+        va[t] = ar[t];
+        vd[t] = dr[t];
+      }
+      float m[5][2];
+#pragma unroll
+      for (int o = 0; o < 2; o++) {
+        float s1 = 0.f, sd = 0.f, s11 = 0.f, s22 = 0.f, sdd = 0.f;
+#pragma unroll
+        for (int t = 0; t < 2 * kRadius + 1; t++) {
+          float k = c_gauss[t], a = va[o + t], d = vd[o + t], b = a - d;
+          s1 = fmaf(k, a, s1);
+          sd = fmaf(k, d, sd);
+          s11 = fmaf(k, a * a, s11);
+          s22 = fmaf(k, b * b, s22);
+          sdd = fmaf(k, d * d, sdd);
+        }
+        m[0][o] = s1; m[1][o] = sd; m[2][o] = s11; m[3][o] = s22; m[4][o] = sdd;
+      }
+#pragma unroll
+      for (int q = 0; q < 5; q++) {
+        float2 v2 = make_float2(m[q][0], m[q][1]);
+        *reinterpret_cast<float2*>(hb + (q * kIH + r) * kTileW + 2 * p) = v2;
+      }
+    }
+    __syncthreads();
+    // Vertical pass + error maps: 4 output rows of one column per thread.
+    float mu[5][4];
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+      float v[4 + 2 * kRadius];
+#pragma unroll
+      for (int t = 0; t < 4 + 2 * kRadius; t++) v[t] = hb[(q * kIH + rg * 4 + t) * kTileW + col];
+#pragma unroll
+      for (int o = 0; o < 4; o++) {
+        float acc = 0.f;
+#pragma unroll
+        for (int t = 0; t < 2 * kRadius + 1; t++) acc = fmaf(c_gauss[t], v[o + t], acc);
+        mu[q][o] = acc;
+      }
+    }
+    const float ca = oa[ch], cd = od[ch], cbv = ca - cd;
+#pragma unroll
+    for (int o = 0; o < 4; o++) {
+      int ry = rg * 4 + o;
+      int gy = y0 + ry;
+      if (gx < w && gy < h) {
+        // Blurred primed moments -> sigma_1^2, sigma_2^2, sigma_(a-b)^2, mu1 - mu2 (exactly, given K).
+        float m1 = mu[0][o], dmp = mu[1][o], m2 = m1 - dmp;
+        float v1 = fmaf(-m1, m1, mu[2][o]);
+        float v2 = fmaf(-m2, m2, mu[3][o]);
+        float vd = fmaf(-dmp, dmp, mu[4][o]);
+        float dmu;
+        if (edge) {
+          v1 = fmaf(omk * ca, fmaf(ca, K, 2.0f * m1), v1);
+          v2 = fmaf(omk * cbv, fmaf(cbv, K, 2.0f * m2), v2);
+          vd = fmaf(omk * cd, fmaf(cd, K, 2.0f * dmp), vd);
+          dmu = fmaf(cd, K, dmp);
+        } else {
+          dmu = dmp + cd;
+        }
+        // SSIM error (core/src/ssimulacra2.rs:427-430) as (sigma_(a-b)^2 + dmu^2 num_s) / denom_s, which equals
+        // 1 - (1 - dmu^2) num_s / denom_s since num_s = denom_s - sigma_(a-b)^2.
+        float den = (v1 + v2) + 0.0009f;
+        float num_s = den - vd;
+        float d = fmaxf(__fdiv_rn(fmaf(dmu * dmu, num_s, vd), den), 0.0f);
+        // Edge maps (:431-433): d1 = (|r2| - |r1|) / (1 + |r1|) with r1 = a - mu1, r2 = b - mu2 = r1 - rd.
+        float a0 = A[(ry + kRadius) * kIW + col + kRadius];
+        float d0 = D[(ry + kRadius) * kIW + col + kRadius];
+        float r1 = a0 - m1, rd = d0 - dmp;
+        if (edge) {
+          r1 = fmaf(ca, omk, r1);
+          rd = fmaf(cd, omk, rd);
+        }
+        float t = fabsf(r1 - rd) + fabsf(r1);
+        float d1 = t > 0.0f ? __fdiv_rn(__fdiv_rn(-rd * (2.0f * r1 - rd), t), 1.0f + fabsf(r1)) : 0.0f;
+        float art = fmaxf(d1, 0.0f), det = fmaxf(-d1, 0.0f);
+        float d2 = d * d, a2 = art * art, e2 = det * det;
+        sums[ch * 6 + 0] += d;
+        sums[ch * 6 + 1] += d2 * d2;
+        sums[ch * 6 + 2] += art;
+        sums[ch * 6 + 3] += a2 * a2;
+        sums[ch * 6 + 4] += det;
+        sums[ch * 6 + 5] += e2 * e2;
+      }
+    }
+  }
+  // Warp sums (f32, 32 threads x 4 pixels), then the 8 warps in f64 in a fixed order.
+#pragma unroll
+  for (int i = 0; i < kScoreSums; i++) {
+    float v = sums[i];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    sums[i] = v;
+  }
+  const int lane = tid & 31, warp = tid >> 5;
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < kScoreSums; i++) s_red[warp][i] = sums[i];
+  }
+  __syncthreads();
+  if (tid < kScoreSums) {
+    double acc = 0.0;
+    for (int wi = 0; wi < kTileThreads / 32; wi++) acc += (double)s_red[wi][tid];
+    partials[(size_t)blk * kScoreSums + tid] = acc;
+  }
+}
+
+// Deterministic reduction of the per-tile sums: CTA (scale, sum index); the last CTA to finish computes the score
+// (core/src/ssimulacra2.rs:457-511) and, in a search, advances the bisection (jpeg/src/target.rs:29-56).
+__global__ void __launch_bounds__(256) k_ssim2_reduce(PyramidDesc pd, const double* __restrict__ partials,
+                                                      double* __restrict__ scale_sums, unsigned* __restrict__ counter,
+                                                      double* __restrict__ score_out, SearchState* __restrict__ ss,
+                                                      const StepDesc* __restrict__ st) {
+  if (st && !st->active) return;
+  __shared__ double red[8];
+  __shared__ bool last;
+  const int s = blockIdx.x, i = blockIdx.y;
+  const ScaleDesc sd = pd.s[s];
+  const int n = sd.tiles_x * sd.tiles_y;
+  double acc = 0.0;
+  for (int t = threadIdx.x; t < n; t += 256) acc += partials[(size_t)(sd.tile0 + t) * kScoreSums + i];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int wi = 0; wi < 8; wi++) tot += red[wi];
+    scale_sums[s * kScoreSums + i] = tot;
+    __threadfence();
+    unsigned prev = atomicAdd(counter, 1u);
+    last = prev == gridDim.x * gridDim.y - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  *counter = 0;
+  const volatile double* vs = scale_sums;
+  double stats[kMaxScales][3][6];
+  for (int sc = 0; sc < pd.nscales; sc++) {
+    double count = (double)pd.s[sc].w * (double)pd.s[sc].h;
+    for (int c = 0; c < 3; c++)
+      for (int m = 0; m < 3; m++) {
+        stats[sc][c][2 * m] = vs[sc * kScoreSums + c * 6 + 2 * m] / count;
+        stats[sc][c][2 * m + 1] = pow(vs[sc * kScoreSums + c * 6 + 2 * m + 1] / count, 0.25);
+      }
+  }
+  double ssim = 0.0;
+  int wi = 0;
+  for (int c = 0; c < 3; c++)
+    for (int sc = 0; sc < pd.nscales; sc++)
+      for (int nrm = 0; nrm < 2; nrm++) {
+        ssim += c_weights[wi++] * fabs(stats[sc][c][nrm]);
+        ssim += c_weights[wi++] * fabs(stats[sc][c][2 + nrm]);
+        ssim += c_weights[wi++] * fabs(stats[sc][c][4 + nrm]);
+      }
+  ssim *= 0.9562382616834844;
+  ssim = 2.326765642916932 * ssim - 0.020884521182843837 * ssim * ssim + 6.248496625763138e-05 * ssim * ssim * ssim;
+  double score = ssim > 0.0 ? 100.0 - 10.0 * pow(ssim, 0.6276336467831387) : 100.0;
+  // A non-finite score is the reference's Err, which the search maps to f64::MIN (cli/src/pipeline.rs:218).
+  bool finite = isfinite(score);
+  *score_out = finite ? score : NAN;
+  if (ss && !ss->done) {
+    double sv = finite ? score : -1.7976931348623157e308;
+    int step = ss->step;
+    int q = ss->qs[step];
+    ss->scores[step] = sv;
+    if (step == 0) {
+      ss->best_q = q;
+      ss->best_score = sv;
+      ss->best_step = 0;
+      if (sv < ss->target) ss->done = 1;
+    } else if (sv >= ss->target) {
+      ss->hi = q;
+      ss->best_q = q;
+      ss->best_score = sv;
+      ss->best_step = step;
+    } else {
+      ss->lo = q + 1;
+    }
+    if (!ss->done) {
+      if (ss->lo < ss->hi && step + 1 < kMaxSteps) {
+        ss->step = step + 1;
+        ss->qs[step + 1] = ss->lo + (ss->hi - ss->lo) / 2;
+      } else {
+        ss->done = 1;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------------ planes, pyramid
+
+// Linear planes of an interleaved image (core/src/ssimulacra2.rs:177-221, with core/src/image.rs:143-190 for alpha:
+// 16-bit samples rounded to 8 bits, then composited onto mid-grey 128).
+__global__ void k_to_linear(const uint8_t* __restrict__ img, int w, int h, int channels, int depth,
+                            const float* __restrict__ lut16, float* __restrict__ out) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= w) return;
+  for (int y = blockIdx.y; y < h; y += gridDim.y) {
+  size_t i = (size_t)y * w + x;
+  size_t np = (size_t)w * h;
+  float v[3];
+  bool alpha = channels == 2 || channels == 4;
+  if (depth == 8 && !alpha) {
+    if (channels == 1) {
+      v[0] = v[1] = v[2] = c_lut8s[img[i]];
+    } else {
+      v[0] = c_lut8s[img[i * 3]];
+      v[1] = c_lut8s[img[i * 3 + 1]];
+      v[2] = c_lut8s[img[i * 3 + 2]];
+    }
+  } else if (!alpha) {
+    auto s16 = [&](int k) -> unsigned {
+      const uint8_t* p = img + (i * channels + k) * 2;
+      return ((unsigned)p[0] << 8) | p[1];
+    };
+    if (channels == 1) {
+      v[0] = v[1] = v[2] = lut16[s16(0)];
+    } else {
+      v[0] = lut16[s16(0)];
+      v[1] = lut16[s16(1)];
+      v[2] = lut16[s16(2)];
+    }
+  } else {
+    unsigned s[4];
+    for (int k = 0; k < channels; k++) {
+      if (depth == 8) {
+        s[k] = img[i * channels + k];
+      } else {
+        const uint8_t* p = img + (i * channels + k) * 2;
+        unsigned u = ((unsigned)p[0] << 8) | p[1];
+        s[k] = (u * 255 + 32767) / 65535;
+      }
+    }
+    unsigned a = s[channels - 1];
+    auto blend = [&](unsigned c) -> unsigned { return (c * a + 128u * (255 - a) + 127) / 255; };
+    if (channels == 2) {
+      v[0] = v[1] = v[2] = c_lut8s[blend(s[0])];
+    } else {
+      v[0] = c_lut8s[blend(s[0])];
+      v[1] = c_lut8s[blend(s[1])];
+      v[2] = c_lut8s[blend(s[2])];
+    }
+  }
+  out[i] = v[0];
+  out[np + i] = v[1];
+  out[2 * np + i] = v[2];
+  }
+}
+
+// Error-free transform: s + e == a + b exactly (Knuth's TwoSum).
+__device__ __forceinline__ float two_sum(float a, float b, float& e) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return s;
+}
+
+// downsample (core/src/ssimulacra2.rs:223-247): mean of the 2x2 block (fewer at odd edges). The reference sums in
+// f64, which is exact for these inputs, then rounds once to f32; the compensated sum here (TwoSum) rounds the same
+// exact sum once, so the planes agree with the reference's except in rare double-rounding cases.
+__global__ void k_downsample(const float* __restrict__ src, int w, int h, float* __restrict__ dst,
+                             const StepDesc* __restrict__ st) {
+  if (st && !st->active) return;
+  int ow = (w + 1) / 2, oh = (h + 1) / 2;
+  int ox = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ox >= ow) return;
+  for (int oy = blockIdx.y; oy < oh; oy += gridDim.y) {
+  int x0 = ox * 2, x1 = min(ox * 2 + 2, w), y0 = oy * 2, y1 = min(oy * 2 + 2, h);
+  float inv = 1.0f / (float)((y1 - y0) * (x1 - x0));
+  size_t np = (size_t)w * h, onp = (size_t)ow * oh;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const float* p = src + c * np;
+    float s = 0.0f, err = 0.0f;
+    for (int y = y0; y < y1; y++)
+      for (int x = x0; x < x1; x++) {
+        float e;
+        s = two_sum(s, p[(size_t)y * w + x], e);
+        err += e;
+      }
+    // count is 1, 2 or 4: the scaling is exact.
+    dst[c * onp + (size_t)oy * ow + ox] = __fadd_rn(s, err) * inv;
+  }
+  }
+}
+
+int to_linear(rcg_ctx* ctx, const uint8_t* d_img, int w, int h, int channels, int depth, float* d_pyr) {
+  const float* lut16 = nullptr;
+  if (depth == 16 && channels != 2 && channels != 4) {
+    lut16 = srgb_lut16_device(ctx);
+    if (!lut16) return RCG_NO_MEMORY;
+  }
+  dim3 grid((w + 255) / 256, std::min(h, 65535));
+  RCG_LAUNCH(ctx, "to_linear", k_to_linear, grid, 256, 0, d_img, w, h, channels, depth, lut16, d_pyr);
+  return RCG_OK;
+}
+
+int build_pyramid_gated(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, const StepDesc* st) {
+  for (int s = 1; s < pd.nscales; s++) {
+    const ScaleDesc& a = pd.s[s - 1];
+    const ScaleDesc& b = pd.s[s];
+    dim3 grid((b.w + 127) / 128, std::min(b.h, 65535));
+    RCG_LAUNCH(ctx, "downsample", k_downsample, grid, 128, 0, d_pyr + a.off, a.w, a.h, d_pyr + b.off, st);
+  }
+  return RCG_OK;
+}
+
+int build_pyramid(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr) {
+  return build_pyramid_gated(ctx, pd, d_pyr, nullptr);
+}
+
+PyramidDesc make_pyramid(int w, int h) {
+  PyramidDesc pd;
+  std::memset(&pd, 0, sizeof pd);
+  long long off = 0;
+  int tiles = 0;
+  for (int s = 0; s < kMaxScales; s++) {
+    if (w < kMinSide || h < kMinSide) break;
+    ScaleDesc& sd = pd.s[s];
+    sd.w = w;
+    sd.h = h;
+    sd.tiles_x = (w + kTileW - 1) / kTileW;
+    sd.tiles_y = (h + kTileH - 1) / kTileH;
+    sd.tile0 = tiles;
+    sd.off = off;
+    tiles += sd.tiles_x * sd.tiles_y;
+    off += 3LL * w * h;
+    pd.nscales = s + 1;
+    w = (w + 1) / 2;
+    h = (h + 1) / 2;
+  }
+  pd.total_tiles = tiles;
+  pd.floats = off;
+  return pd;
+}
+
+static bool g_scorer_ready[64];
+
+int scorer_init(rcg_ctx* ctx) {
+  if (ctx->device >= 0 && ctx->device < 64 && g_scorer_ready[ctx->device]) return RCG_OK;
+  // core/src/ssimulacra2.rs:260-271 (kernel): f64 taps, rounded to f32 here.
+  double k[2 * kRadius + 1], sum = 0.0;
+  for (int i = 0; i < 2 * kRadius + 1; i++) {
+    double x = (double)i - (double)kRadius;
+    k[i] = std::exp(-0.5 / (1.5 * 1.5) * x * x);
+    sum += k[i];
+  }
+  float kf[2 * kRadius + 1];
+  for (int i = 0; i < 2 * kRadius + 1; i++) kf[i] = (float)(k[i] / sum);
+  float lut[256];
+  srgb_lut8(lut);
+  // core/src/ssimulacra2.rs:54-163 (WEIGHTS)
+  static const double W[108] = {
+      0.0, 0.0007376606707406586, 0.0, 0.0, 0.0007793481682867309, 0.0,
+      0.0, 0.0004371155730107379, 0.0, 1.1041726426657346, 0.00066284834129271, 0.00015231632783718752,
+      0.0, 0.0016406437456599754, 0.0, 1.8422455520539298, 11.441172603757666, 0.0,
+      0.0007989109436015163, 0.000176816438078653, 0.0, 1.8787594979546387, 10.94906990605142, 0.0,
+      0.0007289346991508072, 0.9677937080626833, 0.0, 0.00014003424285435884, 0.9981766977854967, 0.00031949755934435053,
+      0.0004550992113792063, 0.0, 0.0, 0.0013648766163243398, 0.0, 0.0,
+      0.0, 0.0, 0.0, 7.466890328078848, 0.0, 17.445833984131262,
+      0.0006235601634041466, 0.0, 0.0, 6.683678146179332, 0.00037724407979611296, 1.027889937768264,
+      225.20515300849274, 0.0, 0.0, 19.213238186143016, 0.0011401524586618361, 0.001237755635509985,
+      176.39317598450694, 0.0, 0.0, 24.43300999870476, 0.28520802612117757, 0.0004485436923833408,
+      0.0, 0.0, 0.0, 34.77906344483772, 44.835625328877896, 0.0,
+      0.0, 0.0, 0.0, 0.0, 0.0, 0.0,
+      0.0, 0.0008680556573291698, 0.0, 0.0, 0.0, 0.0,
+      0.0, 0.0005313191874358747, 0.0, 0.00016533814161379112, 0.0, 0.0,
+      0.0, 0.0, 0.0, 0.0004179171803251336, 0.0017290828234722833, 0.0,
+      0.0020827005846636437, 0.0, 0.0, 8.826982764996862, 23.19243343998926, 0.0,
+      95.1080498811086, 0.9863978034400682, 0.9834382792465353, 0.0012286405048278493, 171.2667255897307, 0.9807858872435379,
+      0.0, 0.0, 0.0, 0.0005130064588990679, 0.0, 0.00010854057858411537};
+  cudaError_t e;
+  if ((e = cudaMemcpyToSymbol(c_gauss, kf, sizeof kf)) != cudaSuccess) return cuda_fail(ctx, e, "gauss upload");
+  if ((e = cudaMemcpyToSymbol(c_lut8s, lut, sizeof lut)) != cudaSuccess) return cuda_fail(ctx, e, "lut upload");
+  if ((e = cudaMemcpyToSymbol(c_weights, W, sizeof W)) != cudaSuccess) return cuda_fail(ctx, e, "weights upload");
+  if (int ce = codec_upload_lut(lut)) return cuda_fail(ctx, (cudaError_t)ce, "codec lut upload");
+  if ((e = cudaFuncSetAttribute(k_ssim2_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem)) !=
+      cudaSuccess)
+    return cuda_fail(ctx, e, "tile kernel attribute");
+  if (ctx->device >= 0 && ctx->device < 64) g_scorer_ready[ctx->device] = true;
+  return RCG_OK;
+}
+
+int score_pyramids(rcg_ctx* ctx, const PyramidDesc& pd, const float* d_ref, const float* d_dist, double* d_score,
+                   SearchState* search, StepDesc* step) {
+  double* partials = (double*)workspace(ctx, "score_partials", (size_t)pd.total_tiles * kScoreSums * sizeof(double));
+  double* scale_sums = (double*)workspace(ctx, "score_scale_sums", kMaxScales * kScoreSums * sizeof(double));
+  unsigned* counter = (unsigned*)workspace(ctx, "score_counter", 256);
+  if (!partials || !scale_sums || !counter) return RCG_NO_MEMORY;
+  RCG_LAUNCH(ctx, "ssim2_tiles", k_ssim2_tiles, pd.total_tiles, kTileThreads, kTileSmem, pd, d_ref, d_dist, partials,
+             step);
+  dim3 rg(pd.nscales, kScoreSums);
+  RCG_LAUNCH(ctx, "ssim2_reduce", k_ssim2_reduce, rg, 256, 0, pd, partials, scale_sums, counter, d_score, search,
+             step);
+  return RCG_OK;
+}
+
+}  // namespace rcg

@@ -1,0 +1,368 @@
+"""Python host side of rcg: the reference's JPEG quality-search interface over the C ABI in include/rcg.h.
+
+Names and argument meaning follow rust-compress:
+  ssimulacra2(reference, distorted) -> float            core/src/ssimulacra2.rs:471
+  build_coefs(src, EncodeOptions) -> CoefImage          jpeg/src/encode.rs:426
+  reconstruct(CoefImage) -> Image                        jpeg/src/decode.rs:334
+  find_quality_ssimulacra2(reference, target, max_q, opts) -> Found
+      = jpeg::target::find_quality_with (jpeg/src/target.rs:29) with make = build_coefs and
+        metric = ssimulacra2(..).unwrap_or(f64::MIN) (cli/src/pipeline.rs:207-222)
+Errors surface as RcgError carrying the C status (Invalid / Unsupported like rc_core::error::Error).
+
+Images are numpy uint8 arrays: (h, w, 3) for Rgb, (h, w) or (h, w, 1) for Gray; the scorer also takes
+(h, w, 2|4) with alpha and uint16 arrays (16-bit samples). The library is loaded from this directory; there is no
+fallback: if librcg.so is missing or cannot be loaded, importing the bindings raises.
+"""
+
+import ctypes
+import enum
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "librcg.so")
+
+RCG_OK, RCG_INVALID, RCG_UNSUPPORTED, RCG_CUDA_ERROR, RCG_TIMEOUT, RCG_NO_MEMORY = range(6)
+_STATUS_NAMES = {1: "Invalid", 2: "Unsupported", 3: "CudaError", 4: "Timeout", 5: "NoMemory"}
+
+
+class RcgError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{_STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+        self.message = message
+
+
+class Subsampling(enum.IntEnum):
+    """jpeg::encode::Subsampling (jpeg/src/encode.rs:12-20)."""
+
+    Auto = 0
+    S444 = 1
+    S422 = 2
+    S420 = 3
+
+
+@dataclass
+class EncodeOptions:
+    """jpeg::encode::EncodeOptions (jpeg/src/encode.rs:22-37); alpha must be flattened by the caller."""
+
+    quality: int = 80
+    subsampling: Subsampling = Subsampling.Auto
+    trellis: bool = True
+
+
+class _Opts(ctypes.Structure):
+    _fields_ = [("quality", ctypes.c_int32), ("subsampling", ctypes.c_int32), ("trellis", ctypes.c_int32)]
+
+
+class _Layout(ctypes.Structure):
+    _fields_ = [
+        ("ncomp", ctypes.c_int32),
+        ("h", ctypes.c_int32 * 3),
+        ("v", ctypes.c_int32 * 3),
+        ("blocks_w", ctypes.c_int32 * 3),
+        ("blocks_h", ctypes.c_int32 * 3),
+        ("ncoefs", ctypes.c_int64),
+    ]
+
+
+class _Found(ctypes.Structure):
+    _fields_ = [
+        ("quality", ctypes.c_int32),
+        ("score", ctypes.c_double),
+        ("nsteps", ctypes.c_int32),
+        ("trace_q", ctypes.c_int32 * 16),
+        ("trace_score", ctypes.c_double * 16),
+    ]
+
+
+@dataclass
+class CoefComponent:
+    """jpeg::encode::CoefComponent (jpeg/src/encode.rs:56-69)."""
+
+    id: int
+    h: int
+    v: int
+    tq: int
+    blocks_w: int
+    blocks_h: int
+    coefs: np.ndarray  # int16, (blocks_h * blocks_w * 64,), zigzag order per block
+
+
+@dataclass
+class CoefImage:
+    """jpeg::encode::CoefImage (jpeg/src/encode.rs:71-83), restricted to what the pixel path produces."""
+
+    width: int
+    height: int
+    comps: list
+    qtables: np.ndarray  # uint8 (2, 64), natural order, slot 0 luma, slot 1 chroma
+
+    def flat(self):
+        return np.concatenate([c.coefs for c in self.comps]).astype(np.int16, copy=False)
+
+    def layout(self):
+        lay = _Layout()
+        lay.ncomp = len(self.comps)
+        for i, c in enumerate(self.comps):
+            lay.h[i], lay.v[i] = c.h, c.v
+            lay.blocks_w[i], lay.blocks_h[i] = c.blocks_w, c.blocks_h
+        lay.ncoefs = sum(c.coefs.size for c in self.comps)
+        return lay
+
+
+@dataclass
+class Found:
+    """jpeg::target::Found (jpeg/src/target.rs:12-18) plus the evaluated (quality, score) trace."""
+
+    quality: int
+    score: float
+    coefs: CoefImage
+    trace: list = field(default_factory=list)
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with __graft_entry__.build() (no CPU fallback exists)")
+    lib = ctypes.CDLL(LIB_PATH)
+    P = ctypes.c_void_p
+    u32, i32, sz = ctypes.c_uint32, ctypes.c_int, ctypes.c_size_t
+    sig = {
+        "rcg_ctx_create": (i32, [i32, ctypes.POINTER(P)]),
+        "rcg_ctx_destroy": (None, [P]),
+        "rcg_last_error": (ctypes.c_char_p, [P]),
+        "rcg_ctx_set_stream": (i32, [P, P]),
+        "rcg_ctx_stream": (P, [P]),
+        "rcg_ctx_synchronize": (i32, [P]),
+        "rcg_ctx_launch_count": (ctypes.c_uint64, [P]),
+        "rcg_ctx_set_profiling": (i32, [P, i32]),
+        "rcg_ctx_kernel_time": (i32, [P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64),
+                                      ctypes.POINTER(ctypes.c_double)]),
+        "rcg_coef_layout_for": (i32, [u32, u32, i32, ctypes.POINTER(_Opts), ctypes.POINTER(_Layout)]),
+        "rcg_ssimulacra2": (i32, [P, P, P, u32, u32, i32, i32, ctypes.POINTER(ctypes.c_double)]),
+        "rcg_ssimulacra2_device": (i32, [P, P, P, u32, u32, i32, ctypes.POINTER(ctypes.c_double)]),
+        "rcg_build_coefs": (i32, [P, P, u32, u32, i32, ctypes.POINTER(_Opts), P, sz, P]),
+        "rcg_reconstruct": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, P, P, sz]),
+        "rcg_search": (i32, [P, P, u32, u32, i32, ctypes.c_double, i32, ctypes.POINTER(_Opts),
+                             ctypes.POINTER(_Found), P, sz, P]),
+        "rcg_search_device": (i32, [P, P, u32, u32, i32, ctypes.c_double, i32, ctypes.POINTER(_Opts),
+                                    ctypes.POINTER(_Found), P, sz, P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+_lib = _load()
+EXPORTED = (
+    "rcg_ctx_create rcg_ctx_destroy rcg_last_error rcg_ctx_set_stream rcg_ctx_stream rcg_ctx_synchronize "
+    "rcg_ctx_launch_count rcg_ctx_set_profiling rcg_ctx_kernel_time rcg_coef_layout_for rcg_ssimulacra2 "
+    "rcg_ssimulacra2_device rcg_build_coefs rcg_reconstruct rcg_search rcg_search_device"
+).split()
+
+
+def lib():
+    return _lib
+
+
+def _opts(o):
+    return _Opts(int(o.quality), int(o.subsampling), 1 if o.trellis else 0)
+
+
+def _image(img):
+    """(data, w, h, channels, depth) of an image array, C-contiguous."""
+    a = np.ascontiguousarray(img)
+    if a.ndim == 2:
+        a = a[:, :, None]
+    if a.ndim != 3:
+        raise ValueError("image must be (h, w) or (h, w, c)")
+    h, w, c = a.shape
+    if a.dtype == np.uint8:
+        depth = 8
+    elif a.dtype == np.uint16:
+        depth = 16
+        a = a.astype(">u2")  # the reference stores 16-bit samples big-endian (core/src/image.rs:103)
+    else:
+        raise ValueError("image samples must be uint8 or uint16")
+    return np.ascontiguousarray(a), w, h, c, depth
+
+
+class Context:
+    """One rcg_ctx: a CUDA stream plus device workspace. Not thread-safe; use one per thread."""
+
+    def __init__(self, device=0):
+        self._ptr = ctypes.c_void_p()
+        rc = _lib.rcg_ctx_create(int(device), ctypes.byref(self._ptr))
+        if rc != RCG_OK:
+            raise RcgError(rc, f"cannot create a context on CUDA device {device}")
+
+    def close(self):
+        if self._ptr:
+            _lib.rcg_ctx_destroy(self._ptr)
+            self._ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._ptr
+
+    def _check(self, rc):
+        if rc != RCG_OK:
+            raise RcgError(rc, _lib.rcg_last_error(self._ptr).decode())
+
+    # ---- plumbing
+    def set_stream(self, stream_ptr):
+        self._check(_lib.rcg_ctx_set_stream(self._ptr, ctypes.c_void_p(stream_ptr or 0)))
+
+    def stream(self):
+        return _lib.rcg_ctx_stream(self._ptr)
+
+    def synchronize(self):
+        self._check(_lib.rcg_ctx_synchronize(self._ptr))
+
+    def launch_count(self):
+        return int(_lib.rcg_ctx_launch_count(self._ptr))
+
+    def set_profiling(self, on):
+        self._check(_lib.rcg_ctx_set_profiling(self._ptr, 1 if on else 0))
+
+    def kernel_time(self, name):
+        n = ctypes.c_uint64()
+        ms = ctypes.c_double()
+        self._check(_lib.rcg_ctx_kernel_time(self._ptr, name.encode(), ctypes.byref(n), ctypes.byref(ms)))
+        return int(n.value), float(ms.value)
+
+    # ---- the path
+    def ssimulacra2(self, reference, distorted):
+        """core/src/ssimulacra2.rs:471: score of `distorted` against `reference` (RcgError on Invalid)."""
+        a, w, h, c, d = _image(reference)
+        b, w2, h2, c2, d2 = _image(distorted)
+        if (w, h) != (w2, h2):
+            raise RcgError(RCG_INVALID, "images differ in size")
+        if (c, d) != (c2, d2):
+            raise RcgError(RCG_INVALID, "images differ in colour type")
+        out = ctypes.c_double()
+        self._check(_lib.rcg_ssimulacra2(self._ptr, a.ctypes.data, b.ctypes.data, w, h, c, d, ctypes.byref(out)))
+        return out.value
+
+    def ssimulacra2_device(self, ref_ptr, dist_ptr, width, height, channels):
+        out = ctypes.c_double()
+        self._check(_lib.rcg_ssimulacra2_device(self._ptr, ctypes.c_void_p(ref_ptr), ctypes.c_void_p(dist_ptr),
+                                                width, height, channels, ctypes.byref(out)))
+        return out.value
+
+    def coef_layout(self, width, height, channels, opts):
+        lay = _Layout()
+        o = _opts(opts)
+        rc = _lib.rcg_coef_layout_for(width, height, channels, ctypes.byref(o), ctypes.byref(lay))
+        if rc != RCG_OK:
+            raise RcgError(rc, "bad layout request")
+        return lay
+
+    def build_coefs(self, src, opts):
+        """jpeg/src/encode.rs:426: quantized DCT coefficients of an 8-bit Gray/Rgb image."""
+        a, w, h, c, d = _image(src)
+        if d != 8 or c not in (1, 3):
+            raise RcgError(RCG_INVALID, "build_coefs takes 8-bit Gray or Rgb")
+        lay = self.coef_layout(w, h, c, opts)
+        coefs = np.zeros(lay.ncoefs, dtype=np.int16)
+        qt = np.zeros((2, 64), dtype=np.uint8)
+        o = _opts(opts)
+        self._check(_lib.rcg_build_coefs(self._ptr, a.ctypes.data, w, h, c, ctypes.byref(o), coefs.ctypes.data,
+                                         coefs.size, qt.ctypes.data))
+        return _coef_image(w, h, lay, coefs, qt)
+
+    def reconstruct(self, ci):
+        """jpeg/src/decode.rs:334: the pixels a viewer would show (Gray (h, w) or Rgb (h, w, 3) uint8)."""
+        lay = ci.layout()
+        flat = np.ascontiguousarray(ci.flat())
+        qt = np.ascontiguousarray(ci.qtables, dtype=np.uint8)
+        nc = len(ci.comps)
+        out = np.zeros((ci.height, ci.width, nc), dtype=np.uint8)
+        self._check(_lib.rcg_reconstruct(self._ptr, ci.width, ci.height, ctypes.byref(lay), qt.ctypes.data,
+                                         flat.ctypes.data, out.ctypes.data, out.size))
+        return out[:, :, 0] if nc == 1 else out
+
+    def find_quality_ssimulacra2(self, reference, target, max_quality=100, opts=None):
+        """The --target-ssimulacra2 search (jpeg/src/target.rs:29 with cli/src/pipeline.rs:207-222), on device."""
+        opts = opts or EncodeOptions()
+        a, w, h, c, d = _image(reference)
+        if d != 8 or c not in (1, 3):
+            raise RcgError(RCG_INVALID, "the search takes 8-bit Gray or Rgb")
+        # Size the output for the largest layout the options allow (Auto switches layout at quality 90).
+        cap = 0
+        for q in (1, 89, 90, 100):
+            cap = max(cap, self.coef_layout(w, h, c, EncodeOptions(q, opts.subsampling, opts.trellis)).ncoefs)
+        coefs = np.zeros(cap, dtype=np.int16)
+        qt = np.zeros((2, 64), dtype=np.uint8)
+        f = _Found()
+        o = _opts(opts)
+        self._check(_lib.rcg_search(self._ptr, a.ctypes.data, w, h, c, float(target), int(max_quality),
+                                    ctypes.byref(o), ctypes.byref(f), coefs.ctypes.data, coefs.size, qt.ctypes.data))
+        lay = self.coef_layout(w, h, c, EncodeOptions(f.quality, opts.subsampling, opts.trellis))
+        ci = _coef_image(w, h, lay, coefs[: lay.ncoefs].copy(), qt)
+        trace = [(int(f.trace_q[i]), float(f.trace_score[i])) for i in range(f.nsteps)]
+        return Found(int(f.quality), float(f.score), ci, trace)
+
+    def search_device(self, src_ptr, width, height, channels, target, max_quality, opts, coefs_ptr=0,
+                      coefs_len=0, qt_ptr=0):
+        """rcg_search_device: image and outputs already on the device; returns (quality, score, trace)."""
+        f = _Found()
+        o = _opts(opts)
+        self._check(_lib.rcg_search_device(self._ptr, ctypes.c_void_p(src_ptr), width, height, channels,
+                                           float(target), int(max_quality), ctypes.byref(o), ctypes.byref(f),
+                                           ctypes.c_void_p(coefs_ptr or 0), coefs_len, ctypes.c_void_p(qt_ptr or 0)))
+        trace = [(int(f.trace_q[i]), float(f.trace_score[i])) for i in range(f.nsteps)]
+        return int(f.quality), float(f.score), trace
+
+
+def _coef_image(w, h, lay, coefs, qt):
+    comps = []
+    off = 0
+    for i in range(lay.ncomp):
+        n = lay.blocks_w[i] * lay.blocks_h[i] * 64
+        comps.append(CoefComponent(i + 1, lay.h[i], lay.v[i], min(i, 1), lay.blocks_w[i], lay.blocks_h[i],
+                                   coefs[off: off + n]))
+        off += n
+    return CoefImage(w, h, comps, qt if lay.ncomp > 1 else qt[:1].repeat(2, axis=0))
+
+
+_default = None
+
+
+def default_context():
+    global _default
+    if _default is None:
+        _default = Context(0)
+    return _default
+
+
+def ssimulacra2(reference, distorted):
+    return default_context().ssimulacra2(reference, distorted)
+
+
+def build_coefs(src, opts):
+    return default_context().build_coefs(src, opts)
+
+
+def reconstruct(ci):
+    return default_context().reconstruct(ci)
+
+
+def find_quality_ssimulacra2(reference, target, max_quality=100, opts=None):
+    return default_context().find_quality_ssimulacra2(reference, target, max_quality, opts)

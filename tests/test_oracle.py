@@ -1,0 +1,310 @@
+"""The CPU oracle pinned against the reference's golden vectors and its own unit-test known answers.
+
+The oracle is the checker of every GPU parity test, so it is checked first: SSIMULACRA2 against the 54 golden
+pairs of fixtures/ssim2/expected.csv (cli/tests/ssimulacra2.rs:10-38), the DCT / rounding / trellis known answers of
+jpeg/src/dct.rs:131-211 and jpeg/src/rdo.rs:122-162, and the scorer unit tests of core/src/ssimulacra2.rs:514-634.
+"""
+
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+# cli/tests/ssimulacra2.rs:8 allows 1e-4; the restatement reproduces the reference's ~7e-6 (README.md:118).
+GOLDEN_TOL = 1e-5
+
+
+def test_golden_pairs(oracle, golden):
+    worst = 0.0
+    for name, ref, dist, want in golden:
+        got = oracle.ssimulacra2(ref, dist)
+        assert math.isfinite(got)
+        worst = max(worst, abs(got - want))
+        assert abs(got - want) <= GOLDEN_TOL, f"{name}: {got} vs {want}"
+    assert len(golden) == 54
+    assert worst < GOLDEN_TOL
+
+
+def test_golden_pairs_fp64_variant(oracle, golden):
+    # The FP64 oracle keeps the planes in f64 like py-ssimulacra2: it agrees with the expected scores to ~1e-10.
+    for name, ref, dist, want in golden:
+        assert abs(oracle.ssimulacra2(ref, dist, fp64=True) - want) < 1e-8, name
+
+
+def test_identical_is_exactly_100(oracle, golden):
+    for name, ref, dist, want in golden:
+        if name.startswith("identical") or name == "gray_identical":
+            assert oracle.ssimulacra2(ref, ref) == 100.0
+            assert want == 100.0
+
+
+# ---- jpeg/src/dct.rs:131-211
+
+
+def _random_block(seed):
+    s = seed
+    b = np.zeros((8, 8), dtype=np.float32)
+    for y in range(8):
+        for x in range(8):
+            s = (s * 1664525 + 1013904223) & 0xFFFFFFFF
+            b[y, x] = float((s >> 24) - 128)
+    return b
+
+
+def _naive_dct(b):
+    out = np.zeros((8, 8))
+    for u in range(8):
+        for v in range(8):
+            s = 0.0
+            for y in range(8):
+                for x in range(8):
+                    s += (b[y, x] * math.cos((2 * x + 1) * u * math.pi / 16.0)
+                          * math.cos((2 * y + 1) * v * math.pi / 16.0))
+            a = lambda k: 1 / math.sqrt(2) if k == 0 else 1.0
+            out[u, v] = 0.25 * a(u) * a(v) * s
+    return out
+
+
+def test_fdct_matches_naive_dct(oracle):
+    aan = np.ctypeslib.as_array(oracle.lib().orc_aan(), shape=(8,))
+    for seed in range(20):
+        b = _random_block(seed)
+        want = _naive_dct(b)
+        got = np.ascontiguousarray(b.copy())
+        oracle.lib().orc_fdct(got.ctypes.data)
+        for u in range(8):
+            for v in range(8):
+                g = got[u, v] / (8.0 * aan[u] * aan[v])
+                assert abs(g - want[u, v]) < 1e-2
+
+
+def test_idct_inverts_dct(oracle):
+    aan = np.ctypeslib.as_array(oracle.lib().orc_aan(), shape=(8,))
+    for seed in range(20):
+        b = _random_block(seed + 100)
+        c = _naive_dct(b)
+        inp = np.zeros((8, 8), dtype=np.float32)
+        for v in range(8):
+            for u in range(8):
+                inp[v, u] = c[u, v] * aan[u] * aan[v]
+        inp = np.ascontiguousarray(inp)
+        oracle.lib().orc_idct(inp.ctypes.data)
+        assert np.all(np.abs(inp - b) < 1e-2)
+
+
+def test_round_f32(oracle):
+    r = oracle.lib().orc_round_f32
+    assert r(2.4) == 2 and r(2.6) == 3 and r(-2.6) == -3 and r(-0.4) == 0
+    assert r(2.5) == 2 and r(3.5) == 4 and r(-2.5) == -2  # ties to even
+
+
+# ---- jpeg/src/rdo.rs:122-162
+
+
+def _flat_sizes():
+    s = np.array([4 + min(i >> 4, 8) + min(i & 15, 4) for i in range(256)], dtype=np.uint8)
+    s[0] = 3
+    s[0xF0] = 8
+    return s
+
+
+def _rdo(oracle, table, kappa, sizes, a):
+    out = np.zeros(64, dtype=np.int16)
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    oracle.lib().orc_rdo_quantize_ac(np.ascontiguousarray(table).ctypes.data, ctypes.c_float(kappa),
+                                     np.ascontiguousarray(sizes).ctypes.data, a.ctypes.data, out.ctypes.data)
+    return out
+
+
+def test_zero_lambda_equals_plain_rounding(oracle):
+    a = np.array([((k * np.float32(7.3)) % np.float32(5.0)) - np.float32(2.43) for k in range(64)], dtype=np.float32)
+    out = _rdo(oracle, np.full(64, 10, np.uint8), 0.0, _flat_sizes(), a)
+    for k in range(1, 64):
+        want = int(np.trunc(a[k] + np.float32(0.5) * np.sign(a[k])))
+        assert out[k] == want, (k, a[k])
+
+
+def test_large_lambda_zeroes_marginal_coefficients(oracle):
+    a = np.zeros(64, dtype=np.float32)
+    a[5] = 0.6
+    a[1] = 9.0
+    out = _rdo(oracle, np.full(64, 10, np.uint8), 4.0, _flat_sizes(), a)
+    assert out[5] == 0
+    assert out[1] >= 8
+
+
+# ---- core/src/util/huffman.rs:10-86
+
+
+def _lengths(oracle, freqs, max_len=16):
+    f = np.ascontiguousarray(freqs, dtype=np.uint32)
+    out = np.zeros(len(f), dtype=np.uint8)
+    oracle.lib().orc_build_lengths(f.ctypes.data, len(f), max_len, out.ctypes.data)
+    return out
+
+
+def test_build_lengths_properties(oracle):
+    rng = np.random.default_rng(0)
+    for trial in range(50):
+        n = int(rng.integers(2, 257))
+        f = rng.integers(0, 1000, size=n).astype(np.uint32)
+        f[rng.integers(0, n)] = 1
+        if trial % 5 == 0:
+            f = (rng.pareto(0.5, size=n) * 10).astype(np.uint32)  # skewed: exercises the length limit
+        L = _lengths(oracle, f)
+        used = f > 0
+        assert np.all((L > 0) == used) or used.sum() == 1
+        assert L.max() <= 16
+        if used.sum() > 1:
+            kraft = sum(2.0 ** -int(l) for l in L[used])
+            assert abs(kraft - 1.0) < 1e-12  # complete code
+
+
+def test_build_lengths_edge_cases(oracle):
+    assert list(_lengths(oracle, [0, 0, 0])) == [0, 0, 0]
+    assert list(_lengths(oracle, [0, 5, 0])) == [0, 1, 0]
+    L = _lengths(oracle, [1, 1])
+    assert list(L) == [1, 1]
+
+
+# ---- core/src/ssimulacra2.rs:514-634
+
+
+def _noise(seed):
+    seed[0] = (seed[0] * 1664525 + 1013904223) & 0xFFFFFFFF
+    return seed[0] >> 24
+
+
+def picture(w, h, amp, seed):
+    """The reference's test picture (core/src/ssimulacra2.rs:524-539)."""
+    s = [seed]
+    out = np.zeros((h, w, 3), dtype=np.uint8)
+    for y in range(h):
+        for x in range(w):
+            base = [x * 255 // max(w, 1), y * 255 // max(h, 1), (x + y) * 255 // max(w + h, 1)]
+            for c, b in enumerate(base):
+                n = 0 if amp == 0 else int((_noise(s) - 128) * amp / 128)
+                out[y, x, c] = min(max(b + n, 0), 255)
+    return out
+
+
+def test_more_damage_scores_lower(oracle):
+    r = picture(96, 80, 0, 3)
+    scores = [oracle.ssimulacra2(r, picture(96, 80, amp, 3)) for amp in (4, 16, 48, 120)]
+    assert all(a > b for a, b in zip(scores, scores[1:])), scores
+    assert scores[0] < 100.0
+
+
+def test_awkward_sizes_give_finite_scores(oracle):
+    for w, h in [(8, 8), (9, 13), (8, 100), (100, 8), (17, 33), (255, 9), (57, 55), (300, 11)]:
+        assert math.isfinite(oracle.ssimulacra2(picture(w, h, 0, 5), picture(w, h, 25, 5)))
+
+
+def test_small_images_are_rejected(oracle):
+    with pytest.raises(ValueError):
+        oracle.ssimulacra2(picture(7, 32, 0, 4), picture(7, 32, 0, 4))
+    with pytest.raises(ValueError):
+        oracle.ssimulacra2(picture(32, 7, 0, 4), picture(32, 7, 0, 4))
+
+
+def test_gray_is_scored_as_replicated_rgb(oracle):
+    w, h = 48, 40
+    s = [7]
+    gray = np.array([((i % w) * 5 + _noise(s) // 8) & 0xFF for i in range(w * h)], dtype=np.uint8).reshape(h, w)
+    s2 = [8]
+    gray2 = np.array([min(255, int(v) + _noise(s2) // 16) for v in gray.ravel()], dtype=np.uint8).reshape(h, w)
+    rgb = lambda g: np.repeat(g[:, :, None], 3, axis=2)
+    assert oracle.ssimulacra2(gray, gray2) == oracle.ssimulacra2(rgb(gray), rgb(gray2))
+
+
+def test_sixteen_bit_replicating_eight_bit_scores_identically(oracle):
+    a, b = picture(50, 44, 0, 9), picture(50, 44, 30, 9)
+    up = lambda i: i.astype(np.uint16) * 257
+    assert oracle.ssimulacra2(a, b) == oracle.ssimulacra2(up(a), up(b))
+
+
+def test_alpha_is_composited(oracle):
+    w = h = 40
+
+    def rgba(hidden):
+        d = np.zeros((h, w, 4), dtype=np.uint8)
+        d[:, :20] = [200, 100, 50, 255]
+        d[:, 20:] = [hidden, hidden // 2, 255 - hidden, 0]
+        return d
+
+    assert oracle.ssimulacra2(rgba(0), rgba(255)) == 100.0
+    rgb = picture(w, h, 0, 11)
+    with_alpha = np.concatenate([rgb, np.full((h, w, 1), 255, np.uint8)], axis=2)
+    other = picture(w, h, 40, 11)
+    other_a = np.concatenate([other, np.full((h, w, 1), 255, np.uint8)], axis=2)
+    assert oracle.ssimulacra2(rgb, other) == oracle.ssimulacra2(with_alpha, other_a)
+
+
+def test_repeated_calls_agree_bit_for_bit(oracle):
+    a, b = picture(130, 97, 0, 12), picture(130, 97, 20, 12)
+    assert oracle.ssimulacra2(a, b) == oracle.ssimulacra2(a, b)
+
+
+# ---- encoder / decoder / search restatement
+
+
+def test_oracle_encode_decode_roundtrip(oracle):
+    import rcg.synth as synth
+
+    img = synth.image(96, 72, 0)
+    for sub in (1, 2, 3, 0):
+        for q in (30, 75, 95, 100):
+            coefs, qt, lay = oracle.build_coefs(img, q, sub, True)
+            rec = oracle.reconstruct(96, 72, lay, qt, coefs)
+            assert rec.shape == img.shape
+            err = np.abs(rec.astype(int) - img.astype(int)).mean()
+            assert err < (12 if q < 50 else 6), (sub, q, err)
+
+
+def test_oracle_threads_do_not_change_results(oracle):
+    import rcg.synth as synth
+
+    img = synth.image(200, 150, 3)
+    oracle.set_threads(1)
+    a = oracle.build_coefs(img, 60, 3, True)[0]
+    s1 = oracle.ssimulacra2(img, synth.image(200, 150, 4))
+    oracle.set_threads(max(2, oracle.max_threads()))
+    b = oracle.build_coefs(img, 60, 3, True)[0]
+    s2 = oracle.ssimulacra2(img, synth.image(200, 150, 4))
+    assert np.array_equal(a, b) and s1 == s2
+
+
+def test_oracle_search_follows_bisection(oracle):
+    import rcg.synth as synth
+
+    img = synth.image(128, 96, 5)
+    for target in (40.0, 60.0, 99.0):
+        q, s, coefs, qt, lay, trace = oracle.search(img, target, 100, 3, True)
+        assert trace[0][0] == 100
+        if trace[0][1] < target:  # even the maximum quality misses: best effort (jpeg/src/target.rs:35-37)
+            assert len(trace) == 1 and q == 100
+            continue
+        lo, hi = 1, 100
+        best = 100
+        for qq, ss in trace[1:]:
+            assert qq == lo + (hi - lo) // 2
+            if ss >= target:
+                hi, best = qq, qq
+            else:
+                lo = qq + 1
+        assert lo == hi and q == best and s >= target
+
+
+def test_write_best_produces_a_jpeg(oracle):
+    import rcg.synth as synth
+
+    img = synth.image(64, 48, 1)
+    coefs, qt, lay = oracle.build_coefs(img, 75, 3, True)
+    data, progressive = oracle.write_best(64, 48, lay, qt, coefs)
+    assert data[:2] == b"\xff\xd8" and data[-2:] == b"\xff\xd9"
+    sof = b"\xff\xc2" if progressive else b"\xff\xc0"
+    i = data.index(sof)
+    # SOF: precision 8, height, width, 3 components with 2x2 luma sampling (jpeg/src/encode.rs:664-671)
+    assert data[i + 4] == 8 and int.from_bytes(data[i + 5: i + 7], "big") == 48
+    assert int.from_bytes(data[i + 7: i + 9], "big") == 64 and data[i + 9] == 3 and data[i + 11] == 0x22
