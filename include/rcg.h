@@ -4,7 +4,8 @@
  * C ABI. Plain pointers and sizes only; every call returns an rcg_status and never aborts the process. Buffers
  * passed in are owned by the caller and never freed here. Device memory is owned by an opaque rcg_ctx. A context
  * holds its own CUDA stream and workspace and is not thread-safe: use one context per calling thread (the
- * reference runs one search per rayon worker, cli/src/main.rs:57-60). There is no global mutable state.
+ * reference runs one search per rayon worker, cli/src/main.rs:57-60). Contexts share no mutable state; the only
+ * global state is the fixed scratch array of rcg_ssimulacra2_device_noalloc (see there).
  *
  * Image data: 8-bit samples, interleaved, row-major, no row padding (rc_core::image::Image, core/src/image.rs:103-113).
  * `channels` is 1 (Gray) or 3 (Rgb) for the encoder and the search (the reference encodes flattened 8-bit Gray/Rgb
@@ -96,6 +97,21 @@ int rcg_ssimulacra2(rcg_ctx* ctx, const uint8_t* reference, const uint8_t* disto
 /* The same on device buffers (8-bit Gray/Rgb only); no host<->device copies besides the 8-byte score. */
 int rcg_ssimulacra2_device(rcg_ctx* ctx, const uint8_t* d_reference, const uint8_t* d_distorted, uint32_t width,
                            uint32_t height, int channels, double* score);
+
+/* SSIMULACRA 2 of two 8-bit Gray/Rgb images already on the device, for callers that cannot allocate device memory:
+ * this call allocates nothing. No counterpart in the reference (which has no device memory at all); it exists for
+ * hosts that own every device allocation themselves -- a framework whose caching allocator holds a fixed device
+ * budget, or a latency-critical loop where cudaMalloc/cudaFree would synchronize the whole device -- and so cannot let
+ * a library call cudaMalloc. It needs no rcg_ctx. Scratch lives in one fixed device array compiled into the library
+ * (about 10 MB, held on every GPU that loads the library until the process exits), so images are limited to
+ * width*height <= 262144 pixels (e.g. 512x512); larger ones return RCG_INVALID, as do sides < 8 and channels other than
+ * 1 or 3. The score (f64; NaN if it is not finite) is written to the device pointer `d_score`; the work is queued on
+ * `stream` (a cudaStream_t, NULL for the legacy default stream) of the current device and the call returns without
+ * waiting. The first call on a device sets up that device (looks up the scratch address and uploads constant tables),
+ * so make it before any stream capture. Every call on a device shares the one scratch array: calls whose work overlaps
+ * on the GPU (different streams, or other host threads) race and corrupt each other's results; serialize them. */
+int rcg_ssimulacra2_device_noalloc(const uint8_t* d_reference, const uint8_t* d_distorted, uint32_t width,
+                                   uint32_t height, int channels, double* d_score, void* stream);
 
 /* jpeg::encode::build_coefs(src, opts) -> CoefImage (jpeg/src/encode.rs:426). `src` is 8-bit Gray/Rgb on the host.
  * `coefs` receives layout.ncoefs int16 (capacity `coefs_len`), `qtables` (nullable) 2*64 bytes. */

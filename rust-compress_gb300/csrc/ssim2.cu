@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "rcg_internal.cuh"
 
@@ -541,10 +542,13 @@ PyramidDesc make_pyramid(int w, int h) {
   return pd;
 }
 
+static std::mutex g_scorer_mu;
 static bool g_scorer_ready[64];
 
-int scorer_init(rcg_ctx* ctx) {
-  if (ctx->device >= 0 && ctx->device < 64 && g_scorer_ready[ctx->device]) return RCG_OK;
+// Upload the scorer's constant tables to the current device once (cudaMemcpyToSymbol only; nothing is allocated).
+static cudaError_t scorer_constants(int device) {
+  std::lock_guard<std::mutex> lk(g_scorer_mu);
+  if (device >= 0 && device < 64 && g_scorer_ready[device]) return cudaSuccess;
   // core/src/ssimulacra2.rs:260-271 (kernel): f64 taps, rounded to f32 here.
   double k[2 * kRadius + 1], sum = 0.0;
   for (int i = 0; i < 2 * kRadius + 1; i++) {
@@ -577,14 +581,20 @@ int scorer_init(rcg_ctx* ctx) {
       95.1080498811086, 0.9863978034400682, 0.9834382792465353, 0.0012286405048278493, 171.2667255897307, 0.9807858872435379,
       0.0, 0.0, 0.0, 0.0005130064588990679, 0.0, 0.00010854057858411537};
   cudaError_t e;
-  if ((e = cudaMemcpyToSymbol(c_gauss, kf, sizeof kf)) != cudaSuccess) return cuda_fail(ctx, e, "gauss upload");
-  if ((e = cudaMemcpyToSymbol(c_lut8s, lut, sizeof lut)) != cudaSuccess) return cuda_fail(ctx, e, "lut upload");
-  if ((e = cudaMemcpyToSymbol(c_weights, W, sizeof W)) != cudaSuccess) return cuda_fail(ctx, e, "weights upload");
-  if (int ce = codec_upload_lut(lut)) return cuda_fail(ctx, (cudaError_t)ce, "codec lut upload");
+  if ((e = cudaMemcpyToSymbol(c_gauss, kf, sizeof kf)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_lut8s, lut, sizeof lut)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_weights, W, sizeof W)) != cudaSuccess) return e;
+  if (int ce = codec_upload_lut(lut)) return (cudaError_t)ce;
   if ((e = cudaFuncSetAttribute(k_ssim2_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem)) !=
       cudaSuccess)
-    return cuda_fail(ctx, e, "tile kernel attribute");
-  if (ctx->device >= 0 && ctx->device < 64) g_scorer_ready[ctx->device] = true;
+    return e;
+  if (device >= 0 && device < 64) g_scorer_ready[device] = true;
+  return cudaSuccess;
+}
+
+int scorer_init(rcg_ctx* ctx) {
+  cudaError_t e = scorer_constants(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "scorer constant tables");
   return RCG_OK;
 }
 
@@ -603,3 +613,94 @@ int score_pyramids(rcg_ctx* ctx, const PyramidDesc& pd, const float* d_ref, cons
 }
 
 }  // namespace rcg
+
+// ------------------------------------------------------------------------------------------------ no-alloc scorer
+
+namespace rcg {
+
+// Fixed scratch of rcg_ssimulacra2_device_noalloc: both images' linear pyramids, the per-tile partial sums, the
+// per-scale sums and the reduction's completion counter. Sized for images of at most kNoAllocMaxPixels pixels; every
+// GPU that loads this library holds it (about 10 MB) until the process exits.
+constexpr long long kNoAllocMaxPixels = 512LL * 512LL;
+constexpr long long kNoAllocPyrFloats = 1200000;  // one image: 3 channels x every scale, with margin
+constexpr int kNoAllocMaxTiles = 4096;
+constexpr size_t kNoAllocPyrBytes = (size_t)kNoAllocPyrFloats * sizeof(float);
+constexpr size_t kNoAllocPartialOff = 2 * kNoAllocPyrBytes;
+constexpr size_t kNoAllocSumsOff = kNoAllocPartialOff + (size_t)kNoAllocMaxTiles * kScoreSums * sizeof(double);
+constexpr size_t kNoAllocCounterOff = kNoAllocSumsOff + (size_t)kMaxScales * kScoreSums * sizeof(double);
+constexpr size_t kNoAllocBytes = kNoAllocCounterOff + 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+static std::mutex g_noalloc_mu;
+static unsigned char* g_noalloc_addr[64];
+
+// Once per device, with that device current: the device address of the scratch (host code cannot use the symbol
+// itself, which names a host-side shadow) and the scorer's constant tables.
+static int noalloc_setup(unsigned char** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return RCG_CUDA_ERROR;
+  }
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      return RCG_CUDA_ERROR;
+    }
+    if (scorer_constants(dev) != cudaSuccess) {
+      cudaGetLastError();
+      return RCG_CUDA_ERROR;
+    }
+    g_noalloc_addr[dev] = (unsigned char*)p;
+  }
+  *out = g_noalloc_addr[dev];
+  return RCG_OK;
+}
+
+}  // namespace rcg
+
+extern "C" int rcg_ssimulacra2_device_noalloc(const uint8_t* d_reference, const uint8_t* d_distorted,
+                                              uint32_t width, uint32_t height, int channels, double* d_score,
+                                              void* stream) {
+  using namespace rcg;
+  if (!d_reference || !d_distorted || !d_score) return RCG_INVALID;
+  if (channels != 1 && channels != 3) return RCG_INVALID;
+  if (width < (uint32_t)kMinSide || height < (uint32_t)kMinSide) return RCG_INVALID;
+  if ((long long)width * (long long)height > kNoAllocMaxPixels) return RCG_INVALID;
+  const int w = (int)width, h = (int)height;
+  PyramidDesc pd = make_pyramid(w, h);
+  if (pd.floats > kNoAllocPyrFloats || pd.total_tiles > kNoAllocMaxTiles) return RCG_INVALID;
+  unsigned char* base = nullptr;
+  int rc = noalloc_setup(&base);
+  if (rc != RCG_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  float* pyr_ref = (float*)base;
+  float* pyr_dist = (float*)(base + kNoAllocPyrBytes);
+  double* partials = (double*)(base + kNoAllocPartialOff);
+  double* sums = (double*)(base + kNoAllocSumsOff);
+  unsigned* counter = (unsigned*)(base + kNoAllocCounterOff);
+  // The scratch keeps whatever the previous call left: the completion counter must start at zero.
+  if (cudaMemsetAsync(counter, 0, sizeof(unsigned), s) != cudaSuccess) {
+    cudaGetLastError();
+    return RCG_CUDA_ERROR;
+  }
+  dim3 lg((w + 255) / 256, std::min(h, 65535));
+  k_to_linear<<<lg, 256, 0, s>>>(d_reference, w, h, channels, 8, nullptr, pyr_ref);
+  k_to_linear<<<lg, 256, 0, s>>>(d_distorted, w, h, channels, 8, nullptr, pyr_dist);
+  for (int sc = 1; sc < pd.nscales; sc++) {
+    const ScaleDesc& a = pd.s[sc - 1];
+    const ScaleDesc& b = pd.s[sc];
+    dim3 dg((b.w + 127) / 128, std::min(b.h, 65535));
+    k_downsample<<<dg, 128, 0, s>>>(pyr_ref + a.off, a.w, a.h, pyr_ref + b.off, nullptr);
+    k_downsample<<<dg, 128, 0, s>>>(pyr_dist + a.off, a.w, a.h, pyr_dist + b.off, nullptr);
+  }
+  k_ssim2_tiles<<<pd.total_tiles, kTileThreads, kTileSmem, s>>>(pd, pyr_ref, pyr_dist, partials, nullptr);
+  k_ssim2_reduce<<<dim3(pd.nscales, kScoreSums), 256, 0, s>>>(pd, partials, sums, counter, d_score, nullptr,
+                                                              nullptr);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? RCG_OK : RCG_CUDA_ERROR;
+}

@@ -143,6 +143,7 @@ def _load():
         "rcg_coef_layout_for": (i32, [u32, u32, i32, ctypes.POINTER(_Opts), ctypes.POINTER(_Layout)]),
         "rcg_ssimulacra2": (i32, [P, P, P, u32, u32, i32, i32, ctypes.POINTER(ctypes.c_double)]),
         "rcg_ssimulacra2_device": (i32, [P, P, P, u32, u32, i32, ctypes.POINTER(ctypes.c_double)]),
+        "rcg_ssimulacra2_device_noalloc": (i32, [P, P, u32, u32, i32, P, P]),
         "rcg_build_coefs": (i32, [P, P, u32, u32, i32, ctypes.POINTER(_Opts), P, sz, P]),
         "rcg_reconstruct": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, P, P, sz]),
         "rcg_search": (i32, [P, P, u32, u32, i32, ctypes.c_double, i32, ctypes.POINTER(_Opts),
@@ -161,7 +162,7 @@ _lib = _load()
 EXPORTED = (
     "rcg_ctx_create rcg_ctx_destroy rcg_last_error rcg_ctx_set_stream rcg_ctx_stream rcg_ctx_synchronize "
     "rcg_ctx_launch_count rcg_ctx_set_profiling rcg_ctx_kernel_time rcg_coef_layout_for rcg_ssimulacra2 "
-    "rcg_ssimulacra2_device rcg_build_coefs rcg_reconstruct rcg_search rcg_search_device"
+    "rcg_ssimulacra2_device rcg_ssimulacra2_device_noalloc rcg_build_coefs rcg_reconstruct rcg_search rcg_search_device"
 ).split()
 
 
