@@ -40,6 +40,14 @@ WORKLOAD = {
 METRIC = "target-ssimulacra2 JPEG searches/s at 12MP"
 
 
+def _set_size(w, h):
+    global W, H
+    W, H = w, h
+    WORKLOAD["width"], WORKLOAD["height"] = w, h
+    if (w, h) != (4000, 3000):
+        WORKLOAD["workload"] = WORKLOAD["workload"].replace("4000x3000", f"{w}x{h}")
+
+
 def _env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK",
                                                                                                         "0"))
@@ -147,7 +155,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="rcg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--width", type=int, default=W, help="smaller cases for profiling only; the bench line uses 4000")
+    ap.add_argument("--height", type=int, default=H)
     args = ap.parse_args()
+    _set_size(args.width, args.height)
     if args.impl == "reference":
         return run_reference(args)
 
