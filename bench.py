@@ -249,7 +249,7 @@ def main():
     for _ in range(3):
         step_device()
     prof = {}
-    for k in ("ssim2_tiles", "trellis", "quantize", "dequant_idct", "upsample_color", "downsample", "ssim2_reduce",
+    for k in ("ssim2_tiles", "trellis", "quantize", "dequant_idct", "upsample_color", "pyramid", "ssim2_reduce",
               "rate_tables", "step_tables", "fdct_cache", "color_pad", "chroma_down", "to_linear"):
         n, ms = ctx.kernel_time(k)
         prof[k] = {"launches": n, "ms": ms}

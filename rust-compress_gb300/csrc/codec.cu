@@ -88,16 +88,6 @@ __device__ __forceinline__ int round_f32(float x) {
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
 
-// jpeg/src/quality.rs:6-15 (scale_table over PERCEPTUAL_Q; luma_table == chroma_table, :37-43)
-__host__ __device__ inline void scale_table(int quality, uint8_t* out) {
-  unsigned q = (unsigned)(quality < 1 ? 1 : (quality > 100 ? 100 : quality));
-  unsigned scale = q < 50 ? 5000 / q : 200 - 2 * q;
-  for (int i = 0; i < 64; i++) {
-    unsigned v = ((unsigned)perceptual_q(i) * scale + 50) / 100;
-    out[i] = (uint8_t)(v < 1 ? 1 : (v > 255 ? 255 : v));
-  }
-}
-
 // Sampling factors build_coefs chooses (jpeg/src/encode.rs:428-439).
 __host__ __device__ inline void sampling(int channels, int subsampling, int quality, int* hmax, int* vmax) {
   if (channels == 1) {
@@ -117,13 +107,30 @@ __host__ __device__ inline void sampling(int channels, int subsampling, int qual
 // FDCT cache slot of a component for a sampling layout: 3 caches (Y, Cb, Cr) per layout kind.
 __host__ __device__ inline int layout_kind(int hmax, int vmax) { return hmax == 2 ? (vmax == 2 ? 0 : 1) : 2; }
 
-// The per-quality tables of one candidate: quantization tables (jpeg/src/quality.rs), fdct divisors
-// (jpeg/src/encode.rs:174-183), dequantization multipliers (jpeg/src/decode.rs:1316-1321), the Rdo parameters that
-// do not depend on the rate model (jpeg/src/rdo.rs:28-45), and the block layout (jpeg/src/encode.rs:440-517).
-// Shared by the host (single calls) and the device (search steps) so both produce identical bits.
-__host__ __device__ inline void fill_step(StepDesc* st, int quality, int subsampling, int channels, int trellis, int w,
-                                          int h) {
-  const float kappa = 0.02f;  // TRELLIS_KAPPA, jpeg/src/encode.rs:42
+// One entry of the per-quality tables, shared by the host (fill_step) and the device (k_step_tables) so both give
+// identical bits. `q` is the quantization table (natural order).
+//   quant value at natural index n (jpeg/src/quality.rs:6-15)
+__host__ __device__ inline uint8_t qtable_entry(int quality, int n) {
+  unsigned q = (unsigned)(quality < 1 ? 1 : (quality > 100 ? 100 : quality));
+  unsigned scale = q < 50 ? 5000 / q : 200 - 2 * q;
+  unsigned v = ((unsigned)perceptual_q(n) * scale + 50) / 100;
+  return (uint8_t)(v < 1 ? 1 : (v > 255 ? 255 : v));
+}
+//   fdct divisor for zigzag position k: fdct_divisors stores 1 / (q[v*8+u] * AAN[u] * AAN[v] * 8) at [u*8+v]
+//   (jpeg/src/encode.rs:174-183) and quantize_plane reads it at ZZ_T[k] = (n%8)*8 + n/8 (:202), i.e. u = n%8,
+//   v = n/8, q[v*8+u] = q[n]
+__host__ __device__ inline float divz_entry(const uint8_t* q, int k) {
+  int n = zigzag(k);
+  return fdiv(1.0f, fmul(fmul(fmul((float)q[n], aan(n % 8)), aan(n / 8)), 8.0f));
+}
+//   dequantization multiplier at natural index n = v*8+u: q[v*8+u] * AAN[u] * AAN[v] (jpeg/src/decode.rs:1316-1321)
+__host__ __device__ inline float mult_entry(const uint8_t* q, int n) {
+  return fmul(fmul((float)q[n], aan(n % 8)), aan(n / 8));
+}
+
+// Block layout of a candidate (jpeg/src/encode.rs:428-443, :511-517).
+__host__ __device__ inline void fill_layout(StepDesc* st, int quality, int subsampling, int channels, int trellis,
+                                            int w, int h) {
   st->quality = quality;
   st->use_trellis = (trellis && quality < 100) ? 1 : 0;
   int hmax, vmax;
@@ -149,34 +156,25 @@ __host__ __device__ inline void fill_step(StepDesc* st, int quality, int subsamp
     poff += (long long)cd.bw * 8 * cd.bh * 8;
   }
   st->nblocks = blk;
+}
+
+// The per-quality tables of one candidate: quantization tables (jpeg/src/quality.rs), fdct divisors
+// (jpeg/src/encode.rs:174-183), dequantization multipliers (jpeg/src/decode.rs:1316-1321), the Rdo parameters that
+// do not depend on the rate model (jpeg/src/rdo.rs:28-45), and the block layout (jpeg/src/encode.rs:440-517).
+// Host version (single calls); k_step_tables computes the same entries in parallel on the device.
+inline void fill_step(StepDesc* st, int quality, int subsampling, int channels, int trellis, int w, int h) {
+  const float kappa = 0.02f;  // TRELLIS_KAPPA, jpeg/src/encode.rs:42
+  fill_layout(st, quality, subsampling, channels, trellis, w, h);
   for (int cls = 0; cls < 2; cls++) {
     uint8_t* qt = st->qt[cls];
-    scale_table(quality, qt);
-    // fdct_divisors: d[u*8+v] = 1 / (q[v*8+u] * AAN[u] * AAN[v] * 8), stored here per zigzag position.
-    float div[64];
-    for (int v = 0; v < 8; v++)
-      for (int u = 0; u < 8; u++)
-        div[u * 8 + v] = fdiv(1.0f, fmul(fmul(fmul((float)qt[v * 8 + u], aan(u)), aan(v)), 8.0f));
-    for (int k = 0; k < 64; k++) {
-      int n = zigzag(k);
-      st->divz[cls][k] = div[(n % 8) * 8 + n / 8];
-    }
-    // idct_planes: mult[v][u] = q[v*8+u] * AAN[u] * AAN[v]
-    for (int v = 0; v < 8; v++)
-      for (int u = 0; u < 8; u++) st->mult[cls][v * 8 + u] = fmul(fmul((float)qt[v * 8 + u], aan(u)), aan(v));
+    for (int n = 0; n < 64; n++) qt[n] = qtable_entry(quality, n);
+    for (int k = 0; k < 64; k++) st->divz[cls][k] = divz_entry(qt, k);
+    for (int n = 0; n < 64; n++) st->mult[cls][n] = mult_entry(qt, n);
     // Rdo::new: q per zigzag position, median of q[1..] (sorted, index 31), w = (median/q)^1, lambda.
     float sorted[63];
     for (int k = 0; k < 64; k++) st->rq[cls][k] = (float)qt[zigzag(k)];
     for (int k = 1; k < 64; k++) sorted[k - 1] = st->rq[cls][k];
-    for (int i = 1; i < 63; i++) {
-      float x = sorted[i];
-      int j = i - 1;
-      while (j >= 0 && sorted[j] > x) {
-        sorted[j + 1] = sorted[j];
-        j--;
-      }
-      sorted[j + 1] = x;
-    }
+    std::sort(sorted, sorted + 63);
     float median = sorted[31];
     st->rw[cls][0] = 1.0f;
     // FREQ_WEIGHT_GAMMA is 1.0 (jpeg/src/rdo.rs:12) and pow(x, 1) == x, so w = median / q exactly.
@@ -189,14 +187,12 @@ void fill_mult(StepDesc* st, const uint8_t* qtables, int ntables) {
   for (int cls = 0; cls < 2; cls++) {
     const uint8_t* qt = qtables + 64 * (cls < ntables ? cls : 0);
     std::memcpy(st->qt[cls], qt, 64);
-    for (int v = 0; v < 8; v++)
-      for (int u = 0; u < 8; u++) st->mult[cls][v * 8 + u] = fmul(fmul((float)qt[v * 8 + u], aan(u)), aan(v));
+    for (int n = 0; n < 64; n++) st->mult[cls][n] = mult_entry(qt, n);
   }
 }
 
 void qtables_for(int quality, uint8_t* out128) {
-  scale_table(quality, out128);
-  scale_table(quality, out128 + 64);
+  for (int n = 0; n < 64; n++) out128[n] = out128[64 + n] = qtable_entry(quality, n);
 }
 
 void host_step_tables(StepDesc* st, int quality, int subsampling, int channels, int trellis, int w, int h) {
@@ -360,37 +356,34 @@ __global__ void __launch_bounds__(128) k_quantize(StepDesc* __restrict__ st, Cac
     for (int i = threadIdx.x; i < 512; i += blockDim.x) (&sh[0][0])[i] = 0;
     __syncthreads();
   }
-  long long gb = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gb = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (gb < st->nblocks) {
     int c = comp_of(st, gb);
     const CompDesc& cd = st->comp[c];
-    long long nb = (long long)cd.bw * cd.bh;
-    long long lb = gb - cd.blk0;
-    const float* cache = cs.p[cd.cache] + lb;
+    const long long nb = (long long)cd.bw * cd.bh;
+    const float* cache = cs.p[cd.cache] + (gb - cd.blk0);
     const float* divz = st->divz[cd.cls];
+    // All 64 loads are issued before any is used (fully unrolled into registers).
+    int v[64];
+#pragma unroll
+    for (int k = 0; k < 64; k++) v[k] = clampi(round_f32(fmul(__ldg(cache + (long long)k * nb), divz[k])), -2047, 2047);
     if (!hist) {
       int16_t* out = st->coefs + gb * 64;
 #pragma unroll
       for (int g = 0; g < 8; g++) {
-        int v[8];
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          int k = g * 8 + j;
-          v[j] = clampi(round_f32(fmul(cache[(long long)k * nb], divz[k])), -2047, 2047);
-        }
         int4 pk;
-        pk.x = (v[0] & 0xFFFF) | (v[1] << 16);
-        pk.y = (v[2] & 0xFFFF) | (v[3] << 16);
-        pk.z = (v[4] & 0xFFFF) | (v[5] << 16);
-        pk.w = (v[6] & 0xFFFF) | (v[7] << 16);
+        pk.x = (v[g * 8 + 0] & 0xFFFF) | (v[g * 8 + 1] << 16);
+        pk.y = (v[g * 8 + 2] & 0xFFFF) | (v[g * 8 + 3] << 16);
+        pk.z = (v[g * 8 + 4] & 0xFFFF) | (v[g * 8 + 5] << 16);
+        pk.w = (v[g * 8 + 6] & 0xFFFF) | (v[g * 8 + 7] << 16);
         reinterpret_cast<int4*>(out)[g] = pk;
       }
     } else {
       unsigned* hs = sh[cd.cls];
       unsigned run = 0;
+#pragma unroll
       for (int k = 1; k < 64; k++) {
-        int v = clampi(round_f32(fmul(cache[(long long)k * nb], divz[k])), -2047, 2047);
-        if (v == 0) {
+        if (v[k] == 0) {
           run++;
           continue;
         }
@@ -398,7 +391,7 @@ __global__ void __launch_bounds__(128) k_quantize(StepDesc* __restrict__ st, Cac
           atomicAdd(&hs[0xF0], 1u);
           run -= 16;
         }
-        unsigned size = (unsigned)bitlen((unsigned)abs(v));
+        unsigned size = (unsigned)bitlen((unsigned)abs(v[k]));
         atomicAdd(&hs[(run << 4) | size], 1u);
         run = 0;
       }
@@ -540,12 +533,12 @@ __global__ void __launch_bounds__(128) k_trellis(StepDesc* __restrict__ st, Cach
   if (!st->active || !st->use_trellis) return;
   for (int i = threadIdx.x; i < 2 * 64 * 16; i += blockDim.x) (&lr[0][0])[i] = (&st->lr[0][0])[i];
   __syncthreads();
-  long long gb = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gb = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (gb >= st->nblocks) return;
-  int c = comp_of(st, gb);
+  const int c = comp_of(st, gb);
   const CompDesc& cd = st->comp[c];
   const int cls = cd.cls;
-  long long nb = (long long)cd.bw * cd.bh;
+  const long long nb = (long long)cd.bw * cd.bh;
   const float* cache = cs.p[cd.cache] + (gb - cd.blk0);
   const float* divz = st->divz[cls];
   const float* rq = st->rq[cls];
@@ -558,63 +551,84 @@ __global__ void __launch_bounds__(128) k_trellis(StepDesc* __restrict__ st, Cach
   signed char nprev[128];
   int nn = 0;
   unsigned long long negmask = 0;
-
-  float a0 = fmul(cache[0], divz[0]);
-  int dc = clampi(round_f32(a0), -2047, 2047);
+  int dc = 0;
   float zprev = 0.0f;  // zd[i-1]
-  for (int i = 1; i < 64; i++) {
-    float a = fmul(cache[(long long)i * nb], divz[i]);
-    float q = rq[i], w = rw[i];
-    if (a < 0.0f) negmask |= 1ull << i;
-    float m = fabsf(a);
-    unsigned v0 = (unsigned)fadd(m, 0.5f);
-    if (v0 != 0) {
-      unsigned lo = v0 > 1 ? v0 - 1 : v0;
-      bool two = lo != v0;
-      // candidate lo (first) and v0 (second, if distinct)
-      float e_lo = fmul(fsub(m, (float)lo), q);
-      float dnz_lo = fmul(fmul(e_lo, e_lo), w);
-      float e_hi = fmul(fsub(m, (float)v0), q);
-      float dnz_hi = fmul(fmul(e_hi, e_hi), w);
-      int s_lo = bitlen(lo), s_hi = bitlen(v0);
-      float best_lo = fadd(fadd(zprev, lrc[(i - 1) * 16 + s_lo]), dnz_lo);
-      float best_hi = fadd(fadd(zprev, lrc[(i - 1) * 16 + s_hi]), dnz_hi);
-      int prev_lo = -1, prev_hi = -1;
-      for (int ni = 0; ni < nn; ni++) {
-        float base = fadd(ncost[ni], fsub(zprev, nzd[ni]));
-        int ridx = (i - npos[ni] - 1) * 16;
-        float c_lo = fadd(fadd(base, lrc[ridx + s_lo]), dnz_lo);
-        float c_hi = fadd(fadd(base, lrc[ridx + s_hi]), dnz_hi);
-        if (c_lo < best_lo) {
-          best_lo = c_lo;
-          prev_lo = ni;
-        }
-        if (c_hi < best_hi) {
-          best_hi = c_hi;
-          prev_hi = ni;
-        }
-      }
-      ncost[nn] = best_lo;
-      nzd[nn] = zprev;
-      npos[nn] = (unsigned char)i;
-      nv[nn] = (short)lo;
-      nprev[nn] = (signed char)prev_lo;
-      nn++;
-      if (two) {
-        ncost[nn] = best_hi;
-        nzd[nn] = zprev;
-        npos[nn] = (unsigned char)i;
-        nv[nn] = (short)v0;
-        nprev[nn] = (signed char)prev_hi;
-        nn++;
-      }
+
+  // The coefficients arrive 16 at a time: the next chunk's loads are in flight while this chunk's DP steps run.
+  constexpr int kChunk = 16;
+  float cur[kChunk], nxt[kChunk];
+#pragma unroll
+  for (int j = 0; j < kChunk; j++) cur[j] = __ldg(cache + (long long)j * nb);
+#pragma unroll 1
+  for (int c0 = 0; c0 < 64; c0 += kChunk) {
+    if (c0 + kChunk < 64) {
+#pragma unroll
+      for (int j = 0; j < kChunk; j++) nxt[j] = __ldg(cache + (long long)(c0 + kChunk + j) * nb);
     }
-    // zd[i] = zd[i-1] + (a*q)^2 * w
-    float e = fmul(a, q);
-    float zcur = fadd(zprev, fmul(fmul(e, e), w));
-    // A node at position i stores zd[i] (the reference reads zd[n.pos]).
-    for (int ni = nn - 1; ni >= 0 && npos[ni] == i; ni--) nzd[ni] = zcur;
-    zprev = zcur;
+#pragma unroll
+    for (int j = 0; j < kChunk; j++) {
+      const int i = c0 + j;
+      // a[k] = flat[ZZ_T[k]] * div[ZZ_T[k]] (jpeg/src/encode.rs:207-211)
+      float a = fmul(cur[j], divz[i]);
+      if (i == 0) {
+        dc = clampi(round_f32(a), -2047, 2047);
+        continue;
+      }
+      float q = rq[i], w = rw[i];
+      if (a < 0.0f) negmask |= 1ull << i;
+      float m = fabsf(a);
+      unsigned v0 = (unsigned)fadd(m, 0.5f);
+      int pushed = 0;
+      if (v0 != 0) {
+        unsigned lo = v0 > 1 ? v0 - 1 : v0;
+        bool two = lo != v0;
+        // candidate lo (first) and v0 (second, if distinct)
+        float e_lo = fmul(fsub(m, (float)lo), q);
+        float dnz_lo = fmul(fmul(e_lo, e_lo), w);
+        float e_hi = fmul(fsub(m, (float)v0), q);
+        float dnz_hi = fmul(fmul(e_hi, e_hi), w);
+        int s_lo = bitlen(lo), s_hi = bitlen(v0);
+        float best_lo = fadd(fadd(zprev, lrc[(i - 1) * 16 + s_lo]), dnz_lo);
+        float best_hi = fadd(fadd(zprev, lrc[(i - 1) * 16 + s_hi]), dnz_hi);
+        int prev_lo = -1, prev_hi = -1;
+        for (int ni = 0; ni < nn; ni++) {
+          float base = fadd(ncost[ni], fsub(zprev, nzd[ni]));
+          int ridx = (i - npos[ni] - 1) * 16;
+          float c_lo = fadd(fadd(base, lrc[ridx + s_lo]), dnz_lo);
+          float c_hi = fadd(fadd(base, lrc[ridx + s_hi]), dnz_hi);
+          if (c_lo < best_lo) {
+            best_lo = c_lo;
+            prev_lo = ni;
+          }
+          if (c_hi < best_hi) {
+            best_hi = c_hi;
+            prev_hi = ni;
+          }
+        }
+        ncost[nn] = best_lo;
+        npos[nn] = (unsigned char)i;
+        nv[nn] = (short)lo;
+        nprev[nn] = (signed char)prev_lo;
+        nn++;
+        pushed = 1;
+        if (two) {
+          ncost[nn] = best_hi;
+          npos[nn] = (unsigned char)i;
+          nv[nn] = (short)v0;
+          nprev[nn] = (signed char)prev_hi;
+          nn++;
+          pushed = 2;
+        }
+      }
+      // zd[i] = zd[i-1] + (a*q)^2 * w; a node at position i keeps zd[i] (the reference reads zd[n.pos]).
+      float e = fmul(a, q);
+      float zcur = fadd(zprev, fmul(fmul(e, e), w));
+      if (pushed >= 1) nzd[nn - 1] = zcur;
+      if (pushed == 2) nzd[nn - 2] = zcur;
+      zprev = zcur;
+    }
+#pragma unroll
+    for (int j = 0; j < kChunk; j++) cur[j] = nxt[j];
   }
   // End of block (jpeg/src/rdo.rs:98-108): zprev is zd[63].
   const float eob = st->eob[cls];
@@ -634,12 +648,12 @@ __global__ void __launch_bounds__(128) k_trellis(StepDesc* __restrict__ st, Cach
   reinterpret_cast<int4*>(out)[0] = first;
 #pragma unroll
   for (int g = 1; g < 8; g++) reinterpret_cast<int4*>(out)[g] = z;
-  int cur = best_end;
-  while (cur >= 0) {
-    int p = npos[cur];
-    short v = nv[cur];
+  int node = best_end;
+  while (node >= 0) {
+    int p = npos[node];
+    short v = nv[node];
     out[p] = ((negmask >> p) & 1) ? (int16_t)(-v) : (int16_t)v;
-    cur = nprev[cur];
+    node = nprev[node];
   }
 }
 
@@ -768,90 +782,166 @@ __device__ __forceinline__ int up_sample(const uint8_t* p, int stride, int cw, i
   return px(x / fx, y / fy);
 }
 
-__device__ __forceinline__ void upsample_color_px(const StepDesc* __restrict__ st, const uint8_t* __restrict__ planes,
-                                                  int w, int h, uint8_t* __restrict__ rgb, float* __restrict__ lin,
-                                                  int x, int y);
-
 // Decoder::finish for an 8-bit YCbCr or Gray CoefImage (jpeg/src/decode.rs:1404-1444): upsample every component to
 // full resolution, then the fixed-point YCbCr->RGB of :1438-1441. Writes interleaved pixels and/or the linear-light
 // planes the scorer starts from (core/src/ssimulacra2.rs:192-203: Gray is replicated to three channels).
 __global__ void k_upsample_color(const StepDesc* __restrict__ st, const uint8_t* __restrict__ planes, int w, int h,
                                  uint8_t* __restrict__ rgb, float* __restrict__ lin) {
   if (!st->active) return;
-  int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= w) return;
-  for (int y = blockIdx.y; y < h; y += gridDim.y) upsample_color_px(st, planes, w, h, rgb, lin, x, y);
-}
-
-__device__ __forceinline__ void upsample_color_px(const StepDesc* __restrict__ st, const uint8_t* __restrict__ planes,
-                                                  int w, int h, uint8_t* __restrict__ rgb, float* __restrict__ lin,
-                                                  int x, int y) {
-  size_t plane_px = (size_t)w * h;
-  size_t i = (size_t)y * w + x;
-  const CompDesc& c0 = st->comp[0];
-  int yv = up_sample(planes + c0.plane_off, c0.bw * 8, (w * c0.h + st->hmax - 1) / st->hmax,
-                     (h * c0.v + st->vmax - 1) / st->vmax, st->hmax / c0.h, st->vmax / c0.v, x, y);
-  if (st->ncomp == 1) {
-    if (rgb) rgb[i] = (uint8_t)yv;
-    if (lin) {
-      float l = c_lut8[yv];
-      lin[i] = l;
-      lin[plane_px + i] = l;
-      lin[2 * plane_px + i] = l;
-    }
-    return;
-  }
-  int s[2];
+  // The sRGB table lives in shared memory: per-thread indices differ, which would serialize constant-memory reads.
+  __shared__ float lut[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = c_lut8[i];
+  __syncthreads();
+  // Four consecutive pixels of one row per thread, so each thread moves enough bytes per request.
+  const int x0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (x0 >= w) return;
+  const int ncomp = st->ncomp, hmax = st->hmax, vmax = st->vmax;
+  const CompDesc c0 = st->comp[0];
+  const size_t np = (size_t)w * h;
+  const bool vec_out = (w % 4 == 0) && (np % 4 == 0) && (x0 + 4 <= w);
+  for (int y = blockIdx.y; y < h; y += gridDim.y) {
+    int yv[4], cbv[4], crv[4];
+    // Luma: full resolution when it carries the maximum sampling factors (always, for this encoder's layouts).
+    if (c0.h == hmax && c0.v == vmax) {
+      const uint8_t* yr = planes + c0.plane_off + (size_t)y * (c0.bw * 8);
+      uint32_t q = *reinterpret_cast<const uint32_t*>(yr + x0);  // x0 % 4 == 0, row stride % 8 == 0
 #pragma unroll
-  for (int c = 1; c < 3; c++) {
-    const CompDesc& cd = st->comp[c];
-    s[c - 1] = up_sample(planes + cd.plane_off, cd.bw * 8, (w * cd.h + st->hmax - 1) / st->hmax,
-                         (h * cd.v + st->vmax - 1) / st->vmax, st->hmax / cd.h, st->vmax / cd.v, x, y);
-  }
-  int cb = s[0] - 128, cr = s[1] - 128;
-  int r = clampi(yv + ((91881 * cr + 32768) >> 16), 0, 255);
-  int g = clampi(yv - ((22554 * cb + 46802 * cr + 32768) >> 16), 0, 255);
-  int b = clampi(yv + ((116130 * cb + 32768) >> 16), 0, 255);
-  if (rgb) {
-    rgb[i * 3] = (uint8_t)r;
-    rgb[i * 3 + 1] = (uint8_t)g;
-    rgb[i * 3 + 2] = (uint8_t)b;
-  }
-  if (lin) {
-    lin[i] = c_lut8[r];
-    lin[plane_px + i] = c_lut8[g];
-    lin[2 * plane_px + i] = c_lut8[b];
+      for (int k = 0; k < 4; k++) yv[k] = (q >> (8 * k)) & 0xFF;
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        int x = min(x0 + k, w - 1);
+        yv[k] = up_sample(planes + c0.plane_off, c0.bw * 8, (w * c0.h + hmax - 1) / hmax,
+                          (h * c0.v + vmax - 1) / vmax, hmax / c0.h, vmax / c0.v, x, y);
+      }
+    }
+    if (ncomp == 3) {
+#pragma unroll
+      for (int c = 1; c < 3; c++) {
+        const CompDesc cd = st->comp[c];
+        const uint8_t* p = planes + cd.plane_off;
+        const int stride = cd.bw * 8;
+        const int cw = (w * cd.h + hmax - 1) / hmax, ch = (h * cd.v + vmax - 1) / vmax;
+        const int fx = hmax / cd.h, fy = vmax / cd.v;
+        int* out = c == 1 ? cbv : crv;
+        if (fx == 2 && fy == 2) {
+          // Triangle filter of jpeg/src/decode.rs:1806-1818 for x0..x0+3 (x0 even): chroma columns i-1..i+2.
+          const int j = y / 2;
+          const int far_y = (y % 2 == 0) ? max(j - 1, 0) : min(j + 1, ch - 1);
+          const uint8_t* rn = p + (size_t)j * stride;
+          const uint8_t* rf = p + (size_t)far_y * stride;
+          const int i = x0 / 2;
+          int vert[4];
+#pragma unroll
+          for (int d = 0; d < 4; d++) {
+            int col = min(max(i - 1 + d, 0), cw - 1);
+            vert[d] = 3 * rn[col] + rf[col];
+          }
+          out[0] = (3 * vert[1] + vert[0] + 8) >> 4;  // x0 even: far = i-1
+          out[1] = (3 * vert[1] + vert[2] + 7) >> 4;  // x0+1 odd: far = i+1
+          out[2] = (3 * vert[2] + vert[1] + 8) >> 4;  // x0+2 even: near i+1, far i
+          out[3] = (3 * vert[2] + vert[3] + 7) >> 4;  // x0+3 odd: near i+1, far i+2
+          // Clamping every column to [0, cw-1] is the reference's rule (saturating i-1, min(i+1, cw-1)); a near
+          // column never needs it for a pixel inside the image (x < w implies x/2 < cw).
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; k++) out[k] = up_sample(p, stride, cw, ch, fx, fy, min(x0 + k, w - 1), y);
+        }
+      }
+    }
+    float l[3][4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (ncomp == 1) {
+        l[0][k] = l[1][k] = l[2][k] = lut[yv[k]];
+        if (rgb && x0 + k < w) rgb[(size_t)y * w + x0 + k] = (uint8_t)yv[k];
+      } else {
+        int cb = cbv[k] - 128, cr = crv[k] - 128;
+        int r = clampi(yv[k] + ((91881 * cr + 32768) >> 16), 0, 255);
+        int g = clampi(yv[k] - ((22554 * cb + 46802 * cr + 32768) >> 16), 0, 255);
+        int b = clampi(yv[k] + ((116130 * cb + 32768) >> 16), 0, 255);
+        l[0][k] = lut[r];
+        l[1][k] = lut[g];
+        l[2][k] = lut[b];
+        if (rgb && x0 + k < w) {
+          size_t i = ((size_t)y * w + x0 + k) * 3;
+          rgb[i] = (uint8_t)r;
+          rgb[i + 1] = (uint8_t)g;
+          rgb[i + 2] = (uint8_t)b;
+        }
+      }
+    }
+    if (lin) {
+      size_t i = (size_t)y * w + x0;
+      if (vec_out) {
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+          *reinterpret_cast<float4*>(lin + c * np + i) = make_float4(l[c][0], l[c][1], l[c][2], l[c][3]);
+      } else {
+        for (int k = 0; k < 4 && x0 + k < w; k++)
+#pragma unroll
+          for (int c = 0; c < 3; c++) lin[c * np + i + k] = l[c][k];
+      }
+    }
   }
 }
 
 int upsample_color(rcg_ctx* ctx, StepDesc* d_step, const uint8_t* d_planes, int w, int h, uint8_t* d_rgb,
                    float* d_lin) {
-  dim3 grid((w + 255) / 256, std::min(h, 65535));
-  RCG_LAUNCH(ctx, "upsample_color", k_upsample_color, grid, 256, 0, d_step, d_planes, w, h, d_rgb, d_lin);
+  dim3 grid(((w + 3) / 4 + 127) / 128, std::min(h, 65535));
+  RCG_LAUNCH(ctx, "upsample_color", k_upsample_color, grid, 128, 0, d_step, d_planes, w, h, d_rgb, d_lin);
   return RCG_OK;
 }
 
 // ------------------------------------------------------------------------------------------------ step tables
 
-// First kernel of every search step: the bisection state names the quality; fill the candidate's tables.
-__global__ void k_step_tables(const SearchState* __restrict__ ss, StepDesc* __restrict__ st, int w, int h,
-                              int16_t* slots, long long slot_stride) {
-  if (threadIdx.x != 0) return;
+// First kernel of every search step: the bisection state names the quality; fill the candidate's tables. 128
+// threads: one per (class, coefficient) entry; the Rdo median is the element of rank 31 among q[1..63] (ties broken
+// by index, which leaves the value unchanged), the same value the reference's sort yields.
+__global__ void __launch_bounds__(128) k_step_tables(const SearchState* __restrict__ ss, StepDesc* __restrict__ st,
+                                                     int w, int h, int16_t* slots, long long slot_stride) {
+  __shared__ uint8_t qt[64];
+  __shared__ float rq[64];
+  __shared__ float median;
+  const int t = threadIdx.x;
   if (ss->done) {
-    st->active = 0;
+    if (t == 0) st->active = 0;
     return;
   }
-  int step = ss->step;
-  int q = ss->qs[step];
-  st->active = 1;
-  fill_step(st, q, ss->subsampling, ss->channels, ss->trellis, w, h);
-  for (int i = 0; i < 512; i++) (&st->hist[0][0])[i] = 0;
-  st->coefs = slots + (long long)step * slot_stride;
+  const int step = ss->step;
+  const int q = ss->qs[step];
+  if (t == 0) {
+    st->active = 1;
+    fill_layout(st, q, ss->subsampling, ss->channels, ss->trellis, w, h);
+    st->coefs = slots + (long long)step * slot_stride;
+  }
+  if (t < 64) {
+    qt[t] = qtable_entry(q, t);
+  }
+  __syncthreads();
+  // luma_table == chroma_table (jpeg/src/quality.rs:37-43): both classes get the same entries
+  const int cls = t / 64, k = t % 64;
+  st->qt[cls][k] = qt[k];
+  st->divz[cls][k] = divz_entry(qt, k);
+  st->mult[cls][k] = mult_entry(qt, k);
+  float rk = (float)qt[zigzag(k)];
+  st->rq[cls][k] = rk;
+  if (cls == 0) rq[k] = rk;
+  for (int i = t; i < 512; i += blockDim.x) (&st->hist[0][0])[i] = 0;
+  __syncthreads();
+  if (cls == 0 && k >= 1) {
+    int rank = 0;
+    for (int j = 1; j < 64; j++) rank += (rq[j] < rk || (rq[j] == rk && j < k)) ? 1 : 0;
+    if (rank == 31) median = rk;
+  }
+  __syncthreads();
+  st->rw[cls][k] = k == 0 ? 1.0f : fdiv(median, rk);
+  if (k == 0) st->lambda[cls] = fmul(fmul(0.02f, median), median);  // TRELLIS_KAPPA (jpeg/src/encode.rs:42)
 }
 
 int step_tables(rcg_ctx* ctx, SearchState* d_search, StepDesc* d_step, int w, int h, int16_t* d_coef_slots,
                 long long slot_stride) {
-  RCG_LAUNCH(ctx, "step_tables", k_step_tables, 1, 32, 0, d_search, d_step, w, h, d_coef_slots, slot_stride);
+  RCG_LAUNCH(ctx, "step_tables", k_step_tables, 1, 128, 0, d_search, d_step, w, h, d_coef_slots, slot_stride);
   return RCG_OK;
 }
 

@@ -110,8 +110,11 @@ __device__ __forceinline__ int mirror_row(int yy, int h) {
   return yy;
 }
 
-constexpr int kIW = kTileW + 2 * kRadius;  // 42
+// Row pitch 45 (>= 42): 8 horizontal-pass items per row read at a stride of 4 words, and 45 = 13 mod 32 puts the
+// four rows a warp covers in distinct bank classes, so those reads are conflict-free.
+constexpr int kIW = 45;
 constexpr int kIH = kTileH + 2 * kRadius;  // 42
+constexpr int kHx = 4;                     // horizontal-pass outputs per item
 constexpr size_t kTileSmem = (size_t)(6 * kIH * kIW + 5 * kIH * kTileW) * sizeof(float);
 
 // One CTA = one 32x32 output tile of one scale. Shared memory: XYB (offset) of both images for the tile plus its
@@ -157,20 +160,41 @@ __global__ void __launch_bounds__(kTileThreads, 3)
   __syncthreads();
   float oa[3] = {s_oa[0], s_oa[1], s_oa[2]}, od[3] = {s_od[0], s_od[1], s_od[2]};
 
-  for (int idx = tid; idx < kIH * kIW; idx += kTileThreads) {
-    int r = idx / kIW, c = idx - r * kIW;
+  // XYB of the tile and its halo; the six plane values of the next pixel are loaded before the current one is
+  // converted, so the global loads overlap the arithmetic.
+  constexpr int kCols = kTileW + 2 * kRadius;  // 42 real columns of the kIW-pitched rows
+  auto load6 = [&](int e, float* v) -> bool {
+    int r = e / kCols, c = e - r * kCols;
     int gy = mirror_row(y0 - kRadius + r, h);
     int gx = x0 - kRadius + c;
-    float v[6] = {0, 0, 0, 0, 0, 0};
-    if (gy >= 0 && gx >= 0 && gx < w) {
+    if (e < kIH * kCols && gy >= 0 && gx >= 0 && gx < w) {
       size_t i = (size_t)gy * w + gx;
-      Pix p = pix(__ldg(ra + i), __ldg(ra + np + i), __ldg(ra + 2 * np + i), __ldg(rb + i), __ldg(rb + np + i),
-                  __ldg(rb + 2 * np + i), oa, od, cb_bias);
+      v[0] = __ldg(ra + i);
+      v[1] = __ldg(ra + np + i);
+      v[2] = __ldg(ra + 2 * np + i);
+      v[3] = __ldg(rb + i);
+      v[4] = __ldg(rb + np + i);
+      v[5] = __ldg(rb + 2 * np + i);
+      return true;
+    }
+    return false;
+  };
+  float cur[6], nxt[6];
+  bool cur_ok = load6(tid, cur);
+  for (int e = tid; e < kIH * kCols; e += kTileThreads) {
+    bool nxt_ok = load6(e + kTileThreads, nxt);
+    float v[6] = {0, 0, 0, 0, 0, 0};
+    if (cur_ok) {
+      Pix p = pix(cur[0], cur[1], cur[2], cur[3], cur[4], cur[5], oa, od, cb_bias);
       v[0] = p.a[0]; v[1] = p.a[1]; v[2] = p.a[2];
       v[3] = p.d[0]; v[4] = p.d[1]; v[5] = p.d[2];
     }
+    const int r = e / kCols, idx = r * kIW + (e - r * kCols);
 #pragma unroll
     for (int k = 0; k < 6; k++) xs[k * kIH * kIW + idx] = v[k];
+#pragma unroll
+    for (int k = 0; k < 6; k++) cur[k] = nxt[k];
+    cur_ok = nxt_ok;
   }
 
   float sums[kScoreSums];
@@ -196,37 +220,41 @@ __global__ void __launch_bounds__(kTileThreads, 3)
     __syncthreads();  // xs complete (ch 0) / previous channel's vertical pass done with hb
     const float* A = xs + ch * kIH * kIW;
     const float* D = xs + (3 + ch) * kIH * kIW;
-    // Horizontal pass: 2 adjacent outputs per item; moments a', d', a'^2, b'^2 (b' = a' - d'), d'^2.
-    for (int item = tid; item < kIH * (kTileW / 2); item += kTileThreads) {
-      int r = item / (kTileW / 2), p = item - r * (kTileW / 2);
-      const float* ar = A + r * kIW + 2 * p;
-      const float* dr = D + r * kIW + 2 * p;
-      float va[12], vd[12];
+    // Horizontal pass: kHx adjacent outputs per item; moments a', d', a'^2, b'^2 (b' = a' - d'), d'^2.
+    for (int item = tid; item < kIH * (kTileW / kHx); item += kTileThreads) {
+      int r = item / (kTileW / kHx), p = item - r * (kTileW / kHx);
+      const float* ar = A + r * kIW + kHx * p;
+      const float* dr = D + r * kIW + kHx * p;
+      float va[kHx + 2 * kRadius], vd[kHx + 2 * kRadius], vaa[kHx + 2 * kRadius], vbb[kHx + 2 * kRadius],
+          vdd[kHx + 2 * kRadius];
 #pragma unroll
-      for (int t = 0; t < 12; t++) {
-        va[t] = ar[t];
-        vd[t] = dr[t];
+      for (int t = 0; t < kHx + 2 * kRadius; t++) {
+        float a = ar[t], d = dr[t], b = a - d;
+        va[t] = a;
+        vd[t] = d;
+        vaa[t] = a * a;
+        vbb[t] = b * b;
+        vdd[t] = d * d;
       }
-      float m[5][2];
+      float m[5][kHx];
 #pragma unroll
-      for (int o = 0; o < 2; o++) {
+      for (int o = 0; o < kHx; o++) {
         float s1 = 0.f, sd = 0.f, s11 = 0.f, s22 = 0.f, sdd = 0.f;
 #pragma unroll
         for (int t = 0; t < 2 * kRadius + 1; t++) {
-          float k = c_gauss[t], a = va[o + t], d = vd[o + t], b = a - d;
-          s1 = fmaf(k, a, s1);
-          sd = fmaf(k, d, sd);
-          s11 = fmaf(k, a * a, s11);
-          s22 = fmaf(k, b * b, s22);
-          sdd = fmaf(k, d * d, sdd);
+          float k = c_gauss[t];
+          s1 = fmaf(k, va[o + t], s1);
+          sd = fmaf(k, vd[o + t], sd);
+          s11 = fmaf(k, vaa[o + t], s11);
+          s22 = fmaf(k, vbb[o + t], s22);
+          sdd = fmaf(k, vdd[o + t], sdd);
         }
         m[0][o] = s1; m[1][o] = sd; m[2][o] = s11; m[3][o] = s22; m[4][o] = sdd;
       }
 #pragma unroll
-      for (int q = 0; q < 5; q++) {
-        float2 v2 = make_float2(m[q][0], m[q][1]);
-        *reinterpret_cast<float2*>(hb + (q * kIH + r) * kTileW + 2 * p) = v2;
-      }
+      for (int q = 0; q < 5; q++)
+        *reinterpret_cast<float4*>(hb + (q * kIH + r) * kTileW + kHx * p) = make_float4(m[q][0], m[q][1], m[q][2],
+                                                                                        m[q][3]);
     }
     __syncthreads();
     // Vertical pass + error maps: 4 output rows of one column per thread.
@@ -268,7 +296,7 @@ __global__ void __launch_bounds__(kTileThreads, 3)
         // 1 - (1 - dmu^2) num_s / denom_s since num_s = denom_s - sigma_(a-b)^2.
         float den = (v1 + v2) + 0.0009f;
         float num_s = den - vd;
-        float d = fmaxf(__fdiv_rn(fmaf(dmu * dmu, num_s, vd), den), 0.0f);
+        float d = fmaxf(__fdividef(fmaf(dmu * dmu, num_s, vd), den), 0.0f);
         // Edge maps (:431-433): d1 = (|r2| - |r1|) / (1 + |r1|) with r1 = a - mu1, r2 = b - mu2 = r1 - rd.
         float a0 = A[(ry + kRadius) * kIW + col + kRadius];
         float d0 = D[(ry + kRadius) * kIW + col + kRadius];
@@ -278,7 +306,7 @@ __global__ void __launch_bounds__(kTileThreads, 3)
           rd = fmaf(cd, omk, rd);
         }
         float t = fabsf(r1 - rd) + fabsf(r1);
-        float d1 = t > 0.0f ? __fdiv_rn(__fdiv_rn(-rd * (2.0f * r1 - rd), t), 1.0f + fabsf(r1)) : 0.0f;
+        float d1 = t > 0.0f ? __fdividef(-rd * (2.0f * r1 - rd), t * (1.0f + fabsf(r1))) : 0.0f;
         float art = fmaxf(d1, 0.0f), det = fmaxf(-d1, 0.0f);
         float d2 = d * d, a2 = art * art, e2 = det * det;
         sums[ch * 6 + 0] += d;
@@ -338,28 +366,25 @@ __global__ void __launch_bounds__(256) k_ssim2_reduce(PyramidDesc pd, const doub
     last = prev == gridDim.x * gridDim.y - 1;
   }
   __syncthreads();
-  if (!last || threadIdx.x != 0) return;
+  if (!last) return;
   __threadfence();
-  *counter = 0;
+  // The last CTA maps the per-scale sums to the score. Term t follows the reference's weight order: channel, scale,
+  // norm (mean, 4-norm), then (ssim, artifact, detail) (core/src/ssimulacra2.rs:491-506); one thread per term.
+  __shared__ double terms[3 * kMaxScales * 6];
   const volatile double* vs = scale_sums;
-  double stats[kMaxScales][3][6];
-  for (int sc = 0; sc < pd.nscales; sc++) {
+  const int ns = pd.nscales, nterms = 3 * ns * 6, t = threadIdx.x;
+  if (t < nterms) {
+    int c = t / (ns * 6), rem = t % (ns * 6), sc = rem / 6, r2 = rem % 6, nrm = r2 / 3, k = r2 % 3;
     double count = (double)pd.s[sc].w * (double)pd.s[sc].h;
-    for (int c = 0; c < 3; c++)
-      for (int m = 0; m < 3; m++) {
-        stats[sc][c][2 * m] = vs[sc * kScoreSums + c * 6 + 2 * m] / count;
-        stats[sc][c][2 * m + 1] = pow(vs[sc * kScoreSums + c * 6 + 2 * m + 1] / count, 0.25);
-      }
+    double v = vs[sc * kScoreSums + c * 6 + 2 * k + nrm] / count;
+    if (nrm == 1) v = sqrt(sqrt(v));  // (sum of 4th powers / count)^0.25 (:462)
+    terms[t] = c_weights[t] * fabs(v);
   }
+  __syncthreads();
+  if (t != 0) return;
+  *counter = 0;
   double ssim = 0.0;
-  int wi = 0;
-  for (int c = 0; c < 3; c++)
-    for (int sc = 0; sc < pd.nscales; sc++)
-      for (int nrm = 0; nrm < 2; nrm++) {
-        ssim += c_weights[wi++] * fabs(stats[sc][c][nrm]);
-        ssim += c_weights[wi++] * fabs(stats[sc][c][2 + nrm]);
-        ssim += c_weights[wi++] * fabs(stats[sc][c][4 + nrm]);
-      }
+  for (int i = 0; i < nterms; i++) ssim += terms[i];
   ssim *= 0.9562382616834844;
   ssim = 2.326765642916932 * ssim - 0.020884521182843837 * ssim * ssim + 6.248496625763138e-05 * ssim * ssim * ssim;
   double score = ssim > 0.0 ? 100.0 - 10.0 * pow(ssim, 0.6276336467831387) : 100.0;
@@ -398,60 +423,84 @@ __global__ void __launch_bounds__(256) k_ssim2_reduce(PyramidDesc pd, const doub
 // ------------------------------------------------------------------------------------------------ planes, pyramid
 
 // Linear planes of an interleaved image (core/src/ssimulacra2.rs:177-221, with core/src/image.rs:143-190 for alpha:
-// 16-bit samples rounded to 8 bits, then composited onto mid-grey 128).
+// 16-bit samples rounded to 8 bits, then composited onto mid-grey 128). Four consecutive pixels per thread (in
+// row-major order; the planes are contiguous [3][h][w]) so each thread moves enough bytes per request.
 __global__ void k_to_linear(const uint8_t* __restrict__ img, int w, int h, int channels, int depth,
                             const float* __restrict__ lut16, float* __restrict__ out) {
-  int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= w) return;
-  for (int y = blockIdx.y; y < h; y += gridDim.y) {
-  size_t i = (size_t)y * w + x;
-  size_t np = (size_t)w * h;
-  float v[3];
-  bool alpha = channels == 2 || channels == 4;
-  if (depth == 8 && !alpha) {
-    if (channels == 1) {
-      v[0] = v[1] = v[2] = c_lut8s[img[i]];
-    } else {
-      v[0] = c_lut8s[img[i * 3]];
-      v[1] = c_lut8s[img[i * 3 + 1]];
-      v[2] = c_lut8s[img[i * 3 + 2]];
-    }
-  } else if (!alpha) {
-    auto s16 = [&](int k) -> unsigned {
-      const uint8_t* p = img + (i * channels + k) * 2;
-      return ((unsigned)p[0] << 8) | p[1];
-    };
-    if (channels == 1) {
-      v[0] = v[1] = v[2] = lut16[s16(0)];
-    } else {
-      v[0] = lut16[s16(0)];
-      v[1] = lut16[s16(1)];
-      v[2] = lut16[s16(2)];
-    }
+  // The table lives in shared memory: per-thread indices differ, which would serialize constant-memory reads.
+  __shared__ float lut8[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) lut8[i] = c_lut8s[i];
+  __syncthreads();
+  const size_t np = (size_t)w * h;
+  const size_t i0 = 4 * ((size_t)blockIdx.x * blockDim.x + threadIdx.x);
+  if (i0 >= np) return;
+  const int n = (int)min((size_t)4, np - i0);
+  float v[3][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+  const bool alpha = channels == 2 || channels == 4;
+  if (depth == 8 && channels == 3 && n == 4 && ((uintptr_t)img & 3) == 0) {
+    // 12 bytes at 12 * (i0/4): 4-byte aligned when the image is (callers may pass any device pointer)
+    const uint32_t* p = reinterpret_cast<const uint32_t*>(img + i0 * 3);
+    uint32_t q0 = p[0], q1 = p[1], q2 = p[2];
+    uint32_t b[12] = {q0 & 0xFF, (q0 >> 8) & 0xFF, (q0 >> 16) & 0xFF, q0 >> 24, q1 & 0xFF, (q1 >> 8) & 0xFF,
+                      (q1 >> 16) & 0xFF, q1 >> 24, q2 & 0xFF, (q2 >> 8) & 0xFF, (q2 >> 16) & 0xFF, q2 >> 24};
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) v[c][k] = lut8[b[3 * k + c]];
   } else {
-    unsigned s[4];
-    for (int k = 0; k < channels; k++) {
-      if (depth == 8) {
-        s[k] = img[i * channels + k];
+    for (int k = 0; k < n; k++) {
+      size_t i = i0 + k;
+      if (depth == 8 && !alpha) {
+        if (channels == 1) {
+          v[0][k] = v[1][k] = v[2][k] = lut8[img[i]];
+        } else {
+          v[0][k] = lut8[img[i * 3]];
+          v[1][k] = lut8[img[i * 3 + 1]];
+          v[2][k] = lut8[img[i * 3 + 2]];
+        }
+      } else if (!alpha) {
+        auto s16 = [&](int c) -> unsigned {
+          const uint8_t* p = img + (i * channels + c) * 2;
+          return ((unsigned)p[0] << 8) | p[1];
+        };
+        if (channels == 1) {
+          v[0][k] = v[1][k] = v[2][k] = lut16[s16(0)];
+        } else {
+          v[0][k] = lut16[s16(0)];
+          v[1][k] = lut16[s16(1)];
+          v[2][k] = lut16[s16(2)];
+        }
       } else {
-        const uint8_t* p = img + (i * channels + k) * 2;
-        unsigned u = ((unsigned)p[0] << 8) | p[1];
-        s[k] = (u * 255 + 32767) / 65535;
+        unsigned sm[4];
+        for (int c = 0; c < channels; c++) {
+          if (depth == 8) {
+            sm[c] = img[i * channels + c];
+          } else {
+            const uint8_t* p = img + (i * channels + c) * 2;
+            unsigned u = ((unsigned)p[0] << 8) | p[1];
+            sm[c] = (u * 255 + 32767) / 65535;
+          }
+        }
+        unsigned a = sm[channels - 1];
+        auto blend = [&](unsigned c) -> unsigned { return (c * a + 128u * (255 - a) + 127) / 255; };
+        if (channels == 2) {
+          v[0][k] = v[1][k] = v[2][k] = lut8[blend(sm[0])];
+        } else {
+          v[0][k] = lut8[blend(sm[0])];
+          v[1][k] = lut8[blend(sm[1])];
+          v[2][k] = lut8[blend(sm[2])];
+        }
       }
     }
-    unsigned a = s[channels - 1];
-    auto blend = [&](unsigned c) -> unsigned { return (c * a + 128u * (255 - a) + 127) / 255; };
-    if (channels == 2) {
-      v[0] = v[1] = v[2] = c_lut8s[blend(s[0])];
-    } else {
-      v[0] = c_lut8s[blend(s[0])];
-      v[1] = c_lut8s[blend(s[1])];
-      v[2] = c_lut8s[blend(s[2])];
-    }
   }
-  out[i] = v[0];
-  out[np + i] = v[1];
-  out[2 * np + i] = v[2];
+  if (n == 4 && np % 4 == 0 && ((uintptr_t)out & 15) == 0) {
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+      *reinterpret_cast<float4*>(out + c * np + i0) = make_float4(v[c][0], v[c][1], v[c][2], v[c][3]);
+  } else {
+    for (int k = 0; k < n; k++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) out[c * np + i0 + k] = v[c][k];
   }
 }
 
@@ -463,32 +512,103 @@ __device__ __forceinline__ float two_sum(float a, float b, float& e) {
   return s;
 }
 
-// downsample (core/src/ssimulacra2.rs:223-247): mean of the 2x2 block (fewer at odd edges). The reference sums in
-// f64, which is exact for these inputs, then rounds once to f32; the compensated sum here (TwoSum) rounds the same
-// exact sum once, so the planes agree with the reference's except in rare double-rounding cases.
-__global__ void k_downsample(const float* __restrict__ src, int w, int h, float* __restrict__ dst,
-                             const StepDesc* __restrict__ st) {
-  if (st && !st->active) return;
-  int ow = (w + 1) / 2, oh = (h + 1) / 2;
-  int ox = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ox >= ow) return;
-  for (int oy = blockIdx.y; oy < oh; oy += gridDim.y) {
+// Mean of the 2x2 block at output (ox, oy) of a plane of w x h (fewer samples at odd edges), as downsample
+// (core/src/ssimulacra2.rs:223-247) computes it: the reference sums in f64, which is exact for these inputs, then
+// rounds once to f32; the compensated sum here (TwoSum) rounds the same exact sum once, so the planes agree with the
+// reference's except in rare double-rounding cases.
+__device__ __forceinline__ float mean2x2(const float* p, int stride, int w, int h, int ox, int oy) {
   int x0 = ox * 2, x1 = min(ox * 2 + 2, w), y0 = oy * 2, y1 = min(oy * 2 + 2, h);
-  float inv = 1.0f / (float)((y1 - y0) * (x1 - x0));
-  size_t np = (size_t)w * h, onp = (size_t)ow * oh;
+  float s = 0.0f, err = 0.0f;
+  for (int y = y0; y < y1; y++)
+    for (int x = x0; x < x1; x++) {
+      float e;
+      s = two_sum(s, p[(size_t)y * stride + x], e);
+      err += e;
+    }
+  // count is 1, 2 or 4: the scaling is exact.
+  return __fadd_rn(s, err) * (1.0f / (float)((y1 - y0) * (x1 - x0)));
+}
+
+// Every coarser scale of a pyramid from scale 0 in one launch. One CTA owns a 32x32 tile of scale 1 (a 64x64 block
+// of scale 0) and the 16x16, 8x8, 4x4, 2x2 tiles of scales 2-5 below it, kept in shared memory between levels: tiles
+// nest exactly because each level halves the previous one, and odd edges occur only in the last tile of a row or
+// column, where mean2x2 clips to the level's size.
+constexpr int kPyrTile = 32;
+__global__ void __launch_bounds__(256) k_pyramid(PyramidDesc pd, float* __restrict__ pyr,
+                                                 const StepDesc* __restrict__ st) {
+  if (st && !st->active) return;
+  __shared__ float buf[2][3][kPyrTile][kPyrTile + 1];
+  const ScaleDesc s0 = pd.s[0], s1 = pd.s[1];
+  const int tiles_x = (s1.w + kPyrTile - 1) / kPyrTile;
+  const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  const size_t np0 = (size_t)s0.w * s0.h, np1 = (size_t)s1.w * s1.h;
+  // scale 1 from global scale 0. Full 2x2 blocks (all but the last odd column/row) load their four samples at once
+  // and sum them in mean2x2's order; partial blocks take the general path.
+  for (int i = threadIdx.x; i < kPyrTile * kPyrTile; i += blockDim.x) {
+    int lx = i % kPyrTile, ly = i / kPyrTile;
+    int ox = tx * kPyrTile + lx, oy = ty * kPyrTile + ly;
+    if (ox < s1.w && oy < s1.h) {
+      const bool full = 2 * ox + 1 < s0.w && 2 * oy + 1 < s0.h;
+      float v[3];
+      if (full) {
+        float q[3][4];
 #pragma unroll
-  for (int c = 0; c < 3; c++) {
-    const float* p = src + c * np;
-    float s = 0.0f, err = 0.0f;
-    for (int y = y0; y < y1; y++)
-      for (int x = x0; x < x1; x++) {
-        float e;
-        s = two_sum(s, p[(size_t)y * w + x], e);
-        err += e;
+        for (int c = 0; c < 3; c++) {
+          const float* p = pyr + s0.off + c * np0 + (size_t)(2 * oy) * s0.w + 2 * ox;
+          q[c][0] = p[0];
+          q[c][1] = p[1];
+          q[c][2] = p[s0.w];
+          q[c][3] = p[s0.w + 1];
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          float e0, e1, e2;
+          float t = two_sum(q[c][0], q[c][1], e0);  // 0 + q0 is exact, so this matches mean2x2's first steps
+          t = two_sum(t, q[c][2], e1);
+          t = two_sum(t, q[c][3], e2);
+          v[c] = __fadd_rn(t, (e0 + e1) + e2) * 0.25f;
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 3; c++) v[c] = mean2x2(pyr + s0.off + c * np0, s0.w, s0.w, s0.h, ox, oy);
       }
-    // count is 1, 2 or 4: the scaling is exact.
-    dst[c * onp + (size_t)oy * ow + ox] = __fadd_rn(s, err) * inv;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        buf[0][c][ly][lx] = v[c];
+        pyr[s1.off + c * np1 + (size_t)oy * s1.w + ox] = v[c];
+      }
+    }
   }
+  int cur = 0, tile = kPyrTile;
+  for (int L = 2; L < pd.nscales; L++) {
+    __syncthreads();
+    const ScaleDesc a = pd.s[L - 1], b = pd.s[L];
+    const size_t npb = (size_t)b.w * b.h;
+    const int half = tile / 2;
+    const int ax0 = tx * tile, ay0 = ty * tile;  // tile origin at level L-1
+    for (int i = threadIdx.x; i < half * half; i += blockDim.x) {
+      int lx = i % half, ly = i / half;
+      int ox = tx * half + lx, oy = ty * half + ly;
+      if (ox < b.w && oy < b.h) {
+        // the 2x2 source block lies in this CTA's level L-1 tile; clip to level L-1's size like mean2x2
+        int x1 = min(ox * 2 + 2, a.w) - ax0, y1 = min(oy * 2 + 2, a.h) - ay0;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          float sum = 0.0f, err = 0.0f;
+          for (int y = 2 * ly; y < y1; y++)
+            for (int x = 2 * lx; x < x1; x++) {
+              float e;
+              sum = two_sum(sum, buf[cur][c][y][x], e);
+              err += e;
+            }
+          float v = __fadd_rn(sum, err) * (1.0f / (float)((y1 - 2 * ly) * (x1 - 2 * lx)));
+          buf[cur ^ 1][c][ly][lx] = v;
+          pyr[b.off + c * npb + (size_t)oy * b.w + ox] = v;
+        }
+      }
+    }
+    cur ^= 1;
+    tile = half;
   }
 }
 
@@ -498,18 +618,16 @@ int to_linear(rcg_ctx* ctx, const uint8_t* d_img, int w, int h, int channels, in
     lut16 = srgb_lut16_device(ctx);
     if (!lut16) return RCG_NO_MEMORY;
   }
-  dim3 grid((w + 255) / 256, std::min(h, 65535));
-  RCG_LAUNCH(ctx, "to_linear", k_to_linear, grid, 256, 0, d_img, w, h, channels, depth, lut16, d_pyr);
+  const long long groups = ((long long)w * h + 3) / 4;
+  RCG_LAUNCH(ctx, "to_linear", k_to_linear, (unsigned)((groups + 255) / 256), 256, 0, d_img, w, h, channels, depth,
+             lut16, d_pyr);
   return RCG_OK;
 }
 
 int build_pyramid_gated(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, const StepDesc* st) {
-  for (int s = 1; s < pd.nscales; s++) {
-    const ScaleDesc& a = pd.s[s - 1];
-    const ScaleDesc& b = pd.s[s];
-    dim3 grid((b.w + 127) / 128, std::min(b.h, 65535));
-    RCG_LAUNCH(ctx, "downsample", k_downsample, grid, 128, 0, d_pyr + a.off, a.w, a.h, d_pyr + b.off, st);
-  }
+  if (pd.nscales < 2) return RCG_OK;
+  const int grid = ((pd.s[1].w + kPyrTile - 1) / kPyrTile) * ((pd.s[1].h + kPyrTile - 1) / kPyrTile);
+  RCG_LAUNCH(ctx, "pyramid", k_pyramid, grid, 256, 0, pd, d_pyr, st);
   return RCG_OK;
 }
 
@@ -688,15 +806,13 @@ extern "C" int rcg_ssimulacra2_device_noalloc(const uint8_t* d_reference, const 
     cudaGetLastError();
     return RCG_CUDA_ERROR;
   }
-  dim3 lg((w + 255) / 256, std::min(h, 65535));
+  const unsigned lg = (unsigned)((((long long)w * h + 3) / 4 + 255) / 256);
   k_to_linear<<<lg, 256, 0, s>>>(d_reference, w, h, channels, 8, nullptr, pyr_ref);
   k_to_linear<<<lg, 256, 0, s>>>(d_distorted, w, h, channels, 8, nullptr, pyr_dist);
-  for (int sc = 1; sc < pd.nscales; sc++) {
-    const ScaleDesc& a = pd.s[sc - 1];
-    const ScaleDesc& b = pd.s[sc];
-    dim3 dg((b.w + 127) / 128, std::min(b.h, 65535));
-    k_downsample<<<dg, 128, 0, s>>>(pyr_ref + a.off, a.w, a.h, pyr_ref + b.off, nullptr);
-    k_downsample<<<dg, 128, 0, s>>>(pyr_dist + a.off, a.w, a.h, pyr_dist + b.off, nullptr);
+  if (pd.nscales > 1) {
+    const int pg = ((pd.s[1].w + kPyrTile - 1) / kPyrTile) * ((pd.s[1].h + kPyrTile - 1) / kPyrTile);
+    k_pyramid<<<pg, 256, 0, s>>>(pd, pyr_ref, nullptr);
+    k_pyramid<<<pg, 256, 0, s>>>(pd, pyr_dist, nullptr);
   }
   k_ssim2_tiles<<<pd.total_tiles, kTileThreads, kTileSmem, s>>>(pd, pyr_ref, pyr_dist, partials, nullptr);
   k_ssim2_reduce<<<dim3(pd.nscales, kScoreSums), 256, 0, s>>>(pd, partials, sums, counter, d_score, nullptr,

@@ -103,3 +103,25 @@ def test_large_pair_vs_oracle_and_fp64(ctx, oracle):
     print(f"gpu {got:.9f} oracle {want:.9f} fp64 {want64:.9f}")
     assert abs(got - want) <= TOL_ORACLE
     assert abs(got - want64) <= TOL_ORACLE
+
+
+def test_device_entry_point_with_unaligned_pointers(ctx, oracle):
+    """rcg_ssimulacra2_device takes any device pointer: odd offsets must give the same score (scalar path)."""
+    import torch
+
+    import rcg.synth as synth
+
+    w, h = 131, 67
+    ref = synth.image(w, h, 31)
+    dist = synth.image(w, h, 31, sensor_sigma=4.0)
+    dev = torch.device("cuda", 0)
+    n = ref.size
+    buf_a = torch.zeros(n + 3, dtype=torch.uint8, device=dev)
+    buf_b = torch.zeros(n + 3, dtype=torch.uint8, device=dev)
+    want = oracle.ssimulacra2(ref, dist)
+    for off in (0, 1, 3):
+        buf_a[off: off + n] = torch.from_numpy(ref.ravel()).to(dev)
+        buf_b[off: off + n] = torch.from_numpy(dist.ravel()).to(dev)
+        torch.cuda.synchronize()
+        got = ctx.ssimulacra2_device(buf_a.data_ptr() + off, buf_b.data_ptr() + off, w, h, 3)
+        assert abs(got - want) <= TOL_ORACLE, (off, got, want)
