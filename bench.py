@@ -49,8 +49,9 @@ def _set_size(w, h):
 
 
 def _env_rank():
-    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK",
-                                                                                                        "0"))
+    from rcg import replicas
+
+    return replicas.env_rank()
 
 
 def _peaks():
@@ -148,6 +149,55 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def scorer_alone(ctx, stream, timed, torch, dev, peaks, with_oracle=True, w=3840, h=2160, steps=20):
+    """SSIMULACRA2 alone on a 3840x2160 pair: the original is the synthetic image (seed 0) at 4K, the distorted one
+    its JPEG round trip at quality 50, 4:2:0, trellis (the bit-exact GPU codec). Images resident on the device;
+    L2 flushed between calls. Reports Mpx/s, the roofline of the launch (6 B per pixel) and the error against the
+    reference-exact and FP64 oracles."""
+    import rcg
+    import rcg.synth as synth
+
+    ref = synth.image(w, h, 0)
+    ci = ctx.build_coefs(ref, rcg.EncodeOptions(50, rcg.Subsampling.S420, True))
+    dist_img = ctx.reconstruct(ci)
+    d_ref = torch.from_numpy(ref).to(dev)
+    d_dist = torch.from_numpy(dist_img).to(dev)
+    torch.cuda.synchronize()
+
+    def one():
+        return ctx.ssimulacra2_device(d_ref.data_ptr(), d_dist.data_ptr(), w, h, 3)
+
+    for _ in range(3):
+        one()
+    times, score = timed(one, steps)
+    ms = sum(times) / len(times)
+    ctx.set_profiling(True)
+    for _ in range(5):
+        one()
+    n, tiles_ms = ctx.kernel_time("ssim2_tiles")
+    ctx.set_profiling(False)
+    tile_ms = tiles_ms / max(1, n)
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    out = {
+        "workload": "SSIMULACRA2 of a 3840x2160 RGB8 pair (synthetic seed 0 vs its q50 4:2:0 JPEG round trip)",
+        "score": score, "ms_per_score": ms, "mpx_per_s": (w * h / 1e6) / (ms / 1000.0),
+        "roofline": {"kernel": "ssim2_tiles", "bound": "hbm", "achieved": 6.0 * w * h / (tile_ms / 1000.0) / 1e9,
+                     "peak": hbm, "unit": "GB/s", "frac": 6.0 * w * h / (tile_ms / 1000.0) / 1e9 / hbm,
+                     "avg_launch_ms": tile_ms},
+    }
+    if with_oracle:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        oracle.build()
+        oracle.set_threads(os.cpu_count() or 1)
+        o = oracle.ssimulacra2(ref, dist_img)
+        o64 = oracle.ssimulacra2(ref, dist_img, fp64=True)
+        out.update({"oracle": o, "oracle_fp64": o64, "abs_err_vs_oracle": abs(score - o),
+                    "abs_err_vs_fp64": abs(score - o64)})
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -155,6 +205,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="rcg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-scorer", action="store_true", help="skip the scorer-alone measurement")
     ap.add_argument("--width", type=int, default=W, help="smaller cases for profiling only; the bench line uses 4000")
     ap.add_argument("--height", type=int, default=H)
     args = ap.parse_args()
@@ -218,11 +269,10 @@ def main():
     times, res = timed(step_device, args.steps)
     launches = ctx.launch_count() - l0
     clocks = sampler.stop()
-    total_ms = sum(times)
+    from rcg import replicas
+
+    total_ms = replicas.max_over_ranks(sum(times), dist)
     if dist:
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
         dist.barrier()
     value = world * args.steps / (total_ms / 1000.0)
 
@@ -237,11 +287,7 @@ def main():
     for _ in range(2):
         step_e2e()
     e2e_times, f = timed(step_e2e, max(3, args.steps // 2))
-    e2e_ms = sum(e2e_times) / len(e2e_times)
-    if dist:
-        t = torch.tensor([e2e_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = replicas.max_over_ranks(sum(e2e_times) / len(e2e_times), dist)
     e2e_value = world * 1000.0 / e2e_ms
 
     # Per-kernel times (CUDA events around every launch) over 3 more searches, for the roofline.
@@ -266,6 +312,9 @@ def main():
             "avg_launch_ms": tile_ms,
             "note": "the scorer is FP32-ALU bound (~1 kflop per full-resolution pixel), far below the HBM roof; "
                     "algorithmic bytes = 6 B per full-resolution pixel (two RGB8 images)"}
+    scorer = None
+    if rank == 0 and not args.no_scorer:
+        scorer = scorer_alone(ctx, stream, timed, torch, dev, peaks, with_oracle=not args.no_cpu_baseline)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
@@ -298,6 +347,7 @@ def main():
             "result": {"quality": res[0], "score": res[1], "candidates": len(res[2])},
             "kernels_ms_per_search": {k: v["ms"] / 3 for k, v in prof.items() if v["launches"]},
             "scorer_mpx_per_s": (W * H / 1e6) / (tile_ms / 1000.0),
+            "scorer_alone": scorer,
         }
         print(json.dumps(out), flush=True)
     if dist:

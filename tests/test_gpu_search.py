@@ -87,3 +87,11 @@ def test_repeated_searches_agree(ctx):
     a = ctx.find_quality_ssimulacra2(img, 70.0)
     b = ctx.find_quality_ssimulacra2(img, 70.0)
     assert a.trace == b.trace and np.array_equal(a.coefs.flat(), b.coefs.flat())
+
+
+@pytest.mark.parametrize("w,h", [(8, 8), (9, 13), (17, 33), (64, 48), (257, 9)])
+def test_search_tiny_and_awkward_sizes(ctx, oracle, w, h):
+    """Every column of these images is near the zero left/right border at some scale: the split scorer's border
+    corrections and the per-scale tiling are exercised on each candidate."""
+    img = synth.image(max(w, 16), max(h, 16), 9, sensor_sigma=4.0)[:h, :w].copy()
+    _compare(ctx, oracle, img, 60.0, rcg.Subsampling.S420)
