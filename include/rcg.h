@@ -137,6 +137,18 @@ int rcg_search_device(rcg_ctx* ctx, const uint8_t* d_src, uint32_t width, uint32
                       double target, int max_quality, const rcg_encode_options* opts, rcg_found* found,
                       int16_t* d_coefs, size_t coefs_len, uint8_t* d_qtables);
 
+/* Many independent searches at once: the images (host buffers, each with its own size, channel count and target)
+ * share max_quality and the options. Up to `parallel` searches (0: 4) run at the same time, each on its own stream and
+ * workspace owned by `ctx`, so small images no longer leave the GPU idle between kernels. Results are exactly those of
+ * rcg_search on each image: found[i], coefs[i] (capacity coefs_len[i]; the array or an entry may be NULL) and
+ * qtables[i] (2*64 bytes; nullable). The cli's per-file loop over rayon workers (cli/src/main.rs:57-60) maps onto this
+ * call; no single reference function corresponds to it. Returns the first failing image's status (the others still
+ * run) with its index in the message. */
+int rcg_search_batch(rcg_ctx* ctx, int n, const uint8_t* const* srcs, const uint32_t* widths,
+                     const uint32_t* heights, const int* channels, const double* targets, int max_quality,
+                     const rcg_encode_options* opts, int parallel, rcg_found* found, int16_t* const* coefs,
+                     const size_t* coefs_len, uint8_t* const* qtables);
+
 #ifdef __cplusplus
 }
 #endif

@@ -10,6 +10,9 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <thread>
+#include <atomic>
+#include <numeric>
 
 #include "rcg_internal.cuh"
 
@@ -87,6 +90,68 @@ void collect_times(rcg_ctx* ctx) {
     ctx->event_pool.push_back(p.b);
   }
   ctx->pending.clear();
+}
+
+// ------------------------------------------------------------------------------------------------ host copies
+
+static bool is_pinned(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+static void* grow_pinned(void** buf, size_t* cap, size_t bytes) {
+  if (*buf && *cap >= bytes) return *buf;
+  if (*buf) cudaFreeHost(*buf);
+  *buf = nullptr;
+  *cap = 0;
+  if (cudaHostAlloc(buf, bytes, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    *buf = nullptr;
+    return nullptr;
+  }
+  *cap = bytes;
+  return *buf;
+}
+
+int copy_to_device(rcg_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  cudaError_t e;
+  if (!ctx->stage_copies || is_pinned(src)) {
+    e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  } else {
+    // the staging buffer may still feed the previous call's copy: wait for the stream before overwriting it
+    cudaStreamSynchronize(ctx->stream);
+    void* st = grow_pinned(&ctx->pinned_in, &ctx->pinned_in_bytes, bytes);
+    if (!st) {
+      e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream);  // pageable fallback
+    } else {
+      std::memcpy(st, src, bytes);
+      e = cudaMemcpyAsync(dst, st, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    }
+  }
+  return e == cudaSuccess ? RCG_OK : cuda_fail(ctx, e, "host to device copy");
+}
+
+int copy_to_host(rcg_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  cudaError_t e;
+  if (!ctx->stage_copies || is_pinned(dst)) {
+    e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  } else {
+    void* st = grow_pinned(&ctx->pinned_out, &ctx->pinned_out_bytes, bytes);
+    if (!st) {
+      e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    } else {
+      e = cudaMemcpyAsync(st, src, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+      if (e == cudaSuccess) std::memcpy(dst, st, bytes);
+    }
+  }
+  return e == cudaSuccess ? RCG_OK : cuda_fail(ctx, e, "device to host copy");
 }
 
 // ------------------------------------------------------------------------------------------------ sRGB tables
@@ -271,11 +336,15 @@ int rcg_ctx_create(int device, rcg_ctx** out) {
 
 void rcg_ctx_destroy(rcg_ctx* ctx) {
   if (!ctx) return;
+  for (rcg_ctx* wk : ctx->workers) rcg_ctx_destroy(wk);
+  ctx->workers.clear();
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   for (auto& kv : ctx->bufs)
     if (kv.second.ptr) cudaFree(kv.second.ptr);
   if (ctx->lut16) cudaFree(ctx->lut16);
+  if (ctx->pinned_in) cudaFreeHost(ctx->pinned_in);
+  if (ctx->pinned_out) cudaFreeHost(ctx->pinned_out);
   for (auto& p : ctx->pending) {
     cudaEventDestroy(p.a);
     cudaEventDestroy(p.b);
@@ -365,8 +434,9 @@ int rcg_ssimulacra2(rcg_ctx* ctx, const uint8_t* reference, const uint8_t* disto
   uint8_t* d_a = (uint8_t*)workspace(ctx, "img_a", bytes);
   uint8_t* d_b = (uint8_t*)workspace(ctx, "img_b", bytes);
   if (!d_a || !d_b) return RCG_NO_MEMORY;
-  cudaMemcpyAsync(d_a, reference, bytes, cudaMemcpyHostToDevice, ctx->stream);
-  cudaMemcpyAsync(d_b, distorted, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  int rc;
+  if ((rc = copy_to_device(ctx, d_a, reference, bytes)) != RCG_OK) return rc;
+  if ((rc = copy_to_device(ctx, d_b, distorted, bytes)) != RCG_OK) return rc;
   return score_device_images(ctx, d_a, d_b, (int)width, (int)height, channels, depth, score);
 }
 
@@ -567,10 +637,11 @@ static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int cha
   const int16_t* best = slots + (size_t)hs.best_step * es.max_coefs;
   if (d_coefs_out || h_coefs_out) {
     if ((long long)coefs_len < lay.ncoefs) return fail(ctx, RCG_INVALID, "coefficient buffer too short");
-    if (d_coefs_out)
+    if (d_coefs_out) {
       cudaMemcpyAsync(d_coefs_out, best, (size_t)lay.ncoefs * 2, cudaMemcpyDeviceToDevice, ctx->stream);
-    else
-      cudaMemcpyAsync(h_coefs_out, best, (size_t)lay.ncoefs * 2, cudaMemcpyDeviceToHost, ctx->stream);
+    } else if ((rc = copy_to_host(ctx, h_coefs_out, best, (size_t)lay.ncoefs * 2)) != RCG_OK) {
+      return rc;
+    }
   }
   uint8_t qt[128];
   qtables_for(hs.best_q, qt);
@@ -595,7 +666,7 @@ int rcg_search(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height
   size_t bytes = (size_t)width * height * channels;
   uint8_t* d_src = (uint8_t*)workspace(ctx, "img_src", bytes);
   if (!d_src) return RCG_NO_MEMORY;
-  cudaMemcpyAsync(d_src, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  if ((rc = copy_to_device(ctx, d_src, src, bytes)) != RCG_OK) return rc;
   return search_impl(ctx, d_src, (int)width, (int)height, channels, target, max_q, opts->subsampling,
                      opts->trellis, found, nullptr, coefs_len, nullptr, coefs, qtables);
 }
@@ -615,6 +686,53 @@ int rcg_search_device(rcg_ctx* ctx, const uint8_t* d_src, uint32_t width, uint32
   cudaSetDevice(ctx->device);
   return search_impl(ctx, d_src, (int)width, (int)height, channels, target, max_q, opts->subsampling, opts->trellis,
                      found, d_coefs, coefs_len, d_qtables, nullptr, nullptr);
+}
+
+int rcg_search_batch(rcg_ctx* ctx, int n, const uint8_t* const* srcs, const uint32_t* widths,
+                     const uint32_t* heights, const int* channels, const double* targets, int max_quality,
+                     const rcg_encode_options* opts, int parallel, rcg_found* found, int16_t* const* coefs,
+                     const size_t* coefs_len, uint8_t* const* qtables) {
+  if (!ctx) return RCG_INVALID;
+  if (n < 0 || (n > 0 && (!srcs || !widths || !heights || !channels || !targets || !found)))
+    return fail(ctx, RCG_INVALID, "null pointer");
+  if (n == 0) return RCG_OK;
+  int rc = check_opts(ctx, opts, false);
+  if (rc != RCG_OK) return rc;
+  const int p = std::max(1, std::min(parallel > 0 ? parallel : 4, n));
+  while ((int)ctx->workers.size() < p) {
+    rcg_ctx* wk = nullptr;
+    int crc = rcg_ctx_create(ctx->device, &wk);
+    if (crc != RCG_OK) return fail(ctx, crc, "cannot create a batch worker context");
+    wk->stage_copies = true;  // several threads copy at once: keep them off the driver's shared pageable path
+    ctx->workers.push_back(wk);
+  }
+  // Largest images first, handed out one at a time: the workers finish at about the same time.
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return (uint64_t)widths[a] * heights[a] > (uint64_t)widths[b] * heights[b];
+  });
+  std::atomic<int> next(0);
+  std::vector<int> status(n, RCG_OK);
+  std::vector<std::string> messages(n);
+  auto work = [&](rcg_ctx* wk) {
+    cudaSetDevice(wk->device);
+    for (int k = next.fetch_add(1); k < n; k = next.fetch_add(1)) {
+      const int i = order[k];
+      int r = rcg_search(wk, srcs[i], widths[i], heights[i], channels[i], targets[i], max_quality, opts, &found[i],
+                         coefs ? coefs[i] : nullptr, coefs_len ? coefs_len[i] : 0, qtables ? qtables[i] : nullptr);
+      status[i] = r;
+      if (r != RCG_OK) messages[i] = wk->last_error;
+    }
+  };
+  std::vector<std::thread> threads;
+  for (int t = 1; t < p; t++) threads.emplace_back(work, ctx->workers[t]);
+  work(ctx->workers[0]);
+  for (auto& th : threads) th.join();
+  for (int i = 0; i < n; i++)
+    if (status[i] != RCG_OK) return fail(ctx, status[i], "image " + std::to_string(i) + ": " + messages[i]);
+  ctx->last_error.clear();
+  return RCG_OK;
 }
 
 }  // extern "C"

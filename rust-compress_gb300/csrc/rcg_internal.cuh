@@ -123,6 +123,14 @@ struct rcg_ctx {
   std::vector<cudaEvent_t> event_pool;
   std::map<std::string, rcg::DeviceBuffer> bufs;
   float* lut16 = nullptr;  // 65536-entry sRGB->linear table for 16-bit samples (allocated on first use)
+  std::vector<rcg_ctx*> workers;  // sub-contexts of rcg_search_batch (own streams and workspaces)
+  // Pinned host staging for host-buffer calls (grow-only): pageable copies go through the driver's own staging and
+  // serialize across threads; these let a worker thread do its memcpy in parallel with other workers' GPU work.
+  bool stage_copies = false;  // set on batch worker contexts
+  void* pinned_in = nullptr;
+  size_t pinned_in_bytes = 0;
+  void* pinned_out = nullptr;
+  size_t pinned_out_bytes = 0;
 };
 
 namespace rcg {
@@ -133,6 +141,12 @@ int cuda_fail(rcg_ctx* ctx, cudaError_t e, const char* what);
 
 // Grow-only named device workspace. Returns nullptr (and sets the error) on allocation failure.
 void* workspace(rcg_ctx* ctx, const char* name, size_t bytes);
+
+// Host<->device copies of caller buffers: the driver's path for single calls; on batch worker contexts direct DMA when
+// the caller's memory is pinned, else through the context's pinned staging buffer. copy_to_device is asynchronous on the context stream (the source may be reused as soon as it
+// returns); copy_to_host synchronizes the stream.
+int copy_to_device(rcg_ctx* ctx, void* dst, const void* src, size_t bytes);
+int copy_to_host(rcg_ctx* ctx, void* dst, const void* src, size_t bytes);
 
 // Kernel launch bookkeeping: counts launches and, when profiling, brackets them with events.
 void launch_begin(rcg_ctx* ctx, const char* name, cudaEvent_t* a, cudaEvent_t* b);

@@ -150,6 +150,7 @@ def _load():
                              ctypes.POINTER(_Found), P, sz, P]),
         "rcg_search_device": (i32, [P, P, u32, u32, i32, ctypes.c_double, i32, ctypes.POINTER(_Opts),
                                     ctypes.POINTER(_Found), P, sz, P]),
+        "rcg_search_batch": (i32, [P, i32, P, P, P, P, P, i32, ctypes.POINTER(_Opts), i32, P, P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -162,7 +163,8 @@ _lib = _load()
 EXPORTED = (
     "rcg_ctx_create rcg_ctx_destroy rcg_last_error rcg_ctx_set_stream rcg_ctx_stream rcg_ctx_synchronize "
     "rcg_ctx_launch_count rcg_ctx_set_profiling rcg_ctx_kernel_time rcg_coef_layout_for rcg_ssimulacra2 "
-    "rcg_ssimulacra2_device rcg_ssimulacra2_device_noalloc rcg_build_coefs rcg_reconstruct rcg_search rcg_search_device"
+    "rcg_ssimulacra2_device rcg_ssimulacra2_device_noalloc rcg_build_coefs rcg_reconstruct rcg_search rcg_search_device "
+    "rcg_search_batch"
 ).split()
 
 
@@ -299,26 +301,72 @@ class Context:
                                          flat.ctypes.data, out.ctypes.data, out.size))
         return out[:, :, 0] if nc == 1 else out
 
-    def find_quality_ssimulacra2(self, reference, target, max_quality=100, opts=None):
-        """The --target-ssimulacra2 search (jpeg/src/target.rs:29 with cli/src/pipeline.rs:207-222), on device."""
+    def coef_capacity(self, width, height, channels, opts):
+        """int16 count that holds the search result for any quality (Auto switches layout at quality 90)."""
+        return max(self.coef_layout(width, height, channels, EncodeOptions(q, opts.subsampling, opts.trellis)).ncoefs
+                   for q in (1, 89, 90, 100))
+
+    def find_quality_ssimulacra2(self, reference, target, max_quality=100, opts=None, out=None):
+        """The --target-ssimulacra2 search (jpeg/src/target.rs:29 with cli/src/pipeline.rs:207-222), on device.
+
+        `out` (optional): a reusable int16 array of at least coef_capacity() entries; the returned coefficients are
+        views into it (valid until it is reused), which spares a fresh allocation per call."""
         opts = opts or EncodeOptions()
         a, w, h, c, d = _image(reference)
         if d != 8 or c not in (1, 3):
             raise RcgError(RCG_INVALID, "the search takes 8-bit Gray or Rgb")
-        # Size the output for the largest layout the options allow (Auto switches layout at quality 90).
-        cap = 0
-        for q in (1, 89, 90, 100):
-            cap = max(cap, self.coef_layout(w, h, c, EncodeOptions(q, opts.subsampling, opts.trellis)).ncoefs)
-        coefs = np.zeros(cap, dtype=np.int16)
+        cap = self.coef_capacity(w, h, c, opts)
+        if out is None:
+            coefs = np.empty(cap, dtype=np.int16)
+        else:
+            if out.dtype != np.int16 or out.size < cap or not out.flags.c_contiguous:
+                raise ValueError(f"out must be a contiguous int16 array of at least {cap} entries")
+            coefs = out
         qt = np.zeros((2, 64), dtype=np.uint8)
         f = _Found()
         o = _opts(opts)
         self._check(_lib.rcg_search(self._ptr, a.ctypes.data, w, h, c, float(target), int(max_quality),
                                     ctypes.byref(o), ctypes.byref(f), coefs.ctypes.data, coefs.size, qt.ctypes.data))
         lay = self.coef_layout(w, h, c, EncodeOptions(f.quality, opts.subsampling, opts.trellis))
-        ci = _coef_image(w, h, lay, coefs[: lay.ncoefs].copy(), qt)
+        ci = _coef_image(w, h, lay, coefs[: lay.ncoefs], qt)
         trace = [(int(f.trace_q[i]), float(f.trace_score[i])) for i in range(f.nsteps)]
         return Found(int(f.quality), float(f.score), ci, trace)
+
+    def search_batch(self, images, targets, max_quality=100, opts=None, parallel=0):
+        """Independent searches over many images at once (rcg_search_batch); same results as one search each."""
+        opts = opts or EncodeOptions()
+        n = len(images)
+        arrs = [_image(im) for im in images]
+        for a, w, h, c, d in arrs:
+            if d != 8 or c not in (1, 3):
+                raise RcgError(RCG_INVALID, "the search takes 8-bit Gray or Rgb")
+        srcs = (ctypes.c_void_p * n)(*[a.ctypes.data for a, *_ in arrs])
+        ws = (ctypes.c_uint32 * n)(*[w for _, w, _, _, _ in arrs])
+        hs = (ctypes.c_uint32 * n)(*[h for _, _, h, _, _ in arrs])
+        cs = (ctypes.c_int * n)(*[c for _, _, _, c, _ in arrs])
+        ts = (ctypes.c_double * n)(*[float(t) for t in targets])
+        found = (_Found * n)()
+        coefs, caps, qts = [], [], []
+        for a, w, h, c, _ in arrs:
+            cap = max(self.coef_layout(w, h, c, EncodeOptions(q, opts.subsampling, opts.trellis)).ncoefs
+                      for q in (1, 89, 90, 100))
+            coefs.append(np.zeros(cap, dtype=np.int16))
+            caps.append(cap)
+            qts.append(np.zeros((2, 64), dtype=np.uint8))
+        cptr = (ctypes.c_void_p * n)(*[x.ctypes.data for x in coefs])
+        clen = (ctypes.c_size_t * n)(*caps)
+        qptr = (ctypes.c_void_p * n)(*[x.ctypes.data for x in qts])
+        o = _opts(opts)
+        self._check(_lib.rcg_search_batch(self._ptr, n, srcs, ws, hs, cs, ts, int(max_quality), ctypes.byref(o),
+                                          int(parallel), found, cptr, clen, qptr))
+        out = []
+        for i, (a, w, h, c, _) in enumerate(arrs):
+            f = found[i]
+            lay = self.coef_layout(w, h, c, EncodeOptions(f.quality, opts.subsampling, opts.trellis))
+            ci = _coef_image(w, h, lay, coefs[i][: lay.ncoefs].copy(), qts[i])
+            trace = [(int(f.trace_q[k]), float(f.trace_score[k])) for k in range(f.nsteps)]
+            out.append(Found(int(f.quality), float(f.score), ci, trace))
+        return out
 
     def search_device(self, src_ptr, width, height, channels, target, max_quality, opts, coefs_ptr=0,
                       coefs_len=0, qt_ptr=0):

@@ -95,3 +95,25 @@ def test_search_tiny_and_awkward_sizes(ctx, oracle, w, h):
     corrections and the per-scale tiling are exercised on each candidate."""
     img = synth.image(max(w, 16), max(h, 16), 9, sensor_sigma=4.0)[:h, :w].copy()
     _compare(ctx, oracle, img, 60.0, rcg.Subsampling.S420)
+
+
+def test_batch_matches_individual_searches(ctx):
+    """rcg_search_batch (concurrent searches on worker streams) gives exactly each image's own search result."""
+    sizes = [(96, 80), (300, 200), (640, 480), (17, 33), (1000, 700), (64, 64), (333, 111)]
+    imgs = [synth.image(w, h, 20 + i, sensor_sigma=2.0) for i, (w, h) in enumerate(sizes)]
+    imgs[5] = np.ascontiguousarray(imgs[5][:, :, 0])  # a gray image in the mix
+    targets = [60.0, 70.0, 80.0, 65.0, 75.0, 55.0, 72.0]
+    opts = rcg.EncodeOptions(90, rcg.Subsampling.S420, True)
+    for parallel in (1, 3, 8):
+        res = ctx.search_batch(imgs, targets, 100, opts, parallel=parallel)
+        for im, t, r in zip(imgs, targets, res):
+            f = ctx.find_quality_ssimulacra2(im, t, 100, opts)
+            assert r.quality == f.quality and r.trace == f.trace
+            assert np.array_equal(r.coefs.flat(), f.coefs.flat())
+
+
+def test_batch_reports_the_failing_image(ctx):
+    imgs = [synth.image(64, 64, 1), np.zeros((4, 40, 3), np.uint8), synth.image(80, 64, 2)]
+    with pytest.raises(rcg.RcgError) as e:
+        ctx.search_batch(imgs, [60.0, 60.0, 60.0], 100, rcg.EncodeOptions(90, rcg.Subsampling.S420, True), 2)
+    assert e.value.status == rcg.RCG_UNSUPPORTED and "image 1" in e.value.message
