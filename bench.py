@@ -226,6 +226,38 @@ def batch_workload(ctx, torch, n=64, parallel=8, steps=2):
             "mean_quality": sum(r.quality for r in res_b) / n}
 
 
+def requantize_workload(ctx, img, timed, with_oracle=True, steps=5):
+    """The JPEG -> JPEG search (cli/src/pipeline.rs:369-386) on the same 12 MP image: the source is its q95 4:2:0
+    trellis encoding; target 70, trellis requantization. Host buffers through the public API (coefficients in,
+    coefficients and tables out). CPU baseline: the oracle's search on all host threads, once."""
+    import rcg
+
+    src = ctx.build_coefs(img, rcg.EncodeOptions(95, rcg.Subsampling.S420, True))
+    for _ in range(2):
+        ctx.find_quality_requantize(src, TARGET)
+    times, f = timed(lambda: ctx.find_quality_requantize(src, TARGET), steps)
+    ms = sum(times) / len(times)
+    out = {"workload": "JPEG->JPEG search: 4000x3000 seed 1 sigma 3 encoded at q95 4:2:0, target 70, trellis",
+           "searches_per_s": 1000.0 / ms, "ms_per_search": ms, "quality": f.quality, "score": f.score,
+           "candidates": len(f.trace)}
+    if with_oracle:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        oracle.build()
+        threads = os.cpu_count() or 1
+        oracle.set_threads(threads)
+        lay = {"ncomp": 3, "h": [c.h for c in src.comps], "v": [c.v for c in src.comps],
+               "blocks_w": [c.blocks_w for c in src.comps], "blocks_h": [c.blocks_h for c in src.comps]}
+        g = oracle.general_from_encoder(src.width, src.height, lay, src.qtables, src.flat())
+        t0 = time.perf_counter()
+        q, s, _, _ = oracle.search_requantize(g, TARGET)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "searches/s", "cores": threads, "kind": "port",
+                               "sample": "one full search", "quality": q, "same_quality": q == f.quality}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -235,6 +267,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-scorer", action="store_true", help="skip the scorer-alone measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the many-image batch measurement")
+    ap.add_argument("--no-requant", action="store_true", help="skip the JPEG->JPEG search measurement")
     ap.add_argument("--width", type=int, default=W, help="smaller cases for profiling only; the bench line uses 4000")
     ap.add_argument("--height", type=int, default=H)
     args = ap.parse_args()
@@ -349,6 +382,9 @@ def main():
     scorer = None
     if rank == 0 and not args.no_scorer:
         scorer = scorer_alone(ctx, stream, timed, torch, dev, peaks, with_oracle=not args.no_cpu_baseline)
+    requant = None
+    if rank == 0 and not args.no_requant:
+        requant = requantize_workload(ctx, img, timed, with_oracle=not args.no_cpu_baseline)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
@@ -383,6 +419,7 @@ def main():
             "scorer_mpx_per_s": (W * H / 1e6) / (tile_ms / 1000.0),
             "scorer_alone": scorer,
             "batch": batch,
+            "requantize": requant,
         }
         print(json.dumps(out), flush=True)
     if dist:

@@ -66,6 +66,13 @@ typedef struct {
   double trace_score[16]; /* its SSIMULACRA2 score (-DBL_MAX when it could not be scored) */
 } rcg_found;
 
+/* Quantization tables of a general CoefImage (jpeg/src/encode.rs:63, :77-78): each component names a table slot. */
+typedef struct {
+  int32_t tq[3];          /* table slot of each component */
+  uint8_t qtables[4][64]; /* natural order, by slot */
+  int32_t present[4];     /* nonzero where the slot holds a table (an absent source table counts as all ones) */
+} rcg_qtables;
+
 typedef struct rcg_ctx rcg_ctx;
 
 /* Context lifetime. `device` is a CUDA device ordinal. */
@@ -136,6 +143,24 @@ int rcg_search(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height
 int rcg_search_device(rcg_ctx* ctx, const uint8_t* d_src, uint32_t width, uint32_t height, int channels,
                       double target, int max_quality, const rcg_encode_options* opts, rcg_found* found,
                       int16_t* d_coefs, size_t coefs_len, uint8_t* d_qtables);
+
+/* reconstruct (jpeg/src/decode.rs:334) of a CoefImage with a general table assignment (requantized images: components
+ * may share a slot or each have their own). */
+int rcg_reconstruct_tables(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                           const rcg_qtables* tables, const int16_t* coefs, uint8_t* out, size_t out_len);
+
+/* jpeg::encode::CoefImage::requantize(quality, trellis) (jpeg/src/encode.rs:111): re-quantize existing coefficients
+ * (1 or 3 components, any integral sampling layout) toward the quality's tables, never finer than the source's, with
+ * the trellis pass when a table changed. Host buffers; `out` receives the new table assignment. */
+int rcg_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                   const rcg_qtables* in, const int16_t* coefs_in, int quality, int trellis, int16_t* coefs_out,
+                   size_t coefs_len, rcg_qtables* out);
+
+/* The JPEG -> JPEG `--target-ssimulacra2` search (cli/src/pipeline.rs:369-386): the reference image is the source
+ * reconstructed, each candidate the source requantized; bisection as rcg_search, on the device. */
+int rcg_search_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                          const rcg_qtables* in, const int16_t* coefs_in, double target, int max_quality,
+                          int trellis, rcg_found* found, int16_t* coefs_out, size_t coefs_len, rcg_qtables* out);
 
 /* Many independent searches at once: the images (host buffers, each with its own size, channel count and target)
  * share max_quality and the options. Up to `parallel` searches (0: 4) run at the same time, each on its own stream and

@@ -1177,6 +1177,117 @@ static Found find_quality(const uint8_t* ref, int w, int h, int channels, double
   return best;
 }
 
+// ------------------------------------------------------------------------------------------------ requantize
+
+// jpeg/src/encode.rs:107-172 (CoefImage::requantize) for 1- and 3-component images (table class = component index
+// min 1, jpeg/src/encode.rs:99-105).
+static void requantize(CoefImage& ci, int quality, bool trellis) {
+  uint8_t tables[2][64];
+  luma_table(quality, tables[0]);
+  chroma_table(quality, tables[1]);
+  uint8_t new_slots[4][64];
+  bool has_new[4] = {false, false, false, false};
+  bool changed = false;
+  struct Plan {
+    int slot;
+    float ratio[64];
+    uint8_t nt[64];
+  };
+  std::vector<Plan> plan;
+  std::vector<std::vector<int16_t>> originals;
+  if (trellis)
+    for (auto& c : ci.comps) originals.push_back(c.coefs);
+  for (size_t k = 0; k < ci.comps.size(); k++) {
+    CoefComponent& c = ci.comps[k];
+    uint8_t old[64];
+    if (ci.has_q[c.tq])
+      std::memcpy(old, ci.qtables[c.tq], 64);
+    else
+      std::memset(old, 1, 64);
+    const uint8_t* base = tables[std::min<size_t>(k, 1)];
+    Plan pl;
+    for (int n = 0; n < 64; n++) pl.nt[n] = std::max(base[n], old[n]);
+    changed |= std::memcmp(pl.nt, old, 64) != 0;
+    for (int z = 0; z < 64; z++) pl.ratio[z] = (float)old[ZIGZAG[z]] / (float)pl.nt[ZIGZAG[z]];
+    size_t nb = c.coefs.size() / 64;
+#pragma omp parallel for schedule(static)
+    for (long b = 0; b < (long)nb; b++) {
+      int16_t* blk = &c.coefs[(size_t)b * 64];
+      for (int z = 0; z < 64; z++) blk[z] = (int16_t)clampi(round_f32((float)blk[z] * pl.ratio[z]), -2047, 2047);
+    }
+    int slot = -1;
+    for (int sl = 0; sl < 4; sl++)
+      if (has_new[sl] && std::memcmp(new_slots[sl], pl.nt, 64) == 0) {
+        slot = sl;
+        break;
+      }
+    if (slot < 0) {
+      for (int sl = 0; sl < 4; sl++)
+        if (!has_new[sl]) {
+          slot = sl;
+          break;
+        }
+      std::memcpy(new_slots[slot], pl.nt, 64);
+      has_new[slot] = true;
+    }
+    c.tq = slot;
+    pl.slot = slot;
+    plan.push_back(pl);
+  }
+  for (int sl = 0; sl < 4; sl++) {
+    ci.has_q[sl] = has_new[sl];
+    if (has_new[sl]) std::memcpy(ci.qtables[sl], new_slots[sl], 64);
+  }
+  if (trellis && changed) {
+    uint8_t lens[2][256];
+    ac_code_lengths(ci, lens);
+    for (size_t k = 0; k < ci.comps.size(); k++) {
+      Rdo rdo(plan[k].nt, TRELLIS_KAPPA, lens[std::min<size_t>(k, 1)]);
+      CoefComponent& c = ci.comps[k];
+      size_t nb = c.coefs.size() / 64;
+#pragma omp parallel for schedule(dynamic, 64)
+      for (long b = 0; b < (long)nb; b++) {
+        float a[64];
+        const int16_t* in = &originals[k][(size_t)b * 64];
+        for (int z = 0; z < 64; z++) a[z] = (float)in[z] * plan[k].ratio[z];
+        rdo.quantize_ac(a, &c.coefs[(size_t)b * 64]);
+      }
+    }
+  }
+}
+
+// cli/src/pipeline.rs:369-386: the JPEG->JPEG search. The reference image is the source reconstructed; each
+// candidate is the source requantized (jpeg/src/target.rs:29-56 drives it).
+static Found find_quality_requantize(const CoefImage& src, double target, int max_quality, bool trellis,
+                                     std::vector<std::pair<int, double>>* trace) {
+  int oc = 0;
+  std::vector<uint8_t> ref = reconstruct(src, &oc);
+  auto make = [&](int q) {
+    CoefImage c = src;
+    requantize(c, q, trellis);
+    return c;
+  };
+  int lo = 1, hi = std::max(max_quality, 1);
+  CoefImage top = make(hi);
+  double top_score = score_coefs(ref.data(), src.width, src.height, oc, top);
+  if (trace) trace->push_back({hi, top_score});
+  Found best{hi, top_score, std::move(top)};
+  if (top_score < target) return best;
+  while (lo < hi) {
+    int mid = lo + (hi - lo) / 2;
+    CoefImage ci = make(mid);
+    double s = score_coefs(ref.data(), src.width, src.height, oc, ci);
+    if (trace) trace->push_back({mid, s});
+    if (s >= target) {
+      hi = mid;
+      best = Found{mid, s, std::move(ci)};
+    } else {
+      lo = mid + 1;
+    }
+  }
+  return best;
+}
+
 // ------------------------------------------------------------------------------------------------ write_best
 
 // jpeg/src/encode.rs:400-413 (segment, write_dht)
@@ -1638,6 +1749,47 @@ static CoefImage coef_from_flat(int w, int h, int ncomp, const int* hs, const in
   return ci;
 }
 
+// General flat form: per-component table slot `tq`, four table slots (has_q marks the present ones).
+static CoefImage coef_from_flat_tq(int w, int h, int ncomp, const int* hs, const int* vs, const int* bws,
+                                   const int* bhs, const int* tq, const uint8_t* qtables4, const uint8_t* has_q,
+                                   const int16_t* coefs) {
+  CoefImage ci;
+  ci.width = w;
+  ci.height = h;
+  for (int sl = 0; sl < 4; sl++) {
+    ci.has_q[sl] = has_q[sl] != 0;
+    std::memcpy(ci.qtables[sl], qtables4 + 64 * sl, 64);
+  }
+  size_t off = 0;
+  for (int i = 0; i < ncomp; i++) {
+    CoefComponent c;
+    c.id = (uint8_t)(i + 1);
+    c.h = hs[i];
+    c.v = vs[i];
+    c.tq = tq[i];
+    c.blocks_w = bws[i];
+    c.blocks_h = bhs[i];
+    size_t n = (size_t)bws[i] * bhs[i] * 64;
+    c.coefs.assign(coefs + off, coefs + off + n);
+    off += n;
+    ci.comps.push_back(std::move(c));
+  }
+  return ci;
+}
+
+static void coef_to_flat_tq(const CoefImage& ci, int16_t* out, int* tq, uint8_t* qtables4, uint8_t* has_q) {
+  size_t off = 0;
+  for (size_t i = 0; i < ci.comps.size(); i++) {
+    std::memcpy(out + off, ci.comps[i].coefs.data(), ci.comps[i].coefs.size() * 2);
+    off += ci.comps[i].coefs.size();
+    if (tq) tq[i] = ci.comps[i].tq;
+  }
+  for (int sl = 0; sl < 4; sl++) {
+    if (has_q) has_q[sl] = ci.has_q[sl] ? 1 : 0;
+    if (qtables4) std::memcpy(qtables4 + 64 * sl, ci.qtables[sl], 64);
+  }
+}
+
 static void coef_to_flat(const CoefImage& ci, int16_t* out, uint8_t* qtables) {
   size_t off = 0;
   for (auto& c : ci.comps) {
@@ -1793,6 +1945,62 @@ int orc_search(const uint8_t* data, int w, int h, int channels, double target, i
     if (trace_s) trace_s[i] = tr[i].second;
   }
   return 0;
+}
+
+// CoefImage::requantize (jpeg/src/encode.rs:111) of a general flat CoefImage (1 or 3 components).
+int orc_requantize(int w, int h, int ncomp, const int* hs, const int* vs, const int* bws, const int* bhs,
+                   const int* tq, const uint8_t* qtables4, const uint8_t* has_q, const int16_t* coefs, int quality,
+                   int trellis, int16_t* coefs_out, int* tq_out, uint8_t* qtables4_out, uint8_t* has_q_out) {
+  if (ncomp != 1 && ncomp != 3) return 1;
+  orc::CoefImage ci = orc::coef_from_flat_tq(w, h, ncomp, hs, vs, bws, bhs, tq, qtables4, has_q, coefs);
+  orc::requantize(ci, quality, trellis != 0);
+  orc::coef_to_flat_tq(ci, coefs_out, tq_out, qtables4_out, has_q_out);
+  return 0;
+}
+
+// reconstruct of a general flat CoefImage.
+int orc_reconstruct_tq(int w, int h, int ncomp, const int* hs, const int* vs, const int* bws, const int* bhs,
+                       const int* tq, const uint8_t* qtables4, const uint8_t* has_q, const int16_t* coefs,
+                       uint8_t* out, int* out_channels) {
+  orc::CoefImage ci = orc::coef_from_flat_tq(w, h, ncomp, hs, vs, bws, bhs, tq, qtables4, has_q, coefs);
+  std::vector<uint8_t> img = orc::reconstruct(ci, out_channels);
+  std::memcpy(out, img.data(), img.size());
+  return 0;
+}
+
+// The JPEG->JPEG search (cli/src/pipeline.rs:369-386) over a general flat CoefImage.
+int orc_search_requantize(int w, int h, int ncomp, const int* hs, const int* vs, const int* bws, const int* bhs,
+                          const int* tq, const uint8_t* qtables4, const uint8_t* has_q, const int16_t* coefs,
+                          double target, int max_quality, int trellis, int* found_q, double* found_score,
+                          int16_t* coefs_out, int* tq_out, uint8_t* qtables4_out, uint8_t* has_q_out, int* trace_q,
+                          double* trace_s, int* ntrace) {
+  if (ncomp != 1 && ncomp != 3) return 1;
+  orc::CoefImage ci = orc::coef_from_flat_tq(w, h, ncomp, hs, vs, bws, bhs, tq, qtables4, has_q, coefs);
+  std::vector<std::pair<int, double>> tr;
+  orc::Found f = orc::find_quality_requantize(ci, target, max_quality, trellis != 0, &tr);
+  *found_q = f.quality;
+  *found_score = f.score;
+  orc::coef_to_flat_tq(f.coefs, coefs_out, tq_out, qtables4_out, has_q_out);
+  if (ntrace) *ntrace = (int)tr.size();
+  for (size_t i = 0; i < tr.size() && i < 16; i++) {
+    if (trace_q) trace_q[i] = tr[i].first;
+    if (trace_s) trace_s[i] = tr[i].second;
+  }
+  return 0;
+}
+
+// write_best of a general flat CoefImage (per-component table slots).
+long orc_write_best_tq(int w, int h, int ncomp, const int* hs, const int* vs, const int* bws, const int* bhs,
+                       const int* tq, const uint8_t* qtables4, const uint8_t* has_q, const int16_t* coefs,
+                       uint8_t* out, long cap, int* progressive) {
+  orc::CoefImage ci = orc::coef_from_flat_tq(w, h, ncomp, hs, vs, bws, bhs, tq, qtables4, has_q, coefs);
+  std::vector<orc::Scan> script;
+  uint64_t prog_est = orc::plan(ci, script);
+  uint64_t base_est = orc::baseline_estimate(ci);
+  std::vector<uint8_t> bytes = base_est <= prog_est ? orc::write_jpeg(ci) : orc::emit_progressive(ci, script);
+  if (progressive) *progressive = base_est <= prog_est ? 0 : 1;
+  if (out) std::memcpy(out, bytes.data(), std::min<size_t>(bytes.size(), (size_t)cap));
+  return (long)bytes.size();
 }
 
 // write_best (jpeg/src/encode.rs:543-546) of a flat CoefImage. Returns the byte count; writes at most `cap` bytes.

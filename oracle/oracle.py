@@ -42,6 +42,12 @@ def lib():
         L.orc_search.argtypes = [P, i32, i32, i32, ctypes.c_double, i32, i32, i32, pi, pd, P, P, P, P, pi]
         L.orc_write_best.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, ctypes.c_long, pi]
         L.orc_write_best.restype = ctypes.c_long
+        L.orc_requantize.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, P, i32, i32, P, P, P, P]
+        L.orc_reconstruct_tq.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, P, P, pi]
+        L.orc_search_requantize.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, P, ctypes.c_double, i32, i32, pi, pd,
+                                            P, P, P, P, P, P, pi]
+        L.orc_write_best_tq.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, P, P, ctypes.c_long, pi]
+        L.orc_write_best_tq.restype = ctypes.c_long
         L.orc_round_f32.argtypes = [ctypes.c_float]
         L.orc_round_f32.restype = ctypes.c_int32
         L.orc_fdct.argtypes = [P]
@@ -175,3 +181,82 @@ def write_best(w, h, lay, qt, coefs):
     lib().orc_write_best(w, h, n, hs.ctypes.data, vs.ctypes.data, bws.ctypes.data, bhs.ctypes.data, qt.ctypes.data,
                          coefs.ctypes.data, out.ctypes.data, size, ctypes.byref(prog))
     return out.tobytes(), bool(prog.value)
+
+
+class GeneralCoefs:
+    """A general flat CoefImage: layout, per-component table slot tq, four table slots (has_q marks present ones)."""
+
+    def __init__(self, w, h, lay, tq, qtables4, has_q, coefs):
+        self.w, self.h, self.lay = w, h, lay
+        self.tq = np.ascontiguousarray(np.pad(np.asarray(tq, np.int32), (0, 3 - len(tq))))
+        self.qtables4 = np.ascontiguousarray(np.asarray(qtables4, np.uint8).reshape(4, 64))
+        self.has_q = np.ascontiguousarray(np.asarray(has_q, np.uint8).reshape(4))
+        self.coefs = np.ascontiguousarray(coefs, dtype=np.int16)
+
+    def args(self):
+        n, hs, vs, bws, bhs = _lay_arrays(self.lay)
+        self._keep = (hs, vs, bws, bhs)
+        return (self.w, self.h, n, hs.ctypes.data, vs.ctypes.data, bws.ctypes.data, bhs.ctypes.data,
+                self.tq.ctypes.data, self.qtables4.ctypes.data, self.has_q.ctypes.data, self.coefs.ctypes.data)
+
+
+def general_from_encoder(w, h, lay, qt, coefs):
+    """The encoder's CoefImage in general form: tq = [0, 1, 1], slots 0 (luma) and 1 (chroma)."""
+    n = lay["ncomp"]
+    q4 = np.zeros((4, 64), np.uint8)
+    q4[0] = qt[0]
+    has = np.zeros(4, np.uint8)
+    has[0] = 1
+    if n > 1:
+        q4[1] = qt[1]
+        has[1] = 1
+    return GeneralCoefs(w, h, lay, [0] + [1] * (n - 1), q4, has, coefs)
+
+
+def requantize(g, quality, trellis=True):
+    out = np.zeros_like(g.coefs)
+    tq = np.zeros(3, np.int32)
+    q4 = np.zeros((4, 64), np.uint8)
+    has = np.zeros(4, np.uint8)
+    rc = lib().orc_requantize(*g.args(), int(quality), 1 if trellis else 0, out.ctypes.data, tq.ctypes.data,
+                              q4.ctypes.data, has.ctypes.data)
+    if rc:
+        raise ValueError("unsupported component count")
+    return GeneralCoefs(g.w, g.h, g.lay, tq[: g.lay["ncomp"]], q4, has, out)
+
+
+def reconstruct_general(g):
+    n = g.lay["ncomp"]
+    out = np.zeros((g.h, g.w, n), np.uint8)
+    oc = ctypes.c_int()
+    lib().orc_reconstruct_tq(*g.args(), out.ctypes.data, ctypes.byref(oc))
+    return out[:, :, 0] if n == 1 else out
+
+
+def search_requantize(g, target, max_quality=100, trellis=True):
+    q = ctypes.c_int()
+    s = ctypes.c_double()
+    out = np.zeros_like(g.coefs)
+    tq = np.zeros(3, np.int32)
+    q4 = np.zeros((4, 64), np.uint8)
+    has = np.zeros(4, np.uint8)
+    tqs = np.zeros(16, np.int32)
+    ts = np.zeros(16, np.float64)
+    nt = ctypes.c_int()
+    rc = lib().orc_search_requantize(*g.args(), float(target), int(max_quality), 1 if trellis else 0,
+                                     ctypes.byref(q), ctypes.byref(s), out.ctypes.data, tq.ctypes.data,
+                                     q4.ctypes.data, has.ctypes.data, tqs.ctypes.data, ts.ctypes.data,
+                                     ctypes.byref(nt))
+    if rc:
+        raise ValueError("unsupported component count")
+    trace = [(int(tqs[i]), float(ts[i])) for i in range(nt.value)]
+    return q.value, s.value, GeneralCoefs(g.w, g.h, g.lay, tq[: g.lay["ncomp"]], q4, has, out), trace
+
+
+def write_best_general(g):
+    prog = ctypes.c_int()
+    size = lib().orc_write_best_tq(*g.args(), None, 0, ctypes.byref(prog))
+    out = np.zeros(size, dtype=np.uint8)
+    lib().orc_write_best_tq(*g.args(), out.ctypes.data, size, ctypes.byref(prog))
+    return out.tobytes(), bool(prog.value)
+

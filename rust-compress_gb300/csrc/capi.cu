@@ -298,6 +298,78 @@ static int check_opts(rcg_ctx* ctx, const rcg_encode_options* o, bool need_quali
   return RCG_OK;
 }
 
+// Block layout of a caller-given CoefImage (jpeg/src/decode.rs:334-357, :1345-1358): integral sampling ratios, block
+// grids at least as large as the MCU grid.
+static int layout_step(rcg_ctx* ctx, StepDesc* st, int w, int h, const rcg_coef_layout* layout) {
+  std::memset(st, 0, sizeof *st);
+  st->active = 1;
+  const int nc = layout->ncomp;
+  st->ncomp = nc;
+  int hmax = 1, vmax = 1;
+  for (int c = 0; c < nc; c++) {
+    hmax = std::max(hmax, (int)layout->h[c]);
+    vmax = std::max(vmax, (int)layout->v[c]);
+  }
+  st->hmax = hmax;
+  st->vmax = vmax;
+  long long blk = 0, poff = 0;
+  int mcus_x = (w + 8 * hmax - 1) / (8 * hmax), mcus_y = (h + 8 * vmax - 1) / (8 * vmax);
+  st->mcus_x = mcus_x;
+  st->mcus_y = mcus_y;
+  for (int c = 0; c < nc; c++) {
+    CompDesc& cd = st->comp[c];
+    cd.h = layout->h[c];
+    cd.v = layout->v[c];
+    cd.bw = layout->blocks_w[c];
+    cd.bh = layout->blocks_h[c];
+    cd.cls = c == 0 ? 0 : 1;
+    if (cd.h < 1 || cd.v < 1 || hmax % cd.h || vmax % cd.v)
+      return fail(ctx, RCG_UNSUPPORTED, "non-integral chroma subsampling ratio");
+    if (cd.bw < mcus_x * cd.h || cd.bh < mcus_y * cd.v)
+      return fail(ctx, RCG_INVALID, "block grid smaller than the MCU grid");
+    cd.blk0 = blk;
+    cd.plane_off = poff;
+    blk += (long long)cd.bw * cd.bh;
+    poff += (long long)cd.bw * 8 * cd.bh * 8;
+  }
+  st->nblocks = blk;
+  if (layout->ncoefs != blk * 64) return fail(ctx, RCG_INVALID, "layout.ncoefs does not match the block grids");
+  return RCG_OK;
+}
+
+static long long plane_bytes(const StepDesc* st) {
+  long long b = 0;
+  for (int c = 0; c < st->ncomp; c++) b += (long long)st->comp[c].bw * 8 * st->comp[c].bh * 8;
+  return b;
+}
+
+// ---- requantization
+
+// Source tables per component (jpeg/src/encode.rs:121): the slot the component names, all ones where it is empty.
+static int requant_inputs(rcg_ctx* ctx, const rcg_qtables* in, StepDesc* st) {
+  if (!in) return fail(ctx, RCG_INVALID, "null tables");
+  for (int c = 0; c < st->ncomp; c++) {
+    int slot = in->tq[c];
+    if (slot < 0 || slot > 3) return fail(ctx, RCG_INVALID, "table slot out of range");
+    if (in->present[slot])
+      std::memcpy(st->src_qt[c], in->qtables[slot], 64);
+    else
+      std::memset(st->src_qt[c], 1, 64);  // jpeg/src/encode.rs:121: unwrap_or([1; 64])
+  }
+  return RCG_OK;
+}
+
+static void qtables_out(const int tq[3], const uint8_t slot_qt[4][64], const int present[4], int ncomp,
+                        rcg_qtables* out) {
+  if (!out) return;
+  std::memset(out, 0, sizeof *out);
+  for (int c = 0; c < ncomp; c++) out->tq[c] = tq[c];
+  for (int sl = 0; sl < 4; sl++) {
+    out->present[sl] = present[sl];
+    if (present[sl]) std::memcpy(out->qtables[sl], slot_qt[sl], 64);
+  }
+}
+
 }  // namespace rcg
 
 using namespace rcg;
@@ -503,58 +575,15 @@ int rcg_build_coefs(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t h
 
 // ---- decoder
 
-int rcg_reconstruct(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
-                    const uint8_t* qtables, const int16_t* coefs, uint8_t* out, size_t out_len) {
-  if (!ctx) return RCG_INVALID;
-  if (!layout || !qtables || !coefs || !out) return fail(ctx, RCG_INVALID, "null pointer");
-  if (width == 0 || height == 0) return fail(ctx, RCG_INVALID, "empty image");
-  int nc = layout->ncomp;
-  if (nc != 1 && nc != 3) return fail(ctx, RCG_UNSUPPORTED, "reconstruct takes 1 or 3 components");
-  int w = (int)width, h = (int)height;
-  StepDesc* st = new StepDesc;
-  std::memset(st, 0, sizeof *st);
-  st->active = 1;
-  st->ncomp = nc;
-  int hmax = 1, vmax = 1;
-  for (int c = 0; c < nc; c++) {
-    hmax = std::max(hmax, (int)layout->h[c]);
-    vmax = std::max(vmax, (int)layout->v[c]);
-  }
-  st->hmax = hmax;
-  st->vmax = vmax;
-  long long blk = 0, poff = 0;
-  int mcus_x = (w + 8 * hmax - 1) / (8 * hmax), mcus_y = (h + 8 * vmax - 1) / (8 * vmax);
-  for (int c = 0; c < nc; c++) {
-    CompDesc& cd = st->comp[c];
-    cd.h = layout->h[c];
-    cd.v = layout->v[c];
-    cd.bw = layout->blocks_w[c];
-    cd.bh = layout->blocks_h[c];
-    cd.cls = c == 0 ? 0 : 1;
-    if (cd.h < 1 || cd.v < 1 || hmax % cd.h || vmax % cd.v) {
-      delete st;
-      return fail(ctx, RCG_UNSUPPORTED, "non-integral chroma subsampling ratio");
-    }
-    if (cd.bw < mcus_x * cd.h || cd.bh < mcus_y * cd.v) {
-      delete st;
-      return fail(ctx, RCG_INVALID, "block grid smaller than the MCU grid");
-    }
-    cd.blk0 = blk;
-    cd.plane_off = poff;
-    blk += (long long)cd.bw * cd.bh;
-    poff += (long long)cd.bw * 8 * cd.bh * 8;
-  }
-  st->nblocks = blk;
-  if (layout->ncoefs != blk * 64) {
-    delete st;
-    return fail(ctx, RCG_INVALID, "layout.ncoefs does not match the block grids");
-  }
+// reconstruct (jpeg/src/decode.rs:334-389) with the multipliers already in `st` (owned; deleted here).
+static int reconstruct_with(rcg_ctx* ctx, StepDesc* st, int w, int h, const int16_t* coefs, uint8_t* out,
+                            size_t out_len) {
+  const int nc = st->ncomp;
+  long long blk = st->nblocks, poff = plane_bytes(st);
   if (out_len < (size_t)w * h * nc) {
     delete st;
     return fail(ctx, RCG_INVALID, "output buffer too short");
   }
-  // idct_planes multipliers from the given tables (jpeg/src/decode.rs:1316-1321)
-  fill_mult(st, qtables, nc == 1 ? 1 : 2);
   cudaSetDevice(ctx->device);
   int16_t* d_coefs = (int16_t*)workspace(ctx, "coefs_single", (size_t)blk * 64 * 2);
   uint8_t* d_planes = (uint8_t*)workspace(ctx, "dec_planes_single", (size_t)poff);
@@ -572,6 +601,47 @@ int rcg_reconstruct(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coe
   cudaStreamSynchronize(ctx->stream);
   delete st;
   return finish(ctx, "reconstruct");
+}
+
+static int reconstruct_checks(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                              const void* tables, const int16_t* coefs, uint8_t* out, StepDesc** st_out) {
+  if (!layout || !tables || !coefs || !out) return fail(ctx, RCG_INVALID, "null pointer");
+  if (width == 0 || height == 0) return fail(ctx, RCG_INVALID, "empty image");
+  if (layout->ncomp != 1 && layout->ncomp != 3) return fail(ctx, RCG_UNSUPPORTED, "reconstruct takes 1 or 3 components");
+  StepDesc* st = new StepDesc;
+  int rc = layout_step(ctx, st, (int)width, (int)height, layout);
+  if (rc != RCG_OK) {
+    delete st;
+    return rc;
+  }
+  *st_out = st;
+  return RCG_OK;
+}
+
+int rcg_reconstruct(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                    const uint8_t* qtables, const int16_t* coefs, uint8_t* out, size_t out_len) {
+  if (!ctx) return RCG_INVALID;
+  StepDesc* st = nullptr;
+  int rc = reconstruct_checks(ctx, width, height, layout, qtables, coefs, out, &st);
+  if (rc != RCG_OK) return rc;
+  // idct_planes multipliers from the given tables (jpeg/src/decode.rs:1316-1321)
+  fill_mult(st, qtables, st->ncomp == 1 ? 1 : 2);
+  return reconstruct_with(ctx, st, (int)width, (int)height, coefs, out, out_len);
+}
+
+int rcg_reconstruct_tables(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                           const rcg_qtables* tables, const int16_t* coefs, uint8_t* out, size_t out_len) {
+  if (!ctx) return RCG_INVALID;
+  StepDesc* st = nullptr;
+  int rc = reconstruct_checks(ctx, width, height, layout, tables, coefs, out, &st);
+  if (rc == RCG_OK) rc = requant_inputs(ctx, tables, st);
+  if (rc != RCG_OK) {
+    delete st;
+    return rc;
+  }
+  for (int c = 0; c < st->ncomp; c++)
+    for (int n = 0; n < 64; n++) st->mult[c][n] = mult_entry_host(st->src_qt[c], n);
+  return reconstruct_with(ctx, st, (int)width, (int)height, coefs, out, out_len);
 }
 
 // ---- search
@@ -733,6 +803,162 @@ int rcg_search_batch(rcg_ctx* ctx, int n, const uint8_t* const* srcs, const uint
     if (status[i] != RCG_OK) return fail(ctx, status[i], "image " + std::to_string(i) + ": " + messages[i]);
   ctx->last_error.clear();
   return RCG_OK;
+}
+
+int rcg_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                   const rcg_qtables* in, const int16_t* coefs_in, int quality, int trellis, int16_t* coefs_out,
+                   size_t coefs_len, rcg_qtables* out) {
+  if (!ctx) return RCG_INVALID;
+  if (!layout || !coefs_in || !coefs_out) return fail(ctx, RCG_INVALID, "null pointer");
+  if (width == 0 || height == 0) return fail(ctx, RCG_INVALID, "empty image");
+  if (layout->ncomp != 1 && layout->ncomp != 3)
+    return fail(ctx, RCG_UNSUPPORTED, "requantization takes 1 or 3 components");
+  if (quality < 1 || quality > 100) return fail(ctx, RCG_INVALID, "quality must be 1..=100");
+  StepDesc* st = new StepDesc;
+  int rc = layout_step(ctx, st, (int)width, (int)height, layout);
+  if (rc == RCG_OK) rc = requant_inputs(ctx, in, st);
+  if (rc == RCG_OK && (long long)coefs_len < st->nblocks * 64) rc = fail(ctx, RCG_INVALID, "coefficient buffer too short");
+  if (rc != RCG_OK) {
+    delete st;
+    return rc;
+  }
+  cudaSetDevice(ctx->device);
+  const size_t cbytes = (size_t)st->nblocks * 64 * 2;
+  int16_t* d_src = (int16_t*)workspace(ctx, "rq_src", cbytes);
+  int16_t* d_out = (int16_t*)workspace(ctx, "coefs_single", cbytes);
+  StepDesc* d_st = (StepDesc*)workspace(ctx, "step_single", sizeof(StepDesc));
+  if (!d_src || !d_out || !d_st) {
+    delete st;
+    return RCG_NO_MEMORY;
+  }
+  int tq[3];
+  uint8_t slot_qt[4][64];
+  int present[4];
+  host_requant_tables(st, quality, trellis, tq, slot_qt, present);
+  st->coef_src = d_src;
+  st->coefs = d_out;
+  copy_to_device(ctx, d_src, coefs_in, cbytes);
+  cudaMemcpyAsync(d_st, st, sizeof(StepDesc), cudaMemcpyHostToDevice, ctx->stream);
+  const float* no_caches[9] = {nullptr};
+  requantize_plain(ctx, d_st, st->nblocks);
+  rate_tables(ctx, d_st);
+  rcg::trellis(ctx, d_st, no_caches, st->nblocks);
+  rc = copy_to_host(ctx, coefs_out, d_out, cbytes);
+  cudaStreamSynchronize(ctx->stream);
+  qtables_out(tq, slot_qt, present, st->ncomp, out);
+  delete st;
+  if (rc != RCG_OK) return rc;
+  return finish(ctx, "requantize");
+}
+
+int rcg_search_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                          const rcg_qtables* in, const int16_t* coefs_in, double target, int max_quality,
+                          int trellis, rcg_found* found, int16_t* coefs_out, size_t coefs_len, rcg_qtables* out) {
+  if (!ctx) return RCG_INVALID;
+  if (!layout || !coefs_in || !found) return fail(ctx, RCG_INVALID, "null pointer");
+  if (width < (uint32_t)kMinSide || height < (uint32_t)kMinSide)
+    return fail(ctx, RCG_UNSUPPORTED, "--target-ssimulacra2 needs an image of at least 8x8 pixels");
+  if (layout->ncomp != 1 && layout->ncomp != 3)
+    return fail(ctx, RCG_UNSUPPORTED, "requantization takes 1 or 3 components");
+  if (!(target == target)) return fail(ctx, RCG_INVALID, "target is NaN");
+  const int w = (int)width, h = (int)height;
+  const int max_q = std::max(1, std::min(max_quality, 100));
+  StepDesc* st = new StepDesc;
+  int rc = layout_step(ctx, st, w, h, layout);
+  if (rc == RCG_OK) rc = requant_inputs(ctx, in, st);
+  if (rc != RCG_OK) {
+    delete st;
+    return rc;
+  }
+  cudaSetDevice(ctx->device);
+  const long long nblocks = st->nblocks;
+  const size_t cbytes = (size_t)nblocks * 64 * 2;
+  int max_steps = 1;
+  for (int span = max_q; span > 1; span = (span + 1) / 2) max_steps++;
+  max_steps = std::min(max_steps, kMaxSteps);
+  PyramidDesc pd = make_pyramid(w, h);
+  int16_t* d_src = (int16_t*)workspace(ctx, "rq_src", cbytes);
+  int16_t* slots = (int16_t*)workspace(ctx, "coef_slots", cbytes * max_steps);
+  uint8_t* planes = (uint8_t*)workspace(ctx, "dec_planes", (size_t)plane_bytes(st));
+  float* ref_pyr = (float*)workspace(ctx, "ref_pyr", (size_t)pd.floats * sizeof(float));
+  float* dist_pyr = (float*)workspace(ctx, "dist_pyr", (size_t)pd.floats * sizeof(float));
+  double* d_score = (double*)workspace(ctx, "score", sizeof(double));
+  SearchState* d_ss = (SearchState*)workspace(ctx, "search_state", sizeof(SearchState));
+  StepDesc* d_st = (StepDesc*)workspace(ctx, "step_search", sizeof(StepDesc));
+  if (!d_src || !slots || !planes || !ref_pyr || !dist_pyr || !d_score || !d_ss || !d_st) {
+    delete st;
+    return RCG_NO_MEMORY;
+  }
+  if ((rc = copy_to_device(ctx, d_src, coefs_in, cbytes)) != RCG_OK) {
+    delete st;
+    return rc;
+  }
+  // The reference image: the source reconstructed with its own tables (cli/src/pipeline.rs:372).
+  for (int c = 0; c < st->ncomp; c++)
+    for (int n = 0; n < 64; n++) st->mult[c][n] = mult_entry_host(st->src_qt[c], n);
+  st->coef_src = d_src;
+  st->coefs = d_src;
+  st->requant = 1;
+  cudaMemcpyAsync(d_st, st, sizeof(StepDesc), cudaMemcpyHostToDevice, ctx->stream);
+  dequant_idct(ctx, d_st, d_src, planes, nblocks);
+  upsample_color(ctx, d_st, planes, w, h, nullptr, ref_pyr);
+  build_pyramid(ctx, pd, ref_pyr);
+  SearchState hs;
+  std::memset(&hs, 0, sizeof hs);
+  hs.lo = 1;
+  hs.hi = max_q;
+  hs.qs[0] = max_q;
+  hs.target = target;
+  hs.max_q = max_q;
+  hs.trellis = trellis;
+  hs.channels = st->ncomp;
+  hs.best_q = max_q;
+  cudaMemcpyAsync(d_ss, &hs, sizeof hs, cudaMemcpyHostToDevice, ctx->stream);
+  const float* no_caches[9] = {nullptr};
+  for (int s = 0; s < max_steps; s++) {
+    step_tables_requant(ctx, d_ss, d_st, slots, nblocks * 64);
+    requantize_plain(ctx, d_st, nblocks);
+    rate_tables(ctx, d_st);
+    rcg::trellis(ctx, d_st, no_caches, nblocks);
+    dequant_idct(ctx, d_st, nullptr, planes, nblocks);
+    upsample_color(ctx, d_st, planes, w, h, nullptr, dist_pyr);
+    build_pyramid_gated(ctx, pd, dist_pyr, d_st);
+    score_pyramids(ctx, pd, ref_pyr, dist_pyr, d_score, d_ss, d_st);
+  }
+  cudaMemcpyAsync(&hs, d_ss, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream);
+  if ((rc = finish(ctx, "search_requantize")) != RCG_OK) {
+    delete st;
+    return rc;
+  }
+  if (!hs.done) {
+    delete st;
+    return fail(ctx, RCG_TIMEOUT, "bisection did not finish within the step budget");
+  }
+  found->quality = hs.best_q;
+  found->score = hs.best_score;
+  found->nsteps = 0;
+  for (int s = 0; s < kMaxSteps && s <= hs.step; s++) {
+    found->trace_q[s] = hs.qs[s];
+    found->trace_score[s] = hs.scores[s];
+    found->nsteps = s + 1;
+  }
+  if (coefs_out) {
+    if (coefs_len < (size_t)nblocks * 64) {
+      delete st;
+      return fail(ctx, RCG_INVALID, "coefficient buffer too short");
+    }
+    if ((rc = copy_to_host(ctx, coefs_out, slots + (size_t)hs.best_step * nblocks * 64, cbytes)) != RCG_OK) {
+      delete st;
+      return rc;
+    }
+  }
+  int tq[3];
+  uint8_t slot_qt[4][64];
+  int present[4];
+  host_requant_tables(st, hs.best_q, trellis, tq, slot_qt, present);
+  qtables_out(tq, slot_qt, present, st->ncomp, out);
+  delete st;
+  return finish(ctx, "search_requantize output");
 }
 
 }  // extern "C"

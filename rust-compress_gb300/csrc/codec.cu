@@ -165,31 +165,34 @@ __host__ __device__ inline void fill_layout(StepDesc* st, int quality, int subsa
 inline void fill_step(StepDesc* st, int quality, int subsampling, int channels, int trellis, int w, int h) {
   const float kappa = 0.02f;  // TRELLIS_KAPPA, jpeg/src/encode.rs:42
   fill_layout(st, quality, subsampling, channels, trellis, w, h);
-  for (int cls = 0; cls < 2; cls++) {
-    uint8_t* qt = st->qt[cls];
+  // luma_table == chroma_table (jpeg/src/quality.rs:37-43): every component gets the same entries
+  for (int c = 0; c < 3; c++) {
+    uint8_t* qt = st->qt[c];
     for (int n = 0; n < 64; n++) qt[n] = qtable_entry(quality, n);
-    for (int k = 0; k < 64; k++) st->divz[cls][k] = divz_entry(qt, k);
-    for (int n = 0; n < 64; n++) st->mult[cls][n] = mult_entry(qt, n);
+    for (int k = 0; k < 64; k++) st->divz[c][k] = divz_entry(qt, k);
+    for (int n = 0; n < 64; n++) st->mult[c][n] = mult_entry(qt, n);
     // Rdo::new: q per zigzag position, median of q[1..] (sorted, index 31), w = (median/q)^1, lambda.
     float sorted[63];
-    for (int k = 0; k < 64; k++) st->rq[cls][k] = (float)qt[zigzag(k)];
-    for (int k = 1; k < 64; k++) sorted[k - 1] = st->rq[cls][k];
+    for (int k = 0; k < 64; k++) st->rq[c][k] = (float)qt[zigzag(k)];
+    for (int k = 1; k < 64; k++) sorted[k - 1] = st->rq[c][k];
     std::sort(sorted, sorted + 63);
     float median = sorted[31];
-    st->rw[cls][0] = 1.0f;
+    st->rw[c][0] = 1.0f;
     // FREQ_WEIGHT_GAMMA is 1.0 (jpeg/src/rdo.rs:12) and pow(x, 1) == x, so w = median / q exactly.
-    for (int k = 1; k < 64; k++) st->rw[cls][k] = fdiv(median, st->rq[cls][k]);
-    st->lambda[cls] = fmul(fmul(kappa, median), median);
+    for (int k = 1; k < 64; k++) st->rw[c][k] = fdiv(median, st->rq[c][k]);
+    st->lambda[c] = fmul(fmul(kappa, median), median);
   }
 }
 
 void fill_mult(StepDesc* st, const uint8_t* qtables, int ntables) {
-  for (int cls = 0; cls < 2; cls++) {
-    const uint8_t* qt = qtables + 64 * (cls < ntables ? cls : 0);
-    std::memcpy(st->qt[cls], qt, 64);
-    for (int n = 0; n < 64; n++) st->mult[cls][n] = mult_entry(qt, n);
+  for (int c = 0; c < 3; c++) {
+    const uint8_t* qt = qtables + 64 * (c == 0 || ntables < 2 ? 0 : 1);
+    std::memcpy(st->qt[c], qt, 64);
+    for (int n = 0; n < 64; n++) st->mult[c][n] = mult_entry(qt, n);
   }
 }
+
+float mult_entry_host(const uint8_t* q, int n) { return mult_entry(q, n); }
 
 void qtables_for(int quality, uint8_t* out128) {
   for (int n = 0; n < 64; n++) out128[n] = out128[64 + n] = qtable_entry(quality, n);
@@ -362,7 +365,7 @@ __global__ void __launch_bounds__(128) k_quantize(StepDesc* __restrict__ st, Cac
     const CompDesc& cd = st->comp[c];
     const long long nb = (long long)cd.bw * cd.bh;
     const float* cache = cs.p[cd.cache] + (gb - cd.blk0);
-    const float* divz = st->divz[cd.cls];
+    const float* divz = st->divz[c];
     // All 64 loads are issued before any is used (fully unrolled into registers).
     int v[64];
 #pragma unroll
@@ -434,7 +437,9 @@ __global__ void __launch_bounds__(288) k_rate_tables(StepDesc* __restrict__ st) 
   __shared__ float len[256];
   __shared__ int n_used;
   if (!st->active || !st->use_trellis) return;
-  const int cls = blockIdx.x;
+  const int comp = blockIdx.x;  // the rate model is per class, lambda per component
+  if (comp >= st->ncomp) return;
+  const int cls = comp < 1 ? comp : 1;
   const int t = threadIdx.x;
   if (t < NS) {
     freq[t] = t < 256 ? st->hist[cls][t] : 1u;
@@ -506,18 +511,18 @@ __global__ void __launch_bounds__(288) k_rate_tables(StepDesc* __restrict__ st) 
     len[t] = size == 0 ? 18.0f : (float)size;
   }
   __syncthreads();
-  const float lambda = st->lambda[cls];
+  const float lambda = st->lambda[comp];
   // rate(run, v) = zrl * len[0xF0] + len[((run % 16) << 4) | size] + size, for size = bit length of v.
   for (int i = t; i < 64 * 16; i += blockDim.x) {
     int run = i / 16, size = i % 16;
     float rate = fadd(fadd(fmul((float)(run / 16), len[0xF0]), len[((run % 16) << 4) | size]), (float)size);
-    st->lr[cls][i] = fmul(lambda, rate);
+    st->lr[comp][i] = fmul(lambda, rate);
   }
-  if (t == 0) st->eob[cls] = fmul(lambda, len[0]);
+  if (t == 0) st->eob[comp] = fmul(lambda, len[0]);
 }
 
 int rate_tables(rcg_ctx* ctx, StepDesc* d_step) {
-  RCG_LAUNCH(ctx, "rate_tables", k_rate_tables, 2, 288, 0, d_step);
+  RCG_LAUNCH(ctx, "rate_tables", k_rate_tables, 3, 288, 0, d_step);
   return RCG_OK;
 }
 
@@ -529,21 +534,24 @@ int rate_tables(rcg_ctx* ctx, StepDesc* d_step) {
 // skips nodes at the same position, :86-88). zd[i-1] is carried as a running sum, and each node keeps zd at its
 // own position, so no 64-entry zd table is needed.
 __global__ void __launch_bounds__(128) k_trellis(StepDesc* __restrict__ st, CacheSet cs) {
-  __shared__ float lr[2][64 * 16];
+  __shared__ float lr[3][64 * 16];
   if (!st->active || !st->use_trellis) return;
-  for (int i = threadIdx.x; i < 2 * 64 * 16; i += blockDim.x) (&lr[0][0])[i] = (&st->lr[0][0])[i];
+  for (int i = threadIdx.x; i < 3 * 64 * 16; i += blockDim.x) (&lr[0][0])[i] = (&st->lr[0][0])[i];
   __syncthreads();
   const long long gb = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (gb >= st->nblocks) return;
   const int c = comp_of(st, gb);
   const CompDesc& cd = st->comp[c];
-  const int cls = cd.cls;
   const long long nb = (long long)cd.bw * cd.bh;
-  const float* cache = cs.p[cd.cache] + (gb - cd.blk0);
-  const float* divz = st->divz[cls];
-  const float* rq = st->rq[cls];
-  const float* rw = st->rw[cls];
-  const float* lrc = lr[cls];
+  // Encoding: a[k] = flat[ZZ_T[k]] * div[ZZ_T[k]] from the FDCT cache (jpeg/src/encode.rs:207-211).
+  // Requantization: a[k] = source[k] * ratio[k] (jpeg/src/encode.rs:162-166); the DC stays the plain value.
+  const bool requant = st->requant != 0;
+  const float* cache = requant ? nullptr : cs.p[cd.cache] + (gb - cd.blk0);
+  const int16_t* src = requant ? st->coef_src + gb * 64 : nullptr;
+  const float* scale = requant ? st->ratio[c] : st->divz[c];
+  const float* rq = st->rq[c];
+  const float* rw = st->rw[c];
+  const float* lrc = lr[c];
 
   float ncost[128], nzd[128];
   unsigned char npos[128];
@@ -556,20 +564,22 @@ __global__ void __launch_bounds__(128) k_trellis(StepDesc* __restrict__ st, Cach
 
   // The coefficients arrive 16 at a time: the next chunk's loads are in flight while this chunk's DP steps run.
   constexpr int kChunk = 16;
+  auto load = [&](int k) -> float {
+    return requant ? (float)__ldg(src + k) : __ldg(cache + (long long)k * nb);
+  };
   float cur[kChunk], nxt[kChunk];
 #pragma unroll
-  for (int j = 0; j < kChunk; j++) cur[j] = __ldg(cache + (long long)j * nb);
+  for (int j = 0; j < kChunk; j++) cur[j] = load(j);
 #pragma unroll 1
   for (int c0 = 0; c0 < 64; c0 += kChunk) {
     if (c0 + kChunk < 64) {
 #pragma unroll
-      for (int j = 0; j < kChunk; j++) nxt[j] = __ldg(cache + (long long)(c0 + kChunk + j) * nb);
+      for (int j = 0; j < kChunk; j++) nxt[j] = load(c0 + kChunk + j);
     }
 #pragma unroll
     for (int j = 0; j < kChunk; j++) {
       const int i = c0 + j;
-      // a[k] = flat[ZZ_T[k]] * div[ZZ_T[k]] (jpeg/src/encode.rs:207-211)
-      float a = fmul(cur[j], divz[i]);
+      float a = fmul(cur[j], scale[i]);
       if (i == 0) {
         dc = clampi(round_f32(a), -2047, 2047);
         continue;
@@ -631,7 +641,7 @@ __global__ void __launch_bounds__(128) k_trellis(StepDesc* __restrict__ st, Cach
     for (int j = 0; j < kChunk; j++) cur[j] = nxt[j];
   }
   // End of block (jpeg/src/rdo.rs:98-108): zprev is zd[63].
-  const float eob = st->eob[cls];
+  const float eob = st->eob[c];
   float best_cost = fadd(zprev, eob);
   int best_end = -1;
   for (int ni = 0; ni < nn; ni++) {
@@ -644,7 +654,9 @@ __global__ void __launch_bounds__(128) k_trellis(StepDesc* __restrict__ st, Cach
   int16_t* out = st->coefs + gb * 64;
   int4 z = make_int4(0, 0, 0, 0);
   int4 first = z;
-  first.x = dc & 0xFFFF;
+  // quantize_ac clears positions 1..63 (jpeg/src/rdo.rs:109-111); the DC is the rounded a[0] when encoding and the
+  // plain requantized value (already in place) when requantizing.
+  first.x = requant ? (reinterpret_cast<const int4*>(out)[0].x & 0xFFFF) : (dc & 0xFFFF);
   reinterpret_cast<int4*>(out)[0] = first;
 #pragma unroll
   for (int g = 1; g < 8; g++) reinterpret_cast<int4*>(out)[g] = z;
@@ -708,7 +720,7 @@ __global__ void __launch_bounds__(128) k_dequant_idct(const StepDesc* __restrict
   const CompDesc& cd = st->comp[c];
   long long lb = gb - cd.blk0;
   int by = (int)(lb / cd.bw), bx = (int)(lb % cd.bw);
-  const float* mult = st->mult[cd.cls];
+  const float* mult = st->mult[c];
   float blk[64];
   const int16_t* base = coefs ? coefs : st->coefs;
   const int4* src = reinterpret_cast<const int4*>(base + gb * 64);
@@ -895,10 +907,10 @@ int upsample_color(rcg_ctx* ctx, StepDesc* d_step, const uint8_t* d_planes, int 
 
 // ------------------------------------------------------------------------------------------------ step tables
 
-// First kernel of every search step: the bisection state names the quality; fill the candidate's tables. 128
-// threads: one per (class, coefficient) entry; the Rdo median is the element of rank 31 among q[1..63] (ties broken
-// by index, which leaves the value unchanged), the same value the reference's sort yields.
-__global__ void __launch_bounds__(128) k_step_tables(const SearchState* __restrict__ ss, StepDesc* __restrict__ st,
+// First kernel of every search step: the bisection state names the quality; fill the candidate's tables. 192
+// threads: one per (component, coefficient) entry; the Rdo median is the element of rank 31 among q[1..63] (ties
+// broken by index, which leaves the value unchanged), the same value the reference's sort yields.
+__global__ void __launch_bounds__(192) k_step_tables(const SearchState* __restrict__ ss, StepDesc* __restrict__ st,
                                                      int w, int h, int16_t* slots, long long slot_stride) {
   __shared__ uint8_t qt[64];
   __shared__ float rq[64];
@@ -912,42 +924,238 @@ __global__ void __launch_bounds__(128) k_step_tables(const SearchState* __restri
   const int q = ss->qs[step];
   if (t == 0) {
     st->active = 1;
+    st->requant = 0;
     fill_layout(st, q, ss->subsampling, ss->channels, ss->trellis, w, h);
     st->coefs = slots + (long long)step * slot_stride;
   }
-  if (t < 64) {
-    qt[t] = qtable_entry(q, t);
-  }
+  if (t < 64) qt[t] = qtable_entry(q, t);
   __syncthreads();
-  // luma_table == chroma_table (jpeg/src/quality.rs:37-43): both classes get the same entries
-  const int cls = t / 64, k = t % 64;
-  st->qt[cls][k] = qt[k];
-  st->divz[cls][k] = divz_entry(qt, k);
-  st->mult[cls][k] = mult_entry(qt, k);
+  // luma_table == chroma_table (jpeg/src/quality.rs:37-43): every component gets the same entries
+  const int c = t / 64, k = t % 64;
+  st->qt[c][k] = qt[k];
+  st->divz[c][k] = divz_entry(qt, k);
+  st->mult[c][k] = mult_entry(qt, k);
   float rk = (float)qt[zigzag(k)];
-  st->rq[cls][k] = rk;
-  if (cls == 0) rq[k] = rk;
+  st->rq[c][k] = rk;
+  if (c == 0) rq[k] = rk;
   for (int i = t; i < 512; i += blockDim.x) (&st->hist[0][0])[i] = 0;
   __syncthreads();
-  if (cls == 0 && k >= 1) {
+  if (c == 0 && k >= 1) {
     int rank = 0;
     for (int j = 1; j < 64; j++) rank += (rq[j] < rk || (rq[j] == rk && j < k)) ? 1 : 0;
     if (rank == 31) median = rk;
   }
   __syncthreads();
-  st->rw[cls][k] = k == 0 ? 1.0f : fdiv(median, rk);
-  if (k == 0) st->lambda[cls] = fmul(fmul(0.02f, median), median);  // TRELLIS_KAPPA (jpeg/src/encode.rs:42)
+  st->rw[c][k] = k == 0 ? 1.0f : fdiv(median, rk);
+  if (k == 0) st->lambda[c] = fmul(fmul(0.02f, median), median);  // TRELLIS_KAPPA (jpeg/src/encode.rs:42)
 }
 
 int step_tables(rcg_ctx* ctx, SearchState* d_search, StepDesc* d_step, int w, int h, int16_t* d_coef_slots,
                 long long slot_stride) {
-  RCG_LAUNCH(ctx, "step_tables", k_step_tables, 1, 128, 0, d_search, d_step, w, h, d_coef_slots, slot_stride);
+  RCG_LAUNCH(ctx, "step_tables", k_step_tables, 1, 192, 0, d_search, d_step, w, h, d_coef_slots, slot_stride);
   return RCG_OK;
 }
 
 int codec_upload_lut(const float* lut8) {
   cudaError_t e = cudaMemcpyToSymbol(c_lut8, lut8, 256 * sizeof(float));
   return e == cudaSuccess ? 0 : (int)e;
+}
+
+// ------------------------------------------------------------------------------------------------ requantization
+
+// Table of one component for a requantization to `quality` (jpeg/src/encode.rs:121-126): the quality's table,
+// never finer than the source's.
+__host__ __device__ inline uint8_t requant_entry(const uint8_t* old, int quality, int n) {
+  uint8_t t = qtable_entry(quality, n);
+  return t > old[n] ? t : old[n];
+}
+
+// Slot assignment of jpeg/src/encode.rs:139-148: components with equal tables share a slot, a new table takes the
+// first free one. Also reports whether any table changed (:127) and the slot tables.
+__host__ __device__ inline int requant_slots(const StepDesc* st, int* tq, uint8_t (*slot_qt)[64], int* present) {
+  int changed = 0;
+  for (int sl = 0; sl < 4; sl++) present[sl] = 0;
+  for (int c = 0; c < st->ncomp; c++) {
+    bool same_as_old = true;
+    for (int n = 0; n < 64; n++) same_as_old &= st->qt[c][n] == st->src_qt[c][n];
+    changed |= same_as_old ? 0 : 1;
+    int slot = -1;
+    for (int sl = 0; sl < 4 && slot < 0; sl++) {
+      if (!present[sl]) continue;
+      bool eq = true;
+      for (int n = 0; n < 64; n++) eq &= slot_qt[sl][n] == st->qt[c][n];
+      if (eq) slot = sl;
+    }
+    if (slot < 0) {
+      for (int sl = 0; sl < 4 && slot < 0; sl++)
+        if (!present[sl]) slot = sl;
+      for (int n = 0; n < 64; n++) slot_qt[slot][n] = st->qt[c][n];
+      present[slot] = 1;
+    }
+    tq[c] = slot;
+  }
+  return changed;
+}
+
+void host_requant_tables(StepDesc* st, int quality, int trellis, int tq_out[3], uint8_t slot_qt_out[4][64],
+                         int present_out[4]) {
+  const float kappa = 0.02f;  // TRELLIS_KAPPA, jpeg/src/encode.rs:42
+  st->quality = quality;
+  st->requant = 1;
+  for (int c = 0; c < st->ncomp; c++) {
+    uint8_t* nt = st->qt[c];
+    for (int n = 0; n < 64; n++) nt[n] = requant_entry(st->src_qt[c], quality, n);
+    for (int k = 0; k < 64; k++) {
+      int n = zigzag(k);
+      st->ratio[c][k] = fdiv((float)st->src_qt[c][n], (float)nt[n]);
+      st->rq[c][k] = (float)nt[n];
+    }
+    for (int n = 0; n < 64; n++) st->mult[c][n] = mult_entry(nt, n);
+    float sorted[63];
+    for (int k = 1; k < 64; k++) sorted[k - 1] = st->rq[c][k];
+    std::sort(sorted, sorted + 63);
+    float median = sorted[31];
+    st->rw[c][0] = 1.0f;
+    for (int k = 1; k < 64; k++) st->rw[c][k] = fdiv(median, st->rq[c][k]);
+    st->lambda[c] = fmul(fmul(kappa, median), median);
+  }
+  st->changed = requant_slots(st, tq_out, slot_qt_out, present_out);
+  st->use_trellis = (trellis && st->changed) ? 1 : 0;
+  std::memset(st->hist, 0, sizeof st->hist);
+}
+
+// Search step of the JPEG->JPEG search: the same tables as host_requant_tables, 192 threads (component,
+// coefficient); each component's Rdo median is the element of rank 31 among its q[1..63].
+__global__ void __launch_bounds__(192) k_step_tables_rq(const SearchState* __restrict__ ss, StepDesc* __restrict__ st,
+                                                        int16_t* slots, long long slot_stride) {
+  __shared__ float rq[3][64];
+  __shared__ float median[3];
+  const int t = threadIdx.x;
+  if (ss->done) {
+    if (t == 0) st->active = 0;
+    return;
+  }
+  const int step = ss->step;
+  const int q = ss->qs[step];
+  const int c = t / 64, k = t % 64;
+  const bool live = c < st->ncomp;
+  if (live) {
+    int n = zigzag(k);
+    uint8_t nn = requant_entry(st->src_qt[c], q, n);
+    st->qt[c][n] = nn;
+    st->ratio[c][k] = fdiv((float)st->src_qt[c][n], (float)nn);
+    st->rq[c][k] = (float)nn;
+    rq[c][k] = (float)nn;
+  }
+  for (int i = t; i < 512; i += blockDim.x) (&st->hist[0][0])[i] = 0;
+  __syncthreads();
+  if (live) {
+    st->mult[c][k] = mult_entry(st->qt[c], k);
+    if (k >= 1) {
+      float rk = rq[c][k];
+      int rank = 0;
+      for (int j = 1; j < 64; j++) rank += (rq[c][j] < rk || (rq[c][j] == rk && j < k)) ? 1 : 0;
+      if (rank == 31) median[c] = rk;
+    }
+  }
+  __syncthreads();
+  if (live) {
+    st->rw[c][k] = k == 0 ? 1.0f : fdiv(median[c], rq[c][k]);
+    if (k == 0) st->lambda[c] = fmul(fmul(0.02f, median[c]), median[c]);
+  }
+  if (t == 0) {
+    int tq[3];
+    uint8_t slot_qt[4][64];
+    int present[4];
+    st->active = 1;
+    st->requant = 1;
+    st->quality = q;
+    st->changed = requant_slots(st, tq, slot_qt, present);
+    st->use_trellis = (ss->trellis && st->changed) ? 1 : 0;
+    st->coefs = slots + (long long)step * slot_stride;
+  }
+}
+
+int step_tables_requant(rcg_ctx* ctx, SearchState* d_search, StepDesc* d_step, int16_t* d_coef_slots,
+                        long long slot_stride) {
+  RCG_LAUNCH(ctx, "step_tables", k_step_tables_rq, 1, 192, 0, d_search, d_step, d_coef_slots, slot_stride);
+  return RCG_OK;
+}
+
+// Plain requantization (jpeg/src/encode.rs:132-138): round_f32(coef * old/new) clamped to +-2047, every position.
+// When the trellis pass follows, also the AC symbol histogram of the result over the blocks of the MCU grid
+// (ac_code_lengths, :155 -> :223-227, :376-398).
+__global__ void __launch_bounds__(128) k_requant_plain(StepDesc* __restrict__ st) {
+  __shared__ unsigned int sh[2][256];
+  if (!st->active) return;
+  const bool hist = st->use_trellis != 0;
+  if (hist) {
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) (&sh[0][0])[i] = 0;
+    __syncthreads();
+  }
+  const long long gb = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gb < st->nblocks) {
+    const int c = comp_of(st, gb);
+    const CompDesc& cd = st->comp[c];
+    const float* ratio = st->ratio[c];
+    const int4* src = reinterpret_cast<const int4*>(st->coef_src + gb * 64);
+    int v[64];
+#pragma unroll
+    for (int g = 0; g < 8; g++) {
+      int4 pk = __ldg(src + g);
+      int w4[4] = {pk.x, pk.y, pk.z, pk.w};
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        int k = g * 8 + j;
+        int x = (int)(short)((w4[j >> 1] >> (16 * (j & 1))) & 0xFFFF);
+        v[k] = clampi(round_f32(fmul((float)x, ratio[k])), -2047, 2047);
+      }
+    }
+    int16_t* out = st->coefs + gb * 64;
+#pragma unroll
+    for (int g = 0; g < 8; g++) {
+      int4 pk;
+      pk.x = (v[g * 8 + 0] & 0xFFFF) | (v[g * 8 + 1] << 16);
+      pk.y = (v[g * 8 + 2] & 0xFFFF) | (v[g * 8 + 3] << 16);
+      pk.z = (v[g * 8 + 4] & 0xFFFF) | (v[g * 8 + 5] << 16);
+      pk.w = (v[g * 8 + 6] & 0xFFFF) | (v[g * 8 + 7] << 16);
+      reinterpret_cast<int4*>(out)[g] = pk;
+    }
+    const long long lb = gb - cd.blk0;
+    const int by = (int)(lb / cd.bw), bx = (int)(lb % cd.bw);
+    if (hist && bx < st->mcus_x * cd.h && by < st->mcus_y * cd.v) {
+      unsigned* hs = sh[cd.cls];
+      unsigned run = 0;
+#pragma unroll
+      for (int k = 1; k < 64; k++) {
+        if (v[k] == 0) {
+          run++;
+          continue;
+        }
+        while (run >= 16) {
+          atomicAdd(&hs[0xF0], 1u);
+          run -= 16;
+        }
+        unsigned size = (unsigned)bitlen((unsigned)abs(v[k]));
+        atomicAdd(&hs[(run << 4) | size], 1u);
+        run = 0;
+      }
+      if (run > 0) atomicAdd(&hs[0], 1u);
+    }
+  }
+  if (hist) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) {
+      unsigned x = (&sh[0][0])[i];
+      if (x) atomicAdd(&(&st->hist[0][0])[i], x);
+    }
+  }
+}
+
+int requantize_plain(rcg_ctx* ctx, StepDesc* d_step, long long max_blocks) {
+  int grid = (int)((max_blocks + 127) / 128);
+  RCG_LAUNCH(ctx, "requant_plain", k_requant_plain, grid, 128, 0, d_step);
+  return RCG_OK;
 }
 
 }  // namespace rcg

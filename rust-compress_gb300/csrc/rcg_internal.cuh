@@ -62,16 +62,25 @@ struct StepDesc {
   int hmax, vmax;
   long long nblocks;     // total blocks of all components
   CompDesc comp[3];
-  uint8_t qt[2][64];     // quantization tables, natural order (slot 0 luma, slot 1 chroma)
-  float divz[2][64];     // fdct divisors per zigzag position: div[ZZ_T[k]] (jpeg/src/encode.rs:174-183, :202)
-  float mult[2][64];     // dequantization multipliers, natural order (jpeg/src/decode.rs:1316-1321)
-  // Trellis (jpeg/src/rdo.rs:14-52)
-  float rq[2][64];       // step per zigzag position
-  float rw[2][64];       // distortion weight per zigzag position
-  float lambda[2];
-  float eob[2];          // lambda * len[0x00]
-  float lr[2][64 * 16];  // lambda * rate(run, v) for run 0..63, size 0..15 (index run*16 + size)
-  unsigned int hist[2][256];  // AC symbol histogram of the plain pass (jpeg/src/encode.rs:223-227)
+  // Per-component tables (index = component). The encoder gives components 1 and 2 the same chroma table
+  // (jpeg/src/quality.rs:37-43); a requantization gives each component its own (jpeg/src/encode.rs:120-126).
+  uint8_t qt[3][64];     // quantization table of each component, natural order
+  float divz[3][64];     // fdct divisors per zigzag position: div[ZZ_T[k]] (jpeg/src/encode.rs:174-183, :202)
+  float mult[3][64];     // dequantization multipliers, natural order (jpeg/src/decode.rs:1316-1321)
+  // Trellis (jpeg/src/rdo.rs:14-52), per component
+  float rq[3][64];       // step per zigzag position
+  float rw[3][64];       // distortion weight per zigzag position
+  float lambda[3];
+  float eob[3];          // lambda * len[0x00]
+  float lr[3][64 * 16];  // lambda * rate(run, v) for run 0..63, size 0..15 (index run*16 + size)
+  unsigned int hist[2][256];  // AC symbol histogram of the plain pass, per class (jpeg/src/encode.rs:223-227)
+  // Requantization of existing coefficients (jpeg/src/encode.rs:107-172)
+  int requant;           // 1: the candidate requantizes coef_src instead of quantizing the FDCT cache
+  int changed;           // some component's table changed (gates the trellis pass, encode.rs:152)
+  int mcus_x, mcus_y;    // MCU grid: the rate model counts only blocks inside it (encode.rs:376-398)
+  const int16_t* coef_src;
+  uint8_t src_qt[3][64]; // the source table of each component (old; all ones where its slot is empty)
+  float ratio[3][64];    // old / new per zigzag position
   int16_t* coefs;        // where this candidate's coefficients go
 };
 
@@ -192,6 +201,8 @@ int chroma_down(rcg_ctx* ctx, const uint8_t* d_src, int src_stride, int pw, int 
 int fdct_cache(rcg_ctx* ctx, const uint8_t* d_plane, int stride, int bw, int bh, float* d_cache);
 // Per-candidate pipeline pieces, all driven by a device StepDesc.
 int quantize(rcg_ctx* ctx, StepDesc* d_step, const float* const* d_caches, long long max_blocks);
+// Plain requantization of st->coef_src into st->coefs, with the AC histogram when the trellis pass follows.
+int requantize_plain(rcg_ctx* ctx, StepDesc* d_step, long long max_blocks);
 int rate_tables(rcg_ctx* ctx, StepDesc* d_step);
 int trellis(rcg_ctx* ctx, StepDesc* d_step, const float* const* d_caches, long long max_blocks);
 // d_coefs null: decode the candidate's own coefficients (d_step->coefs).
@@ -202,12 +213,20 @@ int upsample_color(rcg_ctx* ctx, StepDesc* d_step, const uint8_t* d_planes, int 
                    float* d_lin);
 // Host-side table setup of one quality into a host StepDesc (no device work).
 void host_step_tables(StepDesc* st, int quality, int subsampling, int channels, int trellis, int w, int h);
+// Dequantization multiplier of one entry (jpeg/src/decode.rs:1316-1321), host side.
+float mult_entry_host(const uint8_t* q, int n);
 // Dequantization multipliers from caller-given tables (ntables 1 or 2; natural order).
 void fill_mult(StepDesc* st, const uint8_t* qtables, int ntables);
 // Quantization tables of a quality, slot 0 then slot 1 (jpeg/src/quality.rs:37-43).
 void qtables_for(int quality, uint8_t* out128);
 // Copy the 8-bit sRGB table to the codec's constant memory (current device).
 int codec_upload_lut(const float* lut8);
+// Requantization tables of one quality (new tables, ratios, Rdo parameters, slot assignment) from the source
+// tables in st->src_qt, on the host (single calls) and on the device (search steps): identical bits.
+void host_requant_tables(StepDesc* st, int quality, int trellis, int tq_out[3], uint8_t slot_qt_out[4][64],
+                         int present_out[4]);
+int step_tables_requant(rcg_ctx* ctx, SearchState* d_search, StepDesc* d_step, int16_t* d_coef_slots,
+                        long long slot_stride);
 // Device-side: fill the step tables from the quality the search state holds.
 int step_tables(rcg_ctx* ctx, SearchState* d_search, StepDesc* d_step, int w, int h, int16_t* d_coef_slots,
                 long long slot_stride);

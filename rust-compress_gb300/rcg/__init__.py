@@ -78,6 +78,10 @@ class _Found(ctypes.Structure):
     ]
 
 
+class _QTables(ctypes.Structure):
+    _fields_ = [("tq", ctypes.c_int32 * 3), ("qtables", (ctypes.c_uint8 * 64) * 4), ("present", ctypes.c_int32 * 4)]
+
+
 @dataclass
 class CoefComponent:
     """jpeg::encode::CoefComponent (jpeg/src/encode.rs:56-69)."""
@@ -98,7 +102,10 @@ class CoefImage:
     width: int
     height: int
     comps: list
-    qtables: np.ndarray  # uint8 (2, 64), natural order, slot 0 luma, slot 1 chroma
+    # uint8 natural order. Encoder form: (2, 64), slot 0 luma and slot 1 chroma, `present` None. General form
+    # (requantized images, jpeg/src/encode.rs:77): (4, 64) by slot, `present` marks the slots that hold a table.
+    qtables: np.ndarray
+    present: np.ndarray = None
 
     def flat(self):
         return np.concatenate([c.coefs for c in self.comps]).astype(np.int16, copy=False)
@@ -111,6 +118,21 @@ class CoefImage:
             lay.blocks_w[i], lay.blocks_h[i] = c.blocks_w, c.blocks_h
         lay.ncoefs = sum(c.coefs.size for c in self.comps)
         return lay
+
+    def table_slots(self):
+        """The general table assignment (tq per component, four slots)."""
+        t = _QTables()
+        for i, c in enumerate(self.comps):
+            t.tq[i] = c.tq
+        q = np.asarray(self.qtables, np.uint8)
+        present = [1, 1, 0, 0] if self.present is None else [int(x) for x in self.present]
+        if self.present is None and len(self.comps) == 1:
+            present = [1, 0, 0, 0]
+        for sl in range(4):
+            t.present[sl] = present[sl]
+            if present[sl] and sl < q.shape[0]:
+                ctypes.memmove(t.qtables[sl], q[sl].ctypes.data, 64)
+        return t
 
 
 @dataclass
@@ -150,6 +172,12 @@ def _load():
                              ctypes.POINTER(_Found), P, sz, P]),
         "rcg_search_device": (i32, [P, P, u32, u32, i32, ctypes.c_double, i32, ctypes.POINTER(_Opts),
                                     ctypes.POINTER(_Found), P, sz, P]),
+        "rcg_reconstruct_tables": (i32, [P, u32, u32, ctypes.POINTER(_Layout), ctypes.POINTER(_QTables), P, P, sz]),
+        "rcg_requantize": (i32, [P, u32, u32, ctypes.POINTER(_Layout), ctypes.POINTER(_QTables), P, i32, i32, P, sz,
+                                 ctypes.POINTER(_QTables)]),
+        "rcg_search_requantize": (i32, [P, u32, u32, ctypes.POINTER(_Layout), ctypes.POINTER(_QTables), P,
+                                        ctypes.c_double, i32, i32, ctypes.POINTER(_Found), P, sz,
+                                        ctypes.POINTER(_QTables)]),
         "rcg_search_batch": (i32, [P, i32, P, P, P, P, P, i32, ctypes.POINTER(_Opts), i32, P, P, P, P]),
     }
     for name, (res, args) in sig.items():
@@ -164,7 +192,7 @@ EXPORTED = (
     "rcg_ctx_create rcg_ctx_destroy rcg_last_error rcg_ctx_set_stream rcg_ctx_stream rcg_ctx_synchronize "
     "rcg_ctx_launch_count rcg_ctx_set_profiling rcg_ctx_kernel_time rcg_coef_layout_for rcg_ssimulacra2 "
     "rcg_ssimulacra2_device rcg_ssimulacra2_device_noalloc rcg_build_coefs rcg_reconstruct rcg_search rcg_search_device "
-    "rcg_search_batch"
+    "rcg_search_batch rcg_reconstruct_tables rcg_requantize rcg_search_requantize"
 ).split()
 
 
@@ -294,12 +322,42 @@ class Context:
         """jpeg/src/decode.rs:334: the pixels a viewer would show (Gray (h, w) or Rgb (h, w, 3) uint8)."""
         lay = ci.layout()
         flat = np.ascontiguousarray(ci.flat())
-        qt = np.ascontiguousarray(ci.qtables, dtype=np.uint8)
         nc = len(ci.comps)
         out = np.zeros((ci.height, ci.width, nc), dtype=np.uint8)
-        self._check(_lib.rcg_reconstruct(self._ptr, ci.width, ci.height, ctypes.byref(lay), qt.ctypes.data,
-                                         flat.ctypes.data, out.ctypes.data, out.size))
+        if ci.present is None:
+            qt = np.ascontiguousarray(ci.qtables, dtype=np.uint8)
+            self._check(_lib.rcg_reconstruct(self._ptr, ci.width, ci.height, ctypes.byref(lay), qt.ctypes.data,
+                                             flat.ctypes.data, out.ctypes.data, out.size))
+        else:
+            t = ci.table_slots()
+            self._check(_lib.rcg_reconstruct_tables(self._ptr, ci.width, ci.height, ctypes.byref(lay),
+                                                    ctypes.byref(t), flat.ctypes.data, out.ctypes.data, out.size))
         return out[:, :, 0] if nc == 1 else out
+
+    def requantize(self, ci, quality, trellis=True):
+        """CoefImage::requantize (jpeg/src/encode.rs:111) of a copy of `ci`; returns the new CoefImage."""
+        lay = ci.layout()
+        flat = np.ascontiguousarray(ci.flat())
+        out = np.empty_like(flat)
+        t_in, t_out = ci.table_slots(), _QTables()
+        self._check(_lib.rcg_requantize(self._ptr, ci.width, ci.height, ctypes.byref(lay), ctypes.byref(t_in),
+                                        flat.ctypes.data, int(quality), 1 if trellis else 0, out.ctypes.data,
+                                        out.size, ctypes.byref(t_out)))
+        return _general_image(ci, out, t_out)
+
+    def find_quality_requantize(self, ci, target, max_quality=100, trellis=True):
+        """The JPEG -> JPEG --target-ssimulacra2 search (cli/src/pipeline.rs:369-386) over requantizations of `ci`."""
+        lay = ci.layout()
+        flat = np.ascontiguousarray(ci.flat())
+        out = np.empty_like(flat)
+        t_in, t_out = ci.table_slots(), _QTables()
+        f = _Found()
+        self._check(_lib.rcg_search_requantize(self._ptr, ci.width, ci.height, ctypes.byref(lay),
+                                               ctypes.byref(t_in), flat.ctypes.data, float(target),
+                                               int(max_quality), 1 if trellis else 0, ctypes.byref(f),
+                                               out.ctypes.data, out.size, ctypes.byref(t_out)))
+        trace = [(int(f.trace_q[i]), float(f.trace_score[i])) for i in range(f.nsteps)]
+        return Found(int(f.quality), float(f.score), _general_image(ci, out, t_out), trace)
 
     def coef_capacity(self, width, height, channels, opts):
         """int16 count that holds the search result for any quality (Auto switches layout at quality 90)."""
@@ -389,6 +447,19 @@ def _coef_image(w, h, lay, coefs, qt):
                                    coefs[off: off + n]))
         off += n
     return CoefImage(w, h, comps, qt if lay.ncomp > 1 else qt[:1].repeat(2, axis=0))
+
+
+def _general_image(src, flat, t):
+    """A CoefImage shaped like `src` holding `flat` with the table assignment `t` (general form)."""
+    comps = []
+    off = 0
+    for i, c in enumerate(src.comps):
+        n = c.coefs.size
+        comps.append(CoefComponent(c.id, c.h, c.v, int(t.tq[i]), c.blocks_w, c.blocks_h, flat[off: off + n]))
+        off += n
+    q4 = np.array([list(t.qtables[sl]) for sl in range(4)], dtype=np.uint8)
+    present = np.array([int(t.present[sl]) for sl in range(4)], dtype=np.uint8)
+    return CoefImage(src.width, src.height, comps, q4, present)
 
 
 _default = None

@@ -308,3 +308,82 @@ def test_write_best_produces_a_jpeg(oracle):
     # SOF: precision 8, height, width, 3 components with 2x2 luma sampling (jpeg/src/encode.rs:664-671)
     assert data[i + 4] == 8 and int.from_bytes(data[i + 5: i + 7], "big") == 48
     assert int.from_bytes(data[i + 7: i + 9], "big") == 64 and data[i + 9] == 3 and data[i + 11] == 0x22
+
+
+def _zigzag():
+    """Natural index of each zigzag position (JPEG scan order): anti-diagonals, alternating direction."""
+    order = []
+    for d in range(15):
+        cells = [(y, d - y) for y in range(8) if 0 <= d - y < 8]
+        order += cells if d % 2 else cells[::-1]
+    return [y * 8 + x for y, x in order]
+
+
+ZIGZAG = _zigzag()
+
+
+def _general(oracle, img, q, sub):
+    coefs, qt, lay = oracle.build_coefs(img, q, sub, True)
+    h, w = img.shape[:2]
+    return oracle.general_from_encoder(w, h, lay, qt, coefs)
+
+
+def test_oracle_requantize_plain_formula_and_monotone_tables(oracle):
+    """CoefImage::requantize without trellis (jpeg/src/encode.rs:118-138) restated in numpy: new table =
+    max(standard table, old), coefficient = round-half-even of the f32 product with old/new, clamped to +-2047."""
+    import rcg.synth as synth
+
+    img = synth.image(72, 40, 6, sensor_sigma=3.0)
+    g = _general(oracle, img, 96, 3)
+    zz = np.asarray(ZIGZAG)
+    for q in (20, 70, 100):
+        out = oracle.requantize(g, q, trellis=False)
+        off = 0
+        for c in range(3):
+            old = g.qtables4[g.tq[c]]
+            new = out.qtables4[out.tq[c]]
+            assert np.all(new >= old)
+            nb = int(g.lay["blocks_w"][c] * g.lay["blocks_h"][c])
+            blk = g.coefs[off: off + nb * 64].reshape(nb, 64).astype(np.float32)
+            ratio = old[zz].astype(np.float32) / new[zz].astype(np.float32)
+            want = np.clip(np.rint(blk * ratio[None, :]), -2047, 2047).astype(np.int16)
+            assert np.array_equal(out.coefs[off: off + nb * 64].reshape(nb, 64), want), (q, c)
+            off += nb * 64
+        if q == 100:  # never finer than the source (cli/tests/cmyk.rs:40)
+            assert np.array_equal(out.coefs, g.coefs)
+
+
+def test_oracle_requantize_trellis_keeps_dc_and_shrinks(oracle):
+    import rcg.synth as synth
+
+    img = synth.image(80, 64, 7, sensor_sigma=4.0)
+    g = _general(oracle, img, 95, 3)
+    plain = oracle.requantize(g, 50, trellis=False)
+    rdo = oracle.requantize(g, 50, trellis=True)
+    a, b = plain.coefs.reshape(-1, 64), rdo.coefs.reshape(-1, 64)
+    assert np.array_equal(a[:, 0], b[:, 0])  # quantize_ac writes positions 1..63 only (jpeg/src/rdo.rs:109)
+    assert np.abs(b[:, 1:]).sum() <= np.abs(a[:, 1:]).sum()
+    assert (b[:, 1:] != 0).sum() <= (a[:, 1:] != 0).sum()
+    # an unchanged table skips the trellis pass (jpeg/src/encode.rs:151)
+    same = oracle.requantize(g, 100, trellis=True)
+    assert np.array_equal(same.coefs, g.coefs)
+
+
+def test_oracle_search_requantize_follows_bisection(oracle):
+    import rcg.synth as synth
+
+    img = synth.image(96, 72, 8, sensor_sigma=3.0)
+    g = _general(oracle, img, 95, 3)
+    for target in (50.0, 80.0):
+        q, s, best, trace = oracle.search_requantize(g, target, 100, True)
+        assert trace[0][0] == 100
+        lo, hi, want = 1, 100, 100
+        for qq, ss in trace[1:]:
+            assert qq == lo + (hi - lo) // 2
+            if ss >= target:
+                hi, want = qq, qq
+            else:
+                lo = qq + 1
+        assert q == want and s >= target
+        ref = oracle.reconstruct_general(g)
+        assert abs(oracle.ssimulacra2(ref, oracle.reconstruct_general(best)) - s) < 1e-12
