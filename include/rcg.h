@@ -73,6 +73,27 @@ typedef struct {
   int32_t present[4];     /* nonzero where the slot holds a table (an absent source table counts as all ones) */
 } rcg_qtables;
 
+/* One progressive scan (jpeg/src/progressive.rs:14-21): components, spectral band ss..se, successive approximation
+ * ah/al. */
+typedef struct {
+  int32_t ncomps;
+  int32_t comps[4];
+  int32_t ss, se, ah, al;
+} rcg_scan;
+
+/* write_best's decision (jpeg/src/encode.rs:543-546): progressive::plan (jpeg/src/progressive.rs:335-351) and
+ * baseline_estimate (jpeg/src/encode.rs:548-565). */
+typedef struct {
+  uint64_t progressive_bytes; /* estimated size of the best script */
+  uint64_t baseline_bytes;    /* estimated size of the baseline encoding */
+  int32_t progressive;        /* 1: write the script (baseline_bytes > progressive_bytes); 0: write baseline */
+  int32_t nscans;             /* the best script, in order */
+  rcg_scan scans[16];
+  int32_t ndistinct;          /* every distinct candidate scan, in first-appearance order, with its cost */
+  rcg_scan distinct[48];
+  uint64_t distinct_bytes[48];
+} rcg_plan_result;
+
 typedef struct rcg_ctx rcg_ctx;
 
 /* Context lifetime. `device` is a CUDA device ordinal. */
@@ -148,6 +169,15 @@ int rcg_search_device(rcg_ctx* ctx, const uint8_t* d_src, uint32_t width, uint32
  * may share a slot or each have their own). */
 int rcg_reconstruct_tables(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
                            const rcg_qtables* tables, const int16_t* coefs, uint8_t* out, size_t out_len);
+
+/* Plan write_best for a CoefImage (1 or 3 components): symbol statistics of every candidate scan and of the baseline
+ * scan on the GPU, Huffman code lengths, costs and the cheapest script. The caller then writes baseline
+ * (jpeg/src/encode.rs:571) or the script (jpeg/src/progressive.rs:380) as `result.progressive` says. */
+int rcg_plan(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout, const int16_t* coefs,
+             size_t coefs_len, rcg_plan_result* result);
+/* As rcg_plan with the coefficients already on the device (16-byte aligned), e.g. a search's output. */
+int rcg_plan_device(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                    const int16_t* d_coefs, rcg_plan_result* result);
 
 /* jpeg::encode::CoefImage::requantize(quality, trellis) (jpeg/src/encode.rs:111): re-quantize existing coefficients
  * (1 or 3 components, any integral sampling layout) toward the quality's tables, never finer than the source's, with

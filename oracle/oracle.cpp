@@ -1649,7 +1649,8 @@ static uint64_t scan_cost(const CoefImage& ci, const Scan& sc) {
 }
 
 // jpeg/src/progressive.rs:335-351 (plan). min_by_key keeps the first minimum.
-static uint64_t plan(const CoefImage& ci, std::vector<Scan>& best_script) {
+static uint64_t plan(const CoefImage& ci, std::vector<Scan>& best_script, std::vector<Scan>* distinct_out = nullptr,
+                     std::vector<uint64_t>* cost_out = nullptr) {
   std::vector<std::vector<Scan>> cands = scripts((int)ci.comps.size());
   std::vector<Scan> distinct;
   std::set<Scan> seen;
@@ -1672,6 +1673,8 @@ static uint64_t plan(const CoefImage& ci, std::vector<Scan>& best_script) {
     }
   }
   best_script = cands[best_i];
+  if (distinct_out) *distinct_out = distinct;
+  if (cost_out) *cost_out = cost;
   return best_total;
 }
 
@@ -2001,6 +2004,36 @@ long orc_write_best_tq(int w, int h, int ncomp, const int* hs, const int* vs, co
   if (progressive) *progressive = base_est <= prog_est ? 0 : 1;
   if (out) std::memcpy(out, bytes.data(), std::min<size_t>(bytes.size(), (size_t)cap));
   return (long)bytes.size();
+}
+
+// write_best's plan (jpeg/src/encode.rs:543-565, jpeg/src/progressive.rs:335-351) of a flat CoefImage: estimated
+// sizes, the chosen script and every distinct candidate scan with its cost. Scans are 8 ints each: ncomps,
+// comps[4], ss, se, ah*16+al.
+int orc_plan(int w, int h, int ncomp, const int* hs, const int* vs, const int* bws, const int* bhs,
+             const int16_t* coefs, uint64_t* prog_est, uint64_t* base_est, int* nscans, int* scans, int* ndistinct,
+             int* distinct, uint64_t* costs) {
+  uint8_t ones[128];
+  std::memset(ones, 1, sizeof ones);
+  orc::CoefImage ci = orc::coef_from_flat(w, h, ncomp, hs, vs, bws, bhs, ones, coefs);
+  std::vector<orc::Scan> best, dist;
+  std::vector<uint64_t> cost;
+  *prog_est = orc::plan(ci, best, &dist, &cost);
+  *base_est = orc::baseline_estimate(ci);
+  auto put = [](const orc::Scan& sc, int* o) {
+    o[0] = (int)sc.comps.size();
+    for (int i = 0; i < 4; i++) o[1 + i] = i < (int)sc.comps.size() ? sc.comps[i] : 0;
+    o[5] = sc.ss;
+    o[6] = sc.se;
+    o[7] = (int)(sc.ah * 16 + sc.al);
+  };
+  *nscans = (int)best.size();
+  for (size_t i = 0; i < best.size(); i++) put(best[i], scans + 8 * i);
+  *ndistinct = (int)dist.size();
+  for (size_t i = 0; i < dist.size(); i++) {
+    put(dist[i], distinct + 8 * i);
+    costs[i] = cost[i];
+  }
+  return 0;
 }
 
 // write_best (jpeg/src/encode.rs:543-546) of a flat CoefImage. Returns the byte count; writes at most `cap` bytes.

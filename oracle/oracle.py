@@ -48,6 +48,8 @@ def lib():
                                             P, P, P, P, P, P, pi]
         L.orc_write_best_tq.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, P, P, ctypes.c_long, pi]
         L.orc_write_best_tq.restype = ctypes.c_long
+        pu64 = ctypes.POINTER(ctypes.c_uint64)
+        L.orc_plan.argtypes = [i32, i32, i32, P, P, P, P, P, pu64, pu64, pi, P, pi, P, P]
         L.orc_round_f32.argtypes = [ctypes.c_float]
         L.orc_round_f32.restype = ctypes.c_int32
         L.orc_fdct.argtypes = [P]
@@ -259,4 +261,26 @@ def write_best_general(g):
     out = np.zeros(size, dtype=np.uint8)
     lib().orc_write_best_tq(*g.args(), out.ctypes.data, size, ctypes.byref(prog))
     return out.tobytes(), bool(prog.value)
+
+
+def plan(w, h, lay, coefs):
+    """write_best's plan: (progressive estimate, baseline estimate, best script, [(scan, cost)] of distinct scans).
+    A scan is (comps tuple, ss, se, ah, al)."""
+    n, hs, vs, bws, bhs = _lay_arrays(lay)
+    coefs = np.ascontiguousarray(coefs, dtype=np.int16)
+    pe, be = ctypes.c_uint64(), ctypes.c_uint64()
+    ns, nd = ctypes.c_int(), ctypes.c_int()
+    scans = np.zeros(16 * 8, np.int32)
+    dist = np.zeros(48 * 8, np.int32)
+    costs = np.zeros(48, np.uint64)
+    lib().orc_plan(w, h, n, hs.ctypes.data, vs.ctypes.data, bws.ctypes.data, bhs.ctypes.data, coefs.ctypes.data,
+                   ctypes.byref(pe), ctypes.byref(be), ctypes.byref(ns), scans.ctypes.data, ctypes.byref(nd),
+                   dist.ctypes.data, costs.ctypes.data)
+
+    def scan(a):
+        return (tuple(int(x) for x in a[1: 1 + a[0]]), int(a[5]), int(a[6]), int(a[7]) >> 4, int(a[7]) & 15)
+
+    best = [scan(scans[8 * i: 8 * i + 8]) for i in range(ns.value)]
+    distinct = [(scan(dist[8 * i: 8 * i + 8]), int(costs[i])) for i in range(nd.value)]
+    return int(pe.value), int(be.value), best, distinct
 

@@ -31,6 +31,7 @@ UNITS = {
     "codec.cu": ["-fmad=false"],
     "ssim2.cu": [],
     "capi.cu": [],
+    "plan.cu": [],
 }
 
 

@@ -961,4 +961,50 @@ int rcg_search_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const r
   return finish(ctx, "search_requantize output");
 }
 
+static int plan_common(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                       const int16_t* coefs, size_t coefs_len, bool on_device, rcg_plan_result* result) {
+  if (!ctx) return RCG_INVALID;
+  if (!layout || !coefs || !result) return fail(ctx, RCG_INVALID, "null pointer");
+  if (width == 0 || height == 0 || width > 65535 || height > 65535)
+    return fail(ctx, RCG_INVALID, "JPEG dimensions must be 1..=65535");
+  if (layout->ncomp != 1 && layout->ncomp != 3)
+    return fail(ctx, RCG_UNSUPPORTED, "scan planning takes 1 or 3 components");
+  StepDesc* st = new StepDesc;
+  int rc = layout_step(ctx, st, (int)width, (int)height, layout);
+  if (rc == RCG_OK && !on_device && coefs_len < (size_t)st->nblocks * 64)
+    rc = fail(ctx, RCG_INVALID, "coefficient buffer too short");
+  if (rc != RCG_OK) {
+    delete st;
+    return rc;
+  }
+  cudaSetDevice(ctx->device);
+  const int16_t* d = coefs;
+  if (!on_device) {
+    int16_t* buf = (int16_t*)workspace(ctx, "plan_coefs", (size_t)st->nblocks * 128);
+    if (!buf) {
+      delete st;
+      return RCG_NO_MEMORY;
+    }
+    if ((rc = copy_to_device(ctx, buf, coefs, (size_t)st->nblocks * 128)) != RCG_OK) {
+      delete st;
+      return rc;
+    }
+    d = buf;
+  }
+  rc = plan_scans(ctx, st, (int)width, (int)height, d, result);
+  delete st;
+  if (rc != RCG_OK) return rc;
+  return finish(ctx, "plan");
+}
+
+int rcg_plan(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout, const int16_t* coefs,
+             size_t coefs_len, rcg_plan_result* result) {
+  return plan_common(ctx, width, height, layout, coefs, coefs_len, false, result);
+}
+
+int rcg_plan_device(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                    const int16_t* d_coefs, rcg_plan_result* result) {
+  return plan_common(ctx, width, height, layout, d_coefs, 0, true, result);
+}
+
 }  // extern "C"

@@ -19,6 +19,7 @@
 #include <cstring>
 
 #include "rcg_internal.cuh"
+#include "huffman.cuh"
 
 namespace rcg {
 
@@ -420,88 +421,21 @@ int quantize(rcg_ctx* ctx, StepDesc* d_step, const float* const* d_caches, long 
 
 // ------------------------------------------------------------------------------------------------ K4 rate model
 
-// core/src/util/huffman.rs:10-86 (build_lengths, max_len 16) over 257 symbols (the 256 AC symbols plus the dummy
-// symbol of frequency 1 that optimal_table adds, jpeg/src/encode.rs:241-244), then optimal_table's sizes
-// (jpeg/src/encode.rs:245-262), Rdo's code-length table (jpeg/src/rdo.rs:36-39) and the lambda*rate table
-// (jpeg/src/rdo.rs:47-52). One CTA per class. The sort is a parallel rank sort on the unique keys
-// (freq, reverse symbol); the two-queue merge and the depth pass are sequential, as in the reference.
+// Code lengths of the measured AC statistics (huff_lengths: build_lengths over the 256 symbols plus optimal_table's
+// dummy), then optimal_table's sizes (jpeg/src/encode.rs:245-262), Rdo's code-length table (jpeg/src/rdo.rs:36-39)
+// and the lambda*rate table (jpeg/src/rdo.rs:47-52). One CTA per component.
 __global__ void __launch_bounds__(288) k_rate_tables(StepDesc* __restrict__ st) {
-  constexpr int NS = 257;
-  __shared__ unsigned freq[NS];
-  __shared__ int order[NS];        // sorted position -> symbol
-  __shared__ unsigned long long weight[2 * NS];
-  __shared__ int parent[2 * NS];
-  __shared__ unsigned char depth[2 * NS];
-  __shared__ int count[17];
-  __shared__ unsigned char lens[NS];
+  __shared__ unsigned freq[kHuffSyms];
+  __shared__ unsigned char lens[kHuffSyms];
+  __shared__ HuffScratch scratch;
   __shared__ float len[256];
-  __shared__ int n_used;
   if (!st->active || !st->use_trellis) return;
   const int comp = blockIdx.x;  // the rate model is per class, lambda per component
   if (comp >= st->ncomp) return;
   const int cls = comp < 1 ? comp : 1;
   const int t = threadIdx.x;
-  if (t < NS) {
-    freq[t] = t < 256 ? st->hist[cls][t] : 1u;
-    lens[t] = 0;
-  }
-  if (t == 0) n_used = 0;
-  __syncthreads();
-  if (t < NS && freq[t] > 0) {
-    // rank of (freq[t], -t) among used symbols
-    unsigned f = freq[t];
-    int r = 0;
-    for (int j = 0; j < NS; j++) {
-      unsigned g = freq[j];
-      if (g > 0 && (g < f || (g == f && j > t))) r++;
-    }
-    order[r] = t;
-    atomicAdd(&n_used, 1);
-  }
-  __syncthreads();
-  const int n = n_used;
-  if (t == 0) {
-    if (n == 1) {
-      lens[order[0]] = 1;
-    } else if (n > 1) {
-      for (int i = 0; i < n; i++) weight[i] = freq[order[i]];
-      int leaf = 0, node = n, next = n;
-      while (next < 2 * n - 1) {
-        int ab[2];
-        for (int p = 0; p < 2; p++) {
-          if (leaf < n && (node >= next || weight[leaf] <= weight[node]))
-            ab[p] = leaf++;
-          else
-            ab[p] = node++;
-        }
-        weight[next] = weight[ab[0]] + weight[ab[1]];
-        parent[ab[0]] = next;
-        parent[ab[1]] = next;
-        next++;
-      }
-      depth[2 * n - 2] = 0;
-      for (int i = 2 * n - 3; i >= 0; i--) depth[i] = (unsigned char)(depth[parent[i]] + 1);
-      for (int l = 0; l <= 16; l++) count[l] = 0;
-      for (int i = 0; i < n; i++) count[min((int)depth[i], 16)] += 1;
-      unsigned long long total = 0;
-      for (int l = 1; l <= 16; l++) total += (unsigned long long)count[l] << (16 - l);
-      while (total > (1ull << 16)) {
-        count[16] -= 1;
-        for (int l = 15; l >= 1; l--) {
-          if (count[l] > 0) {
-            count[l] -= 1;
-            count[l + 1] += 2;
-            break;
-          }
-        }
-        total -= 1;
-      }
-      int idx = 0;
-      for (int l = 16; l >= 1; l--)
-        for (int c = 0; c < count[l]; c++) lens[order[idx++]] = (unsigned char)l;
-    }
-  }
-  __syncthreads();
+  if (t < kHuffSyms) freq[t] = t < 256 ? st->hist[cls][t] : 1u;
+  huff_lengths(freq, lens, scratch);
   // optimal_table sizes of the 256 real symbols; an empty table gets symbol 0 at length 1. Rdo: 0 -> 18 bits.
   if (t < 256) {
     bool any = false;

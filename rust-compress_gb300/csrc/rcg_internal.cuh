@@ -213,6 +213,10 @@ int upsample_color(rcg_ctx* ctx, StepDesc* d_step, const uint8_t* d_planes, int 
                    float* d_lin);
 // Host-side table setup of one quality into a host StepDesc (no device work).
 void host_step_tables(StepDesc* st, int quality, int subsampling, int channels, int trellis, int w, int h);
+// write_best's plan (progressive candidates + baseline estimate) of coefficients on the device; `lay` carries the
+// component layout (ncomp, hmax, vmax, comp[]).
+int plan_scans(rcg_ctx* ctx, const StepDesc* lay, int w, int h, const int16_t* d_coefs, rcg_plan_result* res);
+
 // Dequantization multiplier of one entry (jpeg/src/decode.rs:1316-1321), host side.
 float mult_entry_host(const uint8_t* q, int n);
 // Dequantization multipliers from caller-given tables (ntables 1 or 2; natural order).

@@ -82,6 +82,39 @@ class _QTables(ctypes.Structure):
     _fields_ = [("tq", ctypes.c_int32 * 3), ("qtables", (ctypes.c_uint8 * 64) * 4), ("present", ctypes.c_int32 * 4)]
 
 
+class _Scan(ctypes.Structure):
+    _fields_ = [("ncomps", ctypes.c_int32), ("comps", ctypes.c_int32 * 4), ("ss", ctypes.c_int32),
+                ("se", ctypes.c_int32), ("ah", ctypes.c_int32), ("al", ctypes.c_int32)]
+
+
+class _PlanResult(ctypes.Structure):
+    _fields_ = [("progressive_bytes", ctypes.c_uint64), ("baseline_bytes", ctypes.c_uint64),
+                ("progressive", ctypes.c_int32), ("nscans", ctypes.c_int32), ("scans", _Scan * 16),
+                ("ndistinct", ctypes.c_int32), ("distinct", _Scan * 48), ("distinct_bytes", ctypes.c_uint64 * 48)]
+
+
+@dataclass
+class Plan:
+    """write_best's decision (jpeg/src/encode.rs:543-565): the estimated sizes, whether the progressive script wins,
+    the script (scans as (comps, ss, se, ah, al)) and every distinct candidate scan with its cost."""
+
+    progressive_bytes: int
+    baseline_bytes: int
+    progressive: bool
+    scans: list
+    distinct: list
+
+
+def _scan_tuple(sc):
+    return (tuple(int(sc.comps[i]) for i in range(sc.ncomps)), int(sc.ss), int(sc.se), int(sc.ah), int(sc.al))
+
+
+def _plan(r):
+    return Plan(int(r.progressive_bytes), int(r.baseline_bytes), bool(r.progressive),
+                [_scan_tuple(r.scans[i]) for i in range(r.nscans)],
+                [(_scan_tuple(r.distinct[i]), int(r.distinct_bytes[i])) for i in range(r.ndistinct)])
+
+
 @dataclass
 class CoefComponent:
     """jpeg::encode::CoefComponent (jpeg/src/encode.rs:56-69)."""
@@ -178,6 +211,8 @@ def _load():
         "rcg_search_requantize": (i32, [P, u32, u32, ctypes.POINTER(_Layout), ctypes.POINTER(_QTables), P,
                                         ctypes.c_double, i32, i32, ctypes.POINTER(_Found), P, sz,
                                         ctypes.POINTER(_QTables)]),
+        "rcg_plan": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, sz, ctypes.POINTER(_PlanResult)]),
+        "rcg_plan_device": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, ctypes.POINTER(_PlanResult)]),
         "rcg_search_batch": (i32, [P, i32, P, P, P, P, P, i32, ctypes.POINTER(_Opts), i32, P, P, P, P]),
     }
     for name, (res, args) in sig.items():
@@ -192,7 +227,7 @@ EXPORTED = (
     "rcg_ctx_create rcg_ctx_destroy rcg_last_error rcg_ctx_set_stream rcg_ctx_stream rcg_ctx_synchronize "
     "rcg_ctx_launch_count rcg_ctx_set_profiling rcg_ctx_kernel_time rcg_coef_layout_for rcg_ssimulacra2 "
     "rcg_ssimulacra2_device rcg_ssimulacra2_device_noalloc rcg_build_coefs rcg_reconstruct rcg_search rcg_search_device "
-    "rcg_search_batch rcg_reconstruct_tables rcg_requantize rcg_search_requantize"
+    "rcg_search_batch rcg_reconstruct_tables rcg_requantize rcg_search_requantize rcg_plan rcg_plan_device"
 ).split()
 
 
@@ -333,6 +368,22 @@ class Context:
             self._check(_lib.rcg_reconstruct_tables(self._ptr, ci.width, ci.height, ctypes.byref(lay),
                                                     ctypes.byref(t), flat.ctypes.data, out.ctypes.data, out.size))
         return out[:, :, 0] if nc == 1 else out
+
+    def plan(self, ci):
+        """write_best's plan of a CoefImage (jpeg/src/encode.rs:543-565): statistics, costs and choice on the GPU."""
+        lay = ci.layout()
+        flat = np.ascontiguousarray(ci.flat())
+        r = _PlanResult()
+        self._check(_lib.rcg_plan(self._ptr, ci.width, ci.height, ctypes.byref(lay), flat.ctypes.data, flat.size,
+                                  ctypes.byref(r)))
+        return _plan(r)
+
+    def plan_device(self, width, height, layout, coefs_ptr):
+        """rcg_plan_device: coefficients already on the device (layout: the _Layout of coef_layout())."""
+        r = _PlanResult()
+        self._check(_lib.rcg_plan_device(self._ptr, width, height, ctypes.byref(layout), ctypes.c_void_p(coefs_ptr),
+                                         ctypes.byref(r)))
+        return _plan(r)
 
     def requantize(self, ci, quality, trellis=True):
         """CoefImage::requantize (jpeg/src/encode.rs:111) of a copy of `ci`; returns the new CoefImage."""
