@@ -258,6 +258,44 @@ def requantize_workload(ctx, img, timed, with_oracle=True, steps=5):
     return out
 
 
+def plan_workload(ctx, timed, d_coefs, lay, with_oracle=True, steps=10):
+    """write_best's plan of the search result (device-resident coefficients of the 12 MP workload at the found
+    quality): statistics of the 48 distinct candidate scans and the baseline scan, code lengths, costs, choice.
+    CPU baseline: the oracle's plan + baseline estimate on all host threads."""
+    for _ in range(3):
+        ctx.plan_device(W, H, lay, d_coefs.data_ptr())
+    times, r = timed(lambda: ctx.plan_device(W, H, lay, d_coefs.data_ptr()), steps)
+    ms = sum(times) / len(times)
+    ctx.set_profiling(True)
+    for _ in range(3):
+        ctx.plan_device(W, H, lay, d_coefs.data_ptr())
+    kern = {}
+    for k in ("plan_blocks", "plan_chunks", "plan_prefix", "plan_eobruns", "plan_tables", "plan_choose"):
+        n, kms = ctx.kernel_time(k)
+        kern[k] = kms / 3
+    ctx.set_profiling(False)
+    out = {"workload": "write_best plan of the 12 MP search result (48 candidate scans + baseline)",
+           "ms_per_plan": ms, "kernels_ms": kern, "progressive": r.progressive,
+           "progressive_bytes": r.progressive_bytes, "baseline_bytes": r.baseline_bytes, "scans": len(r.scans)}
+    if with_oracle:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        oracle.build()
+        threads = os.cpu_count() or 1
+        oracle.set_threads(threads)
+        flat = d_coefs[: lay.ncoefs].cpu().numpy()
+        lay_o = {"ncomp": lay.ncomp, "h": list(lay.h)[: lay.ncomp], "v": list(lay.v)[: lay.ncomp],
+                 "blocks_w": list(lay.blocks_w)[: lay.ncomp], "blocks_h": list(lay.blocks_h)[: lay.ncomp]}
+        t0 = time.perf_counter()
+        pe, be, best, _ = oracle.plan(W, H, lay_o, flat)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": dt * 1000.0, "unit": "ms per plan", "cores": threads, "kind": "port",
+                               "sample": "one plan of the same coefficients",
+                               "same_choice": (pe, be) == (r.progressive_bytes, r.baseline_bytes)}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -382,6 +420,11 @@ def main():
     scorer = None
     if rank == 0 and not args.no_scorer:
         scorer = scorer_alone(ctx, stream, timed, torch, dev, peaks, with_oracle=not args.no_cpu_baseline)
+    plan = None
+    if rank == 0:
+        lay_found = ctx.coef_layout(W, H, 3, rcg.EncodeOptions(res[0], opts.subsampling, opts.trellis))
+        step_device()  # leaves the last search's chosen coefficients in d_coefs
+        plan = plan_workload(ctx, timed, d_coefs, lay_found, with_oracle=not args.no_cpu_baseline)
     requant = None
     if rank == 0 and not args.no_requant:
         requant = requantize_workload(ctx, img, timed, with_oracle=not args.no_cpu_baseline)
@@ -420,6 +463,7 @@ def main():
             "scorer_alone": scorer,
             "batch": batch,
             "requantize": requant,
+            "write_best_plan": plan,
         }
         print(json.dumps(out), flush=True)
     if dist:

@@ -73,6 +73,15 @@ typedef struct {
   int32_t present[4];     /* nonzero where the slot holds a table (an absent source table counts as all ones) */
 } rcg_qtables;
 
+/* Image metrics (cli/src/pipeline.rs:130-138). SSIMULACRA2 and SSIM are the JPEG search goals
+ * (cli/src/pipeline.rs:197-222). */
+typedef enum {
+  RCG_METRIC_SSIMULACRA2 = 0, /* core/src/ssimulacra2.rs:471 */
+  RCG_METRIC_SSIM = 1,        /* core/src/metrics.rs:13 */
+  RCG_METRIC_PSNR = 2,        /* core/src/metrics.rs:67 */
+  RCG_METRIC_MS_SSIM = 3      /* core/src/metrics.rs:111 */
+} rcg_metric;
+
 /* One progressive scan (jpeg/src/progressive.rs:14-21): components, spectral band ss..se, successive approximation
  * ah/al. */
 typedef struct {
@@ -170,6 +179,21 @@ int rcg_search_device(rcg_ctx* ctx, const uint8_t* d_src, uint32_t width, uint32
 int rcg_reconstruct_tables(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
                            const rcg_qtables* tables, const int16_t* coefs, uint8_t* out, size_t out_len);
 
+/* score(reference, candidate, metric) (cli/src/pipeline.rs:130-138) of two 8-bit interleaved images with 1..=4
+ * channels (SSIM and PSNR count every channel, alpha included; MS-SSIM uses luma), host buffers. SSIMULACRA2 here is
+ * rcg_ssimulacra2 at depth 8. PSNR of identical images is +infinity, as in the reference. */
+int rcg_metric_score(rcg_ctx* ctx, int metric, const uint8_t* reference, const uint8_t* candidate, uint32_t width,
+                     uint32_t height, int channels, double* score);
+/* As rcg_metric_score with both images on the device. */
+int rcg_metric_score_device(rcg_ctx* ctx, int metric, const uint8_t* d_reference, const uint8_t* d_candidate,
+                            uint32_t width, uint32_t height, int channels, double* score);
+
+/* The JPEG quality search for a goal metric (cli/src/pipeline.rs:207-222): RCG_METRIC_SSIMULACRA2 (as rcg_search) or
+ * RCG_METRIC_SSIM (`--target-ssim`, jpeg/src/target.rs:24; any image size). */
+int rcg_search_metric(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels, int metric,
+                      double target, int max_quality, const rcg_encode_options* opts, rcg_found* found,
+                      int16_t* coefs, size_t coefs_len, uint8_t* qtables);
+
 /* Plan write_best for a CoefImage (1 or 3 components): symbol statistics of every candidate scan and of the baseline
  * scan on the GPU, Huffman code lengths, costs and the cheapest script. The caller then writes baseline
  * (jpeg/src/encode.rs:571) or the script (jpeg/src/progressive.rs:380) as `result.progressive` says. */
@@ -187,9 +211,10 @@ int rcg_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef
                    size_t coefs_len, rcg_qtables* out);
 
 /* The JPEG -> JPEG `--target-ssimulacra2` search (cli/src/pipeline.rs:369-386): the reference image is the source
- * reconstructed, each candidate the source requantized; bisection as rcg_search, on the device. */
+ * reconstructed, each candidate the source requantized; bisection as rcg_search, on the device. `metric`:
+ * RCG_METRIC_SSIMULACRA2 or RCG_METRIC_SSIM. */
 int rcg_search_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
-                          const rcg_qtables* in, const int16_t* coefs_in, double target, int max_quality,
+                          const rcg_qtables* in, const int16_t* coefs_in, int metric, double target, int max_quality,
                           int trellis, rcg_found* found, int16_t* coefs_out, size_t coefs_len, rcg_qtables* out);
 
 /* Many independent searches at once: the images (host buffers, each with its own size, channel count and target)

@@ -1145,27 +1145,142 @@ struct Found {
   CoefImage coefs;
 };
 
-static double score_coefs(const uint8_t* ref, int w, int h, int channels, const CoefImage& ci) {
+// ------------------------------------------------------------------------------------------------ metrics
+
+static const double SSIM_C1 = 6.5025;   // (0.01 * 255)^2, core/src/metrics.rs:6
+static const double SSIM_C2 = 58.5225;  // (0.03 * 255)^2, core/src/metrics.rs:7
+
+// core/src/metrics.rs:39-62 (window_ssim): per channel f64 sums over the window, then the SSIM formula.
+static double window_ssim(const uint8_t* a, const uint8_t* b, int w, int x0, int y0, int ww, int wh, int ch) {
+  double total = 0.0;
+  for (int c = 0; c < ch; c++) {
+    double sx = 0, sy = 0, sxx = 0, syy = 0, sxy = 0;
+    for (int y = y0; y < y0 + wh; y++) {
+      size_t row = ((size_t)y * w + x0) * ch + c;
+      for (int i = 0; i < ww; i++) {
+        double p = a[row + (size_t)i * ch], q = b[row + (size_t)i * ch];
+        sx += p;
+        sy += q;
+        sxx += p * p;
+        syy += q * q;
+        sxy += p * q;
+      }
+    }
+    double n = (double)ww * (double)wh;
+    double mx = sx / n, my = sy / n;
+    double vx = sxx / n - mx * mx, vy = syy / n - my * my, cov = sxy / n - mx * my;
+    total += ((2.0 * mx * my + SSIM_C1) * (2.0 * cov + SSIM_C2)) / ((mx * mx + my * my + SSIM_C1) * (vx + vy + SSIM_C2));
+  }
+  return total / ch;
+}
+
+// core/src/metrics.rs:13-37 (ssim): 8x8 windows every 4 pixels, or one global window below 8 pixels. Each row of
+// windows is summed left to right; the rows are added in order (the reference adds them with rayon's reduce, whose
+// association is unspecified: the two agree to rounding).
+static double ssim(const uint8_t* a, const uint8_t* b, int w, int h, int ch) {
+  if (w < 8 || h < 8) return window_ssim(a, b, w, 0, 0, w, h, ch);
+  int ny = (h - 8) / 4 + 1, nx = (w - 8) / 4 + 1;
+  std::vector<double> rows(ny);
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j < ny; j++) {
+    double sum = 0.0;
+    for (int i = 0; i < nx; i++) sum += window_ssim(a, b, w, 4 * i, 4 * j, 8, 8, ch);
+    rows[j] = sum;
+  }
+  double sum = 0.0;
+  for (int j = 0; j < ny; j++) sum += rows[j];
+  return sum / (double)((size_t)ny * nx);
+}
+
+// core/src/metrics.rs:64-73 (psnr)
+static double psnr(const uint8_t* a, const uint8_t* b, size_t n) {
+  double se = 0.0;
+  for (size_t i = 0; i < n; i++) {
+    double d = (double)a[i] - (double)b[i];
+    se += d * d;
+  }
+  double mse = se / (double)std::max<size_t>(n, 1);
+  return mse == 0.0 ? INFINITY : 10.0 * std::log10(255.0 * 255.0 / mse);
+}
+
+// core/src/metrics.rs:75-87 (luma): Gray as is, GrayAlpha's gray, Rgb/Rgba -> (299R + 587G + 114B + 500) / 1000.
+static std::vector<uint8_t> luma(const uint8_t* a, size_t npx, int ch) {
+  std::vector<uint8_t> out(npx);
+  for (size_t i = 0; i < npx; i++) {
+    const uint8_t* p = a + i * ch;
+    out[i] = ch <= 2 ? p[0] : (uint8_t)((299u * p[0] + 587u * p[1] + 114u * p[2] + 500u) / 1000u);
+  }
+  return out;
+}
+
+// core/src/metrics.rs:89-106 (downsample2)
+static std::vector<uint8_t> downsample2(const std::vector<uint8_t>& img, int& w, int& h) {
+  int nw = w / 2, nh = h / 2;
+  if (nw == 0 || nh == 0) return img;
+  std::vector<uint8_t> out((size_t)nw * nh);
+  for (int y = 0; y < nh; y++)
+    for (int x = 0; x < nw; x++) {
+      unsigned s = 0;
+      for (int dy = 0; dy < 2; dy++)
+        for (int dx = 0; dx < 2; dx++) s += img[(size_t)(2 * y + dy) * w + 2 * x + dx];
+      out[(size_t)y * nw + x] = (uint8_t)(s / 4);
+    }
+  w = nw;
+  h = nh;
+  return out;
+}
+
+// core/src/metrics.rs:108-127 (ms_ssim)
+static double ms_ssim(const uint8_t* a, const uint8_t* b, int w, int h, int ch, double* per_scale) {
+  static const double W[5] = {0.0448, 0.2856, 0.3001, 0.2363, 0.1333};
+  std::vector<uint8_t> x = luma(a, (size_t)w * h, ch), y = luma(b, (size_t)w * h, ch);
+  double out = 1.0;
+  int cw = w, chh = h;
+  for (int i = 0; i < 5; i++) {
+    double s = std::max(ssim(x.data(), y.data(), cw, chh, 1), 1e-9);
+    if (per_scale) per_scale[i] = s;
+    out *= std::pow(s, W[i]);
+    if (i + 1 < 5) {
+      int w2 = cw, h2 = chh;
+      x = downsample2(x, w2, h2);
+      w2 = cw;
+      h2 = chh;
+      y = downsample2(y, w2, h2);
+      cw = w2;
+      chh = h2;
+    }
+  }
+  return out;
+}
+
+enum { METRIC_SSIMULACRA2 = 0, METRIC_SSIM = 1 };
+
+// The search's metric on a candidate (jpeg/src/target.rs:38): ssimulacra2 maps a failure to f64::MIN
+// (cli/src/pipeline.rs:218); ssim always scores.
+static double score_coefs(const uint8_t* ref, int w, int h, int channels, const CoefImage& ci,
+                          int metric = METRIC_SSIMULACRA2) {
   (void)channels;
   int oc = 0;
   std::vector<uint8_t> img = reconstruct(ci, &oc);
+  if (metric == METRIC_SSIM) return ssim(ref, img.data(), w, h, oc);
   double s = 0.0;
   if (ssimulacra2_t<float>(ref, img.data(), w, h, oc, 8, &s, nullptr, nullptr) != 0) return -1.7976931348623157e308;
   return s;
 }
 
 static Found find_quality(const uint8_t* ref, int w, int h, int channels, double target, int max_quality,
-                          int subsampling, bool trellis, std::vector<std::pair<int, double>>* trace) {
+                          int subsampling, bool trellis, std::vector<std::pair<int, double>>* trace,
+                          int metric = METRIC_SSIMULACRA2) {
   int lo = 1, hi = std::max(max_quality, 1);
   CoefImage top = build_coefs(ref, w, h, channels, hi, subsampling, trellis);
-  double top_score = score_coefs(ref, w, h, channels, top);
+  double top_score = score_coefs(ref, w, h, channels, top, metric);
   if (trace) trace->push_back({hi, top_score});
   Found best{hi, top_score, std::move(top)};
   if (top_score < target) return best;
   while (lo < hi) {
     int mid = lo + (hi - lo) / 2;
     CoefImage ci = build_coefs(ref, w, h, channels, mid, subsampling, trellis);
-    double s = score_coefs(ref, w, h, channels, ci);
+    double s = score_coefs(ref, w, h, channels, ci, metric);
     if (trace) trace->push_back({mid, s});
     if (s >= target) {
       hi = mid;
@@ -1259,7 +1374,7 @@ static void requantize(CoefImage& ci, int quality, bool trellis) {
 // cli/src/pipeline.rs:369-386: the JPEG->JPEG search. The reference image is the source reconstructed; each
 // candidate is the source requantized (jpeg/src/target.rs:29-56 drives it).
 static Found find_quality_requantize(const CoefImage& src, double target, int max_quality, bool trellis,
-                                     std::vector<std::pair<int, double>>* trace) {
+                                     std::vector<std::pair<int, double>>* trace, int metric = METRIC_SSIMULACRA2) {
   int oc = 0;
   std::vector<uint8_t> ref = reconstruct(src, &oc);
   auto make = [&](int q) {
@@ -1269,14 +1384,14 @@ static Found find_quality_requantize(const CoefImage& src, double target, int ma
   };
   int lo = 1, hi = std::max(max_quality, 1);
   CoefImage top = make(hi);
-  double top_score = score_coefs(ref.data(), src.width, src.height, oc, top);
+  double top_score = score_coefs(ref.data(), src.width, src.height, oc, top, metric);
   if (trace) trace->push_back({hi, top_score});
   Found best{hi, top_score, std::move(top)};
   if (top_score < target) return best;
   while (lo < hi) {
     int mid = lo + (hi - lo) / 2;
     CoefImage ci = make(mid);
-    double s = score_coefs(ref.data(), src.width, src.height, oc, ci);
+    double s = score_coefs(ref.data(), src.width, src.height, oc, ci, metric);
     if (trace) trace->push_back({mid, s});
     if (s >= target) {
       hi = mid;
@@ -1935,10 +2050,12 @@ int orc_ssimulacra2_fp64(const uint8_t* ref, const uint8_t* dist, int w, int h, 
 // every evaluated (quality, score) in order; *ntrace their count.
 int orc_search(const uint8_t* data, int w, int h, int channels, double target, int max_quality, int subsampling,
                int trellis, int* found_q, double* found_score, int16_t* coefs_out, uint8_t* qtables_out, int* trace_q,
-               double* trace_s, int* ntrace) {
-  if (w < 8 || h < 8 || (channels != 1 && channels != 3)) return 1;
+               double* trace_s, int* ntrace, int metric) {
+  if (channels != 1 && channels != 3) return 1;
+  if (metric == orc::METRIC_SSIMULACRA2 && (w < 8 || h < 8)) return 1;
   std::vector<std::pair<int, double>> tr;
-  orc::Found f = orc::find_quality(data, w, h, channels, target, max_quality, subsampling, trellis != 0, &tr);
+  orc::Found f =
+      orc::find_quality(data, w, h, channels, target, max_quality, subsampling, trellis != 0, &tr, metric);
   *found_q = f.quality;
   *found_score = f.score;
   if (coefs_out) orc::coef_to_flat(f.coefs, coefs_out, qtables_out);
@@ -1948,6 +2065,15 @@ int orc_search(const uint8_t* data, int w, int h, int channels, double target, i
     if (trace_s) trace_s[i] = tr[i].second;
   }
   return 0;
+}
+
+// core/src/metrics.rs:13 (ssim), :67 (psnr), :111 (ms_ssim) of two 8-bit interleaved images with `ch` channels.
+double orc_ssim(const uint8_t* a, const uint8_t* b, int w, int h, int ch) { return orc::ssim(a, b, w, h, ch); }
+double orc_psnr(const uint8_t* a, const uint8_t* b, int w, int h, int ch) {
+  return orc::psnr(a, b, (size_t)w * h * ch);
+}
+double orc_ms_ssim(const uint8_t* a, const uint8_t* b, int w, int h, int ch, double* per_scale) {
+  return orc::ms_ssim(a, b, w, h, ch, per_scale);
 }
 
 // CoefImage::requantize (jpeg/src/encode.rs:111) of a general flat CoefImage (1 or 3 components).
@@ -1976,11 +2102,11 @@ int orc_search_requantize(int w, int h, int ncomp, const int* hs, const int* vs,
                           const int* tq, const uint8_t* qtables4, const uint8_t* has_q, const int16_t* coefs,
                           double target, int max_quality, int trellis, int* found_q, double* found_score,
                           int16_t* coefs_out, int* tq_out, uint8_t* qtables4_out, uint8_t* has_q_out, int* trace_q,
-                          double* trace_s, int* ntrace) {
+                          double* trace_s, int* ntrace, int metric) {
   if (ncomp != 1 && ncomp != 3) return 1;
   orc::CoefImage ci = orc::coef_from_flat_tq(w, h, ncomp, hs, vs, bws, bhs, tq, qtables4, has_q, coefs);
   std::vector<std::pair<int, double>> tr;
-  orc::Found f = orc::find_quality_requantize(ci, target, max_quality, trellis != 0, &tr);
+  orc::Found f = orc::find_quality_requantize(ci, target, max_quality, trellis != 0, &tr, metric);
   *found_q = f.quality;
   *found_score = f.score;
   orc::coef_to_flat_tq(f.coefs, coefs_out, tq_out, qtables4_out, has_q_out);

@@ -39,13 +39,18 @@ def lib():
         L.orc_coef_layout.argtypes = [i32, i32, i32, i32, i32, pi, P, P, P, P]
         L.orc_reconstruct.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, pi]
         L.orc_ac_code_lengths.argtypes = [i32, i32, i32, P, P, P, P, P, P, P]
-        L.orc_search.argtypes = [P, i32, i32, i32, ctypes.c_double, i32, i32, i32, pi, pd, P, P, P, P, pi]
+        L.orc_search.argtypes = [P, i32, i32, i32, ctypes.c_double, i32, i32, i32, pi, pd, P, P, P, P, pi, i32]
+        for name in ("orc_ssim", "orc_psnr"):
+            getattr(L, name).argtypes = [P, P, i32, i32, i32]
+            getattr(L, name).restype = ctypes.c_double
+        L.orc_ms_ssim.argtypes = [P, P, i32, i32, i32, P]
+        L.orc_ms_ssim.restype = ctypes.c_double
         L.orc_write_best.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, ctypes.c_long, pi]
         L.orc_write_best.restype = ctypes.c_long
         L.orc_requantize.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, P, i32, i32, P, P, P, P]
         L.orc_reconstruct_tq.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, P, P, pi]
         L.orc_search_requantize.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, P, ctypes.c_double, i32, i32, pi, pd,
-                                            P, P, P, P, P, P, pi]
+                                            P, P, P, P, P, P, pi, i32]
         L.orc_write_best_tq.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, P, P, ctypes.c_long, pi]
         L.orc_write_best_tq.restype = ctypes.c_long
         pu64 = ctypes.POINTER(ctypes.c_uint64)
@@ -151,7 +156,10 @@ def ac_code_lengths(w, h, lay, qt, coefs):
     return out
 
 
-def search(src, target, max_quality=100, subsampling=0, trellis=True):
+METRIC_SSIMULACRA2, METRIC_SSIM = 0, 1
+
+
+def search(src, target, max_quality=100, subsampling=0, trellis=True, metric=METRIC_SSIMULACRA2):
     a, w, h, c, _ = _img(src)
     q = ctypes.c_int()
     s = ctypes.c_double()
@@ -164,7 +172,7 @@ def search(src, target, max_quality=100, subsampling=0, trellis=True):
     qt = np.zeros((2, 64), dtype=np.uint8)
     rc = lib().orc_search(a.ctypes.data, w, h, c, float(target), int(max_quality), int(subsampling),
                           1 if trellis else 0, ctypes.byref(q), ctypes.byref(s), coefs.ctypes.data, qt.ctypes.data,
-                          tq.ctypes.data, ts.ctypes.data, ctypes.byref(nt))
+                          tq.ctypes.data, ts.ctypes.data, ctypes.byref(nt), int(metric))
     if rc != 0:
         raise ValueError("bad input")
     lay = layout(w, h, c, q.value, subsampling)
@@ -235,7 +243,7 @@ def reconstruct_general(g):
     return out[:, :, 0] if n == 1 else out
 
 
-def search_requantize(g, target, max_quality=100, trellis=True):
+def search_requantize(g, target, max_quality=100, trellis=True, metric=METRIC_SSIMULACRA2):
     q = ctypes.c_int()
     s = ctypes.c_double()
     out = np.zeros_like(g.coefs)
@@ -248,7 +256,7 @@ def search_requantize(g, target, max_quality=100, trellis=True):
     rc = lib().orc_search_requantize(*g.args(), float(target), int(max_quality), 1 if trellis else 0,
                                      ctypes.byref(q), ctypes.byref(s), out.ctypes.data, tq.ctypes.data,
                                      q4.ctypes.data, has.ctypes.data, tqs.ctypes.data, ts.ctypes.data,
-                                     ctypes.byref(nt))
+                                     ctypes.byref(nt), int(metric))
     if rc:
         raise ValueError("unsupported component count")
     trace = [(int(tqs[i]), float(ts[i])) for i in range(nt.value)]
@@ -283,4 +291,34 @@ def plan(w, h, lay, coefs):
     best = [scan(scans[8 * i: 8 * i + 8]) for i in range(ns.value)]
     distinct = [(scan(dist[8 * i: 8 * i + 8]), int(costs[i])) for i in range(nd.value)]
     return int(pe.value), int(be.value), best, distinct
+
+
+def _pair(a, b):
+    a = np.ascontiguousarray(a, dtype=np.uint8)
+    b = np.ascontiguousarray(b, dtype=np.uint8)
+    if a.shape != b.shape:
+        raise ValueError("images differ in shape")
+    h, w = a.shape[:2]
+    ch = 1 if a.ndim == 2 else a.shape[2]
+    return a, b, w, h, ch
+
+
+def ssim(a, b):
+    """core/src/metrics.rs:13 (8-bit, every channel including alpha)."""
+    a, b, w, h, ch = _pair(a, b)
+    return lib().orc_ssim(a.ctypes.data, b.ctypes.data, w, h, ch)
+
+
+def psnr(a, b):
+    """core/src/metrics.rs:67."""
+    a, b, w, h, ch = _pair(a, b)
+    return lib().orc_psnr(a.ctypes.data, b.ctypes.data, w, h, ch)
+
+
+def ms_ssim(a, b, per_scale=False):
+    """core/src/metrics.rs:111; with per_scale, also the five clamped luma SSIM values."""
+    a, b, w, h, ch = _pair(a, b)
+    ps = np.zeros(5, np.float64)
+    v = lib().orc_ms_ssim(a.ctypes.data, b.ctypes.data, w, h, ch, ps.ctypes.data)
+    return (v, ps) if per_scale else v
 

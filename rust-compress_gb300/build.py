@@ -32,6 +32,7 @@ UNITS = {
     "ssim2.cu": [],
     "capi.cu": [],
     "plan.cu": [],
+    "metrics.cu": [],
 }
 
 

@@ -523,6 +523,97 @@ int rcg_ssimulacra2_device(rcg_ctx* ctx, const uint8_t* d_reference, const uint8
   return score_device_images(ctx, d_reference, d_distorted, (int)width, (int)height, channels, 8, score);
 }
 
+// ---- other metrics
+
+static int metric_on_device(rcg_ctx* ctx, int metric, const uint8_t* d_a, const uint8_t* d_b, int w, int h, int ch,
+                            double* score) {
+  int rc;
+  if (metric == RCG_METRIC_SSIMULACRA2) {
+    if (w < kMinSide || h < kMinSide) return fail(ctx, RCG_INVALID, "SSIMULACRA 2 needs at least 8x8 pixels");
+    return score_device_images(ctx, d_a, d_b, w, h, ch, 8, score);
+  }
+  if (metric == RCG_METRIC_SSIM) {
+    double* d = (double*)workspace(ctx, "metric_score", sizeof(double) * 8);
+    if (!d) return RCG_NO_MEMORY;
+    if ((rc = ssim_score(ctx, d_a, d_b, w, h, ch, d, nullptr, nullptr)) != RCG_OK) return rc;
+    cudaMemcpyAsync(score, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+    return finish(ctx, "ssim");
+  }
+  if (metric == RCG_METRIC_PSNR) {
+    // core/src/metrics.rs:67-73: mean squared error over every sample, +infinity for identical images
+    unsigned long long* d = (unsigned long long*)workspace(ctx, "metric_sq", sizeof(unsigned long long));
+    if (!d) return RCG_NO_MEMORY;
+    const size_t n = (size_t)w * h * ch;
+    squared_error(ctx, d_a, d_b, n, d);
+    unsigned long long se = 0;
+    cudaMemcpyAsync(&se, d, sizeof se, cudaMemcpyDeviceToHost, ctx->stream);
+    if ((rc = finish(ctx, "psnr")) != RCG_OK) return rc;
+    const double mse = (double)se / (double)std::max<size_t>(n, 1);
+    *score = mse == 0.0 ? INFINITY : 10.0 * std::log10(255.0 * 255.0 / mse);
+    return RCG_OK;
+  }
+  if (metric == RCG_METRIC_MS_SSIM) {
+    // core/src/metrics.rs:111-127: luma SSIM at five dyadic scales, clamped at 1e-9, combined with the weights.
+    static const double kW[5] = {0.0448, 0.2856, 0.3001, 0.2363, 0.1333};
+    const size_t npx = (size_t)w * h;
+    uint8_t* x = (uint8_t*)workspace(ctx, "msssim_x", npx);
+    uint8_t* y = (uint8_t*)workspace(ctx, "msssim_y", npx);
+    uint8_t* x2 = (uint8_t*)workspace(ctx, "msssim_x2", npx / 4 + 1);
+    uint8_t* y2 = (uint8_t*)workspace(ctx, "msssim_y2", npx / 4 + 1);
+    double* d = (double*)workspace(ctx, "metric_score", sizeof(double) * 8);
+    if (!x || !y || !x2 || !y2 || !d) return RCG_NO_MEMORY;
+    luma8(ctx, d_a, npx, ch, x);
+    luma8(ctx, d_b, npx, ch, y);
+    int cw = w, chh = h;
+    for (int i = 0; i < 5; i++) {
+      if ((rc = ssim_score(ctx, x, y, cw, chh, 1, d + i, nullptr, nullptr)) != RCG_OK) return rc;
+      if (i + 1 < 5 && cw / 2 > 0 && chh / 2 > 0) {
+        downsample2(ctx, x, cw, chh, x2);
+        downsample2(ctx, y, cw, chh, y2);
+        std::swap(x, x2);
+        std::swap(y, y2);
+        cw /= 2;
+        chh /= 2;
+      }
+    }
+    double s[5];
+    cudaMemcpyAsync(s, d, sizeof s, cudaMemcpyDeviceToHost, ctx->stream);
+    if ((rc = finish(ctx, "ms_ssim")) != RCG_OK) return rc;
+    double out = 1.0;
+    for (int i = 0; i < 5; i++) out *= std::pow(std::max(s[i], 1e-9), kW[i]);
+    *score = out;
+    return RCG_OK;
+  }
+  return fail(ctx, RCG_INVALID, "unknown metric");
+}
+
+int rcg_metric_score(rcg_ctx* ctx, int metric, const uint8_t* reference, const uint8_t* candidate, uint32_t width,
+                     uint32_t height, int channels, double* score) {
+  if (!ctx) return RCG_INVALID;
+  if (!reference || !candidate || !score) return fail(ctx, RCG_INVALID, "null pointer");
+  if (channels < 1 || channels > 4) return fail(ctx, RCG_INVALID, "channels must be 1..4");
+  if (width == 0 || height == 0) return fail(ctx, RCG_INVALID, "empty image");
+  cudaSetDevice(ctx->device);
+  const size_t bytes = (size_t)width * height * channels;
+  uint8_t* d_a = (uint8_t*)workspace(ctx, "img_a", bytes);
+  uint8_t* d_b = (uint8_t*)workspace(ctx, "img_b", bytes);
+  if (!d_a || !d_b) return RCG_NO_MEMORY;
+  int rc;
+  if ((rc = copy_to_device(ctx, d_a, reference, bytes)) != RCG_OK) return rc;
+  if ((rc = copy_to_device(ctx, d_b, candidate, bytes)) != RCG_OK) return rc;
+  return metric_on_device(ctx, metric, d_a, d_b, (int)width, (int)height, channels, score);
+}
+
+int rcg_metric_score_device(rcg_ctx* ctx, int metric, const uint8_t* d_reference, const uint8_t* d_candidate,
+                            uint32_t width, uint32_t height, int channels, double* score) {
+  if (!ctx) return RCG_INVALID;
+  if (!d_reference || !d_candidate || !score) return fail(ctx, RCG_INVALID, "null pointer");
+  if (channels < 1 || channels > 4) return fail(ctx, RCG_INVALID, "channels must be 1..4");
+  if (width == 0 || height == 0) return fail(ctx, RCG_INVALID, "empty image");
+  cudaSetDevice(ctx->device);
+  return metric_on_device(ctx, metric, d_reference, d_candidate, (int)width, (int)height, channels, score);
+}
+
 // ---- encoder
 
 int rcg_build_coefs(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
@@ -646,20 +737,62 @@ int rcg_reconstruct_tables(rcg_ctx* ctx, uint32_t width, uint32_t height, const 
 
 // ---- search
 
-static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, double target, int max_q,
-                       int subsampling, int trellis_on, rcg_found* found, int16_t* d_coefs_out, size_t coefs_len,
-                       uint8_t* d_qt_out, int16_t* h_coefs_out, uint8_t* h_qt_out) {
+// Per-candidate scorer of the device searches: SSIMULACRA2 from the candidate's linear pyramid against the
+// reference's, or SSIM from the candidate's 8-bit pixels against the reference's.
+struct SearchScorer {
+  int metric;
+  PyramidDesc pd;
+  float* ref_pyr = nullptr;
+  float* dist_pyr = nullptr;
+  const uint8_t* ref_px = nullptr;
+  uint8_t* cand_px = nullptr;
+  double* d_score = nullptr;
+};
+
+static int scorer_setup(rcg_ctx* ctx, int metric, int w, int h, int channels, SearchScorer* sc) {
+  sc->metric = metric;
+  sc->d_score = (double*)workspace(ctx, "score", sizeof(double));
+  if (!sc->d_score) return RCG_NO_MEMORY;
+  if (metric == RCG_METRIC_SSIM) {
+    sc->cand_px = (uint8_t*)workspace(ctx, "cand_px", (size_t)w * h * channels);
+    return sc->cand_px ? RCG_OK : RCG_NO_MEMORY;
+  }
+  sc->pd = make_pyramid(w, h);
+  sc->ref_pyr = (float*)workspace(ctx, "ref_pyr", (size_t)sc->pd.floats * sizeof(float));
+  sc->dist_pyr = (float*)workspace(ctx, "dist_pyr", (size_t)sc->pd.floats * sizeof(float));
+  return sc->ref_pyr && sc->dist_pyr ? RCG_OK : RCG_NO_MEMORY;
+}
+
+// Decoded planes of one candidate -> score -> one bisection step (all gated by the step's `active`).
+static void score_candidate(rcg_ctx* ctx, const SearchScorer& sc, StepDesc* d_st, const uint8_t* planes, int w,
+                            int h, int channels, SearchState* d_ss) {
+  if (sc.metric == RCG_METRIC_SSIM) {
+    upsample_color(ctx, d_st, planes, w, h, sc.cand_px, nullptr);
+    ssim_score(ctx, sc.ref_px, sc.cand_px, w, h, channels, sc.d_score, d_ss, d_st);
+    return;
+  }
+  upsample_color(ctx, d_st, planes, w, h, nullptr, sc.dist_pyr);
+  build_pyramid_gated(ctx, sc.pd, sc.dist_pyr, d_st);
+  score_pyramids(ctx, sc.pd, sc.ref_pyr, sc.dist_pyr, sc.d_score, d_ss, d_st);
+}
+
+static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, int metric, double target,
+                       int max_q, int subsampling, int trellis_on, rcg_found* found, int16_t* d_coefs_out,
+                       size_t coefs_len, uint8_t* d_qt_out, int16_t* h_coefs_out, uint8_t* h_qt_out) {
   int rc;
-  PyramidDesc pd = make_pyramid(w, h);
-  float* ref_pyr = (float*)workspace(ctx, "ref_pyr", (size_t)pd.floats * sizeof(float));
-  float* dist_pyr = (float*)workspace(ctx, "dist_pyr", (size_t)pd.floats * sizeof(float));
-  double* d_score = (double*)workspace(ctx, "score", sizeof(double));
+  SearchScorer sc;
   SearchState* d_ss = (SearchState*)workspace(ctx, "search_state", sizeof(SearchState));
   StepDesc* d_st = (StepDesc*)workspace(ctx, "step_search", sizeof(StepDesc));
-  if (!ref_pyr || !dist_pyr || !d_score || !d_ss || !d_st) return RCG_NO_MEMORY;
-  // Quality-independent work, once per search: the reference image's linear pyramid, colour planes, FDCTs.
-  if ((rc = to_linear(ctx, d_src, w, h, channels, 8, ref_pyr)) != RCG_OK) return rc;
-  build_pyramid(ctx, pd, ref_pyr);
+  if (!d_ss || !d_st) return RCG_NO_MEMORY;
+  if ((rc = scorer_setup(ctx, metric, w, h, channels, &sc)) != RCG_OK) return rc;
+  // Quality-independent work, once per search: the reference image's linear pyramid (SSIMULACRA2; SSIM reads the
+  // source pixels as they are), colour planes, FDCTs.
+  if (metric == RCG_METRIC_SSIM) {
+    sc.ref_px = d_src;
+  } else {
+    if ((rc = to_linear(ctx, d_src, w, h, channels, 8, sc.ref_pyr)) != RCG_OK) return rc;
+    build_pyramid(ctx, sc.pd, sc.ref_pyr);
+  }
   EncoderSetup es;
   if ((rc = setup_encoder(ctx, d_src, w, h, channels, subsampling, &es)) != RCG_OK) return rc;
   int max_steps = 1;
@@ -687,9 +820,7 @@ static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int cha
     rate_tables(ctx, d_st);
     trellis(ctx, d_st, es.caches, es.max_blocks);
     dequant_idct(ctx, d_st, nullptr, planes, es.max_blocks);
-    upsample_color(ctx, d_st, planes, w, h, nullptr, dist_pyr);
-    build_pyramid_gated(ctx, pd, dist_pyr, d_st);
-    score_pyramids(ctx, pd, ref_pyr, dist_pyr, d_score, d_ss, d_st);
+    score_candidate(ctx, sc, d_st, planes, w, h, channels, d_ss);
   }
   cudaMemcpyAsync(&hs, d_ss, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream);
   if ((rc = finish(ctx, "search")) != RCG_OK) return rc;
@@ -720,25 +851,40 @@ static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int cha
   return finish(ctx, "search output");
 }
 
-int rcg_search(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels, double target,
-               int max_quality, const rcg_encode_options* opts, rcg_found* found, int16_t* coefs, size_t coefs_len,
-               uint8_t* qtables) {
+// The goal checks of find_jpeg_quality (cli/src/pipeline.rs:211-218).
+static int check_goal(rcg_ctx* ctx, int metric, uint32_t width, uint32_t height, double target) {
+  if (metric != RCG_METRIC_SSIMULACRA2 && metric != RCG_METRIC_SSIM)
+    return fail(ctx, RCG_INVALID, "the JPEG search goal is SSIMULACRA2 or SSIM");
+  if (metric == RCG_METRIC_SSIMULACRA2 && (width < (uint32_t)kMinSide || height < (uint32_t)kMinSide))
+    return fail(ctx, RCG_UNSUPPORTED, "--target-ssimulacra2 needs an image of at least 8x8 pixels");
+  if (!(target == target)) return fail(ctx, RCG_INVALID, "target is NaN");
+  return RCG_OK;
+}
+
+int rcg_search_metric(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels, int metric,
+                      double target, int max_quality, const rcg_encode_options* opts, rcg_found* found,
+                      int16_t* coefs, size_t coefs_len, uint8_t* qtables) {
   if (!ctx) return RCG_INVALID;
   int rc;
   if ((rc = check_image(ctx, width, height, channels)) != RCG_OK) return rc;
   if ((rc = check_opts(ctx, opts, false)) != RCG_OK) return rc;
   if (!src || !found) return fail(ctx, RCG_INVALID, "null pointer");
-  if (width < (uint32_t)kMinSide || height < (uint32_t)kMinSide)
-    return fail(ctx, RCG_UNSUPPORTED, "--target-ssimulacra2 needs an image of at least 8x8 pixels");
-  if (!(target == target)) return fail(ctx, RCG_INVALID, "target is NaN");
+  if ((rc = check_goal(ctx, metric, width, height, target)) != RCG_OK) return rc;
   int max_q = std::max(1, std::min(max_quality, 100));
   cudaSetDevice(ctx->device);
   size_t bytes = (size_t)width * height * channels;
   uint8_t* d_src = (uint8_t*)workspace(ctx, "img_src", bytes);
   if (!d_src) return RCG_NO_MEMORY;
   if ((rc = copy_to_device(ctx, d_src, src, bytes)) != RCG_OK) return rc;
-  return search_impl(ctx, d_src, (int)width, (int)height, channels, target, max_q, opts->subsampling,
+  return search_impl(ctx, d_src, (int)width, (int)height, channels, metric, target, max_q, opts->subsampling,
                      opts->trellis, found, nullptr, coefs_len, nullptr, coefs, qtables);
+}
+
+int rcg_search(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels, double target,
+               int max_quality, const rcg_encode_options* opts, rcg_found* found, int16_t* coefs, size_t coefs_len,
+               uint8_t* qtables) {
+  return rcg_search_metric(ctx, src, width, height, channels, RCG_METRIC_SSIMULACRA2, target, max_quality, opts,
+                           found, coefs, coefs_len, qtables);
 }
 
 int rcg_search_device(rcg_ctx* ctx, const uint8_t* d_src, uint32_t width, uint32_t height, int channels,
@@ -754,8 +900,8 @@ int rcg_search_device(rcg_ctx* ctx, const uint8_t* d_src, uint32_t width, uint32
   if (!(target == target)) return fail(ctx, RCG_INVALID, "target is NaN");
   int max_q = std::max(1, std::min(max_quality, 100));
   cudaSetDevice(ctx->device);
-  return search_impl(ctx, d_src, (int)width, (int)height, channels, target, max_q, opts->subsampling, opts->trellis,
-                     found, d_coefs, coefs_len, d_qtables, nullptr, nullptr);
+  return search_impl(ctx, d_src, (int)width, (int)height, channels, RCG_METRIC_SSIMULACRA2, target, max_q,
+                     opts->subsampling, opts->trellis, found, d_coefs, coefs_len, d_qtables, nullptr, nullptr);
 }
 
 int rcg_search_batch(rcg_ctx* ctx, int n, const uint8_t* const* srcs, const uint32_t* widths,
@@ -852,15 +998,16 @@ int rcg_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef
 }
 
 int rcg_search_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
-                          const rcg_qtables* in, const int16_t* coefs_in, double target, int max_quality,
+                          const rcg_qtables* in, const int16_t* coefs_in, int metric, double target, int max_quality,
                           int trellis, rcg_found* found, int16_t* coefs_out, size_t coefs_len, rcg_qtables* out) {
   if (!ctx) return RCG_INVALID;
   if (!layout || !coefs_in || !found) return fail(ctx, RCG_INVALID, "null pointer");
-  if (width < (uint32_t)kMinSide || height < (uint32_t)kMinSide)
-    return fail(ctx, RCG_UNSUPPORTED, "--target-ssimulacra2 needs an image of at least 8x8 pixels");
+  if (width == 0 || height == 0 || width > 65535 || height > 65535)
+    return fail(ctx, RCG_INVALID, "JPEG dimensions must be 1..=65535");
+  int grc = check_goal(ctx, metric, width, height, target);
+  if (grc != RCG_OK) return grc;
   if (layout->ncomp != 1 && layout->ncomp != 3)
     return fail(ctx, RCG_UNSUPPORTED, "requantization takes 1 or 3 components");
-  if (!(target == target)) return fail(ctx, RCG_INVALID, "target is NaN");
   const int w = (int)width, h = (int)height;
   const int max_q = std::max(1, std::min(max_quality, 100));
   StepDesc* st = new StepDesc;
@@ -876,19 +1023,20 @@ int rcg_search_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const r
   int max_steps = 1;
   for (int span = max_q; span > 1; span = (span + 1) / 2) max_steps++;
   max_steps = std::min(max_steps, kMaxSteps);
-  PyramidDesc pd = make_pyramid(w, h);
+  const int channels = st->ncomp;
+  SearchScorer sc;
   int16_t* d_src = (int16_t*)workspace(ctx, "rq_src", cbytes);
   int16_t* slots = (int16_t*)workspace(ctx, "coef_slots", cbytes * max_steps);
   uint8_t* planes = (uint8_t*)workspace(ctx, "dec_planes", (size_t)plane_bytes(st));
-  float* ref_pyr = (float*)workspace(ctx, "ref_pyr", (size_t)pd.floats * sizeof(float));
-  float* dist_pyr = (float*)workspace(ctx, "dist_pyr", (size_t)pd.floats * sizeof(float));
-  double* d_score = (double*)workspace(ctx, "score", sizeof(double));
+  uint8_t* ref_px = metric == RCG_METRIC_SSIM ? (uint8_t*)workspace(ctx, "ref_px", (size_t)w * h * channels) : nullptr;
   SearchState* d_ss = (SearchState*)workspace(ctx, "search_state", sizeof(SearchState));
   StepDesc* d_st = (StepDesc*)workspace(ctx, "step_search", sizeof(StepDesc));
-  if (!d_src || !slots || !planes || !ref_pyr || !dist_pyr || !d_score || !d_ss || !d_st) {
+  if (!d_src || !slots || !planes || !d_ss || !d_st || (metric == RCG_METRIC_SSIM && !ref_px) ||
+      scorer_setup(ctx, metric, w, h, channels, &sc) != RCG_OK) {
     delete st;
     return RCG_NO_MEMORY;
   }
+  sc.ref_px = ref_px;
   if ((rc = copy_to_device(ctx, d_src, coefs_in, cbytes)) != RCG_OK) {
     delete st;
     return rc;
@@ -901,8 +1049,12 @@ int rcg_search_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const r
   st->requant = 1;
   cudaMemcpyAsync(d_st, st, sizeof(StepDesc), cudaMemcpyHostToDevice, ctx->stream);
   dequant_idct(ctx, d_st, d_src, planes, nblocks);
-  upsample_color(ctx, d_st, planes, w, h, nullptr, ref_pyr);
-  build_pyramid(ctx, pd, ref_pyr);
+  if (metric == RCG_METRIC_SSIM) {
+    upsample_color(ctx, d_st, planes, w, h, ref_px, nullptr);
+  } else {
+    upsample_color(ctx, d_st, planes, w, h, nullptr, sc.ref_pyr);
+    build_pyramid(ctx, sc.pd, sc.ref_pyr);
+  }
   SearchState hs;
   std::memset(&hs, 0, sizeof hs);
   hs.lo = 1;
@@ -911,7 +1063,7 @@ int rcg_search_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const r
   hs.target = target;
   hs.max_q = max_q;
   hs.trellis = trellis;
-  hs.channels = st->ncomp;
+  hs.channels = channels;
   hs.best_q = max_q;
   cudaMemcpyAsync(d_ss, &hs, sizeof hs, cudaMemcpyHostToDevice, ctx->stream);
   const float* no_caches[9] = {nullptr};
@@ -921,9 +1073,7 @@ int rcg_search_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const r
     rate_tables(ctx, d_st);
     rcg::trellis(ctx, d_st, no_caches, nblocks);
     dequant_idct(ctx, d_st, nullptr, planes, nblocks);
-    upsample_color(ctx, d_st, planes, w, h, nullptr, dist_pyr);
-    build_pyramid_gated(ctx, pd, dist_pyr, d_st);
-    score_pyramids(ctx, pd, ref_pyr, dist_pyr, d_score, d_ss, d_st);
+    score_candidate(ctx, sc, d_st, planes, w, h, channels, d_ss);
   }
   cudaMemcpyAsync(&hs, d_ss, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream);
   if ((rc = finish(ctx, "search_requantize")) != RCG_OK) {

@@ -102,6 +102,37 @@ struct SearchState {
   int status;            // nonzero: a device-side check failed
 };
 
+// One bisection step of jpeg/src/target.rs:35-53 on the device, after candidate `ss->step` scored `sv`: the first
+// candidate (max quality) ends the search when it misses the target; later ones move hi (accepted, s >= target) or
+// lo; the next quality is lo + (hi - lo) / 2 until lo == hi.
+__device__ __forceinline__ void search_record(SearchState* ss, double sv) {
+  if (ss->done) return;
+  const int step = ss->step;
+  const int q = ss->qs[step];
+  ss->scores[step] = sv;
+  if (step == 0) {
+    ss->best_q = q;
+    ss->best_score = sv;
+    ss->best_step = 0;
+    if (sv < ss->target) ss->done = 1;
+  } else if (sv >= ss->target) {
+    ss->hi = q;
+    ss->best_q = q;
+    ss->best_score = sv;
+    ss->best_step = step;
+  } else {
+    ss->lo = q + 1;
+  }
+  if (!ss->done) {
+    if (ss->lo < ss->hi && step + 1 < kMaxSteps) {
+      ss->step = step + 1;
+      ss->qs[step + 1] = ss->lo + (ss->hi - ss->lo) / 2;
+    } else {
+      ss->done = 1;
+    }
+  }
+}
+
 // ------------------------------------------------------------------------------------------------ context
 
 struct KernelTimes {
@@ -213,6 +244,14 @@ int upsample_color(rcg_ctx* ctx, StepDesc* d_step, const uint8_t* d_planes, int 
                    float* d_lin);
 // Host-side table setup of one quality into a host StepDesc (no device work).
 void host_step_tables(StepDesc* st, int quality, int subsampling, int channels, int trellis, int w, int h);
+// core/src/metrics.rs on device images: ssim (score to d_score; with ss, one bisection step; gated by st), the
+// squared-error sum of psnr, luma and downsample2 of ms_ssim.
+int ssim_score(rcg_ctx* ctx, const uint8_t* d_a, const uint8_t* d_b, int w, int h, int ch, double* d_score,
+               SearchState* ss, const StepDesc* st);
+int squared_error(rcg_ctx* ctx, const uint8_t* d_a, const uint8_t* d_b, size_t n, unsigned long long* d_out);
+int luma8(rcg_ctx* ctx, const uint8_t* d_a, size_t npx, int ch, uint8_t* d_out);
+int downsample2(rcg_ctx* ctx, const uint8_t* d_in, int w, int h, uint8_t* d_out);
+
 // write_best's plan (progressive candidates + baseline estimate) of coefficients on the device; `lay` carries the
 // component layout (ncomp, hmax, vmax, comp[]).
 int plan_scans(rcg_ctx* ctx, const StepDesc* lay, int w, int h, const int16_t* d_coefs, rcg_plan_result* res);

@@ -391,33 +391,7 @@ __global__ void __launch_bounds__(256) k_ssim2_reduce(PyramidDesc pd, const doub
   // A non-finite score is the reference's Err, which the search maps to f64::MIN (cli/src/pipeline.rs:218).
   bool finite = isfinite(score);
   *score_out = finite ? score : NAN;
-  if (ss && !ss->done) {
-    double sv = finite ? score : -1.7976931348623157e308;
-    int step = ss->step;
-    int q = ss->qs[step];
-    ss->scores[step] = sv;
-    if (step == 0) {
-      ss->best_q = q;
-      ss->best_score = sv;
-      ss->best_step = 0;
-      if (sv < ss->target) ss->done = 1;
-    } else if (sv >= ss->target) {
-      ss->hi = q;
-      ss->best_q = q;
-      ss->best_score = sv;
-      ss->best_step = step;
-    } else {
-      ss->lo = q + 1;
-    }
-    if (!ss->done) {
-      if (ss->lo < ss->hi && step + 1 < kMaxSteps) {
-        ss->step = step + 1;
-        ss->qs[step + 1] = ss->lo + (ss->hi - ss->lo) / 2;
-      } else {
-        ss->done = 1;
-      }
-    }
-  }
+  if (ss) search_record(ss, finite ? score : -1.7976931348623157e308);
 }
 
 // ------------------------------------------------------------------------------------------------ planes, pyramid

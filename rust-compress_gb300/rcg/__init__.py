@@ -28,6 +28,9 @@ RCG_OK, RCG_INVALID, RCG_UNSUPPORTED, RCG_CUDA_ERROR, RCG_TIMEOUT, RCG_NO_MEMORY
 _STATUS_NAMES = {1: "Invalid", 2: "Unsupported", 3: "CudaError", 4: "Timeout", 5: "NoMemory"}
 
 
+METRIC_SSIMULACRA2, METRIC_SSIM, METRIC_PSNR, METRIC_MS_SSIM = 0, 1, 2, 3
+
+
 class RcgError(RuntimeError):
     def __init__(self, status, message):
         super().__init__(f"{_STATUS_NAMES.get(status, status)}: {message}")
@@ -208,9 +211,13 @@ def _load():
         "rcg_reconstruct_tables": (i32, [P, u32, u32, ctypes.POINTER(_Layout), ctypes.POINTER(_QTables), P, P, sz]),
         "rcg_requantize": (i32, [P, u32, u32, ctypes.POINTER(_Layout), ctypes.POINTER(_QTables), P, i32, i32, P, sz,
                                  ctypes.POINTER(_QTables)]),
-        "rcg_search_requantize": (i32, [P, u32, u32, ctypes.POINTER(_Layout), ctypes.POINTER(_QTables), P,
+        "rcg_search_requantize": (i32, [P, u32, u32, ctypes.POINTER(_Layout), ctypes.POINTER(_QTables), P, i32,
                                         ctypes.c_double, i32, i32, ctypes.POINTER(_Found), P, sz,
                                         ctypes.POINTER(_QTables)]),
+        "rcg_metric_score": (i32, [P, i32, P, P, u32, u32, i32, ctypes.POINTER(ctypes.c_double)]),
+        "rcg_metric_score_device": (i32, [P, i32, P, P, u32, u32, i32, ctypes.POINTER(ctypes.c_double)]),
+        "rcg_search_metric": (i32, [P, P, u32, u32, i32, i32, ctypes.c_double, i32, ctypes.POINTER(_Opts),
+                                    ctypes.POINTER(_Found), P, sz, P]),
         "rcg_plan": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, sz, ctypes.POINTER(_PlanResult)]),
         "rcg_plan_device": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, ctypes.POINTER(_PlanResult)]),
         "rcg_search_batch": (i32, [P, i32, P, P, P, P, P, i32, ctypes.POINTER(_Opts), i32, P, P, P, P]),
@@ -227,7 +234,8 @@ EXPORTED = (
     "rcg_ctx_create rcg_ctx_destroy rcg_last_error rcg_ctx_set_stream rcg_ctx_stream rcg_ctx_synchronize "
     "rcg_ctx_launch_count rcg_ctx_set_profiling rcg_ctx_kernel_time rcg_coef_layout_for rcg_ssimulacra2 "
     "rcg_ssimulacra2_device rcg_ssimulacra2_device_noalloc rcg_build_coefs rcg_reconstruct rcg_search rcg_search_device "
-    "rcg_search_batch rcg_reconstruct_tables rcg_requantize rcg_search_requantize rcg_plan rcg_plan_device"
+    "rcg_search_batch rcg_reconstruct_tables rcg_requantize rcg_search_requantize rcg_plan rcg_plan_device "
+    "rcg_metric_score rcg_metric_score_device rcg_search_metric"
 ).split()
 
 
@@ -332,6 +340,36 @@ class Context:
                                                 width, height, channels, ctypes.byref(out)))
         return out.value
 
+    def metric(self, metric, reference, candidate):
+        """score(reference, candidate, metric) (cli/src/pipeline.rs:130): 8-bit images with 1..=4 channels."""
+        a, w, h, c, d = _image(reference)
+        b, w2, h2, c2, d2 = _image(candidate)
+        if (w, h, c, d) != (w2, h2, c2, d2) or d != 8:
+            raise RcgError(RCG_INVALID, "the metrics take two 8-bit images of the same shape")
+        out = ctypes.c_double()
+        self._check(_lib.rcg_metric_score(self._ptr, int(metric), a.ctypes.data, b.ctypes.data, w, h, c,
+                                          ctypes.byref(out)))
+        return out.value
+
+    def ssim(self, reference, candidate):
+        """core/src/metrics.rs:13."""
+        return self.metric(METRIC_SSIM, reference, candidate)
+
+    def psnr(self, reference, candidate):
+        """core/src/metrics.rs:67."""
+        return self.metric(METRIC_PSNR, reference, candidate)
+
+    def ms_ssim(self, reference, candidate):
+        """core/src/metrics.rs:111."""
+        return self.metric(METRIC_MS_SSIM, reference, candidate)
+
+    def metric_device(self, metric, ref_ptr, cand_ptr, width, height, channels):
+        out = ctypes.c_double()
+        self._check(_lib.rcg_metric_score_device(self._ptr, int(metric), ctypes.c_void_p(ref_ptr),
+                                                 ctypes.c_void_p(cand_ptr), width, height, channels,
+                                                 ctypes.byref(out)))
+        return out.value
+
     def coef_layout(self, width, height, channels, opts):
         lay = _Layout()
         o = _opts(opts)
@@ -396,7 +434,7 @@ class Context:
                                         out.size, ctypes.byref(t_out)))
         return _general_image(ci, out, t_out)
 
-    def find_quality_requantize(self, ci, target, max_quality=100, trellis=True):
+    def find_quality_requantize(self, ci, target, max_quality=100, trellis=True, metric=METRIC_SSIMULACRA2):
         """The JPEG -> JPEG --target-ssimulacra2 search (cli/src/pipeline.rs:369-386) over requantizations of `ci`."""
         lay = ci.layout()
         flat = np.ascontiguousarray(ci.flat())
@@ -404,7 +442,7 @@ class Context:
         t_in, t_out = ci.table_slots(), _QTables()
         f = _Found()
         self._check(_lib.rcg_search_requantize(self._ptr, ci.width, ci.height, ctypes.byref(lay),
-                                               ctypes.byref(t_in), flat.ctypes.data, float(target),
+                                               ctypes.byref(t_in), flat.ctypes.data, int(metric), float(target),
                                                int(max_quality), 1 if trellis else 0, ctypes.byref(f),
                                                out.ctypes.data, out.size, ctypes.byref(t_out)))
         trace = [(int(f.trace_q[i]), float(f.trace_score[i])) for i in range(f.nsteps)]
@@ -420,6 +458,13 @@ class Context:
 
         `out` (optional): a reusable int16 array of at least coef_capacity() entries; the returned coefficients are
         views into it (valid until it is reused), which spares a fresh allocation per call."""
+        return self._find_quality(reference, target, max_quality, opts, out, METRIC_SSIMULACRA2)
+
+    def find_quality(self, reference, target, max_quality=100, opts=None, out=None):
+        """The --target-ssim search (jpeg/src/target.rs:24, cli/src/pipeline.rs:213), on device."""
+        return self._find_quality(reference, target, max_quality, opts, out, METRIC_SSIM)
+
+    def _find_quality(self, reference, target, max_quality, opts, out, metric):
         opts = opts or EncodeOptions()
         a, w, h, c, d = _image(reference)
         if d != 8 or c not in (1, 3):
@@ -434,8 +479,9 @@ class Context:
         qt = np.zeros((2, 64), dtype=np.uint8)
         f = _Found()
         o = _opts(opts)
-        self._check(_lib.rcg_search(self._ptr, a.ctypes.data, w, h, c, float(target), int(max_quality),
-                                    ctypes.byref(o), ctypes.byref(f), coefs.ctypes.data, coefs.size, qt.ctypes.data))
+        self._check(_lib.rcg_search_metric(self._ptr, a.ctypes.data, w, h, c, int(metric), float(target),
+                                           int(max_quality), ctypes.byref(o), ctypes.byref(f), coefs.ctypes.data,
+                                           coefs.size, qt.ctypes.data))
         lay = self.coef_layout(w, h, c, EncodeOptions(f.quality, opts.subsampling, opts.trellis))
         ci = _coef_image(w, h, lay, coefs[: lay.ncoefs], qt)
         trace = [(int(f.trace_q[i]), float(f.trace_score[i])) for i in range(f.nsteps)]

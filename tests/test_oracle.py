@@ -387,3 +387,85 @@ def test_oracle_search_requantize_follows_bisection(oracle):
         assert q == want and s >= target
         ref = oracle.reconstruct_general(g)
         assert abs(oracle.ssimulacra2(ref, oracle.reconstruct_general(best)) - s) < 1e-12
+
+
+def _np_ssim(a, b):
+    """core/src/metrics.rs:13-62 restated with numpy: integer window sums from 4x4 group sums, the f64 formula in
+    the reference's order, each row of windows summed left to right, rows added in order."""
+    a = a.astype(np.int64)
+    b = b.astype(np.int64)
+    if a.ndim == 2:
+        a, b = a[:, :, None], b[:, :, None]
+    h, w, ch = a.shape
+    c1, c2 = 6.5025, 58.5225
+
+    def term(sx, sy, sxx, syy, sxy, n):
+        mx, my = sx / n, sy / n
+        vx, vy, cov = sxx / n - mx * mx, syy / n - my * my, sxy / n - mx * my
+        return ((2.0 * mx * my + c1) * (2.0 * cov + c2)) / ((mx * mx + my * my + c1) * (vx + vy + c2))
+
+    if w < 8 or h < 8:
+        total = 0.0
+        for c in range(ch):
+            p, q = a[:, :, c], b[:, :, c]
+            total += term(*(float(x.sum()) for x in (p, q, p * p, q * q, p * q)), float(w * h))
+        return total / ch
+    ny, nx = (h - 8) // 4 + 1, (w - 8) // 4 + 1
+    gh, gw = ny + 1, nx + 1
+    vals = np.zeros((ny, nx))
+    for c in range(ch):
+        p = a[: 4 * gh, : 4 * gw, c]
+        q = b[: 4 * gh, : 4 * gw, c]
+        sums = []
+        for x in (p, q, p * p, q * q, p * q):
+            g = x.reshape(gh, 4, gw, 4).sum(axis=(1, 3))
+            sums.append((g[:-1, :-1] + g[:-1, 1:] + g[1:, :-1] + g[1:, 1:]).astype(np.float64))
+        vals = vals + term(*sums, 64.0)
+    vals = vals / ch
+    rows = np.zeros(ny)
+    for i in range(nx):
+        rows = rows + vals[:, i]
+    total = 0.0
+    for j in range(ny):
+        total += rows[j]
+    return total / (ny * nx)
+
+
+def test_oracle_metrics_against_numpy_and_reference_properties(oracle):
+    import rcg.synth as synth
+
+    def img(w, h, f):
+        y, x = np.mgrid[0:h, 0:w]
+        return f(x, y).astype(np.uint8)
+
+    # core/src/metrics.rs:141-175 (the reference's own tests)
+    a = img(40, 33, lambda x, y: x * 5 + y * 3)
+    assert abs(oracle.ssim(a, a) - 1.0) < 1e-12
+    a = img(64, 64, lambda x, y: (x * 7 + y * 5) % 256)
+    s = oracle.ssim(a, a // 8 * 8)
+    hv = oracle.ssim(a, a // 64 * 64)
+    assert s > hv and s < 1.0 and hv > -1.0
+    t = img(3, 2, lambda x, y: x + y)
+    assert oracle.ssim(t, t) > 0.99
+    a = img(32, 32, lambda x, y: (x * 3 + y * 5) % 256)
+    assert oracle.psnr(a, a) == float("inf")
+    p = oracle.psnr(a, (a + 8).astype(np.uint8))
+    assert 20.0 < p < 40.0
+    a = img(64, 64, lambda x, y: (x * 7 + y * 11) % 256)
+    same, sl = oracle.ms_ssim(a, a), oracle.ms_ssim(a, a // 16 * 16)
+    assert same > 0.99 and sl < same
+    # independent numpy restatement: bit-exact SSIM, exact PSNR
+    for w, h, ch in ((200, 150, 3), (37, 21, 1), (64, 9, 4), (7, 30, 3), (5, 5, 2)):
+        ref = synth.image(max(w, 8), max(h, 8), 12)[:h, :w]
+        dist = synth.image(max(w, 8), max(h, 8), 12, sensor_sigma=6.0)[:h, :w]
+        if ch == 1:
+            ref, dist = ref[:, :, 0].copy(), dist[:, :, 0].copy()
+        elif ch == 2:
+            ref, dist = ref[:, :, :2].copy(), dist[:, :, :2].copy()
+        elif ch == 4:
+            ref = np.concatenate([ref, ref[:, :, :1]], 2)
+            dist = np.concatenate([dist, dist[:, :, 1:2]], 2)
+        assert oracle.ssim(ref, dist) == _np_ssim(ref, dist), (w, h, ch)
+        d = ref.astype(np.float64) - dist.astype(np.float64)
+        mse = (d * d).sum() / d.size
+        assert oracle.psnr(ref, dist) == 10.0 * np.log10(255.0 * 255.0 / mse)
