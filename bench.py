@@ -258,6 +258,42 @@ def requantize_workload(ctx, img, timed, with_oracle=True, steps=5):
     return out
 
 
+def ssim_workload(ctx, img, timed, torch, dev, with_oracle=True, steps=5):
+    """`--target-ssim` (jpeg/src/target.rs:24): the same 12 MP image, target SSIM 0.95, 4:2:0, trellis, host
+    buffers; and SSIM alone on a device-resident 12 MP pair (the source vs its q50 round trip)."""
+    import rcg
+
+    opts = rcg.EncodeOptions(90, rcg.Subsampling.S420, True)
+    for _ in range(2):
+        ctx.find_quality(img, 0.95, 100, opts)
+    times, f = timed(lambda: ctx.find_quality(img, 0.95, 100, opts), steps)
+    ms = sum(times) / len(times)
+    dist_img = ctx.reconstruct(ctx.build_coefs(img, rcg.EncodeOptions(50, rcg.Subsampling.S420, True)))
+    d_a = torch.from_numpy(img).to(dev)
+    d_b = torch.from_numpy(dist_img).to(dev)
+    torch.cuda.synchronize()
+    one = lambda: ctx.metric_device(rcg.METRIC_SSIM, d_a.data_ptr(), d_b.data_ptr(), W, H, 3)
+    for _ in range(3):
+        one()
+    mt, score = timed(one, 10)
+    out = {"workload": "--target-ssim 0.95 search of the 12 MP image (4:2:0, trellis), host buffers",
+           "searches_per_s": 1000.0 / ms, "ms_per_search": ms, "quality": f.quality, "score": f.score,
+           "candidates": len(f.trace), "ssim_alone_ms": sum(mt) / len(mt), "ssim_alone_score": score}
+    if with_oracle:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        oracle.build()
+        oracle.set_threads(os.cpu_count() or 1)
+        t0 = time.perf_counter()
+        o = oracle.ssim(img, dist_img)
+        dt = time.perf_counter() - t0
+        out["ssim_oracle"] = o
+        out["ssim_abs_err"] = abs(o - score)
+        out["cpu_baseline_ssim_ms"] = dt * 1000.0
+    return out
+
+
 def plan_workload(ctx, timed, d_coefs, lay, with_oracle=True, steps=10):
     """write_best's plan of the search result (device-resident coefficients of the 12 MP workload at the found
     quality): statistics of the 48 distinct candidate scans and the baseline scan, code lengths, costs, choice.
@@ -296,6 +332,24 @@ def plan_workload(ctx, timed, d_coefs, lay, with_oracle=True, steps=10):
     return out
 
 
+def kernel_case(name):
+    """A handful of launches of one workload on the W x H image (for ncu captures of a single kernel)."""
+    import rcg
+    import rcg.synth as synth
+
+    ctx = rcg.Context(0)
+    img = synth.image(W, H, SEED, SIGMA)
+    ci = ctx.build_coefs(img, rcg.EncodeOptions(70, rcg.Subsampling.S420, True))
+    if name == "plan":
+        for _ in range(2):
+            ctx.plan(ci)
+    else:
+        dist = ctx.reconstruct(ci)
+        for _ in range(2):
+            ctx.ssim(img, dist) if name == "ssim" else ctx.ssimulacra2(img, dist)
+    ctx.synchronize()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -306,12 +360,16 @@ def main():
     ap.add_argument("--no-scorer", action="store_true", help="skip the scorer-alone measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the many-image batch measurement")
     ap.add_argument("--no-requant", action="store_true", help="skip the JPEG->JPEG search measurement")
+    ap.add_argument("--kernel-case", choices=["plan", "ssim", "ssim2"], default=None,
+                    help="profiling aid: run only a few calls of one workload at --width x --height, print nothing")
     ap.add_argument("--width", type=int, default=W, help="smaller cases for profiling only; the bench line uses 4000")
     ap.add_argument("--height", type=int, default=H)
     args = ap.parse_args()
     _set_size(args.width, args.height)
     if args.impl == "reference":
         return run_reference(args)
+    if args.kernel_case:
+        return kernel_case(args.kernel_case)
 
     import numpy as np
     import torch
@@ -425,6 +483,9 @@ def main():
         lay_found = ctx.coef_layout(W, H, 3, rcg.EncodeOptions(res[0], opts.subsampling, opts.trellis))
         step_device()  # leaves the last search's chosen coefficients in d_coefs
         plan = plan_workload(ctx, timed, d_coefs, lay_found, with_oracle=not args.no_cpu_baseline)
+    ssim_w = None
+    if rank == 0 and not args.no_requant:
+        ssim_w = ssim_workload(ctx, img, timed, torch, dev, with_oracle=not args.no_cpu_baseline)
     requant = None
     if rank == 0 and not args.no_requant:
         requant = requantize_workload(ctx, img, timed, with_oracle=not args.no_cpu_baseline)
@@ -464,6 +525,7 @@ def main():
             "batch": batch,
             "requantize": requant,
             "write_best_plan": plan,
+            "target_ssim": ssim_w,
         }
         print(json.dumps(out), flush=True)
     if dist:

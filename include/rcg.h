@@ -103,6 +103,13 @@ typedef struct {
   uint64_t distinct_bytes[48];
 } rcg_plan_result;
 
+/* What rcg_decode_coefs learned about a JPEG besides its coefficients. */
+typedef struct {
+  uint32_t width, height;
+  uint8_t ids[4]; /* component identifiers (SOF order) */
+  int32_t scans;  /* scans decoded */
+} rcg_jpeg_info;
+
 typedef struct rcg_ctx rcg_ctx;
 
 /* Context lifetime. `device` is a CUDA device ordinal. */
@@ -193,6 +200,24 @@ int rcg_metric_score_device(rcg_ctx* ctx, int metric, const uint8_t* d_reference
 int rcg_search_metric(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels, int metric,
                       double target, int max_quality, const rcg_encode_options* opts, rcg_found* found,
                       int16_t* coefs, size_t coefs_len, uint8_t* qtables);
+
+/* jpeg::decode::parse(data)?.into_coefs() (jpeg/src/decode.rs:397, :540) for sequential Huffman JPEGs (SOF0/SOF1,
+ * 8-bit, 1 or 3 components, any sampling, restart intervals, any number of scans): markers on the host, the
+ * entropy-coded data decoded on the GPU. Progressive, arithmetic, lossless, hierarchical, 12-bit, RGB-coded and
+ * 4-component files answer RCG_UNSUPPORTED (decode them on the host). With coefs == NULL only the header is parsed
+ * (info, layout, tables: size the buffer from layout.ncoefs). Metadata segments are not returned. */
+int rcg_decode_coefs(rcg_ctx* ctx, const uint8_t* jpeg, size_t len, rcg_jpeg_info* info, rcg_coef_layout* layout,
+                     rcg_qtables* tables, int16_t* coefs, size_t coefs_len);
+/* As rcg_decode_coefs with the coefficients written to device memory. */
+int rcg_decode_coefs_device(rcg_ctx* ctx, const uint8_t* jpeg, size_t len, rcg_jpeg_info* info,
+                            rcg_coef_layout* layout, rcg_qtables* tables, int16_t* d_coefs, size_t coefs_len);
+
+/* As rcg_search_requantize with the source and output coefficients in device memory (16-byte aligned), e.g. from
+ * rcg_decode_coefs_device: the JPEG -> JPEG search without host copies of the coefficients. */
+int rcg_search_requantize_device(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                                 const rcg_qtables* in, const int16_t* d_coefs_in, int metric, double target,
+                                 int max_quality, int trellis, rcg_found* found, int16_t* d_coefs_out,
+                                 size_t coefs_len, rcg_qtables* out);
 
 /* Plan write_best for a CoefImage (1 or 3 components): symbol statistics of every candidate scan and of the baseline
  * scan on the GPU, Huffman code lengths, costs and the cheapest script. The caller then writes baseline

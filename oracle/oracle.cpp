@@ -1920,6 +1920,437 @@ static void coef_to_flat(const CoefImage& ci, int16_t* out, uint8_t* qtables) {
   }
 }
 
+// ------------------------------------------------------------------------------------------------ sequential decode
+
+// jpeg/src/decode.rs:16-114 (BitReader): bytes with 0xFF00 stuffing; at a marker (0xFF not followed by 0) or the end
+// of the data it feeds zero bits; restart() drops the buffer and skips to just past the next RSTn.
+struct BitReader {
+  const uint8_t* d;
+  size_t len, pos;
+  uint64_t acc = 0;
+  uint32_t n = 0;
+  bool marker = false;
+  void fill() {
+    while (n <= 56) {
+      uint8_t byte = 0;
+      if (!marker) {
+        if (pos >= len) {
+          marker = true;
+        } else if (d[pos] == 0xFF) {
+          if (pos + 1 < len && d[pos + 1] == 0) {
+            pos += 2;
+            byte = 0xFF;
+          } else {
+            marker = true;
+          }
+        } else {
+          byte = d[pos++];
+        }
+      }
+      acc = (acc << 8) | byte;
+      n += 8;
+    }
+  }
+  uint32_t peek(uint32_t k) {
+    if (n < k) fill();
+    return (uint32_t)((acc >> (n - k)) & ((1ull << k) - 1));
+  }
+  void skip(uint32_t k) { n -= k; }
+  uint32_t bits(uint32_t k) {
+    if (k == 0) return 0;
+    uint32_t v = peek(k);
+    skip(k);
+    return v;
+  }
+  void restart() {
+    acc = 0;
+    n = 0;
+    marker = false;
+    while (pos + 1 < len) {
+      if (d[pos] != 0xFF) {
+        pos++;
+        continue;
+      }
+      uint8_t m = d[pos + 1];
+      if (m == 0) {
+        pos += 2;
+      } else if (m >= 0xD0 && m <= 0xD7) {
+        pos += 2;
+        return;
+      } else {
+        return;
+      }
+    }
+  }
+};
+
+// jpeg/src/decode.rs:117-188 (HuffDec): 9-bit lookup, canonical search for longer codes.
+struct HuffDec {
+  uint16_t fast[512];
+  int mincode[17], maxcode[18], valptr[17];
+  std::vector<uint8_t> vals;
+};
+
+static int huffdec_build(const uint8_t bits[16], const uint8_t* vals, size_t nvals, HuffDec& h) {
+  size_t total = 0;
+  for (int i = 0; i < 16; i++) total += bits[i];
+  if (total > 256 || total > nvals) return 1;
+  std::memset(h.fast, 0, sizeof h.fast);
+  for (int i = 0; i < 17; i++) h.mincode[i] = h.valptr[i] = 0;
+  for (int i = 0; i < 18; i++) h.maxcode[i] = -1;
+  h.vals.assign(vals, vals + total);
+  int code = 0;
+  size_t k = 0;
+  for (int len = 1; len <= 16; len++) {
+    int n = bits[len - 1];
+    h.valptr[len] = (int)k;
+    h.mincode[len] = code;
+    if (n > 0) {
+      if (code + n > (1 << len)) return 1;
+      if (len <= 9)
+        for (int i = 0; i < n; i++) {
+          int c = code + i;
+          uint8_t sym = h.vals[k + i];
+          int shift = 9 - len;
+          for (int f = 0; f < (1 << shift); f++) h.fast[(c << shift) | f] = (uint16_t)((len << 8) | sym);
+        }
+      code += n;
+      k += n;
+      h.maxcode[len] = code - 1;
+    }
+    code <<= 1;
+  }
+  return 0;
+}
+
+static int huff_decode(const HuffDec& h, BitReader& br, int* sym) {
+  uint16_t e = h.fast[br.peek(9)];
+  if (e != 0) {
+    br.skip(e >> 8);
+    *sym = e & 0xFF;
+    return 0;
+  }
+  for (int len = 1; len <= 16; len++) {
+    int code = (int)br.peek(len);
+    if (h.maxcode[len] >= 0 && code <= h.maxcode[len] && code >= h.mincode[len]) {
+      br.skip(len);
+      *sym = h.vals[h.valptr[len] + code - h.mincode[len]];
+      return 0;
+    }
+  }
+  return 1;
+}
+
+static int32_t extend_bits(uint32_t v, uint32_t t) {
+  if (t == 0) return 0;
+  if (v < (1u << (t - 1))) return (int32_t)v - (int32_t)(1u << t) + 1;
+  return (int32_t)v;
+}
+
+// jpeg/src/decode.rs:1480-1507 (decode_sequential)
+static int decode_sequential(BitReader& br, const HuffDec& dc, const HuffDec& ac, int16_t* blk, int32_t* pred) {
+  int t;
+  if (huff_decode(dc, br, &t)) return 1;
+  if (t > 16) return 1;
+  int32_t diff = extend_bits(br.bits((uint32_t)t), (uint32_t)t);
+  *pred = (int32_t)((uint32_t)*pred + (uint32_t)diff);
+  blk[0] = (int16_t)*pred;
+  int k = 1;
+  while (k < 64) {
+    int rs;
+    if (huff_decode(ac, br, &rs)) return 1;
+    int r = rs >> 4, sz = rs & 15;
+    if (sz == 0) {
+      if (r == 15) {
+        k += 16;
+        continue;
+      }
+      break;
+    }
+    k += r;
+    if (k > 63) return 1;
+    blk[k] = (int16_t)extend_bits(br.bits((uint32_t)sz), (uint32_t)sz);
+    k++;
+  }
+  return 0;
+}
+
+struct ParsedComp {
+  uint8_t id = 0;
+  int h = 1, v = 1, tq = 0, blocks_w = 0, blocks_h = 0, real_bw = 0, real_bh = 0;
+  std::vector<int16_t> coefs;
+  bool has_snap = false;
+  uint16_t snap[64] = {0};
+};
+
+// jpeg::decode::parse(data)?.into_coefs() (jpeg/src/decode.rs:397-445, :540-570, :622-697, :906-1103, :1230-1309)
+// for sequential Huffman frames. Returns 0, 1 (invalid) or 2 (unsupported: other frame kinds, 12-bit, RGB-coded,
+// 16-bit tables, four components).
+static int parse_sequential(const uint8_t* d, size_t len, CoefImage& out) {
+  if (len < 4 || d[0] != 0xFF || d[1] != 0xD8) return 1;
+  size_t pos = 2;
+  bool has_qt[4] = {false, false, false, false};
+  uint16_t qt[4][64];
+  bool has_dc[4] = {false, false, false, false}, has_ac[4] = {false, false, false, false};
+  HuffDec dct[4], act[4];
+  std::vector<ParsedComp> comps;
+  int width = 0, height = 0, hmax = 1, vmax = 1, mcus_x = 0, mcus_y = 0;
+  size_t ri = 0;
+  int scans = 0;
+  int adobe = -1;
+  auto be16 = [&](size_t at, size_t* v) -> bool {
+    if (at + 2 > len) return false;
+    *v = ((size_t)d[at] << 8) | d[at + 1];
+    return true;
+  };
+  for (;;) {
+    // next_marker (:623-640)
+    while (pos < len && d[pos] != 0xFF) pos++;
+    while (pos < len && d[pos] == 0xFF) pos++;
+    if (pos >= len) return 1;
+    uint8_t m = d[pos++];
+    if (m == 0 || (m >= 0xD0 && m <= 0xD7)) continue;
+    if (m == 0xD9) break;
+    if (m == 0x01) continue;
+    size_t slen;
+    if (!be16(pos, &slen)) return 1;
+    if (slen < 2 || pos + slen > len) {
+      if (scans > 0) break;
+      return 1;
+    }
+    const uint8_t* b = d + pos + 2;
+    size_t bl = slen - 2;
+    pos += slen;
+    if (m == 0xDB) {
+      while (bl > 0) {
+        int pq = b[0] >> 4, tq = b[0] & 15;
+        if (tq > 3 || pq > 1) return 1;
+        size_t need = 1 + 64 * (size_t)(pq + 1);
+        if (bl < need) return 1;
+        for (int k = 0; k < 64; k++)
+          qt[tq][ZIGZAG[k]] = pq == 0 ? b[1 + k] : (uint16_t)((b[1 + 2 * k] << 8) | b[2 + 2 * k]);
+        has_qt[tq] = true;
+        b += need;
+        bl -= need;
+      }
+    } else if (m == 0xC4) {
+      while (bl > 0) {
+        if (bl < 17) return 1;
+        int tc = b[0] >> 4, th = b[0] & 15;
+        if (tc > 1 || th > 3) return 1;
+        size_t total = 0;
+        for (int i = 0; i < 16; i++) total += b[1 + i];
+        if (bl < 17 + total) return 1;
+        HuffDec& hd = tc == 0 ? dct[th] : act[th];
+        if (huffdec_build(b + 1, b + 17, total, hd)) return 1;
+        (tc == 0 ? has_dc : has_ac)[th] = true;
+        b += 17 + total;
+        bl -= 17 + total;
+      }
+    } else if (m == 0xC0 || m == 0xC1) {
+      if (!comps.empty()) return 2;  // a second frame: hierarchical
+      if (bl < 6) return 1;
+      if (b[0] != 8) return b[0] == 12 ? 2 : 2;
+      height = (b[1] << 8) | b[2];
+      width = (b[3] << 8) | b[4];
+      int nc = b[5];
+      if (width == 0 || height == 0) return 1;
+      if (nc == 4) return 2;
+      if (nc != 1 && nc != 3) return 2;
+      if (bl < 6 + 3 * (size_t)nc) return 1;
+      for (int i = 0; i < nc; i++) {
+        const uint8_t* c = b + 6 + 3 * i;
+        int hs = c[1] >> 4, vs = c[1] & 15;
+        if (hs < 1 || hs > 4 || vs < 1 || vs > 4 || c[2] > 3) return 1;
+        ParsedComp pc;
+        pc.id = c[0];
+        pc.h = nc == 1 ? 1 : hs;
+        pc.v = nc == 1 ? 1 : vs;
+        pc.tq = c[2];
+        comps.push_back(pc);
+      }
+      for (auto& c : comps) {
+        hmax = std::max(hmax, c.h);
+        vmax = std::max(vmax, c.v);
+      }
+      mcus_x = (width + 8 * hmax - 1) / (8 * hmax);
+      mcus_y = (height + 8 * vmax - 1) / (8 * vmax);
+      for (auto& c : comps) {
+        c.blocks_w = mcus_x * c.h;
+        c.blocks_h = mcus_y * c.v;
+        int cw = (width * c.h + hmax - 1) / hmax, chh = (height * c.v + vmax - 1) / vmax;
+        c.real_bw = (cw + 7) / 8;
+        c.real_bh = (chh + 7) / 8;
+        c.coefs.assign((size_t)c.blocks_w * c.blocks_h * 64, 0);
+      }
+    } else if ((m >= 0xC2 && m <= 0xCF && m != 0xC4 && m != 0xC8 && m != 0xCC) || m == 0xDE || m == 0xDF) {
+      return 2;  // progressive, lossless, hierarchical or arithmetic frames
+    } else if (m == 0xDD) {
+      if (bl < 2) return 1;
+      ri = ((size_t)b[0] << 8) | b[1];
+    } else if (m == 0xEE && bl >= 12 && std::memcmp(b, "Adobe", 5) == 0) {
+      adobe = b[11];
+    } else if (m == 0xDA) {
+      if (comps.empty()) return 1;
+      if (bl < 1) return 1;
+      int ns = b[0];
+      if (ns == 0 || ns > (int)comps.size() || bl < 1 + 2 * (size_t)ns + 3) return 1;
+      int idx[4], dci[4], aci[4];
+      for (int i = 0; i < ns; i++) {
+        uint8_t cid = b[1 + 2 * i], t = b[2 + 2 * i];
+        int k = -1;
+        for (size_t j = 0; j < comps.size(); j++)
+          if (comps[j].id == cid) {
+            k = (int)j;
+            break;
+          }
+        if (k < 0) return 1;
+        for (int j = 0; j < i; j++)
+          if (idx[j] == k) return 1;
+        idx[i] = k;
+        dci[i] = (t >> 4) & 3;
+        aci[i] = (t & 15) & 3;
+      }
+      for (int i = 0; i < ns; i++) {
+        ParsedComp& c = comps[idx[i]];
+        if (!c.has_snap && has_qt[c.tq]) {
+          std::memcpy(c.snap, qt[c.tq], sizeof c.snap);
+          c.has_snap = true;
+        }
+        if (!has_dc[dci[i]] || !has_ac[aci[i]]) return 1;
+      }
+      // decode_scan (:1230-1309), sequential Huffman
+      BitReader br{d, len, pos};
+      int32_t pred[4] = {0, 0, 0, 0};
+      bool inter = ns > 1;
+      size_t mx_n = inter ? (size_t)mcus_x : (size_t)comps[idx[0]].real_bw;
+      size_t my_n = inter ? (size_t)mcus_y : (size_t)comps[idx[0]].real_bh;
+      size_t total = mx_n * my_n;
+      for (size_t mcu = 0; mcu < total; mcu++) {
+        if (ri > 0 && mcu > 0 && mcu % ri == 0) {
+          br.restart();
+          for (int i = 0; i < 4; i++) pred[i] = 0;
+        }
+        size_t mx = mcu % mx_n, my = mcu / mx_n;
+        for (int si = 0; si < ns; si++) {
+          ParsedComp& c = comps[idx[si]];
+          int bh = inter ? c.h : 1, bv = inter ? c.v : 1;
+          for (int by = 0; by < bv; by++)
+            for (int bx = 0; bx < bh; bx++) {
+              size_t col = mx * bh + bx, row = my * bv + by;
+              int16_t* blk = &c.coefs[(row * c.blocks_w + col) * 64];
+              if (decode_sequential(br, dct[dci[si]], act[aci[si]], blk, &pred[si])) return 1;
+            }
+        }
+      }
+      pos = br.pos;
+      scans++;
+    }
+  }
+  if (scans == 0 || comps.empty()) return 1;
+  // into_coefs (:540-570)
+  std::vector<uint8_t> ids;
+  for (auto& c : comps) ids.push_back(c.id);
+  bool coded_rgb = comps.size() == 3 && (adobe == 0 || (adobe < 0 && ids[0] == 'R' && ids[1] == 'G' && ids[2] == 'B'));
+  if (coded_rgb) return 2;
+  out.width = width;
+  out.height = height;
+  out.comps.clear();
+  for (int sl = 0; sl < 4; sl++) out.has_q[sl] = false;
+  for (auto& c : comps) {
+    const uint16_t* t = c.has_snap ? c.snap : (has_qt[c.tq] ? qt[c.tq] : nullptr);
+    if (!t) return 1;
+    for (int i = 0; i < 64; i++)
+      if (t[i] > 255 || t[i] == 0) return 2;
+    for (int i = 0; i < 64; i++) out.qtables[c.tq][i] = (uint8_t)t[i];
+    out.has_q[c.tq] = true;
+  }
+  for (auto& c : comps) out.comps.push_back(CoefComponent{c.id, c.h, c.v, c.tq, c.blocks_w, c.blocks_h, c.coefs});
+  return 0;
+}
+
+// A baseline writer with options the reference's writer never uses, for decoder tests only (T.81 restart intervals
+// and one scan per component): the tables and entropy coding of write_jpeg, then DRI/RSTn or per-component SOS.
+static std::vector<uint8_t> write_jpeg_variant(const CoefImage& ci, int restart_interval, bool per_component) {
+  int mx, my;
+  ci.mcus(mx, my);
+  const int nc = (int)ci.comps.size();
+  const int hmax = ci.hv_max_h(), vmax = ci.hv_max_v();
+  std::vector<std::vector<int>> scans;
+  if (per_component) {
+    for (int k = 0; k < nc; k++) scans.push_back({k});
+  } else {
+    std::vector<int> all;
+    for (int k = 0; k < nc; k++) all.push_back(k);
+    scans.push_back(all);
+  }
+  // Visit the blocks of one scan as a decoder would, with the DC predictions reset at every restart.
+  auto visit = [&](const std::vector<int>& sc, auto&& on_restart, auto&& on_block) {
+    int16_t pred[4] = {0, 0, 0, 0};
+    const bool inter = sc.size() > 1;
+    const int nx = inter ? mx : ((ci.width * ci.comps[sc[0]].h + hmax - 1) / hmax + 7) / 8;
+    const int ny = inter ? my : ((ci.height * ci.comps[sc[0]].v + vmax - 1) / vmax + 7) / 8;
+    int rst = 0;
+    for (int m = 0; m < nx * ny; m++) {
+      if (restart_interval > 0 && m > 0 && m % restart_interval == 0) {
+        on_restart(rst++);
+        for (int i = 0; i < 4; i++) pred[i] = 0;
+      }
+      const int x = m % nx, y = m / nx;
+      for (int k : sc) {
+        const CoefComponent& c = ci.comps[k];
+        const int bh = inter ? c.h : 1, bv = inter ? c.v : 1;
+        for (int by = 0; by < bv; by++)
+          for (int bx = 0; bx < bh; bx++) {
+            const size_t bi = (size_t)(y * bv + by) * c.blocks_w + x * bh + bx;
+            on_block(&c.coefs[bi * 64], &pred[k], std::min(k, 1));
+          }
+      }
+    }
+  };
+  // Tables from the statistics of exactly what is written (restart resets change the DC differences).
+  Stats st;
+  for (auto& sc : scans)
+    visit(sc, [](int) {}, [&](const int16_t* blk, int16_t* pred, int tbl) { code_block(st, blk, pred, tbl); });
+  HuffTable dct2[2] = {optimal_table(st.dc[0]), optimal_table(st.dc[1])};
+  HuffTable act2[2] = {optimal_table(st.ac[0]), optimal_table(st.ac[1])};
+  std::vector<uint8_t> out = write_headers(ci, 0xC0);
+  const int ntables = nc == 1 ? 1 : 2;
+  for (int t = 0; t < ntables; t++) {
+    write_dht(out, (uint8_t)t, dct2[t]);
+    write_dht(out, (uint8_t)(0x10 | t), act2[t]);
+  }
+  if (restart_interval > 0) segment(out, 0xDD, {(uint8_t)(restart_interval >> 8), (uint8_t)restart_interval});
+  for (auto& sc : scans) {
+    std::vector<uint8_t> sos{(uint8_t)sc.size()};
+    for (int k : sc) {
+      const uint8_t s = (uint8_t)std::min(k, 1);
+      sos.push_back(ci.comps[k].id);
+      sos.push_back((uint8_t)(s << 4 | s));
+    }
+    sos.push_back(0);
+    sos.push_back(63);
+    sos.push_back(0);
+    segment(out, 0xDA, sos);
+    Writer wr{MsbWriter{}, dct2, act2};
+    visit(
+        sc,
+        [&](int rst) {
+          wr.w.finish();
+          wr.w.out.push_back(0xFF);
+          wr.w.out.push_back((uint8_t)(0xD0 + (rst & 7)));
+          wr.w.acc = 0;
+          wr.w.n = 0;
+        },
+        [&](const int16_t* blk, int16_t* pred, int tbl) { code_block(wr, blk, pred, tbl); });
+    wr.w.finish();
+    out.insert(out.end(), wr.w.out.begin(), wr.w.out.end());
+  }
+  out.push_back(0xFF);
+  out.push_back(0xD9);
+  return out;
+}
+
 }  // namespace orc
 
 extern "C" {
@@ -2175,4 +2606,37 @@ long orc_write_best(int w, int h, int ncomp, const int* hs, const int* vs, const
   return (long)bytes.size();
 }
 
+// parse(data)?.into_coefs() for sequential Huffman JPEGs. Query with coefs_out == NULL: fills w, h, ncomp, layout,
+// ids. Returns 0, 1 (invalid), 2 (unsupported).
+int orc_decode_sequential(const uint8_t* data, long len, int* w, int* h, int* ncomp, int* hs, int* vs, int* bws,
+                          int* bhs, uint8_t* ids, int16_t* coefs_out, int* tq, uint8_t* qtables4, uint8_t* has_q) {
+  orc::CoefImage ci;
+  int rc = orc::parse_sequential(data, (size_t)len, ci);
+  if (rc) return rc;
+  *w = ci.width;
+  *h = ci.height;
+  *ncomp = (int)ci.comps.size();
+  for (size_t i = 0; i < ci.comps.size(); i++) {
+    hs[i] = ci.comps[i].h;
+    vs[i] = ci.comps[i].v;
+    bws[i] = ci.comps[i].blocks_w;
+    bhs[i] = ci.comps[i].blocks_h;
+    ids[i] = ci.comps[i].id;
+  }
+  if (coefs_out) orc::coef_to_flat_tq(ci, coefs_out, tq, qtables4, has_q);
+  return 0;
+}
+
+// Baseline JPEG bytes of a general flat CoefImage, with an optional restart interval and one scan per component
+// (decoder tests). Returns the size; writes at most cap bytes.
+long orc_write_jpeg_variant(int w, int h, int ncomp, const int* hs, const int* vs, const int* bws, const int* bhs,
+                            const int* tq, const uint8_t* qtables4, const uint8_t* has_q, const int16_t* coefs,
+                            int restart_interval, int per_component, uint8_t* out, long cap) {
+  orc::CoefImage ci = orc::coef_from_flat_tq(w, h, ncomp, hs, vs, bws, bhs, tq, qtables4, has_q, coefs);
+  std::vector<uint8_t> bytes = orc::write_jpeg_variant(ci, restart_interval, per_component != 0);
+  if (out) std::memcpy(out, bytes.data(), std::min<size_t>(bytes.size(), (size_t)cap));
+  return (long)bytes.size();
+}
+
 }  // extern "C"
+

@@ -54,6 +54,9 @@ def lib():
         L.orc_write_best_tq.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, P, P, ctypes.c_long, pi]
         L.orc_write_best_tq.restype = ctypes.c_long
         pu64 = ctypes.POINTER(ctypes.c_uint64)
+        L.orc_decode_sequential.argtypes = [P, ctypes.c_long, pi, pi, pi, P, P, P, P, P, P, P, P, P]
+        L.orc_write_jpeg_variant.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, P, i32, i32, P, ctypes.c_long]
+        L.orc_write_jpeg_variant.restype = ctypes.c_long
         L.orc_plan.argtypes = [i32, i32, i32, P, P, P, P, P, pu64, pu64, pi, P, pi, P, P]
         L.orc_round_f32.argtypes = [ctypes.c_float]
         L.orc_round_f32.restype = ctypes.c_int32
@@ -321,4 +324,35 @@ def ms_ssim(a, b, per_scale=False):
     ps = np.zeros(5, np.float64)
     v = lib().orc_ms_ssim(a.ctypes.data, b.ctypes.data, w, h, ch, ps.ctypes.data)
     return (v, ps) if per_scale else v
+
+
+def decode_sequential(data):
+    """parse(data)?.into_coefs() for sequential Huffman JPEGs: (GeneralCoefs, ids) or raises ValueError with
+    "invalid" / "unsupported"."""
+    data = np.frombuffer(bytes(data), np.uint8)
+    w, h, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    hs, vs, bws, bhs = (np.zeros(4, np.int32) for _ in range(4))
+    ids = np.zeros(4, np.uint8)
+    args = lambda *rest: (data.ctypes.data, data.size, ctypes.byref(w), ctypes.byref(h), ctypes.byref(n),
+                          hs.ctypes.data, vs.ctypes.data, bws.ctypes.data, bhs.ctypes.data, ids.ctypes.data) + rest
+    rc = lib().orc_decode_sequential(*args(None, None, None, None))
+    if rc:
+        raise ValueError("invalid" if rc == 1 else "unsupported")
+    k = n.value
+    lay = dict(ncomp=k, h=hs[:k].copy(), v=vs[:k].copy(), blocks_w=bws[:k].copy(), blocks_h=bhs[:k].copy(),
+               ncoefs=int(sum(bws[i] * bhs[i] for i in range(k)) * 64))
+    coefs = np.zeros(lay["ncoefs"], np.int16)
+    tq = np.zeros(4, np.int32)
+    q4 = np.zeros((4, 64), np.uint8)
+    has = np.zeros(4, np.uint8)
+    lib().orc_decode_sequential(*args(coefs.ctypes.data, tq.ctypes.data, q4.ctypes.data, has.ctypes.data))
+    return GeneralCoefs(w.value, h.value, lay, tq[:k], q4, has, coefs), bytes(ids[:k])
+
+
+def write_jpeg_variant(g, restart_interval=0, per_component=False):
+    """Baseline JPEG of a GeneralCoefs with a restart interval and/or one scan per component (decoder tests)."""
+    size = lib().orc_write_jpeg_variant(*g.args(), int(restart_interval), 1 if per_component else 0, None, 0)
+    out = np.zeros(size, np.uint8)
+    lib().orc_write_jpeg_variant(*g.args(), int(restart_interval), 1 if per_component else 0, out.ctypes.data, size)
+    return out.tobytes()
 

@@ -33,6 +33,7 @@ UNITS = {
     "capi.cu": [],
     "plan.cu": [],
     "metrics.cu": [],
+    "jpegdec.cu": [],
 }
 
 

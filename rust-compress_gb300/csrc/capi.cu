@@ -737,10 +737,20 @@ int rcg_reconstruct_tables(rcg_ctx* ctx, uint32_t width, uint32_t height, const 
 
 // ---- search
 
+// An interleaved 8-bit Gray or Rgb image as scale 0 of a linear pyramid.
+static Src8 px8(const uint8_t* p, int channels) {
+  Src8 s;
+  s.p = p;
+  s.ps = channels;
+  s.cs = channels == 3 ? 1 : 0;
+  return s;
+}
+
 // Per-candidate scorer of the device searches: SSIMULACRA2 from the candidate's linear pyramid against the
 // reference's, or SSIM from the candidate's 8-bit pixels against the reference's.
 struct SearchScorer {
   int metric;
+  int channels = 3;
   PyramidDesc pd;
   float* ref_pyr = nullptr;
   float* dist_pyr = nullptr;
@@ -751,12 +761,14 @@ struct SearchScorer {
 
 static int scorer_setup(rcg_ctx* ctx, int metric, int w, int h, int channels, SearchScorer* sc) {
   sc->metric = metric;
+  sc->channels = channels;
   sc->d_score = (double*)workspace(ctx, "score", sizeof(double));
   if (!sc->d_score) return RCG_NO_MEMORY;
-  if (metric == RCG_METRIC_SSIM) {
-    sc->cand_px = (uint8_t*)workspace(ctx, "cand_px", (size_t)w * h * channels);
-    return sc->cand_px ? RCG_OK : RCG_NO_MEMORY;
-  }
+  // Candidates are decoded to 8-bit pixels: SSIM reads them as they are, SSIMULACRA2 takes them as scale 0 of the
+  // candidate's linear pyramid through the sRGB table.
+  sc->cand_px = (uint8_t*)workspace(ctx, "cand_px", (size_t)w * h * channels);
+  if (!sc->cand_px) return RCG_NO_MEMORY;
+  if (metric == RCG_METRIC_SSIM) return RCG_OK;
   sc->pd = make_pyramid(w, h);
   sc->ref_pyr = (float*)workspace(ctx, "ref_pyr", (size_t)sc->pd.floats * sizeof(float));
   sc->dist_pyr = (float*)workspace(ctx, "dist_pyr", (size_t)sc->pd.floats * sizeof(float));
@@ -771,9 +783,10 @@ static void score_candidate(rcg_ctx* ctx, const SearchScorer& sc, StepDesc* d_st
     ssim_score(ctx, sc.ref_px, sc.cand_px, w, h, channels, sc.d_score, d_ss, d_st);
     return;
   }
-  upsample_color(ctx, d_st, planes, w, h, nullptr, sc.dist_pyr);
-  build_pyramid_gated(ctx, sc.pd, sc.dist_pyr, d_st);
-  score_pyramids(ctx, sc.pd, sc.ref_pyr, sc.dist_pyr, sc.d_score, d_ss, d_st);
+  upsample_color(ctx, d_st, planes, w, h, sc.cand_px, nullptr);
+  const Src8 ref8 = px8(sc.ref_px, channels), dist8 = px8(sc.cand_px, channels);
+  build_pyramid_gated(ctx, sc.pd, sc.dist_pyr, d_st, dist8);
+  score_pyramids(ctx, sc.pd, sc.ref_pyr, sc.dist_pyr, sc.d_score, d_ss, d_st, ref8, dist8);
 }
 
 static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, int metric, double target,
@@ -787,12 +800,8 @@ static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int cha
   if ((rc = scorer_setup(ctx, metric, w, h, channels, &sc)) != RCG_OK) return rc;
   // Quality-independent work, once per search: the reference image's linear pyramid (SSIMULACRA2; SSIM reads the
   // source pixels as they are), colour planes, FDCTs.
-  if (metric == RCG_METRIC_SSIM) {
-    sc.ref_px = d_src;
-  } else {
-    if ((rc = to_linear(ctx, d_src, w, h, channels, 8, sc.ref_pyr)) != RCG_OK) return rc;
-    build_pyramid(ctx, sc.pd, sc.ref_pyr);
-  }
+  sc.ref_px = d_src;
+  if (metric != RCG_METRIC_SSIM) build_pyramid(ctx, sc.pd, sc.ref_pyr, px8(d_src, channels));
   EncoderSetup es;
   if ((rc = setup_encoder(ctx, d_src, w, h, channels, subsampling, &es)) != RCG_OK) return rc;
   int max_steps = 1;
@@ -997,11 +1006,14 @@ int rcg_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef
   return finish(ctx, "requantize");
 }
 
-int rcg_search_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
-                          const rcg_qtables* in, const int16_t* coefs_in, int metric, double target, int max_quality,
-                          int trellis, rcg_found* found, int16_t* coefs_out, size_t coefs_len, rcg_qtables* out) {
+static int search_requantize_impl(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                                  const rcg_qtables* in, const int16_t* coefs_in, int metric, double target,
+                                  int max_quality, int trellis, rcg_found* found, int16_t* coefs_out,
+                                  size_t coefs_len, rcg_qtables* out, bool on_device) {
   if (!ctx) return RCG_INVALID;
   if (!layout || !coefs_in || !found) return fail(ctx, RCG_INVALID, "null pointer");
+  if (on_device && ((reinterpret_cast<uintptr_t>(coefs_in) | reinterpret_cast<uintptr_t>(coefs_out)) & 15))
+    return fail(ctx, RCG_INVALID, "device coefficients must be 16-byte aligned");
   if (width == 0 || height == 0 || width > 65535 || height > 65535)
     return fail(ctx, RCG_INVALID, "JPEG dimensions must be 1..=65535");
   int grc = check_goal(ctx, metric, width, height, target);
@@ -1025,19 +1037,19 @@ int rcg_search_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const r
   max_steps = std::min(max_steps, kMaxSteps);
   const int channels = st->ncomp;
   SearchScorer sc;
-  int16_t* d_src = (int16_t*)workspace(ctx, "rq_src", cbytes);
+  int16_t* d_src = on_device ? const_cast<int16_t*>(coefs_in) : (int16_t*)workspace(ctx, "rq_src", cbytes);
   int16_t* slots = (int16_t*)workspace(ctx, "coef_slots", cbytes * max_steps);
   uint8_t* planes = (uint8_t*)workspace(ctx, "dec_planes", (size_t)plane_bytes(st));
-  uint8_t* ref_px = metric == RCG_METRIC_SSIM ? (uint8_t*)workspace(ctx, "ref_px", (size_t)w * h * channels) : nullptr;
+  uint8_t* ref_px = (uint8_t*)workspace(ctx, "ref_px", (size_t)w * h * channels);
   SearchState* d_ss = (SearchState*)workspace(ctx, "search_state", sizeof(SearchState));
   StepDesc* d_st = (StepDesc*)workspace(ctx, "step_search", sizeof(StepDesc));
-  if (!d_src || !slots || !planes || !d_ss || !d_st || (metric == RCG_METRIC_SSIM && !ref_px) ||
+  if (!d_src || !slots || !planes || !d_ss || !d_st || !ref_px ||
       scorer_setup(ctx, metric, w, h, channels, &sc) != RCG_OK) {
     delete st;
     return RCG_NO_MEMORY;
   }
   sc.ref_px = ref_px;
-  if ((rc = copy_to_device(ctx, d_src, coefs_in, cbytes)) != RCG_OK) {
+  if (!on_device && (rc = copy_to_device(ctx, d_src, coefs_in, cbytes)) != RCG_OK) {
     delete st;
     return rc;
   }
@@ -1049,12 +1061,8 @@ int rcg_search_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const r
   st->requant = 1;
   cudaMemcpyAsync(d_st, st, sizeof(StepDesc), cudaMemcpyHostToDevice, ctx->stream);
   dequant_idct(ctx, d_st, d_src, planes, nblocks);
-  if (metric == RCG_METRIC_SSIM) {
-    upsample_color(ctx, d_st, planes, w, h, ref_px, nullptr);
-  } else {
-    upsample_color(ctx, d_st, planes, w, h, nullptr, sc.ref_pyr);
-    build_pyramid(ctx, sc.pd, sc.ref_pyr);
-  }
+  upsample_color(ctx, d_st, planes, w, h, ref_px, nullptr);
+  if (metric != RCG_METRIC_SSIM) build_pyramid(ctx, sc.pd, sc.ref_pyr, px8(ref_px, channels));
   SearchState hs;
   std::memset(&hs, 0, sizeof hs);
   hs.lo = 1;
@@ -1097,7 +1105,10 @@ int rcg_search_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const r
       delete st;
       return fail(ctx, RCG_INVALID, "coefficient buffer too short");
     }
-    if ((rc = copy_to_host(ctx, coefs_out, slots + (size_t)hs.best_step * nblocks * 64, cbytes)) != RCG_OK) {
+    const int16_t* best = slots + (size_t)hs.best_step * nblocks * 64;
+    if (on_device) {
+      cudaMemcpyAsync(coefs_out, best, cbytes, cudaMemcpyDeviceToDevice, ctx->stream);
+    } else if ((rc = copy_to_host(ctx, coefs_out, best, cbytes)) != RCG_OK) {
       delete st;
       return rc;
     }
@@ -1109,6 +1120,21 @@ int rcg_search_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const r
   qtables_out(tq, slot_qt, present, st->ncomp, out);
   delete st;
   return finish(ctx, "search_requantize output");
+}
+
+int rcg_search_requantize(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                          const rcg_qtables* in, const int16_t* coefs_in, int metric, double target, int max_quality,
+                          int trellis, rcg_found* found, int16_t* coefs_out, size_t coefs_len, rcg_qtables* out) {
+  return search_requantize_impl(ctx, width, height, layout, in, coefs_in, metric, target, max_quality, trellis, found,
+                                coefs_out, coefs_len, out, false);
+}
+
+int rcg_search_requantize_device(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
+                                 const rcg_qtables* in, const int16_t* d_coefs_in, int metric, double target,
+                                 int max_quality, int trellis, rcg_found* found, int16_t* d_coefs_out,
+                                 size_t coefs_len, rcg_qtables* out) {
+  return search_requantize_impl(ctx, width, height, layout, in, d_coefs_in, metric, target, max_quality, trellis,
+                                found, d_coefs_out, coefs_len, out, true);
 }
 
 static int plan_common(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coef_layout* layout,
@@ -1157,4 +1183,23 @@ int rcg_plan_device(rcg_ctx* ctx, uint32_t width, uint32_t height, const rcg_coe
   return plan_common(ctx, width, height, layout, d_coefs, 0, true, result);
 }
 
+int rcg_decode_coefs(rcg_ctx* ctx, const uint8_t* jpeg, size_t len, rcg_jpeg_info* info, rcg_coef_layout* layout,
+                     rcg_qtables* tables, int16_t* coefs, size_t coefs_len) {
+  if (!ctx) return RCG_INVALID;
+  if (!jpeg || !layout) return fail(ctx, RCG_INVALID, "null pointer");
+  int rc = jpeg_decode(ctx, jpeg, len, info, layout, tables, coefs, coefs_len, false);
+  if (rc != RCG_OK) return rc;
+  return coefs ? finish(ctx, "decode") : RCG_OK;
+}
+
+int rcg_decode_coefs_device(rcg_ctx* ctx, const uint8_t* jpeg, size_t len, rcg_jpeg_info* info,
+                            rcg_coef_layout* layout, rcg_qtables* tables, int16_t* d_coefs, size_t coefs_len) {
+  if (!ctx) return RCG_INVALID;
+  if (!jpeg || !layout) return fail(ctx, RCG_INVALID, "null pointer");
+  int rc = jpeg_decode(ctx, jpeg, len, info, layout, tables, d_coefs, coefs_len, true);
+  if (rc != RCG_OK) return rc;
+  return d_coefs ? finish(ctx, "decode") : RCG_OK;
+}
+
 }  // extern "C"
+

@@ -1,0 +1,770 @@
+// Entropy decoding of sequential Huffman JPEGs on the GPU: jpeg::decode::parse(data)?.into_coefs()
+// (jpeg/src/decode.rs:397-445, :540-570) for SOF0/SOF1 8-bit frames with 1 or 3 components, any sampling, restart
+// intervals and any number of scans.
+//
+// The host walks the markers (decode.rs:622-697: DQT, DHT, SOF, DRI, SOS, APP14), builds each scan's Huffman tables
+// as they stand when the scan starts, removes the 0xFF00 stuffing and cuts each scan into its restart segments,
+// following the bit reader's rules exactly (decode.rs:16-114): a segment's bits end at the first 0xFF not followed
+// by 0x00, reads past the end give zero bits, and the next segment starts just past the next RSTn (if the marker
+// found there is not an RSTn, that segment and all later ones read zero bits).
+//
+// The device decodes each segment in parallel by self-synchronization. The segment's bits are cut into
+// subsequences of 1024 bits, one thread each. A decoding state at a codeword boundary is (bit position, block of the
+// MCU, next coefficient index). Round after round every thread decodes its subsequence from its current start state
+// and hands the state where it crosses into the next subsequence to its successor; the first subsequence of a
+// segment starts from the exact state, so the states become exact from front to back, and Huffman codes
+// resynchronize after a few codewords, so a couple of rounds settle almost every start. When a round changes
+// nothing, every start is exact; the block counts and DC-difference sums of that round give each subsequence its
+// first block and DC predictions (prefix sums), and a last pass decodes again and writes the coefficients. If the
+// rounds do not settle within a bound, one thread per segment follows the chain of states instead.
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <vector>
+
+#include "rcg_internal.cuh"
+
+namespace rcg {
+
+namespace {
+
+constexpr int kSubBits = 1024;
+constexpr int kMaxRounds = 48;
+constexpr int kMaxMcuBlocks = 48;
+constexpr unsigned long long kMaxPixels = 150000000ull;  // core/src/image.rs:33 (MAX_PIXELS)
+constexpr size_t kMaxScans = 1000;                         // jpeg/src/decode.rs:282 (MAX_SCANS)
+
+const int kZigzag[64] = {0,  1,  8,  16, 9,  2,  3,  10, 17, 24, 32, 25, 18, 11, 4,  5,  12, 19, 26, 33, 40, 48,
+                         41, 34, 27, 20, 13, 6,  7,  14, 21, 28, 35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23,
+                         30, 37, 44, 51, 58, 59, 52, 45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63};
+
+// A Huffman table for decoding (decode.rs:117-188): 9-bit lookup (length << 8 | symbol, 0 = longer code), then the
+// canonical search over lengths 10..16.
+struct DevHuff {
+  uint16_t fast[512];
+  int32_t mincode[17];
+  int32_t maxcode[18];
+  int32_t valptr[17];
+  uint8_t vals[256];
+};
+
+// decode.rs:126-166 (HuffDec::new). Returns false for an oversubscribed or overlong table.
+bool build_huff(const uint8_t bits[16], const uint8_t* vals, size_t nvals, DevHuff* h) {
+  size_t total = 0;
+  for (int i = 0; i < 16; i++) total += bits[i];
+  if (total > 256 || total > nvals) return false;
+  std::memset(h, 0, sizeof *h);
+  for (int i = 0; i < 18; i++) h->maxcode[i] = -1;
+  std::memcpy(h->vals, vals, total);
+  int code = 0;
+  int k = 0;
+  for (int len = 1; len <= 16; len++) {
+    const int n = bits[len - 1];
+    h->valptr[len] = k;
+    h->mincode[len] = code;
+    if (n > 0) {
+      if (code + n > (1 << len)) return false;
+      if (len <= 9)
+        for (int i = 0; i < n; i++) {
+          const int c = code + i, shift = 9 - len;
+          for (int f = 0; f < (1 << shift); f++) h->fast[(c << shift) | f] = (uint16_t)((len << 8) | h->vals[k + i]);
+        }
+      code += n;
+      k += n;
+      h->maxcode[len] = code - 1;
+    }
+    code <<= 1;
+  }
+  return true;
+}
+
+struct Segment {
+  long long byte0;    // first destuffed byte of the segment in the scan's buffer
+  long long nbytes;   // destuffed bytes of the segment (reads beyond give zeros)
+  long long block0;   // first block of the segment in the scan's visiting order
+  long long nblocks;  // blocks the segment decodes
+  long long sub0;     // first subsequence of the segment
+  int nsub;
+};
+
+struct ScanDesc {
+  int ns;                     // components in the scan
+  int bmcu;                   // blocks per MCU (1 for a single-component scan)
+  int mcus_x;                 // MCUs per row
+  int mcu_si[kMaxMcuBlocks];  // scan component of each block of the MCU
+  int mcu_dy[kMaxMcuBlocks], mcu_dx[kMaxMcuBlocks];
+  int comp[4];                // frame component of each scan component
+  int dc[4], ac[4];           // table slot of each scan component
+  CompDesc fc[3];             // frame components (block grids, offsets)
+  int nseg;
+  long long nsub;
+};
+
+struct SubState {
+  long long bit;  // segment-relative bit position of a codeword boundary
+  int u;          // block of the MCU
+  int k;          // next coefficient (0: the DC)
+};
+
+struct SubCount {
+  long long blocks;  // blocks completed
+  uint32_t dc[4];    // sums of DC differences per scan component (wrapping, as the reference's i32 predictor)
+};
+
+struct Reader {
+  const uint8_t* p;
+  long long len, next;
+  uint64_t buf;
+  int n;
+  long long bit;
+  __device__ void init(const uint8_t* base, long long nbytes, long long at) {
+    p = base;
+    len = nbytes;
+    next = at >> 3;
+    buf = 0;
+    n = 0;
+    bit = at;
+    refill();
+    skip((int)(at & 7));
+    bit = at;
+  }
+  __device__ __forceinline__ void refill() {
+    while (n <= 56) {
+      const uint64_t byte = next < len ? p[next] : 0;
+      next++;
+      buf |= byte << (56 - n);
+      n += 8;
+    }
+  }
+  __device__ __forceinline__ uint32_t peek(int k) {
+    if (n < k) refill();
+    return (uint32_t)(buf >> (64 - k));
+  }
+  __device__ __forceinline__ void skip(int k) {
+    buf <<= k;
+    n -= k;
+    bit += k;
+  }
+  __device__ __forceinline__ uint32_t bits(int k) {
+    if (k == 0) return 0;
+    const uint32_t v = peek(k);
+    skip(k);
+    return v;
+  }
+};
+
+__device__ __forceinline__ int huff_decode(const DevHuff& h, Reader& r) {
+  const uint16_t e = h.fast[r.peek(9)];
+  if (e != 0) {
+    r.skip(e >> 8);
+    return e & 0xFF;
+  }
+  const uint32_t w = r.peek(16);
+  for (int len = 10; len <= 16; len++) {
+    const int code = (int)(w >> (16 - len));
+    if (h.maxcode[len] >= 0 && code <= h.maxcode[len] && code >= h.mincode[len]) {
+      r.skip(len);
+      return h.vals[h.valptr[len] + code - h.mincode[len]];
+    }
+  }
+  return -1;
+}
+
+__device__ __forceinline__ int extend_bits(uint32_t v, int t) {
+  if (t == 0) return 0;
+  return v < (1u << (t - 1)) ? (int)v - (1 << t) + 1 : (int)v;
+}
+
+struct Tables {
+  DevHuff dc[4], ac[4];
+};
+
+// Decodes from `st` until the bit position reaches `stop_bit` or `max_blocks` blocks are complete. WRITE: also
+// stores the coefficients of block `block_base + blocks` onward (zigzag order), with DC predictors `pred`.
+// Returns 0, or 1 on a bad code (decode.rs:1482-1506).
+template <bool WRITE>
+__device__ int decode_run(const Tables& tb, const ScanDesc& sd, Reader& r, SubState& st, long long stop_bit,
+                          long long max_blocks, SubCount& cnt, long long block_base, uint32_t* pred,
+                          int16_t* __restrict__ out) {
+  int u = st.u, k = st.k;
+  int16_t* blk = nullptr;
+  auto block_ptr = [&](long long b) -> int16_t* {
+    const long long mcu = b / sd.bmcu;
+    const int uu = (int)(b - mcu * sd.bmcu);
+    const int si = sd.mcu_si[uu];
+    const CompDesc& c = sd.fc[sd.comp[si]];
+    const long long my = mcu / sd.mcus_x, mx = mcu - my * sd.mcus_x;
+    const long long row = my * (sd.bmcu == 1 ? 1 : c.v) + sd.mcu_dy[uu];
+    const long long col = mx * (sd.bmcu == 1 ? 1 : c.h) + sd.mcu_dx[uu];
+    return out + (c.blk0 + row * c.bw + col) * 64;
+  };
+  if (WRITE && cnt.blocks < max_blocks) blk = block_ptr(block_base + cnt.blocks);
+  int err = 0;
+  while (cnt.blocks < max_blocks && r.bit < stop_bit) {
+    const int si = sd.mcu_si[u];
+    if (k == 0) {
+      const int t = huff_decode(tb.dc[sd.dc[si]], r);
+      if (t < 0 || t > 16) {
+        err = 1;
+        break;
+      }
+      const int diff = extend_bits(r.bits(t), t);
+      cnt.dc[si] += (uint32_t)diff;
+      if (WRITE) {
+        pred[si] += (uint32_t)diff;
+        blk[0] = (int16_t)pred[si];
+      }
+      k = 1;
+      continue;
+    }
+    const int rs = huff_decode(tb.ac[sd.ac[si]], r);
+    if (rs < 0) {
+      err = 1;
+      break;
+    }
+    const int run = rs >> 4, sz = rs & 15;
+    bool end = false;
+    if (sz == 0) {
+      if (run == 15) {
+        k += 16;
+        end = k >= 64;
+      } else {
+        end = true;
+      }
+    } else {
+      k += run;
+      if (k > 63) {
+        err = 1;
+        break;
+      }
+      const int v = extend_bits(r.bits(sz), sz);
+      if (WRITE) blk[k] = (int16_t)v;
+      k++;
+      end = k >= 64;
+    }
+    if (end) {
+      k = 0;
+      u = u + 1 == sd.bmcu ? 0 : u + 1;
+      cnt.blocks++;
+      if (WRITE && cnt.blocks < max_blocks) blk = block_ptr(block_base + cnt.blocks);
+    }
+  }
+  st.bit = r.bit;
+  st.u = u;
+  st.k = k;
+  return err;
+}
+
+struct SubRef {
+  int seg;
+  int local;  // subsequence index within the segment
+};
+
+__device__ __forceinline__ SubRef find_sub(const Segment* segs, int nseg, long long t) {
+  int lo = 0, hi = nseg - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (segs[mid].sub0 <= t)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return {lo, (int)(t - segs[lo].sub0)};
+}
+
+__device__ __forceinline__ void load_tables(Tables& sh, const Tables* g) {
+  const int4* src = reinterpret_cast<const int4*>(g);
+  int4* dst = reinterpret_cast<int4*>(&sh);
+  for (int i = threadIdx.x; i < (int)(sizeof(Tables) / 16); i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+}
+
+// One round: every non-final subsequence decodes from its current start and proposes its successor's start.
+__global__ void __launch_bounds__(128) k_seq_sync(const ScanDesc* __restrict__ sdp, const Tables* __restrict__ tg,
+                                                  const Segment* __restrict__ segs, const uint8_t* __restrict__ data,
+                                                  const SubState* __restrict__ cur, SubState* __restrict__ nxt,
+                                                  SubCount* __restrict__ counts, int* __restrict__ changed) {
+  __shared__ __align__(16) Tables tb;
+  __shared__ ScanDesc sd;
+  if (threadIdx.x == 0) sd = *sdp;
+  load_tables(tb, tg);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= sd.nsub) return;
+  const SubRef ref = find_sub(segs, sd.nseg, t);
+  const Segment& sg = segs[ref.seg];
+  if (ref.local == 0) nxt[t] = SubState{0, 0, 0};
+  if (ref.local + 1 >= sg.nsub) return;  // the last subsequence proposes nothing
+  SubState st = cur[t];
+  SubCount cnt{};
+  Reader r;
+  r.init(data + sg.byte0, sg.nbytes, st.bit);
+  const long long stop = (long long)(ref.local + 1) * kSubBits;
+  if (decode_run<false>(tb, sd, r, st, stop, LLONG_MAX, cnt, 0, nullptr, nullptr)) {
+    st = SubState{stop, 0, 0};  // desynchronized: any guess will do
+  }
+  counts[t] = cnt;
+  nxt[t + 1] = st;
+  const SubState& old = cur[t + 1];
+  if (old.bit != st.bit || old.u != st.u || old.k != st.k) atomicOr(changed, 1);
+}
+
+// Fallback when the rounds do not settle: one thread per segment follows the chain of exact states.
+__global__ void k_seq_chain(const ScanDesc* __restrict__ sdp, const Tables* __restrict__ tg,
+                            const Segment* __restrict__ segs, const uint8_t* __restrict__ data,
+                            SubState* __restrict__ states, SubCount* __restrict__ counts) {
+  __shared__ __align__(16) Tables tb;
+  __shared__ ScanDesc sd;
+  if (threadIdx.x == 0) sd = *sdp;
+  load_tables(tb, tg);
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < sd.nseg; s += gridDim.x * blockDim.x) {
+    const Segment& sg = segs[s];
+    SubState st{0, 0, 0};
+    for (int i = 0; i + 1 < sg.nsub; i++) {
+      states[sg.sub0 + i] = st;
+      SubCount cnt{};
+      Reader r;
+      r.init(data + sg.byte0, sg.nbytes, st.bit);
+      const long long stop = (long long)(i + 1) * kSubBits;
+      if (decode_run<false>(tb, sd, r, st, stop, LLONG_MAX, cnt, 0, nullptr, nullptr)) st = SubState{stop, 0, 0};
+      counts[sg.sub0 + i] = cnt;
+    }
+    states[sg.sub0 + sg.nsub - 1] = st;
+  }
+}
+
+// Per segment, exclusive prefix sums of the block counts and DC sums over its subsequences (one thread per segment;
+// segments hold few subsequences on average, and a scan without restarts is one segment handled by a CTA-wide
+// scan below).
+__global__ void __launch_bounds__(1024) k_seq_prefix(const ScanDesc* __restrict__ sdp, const Segment* __restrict__ segs,
+                                                     const SubCount* __restrict__ counts, SubCount* __restrict__ base) {
+  __shared__ long long sb[1024];
+  __shared__ uint32_t sdc[4][1024];
+  const ScanDesc& sd = *sdp;
+  for (int s = blockIdx.x; s < sd.nseg; s += gridDim.x) {
+    const Segment& sg = segs[s];
+    long long carry_b = 0;
+    uint32_t carry_dc[4] = {0, 0, 0, 0};
+    for (int off = 0; off < sg.nsub; off += 1024) {
+      const int i = off + threadIdx.x;
+      // subsequence i starts after subsequences 0..i-1: shift by one (the last subsequence's counts are unused)
+      SubCount c{};
+      if (i >= 1 && i < sg.nsub) c = counts[sg.sub0 + i - 1];
+      sb[threadIdx.x] = c.blocks;
+      for (int q = 0; q < 4; q++) sdc[q][threadIdx.x] = c.dc[q];
+      __syncthreads();
+      for (int o = 1; o < 1024; o <<= 1) {
+        long long vb = threadIdx.x >= o ? sb[threadIdx.x - o] : 0;
+        uint32_t vd[4];
+        for (int q = 0; q < 4; q++) vd[q] = threadIdx.x >= o ? sdc[q][threadIdx.x - o] : 0;
+        __syncthreads();
+        sb[threadIdx.x] += vb;
+        for (int q = 0; q < 4; q++) sdc[q][threadIdx.x] += vd[q];
+        __syncthreads();
+      }
+      if (i < sg.nsub) {
+        SubCount o;
+        o.blocks = carry_b + sb[threadIdx.x];
+        for (int q = 0; q < 4; q++) o.dc[q] = carry_dc[q] + sdc[q][threadIdx.x];
+        base[sg.sub0 + i] = o;
+      }
+      carry_b += sb[1023];
+      for (int q = 0; q < 4; q++) carry_dc[q] += sdc[q][1023];
+      __syncthreads();
+    }
+  }
+}
+
+// Final pass: decode each subsequence from its exact start and write the coefficients.
+__global__ void __launch_bounds__(128) k_seq_write(const ScanDesc* __restrict__ sdp, const Tables* __restrict__ tg,
+                                                   const Segment* __restrict__ segs, const uint8_t* __restrict__ data,
+                                                   const SubState* __restrict__ states,
+                                                   const SubCount* __restrict__ base, int16_t* __restrict__ out,
+                                                   int* __restrict__ error) {
+  __shared__ __align__(16) Tables tb;
+  __shared__ ScanDesc sd;
+  if (threadIdx.x == 0) sd = *sdp;
+  load_tables(tb, tg);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= sd.nsub) return;
+  const SubRef ref = find_sub(segs, sd.nseg, t);
+  const Segment& sg = segs[ref.seg];
+  const SubCount b = base[t];
+  if (b.blocks >= sg.nblocks) return;  // past the segment's last block: padding
+  SubState st = states[t];
+  if (st.u != (int)((sg.block0 + b.blocks) % sd.bmcu)) {
+    atomicCAS(error, 0, 2);  // inconsistent start (cannot happen for exact states)
+    return;
+  }
+  SubCount cnt{};
+  uint32_t pred[4] = {b.dc[0], b.dc[1], b.dc[2], b.dc[3]};
+  Reader r;
+  r.init(data + sg.byte0, sg.nbytes, st.bit);
+  const long long stop = ref.local + 1 < sg.nsub ? (long long)(ref.local + 1) * kSubBits : LLONG_MAX;
+  if (decode_run<true>(tb, sd, r, st, stop, sg.nblocks - b.blocks, cnt, sg.block0 + b.blocks, pred, out))
+    atomicCAS(error, 0, 1);
+}
+
+struct HostComp {
+  uint8_t id;
+  int h, v, tq, bw, bh, real_bw, real_bh;
+  bool snap = false;
+  uint16_t snapq[64];
+};
+
+struct HostScan {
+  ScanDesc sd;
+  Tables tables;
+  std::vector<Segment> segs;
+  std::vector<uint8_t> bytes;  // destuffed segments
+};
+
+struct Parsed {
+  int width = 0, height = 0;
+  std::vector<HostComp> comps;
+  std::vector<HostScan> scans;
+  uint8_t qt8[4][64];
+  int present[4] = {0, 0, 0, 0};
+  int tq[3] = {0, 0, 0};
+};
+
+// Destuffed bytes of one segment starting at `pos`: until the first 0xFF not followed by 0x00 (or the end).
+// Returns the position of that 0xFF (or len).
+size_t destuff(const uint8_t* d, size_t len, size_t pos, std::vector<uint8_t>& out) {
+  for (;;) {
+    const void* f = pos < len ? std::memchr(d + pos, 0xFF, len - pos) : nullptr;
+    const size_t ff = f ? (size_t)((const uint8_t*)f - d) : len;
+    out.insert(out.end(), d + pos, d + ff);
+    if (ff >= len) return len;
+    if (ff + 1 < len && d[ff + 1] == 0) {
+      out.push_back(0xFF);
+      pos = ff + 2;
+      continue;
+    }
+    return ff;
+  }
+}
+
+int fail_parse(rcg_ctx* ctx, int status, const char* msg) { return fail(ctx, status, msg); }
+
+// The host part of parse() (decode.rs:622-697, :906-1103) for sequential Huffman frames.
+int parse_jpeg(rcg_ctx* ctx, const uint8_t* d, size_t len, Parsed& P) {
+  if (len < 4 || d[0] != 0xFF || d[1] != 0xD8) return fail_parse(ctx, RCG_INVALID, "not a JPEG file");
+  size_t pos = 2;
+  bool has_qt[4] = {false, false, false, false};
+  uint16_t qt[4][64];
+  bool has_dc[4] = {false, false, false, false}, has_ac[4] = {false, false, false, false};
+  DevHuff dct[4], act[4];
+  int hmax = 1, vmax = 1, mcus_x = 0, mcus_y = 0;
+  size_t ri = 0;
+  int adobe = -1;
+  for (;;) {
+    while (pos < len && d[pos] != 0xFF) pos++;
+    while (pos < len && d[pos] == 0xFF) pos++;
+    if (pos >= len) return fail_parse(ctx, RCG_INVALID, "unexpected end of JPEG");
+    const uint8_t m = d[pos++];
+    if (m == 0 || (m >= 0xD0 && m <= 0xD7) || m == 0x01) continue;
+    if (m == 0xD9) break;
+    if (pos + 2 > len) return fail_parse(ctx, RCG_INVALID, "unexpected end of JPEG");
+    const size_t slen = ((size_t)d[pos] << 8) | d[pos + 1];
+    if (slen < 2 || pos + slen > len) {
+      if (!P.scans.empty()) break;
+      return fail_parse(ctx, RCG_INVALID, "truncated JPEG segment");
+    }
+    const uint8_t* b = d + pos + 2;
+    size_t bl = slen - 2;
+    pos += slen;
+    if (m == 0xDB) {
+      while (bl > 0) {
+        const int pq = b[0] >> 4, t = b[0] & 15;
+        if (t > 3 || pq > 1) return fail_parse(ctx, RCG_INVALID, "bad DQT");
+        const size_t need = 1 + 64 * (size_t)(pq + 1);
+        if (bl < need) return fail_parse(ctx, RCG_INVALID, "truncated DQT");
+        for (int k = 0; k < 64; k++)
+          qt[t][kZigzag[k]] = pq == 0 ? b[1 + k] : (uint16_t)((b[1 + 2 * k] << 8) | b[2 + 2 * k]);
+        has_qt[t] = true;
+        b += need;
+        bl -= need;
+      }
+    } else if (m == 0xC4) {
+      while (bl > 0) {
+        if (bl < 17) return fail_parse(ctx, RCG_INVALID, "truncated DHT");
+        const int tc = b[0] >> 4, th = b[0] & 15;
+        if (tc > 1 || th > 3) return fail_parse(ctx, RCG_INVALID, "bad DHT");
+        size_t total = 0;
+        for (int i = 0; i < 16; i++) total += b[1 + i];
+        if (bl < 17 + total) return fail_parse(ctx, RCG_INVALID, "truncated DHT");
+        if (!build_huff(b + 1, b + 17, total, tc == 0 ? &dct[th] : &act[th]))
+          return fail_parse(ctx, RCG_INVALID, "bad JPEG huffman table");
+        (tc == 0 ? has_dc : has_ac)[th] = true;
+        b += 17 + total;
+        bl -= 17 + total;
+      }
+    } else if (m == 0xC0 || m == 0xC1) {
+      if (!P.comps.empty()) return fail_parse(ctx, RCG_INVALID, "multiple SOF markers");
+      if (bl < 6) return fail_parse(ctx, RCG_INVALID, "bad SOF");
+      if (b[0] != 8) return fail_parse(ctx, RCG_UNSUPPORTED, "only 8-bit JPEGs are decoded on the GPU");
+      P.height = (b[1] << 8) | b[2];
+      P.width = (b[3] << 8) | b[4];
+      const int nc = b[5];
+      if (P.width == 0 || P.height == 0) return fail_parse(ctx, RCG_INVALID, "zero JPEG dimension (DNL not supported)");
+      if ((unsigned long long)P.width * (unsigned long long)P.height > kMaxPixels)
+        return fail_parse(ctx, RCG_INVALID, "unreasonable image dimensions");
+      if (nc != 1 && nc != 3) return fail_parse(ctx, RCG_UNSUPPORTED, "only 1- or 3-component JPEGs are decoded");
+      if (bl < 6 + 3 * (size_t)nc) return fail_parse(ctx, RCG_INVALID, "bad SOF");
+      for (int i = 0; i < nc; i++) {
+        const uint8_t* c = b + 6 + 3 * i;
+        const int hs = c[1] >> 4, vs = c[1] & 15;
+        if (hs < 1 || hs > 4 || vs < 1 || vs > 4 || c[2] > 3)
+          return fail_parse(ctx, RCG_INVALID, "bad component description");
+        HostComp hc;
+        hc.id = c[0];
+        hc.h = nc == 1 ? 1 : hs;
+        hc.v = nc == 1 ? 1 : vs;
+        hc.tq = c[2];
+        P.comps.push_back(hc);
+      }
+      for (auto& c : P.comps) {
+        hmax = std::max(hmax, c.h);
+        vmax = std::max(vmax, c.v);
+      }
+      mcus_x = (P.width + 8 * hmax - 1) / (8 * hmax);
+      mcus_y = (P.height + 8 * vmax - 1) / (8 * vmax);
+      for (auto& c : P.comps) {
+        c.bw = mcus_x * c.h;
+        c.bh = mcus_y * c.v;
+        c.real_bw = ((P.width * c.h + hmax - 1) / hmax + 7) / 8;
+        c.real_bh = ((P.height * c.v + vmax - 1) / vmax + 7) / 8;
+      }
+    } else if ((m >= 0xC2 && m <= 0xCF && m != 0xC4 && m != 0xC8 && m != 0xCC) || m == 0xDE || m == 0xDF) {
+      return fail_parse(ctx, RCG_UNSUPPORTED,
+                        "progressive, lossless, hierarchical and arithmetic JPEGs are decoded on the host");
+    } else if (m == 0xDD) {
+      if (bl < 2) return fail_parse(ctx, RCG_INVALID, "bad DRI");
+      ri = ((size_t)b[0] << 8) | b[1];
+    } else if (m == 0xEE && bl >= 12 && std::memcmp(b, "Adobe", 5) == 0) {
+      adobe = b[11];
+    } else if (m == 0xDA) {
+      if (P.scans.size() >= kMaxScans) return fail_parse(ctx, RCG_UNSUPPORTED, "too many scans in a JPEG frame");
+      if (P.comps.empty()) return fail_parse(ctx, RCG_INVALID, "SOS before SOF");
+      if (bl < 1) return fail_parse(ctx, RCG_INVALID, "bad SOS");
+      const int ns = b[0];
+      if (ns == 0 || ns > (int)P.comps.size() || bl < 1 + 2 * (size_t)ns + 3)
+        return fail_parse(ctx, RCG_INVALID, "bad SOS");
+      HostScan sc;
+      std::memset(&sc.sd, 0, sizeof sc.sd);
+      std::memset(&sc.tables, 0, sizeof sc.tables);
+      sc.sd.ns = ns;
+      for (int i = 0; i < ns; i++) {
+        const uint8_t cid = b[1 + 2 * i], t = b[2 + 2 * i];
+        int k = -1;
+        for (size_t j = 0; j < P.comps.size(); j++)
+          if (P.comps[j].id == cid) {
+            k = (int)j;
+            break;
+          }
+        if (k < 0) return fail_parse(ctx, RCG_INVALID, "SOS references unknown component");
+        for (int j = 0; j < i; j++)
+          if (sc.sd.comp[j] == k) return fail_parse(ctx, RCG_INVALID, "duplicate component in scan");
+        sc.sd.comp[i] = k;
+        sc.sd.dc[i] = (t >> 4) & 3;
+        sc.sd.ac[i] = (t & 15) & 3;
+      }
+      for (int i = 0; i < ns; i++) {
+        HostComp& c = P.comps[sc.sd.comp[i]];
+        if (!c.snap && has_qt[c.tq]) {
+          std::memcpy(c.snapq, qt[c.tq], sizeof c.snapq);
+          c.snap = true;
+        }
+        if (!has_dc[sc.sd.dc[i]] || !has_ac[sc.sd.ac[i]])
+          return fail_parse(ctx, RCG_INVALID, "scan uses undefined huffman table");
+        sc.tables.dc[sc.sd.dc[i]] = dct[sc.sd.dc[i]];
+        sc.tables.ac[sc.sd.ac[i]] = act[sc.sd.ac[i]];
+      }
+      // MCU pattern and geometry (decode.rs:1251-1258, :1270-1275)
+      const bool inter = ns > 1;
+      int bm = 0;
+      for (int i = 0; i < ns; i++) {
+        const HostComp& c = P.comps[sc.sd.comp[i]];
+        const int bh = inter ? c.h : 1, bv = inter ? c.v : 1;
+        for (int by = 0; by < bv; by++)
+          for (int bx = 0; bx < bh; bx++) {
+            if (bm >= kMaxMcuBlocks) return fail_parse(ctx, RCG_UNSUPPORTED, "MCU too large");
+            sc.sd.mcu_si[bm] = i;
+            sc.sd.mcu_dy[bm] = by;
+            sc.sd.mcu_dx[bm] = bx;
+            bm++;
+          }
+      }
+      sc.sd.bmcu = bm;
+      const long long nx = inter ? mcus_x : P.comps[sc.sd.comp[0]].real_bw;
+      const long long ny = inter ? mcus_y : P.comps[sc.sd.comp[0]].real_bh;
+      sc.sd.mcus_x = (int)nx;
+      const long long total = nx * ny;
+      // Restart segments as the bit reader sees them (decode.rs:90-114): each ends at the first 0xFF not followed
+      // by 0x00; the next starts past an RSTn found there, else it (and every later one) reads zero bits.
+      const long long seg_mcus = ri > 0 ? (long long)ri : total;
+      const long long nseg = (total + seg_mcus - 1) / seg_mcus;
+      size_t p = pos;
+      bool dead = false;
+      long long sub = 0;
+      for (long long s = 0; s < nseg; s++) {
+        Segment g;
+        g.byte0 = (long long)sc.bytes.size();
+        g.block0 = s * seg_mcus * bm;
+        g.nblocks = std::min(seg_mcus, total - s * seg_mcus) * bm;
+        if (s > 0 && !dead) {
+          // restart(): past an RSTn at p, else stay (a different marker: zero bits from here on)
+          if (p + 1 < len && d[p] == 0xFF && d[p + 1] >= 0xD0 && d[p + 1] <= 0xD7)
+            p += 2;
+          else
+            dead = true;
+        }
+        if (!dead) p = destuff(d, len, p, sc.bytes);
+        g.nbytes = (long long)sc.bytes.size() - g.byte0;
+        g.nsub = (int)std::max<long long>(1, (g.nbytes * 8 + kSubBits - 1) / kSubBits);
+        g.sub0 = sub;
+        sub += g.nsub;
+        sc.segs.push_back(g);
+        // keep segments 4-byte aligned in the buffer
+        while (sc.bytes.size() % 4) sc.bytes.push_back(0);
+      }
+      sc.sd.nseg = (int)nseg;
+      sc.sd.nsub = sub;
+      pos = p;  // the marker search resumes where the entropy data stopped (decode.rs:1100-1101)
+      P.scans.push_back(std::move(sc));
+    }
+  }
+  if (P.scans.empty() || P.comps.empty()) return fail_parse(ctx, RCG_INVALID, "JPEG contains no image data");
+  // into_coefs (decode.rs:540-570)
+  if (P.comps.size() == 3 && (adobe == 0 || (adobe < 0 && P.comps[0].id == 'R' && P.comps[1].id == 'G' &&
+                                             P.comps[2].id == 'B')))
+    return fail_parse(ctx, RCG_UNSUPPORTED, "RGB-coded JPEG");
+  for (size_t i = 0; i < P.comps.size(); i++) {
+    const HostComp& c = P.comps[i];
+    const uint16_t* t = c.snap ? c.snapq : (has_qt[c.tq] ? qt[c.tq] : nullptr);
+    if (!t) return fail_parse(ctx, RCG_INVALID, "missing quantization table");
+    for (int n = 0; n < 64; n++)
+      if (t[n] > 255 || t[n] == 0) return fail_parse(ctx, RCG_UNSUPPORTED, "16-bit quantization table");
+    for (int n = 0; n < 64; n++) P.qt8[c.tq][n] = (uint8_t)t[n];
+    P.present[c.tq] = 1;
+    P.tq[i] = c.tq;
+  }
+  return RCG_OK;
+}
+
+}  // namespace
+
+int jpeg_decode(rcg_ctx* ctx, const uint8_t* data, size_t len, rcg_jpeg_info* info, rcg_coef_layout* layout,
+                rcg_qtables* tables, int16_t* coefs, size_t coefs_len, bool coefs_on_device) {
+  Parsed P;
+  int rc = parse_jpeg(ctx, data, len, P);
+  if (rc != RCG_OK) return rc;
+  const int nc = (int)P.comps.size();
+  std::memset(layout, 0, sizeof *layout);
+  layout->ncomp = nc;
+  long long nblocks = 0;
+  CompDesc fc[3];
+  std::memset(fc, 0, sizeof fc);
+  for (int i = 0; i < nc; i++) {
+    const HostComp& c = P.comps[i];
+    layout->h[i] = c.h;
+    layout->v[i] = c.v;
+    layout->blocks_w[i] = c.bw;
+    layout->blocks_h[i] = c.bh;
+    fc[i].bw = c.bw;
+    fc[i].bh = c.bh;
+    fc[i].h = c.h;
+    fc[i].v = c.v;
+    fc[i].cls = i == 0 ? 0 : 1;
+    fc[i].blk0 = nblocks;
+    nblocks += (long long)c.bw * c.bh;
+  }
+  layout->ncoefs = nblocks * 64;
+  if (info) {
+    std::memset(info, 0, sizeof *info);
+    info->width = (uint32_t)P.width;
+    info->height = (uint32_t)P.height;
+    for (int i = 0; i < nc; i++) info->ids[i] = P.comps[i].id;
+    info->scans = (int)P.scans.size();
+  }
+  if (tables) {
+    std::memset(tables, 0, sizeof *tables);
+    for (int i = 0; i < nc; i++) tables->tq[i] = P.tq[i];
+    for (int s = 0; s < 4; s++) {
+      tables->present[s] = P.present[s];
+      if (P.present[s]) std::memcpy(tables->qtables[s], P.qt8[s], 64);
+    }
+  }
+  if (!coefs) return RCG_OK;
+  if ((long long)coefs_len < nblocks * 64) return fail(ctx, RCG_INVALID, "coefficient buffer too short");
+  cudaSetDevice(ctx->device);
+  int16_t* d_out = coefs_on_device ? coefs : (int16_t*)workspace(ctx, "dec_coefs", (size_t)nblocks * 128);
+  int* d_err = (int*)workspace(ctx, "dec_error", sizeof(int) * 4);
+  ScanDesc* d_sd = (ScanDesc*)workspace(ctx, "dec_scan", sizeof(ScanDesc));
+  Tables* d_tab = (Tables*)workspace(ctx, "dec_tables", sizeof(Tables));
+  if (!d_out || !d_err || !d_sd || !d_tab) return RCG_NO_MEMORY;
+  cudaMemsetAsync(d_out, 0, (size_t)nblocks * 128, ctx->stream);
+  cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream);
+  int h_changed = 0;
+  for (HostScan& sc : P.scans) {
+    std::memcpy(sc.sd.fc, fc, sizeof fc);
+    const long long nsub = sc.sd.nsub;
+    uint8_t* d_bytes = (uint8_t*)workspace(ctx, "dec_bytes", std::max<size_t>(sc.bytes.size(), 16));
+    Segment* d_segs = (Segment*)workspace(ctx, "dec_segs", sizeof(Segment) * sc.segs.size());
+    SubState* d_s0 = (SubState*)workspace(ctx, "dec_state0", sizeof(SubState) * (size_t)nsub);
+    SubState* d_s1 = (SubState*)workspace(ctx, "dec_state1", sizeof(SubState) * (size_t)nsub);
+    SubCount* d_cnt = (SubCount*)workspace(ctx, "dec_counts", sizeof(SubCount) * (size_t)nsub);
+    SubCount* d_base = (SubCount*)workspace(ctx, "dec_base", sizeof(SubCount) * (size_t)nsub);
+    int* d_changed = (int*)workspace(ctx, "dec_changed", sizeof(int));
+    if (!d_bytes || !d_segs || !d_s0 || !d_s1 || !d_cnt || !d_base || !d_changed) return RCG_NO_MEMORY;
+    if (!sc.bytes.empty() && (rc = copy_to_device(ctx, d_bytes, sc.bytes.data(), sc.bytes.size())) != RCG_OK)
+      return rc;
+    cudaMemcpyAsync(d_segs, sc.segs.data(), sizeof(Segment) * sc.segs.size(), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(d_sd, &sc.sd, sizeof(ScanDesc), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(d_tab, &sc.tables, sizeof(Tables), cudaMemcpyHostToDevice, ctx->stream);
+    // Initial guesses: every subsequence starts at its first bit, first block of the MCU, at a DC.
+    std::vector<SubState> init((size_t)nsub);
+    for (const Segment& g : sc.segs)
+      for (int i = 0; i < g.nsub; i++) init[g.sub0 + i] = SubState{(long long)i * kSubBits, 0, 0};
+    cudaMemcpyAsync(d_s0, init.data(), sizeof(SubState) * (size_t)nsub, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemsetAsync(d_cnt, 0, sizeof(SubCount) * (size_t)nsub, ctx->stream);
+    const unsigned grid = (unsigned)((nsub + 127) / 128);
+    SubState* cur = d_s0;
+    SubState* nxt = d_s1;
+    bool settled = false;
+    for (int round = 0; round < kMaxRounds; round++) {
+      cudaMemsetAsync(d_changed, 0, sizeof(int), ctx->stream);
+      RCG_LAUNCH(ctx, "seq_sync", k_seq_sync, grid, 128, 0, d_sd, d_tab, d_segs, d_bytes, cur, nxt, d_cnt,
+                 d_changed);
+      cudaMemcpyAsync(&h_changed, d_changed, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+      cudaError_t e = cudaStreamSynchronize(ctx->stream);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "JPEG decode");
+      std::swap(cur, nxt);
+      if (!h_changed) {
+        settled = true;
+        break;
+      }
+    }
+    if (!settled) {
+      RCG_LAUNCH(ctx, "seq_chain", k_seq_chain, (unsigned)std::min<long long>((sc.sd.nseg + 127) / 128, 1024), 128, 0,
+                 d_sd, d_tab, d_segs, d_bytes, cur, d_cnt);
+    }
+    RCG_LAUNCH(ctx, "seq_prefix", k_seq_prefix, (unsigned)std::min(sc.sd.nseg, 1024), 1024, 0, d_sd, d_segs, d_cnt,
+               d_base);
+    RCG_LAUNCH(ctx, "seq_write", k_seq_write, grid, 128, 0, d_sd, d_tab, d_segs, d_bytes, cur, d_base, d_out, d_err);
+  }
+  int h_err = 0;
+  cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "JPEG decode");
+  if (h_err) return fail(ctx, RCG_INVALID, h_err == 1 ? "bad JPEG entropy-coded data" : "JPEG decode lost its place");
+  if (!coefs_on_device) return copy_to_host(ctx, coefs, d_out, (size_t)nblocks * 128);
+  return RCG_OK;
+}
+
+}  // namespace rcg

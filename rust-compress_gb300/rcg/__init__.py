@@ -85,6 +85,11 @@ class _QTables(ctypes.Structure):
     _fields_ = [("tq", ctypes.c_int32 * 3), ("qtables", (ctypes.c_uint8 * 64) * 4), ("present", ctypes.c_int32 * 4)]
 
 
+class _JpegInfo(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("ids", ctypes.c_uint8 * 4),
+                ("scans", ctypes.c_int32)]
+
+
 class _Scan(ctypes.Structure):
     _fields_ = [("ncomps", ctypes.c_int32), ("comps", ctypes.c_int32 * 4), ("ss", ctypes.c_int32),
                 ("se", ctypes.c_int32), ("ah", ctypes.c_int32), ("al", ctypes.c_int32)]
@@ -218,6 +223,13 @@ def _load():
         "rcg_metric_score_device": (i32, [P, i32, P, P, u32, u32, i32, ctypes.POINTER(ctypes.c_double)]),
         "rcg_search_metric": (i32, [P, P, u32, u32, i32, i32, ctypes.c_double, i32, ctypes.POINTER(_Opts),
                                     ctypes.POINTER(_Found), P, sz, P]),
+        "rcg_decode_coefs": (i32, [P, P, sz, ctypes.POINTER(_JpegInfo), ctypes.POINTER(_Layout),
+                                   ctypes.POINTER(_QTables), P, sz]),
+        "rcg_decode_coefs_device": (i32, [P, P, sz, ctypes.POINTER(_JpegInfo), ctypes.POINTER(_Layout),
+                                          ctypes.POINTER(_QTables), P, sz]),
+        "rcg_search_requantize_device": (i32, [P, u32, u32, ctypes.POINTER(_Layout), ctypes.POINTER(_QTables), P,
+                                               i32, ctypes.c_double, i32, i32, ctypes.POINTER(_Found), P, sz,
+                                               ctypes.POINTER(_QTables)]),
         "rcg_plan": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, sz, ctypes.POINTER(_PlanResult)]),
         "rcg_plan_device": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, ctypes.POINTER(_PlanResult)]),
         "rcg_search_batch": (i32, [P, i32, P, P, P, P, P, i32, ctypes.POINTER(_Opts), i32, P, P, P, P]),
@@ -235,7 +247,8 @@ EXPORTED = (
     "rcg_ctx_launch_count rcg_ctx_set_profiling rcg_ctx_kernel_time rcg_coef_layout_for rcg_ssimulacra2 "
     "rcg_ssimulacra2_device rcg_ssimulacra2_device_noalloc rcg_build_coefs rcg_reconstruct rcg_search rcg_search_device "
     "rcg_search_batch rcg_reconstruct_tables rcg_requantize rcg_search_requantize rcg_plan rcg_plan_device "
-    "rcg_metric_score rcg_metric_score_device rcg_search_metric"
+    "rcg_metric_score rcg_metric_score_device rcg_search_metric rcg_decode_coefs rcg_decode_coefs_device "
+    "rcg_search_requantize_device"
 ).split()
 
 
@@ -406,6 +419,47 @@ class Context:
             self._check(_lib.rcg_reconstruct_tables(self._ptr, ci.width, ci.height, ctypes.byref(lay),
                                                     ctypes.byref(t), flat.ctypes.data, out.ctypes.data, out.size))
         return out[:, :, 0] if nc == 1 else out
+
+    def decode_coefs(self, data):
+        """jpeg::decode::parse(data)?.into_coefs() (jpeg/src/decode.rs:397, :540) of a sequential Huffman JPEG, with
+        the entropy-coded data decoded on the GPU. Returns a CoefImage (general table form; component ids kept)."""
+        buf = np.frombuffer(bytes(data), dtype=np.uint8)
+        info, lay, t = _JpegInfo(), _Layout(), _QTables()
+        self._check(_lib.rcg_decode_coefs(self._ptr, buf.ctypes.data, buf.size, ctypes.byref(info), ctypes.byref(lay),
+                                          ctypes.byref(t), None, 0))
+        coefs = np.empty(lay.ncoefs, dtype=np.int16)
+        self._check(_lib.rcg_decode_coefs(self._ptr, buf.ctypes.data, buf.size, ctypes.byref(info), ctypes.byref(lay),
+                                          ctypes.byref(t), coefs.ctypes.data, coefs.size))
+        comps, off = [], 0
+        for i in range(lay.ncomp):
+            n = lay.blocks_w[i] * lay.blocks_h[i] * 64
+            comps.append(CoefComponent(int(info.ids[i]), lay.h[i], lay.v[i], int(t.tq[i]), lay.blocks_w[i],
+                                       lay.blocks_h[i], coefs[off: off + n]))
+            off += n
+        q4 = np.array([list(t.qtables[sl]) for sl in range(4)], dtype=np.uint8)
+        present = np.array([int(t.present[sl]) for sl in range(4)], dtype=np.uint8)
+        return CoefImage(int(info.width), int(info.height), comps, q4, present)
+
+    def decode_coefs_device(self, data, coefs_ptr, coefs_len):
+        """rcg_decode_coefs_device: decode into device memory; returns (width, height, layout, tables, ids)."""
+        buf = np.frombuffer(bytes(data), dtype=np.uint8)
+        info, lay, t = _JpegInfo(), _Layout(), _QTables()
+        self._check(_lib.rcg_decode_coefs_device(self._ptr, buf.ctypes.data, buf.size, ctypes.byref(info),
+                                                 ctypes.byref(lay), ctypes.byref(t), ctypes.c_void_p(coefs_ptr),
+                                                 coefs_len))
+        return int(info.width), int(info.height), lay, t, bytes(info.ids[: lay.ncomp])
+
+    def search_requantize_device(self, width, height, layout, tables, src_ptr, out_ptr, coefs_len, target,
+                                 max_quality=100, trellis=True, metric=METRIC_SSIMULACRA2):
+        """rcg_search_requantize_device: (quality, score, trace, output tables)."""
+        f, t_out = _Found(), _QTables()
+        self._check(_lib.rcg_search_requantize_device(self._ptr, width, height, ctypes.byref(layout),
+                                                      ctypes.byref(tables), ctypes.c_void_p(src_ptr), int(metric),
+                                                      float(target), int(max_quality), 1 if trellis else 0,
+                                                      ctypes.byref(f), ctypes.c_void_p(out_ptr), coefs_len,
+                                                      ctypes.byref(t_out)))
+        trace = [(int(f.trace_q[i]), float(f.trace_score[i])) for i in range(f.nsteps)]
+        return int(f.quality), float(f.score), trace, t_out
 
     def plan(self, ci):
         """write_best's plan of a CoefImage (jpeg/src/encode.rs:543-565): statistics, costs and choice on the GPU."""

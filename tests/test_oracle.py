@@ -469,3 +469,53 @@ def test_oracle_metrics_against_numpy_and_reference_properties(oracle):
         d = ref.astype(np.float64) - dist.astype(np.float64)
         mse = (d * d).sum() / d.size
         assert oracle.psnr(ref, dist) == 10.0 * np.log10(255.0 * 255.0 / mse)
+
+
+def _fixtures():
+    import os
+
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "jpeg_fixtures.npz"))
+    off = z["offsets"]
+    return [(str(n), z["data"][off[i]: off[i + 1]].tobytes(), str(s)) for i, (n, s) in enumerate(zip(z["names"],
+                                                                                                      z["shas"]))]
+
+
+def test_oracle_sequential_decoder_round_trips_and_fixtures(oracle):
+    """parse().into_coefs() restated: the restated writer's baseline files (with restart intervals and per-component
+    scans too) decode to the coefficients written, and the reference's sequential fixture files decode to pinned
+    coefficients that survive a baseline re-encode unchanged (jpeg/tests/jpeg_decode.rs:95-110)."""
+    import hashlib
+
+    import rcg.synth as synth
+
+    img = synth.image(123, 61, 9, sensor_sigma=3.0)
+    for sub in (1, 2, 3):
+        coefs, qt, lay = oracle.build_coefs(img, 85, sub, True)
+        g = oracle.general_from_encoder(123, 61, lay, qt, coefs)
+        for ri, pc in ((0, False), (1, False), (5, True), (13, False)):
+            d, ids = oracle.decode_sequential(oracle.write_jpeg_variant(g, ri, pc))
+            assert np.array_equal(d.coefs, g.coefs) and (d.w, d.h) == (123, 61)
+    gray = img[:, :, 0].copy()
+    coefs, qt, lay = oracle.build_coefs(gray, 60, 3, True)
+    g = oracle.general_from_encoder(123, 61, lay, qt, coefs)
+    d, _ = oracle.decode_sequential(oracle.write_jpeg_variant(g, 3, False))
+    assert np.array_equal(d.coefs, g.coefs)
+    fx = _fixtures()
+    assert len(fx) >= 10
+    for name, data, sha in fx:
+        d, ids = oracle.decode_sequential(data)
+        assert hashlib.sha256(d.coefs.tobytes()).hexdigest() == sha, name
+        again, _ = oracle.decode_sequential(oracle.write_jpeg_variant(d, 0, False))
+        assert np.array_equal(again.coefs, d.coefs), name
+    # corrupt and truncated files end in an error or a decode, never a crash (jpeg/tests/jpeg_decode.rs:46-62)
+    data = bytearray(fx[0][1])
+    rng = np.random.default_rng(3)
+    for _ in range(50):
+        m = bytearray(data)
+        for i in rng.integers(2, len(m), 3):
+            m[i] = int(rng.integers(0, 256))
+        for blob in (bytes(m), bytes(m[: int(rng.integers(0, len(m) + 1))])):
+            try:
+                oracle.decode_sequential(blob)
+            except ValueError:
+                pass
