@@ -294,6 +294,41 @@ def ssim_workload(ctx, img, timed, torch, dev, with_oracle=True, steps=5):
     return out
 
 
+def decode_workload(ctx, img, timed, torch, steps=10):
+    """GPU entropy decoding of a 12 MP baseline JPEG (the workload image encoded at q90 4:2:0 with trellis, written
+    with optimized Huffman tables and no restart markers) into device memory, against the oracle's sequential
+    decoder on all host threads. The input file is written inside this CPU-baseline leg (the library has no JPEG
+    writer), so the workload runs only when the CPU baseline does."""
+    import numpy as np
+
+    import rcg
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    coefs, qt, lay = oracle.build_coefs(img, 90, 3, True)
+    g = oracle.general_from_encoder(W, H, lay, qt, coefs)
+    data = oracle.write_jpeg_variant(g, 0, False)
+    t0 = time.perf_counter()
+    og, _ = oracle.decode_sequential(data)
+    cpu_ms = (time.perf_counter() - t0) * 1000.0
+    n = lay["ncoefs"]
+    d_out = torch.empty(n, dtype=torch.int16, device="cuda")
+    for _ in range(3):
+        ctx.decode_coefs_device(data, d_out.data_ptr(), n)
+    times, _ = timed(lambda: ctx.decode_coefs_device(data, d_out.data_ptr(), n), steps)
+    ms = sum(times) / len(times)
+    same = bool(np.array_equal(d_out.cpu().numpy(), og.coefs))
+    return {"workload": "decode a 4000x3000 4:2:0 baseline JPEG (q90, trellis, optimized tables) to device coefficients",
+            "jpeg_bytes": len(data), "ms_per_decode": ms, "mb_per_s": len(data) / 1e6 / (ms / 1000.0),
+            "identical_to_oracle": same,
+            "cpu_baseline": {"value": cpu_ms, "unit": "ms per decode", "cores": 1, "kind": "port",
+                             "sample": "one decode of the same file (the restated sequential decoder is serial)"}}
+
+
 def plan_workload(ctx, timed, d_coefs, lay, with_oracle=True, steps=10):
     """write_best's plan of the search result (device-resident coefficients of the 12 MP workload at the found
     quality): statistics of the 48 distinct candidate scans and the baseline scan, code lengths, costs, choice.
@@ -486,6 +521,9 @@ def main():
     ssim_w = None
     if rank == 0 and not args.no_requant:
         ssim_w = ssim_workload(ctx, img, timed, torch, dev, with_oracle=not args.no_cpu_baseline)
+    decode = None
+    if rank == 0 and not args.no_cpu_baseline and not args.no_requant:
+        decode = decode_workload(ctx, img, timed, torch)
     requant = None
     if rank == 0 and not args.no_requant:
         requant = requantize_workload(ctx, img, timed, with_oracle=not args.no_cpu_baseline)
@@ -526,6 +564,7 @@ def main():
             "requantize": requant,
             "write_best_plan": plan,
             "target_ssim": ssim_w,
+            "jpeg_decode": decode,
         }
         print(json.dumps(out), flush=True)
     if dist:

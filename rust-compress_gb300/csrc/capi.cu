@@ -737,20 +737,10 @@ int rcg_reconstruct_tables(rcg_ctx* ctx, uint32_t width, uint32_t height, const 
 
 // ---- search
 
-// An interleaved 8-bit Gray or Rgb image as scale 0 of a linear pyramid.
-static Src8 px8(const uint8_t* p, int channels) {
-  Src8 s;
-  s.p = p;
-  s.ps = channels;
-  s.cs = channels == 3 ? 1 : 0;
-  return s;
-}
-
 // Per-candidate scorer of the device searches: SSIMULACRA2 from the candidate's linear pyramid against the
 // reference's, or SSIM from the candidate's 8-bit pixels against the reference's.
 struct SearchScorer {
   int metric;
-  int channels = 3;
   PyramidDesc pd;
   float* ref_pyr = nullptr;
   float* dist_pyr = nullptr;
@@ -761,14 +751,12 @@ struct SearchScorer {
 
 static int scorer_setup(rcg_ctx* ctx, int metric, int w, int h, int channels, SearchScorer* sc) {
   sc->metric = metric;
-  sc->channels = channels;
   sc->d_score = (double*)workspace(ctx, "score", sizeof(double));
   if (!sc->d_score) return RCG_NO_MEMORY;
-  // Candidates are decoded to 8-bit pixels: SSIM reads them as they are, SSIMULACRA2 takes them as scale 0 of the
-  // candidate's linear pyramid through the sRGB table.
-  sc->cand_px = (uint8_t*)workspace(ctx, "cand_px", (size_t)w * h * channels);
-  if (!sc->cand_px) return RCG_NO_MEMORY;
-  if (metric == RCG_METRIC_SSIM) return RCG_OK;
+  if (metric == RCG_METRIC_SSIM) {
+    sc->cand_px = (uint8_t*)workspace(ctx, "cand_px", (size_t)w * h * channels);
+    return sc->cand_px ? RCG_OK : RCG_NO_MEMORY;
+  }
   sc->pd = make_pyramid(w, h);
   sc->ref_pyr = (float*)workspace(ctx, "ref_pyr", (size_t)sc->pd.floats * sizeof(float));
   sc->dist_pyr = (float*)workspace(ctx, "dist_pyr", (size_t)sc->pd.floats * sizeof(float));
@@ -783,10 +771,9 @@ static void score_candidate(rcg_ctx* ctx, const SearchScorer& sc, StepDesc* d_st
     ssim_score(ctx, sc.ref_px, sc.cand_px, w, h, channels, sc.d_score, d_ss, d_st);
     return;
   }
-  upsample_color(ctx, d_st, planes, w, h, sc.cand_px, nullptr);
-  const Src8 ref8 = px8(sc.ref_px, channels), dist8 = px8(sc.cand_px, channels);
-  build_pyramid_gated(ctx, sc.pd, sc.dist_pyr, d_st, dist8);
-  score_pyramids(ctx, sc.pd, sc.ref_pyr, sc.dist_pyr, sc.d_score, d_ss, d_st, ref8, dist8);
+  upsample_color(ctx, d_st, planes, w, h, nullptr, sc.dist_pyr);
+  build_pyramid_gated(ctx, sc.pd, sc.dist_pyr, d_st);
+  score_pyramids(ctx, sc.pd, sc.ref_pyr, sc.dist_pyr, sc.d_score, d_ss, d_st);
 }
 
 static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, int metric, double target,
@@ -800,8 +787,12 @@ static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int cha
   if ((rc = scorer_setup(ctx, metric, w, h, channels, &sc)) != RCG_OK) return rc;
   // Quality-independent work, once per search: the reference image's linear pyramid (SSIMULACRA2; SSIM reads the
   // source pixels as they are), colour planes, FDCTs.
-  sc.ref_px = d_src;
-  if (metric != RCG_METRIC_SSIM) build_pyramid(ctx, sc.pd, sc.ref_pyr, px8(d_src, channels));
+  if (metric == RCG_METRIC_SSIM) {
+    sc.ref_px = d_src;
+  } else {
+    if ((rc = to_linear(ctx, d_src, w, h, channels, 8, sc.ref_pyr)) != RCG_OK) return rc;
+    build_pyramid(ctx, sc.pd, sc.ref_pyr);
+  }
   EncoderSetup es;
   if ((rc = setup_encoder(ctx, d_src, w, h, channels, subsampling, &es)) != RCG_OK) return rc;
   int max_steps = 1;
@@ -1040,10 +1031,10 @@ static int search_requantize_impl(rcg_ctx* ctx, uint32_t width, uint32_t height,
   int16_t* d_src = on_device ? const_cast<int16_t*>(coefs_in) : (int16_t*)workspace(ctx, "rq_src", cbytes);
   int16_t* slots = (int16_t*)workspace(ctx, "coef_slots", cbytes * max_steps);
   uint8_t* planes = (uint8_t*)workspace(ctx, "dec_planes", (size_t)plane_bytes(st));
-  uint8_t* ref_px = (uint8_t*)workspace(ctx, "ref_px", (size_t)w * h * channels);
+  uint8_t* ref_px = metric == RCG_METRIC_SSIM ? (uint8_t*)workspace(ctx, "ref_px", (size_t)w * h * channels) : nullptr;
   SearchState* d_ss = (SearchState*)workspace(ctx, "search_state", sizeof(SearchState));
   StepDesc* d_st = (StepDesc*)workspace(ctx, "step_search", sizeof(StepDesc));
-  if (!d_src || !slots || !planes || !d_ss || !d_st || !ref_px ||
+  if (!d_src || !slots || !planes || !d_ss || !d_st || (metric == RCG_METRIC_SSIM && !ref_px) ||
       scorer_setup(ctx, metric, w, h, channels, &sc) != RCG_OK) {
     delete st;
     return RCG_NO_MEMORY;
@@ -1061,8 +1052,12 @@ static int search_requantize_impl(rcg_ctx* ctx, uint32_t width, uint32_t height,
   st->requant = 1;
   cudaMemcpyAsync(d_st, st, sizeof(StepDesc), cudaMemcpyHostToDevice, ctx->stream);
   dequant_idct(ctx, d_st, d_src, planes, nblocks);
-  upsample_color(ctx, d_st, planes, w, h, ref_px, nullptr);
-  if (metric != RCG_METRIC_SSIM) build_pyramid(ctx, sc.pd, sc.ref_pyr, px8(ref_px, channels));
+  if (metric == RCG_METRIC_SSIM) {
+    upsample_color(ctx, d_st, planes, w, h, ref_px, nullptr);
+  } else {
+    upsample_color(ctx, d_st, planes, w, h, nullptr, sc.ref_pyr);
+    build_pyramid(ctx, sc.pd, sc.ref_pyr);
+  }
   SearchState hs;
   std::memset(&hs, 0, sizeof hs);
   hs.lo = 1;

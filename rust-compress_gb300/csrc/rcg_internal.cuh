@@ -35,13 +35,6 @@ struct ScaleDesc {
   long long off;    // float offset of channel 0 of this scale
 };
 
-// An 8-bit image standing in for scale 0 of a linear pyramid: sample (c, i) is lut8[p[i * ps + c * cs]] (interleaved
-// RGB: ps 3, cs 1; gray: ps 1, cs 0). p == nullptr: scale 0 is in the f32 pyramid.
-struct Src8 {
-  const uint8_t* p = nullptr;
-  int ps = 0, cs = 0;
-};
-
 struct PyramidDesc {
   int nscales;
   int total_tiles;
@@ -221,13 +214,13 @@ int scorer_init(rcg_ctx* ctx);
 // Interleaved 8-bit Gray/Rgb (or GrayAlpha/Rgba, or 16-bit) image -> linear planes at scale 0 of `pyr`.
 int to_linear(rcg_ctx* ctx, const uint8_t* d_img, int w, int h, int channels, int depth, float* d_pyr);
 // Fill scales 1.. of a pyramid from scale 0 (core/src/ssimulacra2.rs:225-247).
-int build_pyramid(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, Src8 s8 = Src8());
+int build_pyramid(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr);
 // The same, skipped on the device when the search step is inactive.
-int build_pyramid_gated(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, const StepDesc* st, Src8 s8 = Src8());
+int build_pyramid_gated(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, const StepDesc* st);
 // Score: per-tile sums of every scale, then the final mapping. `d_score` receives the score (f64); when
 // `search` is non-null the final kernel also advances the device-side bisection.
 int score_pyramids(rcg_ctx* ctx, const PyramidDesc& pd, const float* d_ref, const float* d_dist, double* d_score,
-                   SearchState* search, StepDesc* step, Src8 ref8 = Src8(), Src8 dist8 = Src8());
+                   SearchState* search, StepDesc* step);
 
 // ---- codec (codec.cu)
 // Colour conversion + edge padding (jpeg/src/encode.rs:463-477): full-resolution padded Y/Cb/Cr planes.

@@ -121,10 +121,9 @@ constexpr size_t kTileSmem = (size_t)(6 * kIH * kIW + 5 * kIH * kTileW) * sizeof
 // 5-pixel halo, 3 channels each; then per channel the horizontally blurred five moments of the 42 halo rows.
 __global__ void __launch_bounds__(kTileThreads, 3)
     k_ssim2_tiles(PyramidDesc pd, const float* __restrict__ ref, const float* __restrict__ dist,
-                  double* __restrict__ partials, const StepDesc* __restrict__ st, Src8 ref8, Src8 dist8) {
+                  double* __restrict__ partials, const StepDesc* __restrict__ st) {
   if (st && !st->active) return;
   extern __shared__ float smem[];
-  __shared__ float lut8[256];
   float* xs = smem;                      // [6][kIH][kIW]: ref X,Y,B then dist X,Y,B
   float* hb = smem + 6 * kIH * kIW;      // [5][kIH][kTileW]
   __shared__ float s_red[kTileThreads / 32][kScoreSums];
@@ -142,18 +141,6 @@ __global__ void __launch_bounds__(kTileThreads, 3)
   const float* rb = dist + sd.off;
   const float cb_bias = cbrtf((float)kBias);
   const int tid = threadIdx.x;
-  // Scale 0 may come from 8-bit images through the sRGB table (the same values the f32 planes would hold).
-  const bool a8 = s == 0 && ref8.p != nullptr, b8 = s == 0 && dist8.p != nullptr;
-  if (a8 || b8)
-    for (int i = tid; i < 256; i += kTileThreads) lut8[i] = c_lut8s[i];
-  __syncthreads();
-  auto sample3 = [&](bool is8, const Src8& s8, const float* f, size_t i) -> float3 {
-    if (is8) {
-      const uint8_t* q = s8.p + i * s8.ps;
-      return make_float3(lut8[q[0]], lut8[q[s8.cs]], lut8[q[2 * s8.cs]]);
-    }
-    return make_float3(__ldg(f + i), __ldg(f + np + i), __ldg(f + 2 * np + i));
-  };
 
   // Per-tile offsets: the reference's XYB and the XYB difference at the tile centre. Stored values are
   // a' = a - oa and d' = (a - b) - od inside the image and 0 outside (the zero border). Every moment the maps need
@@ -164,8 +151,7 @@ __global__ void __launch_bounds__(kTileThreads, 3)
     int cx = min(x0 + kTileW / 2, w - 1), cy = min(y0 + kTileH / 2, h - 1);
     size_t i = (size_t)cy * w + cx;
     const float z[3] = {0.f, 0.f, 0.f};
-    const float3 va = sample3(a8, ref8, ra, i), vb = sample3(b8, dist8, rb, i);
-    Pix c = pix(va.x, va.y, va.z, vb.x, vb.y, vb.z, z, z, cb_bias);
+    Pix c = pix(ra[i], ra[np + i], ra[2 * np + i], rb[i], rb[np + i], rb[2 * np + i], z, z, cb_bias);
     for (int k = 0; k < 3; k++) {
       s_oa[k] = c.a[k];
       s_od[k] = c.d[k];
@@ -183,13 +169,12 @@ __global__ void __launch_bounds__(kTileThreads, 3)
     int gx = x0 - kRadius + c;
     if (e < kIH * kCols && gy >= 0 && gx >= 0 && gx < w) {
       size_t i = (size_t)gy * w + gx;
-      const float3 va = sample3(a8, ref8, ra, i), vb = sample3(b8, dist8, rb, i);
-      v[0] = va.x;
-      v[1] = va.y;
-      v[2] = va.z;
-      v[3] = vb.x;
-      v[4] = vb.y;
-      v[5] = vb.z;
+      v[0] = __ldg(ra + i);
+      v[1] = __ldg(ra + np + i);
+      v[2] = __ldg(ra + 2 * np + i);
+      v[3] = __ldg(rb + i);
+      v[4] = __ldg(rb + np + i);
+      v[5] = __ldg(rb + 2 * np + i);
       return true;
     }
     return false;
@@ -524,19 +509,10 @@ __device__ __forceinline__ float mean2x2(const float* p, int stride, int w, int 
 // column, where mean2x2 clips to the level's size.
 constexpr int kPyrTile = 32;
 __global__ void __launch_bounds__(256) k_pyramid(PyramidDesc pd, float* __restrict__ pyr,
-                                                 const StepDesc* __restrict__ st, Src8 s8) {
+                                                 const StepDesc* __restrict__ st) {
   if (st && !st->active) return;
   __shared__ float buf[2][3][kPyrTile][kPyrTile + 1];
-  __shared__ float lut8[256];
   const ScaleDesc s0 = pd.s[0], s1 = pd.s[1];
-  if (s8.p)
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) lut8[i] = c_lut8s[i];
-  __syncthreads();
-  // Scale-0 sample of channel c at (x, y): from the f32 pyramid or the 8-bit source.
-  auto at0 = [&](int c, int x, int y) -> float {
-    const size_t i = (size_t)y * s0.w + x;
-    return s8.p ? lut8[s8.p[i * s8.ps + (size_t)c * s8.cs]] : pyr[s0.off + c * ((size_t)s0.w * s0.h) + i];
-  };
   const int tiles_x = (s1.w + kPyrTile - 1) / kPyrTile;
   const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
   const size_t np0 = (size_t)s0.w * s0.h, np1 = (size_t)s1.w * s1.h;
@@ -552,10 +528,11 @@ __global__ void __launch_bounds__(256) k_pyramid(PyramidDesc pd, float* __restri
         float q[3][4];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-          q[c][0] = at0(c, 2 * ox, 2 * oy);
-          q[c][1] = at0(c, 2 * ox + 1, 2 * oy);
-          q[c][2] = at0(c, 2 * ox, 2 * oy + 1);
-          q[c][3] = at0(c, 2 * ox + 1, 2 * oy + 1);
+          const float* p = pyr + s0.off + c * np0 + (size_t)(2 * oy) * s0.w + 2 * ox;
+          q[c][0] = p[0];
+          q[c][1] = p[1];
+          q[c][2] = p[s0.w];
+          q[c][3] = p[s0.w + 1];
         }
 #pragma unroll
         for (int c = 0; c < 3; c++) {
@@ -567,18 +544,7 @@ __global__ void __launch_bounds__(256) k_pyramid(PyramidDesc pd, float* __restri
         }
       } else {
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-          // mean2x2 (core/src/ssimulacra2.rs:225-247) of a partial block at the right/bottom edge
-          const int x1 = min(ox * 2 + 2, s0.w), y1 = min(oy * 2 + 2, s0.h);
-          float sum = 0.0f, err = 0.0f;
-          for (int y = oy * 2; y < y1; y++)
-            for (int x = ox * 2; x < x1; x++) {
-              float e;
-              sum = two_sum(sum, at0(c, x, y), e);
-              err += e;
-            }
-          v[c] = __fadd_rn(sum, err) * (1.0f / (float)((y1 - oy * 2) * (x1 - ox * 2)));
-        }
+        for (int c = 0; c < 3; c++) v[c] = mean2x2(pyr + s0.off + c * np0, s0.w, s0.w, s0.h, ox, oy);
       }
 #pragma unroll
       for (int c = 0; c < 3; c++) {
@@ -632,15 +598,15 @@ int to_linear(rcg_ctx* ctx, const uint8_t* d_img, int w, int h, int channels, in
   return RCG_OK;
 }
 
-int build_pyramid_gated(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, const StepDesc* st, Src8 s8) {
+int build_pyramid_gated(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, const StepDesc* st) {
   if (pd.nscales < 2) return RCG_OK;
   const int grid = ((pd.s[1].w + kPyrTile - 1) / kPyrTile) * ((pd.s[1].h + kPyrTile - 1) / kPyrTile);
-  RCG_LAUNCH(ctx, "pyramid", k_pyramid, grid, 256, 0, pd, d_pyr, st, s8);
+  RCG_LAUNCH(ctx, "pyramid", k_pyramid, grid, 256, 0, pd, d_pyr, st);
   return RCG_OK;
 }
 
-int build_pyramid(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, Src8 s8) {
-  return build_pyramid_gated(ctx, pd, d_pyr, nullptr, s8);
+int build_pyramid(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr) {
+  return build_pyramid_gated(ctx, pd, d_pyr, nullptr);
 }
 
 PyramidDesc make_pyramid(int w, int h) {
@@ -725,13 +691,13 @@ int scorer_init(rcg_ctx* ctx) {
 }
 
 int score_pyramids(rcg_ctx* ctx, const PyramidDesc& pd, const float* d_ref, const float* d_dist, double* d_score,
-                   SearchState* search, StepDesc* step, Src8 ref8, Src8 dist8) {
+                   SearchState* search, StepDesc* step) {
   double* partials = (double*)workspace(ctx, "score_partials", (size_t)pd.total_tiles * kScoreSums * sizeof(double));
   double* scale_sums = (double*)workspace(ctx, "score_scale_sums", kMaxScales * kScoreSums * sizeof(double));
   unsigned* counter = (unsigned*)workspace(ctx, "score_counter", 256);
   if (!partials || !scale_sums || !counter) return RCG_NO_MEMORY;
   RCG_LAUNCH(ctx, "ssim2_tiles", k_ssim2_tiles, pd.total_tiles, kTileThreads, kTileSmem, pd, d_ref, d_dist, partials,
-             step, ref8, dist8);
+             step);
   dim3 rg(pd.nscales, kScoreSums);
   RCG_LAUNCH(ctx, "ssim2_reduce", k_ssim2_reduce, rg, 256, 0, pd, partials, scale_sums, counter, d_score, search,
              step);
@@ -819,11 +785,10 @@ extern "C" int rcg_ssimulacra2_device_noalloc(const uint8_t* d_reference, const 
   k_to_linear<<<lg, 256, 0, s>>>(d_distorted, w, h, channels, 8, nullptr, pyr_dist);
   if (pd.nscales > 1) {
     const int pg = ((pd.s[1].w + kPyrTile - 1) / kPyrTile) * ((pd.s[1].h + kPyrTile - 1) / kPyrTile);
-    k_pyramid<<<pg, 256, 0, s>>>(pd, pyr_ref, nullptr, Src8());
-    k_pyramid<<<pg, 256, 0, s>>>(pd, pyr_dist, nullptr, Src8());
+    k_pyramid<<<pg, 256, 0, s>>>(pd, pyr_ref, nullptr);
+    k_pyramid<<<pg, 256, 0, s>>>(pd, pyr_dist, nullptr);
   }
-  k_ssim2_tiles<<<pd.total_tiles, kTileThreads, kTileSmem, s>>>(pd, pyr_ref, pyr_dist, partials, nullptr, Src8(),
-                                                                 Src8());
+  k_ssim2_tiles<<<pd.total_tiles, kTileThreads, kTileSmem, s>>>(pd, pyr_ref, pyr_dist, partials, nullptr);
   k_ssim2_reduce<<<dim3(pd.nscales, kScoreSums), 256, 0, s>>>(pd, partials, sums, counter, d_score, nullptr,
                                                               nullptr);
   cudaError_t e = cudaGetLastError();
