@@ -108,6 +108,7 @@ typedef struct {
   uint32_t width, height;
   uint8_t ids[4]; /* component identifiers (SOF order) */
   int32_t scans;  /* scans decoded */
+  int32_t sync_rounds; /* most synchronization rounds a scan needed (-1: a scan fell back to the serial chain) */
 } rcg_jpeg_info;
 
 typedef struct rcg_ctx rcg_ctx;

@@ -8,15 +8,17 @@
 // by 0x00, reads past the end give zero bits, and the next segment starts just past the next RSTn (if the marker
 // found there is not an RSTn, that segment and all later ones read zero bits).
 //
-// The device decodes each segment in parallel by self-synchronization. The segment's bits are cut into
-// subsequences of 1024 bits, one thread each. A decoding state at a codeword boundary is (bit position, block of the
-// MCU, next coefficient index). Round after round every thread decodes its subsequence from its current start state
-// and hands the state where it crosses into the next subsequence to its successor; the first subsequence of a
-// segment starts from the exact state, so the states become exact from front to back, and Huffman codes
-// resynchronize after a few codewords, so a couple of rounds settle almost every start. When a round changes
-// nothing, every start is exact; the block counts and DC-difference sums of that round give each subsequence its
-// first block and DC predictions (prefix sums), and a last pass decodes again and writes the coefficients. If the
-// rounds do not settle within a bound, one thread per segment follows the chain of states instead.
+// The device decodes each segment in parallel by self-synchronization. A decoding state at a codeword boundary is
+// (bit position, block of the MCU, next coefficient index). The segment's bits are cut into spans of 2048 bits, one
+// thread each, and each span into pieces of 256 bits. Round after round every thread decodes its span from its
+// current start state, records the state and the block count and DC-difference sums at every piece boundary, and
+// hands the state where it crosses into the next span to its successor. The first span of a segment starts from
+// the exact state, so the states become exact from front to back; Huffman codes resynchronize within a few
+// codewords, but the block-of-the-MCU part of the state only when a desynchronization happens to realign it, which
+// takes a few MCUs, hence spans long enough to settle in a few rounds. When a round changes nothing, every piece
+// start is exact; prefix sums of the counts give each piece its first block and DC predictions, and a last pass,
+// one thread per piece, decodes again and writes the coefficients. If the rounds do not settle within a bound, one
+// thread per segment follows the chain of states instead.
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -32,7 +34,10 @@ namespace rcg {
 
 namespace {
 
-constexpr int kSubBits = 1024;
+constexpr int kSubBits = 256;   // a piece: the unit of the writing pass
+constexpr int kSpanSubs = 8;    // a span (8 pieces, 2048 bits): the unit of the synchronization rounds
+constexpr int kDecThreads = 64;
+constexpr int kFirstBatch = 3;  // rounds launched before the first convergence check
 constexpr int kMaxRounds = 48;
 constexpr int kMaxMcuBlocks = 48;
 constexpr unsigned long long kMaxPixels = 150000000ull;  // core/src/image.rs:33 (MAX_PIXELS)
@@ -87,8 +92,10 @@ struct Segment {
   long long nbytes;   // destuffed bytes of the segment (reads beyond give zeros)
   long long block0;   // first block of the segment in the scan's visiting order
   long long nblocks;  // blocks the segment decodes
-  long long sub0;     // first subsequence of the segment
-  int nsub;
+  long long sub0;     // first piece of the segment
+  int nsub;           // pieces
+  long long span0;    // first span of the segment
+  int nspan;          // spans
 };
 
 struct ScanDesc {
@@ -101,7 +108,8 @@ struct ScanDesc {
   int dc[4], ac[4];           // table slot of each scan component
   CompDesc fc[3];             // frame components (block grids, offsets)
   int nseg;
-  long long nsub;
+  long long nsub;   // pieces of the scan
+  long long nspan;  // spans of the scan
 };
 
 struct SubState {
@@ -115,14 +123,25 @@ struct SubCount {
   uint32_t dc[4];    // sums of DC differences per scan component (wrapping, as the reference's i32 predictor)
 };
 
+// Bit reader over a segment's unstuffed bytes: reads past the segment's end give zeros (decode.rs:30-60). Bytes
+// inside a shared-memory window (the CTA's slice of the buffer, loaded once, coalesced) come from there; the rest
+// from global memory.
 struct Reader {
-  const uint8_t* p;
+  const uint8_t* p;       // segment start in global memory
+  const uint8_t* win;     // shared-memory copy of global bytes [win_lo, win_hi) of the scan buffer
+  long long seg_at;       // scan-buffer offset of the segment start
+  long long win_lo, win_hi;
   long long len, next;
   uint64_t buf;
   int n;
   long long bit;
-  __device__ void init(const uint8_t* base, long long nbytes, long long at) {
-    p = base;
+  __device__ void init(const uint8_t* data, long long seg_byte0, long long nbytes, long long at,
+                       const uint8_t* window = nullptr, long long lo = 0, long long hi = 0) {
+    p = data + seg_byte0;
+    seg_at = seg_byte0;
+    win = window;
+    win_lo = lo;
+    win_hi = hi;
     len = nbytes;
     next = at >> 3;
     buf = 0;
@@ -132,12 +151,27 @@ struct Reader {
     skip((int)(at & 7));
     bit = at;
   }
+  __device__ __forceinline__ uint64_t byte_at(long long j) const {
+    if (j >= len) return 0;
+    const long long g = seg_at + j;
+    if (g >= win_lo && g < win_hi) return win[g - win_lo];
+    return p[j];
+  }
   __device__ __forceinline__ void refill() {
-    while (n <= 56) {
-      const uint64_t byte = next < len ? p[next] : 0;
-      next++;
-      buf |= byte << (56 - n);
-      n += 8;
+    // Four bytes at a time (whole window hits take no per-byte checks); keeps at least 32 bits buffered.
+    while (n <= 32) {
+      const long long g = seg_at + next;
+      uint32_t w;
+      if (next + 4 <= len && g >= win_lo && g + 4 <= win_hi) {
+        const uint8_t* q = win + (g - win_lo);
+        w = ((uint32_t)q[0] << 24) | ((uint32_t)q[1] << 16) | ((uint32_t)q[2] << 8) | q[3];
+      } else {
+        w = (uint32_t)((byte_at(next) << 24) | (byte_at(next + 1) << 16) | (byte_at(next + 2) << 8) |
+                       byte_at(next + 3));
+      }
+      buf |= (uint64_t)w << (32 - n);
+      next += 4;
+      n += 32;
     }
   }
   __device__ __forceinline__ uint32_t peek(int k) {
@@ -187,10 +221,13 @@ struct Tables {
 // stores the coefficients of block `block_base + blocks` onward (zigzag order), with DC predictors `pred`.
 // Returns 0, or 1 on a bad code (decode.rs:1482-1506).
 template <bool WRITE>
-__device__ int decode_run(const Tables& tb, const ScanDesc& sd, Reader& r, SubState& st, long long stop_bit,
+__device__ __forceinline__ int decode_run(const Tables& tb, const ScanDesc& sd, Reader& r, SubState& st, long long stop_bit,
                           long long max_blocks, SubCount& cnt, long long block_base, uint32_t* pred,
                           int16_t* __restrict__ out) {
   int u = st.u, k = st.k;
+  uint32_t d0 = cnt.dc[0], d1 = cnt.dc[1], d2 = cnt.dc[2], d3 = cnt.dc[3];
+  const uint32_t p0 = WRITE ? pred[0] - d0 : 0u, p1 = WRITE ? pred[1] - d1 : 0u, p2 = WRITE ? pred[2] - d2 : 0u,
+                 p3 = WRITE ? pred[3] - d3 : 0u;
   int16_t* blk = nullptr;
   auto block_ptr = [&](long long b) -> int16_t* {
     const long long mcu = b / sd.bmcu;
@@ -204,76 +241,92 @@ __device__ int decode_run(const Tables& tb, const ScanDesc& sd, Reader& r, SubSt
   };
   if (WRITE && cnt.blocks < max_blocks) blk = block_ptr(block_base + cnt.blocks);
   int err = 0;
-  while (cnt.blocks < max_blocks && r.bit < stop_bit) {
+  // One symbol per iteration with a single code path for DC and AC symbols (the lanes of a warp decode different
+  // streams; branches would serialize them). decode_sequential (decode.rs:1482-1506) in select form: a DC symbol is
+  // a size t <= 16 and t extra bits; an AC symbol (run, size) is EOB (size 0, run < 15), ZRL (size 0, run 15: k += 16)
+  // or a coefficient at k + run (error past 63); the block ends when k reaches 64 or at EOB.
+  long long blocks = cnt.blocks;
+  while (blocks < max_blocks && r.bit < stop_bit) {
     const int si = sd.mcu_si[u];
-    if (k == 0) {
-      const int t = huff_decode(tb.dc[sd.dc[si]], r);
-      if (t < 0 || t > 16) {
-        err = 1;
-        break;
-      }
-      const int diff = extend_bits(r.bits(t), t);
-      cnt.dc[si] += (uint32_t)diff;
-      if (WRITE) {
-        pred[si] += (uint32_t)diff;
-        blk[0] = (int16_t)pred[si];
-      }
-      k = 1;
-      continue;
-    }
-    const int rs = huff_decode(tb.ac[sd.ac[si]], r);
-    if (rs < 0) {
+    const bool dc = k == 0;
+    const int sym = huff_decode(dc ? tb.dc[sd.dc[si]] : tb.ac[sd.ac[si]], r);
+    const int run = dc ? 0 : (sym >> 4);
+    const int sz = dc ? sym : (sym & 15);
+    if (sym < 0 || sz > 16 || (!dc && sz > 0 && k + run > 63)) {
       err = 1;
       break;
     }
-    const int run = rs >> 4, sz = rs & 15;
-    bool end = false;
-    if (sz == 0) {
-      if (run == 15) {
-        k += 16;
-        end = k >= 64;
-      } else {
-        end = true;
-      }
-    } else {
-      k += run;
-      if (k > 63) {
-        err = 1;
-        break;
-      }
-      const int v = extend_bits(r.bits(sz), sz);
-      if (WRITE) blk[k] = (int16_t)v;
-      k++;
-      end = k >= 64;
+    const int v = extend_bits(r.bits(sz), sz);
+    const uint32_t ud = dc ? (uint32_t)v : 0u;  // selects instead of indexing by si: the sums stay in registers
+    d0 += si == 0 ? ud : 0u;
+    d1 += si == 1 ? ud : 0u;
+    d2 += si == 2 ? ud : 0u;
+    d3 += si == 3 ? ud : 0u;
+    if (WRITE) {
+      if (dc)
+        blk[0] = (int16_t)(si == 0 ? p0 + d0 : si == 1 ? p1 + d1 : si == 2 ? p2 + d2 : p3 + d3);
+      else if (sz > 0)
+        blk[k + run] = (int16_t)v;
     }
+    const int nk = dc ? 1 : (sz == 0 ? (run == 15 ? k + 16 : 64) : k + run + 1);
+    const bool end = nk >= 64;
+    k = end ? 0 : nk;
     if (end) {
-      k = 0;
       u = u + 1 == sd.bmcu ? 0 : u + 1;
-      cnt.blocks++;
-      if (WRITE && cnt.blocks < max_blocks) blk = block_ptr(block_base + cnt.blocks);
+      blocks++;
+      if (WRITE && blocks < max_blocks) blk = block_ptr(block_base + blocks);
     }
   }
+  cnt.blocks = blocks;
   st.bit = r.bit;
   st.u = u;
   st.k = k;
+  cnt.dc[0] = d0;
+  cnt.dc[1] = d1;
+  cnt.dc[2] = d2;
+  cnt.dc[3] = d3;
   return err;
 }
 
 struct SubRef {
   int seg;
-  int local;  // subsequence index within the segment
+  int local;  // index within the segment
 };
 
-__device__ __forceinline__ SubRef find_sub(const Segment* segs, int nseg, long long t) {
+// The segment holding piece (spans == false) or span (spans == true) t.
+__device__ __forceinline__ SubRef find_sub(const Segment* segs, int nseg, long long t, bool spans) {
   int lo = 0, hi = nseg - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) / 2;
-    if (segs[mid].sub0 <= t)
+    if ((spans ? segs[mid].span0 : segs[mid].sub0) <= t)
       lo = mid;
     else
       hi = mid - 1;
   }
-  return {lo, (int)(t - segs[lo].sub0)};
+  return {lo, (int)(t - (spans ? segs[lo].span0 : segs[lo].sub0))};
+}
+
+constexpr int kTail = 64;  // bytes past a unit a decode may read (last codeword, reader look-ahead)
+
+// Scan-buffer byte range [lo, hi) of the units (spans or pieces) [t0, t0 + count) of one CTA, rounded out to
+// 16 bytes and capped at `cap` bytes. Units of consecutive segments are consecutive in the buffer.
+__device__ __forceinline__ void unit_window(const Segment* segs, int nseg, long long t0, long long count,
+                                            long long nunits, bool spans, long long cap, long long* lo,
+                                            long long* hi) {
+  const int ub = spans ? kSpanSubs * kSubBits / 8 : kSubBits / 8;
+  const SubRef a = find_sub(segs, nseg, t0, spans);
+  const SubRef b = find_sub(segs, nseg, min(t0 + count, nunits) - 1, spans);
+  const long long l = (segs[a.seg].byte0 + (long long)a.local * ub) & ~15ll;
+  const long long h = (segs[b.seg].byte0 + (long long)(b.local + 1) * ub + kTail + 15) & ~15ll;
+  *lo = l;
+  *hi = min(h, l + cap);
+}
+
+// Copies scan-buffer bytes [lo, hi) (16-byte aligned; the buffer is padded past its end) into shared memory.
+__device__ __forceinline__ void load_window(const uint8_t* data, long long lo, long long hi, uint8_t* win) {
+  const int4* src = reinterpret_cast<const int4*>(data + lo);
+  int4* dst = reinterpret_cast<int4*>(win);
+  for (long long i = threadIdx.x; i < (hi - lo) / 16; i += blockDim.x) dst[i] = __ldg(src + i);
 }
 
 __device__ __forceinline__ void load_tables(Tables& sh, const Tables* g) {
@@ -283,39 +336,56 @@ __device__ __forceinline__ void load_tables(Tables& sh, const Tables* g) {
   __syncthreads();
 }
 
-// One round: every non-final subsequence decodes from its current start and proposes its successor's start.
-__global__ void __launch_bounds__(128) k_seq_sync(const ScanDesc* __restrict__ sdp, const Tables* __restrict__ tg,
-                                                  const Segment* __restrict__ segs, const uint8_t* __restrict__ data,
-                                                  const SubState* __restrict__ cur, SubState* __restrict__ nxt,
-                                                  SubCount* __restrict__ counts, int* __restrict__ changed) {
+// One round, one thread per span: decode the span's pieces from the span's current start, record the state and
+// the counts at every piece boundary, and propose the state at the span's end as the next span's start.
+__global__ void __launch_bounds__(kDecThreads) k_seq_sync(const ScanDesc* __restrict__ sdp, const Tables* __restrict__ tg,
+                                                          const Segment* __restrict__ segs,
+                                                          const uint8_t* __restrict__ data,
+                                                          const SubState* __restrict__ cur, SubState* __restrict__ nxt,
+                                                          SubState* __restrict__ piece_state,
+                                                          SubCount* __restrict__ counts, int* __restrict__ changed) {
   __shared__ __align__(16) Tables tb;
   __shared__ ScanDesc sd;
   if (threadIdx.x == 0) sd = *sdp;
   load_tables(tb, tg);
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= sd.nsub) return;
-  const SubRef ref = find_sub(segs, sd.nseg, t);
+  constexpr long long kWin = (long long)kDecThreads * (kSpanSubs * kSubBits / 8 + 4) + kTail + 32;
+  __shared__ __align__(16) uint8_t win[kWin];
+  __shared__ long long w_lo, w_hi;
+  const long long t0 = (long long)blockIdx.x * blockDim.x;
+  if (threadIdx.x == 0) unit_window(segs, sd.nseg, t0, blockDim.x, sd.nspan, true, kWin & ~15ll, &w_lo, &w_hi);
+  __syncthreads();
+  load_window(data, w_lo, w_hi, win);
+  __syncthreads();
+  const long long t = t0 + threadIdx.x;
+  if (t >= sd.nspan) return;
+  const SubRef ref = find_sub(segs, sd.nseg, t, true);
   const Segment& sg = segs[ref.seg];
   if (ref.local == 0) nxt[t] = SubState{0, 0, 0};
-  if (ref.local + 1 >= sg.nsub) return;  // the last subsequence proposes nothing
+  const int f0 = ref.local * kSpanSubs, f1 = min(f0 + kSpanSubs, sg.nsub);
   SubState st = cur[t];
-  SubCount cnt{};
+  piece_state[sg.sub0 + f0] = st;
   Reader r;
-  r.init(data + sg.byte0, sg.nbytes, st.bit);
-  const long long stop = (long long)(ref.local + 1) * kSubBits;
-  if (decode_run<false>(tb, sd, r, st, stop, LLONG_MAX, cnt, 0, nullptr, nullptr)) {
-    st = SubState{stop, 0, 0};  // desynchronized: any guess will do
+  r.init(data, sg.byte0, sg.nbytes, st.bit, win, w_lo, w_hi);
+  for (int f = f0; f < f1 && f + 1 < sg.nsub; f++) {
+    SubCount cnt{};
+    const long long stop = (long long)(f + 1) * kSubBits;
+    if (decode_run<false>(tb, sd, r, st, stop, LLONG_MAX, cnt, 0, nullptr, nullptr)) {
+      st = SubState{stop, 0, 0};  // desynchronized: any guess will do
+      r.init(data, sg.byte0, sg.nbytes, stop, win, w_lo, w_hi);
+    }
+    counts[sg.sub0 + f] = cnt;
+    piece_state[sg.sub0 + f + 1] = st;
   }
-  counts[t] = cnt;
+  if (ref.local + 1 >= sg.nspan) return;  // the segment's last span proposes nothing
   nxt[t + 1] = st;
   const SubState& old = cur[t + 1];
   if (old.bit != st.bit || old.u != st.u || old.k != st.k) atomicOr(changed, 1);
 }
 
-// Fallback when the rounds do not settle: one thread per segment follows the chain of exact states.
+// Fallback when the rounds do not settle: one thread per segment follows the chain of exact piece states.
 __global__ void k_seq_chain(const ScanDesc* __restrict__ sdp, const Tables* __restrict__ tg,
                             const Segment* __restrict__ segs, const uint8_t* __restrict__ data,
-                            SubState* __restrict__ states, SubCount* __restrict__ counts) {
+                            SubState* __restrict__ piece_state, SubCount* __restrict__ counts) {
   __shared__ __align__(16) Tables tb;
   __shared__ ScanDesc sd;
   if (threadIdx.x == 0) sd = *sdp;
@@ -323,63 +393,101 @@ __global__ void k_seq_chain(const ScanDesc* __restrict__ sdp, const Tables* __re
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < sd.nseg; s += gridDim.x * blockDim.x) {
     const Segment& sg = segs[s];
     SubState st{0, 0, 0};
+    Reader r;
+    r.init(data, sg.byte0, sg.nbytes, 0);
     for (int i = 0; i + 1 < sg.nsub; i++) {
-      states[sg.sub0 + i] = st;
+      piece_state[sg.sub0 + i] = st;
       SubCount cnt{};
-      Reader r;
-      r.init(data + sg.byte0, sg.nbytes, st.bit);
       const long long stop = (long long)(i + 1) * kSubBits;
-      if (decode_run<false>(tb, sd, r, st, stop, LLONG_MAX, cnt, 0, nullptr, nullptr)) st = SubState{stop, 0, 0};
+      if (decode_run<false>(tb, sd, r, st, stop, LLONG_MAX, cnt, 0, nullptr, nullptr)) {
+        st = SubState{stop, 0, 0};
+        r.init(data, sg.byte0, sg.nbytes, stop);
+      }
       counts[sg.sub0 + i] = cnt;
     }
-    states[sg.sub0 + sg.nsub - 1] = st;
+    piece_state[sg.sub0 + sg.nsub - 1] = st;
   }
 }
 
-// Per segment, exclusive prefix sums of the block counts and DC sums over its subsequences (one thread per segment;
-// segments hold few subsequences on average, and a scan without restarts is one segment handled by a CTA-wide
-// scan below).
+// Per segment, exclusive prefix sums of the pieces' block counts and DC sums (one CTA per segment, 1024 pieces at a
+// time: warp shuffles, then the 32 warp totals).
 __global__ void __launch_bounds__(1024) k_seq_prefix(const ScanDesc* __restrict__ sdp, const Segment* __restrict__ segs,
                                                      const SubCount* __restrict__ counts, SubCount* __restrict__ base) {
-  __shared__ long long sb[1024];
-  __shared__ uint32_t sdc[4][1024];
+  __shared__ long long wb[32];
+  __shared__ uint32_t wd[4][32];
   const ScanDesc& sd = *sdp;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int s = blockIdx.x; s < sd.nseg; s += gridDim.x) {
     const Segment& sg = segs[s];
     long long carry_b = 0;
-    uint32_t carry_dc[4] = {0, 0, 0, 0};
+    uint32_t carry_d[4] = {0, 0, 0, 0};
     for (int off = 0; off < sg.nsub; off += 1024) {
       const int i = off + threadIdx.x;
-      // subsequence i starts after subsequences 0..i-1: shift by one (the last subsequence's counts are unused)
+      // piece i starts after pieces 0..i-1 (the last piece's counts are never needed)
       SubCount c{};
       if (i >= 1 && i < sg.nsub) c = counts[sg.sub0 + i - 1];
-      sb[threadIdx.x] = c.blocks;
-      for (int q = 0; q < 4; q++) sdc[q][threadIdx.x] = c.dc[q];
+      long long b = c.blocks;
+      uint32_t d[4] = {c.dc[0], c.dc[1], c.dc[2], c.dc[3]};
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long bo = __shfl_up_sync(0xffffffffu, b, o);
+        uint32_t dq[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) dq[q] = __shfl_up_sync(0xffffffffu, d[q], o);
+        if (lane >= o) {
+          b += bo;
+#pragma unroll
+          for (int q = 0; q < 4; q++) d[q] += dq[q];
+        }
+      }
+      if (lane == 31) {
+        wb[warp] = b;
+#pragma unroll
+        for (int q = 0; q < 4; q++) wd[q][warp] = d[q];
+      }
       __syncthreads();
-      for (int o = 1; o < 1024; o <<= 1) {
-        long long vb = threadIdx.x >= o ? sb[threadIdx.x - o] : 0;
-        uint32_t vd[4];
-        for (int q = 0; q < 4; q++) vd[q] = threadIdx.x >= o ? sdc[q][threadIdx.x - o] : 0;
-        __syncthreads();
-        sb[threadIdx.x] += vb;
-        for (int q = 0; q < 4; q++) sdc[q][threadIdx.x] += vd[q];
-        __syncthreads();
+      if (warp == 0) {
+        long long x = wb[lane];
+        uint32_t y[4] = {wd[0][lane], wd[1][lane], wd[2][lane], wd[3][lane]};
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const long long xo = __shfl_up_sync(0xffffffffu, x, o);
+          uint32_t yo[4];
+#pragma unroll
+          for (int q = 0; q < 4; q++) yo[q] = __shfl_up_sync(0xffffffffu, y[q], o);
+          if (lane >= o) {
+            x += xo;
+#pragma unroll
+            for (int q = 0; q < 4; q++) y[q] += yo[q];
+          }
+        }
+        wb[lane] = x;
+#pragma unroll
+        for (int q = 0; q < 4; q++) wd[q][lane] = y[q];
+      }
+      __syncthreads();
+      if (warp > 0) {
+        b += wb[warp - 1];
+#pragma unroll
+        for (int q = 0; q < 4; q++) d[q] += wd[q][warp - 1];
       }
       if (i < sg.nsub) {
         SubCount o;
-        o.blocks = carry_b + sb[threadIdx.x];
-        for (int q = 0; q < 4; q++) o.dc[q] = carry_dc[q] + sdc[q][threadIdx.x];
+        o.blocks = carry_b + b;
+#pragma unroll
+        for (int q = 0; q < 4; q++) o.dc[q] = carry_d[q] + d[q];
         base[sg.sub0 + i] = o;
       }
-      carry_b += sb[1023];
-      for (int q = 0; q < 4; q++) carry_dc[q] += sdc[q][1023];
+      carry_b += wb[31];
+#pragma unroll
+      for (int q = 0; q < 4; q++) carry_d[q] += wd[q][31];
       __syncthreads();
     }
   }
 }
 
 // Final pass: decode each subsequence from its exact start and write the coefficients.
-__global__ void __launch_bounds__(128) k_seq_write(const ScanDesc* __restrict__ sdp, const Tables* __restrict__ tg,
+__global__ void __launch_bounds__(kDecThreads) k_seq_write(const ScanDesc* __restrict__ sdp, const Tables* __restrict__ tg,
                                                    const Segment* __restrict__ segs, const uint8_t* __restrict__ data,
                                                    const SubState* __restrict__ states,
                                                    const SubCount* __restrict__ base, int16_t* __restrict__ out,
@@ -388,9 +496,17 @@ __global__ void __launch_bounds__(128) k_seq_write(const ScanDesc* __restrict__ 
   __shared__ ScanDesc sd;
   if (threadIdx.x == 0) sd = *sdp;
   load_tables(tb, tg);
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr long long kWin = (long long)kDecThreads * (kSubBits / 8 + 4) + kTail + 32;
+  __shared__ __align__(16) uint8_t win[kWin];
+  __shared__ long long w_lo, w_hi;
+  const long long t0 = (long long)blockIdx.x * blockDim.x;
+  if (threadIdx.x == 0) unit_window(segs, sd.nseg, t0, blockDim.x, sd.nsub, false, kWin & ~15ll, &w_lo, &w_hi);
+  __syncthreads();
+  load_window(data, w_lo, w_hi, win);
+  __syncthreads();
+  const long long t = t0 + threadIdx.x;
   if (t >= sd.nsub) return;
-  const SubRef ref = find_sub(segs, sd.nseg, t);
+  const SubRef ref = find_sub(segs, sd.nseg, t, false);
   const Segment& sg = segs[ref.seg];
   const SubCount b = base[t];
   if (b.blocks >= sg.nblocks) return;  // past the segment's last block: padding
@@ -402,7 +518,7 @@ __global__ void __launch_bounds__(128) k_seq_write(const ScanDesc* __restrict__ 
   SubCount cnt{};
   uint32_t pred[4] = {b.dc[0], b.dc[1], b.dc[2], b.dc[3]};
   Reader r;
-  r.init(data + sg.byte0, sg.nbytes, st.bit);
+  r.init(data, sg.byte0, sg.nbytes, st.bit, win, w_lo, w_hi);
   const long long stop = ref.local + 1 < sg.nsub ? (long long)(ref.local + 1) * kSubBits : LLONG_MAX;
   if (decode_run<true>(tb, sd, r, st, stop, sg.nblocks - b.blocks, cnt, sg.block0 + b.blocks, pred, out))
     atomicCAS(error, 0, 1);
@@ -610,7 +726,7 @@ int parse_jpeg(rcg_ctx* ctx, const uint8_t* d, size_t len, Parsed& P) {
       const long long nseg = (total + seg_mcus - 1) / seg_mcus;
       size_t p = pos;
       bool dead = false;
-      long long sub = 0;
+      long long sub = 0, span = 0;
       for (long long s = 0; s < nseg; s++) {
         Segment g;
         g.byte0 = (long long)sc.bytes.size();
@@ -628,12 +744,16 @@ int parse_jpeg(rcg_ctx* ctx, const uint8_t* d, size_t len, Parsed& P) {
         g.nsub = (int)std::max<long long>(1, (g.nbytes * 8 + kSubBits - 1) / kSubBits);
         g.sub0 = sub;
         sub += g.nsub;
+        g.nspan = (g.nsub + kSpanSubs - 1) / kSpanSubs;
+        g.span0 = span;
+        span += g.nspan;
         sc.segs.push_back(g);
         // keep segments 4-byte aligned in the buffer
         while (sc.bytes.size() % 4) sc.bytes.push_back(0);
       }
       sc.sd.nseg = (int)nseg;
       sc.sd.nsub = sub;
+      sc.sd.nspan = span;
       pos = p;  // the marker search resumes where the entropy data stopped (decode.rs:1100-1101)
       P.scans.push_back(std::move(sc));
     }
@@ -710,52 +830,69 @@ int jpeg_decode(rcg_ctx* ctx, const uint8_t* data, size_t len, rcg_jpeg_info* in
   cudaMemsetAsync(d_out, 0, (size_t)nblocks * 128, ctx->stream);
   cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream);
   int h_changed = 0;
+  int rounds_max = 0;
+  bool fell_back = false;
   for (HostScan& sc : P.scans) {
     std::memcpy(sc.sd.fc, fc, sizeof fc);
-    const long long nsub = sc.sd.nsub;
-    uint8_t* d_bytes = (uint8_t*)workspace(ctx, "dec_bytes", std::max<size_t>(sc.bytes.size(), 16));
+    const long long nsub = sc.sd.nsub, nspan = sc.sd.nspan;
+    // Padded: a CTA's shared-memory window covers whole units plus kTail bytes, rounded up to 16, so it may run up
+    // to one span (256 B) + kTail + 15 bytes past the last segment's data.
+    uint8_t* d_bytes = (uint8_t*)workspace(ctx, "dec_bytes", sc.bytes.size() + 1024);
     Segment* d_segs = (Segment*)workspace(ctx, "dec_segs", sizeof(Segment) * sc.segs.size());
-    SubState* d_s0 = (SubState*)workspace(ctx, "dec_state0", sizeof(SubState) * (size_t)nsub);
-    SubState* d_s1 = (SubState*)workspace(ctx, "dec_state1", sizeof(SubState) * (size_t)nsub);
+    SubState* d_s0 = (SubState*)workspace(ctx, "dec_state0", sizeof(SubState) * (size_t)nspan);
+    SubState* d_s1 = (SubState*)workspace(ctx, "dec_state1", sizeof(SubState) * (size_t)nspan);
+    SubState* d_piece = (SubState*)workspace(ctx, "dec_pieces", sizeof(SubState) * (size_t)nsub);
     SubCount* d_cnt = (SubCount*)workspace(ctx, "dec_counts", sizeof(SubCount) * (size_t)nsub);
     SubCount* d_base = (SubCount*)workspace(ctx, "dec_base", sizeof(SubCount) * (size_t)nsub);
     int* d_changed = (int*)workspace(ctx, "dec_changed", sizeof(int));
-    if (!d_bytes || !d_segs || !d_s0 || !d_s1 || !d_cnt || !d_base || !d_changed) return RCG_NO_MEMORY;
+    if (!d_bytes || !d_segs || !d_s0 || !d_s1 || !d_piece || !d_cnt || !d_base || !d_changed) return RCG_NO_MEMORY;
     if (!sc.bytes.empty() && (rc = copy_to_device(ctx, d_bytes, sc.bytes.data(), sc.bytes.size())) != RCG_OK)
       return rc;
     cudaMemcpyAsync(d_segs, sc.segs.data(), sizeof(Segment) * sc.segs.size(), cudaMemcpyHostToDevice, ctx->stream);
     cudaMemcpyAsync(d_sd, &sc.sd, sizeof(ScanDesc), cudaMemcpyHostToDevice, ctx->stream);
     cudaMemcpyAsync(d_tab, &sc.tables, sizeof(Tables), cudaMemcpyHostToDevice, ctx->stream);
-    // Initial guesses: every subsequence starts at its first bit, first block of the MCU, at a DC.
-    std::vector<SubState> init((size_t)nsub);
+    // Initial guesses: every span starts at its first bit, first block of the MCU, at a DC.
+    std::vector<SubState> init((size_t)nspan);
     for (const Segment& g : sc.segs)
-      for (int i = 0; i < g.nsub; i++) init[g.sub0 + i] = SubState{(long long)i * kSubBits, 0, 0};
-    cudaMemcpyAsync(d_s0, init.data(), sizeof(SubState) * (size_t)nsub, cudaMemcpyHostToDevice, ctx->stream);
+      for (int i = 0; i < g.nspan; i++) init[g.span0 + i] = SubState{(long long)i * kSpanSubs * kSubBits, 0, 0};
+    cudaMemcpyAsync(d_s0, init.data(), sizeof(SubState) * (size_t)nspan, cudaMemcpyHostToDevice, ctx->stream);
     cudaMemsetAsync(d_cnt, 0, sizeof(SubCount) * (size_t)nsub, ctx->stream);
-    const unsigned grid = (unsigned)((nsub + 127) / 128);
+    const unsigned grid_span = (unsigned)((nspan + kDecThreads - 1) / kDecThreads);
+    const unsigned grid = (unsigned)((nsub + kDecThreads - 1) / kDecThreads);
     SubState* cur = d_s0;
     SubState* nxt = d_s1;
     bool settled = false;
-    for (int round = 0; round < kMaxRounds; round++) {
-      cudaMemsetAsync(d_changed, 0, sizeof(int), ctx->stream);
-      RCG_LAUNCH(ctx, "seq_sync", k_seq_sync, grid, 128, 0, d_sd, d_tab, d_segs, d_bytes, cur, nxt, d_cnt,
-                 d_changed);
+    int round = 0;
+    while (round < kMaxRounds) {
+      // A few rounds back to back (most streams settle within them), then one round per check: the check of a
+      // batch looks at its last round only, which changes nothing exactly when the states have settled.
+      const int batch = round == 0 ? kFirstBatch : 1;
+      for (int b = 0; b < batch; b++, round++) {
+        if (b == batch - 1) cudaMemsetAsync(d_changed, 0, sizeof(int), ctx->stream);
+        RCG_LAUNCH(ctx, "seq_sync", k_seq_sync, grid_span, kDecThreads, 0, d_sd, d_tab, d_segs, d_bytes, cur, nxt,
+                   d_piece, d_cnt, d_changed);
+        std::swap(cur, nxt);
+      }
       cudaMemcpyAsync(&h_changed, d_changed, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
       cudaError_t e = cudaStreamSynchronize(ctx->stream);
       if (e != cudaSuccess) return cuda_fail(ctx, e, "JPEG decode");
-      std::swap(cur, nxt);
       if (!h_changed) {
         settled = true;
         break;
       }
     }
+    if (settled)
+      rounds_max = std::max(rounds_max, round);
+    else
+      fell_back = true;
     if (!settled) {
       RCG_LAUNCH(ctx, "seq_chain", k_seq_chain, (unsigned)std::min<long long>((sc.sd.nseg + 127) / 128, 1024), 128, 0,
-                 d_sd, d_tab, d_segs, d_bytes, cur, d_cnt);
+                 d_sd, d_tab, d_segs, d_bytes, d_piece, d_cnt);
     }
     RCG_LAUNCH(ctx, "seq_prefix", k_seq_prefix, (unsigned)std::min(sc.sd.nseg, 1024), 1024, 0, d_sd, d_segs, d_cnt,
                d_base);
-    RCG_LAUNCH(ctx, "seq_write", k_seq_write, grid, 128, 0, d_sd, d_tab, d_segs, d_bytes, cur, d_base, d_out, d_err);
+    RCG_LAUNCH(ctx, "seq_write", k_seq_write, grid, kDecThreads, 0, d_sd, d_tab, d_segs, d_bytes, d_piece, d_base,
+               d_out, d_err);
   }
   int h_err = 0;
   cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
@@ -763,6 +900,7 @@ int jpeg_decode(rcg_ctx* ctx, const uint8_t* data, size_t len, rcg_jpeg_info* in
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "JPEG decode");
   if (h_err) return fail(ctx, RCG_INVALID, h_err == 1 ? "bad JPEG entropy-coded data" : "JPEG decode lost its place");
+  if (info) info->sync_rounds = fell_back ? -1 : rounds_max;
   if (!coefs_on_device) return copy_to_host(ctx, coefs, d_out, (size_t)nblocks * 128);
   return RCG_OK;
 }

@@ -87,7 +87,7 @@ class _QTables(ctypes.Structure):
 
 class _JpegInfo(ctypes.Structure):
     _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("ids", ctypes.c_uint8 * 4),
-                ("scans", ctypes.c_int32)]
+                ("scans", ctypes.c_int32), ("sync_rounds", ctypes.c_int32)]
 
 
 class _Scan(ctypes.Structure):
@@ -430,6 +430,7 @@ class Context:
         coefs = np.empty(lay.ncoefs, dtype=np.int16)
         self._check(_lib.rcg_decode_coefs(self._ptr, buf.ctypes.data, buf.size, ctypes.byref(info), ctypes.byref(lay),
                                           ctypes.byref(t), coefs.ctypes.data, coefs.size))
+        self.last_decode_rounds = int(info.sync_rounds)
         comps, off = [], 0
         for i in range(lay.ncomp):
             n = lay.blocks_w[i] * lay.blocks_h[i] * 64
@@ -447,6 +448,7 @@ class Context:
         self._check(_lib.rcg_decode_coefs_device(self._ptr, buf.ctypes.data, buf.size, ctypes.byref(info),
                                                  ctypes.byref(lay), ctypes.byref(t), ctypes.c_void_p(coefs_ptr),
                                                  coefs_len))
+        self.last_decode_rounds = int(info.sync_rounds)
         return int(info.width), int(info.height), lay, t, bytes(info.ids[: lay.ncomp])
 
     def search_requantize_device(self, width, height, layout, tables, src_ptr, out_ptr, coefs_len, target,

@@ -80,6 +80,7 @@ def test_decode_12mp(ctx, oracle):
         data = oracle.write_jpeg_variant(g, ri, False)
         ci = ctx.decode_coefs(data)
         assert np.array_equal(ci.flat(), g.coefs), (ri, q)
+        print(f"q{q} ri{ri}: {len(data)} bytes, {ctx.last_decode_rounds} synchronization rounds")
 
 
 def test_decode_reference_fixtures(ctx, oracle):
