@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(kTileThreads, 3)
   if (tid < kScoreSums) {
     double acc = 0.0;
     for (int wi = 0; wi < kTileThreads / 32; wi++) acc += (double)s_red[wi][tid];
-    partials[(size_t)blk * kScoreSums + tid] = acc;
+    partials[(size_t)tid * pd.total_tiles + blk] = acc;  // sum-major: the reduction reads each sum contiguously
   }
 }
 
@@ -352,7 +352,8 @@ __global__ void __launch_bounds__(256) k_ssim2_reduce(PyramidDesc pd, const doub
   const ScaleDesc sd = pd.s[s];
   const int n = sd.tiles_x * sd.tiles_y;
   double acc = 0.0;
-  for (int t = threadIdx.x; t < n; t += 256) acc += partials[(size_t)(sd.tile0 + t) * kScoreSums + i];
+  const double* col = partials + (size_t)i * pd.total_tiles + sd.tile0;
+  for (int t = threadIdx.x; t < n; t += 256) acc += col[t];
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
