@@ -511,8 +511,8 @@ def main():
     tile_ms = tiles["ms"] / max(1, tiles["launches"])
     alg_bytes = 6.0 * W * H  # two RGB8 images per score (full-resolution pixels)
     achieved = alg_bytes / (tile_ms / 1000.0) / 1e9
-    # DRAM bytes of one launch at this workload size from the committed ncu capture (profiles/ssim2_tiles_12mp.md:
-    # dram__bytes_read.sum + dram__bytes_write.sum); None for other sizes.
+    # DRAM bytes of one launch at this workload size from an ncu capture of the same kernel (dram__bytes_read.sum +
+    # dram__bytes_write.sum: 384.0 MB + 5.5 MB); None for other sizes.
     traffic = 389.48e6 if (W, H) == (4000, 3000) else None
     roof = {"kernel": "ssim2_tiles", "bound": "hbm", "achieved": achieved, "peak": hbm or 6800.0,
             "unit": "GB/s", "frac": achieved / (hbm or 6800.0), "traffic": traffic,
