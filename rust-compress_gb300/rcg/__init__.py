@@ -574,7 +574,7 @@ class Context:
         for i, (a, w, h, c, _) in enumerate(arrs):
             f = found[i]
             lay = self.coef_layout(w, h, c, EncodeOptions(f.quality, opts.subsampling, opts.trellis))
-            ci = _coef_image(w, h, lay, coefs[i][: lay.ncoefs].copy(), qts[i])
+            ci = _coef_image(w, h, lay, coefs[i][: lay.ncoefs], qts[i])  # each image has its own buffer
             trace = [(int(f.trace_q[k]), float(f.trace_score[k])) for k in range(f.nsteps)]
             out.append(Found(int(f.quality), float(f.score), ci, trace))
         return out
