@@ -196,6 +196,16 @@ int rcg_metric_score(rcg_ctx* ctx, int metric, const uint8_t* reference, const u
 int rcg_metric_score_device(rcg_ctx* ctx, int metric, const uint8_t* d_reference, const uint8_t* d_candidate,
                             uint32_t width, uint32_t height, int channels, double* score);
 
+/* The derivative of SSIMULACRA2 (core/src/ssimulacra2.rs:471) with respect to the distorted image, in FP64: the
+ * reference is 8-bit RGB, the distorted image RGB float samples in [0, 255] taken as continuous values (linear light
+ * by the sRGB curve itself, of which the scorer's 8-bit table is a sampling). Writes the FP64 score and
+ * d score / d sample (w x h x 3 doubles, interleaved like the image; grad NULL: the score alone). Host buffers. */
+int rcg_ssimulacra2_grad(rcg_ctx* ctx, const uint8_t* reference, const float* distorted, uint32_t width,
+                         uint32_t height, double* score, double* grad);
+/* As rcg_ssimulacra2_grad with all three images in device memory. */
+int rcg_ssimulacra2_grad_device(rcg_ctx* ctx, const uint8_t* d_reference, const float* d_distorted, uint32_t width,
+                                uint32_t height, double* score, double* d_grad);
+
 /* The JPEG quality search for a goal metric (cli/src/pipeline.rs:207-222): RCG_METRIC_SSIMULACRA2 (as rcg_search) or
  * RCG_METRIC_SSIM (`--target-ssim`, jpeg/src/target.rs:24; any image size). */
 int rcg_search_metric(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels, int metric,

@@ -1135,6 +1135,304 @@ static int ssimulacra2_t(const uint8_t* ra, const uint8_t* da, int w, int h, int
   return 0;
 }
 
+// ------------------------------------------------------------------------------------------------ SSIMULACRA2 adjoint
+
+// The score as a differentiable function of the distorted image's RGB samples taken as continuous values in
+// [0, 255] (FP64 throughout): linear light by the sRGB curve itself (core/src/ssimulacra2.rs:172-175, of which the
+// reference's 8-bit table is a sampling), then exactly the scorer's steps (:471-512). For integer samples it equals
+// the FP64 scorer. grad64 is its reverse-mode derivative, every step's adjoint taken in turn: the 108-term sum and
+// the final mapping, the L1/L4 norms, the SSIM and edge maps (one-sided derivatives at the max(., 0) and |.|
+// kinks), the separable blurs (the horizontal pass with zero padding is its own transpose; the vertical pass's
+// mirrored taps scatter back), the XYB transform, the 2x2 pyramid and the sRGB curve.
+
+struct Img64 {
+  int w = 0, h = 0;
+  std::vector<double> ch[3];
+};
+
+static double srgb_deriv(double v255) {  // d srgb_to_linear(v / 255) / dv
+  const double v = v255 / 255.0;
+  if (v <= 0.04045) return 1.0 / (12.92 * 255.0);
+  return 2.4 * std::pow((v + 0.055) / 1.055, 1.4) / (1.055 * 255.0);
+}
+
+static Img64 down64(const Img64& p) {
+  Img64 o;
+  o.w = (p.w + 1) / 2;
+  o.h = (p.h + 1) / 2;
+  for (int c = 0; c < 3; c++) {
+    o.ch[c].assign((size_t)o.w * o.h, 0.0);
+    for (int oy = 0; oy < o.h; oy++)
+      for (int ox = 0; ox < o.w; ox++) {
+        int x1 = std::min(2 * ox + 2, p.w), y1 = std::min(2 * oy + 2, p.h);
+        double sum = 0.0;
+        for (int y = 2 * oy; y < y1; y++)
+          for (int x = 2 * ox; x < x1; x++) sum += p.ch[c][(size_t)y * p.w + x];
+        o.ch[c][(size_t)oy * o.w + ox] = sum / (double)((y1 - 2 * oy) * (x1 - 2 * ox));
+      }
+  }
+  return o;
+}
+
+// Row blur with zero padding (blur_row, :273-319) and column blur with mirrored rows (:385-397).
+static void hblur64(const std::vector<double>& src, std::vector<double>& dst, int w, int h, const double* k) {
+  dst.assign((size_t)w * h, 0.0);
+  for (int y = 0; y < h; y++)
+    for (int x = 0; x < w; x++) {
+      double s = 0.0;
+      for (int t = 0; t <= 2 * RADIUS; t++) {
+        int xx = x + t - RADIUS;
+        if (xx >= 0 && xx < w) s += k[t] * src[(size_t)y * w + xx];
+      }
+      dst[(size_t)y * w + x] = s;
+    }
+}
+static inline int mirror64(int yy, int h) { return yy < 0 ? -yy - 1 : (yy >= h ? 2 * h - 1 - yy : yy); }
+static void vblur64(const std::vector<double>& src, std::vector<double>& dst, int w, int h, const double* k) {
+  dst.assign((size_t)w * h, 0.0);
+  for (int y = 0; y < h; y++)
+    for (int t = 0; t <= 2 * RADIUS; t++) {
+      const double* r = &src[(size_t)mirror64(y + t - RADIUS, h) * w];
+      for (int x = 0; x < w; x++) dst[(size_t)y * w + x] += k[t] * r[x];
+    }
+}
+static void vblur64_t(const std::vector<double>& g, std::vector<double>& out, int w, int h, const double* k) {
+  out.assign((size_t)w * h, 0.0);
+  for (int y = 0; y < h; y++)
+    for (int t = 0; t <= 2 * RADIUS; t++) {
+      double* r = &out[(size_t)mirror64(y + t - RADIUS, h) * w];
+      for (int x = 0; x < w; x++) r[x] += k[t] * g[(size_t)y * w + x];
+    }
+}
+
+struct ScaleFwd {
+  int w, h;
+  std::vector<double> xa[3], xb[3];   // XYB of both images
+  std::vector<double> mom[3][5];      // blurred m1, m2, s11, s22, s12 per channel
+  double sums[3][6];
+};
+
+static void xyb_planes(const Img64& p, std::vector<double> out[3]) {
+  const size_t n = (size_t)p.w * p.h;
+  for (int c = 0; c < 3; c++) out[c].assign(n, 0.0);
+  for (size_t i = 0; i < n; i++) {
+    double v[3];
+    xyb(p.ch[0][i], p.ch[1][i], p.ch[2][i], v);
+    for (int c = 0; c < 3; c++) out[c][i] = v[c];
+  }
+}
+
+static void scale_forward(const Img64& a, const Img64& b, const double* k, ScaleFwd& f) {
+  f.w = a.w;
+  f.h = a.h;
+  const int w = a.w, h = a.h;
+  const size_t n = (size_t)w * h;
+  xyb_planes(a, f.xa);
+  xyb_planes(b, f.xb);
+  std::vector<double> tmp(n), hb;
+  for (int c = 0; c < 3; c++) {
+    for (int q = 0; q < 5; q++) {
+      for (size_t i = 0; i < n; i++) {
+        const double xa = f.xa[c][i], xb = f.xb[c][i];
+        tmp[i] = q == 0 ? xa : q == 1 ? xb : q == 2 ? xa * xa : q == 3 ? xb * xb : xa * xb;
+      }
+      hblur64(tmp, hb, w, h, k);
+      vblur64(hb, f.mom[c][q], w, h, k);
+    }
+    for (int j = 0; j < 6; j++) f.sums[c][j] = 0.0;
+    for (size_t i = 0; i < n; i++) {
+      const double m1 = f.mom[c][0][i], m2 = f.mom[c][1][i];
+      const double num_m = 1.0 - (m1 - m2) * (m1 - m2);
+      const double num_s = 2.0 * (f.mom[c][4][i] - m1 * m2) + C2;
+      const double den_s = (f.mom[c][2][i] - m1 * m1) + (f.mom[c][3][i] - m2 * m2) + C2;
+      const double d = std::max(1.0 - num_m * num_s / den_s, 0.0);
+      const double d1 = (1.0 + std::fabs(f.xb[c][i] - m2)) / (1.0 + std::fabs(f.xa[c][i] - m1)) - 1.0;
+      const double art = std::max(d1, 0.0), det = std::max(-d1, 0.0);
+      f.sums[c][0] += d;
+      f.sums[c][1] += (d * d) * (d * d);
+      f.sums[c][2] += art;
+      f.sums[c][3] += (art * art) * (art * art);
+      f.sums[c][4] += det;
+      f.sums[c][5] += (det * det) * (det * det);
+    }
+  }
+}
+
+static Img64 linear64(const double* rgb, int w, int h) {
+  Img64 o;
+  o.w = w;
+  o.h = h;
+  for (int c = 0; c < 3; c++) o.ch[c].assign((size_t)w * h, 0.0);
+  for (size_t i = 0; i < (size_t)w * h; i++)
+    for (int c = 0; c < 3; c++) o.ch[c][i] = srgb_to_linear(rgb[i * 3 + c] / 255.0);
+  return o;
+}
+
+// Forward pass at every scale; returns the score (100 when the weighted sum is not positive).
+static double score64(const double* ref, const double* dist, int w, int h, std::vector<ScaleFwd>* keep,
+                      std::vector<Img64>* pyr_b) {
+  double k[2 * RADIUS + 1];
+  gauss_kernel(k);
+  Img64 a = linear64(ref, w, h), b = linear64(dist, w, h);
+  std::vector<std::array<std::array<double, 6>, 3>> scales;
+  for (int s = 0; s < NUM_SCALES; s++) {
+    if (a.w < 8 || a.h < 8) break;
+    ScaleFwd f;
+    scale_forward(a, b, k, f);
+    const double count = (double)a.w * (double)a.h;
+    std::array<std::array<double, 6>, 3> arr;
+    for (int c = 0; c < 3; c++)
+      for (int m = 0; m < 3; m++) {
+        arr[c][2 * m] = f.sums[c][2 * m] / count;
+        arr[c][2 * m + 1] = std::pow(f.sums[c][2 * m + 1] / count, 0.25);
+      }
+    scales.push_back(arr);
+    if (pyr_b) pyr_b->push_back(b);
+    if (keep) keep->push_back(std::move(f));
+    if (s + 1 < NUM_SCALES) {
+      a = down64(a);
+      b = down64(b);
+    }
+  }
+  return final_score(scales);
+}
+
+// d score / d dist (RGB, w x h x 3). Returns the score.
+static double grad64(const double* ref, const double* dist, int w, int h, double* grad) {
+  double k[2 * RADIUS + 1];
+  gauss_kernel(k);
+  std::vector<ScaleFwd> F;
+  std::vector<Img64> B;
+  const double score = score64(ref, dist, w, h, &F, &B);
+  const int ns = (int)F.size();
+  std::memset(grad, 0, sizeof(double) * (size_t)w * h * 3);
+  // final mapping and the weighted sum (:491-511): d score / d stat
+  double sum = 0.0;
+  std::vector<std::array<std::array<double, 6>, 3>> st(ns);
+  for (int s = 0; s < ns; s++) {
+    const double count = (double)F[s].w * F[s].h;
+    for (int c = 0; c < 3; c++)
+      for (int m = 0; m < 3; m++) {
+        st[s][c][2 * m] = F[s].sums[c][2 * m] / count;
+        st[s][c][2 * m + 1] = std::pow(F[s].sums[c][2 * m + 1] / count, 0.25);
+      }
+  }
+  std::vector<std::array<std::array<double, 6>, 3>> wst(ns);  // weight of each stat in the sum
+  int i = 0;
+  for (int c = 0; c < 3; c++)
+    for (int s = 0; s < ns; s++)
+      for (int n = 0; n < 2; n++)
+        for (int m = 0; m < 3; m++) {
+          wst[s][c][2 * m + n] = WEIGHTS[i];
+          sum += WEIGHTS[i] * std::fabs(st[s][c][2 * m + n]);
+          i++;
+        }
+  const double kq = 0.9562382616834844;
+  const double q = sum * kq;
+  const double P = 2.326765642916932 * q - 0.020884521182843837 * q * q + 6.248496625763138e-05 * q * q * q;
+  if (!(P > 0.0)) return score;
+  const double e = 0.6276336467831387;
+  const double dscore_dsum =
+      -10.0 * e * std::pow(P, e - 1.0) *
+      (2.326765642916932 - 2.0 * 0.020884521182843837 * q + 3.0 * 6.248496625763138e-05 * q * q) * kq;
+  std::vector<double> gB[3];  // gradient w.r.t. the linear dist planes of the current scale (coarsest first)
+  for (int s = ns - 1; s >= 0; s--) {
+    const ScaleFwd& f = F[s];
+    const int sw = f.w, sh = f.h;
+    const size_t n = (size_t)sw * sh;
+    const double count = (double)n;
+    std::vector<double> gLin[3];
+    for (int c = 0; c < 3; c++) gLin[c].assign(n, 0.0);
+    std::vector<double> gxb[3];
+    for (int c = 0; c < 3; c++) {
+      // d score / d map(x) for the six norms: L1 -> 1/count, L4 -> map^3 (S/count)^-3/4 / count
+      double g1[3], g4[3];
+      for (int m = 0; m < 3; m++) {
+        // stats are >= 0: |.| has derivative 1
+        g1[m] = dscore_dsum * wst[s][c][2 * m] / count;
+        const double mean4 = f.sums[c][2 * m + 1] / count;
+        g4[m] = mean4 > 0.0 ? dscore_dsum * wst[s][c][2 * m + 1] * std::pow(mean4, -0.75) / count : 0.0;
+      }
+      std::vector<double> gm[5];
+      for (int qq = 0; qq < 5; qq++) gm[qq].assign(n, 0.0);
+      gxb[c].assign(n, 0.0);
+      for (size_t p = 0; p < n; p++) {
+        const double m1 = f.mom[c][0][p], m2 = f.mom[c][1][p];
+        const double s11 = f.mom[c][2][p], s22 = f.mom[c][3][p], s12 = f.mom[c][4][p];
+        const double num_m = 1.0 - (m1 - m2) * (m1 - m2);
+        const double num_s = 2.0 * (s12 - m1 * m2) + C2;
+        const double den_s = (s11 - m1 * m1) + (s22 - m2 * m2) + C2;
+        const double dv = 1.0 - num_m * num_s / den_s;
+        const double d = std::max(dv, 0.0);
+        const double gd = g1[0] + g4[0] * d * d * d;
+        if (dv > 0.0) {
+          const double g_num_m = -gd * num_s / den_s, g_num_s = -gd * num_m / den_s;
+          const double g_den = gd * num_m * num_s / (den_s * den_s);
+          gm[0][p] += g_num_m * (-2.0 * (m1 - m2)) + g_num_s * (-2.0 * m2) + g_den * (-2.0 * m1);
+          gm[1][p] += g_num_m * (2.0 * (m1 - m2)) + g_num_s * (-2.0 * m1) + g_den * (-2.0 * m2);
+          gm[2][p] += g_den;
+          gm[3][p] += g_den;
+          gm[4][p] += 2.0 * g_num_s;
+        }
+        const double xa = f.xa[c][p], xb = f.xb[c][p];
+        const double Nn = 1.0 + std::fabs(xb - m2), Dn = 1.0 + std::fabs(xa - m1);
+        const double d1 = Nn / Dn - 1.0;
+        const double art = std::max(d1, 0.0), det = std::max(-d1, 0.0);
+        const double gd1 = (d1 > 0.0 ? g1[1] + g4[1] * art * art * art : 0.0) -
+                           (d1 < 0.0 ? g1[2] + g4[2] * det * det * det : 0.0);
+        const double sb = xb - m2 > 0.0 ? 1.0 : (xb - m2 < 0.0 ? -1.0 : 0.0);
+        const double sa = xa - m1 > 0.0 ? 1.0 : (xa - m1 < 0.0 ? -1.0 : 0.0);
+        gxb[c][p] += gd1 * sb / Dn;
+        gm[1][p] += -gd1 * sb / Dn;
+        gm[0][p] += gd1 * Nn / (Dn * Dn) * sa;
+      }
+      // blur adjoints for the moments that depend on the dist image: m2 = G(xb), s22 = G(xb^2), s12 = G(xa xb)
+      std::vector<double> t1, t2;
+      for (int qq : {1, 3, 4}) {
+        vblur64_t(gm[qq], t1, sw, sh, k);
+        hblur64(t1, t2, sw, sh, k);  // zero-padded symmetric row blur is its own transpose
+        for (size_t p = 0; p < n; p++) {
+          const double fac = qq == 1 ? 1.0 : qq == 3 ? 2.0 * f.xb[c][p] : f.xa[c][p];
+          gxb[c][p] += fac * t2[p];
+        }
+      }
+    }
+    // XYB adjoint (:249-258) to the linear dist planes of this scale
+    const double cbb = std::cbrt(BIAS);
+    (void)cbb;
+    const Img64& lb = B[s];
+    for (size_t p = 0; p < n; p++) {
+      const double r = lb.ch[0][p], g = lb.ch[1][p], bl = lb.ch[2][p];
+      const double u[3] = {M00 * r + M01 * g + M02 * bl + BIAS, M10 * r + M11 * g + M12 * bl + BIAS,
+                           M20 * r + M21 * g + M22 * bl + BIAS};
+      double dm[3];
+      for (int j = 0; j < 3; j++) dm[j] = u[j] > 0.0 ? 1.0 / (3.0 * std::cbrt(u[j]) * std::cbrt(u[j])) : 0.0;
+      // X = 7 (m0 - m1) + 0.42, Y = (m0 + m1) / 2 + 0.01, B = m2 - (m0 + m1) / 2 + 0.55
+      const double gX = gxb[0][p], gY = gxb[1][p], gBb = gxb[2][p];
+      const double g_m0 = 7.0 * gX + 0.5 * gY - 0.5 * gBb, g_m1 = -7.0 * gX + 0.5 * gY - 0.5 * gBb, g_m2 = gBb;
+      const double gu[3] = {g_m0 * dm[0], g_m1 * dm[1], g_m2 * dm[2]};
+      gLin[0][p] += gu[0] * M00 + gu[1] * M10 + gu[2] * M20;
+      gLin[1][p] += gu[0] * M01 + gu[1] * M11 + gu[2] * M21;
+      gLin[2][p] += gu[0] * M02 + gu[1] * M12 + gu[2] * M22;
+    }
+    // plus the coarser scales' gradients, spread back over each 2x2 block
+    if (s + 1 < ns) {
+      const int cw = F[s + 1].w;
+      for (int c = 0; c < 3; c++)
+        for (int y = 0; y < sh; y++)
+          for (int x = 0; x < sw; x++) {
+            const int ox = x / 2, oy = y / 2;
+            const int nx = std::min(2 * ox + 2, sw) - 2 * ox, ny = std::min(2 * oy + 2, sh) - 2 * oy;
+            gLin[c][(size_t)y * sw + x] += gB[c][(size_t)oy * cw + ox] / (double)(nx * ny);
+          }
+    }
+    for (int c = 0; c < 3; c++) gB[c] = std::move(gLin[c]);
+  }
+  for (size_t p = 0; p < (size_t)w * h; p++)
+    for (int c = 0; c < 3; c++) grad[p * 3 + c] = gB[c][p] * srgb_deriv(dist[p * 3 + c]);
+  return score;
+}
+
 // ------------------------------------------------------------------------------------------------ search
 
 // jpeg/src/target.rs:12-56 (find_quality_with) with the metric of cli/src/pipeline.rs:214-219
@@ -2636,6 +2934,15 @@ long orc_write_jpeg_variant(int w, int h, int ncomp, const int* hs, const int* v
   std::vector<uint8_t> bytes = orc::write_jpeg_variant(ci, restart_interval, per_component != 0);
   if (out) std::memcpy(out, bytes.data(), std::min<size_t>(bytes.size(), (size_t)cap));
   return (long)bytes.size();
+}
+
+// The FP64 score of a continuous-valued distorted image (RGB, w x h x 3 doubles in [0, 255]) against ref, and its
+// gradient (grad may be NULL).
+double orc_score64(const double* ref, const double* dist, int w, int h) {
+  return orc::score64(ref, dist, w, h, nullptr, nullptr);
+}
+double orc_grad64(const double* ref, const double* dist, int w, int h, double* grad) {
+  return orc::grad64(ref, dist, w, h, grad);
 }
 
 }  // extern "C"

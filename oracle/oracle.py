@@ -44,6 +44,10 @@ def lib():
             getattr(L, name).argtypes = [P, P, i32, i32, i32]
             getattr(L, name).restype = ctypes.c_double
         L.orc_ms_ssim.argtypes = [P, P, i32, i32, i32, P]
+        for name in ("orc_score64", "orc_grad64"):
+            getattr(L, name).restype = ctypes.c_double
+        L.orc_score64.argtypes = [P, P, i32, i32]
+        L.orc_grad64.argtypes = [P, P, i32, i32, P]
         L.orc_ms_ssim.restype = ctypes.c_double
         L.orc_write_best.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, ctypes.c_long, pi]
         L.orc_write_best.restype = ctypes.c_long
@@ -355,4 +359,22 @@ def write_jpeg_variant(g, restart_interval=0, per_component=False):
     out = np.zeros(size, np.uint8)
     lib().orc_write_jpeg_variant(*g.args(), int(restart_interval), 1 if per_component else 0, out.ctypes.data, size)
     return out.tobytes()
+
+
+def score64(ref, dist):
+    """FP64 SSIMULACRA2 with the distorted RGB image as continuous values (float array (h, w, 3) in [0, 255])."""
+    r = np.ascontiguousarray(ref, dtype=np.float64)
+    d = np.ascontiguousarray(dist, dtype=np.float64)
+    h, w = r.shape[:2]
+    return lib().orc_score64(r.ctypes.data, d.ctypes.data, w, h)
+
+
+def grad64(ref, dist):
+    """(score, d score / d dist) of score64, the gradient as a float64 (h, w, 3) array."""
+    r = np.ascontiguousarray(ref, dtype=np.float64)
+    d = np.ascontiguousarray(dist, dtype=np.float64)
+    h, w = r.shape[:2]
+    g = np.zeros((h, w, 3), np.float64)
+    s = lib().orc_grad64(r.ctypes.data, d.ctypes.data, w, h, g.ctypes.data)
+    return s, g
 

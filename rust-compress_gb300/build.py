@@ -34,6 +34,7 @@ UNITS = {
     "plan.cu": [],
     "metrics.cu": [],
     "jpegdec.cu": [],
+    "adjoint.cu": [],
 }
 
 

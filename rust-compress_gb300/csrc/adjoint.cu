@@ -1,0 +1,410 @@
+// Reverse-mode derivative of SSIMULACRA2 (core/src/ssimulacra2.rs:171-512) with respect to the distorted image's
+// RGB samples, taken as continuous values in [0, 255], in FP64 on the GPU.
+//
+// Forward: linear light by the sRGB curve itself (:172-175; the reference's 8-bit table samples it), the 2x2
+// pyramid, and per scale the XYB planes, the five blurred moments per channel and the six map sums. Backward, from
+// the coarsest scale to the finest: d score / d map from the 108-term sum, the final mapping and the L1/L4 norms;
+// through the SSIM and edge maps to the moments and the XYB samples (one-sided derivatives at the max(., 0) and |.|
+// kinks); through the blurs (the zero-padded row blur is its own transpose, the mirrored column blur scatters
+// back); through XYB to linear light; plus the coarser scales' gradients spread back over their 2x2 blocks; and
+// finally through the sRGB curve. The blur intermediates are recomputed per scale in the backward pass, not kept
+// from the forward one. Plane kernels, one thread per sample, f64 throughout: this runs once per search, not per
+// candidate, so it trades speed for an exact match with the FP64 CPU gradient.
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "rcg_internal.cuh"
+
+namespace rcg {
+
+namespace {
+
+constexpr int kR = 5;  // kernel radius (:16)
+constexpr double kBiasD = 0.0037930732552754493;
+constexpr double kM00 = 0.30, kM02 = 0.078, kM01 = 1.0 - kM02 - kM00;
+constexpr double kM10 = 0.23, kM12 = 0.078, kM11 = 1.0 - kM12 - kM10;
+constexpr double kM20 = 0.2434226892454782, kM21 = 0.2047674442449682, kM22 = 1.0 - kM20 - kM21;
+constexpr double kC2 = 0.0009;
+
+__constant__ double c_k64[2 * kR + 1];  // normalized Gaussian taps (sigma 1.5)
+
+__device__ __forceinline__ double srgb64(double v) {
+  return v <= 0.04045 ? v / 12.92 : pow((v + 0.055) / 1.055, 2.4);
+}
+__device__ __forceinline__ double srgb64_deriv(double v255) {
+  const double v = v255 / 255.0;
+  return v <= 0.04045 ? 1.0 / (12.92 * 255.0) : 2.4 * pow((v + 0.055) / 1.055, 1.4) / (1.055 * 255.0);
+}
+
+__device__ __forceinline__ long long tid1() { return (long long)blockIdx.x * blockDim.x + threadIdx.x; }
+
+// Linear planes [3][n] of the reference (8-bit samples) and of the distorted image (f32 samples), by the curve.
+__global__ void k_lin64(const uint8_t* __restrict__ ref, const float* __restrict__ dist, long long n,
+                        double* __restrict__ la, double* __restrict__ lb) {
+  for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x)
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      // both images through the same curve: identical inputs give identical planes (and the score 100)
+      la[c * n + i] = srgb64((double)ref[i * 3 + c] / 255.0);
+      lb[c * n + i] = srgb64((double)dist[i * 3 + c] / 255.0);
+    }
+}
+
+// 2x2 means (:225-247), fewer samples at odd edges; 3 channels.
+__global__ void k_down64(const double* __restrict__ src, int w, int h, double* __restrict__ dst, int ow, int oh) {
+  const long long n = (long long)ow * oh;
+  for (long long i = tid1(); i < 3 * n; i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i / n);
+    const long long o = i - c * n;
+    const int oy = (int)(o / ow), ox = (int)(o % ow);
+    const int x1 = min(2 * ox + 2, w), y1 = min(2 * oy + 2, h);
+    const double* p = src + (long long)c * w * h;
+    double s = 0.0;
+    for (int y = 2 * oy; y < y1; y++)
+      for (int x = 2 * ox; x < x1; x++) s += p[(long long)y * w + x];
+    dst[i] = s / (double)((y1 - 2 * oy) * (x1 - 2 * ox));
+  }
+}
+
+// XYB (:249-258) of 3 linear planes.
+__global__ void k_xyb64(const double* __restrict__ lin, long long n, double* __restrict__ xyb) {
+  const double cb = cbrt(kBiasD);
+  for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double r = lin[i], g = lin[n + i], b = lin[2 * n + i];
+    const double m0 = cbrt(fmax(kM00 * r + kM01 * g + kM02 * b + kBiasD, 0.0)) - cb;
+    const double m1 = cbrt(fmax(kM10 * r + kM11 * g + kM12 * b + kBiasD, 0.0)) - cb;
+    const double m2 = cbrt(fmax(kM20 * r + kM21 * g + kM22 * b + kBiasD, 0.0)) - cb;
+    const double x = 0.5 * (m0 - m1), y = 0.5 * (m0 + m1);
+    xyb[i] = x * 14.0 + 0.42;
+    xyb[n + i] = y + 0.01;
+    xyb[2 * n + i] = (m2 - y) + 0.55;
+  }
+}
+
+// Row blur (zero outside) of the product `q` of one channel's XYB planes: 0 xa, 1 xb, 2 xa^2, 3 xb^2, 4 xa xb;
+// q = -1 blurs `src` itself (the adjoint's rows).
+__global__ void k_hblur64(const double* __restrict__ xa, const double* __restrict__ xb, const double* __restrict__ src,
+                          int q, int w, int h, double* __restrict__ dst) {
+  const long long n = (long long)w * h;
+  for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(i / w), x = (int)(i % w);
+    double s = 0.0;
+#pragma unroll
+    for (int t = 0; t <= 2 * kR; t++) {
+      const int xx = x + t - kR;
+      if (xx < 0 || xx >= w) continue;
+      const long long j = (long long)y * w + xx;
+      double v;
+      if (q < 0)
+        v = src[j];
+      else if (q == 0)
+        v = xa[j];
+      else if (q == 1)
+        v = xb[j];
+      else if (q == 2)
+        v = xa[j] * xa[j];
+      else if (q == 3)
+        v = xb[j] * xb[j];
+      else
+        v = xa[j] * xb[j];
+      s += c_k64[t] * v;
+    }
+    dst[i] = s;
+  }
+}
+
+__device__ __forceinline__ int mirror64(int yy, int h) { return yy < 0 ? -yy - 1 : (yy >= h ? 2 * h - 1 - yy : yy); }
+
+// Column blur with mirrored rows (:385-397).
+__global__ void k_vblur64(const double* __restrict__ src, int w, int h, double* __restrict__ dst) {
+  const long long n = (long long)w * h;
+  for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(i / w), x = (int)(i % w);
+    double s = 0.0;
+#pragma unroll
+    for (int t = 0; t <= 2 * kR; t++) s += c_k64[t] * src[(long long)mirror64(y + t - kR, h) * w + x];
+    dst[i] = s;
+  }
+}
+
+// Transpose of k_vblur64 as a gather: row y' receives tap t from the rows y whose mirrored source row is y', i.e.
+// from source index y' (y = y' - t + R), -y' - 1 (mirrored at the top) and 2h - 1 - y' (at the bottom).
+__global__ void k_vblur64_t(const double* __restrict__ g, int w, int h, double* __restrict__ dst) {
+  const long long n = (long long)w * h;
+  for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int yp = (int)(i / w), x = (int)(i % w);
+    double s = 0.0;
+#pragma unroll
+    for (int t = 0; t <= 2 * kR; t++) {
+      const int ys[3] = {yp - t + kR, -yp - 1 - t + kR, 2 * h - 1 - yp - t + kR};
+#pragma unroll
+      for (int e = 0; e < 3; e++)
+        if (ys[e] >= 0 && ys[e] < h) s += c_k64[t] * g[(long long)ys[e] * w + x];
+    }
+    dst[i] = s;
+  }
+}
+
+// The six map sums of one channel (:421-440): block partial sums, then one double atomic each.
+__global__ void __launch_bounds__(256) k_maps64(const double* __restrict__ mom, const double* __restrict__ xa,
+                                                const double* __restrict__ xb, long long n, double* __restrict__ sums) {
+  __shared__ double red[6][8];
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double m1 = mom[i], m2 = mom[n + i], s11 = mom[2 * n + i], s22 = mom[3 * n + i], s12 = mom[4 * n + i];
+    const double num_m = 1.0 - (m1 - m2) * (m1 - m2);
+    const double num_s = 2.0 * (s12 - m1 * m2) + kC2;
+    const double den_s = (s11 - m1 * m1) + (s22 - m2 * m2) + kC2;
+    const double d = fmax(1.0 - num_m * num_s / den_s, 0.0);
+    const double d1 = (1.0 + fabs(xb[i] - m2)) / (1.0 + fabs(xa[i] - m1)) - 1.0;
+    const double art = fmax(d1, 0.0), det = fmax(-d1, 0.0);
+    acc[0] += d;
+    acc[1] += (d * d) * (d * d);
+    acc[2] += art;
+    acc[3] += (art * art) * (art * art);
+    acc[4] += det;
+    acc[5] += (det * det) * (det * det);
+  }
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    double v = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double v = 0.0;
+    for (int wi = 0; wi < 8; wi++) v += red[threadIdx.x][wi];
+    atomicAdd(&sums[threadIdx.x], v);
+  }
+}
+
+// Per sample of one channel: d score / d (m2, s22, s12) and the direct d score / d xb of the edge maps, given the
+// norms' coefficients g1 (L1: weight / count) and g4 (L4: weight (S/count)^-3/4 / count) of (ssim, artifact,
+// detail).
+struct NormCoef {
+  double g1[3], g4[3];
+};
+
+__global__ void k_mapgrad64(const double* __restrict__ mom, const double* __restrict__ xa,
+                            const double* __restrict__ xb, long long n, NormCoef nc, double* __restrict__ g_m2,
+                            double* __restrict__ g_s22, double* __restrict__ g_s12, double* __restrict__ g_xb) {
+  for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double m1 = mom[i], m2 = mom[n + i], s11 = mom[2 * n + i], s22 = mom[3 * n + i], s12 = mom[4 * n + i];
+    const double num_m = 1.0 - (m1 - m2) * (m1 - m2);
+    const double num_s = 2.0 * (s12 - m1 * m2) + kC2;
+    const double den_s = (s11 - m1 * m1) + (s22 - m2 * m2) + kC2;
+    const double dv = 1.0 - num_m * num_s / den_s;
+    double gm2 = 0.0, gs22 = 0.0, gs12 = 0.0;
+    if (dv > 0.0) {
+      const double gd = nc.g1[0] + nc.g4[0] * dv * dv * dv;
+      const double g_num_m = -gd * num_s / den_s, g_num_s = -gd * num_m / den_s;
+      const double g_den = gd * num_m * num_s / (den_s * den_s);
+      gm2 = g_num_m * (2.0 * (m1 - m2)) + g_num_s * (-2.0 * m1) + g_den * (-2.0 * m2);
+      gs22 = g_den;
+      gs12 = 2.0 * g_num_s;
+    }
+    const double a = xa[i], b = xb[i];
+    const double Nn = 1.0 + fabs(b - m2), Dn = 1.0 + fabs(a - m1);
+    const double d1 = Nn / Dn - 1.0;
+    const double gd1 = (d1 > 0.0 ? nc.g1[1] + nc.g4[1] * d1 * d1 * d1 : 0.0) -
+                       (d1 < 0.0 ? nc.g1[2] + nc.g4[2] * (-d1) * (-d1) * (-d1) : 0.0);
+    const double sb = b - m2 > 0.0 ? 1.0 : (b - m2 < 0.0 ? -1.0 : 0.0);
+    g_xb[i] = gd1 * sb / Dn;
+    g_m2[i] = gm2 - gd1 * sb / Dn;
+    g_s22[i] = gs22;
+    g_s12[i] = gs12;
+  }
+}
+
+// d score / d xb = direct + G^T(g_m2) + 2 xb G^T(g_s22) + xa G^T(g_s12) for one channel.
+__global__ void k_combine64(const double* __restrict__ t_m2, const double* __restrict__ t_s22,
+                            const double* __restrict__ t_s12, const double* __restrict__ xa,
+                            const double* __restrict__ xb, long long n, double* __restrict__ g_xb) {
+  for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x)
+    g_xb[i] += t_m2[i] + 2.0 * xb[i] * t_s22[i] + xa[i] * t_s12[i];
+}
+
+// XYB adjoint to the linear planes of this scale, plus the coarser scale's gradient spread over its 2x2 blocks.
+__global__ void k_xyb_adj64(const double* __restrict__ lin, const double* __restrict__ g_xyb, int w, int h,
+                            const double* __restrict__ g_coarse, int cw, double* __restrict__ g_lin) {
+  const long long n = (long long)w * h, cn = (long long)cw * ((h + 1) / 2);
+  for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double r = lin[i], g = lin[n + i], b = lin[2 * n + i];
+    const double u0 = kM00 * r + kM01 * g + kM02 * b + kBiasD, u1 = kM10 * r + kM11 * g + kM12 * b + kBiasD,
+                 u2 = kM20 * r + kM21 * g + kM22 * b + kBiasD;
+    const double d0 = u0 > 0.0 ? 1.0 / (3.0 * cbrt(u0) * cbrt(u0)) : 0.0;
+    const double d1 = u1 > 0.0 ? 1.0 / (3.0 * cbrt(u1) * cbrt(u1)) : 0.0;
+    const double d2 = u2 > 0.0 ? 1.0 / (3.0 * cbrt(u2) * cbrt(u2)) : 0.0;
+    const double gX = g_xyb[i], gY = g_xyb[n + i], gB = g_xyb[2 * n + i];
+    const double gu0 = (7.0 * gX + 0.5 * gY - 0.5 * gB) * d0, gu1 = (-7.0 * gX + 0.5 * gY - 0.5 * gB) * d1,
+                 gu2 = gB * d2;
+    double o[3] = {gu0 * kM00 + gu1 * kM10 + gu2 * kM20, gu0 * kM01 + gu1 * kM11 + gu2 * kM21,
+                   gu0 * kM02 + gu1 * kM12 + gu2 * kM22};
+    if (g_coarse) {
+      const int y = (int)(i / w), x = (int)(i % w), ox = x / 2, oy = y / 2;
+      const int nx = min(2 * ox + 2, w) - 2 * ox, ny = min(2 * oy + 2, h) - 2 * oy;
+      const double inv = 1.0 / (double)(nx * ny);
+#pragma unroll
+      for (int c = 0; c < 3; c++) o[c] += g_coarse[c * cn + (long long)oy * cw + ox] * inv;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) g_lin[c * n + i] = o[c];
+  }
+}
+
+// Through the sRGB curve to the samples (interleaved RGB).
+__global__ void k_grad_out64(const double* __restrict__ g_lin, const float* __restrict__ dist, long long n,
+                             double* __restrict__ grad) {
+  for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x)
+#pragma unroll
+    for (int c = 0; c < 3; c++) grad[i * 3 + c] = g_lin[c * n + i] * srgb64_deriv((double)dist[i * 3 + c]);
+}
+
+unsigned grid_of(long long n) { return (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 32)); }
+
+}  // namespace
+
+int ssim2_grad_device(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, int w, int h, double* score,
+                      double* d_grad) {
+  // constants
+  double k[2 * kR + 1], sum = 0.0;
+  for (int i = 0; i <= 2 * kR; i++) {
+    const double x = (double)(i - kR);
+    k[i] = std::exp(-0.5 / (1.5 * 1.5) * x * x);
+    sum += k[i];
+  }
+  for (int i = 0; i <= 2 * kR; i++) k[i] /= sum;
+  cudaMemcpyToSymbolAsync(c_k64, k, sizeof k, 0, cudaMemcpyHostToDevice, ctx->stream);
+  // pyramid of both images (linear, f64)
+  struct Sc {
+    int w, h;
+    long long n, off;
+  };
+  std::vector<Sc> sc;
+  long long total = 0;
+  for (int s = 0, sw = w, sh = h; s < kMaxScales && sw >= kMinSide && sh >= kMinSide; s++) {
+    sc.push_back({sw, sh, (long long)sw * sh, total});
+    total += 3LL * sw * sh;
+    sw = (sw + 1) / 2;
+    sh = (sh + 1) / 2;
+  }
+  const int ns = (int)sc.size();
+  if (ns == 0) return fail(ctx, RCG_INVALID, "SSIMULACRA 2 needs at least 8x8 pixels");
+  const long long n0 = sc[0].n;
+  double* pa = (double*)workspace(ctx, "adj_pa", sizeof(double) * total);
+  double* pb = (double*)workspace(ctx, "adj_pb", sizeof(double) * total);
+  double* xa = (double*)workspace(ctx, "adj_xa", sizeof(double) * 3 * n0);
+  double* xb = (double*)workspace(ctx, "adj_xb", sizeof(double) * 3 * n0);
+  double* hb = (double*)workspace(ctx, "adj_hb", sizeof(double) * n0);
+  double* mom = (double*)workspace(ctx, "adj_mom", sizeof(double) * 5 * n0);
+  double* gq = (double*)workspace(ctx, "adj_gq", sizeof(double) * 3 * n0);   // g_m2, g_s22, g_s12
+  double* tq = (double*)workspace(ctx, "adj_tq", sizeof(double) * 3 * n0);   // their blur adjoints
+  double* gx = (double*)workspace(ctx, "adj_gx", sizeof(double) * 3 * n0);   // d score / d xb
+  double* gl = (double*)workspace(ctx, "adj_gl", sizeof(double) * total);     // d score / d linear, per scale
+  double* sums = (double*)workspace(ctx, "adj_sums", sizeof(double) * kMaxScales * 18);
+  if (!pa || !pb || !xa || !xb || !hb || !mom || !gq || !tq || !gx || !gl || !sums) return RCG_NO_MEMORY;
+  RCG_LAUNCH(ctx, "adj_lin", k_lin64, grid_of(n0), 256, 0, d_ref, d_dist, n0, pa, pb);
+  for (int s = 1; s < ns; s++) {
+    RCG_LAUNCH(ctx, "adj_down", k_down64, grid_of(3 * sc[s].n), 256, 0, pa + sc[s - 1].off, sc[s - 1].w, sc[s - 1].h,
+               pa + sc[s].off, sc[s].w, sc[s].h);
+    RCG_LAUNCH(ctx, "adj_down", k_down64, grid_of(3 * sc[s].n), 256, 0, pb + sc[s - 1].off, sc[s - 1].w, sc[s - 1].h,
+               pb + sc[s].off, sc[s].w, sc[s].h);
+  }
+  // forward: the moments and map sums of every scale
+  auto moments = [&](int s, int c) {
+    const long long n = sc[s].n;
+    for (int q = 0; q < 5; q++) {
+      RCG_LAUNCH(ctx, "adj_hblur", k_hblur64, grid_of(n), 256, 0, xa + c * n, xb + c * n, (const double*)nullptr, q,
+                 sc[s].w, sc[s].h, hb);
+      RCG_LAUNCH(ctx, "adj_vblur", k_vblur64, grid_of(n), 256, 0, hb, sc[s].w, sc[s].h, mom + q * n);
+    }
+  };
+  cudaMemsetAsync(sums, 0, sizeof(double) * kMaxScales * 18, ctx->stream);
+  for (int s = 0; s < ns; s++) {
+    const long long n = sc[s].n;
+    RCG_LAUNCH(ctx, "adj_xyb", k_xyb64, grid_of(n), 256, 0, pa + sc[s].off, n, xa);
+    RCG_LAUNCH(ctx, "adj_xyb", k_xyb64, grid_of(n), 256, 0, pb + sc[s].off, n, xb);
+    for (int c = 0; c < 3; c++) {
+      moments(s, c);
+      RCG_LAUNCH(ctx, "adj_maps", k_maps64, grid_of(n), 256, 0, mom, xa + c * n, xb + c * n, n,
+                 sums + s * 18 + c * 6);
+    }
+  }
+  double hs[kMaxScales * 18];
+  cudaMemcpyAsync(hs, sums, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "ssimulacra2 gradient");
+  // final mapping (:491-511) and d score / d stat
+  double st[kMaxScales][3][6], wst[kMaxScales][3][6];
+  for (int s = 0; s < ns; s++) {
+    const double count = (double)sc[s].n;
+    for (int c = 0; c < 3; c++)
+      for (int m = 0; m < 3; m++) {
+        st[s][c][2 * m] = hs[s * 18 + c * 6 + 2 * m] / count;
+        st[s][c][2 * m + 1] = std::pow(hs[s * 18 + c * 6 + 2 * m + 1] / count, 0.25);
+      }
+  }
+  const double* W = scorer_weights();
+  double wsum = 0.0;
+  int i = 0;
+  for (int c = 0; c < 3; c++)
+    for (int s = 0; s < ns; s++)
+      for (int nrm = 0; nrm < 2; nrm++)
+        for (int m = 0; m < 3; m++) {
+          wst[s][c][2 * m + nrm] = W[i];
+          wsum += W[i] * std::fabs(st[s][c][2 * m + nrm]);
+          i++;
+        }
+  const double kq = 0.9562382616834844, q = wsum * kq;
+  const double P = 2.326765642916932 * q - 0.020884521182843837 * q * q + 6.248496625763138e-05 * q * q * q;
+  const double ex = 0.6276336467831387;
+  *score = P > 0.0 ? 100.0 - 10.0 * std::pow(P, ex) : 100.0;
+  const long long npx = (long long)w * h;
+  if (!d_grad) return RCG_OK;  // the score alone
+  if (!(P > 0.0)) {
+    cudaMemsetAsync(d_grad, 0, sizeof(double) * 3 * npx, ctx->stream);
+    return RCG_OK;
+  }
+  const double dsum = -10.0 * ex * std::pow(P, ex - 1.0) *
+                      (2.326765642916932 - 2.0 * 0.020884521182843837 * q + 3.0 * 6.248496625763138e-05 * q * q) *
+                      kq;
+  // backward, coarsest scale first
+  for (int s = ns - 1; s >= 0; s--) {
+    const long long n = sc[s].n;
+    const double count = (double)n;
+    RCG_LAUNCH(ctx, "adj_xyb", k_xyb64, grid_of(n), 256, 0, pa + sc[s].off, n, xa);
+    RCG_LAUNCH(ctx, "adj_xyb", k_xyb64, grid_of(n), 256, 0, pb + sc[s].off, n, xb);
+    for (int c = 0; c < 3; c++) {
+      NormCoef nc;
+      for (int m = 0; m < 3; m++) {
+        nc.g1[m] = dsum * wst[s][c][2 * m] / count;
+        const double mean4 = hs[s * 18 + c * 6 + 2 * m + 1] / count;
+        nc.g4[m] = mean4 > 0.0 ? dsum * wst[s][c][2 * m + 1] * std::pow(mean4, -0.75) / count : 0.0;
+      }
+      moments(s, c);  // recomputed, not stored
+      RCG_LAUNCH(ctx, "adj_mapgrad", k_mapgrad64, grid_of(n), 256, 0, mom, xa + c * n, xb + c * n, n, nc, gq,
+                 gq + n, gq + 2 * n, gx + c * n);
+      for (int j = 0; j < 3; j++) {
+        RCG_LAUNCH(ctx, "adj_vblur_t", k_vblur64_t, grid_of(n), 256, 0, gq + j * n, sc[s].w, sc[s].h, hb);
+        RCG_LAUNCH(ctx, "adj_hblur", k_hblur64, grid_of(n), 256, 0, (const double*)nullptr, (const double*)nullptr,
+                   hb, -1, sc[s].w, sc[s].h, tq + j * n);
+      }
+      RCG_LAUNCH(ctx, "adj_combine", k_combine64, grid_of(n), 256, 0, tq, tq + n, tq + 2 * n, xa + c * n, xb + c * n,
+                 n, gx + c * n);
+    }
+    RCG_LAUNCH(ctx, "adj_xyb_adj", k_xyb_adj64, grid_of(n), 256, 0, pb + sc[s].off, gx, sc[s].w, sc[s].h,
+               s + 1 < ns ? gl + sc[s + 1].off : nullptr, s + 1 < ns ? sc[s + 1].w : 0, gl + sc[s].off);
+  }
+  RCG_LAUNCH(ctx, "adj_out", k_grad_out64, grid_of(npx), 256, 0, gl + sc[0].off, d_dist, npx, d_grad);
+  return RCG_OK;
+}
+
+}  // namespace rcg

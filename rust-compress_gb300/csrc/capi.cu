@@ -1196,5 +1196,39 @@ int rcg_decode_coefs_device(rcg_ctx* ctx, const uint8_t* jpeg, size_t len, rcg_j
   return d_coefs ? finish(ctx, "decode") : RCG_OK;
 }
 
+int rcg_ssimulacra2_grad_device(rcg_ctx* ctx, const uint8_t* d_reference, const float* d_distorted, uint32_t width,
+                                uint32_t height, double* score, double* d_grad) {
+  if (!ctx) return RCG_INVALID;
+  if (!d_reference || !d_distorted || !score) return fail(ctx, RCG_INVALID, "null pointer");
+  if (width < (uint32_t)kMinSide || height < (uint32_t)kMinSide)
+    return fail(ctx, RCG_INVALID, "SSIMULACRA 2 needs at least 8x8 pixels");
+  cudaSetDevice(ctx->device);
+  int rc = ssim2_grad_device(ctx, d_reference, d_distorted, (int)width, (int)height, score, d_grad);
+  if (rc != RCG_OK) return rc;
+  return finish(ctx, "ssimulacra2 gradient");
+}
+
+int rcg_ssimulacra2_grad(rcg_ctx* ctx, const uint8_t* reference, const float* distorted, uint32_t width,
+                         uint32_t height, double* score, double* grad) {
+  if (!ctx) return RCG_INVALID;
+  if (!reference || !distorted || !score) return fail(ctx, RCG_INVALID, "null pointer");
+  if (width < (uint32_t)kMinSide || height < (uint32_t)kMinSide)
+    return fail(ctx, RCG_INVALID, "SSIMULACRA 2 needs at least 8x8 pixels");
+  cudaSetDevice(ctx->device);
+  const size_t n = (size_t)width * height * 3;
+  uint8_t* d_ref = (uint8_t*)workspace(ctx, "img_a", n);
+  float* d_dist = (float*)workspace(ctx, "grad_dist", n * sizeof(float));
+  double* d_grad = (double*)workspace(ctx, "grad_out", n * sizeof(double));
+  if (!d_ref || !d_dist || !d_grad) return RCG_NO_MEMORY;
+  int rc;
+  if ((rc = copy_to_device(ctx, d_ref, reference, n)) != RCG_OK) return rc;
+  if ((rc = copy_to_device(ctx, d_dist, distorted, n * sizeof(float))) != RCG_OK) return rc;
+  if ((rc = ssim2_grad_device(ctx, d_ref, d_dist, (int)width, (int)height, score, grad ? d_grad : nullptr)) !=
+      RCG_OK)
+    return rc;
+  if (grad && (rc = copy_to_host(ctx, grad, d_grad, n * sizeof(double))) != RCG_OK) return rc;
+  return finish(ctx, "ssimulacra2 gradient");
+}
+
 }  // extern "C"
 

@@ -256,6 +256,12 @@ int downsample2(rcg_ctx* ctx, const uint8_t* d_in, int w, int h, uint8_t* d_out)
 int jpeg_decode(rcg_ctx* ctx, const uint8_t* data, size_t len, rcg_jpeg_info* info, rcg_coef_layout* layout,
                 rcg_qtables* tables, int16_t* coefs, size_t coefs_len, bool coefs_on_device);
 
+// The scorer's 108 weights (core/src/ssimulacra2.rs:54-163), host side.
+const double* scorer_weights();
+// d SSIMULACRA2 / d distorted RGB samples (continuous, f32 in [0, 255]) in FP64; the reference image is 8-bit RGB.
+int ssim2_grad_device(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, int w, int h, double* score,
+                      double* d_grad);
+
 // write_best's plan (progressive candidates + baseline estimate) of coefficients on the device; `lay` carries the
 // component layout (ncomp, hmax, vmax, comp[]).
 int plan_scans(rcg_ctx* ctx, const StepDesc* lay, int w, int h, const int16_t* d_coefs, rcg_plan_result* res);

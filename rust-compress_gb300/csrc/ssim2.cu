@@ -639,6 +639,29 @@ static std::mutex g_scorer_mu;
 static bool g_scorer_ready[64];
 
 // Upload the scorer's constant tables to the current device once (cudaMemcpyToSymbol only; nothing is allocated).
+// core/src/ssimulacra2.rs:54-163 (WEIGHTS)
+static const double kScorerWeights[108] = {
+    0.0, 0.0007376606707406586, 0.0, 0.0, 0.0007793481682867309, 0.0,
+    0.0, 0.0004371155730107379, 0.0, 1.1041726426657346, 0.00066284834129271, 0.00015231632783718752,
+    0.0, 0.0016406437456599754, 0.0, 1.8422455520539298, 11.441172603757666, 0.0,
+    0.0007989109436015163, 0.000176816438078653, 0.0, 1.8787594979546387, 10.94906990605142, 0.0,
+    0.0007289346991508072, 0.9677937080626833, 0.0, 0.00014003424285435884, 0.9981766977854967, 0.00031949755934435053,
+    0.0004550992113792063, 0.0, 0.0, 0.0013648766163243398, 0.0, 0.0,
+    0.0, 0.0, 0.0, 7.466890328078848, 0.0, 17.445833984131262,
+    0.0006235601634041466, 0.0, 0.0, 6.683678146179332, 0.00037724407979611296, 1.027889937768264,
+    225.20515300849274, 0.0, 0.0, 19.213238186143016, 0.0011401524586618361, 0.001237755635509985,
+    176.39317598450694, 0.0, 0.0, 24.43300999870476, 0.28520802612117757, 0.0004485436923833408,
+    0.0, 0.0, 0.0, 34.77906344483772, 44.835625328877896, 0.0,
+    0.0, 0.0, 0.0, 0.0, 0.0, 0.0,
+    0.0, 0.0008680556573291698, 0.0, 0.0, 0.0, 0.0,
+    0.0, 0.0005313191874358747, 0.0, 0.00016533814161379112, 0.0, 0.0,
+    0.0, 0.0, 0.0, 0.0004179171803251336, 0.0017290828234722833, 0.0,
+    0.0020827005846636437, 0.0, 0.0, 8.826982764996862, 23.19243343998926, 0.0,
+    95.1080498811086, 0.9863978034400682, 0.9834382792465353, 0.0012286405048278493, 171.2667255897307, 0.9807858872435379,
+    0.0, 0.0, 0.0, 0.0005130064588990679, 0.0, 0.00010854057858411537};
+
+const double* scorer_weights() { return kScorerWeights; }
+
 static cudaError_t scorer_constants(int device) {
   std::lock_guard<std::mutex> lk(g_scorer_mu);
   if (device >= 0 && device < 64 && g_scorer_ready[device]) return cudaSuccess;
@@ -653,26 +676,7 @@ static cudaError_t scorer_constants(int device) {
   for (int i = 0; i < 2 * kRadius + 1; i++) kf[i] = (float)(k[i] / sum);
   float lut[256];
   srgb_lut8(lut);
-  // core/src/ssimulacra2.rs:54-163 (WEIGHTS)
-  static const double W[108] = {
-      0.0, 0.0007376606707406586, 0.0, 0.0, 0.0007793481682867309, 0.0,
-      0.0, 0.0004371155730107379, 0.0, 1.1041726426657346, 0.00066284834129271, 0.00015231632783718752,
-      0.0, 0.0016406437456599754, 0.0, 1.8422455520539298, 11.441172603757666, 0.0,
-      0.0007989109436015163, 0.000176816438078653, 0.0, 1.8787594979546387, 10.94906990605142, 0.0,
-      0.0007289346991508072, 0.9677937080626833, 0.0, 0.00014003424285435884, 0.9981766977854967, 0.00031949755934435053,
-      0.0004550992113792063, 0.0, 0.0, 0.0013648766163243398, 0.0, 0.0,
-      0.0, 0.0, 0.0, 7.466890328078848, 0.0, 17.445833984131262,
-      0.0006235601634041466, 0.0, 0.0, 6.683678146179332, 0.00037724407979611296, 1.027889937768264,
-      225.20515300849274, 0.0, 0.0, 19.213238186143016, 0.0011401524586618361, 0.001237755635509985,
-      176.39317598450694, 0.0, 0.0, 24.43300999870476, 0.28520802612117757, 0.0004485436923833408,
-      0.0, 0.0, 0.0, 34.77906344483772, 44.835625328877896, 0.0,
-      0.0, 0.0, 0.0, 0.0, 0.0, 0.0,
-      0.0, 0.0008680556573291698, 0.0, 0.0, 0.0, 0.0,
-      0.0, 0.0005313191874358747, 0.0, 0.00016533814161379112, 0.0, 0.0,
-      0.0, 0.0, 0.0, 0.0004179171803251336, 0.0017290828234722833, 0.0,
-      0.0020827005846636437, 0.0, 0.0, 8.826982764996862, 23.19243343998926, 0.0,
-      95.1080498811086, 0.9863978034400682, 0.9834382792465353, 0.0012286405048278493, 171.2667255897307, 0.9807858872435379,
-      0.0, 0.0, 0.0, 0.0005130064588990679, 0.0, 0.00010854057858411537};
+  const double* W = scorer_weights();
   cudaError_t e;
   if ((e = cudaMemcpyToSymbol(c_gauss, kf, sizeof kf)) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(c_lut8s, lut, sizeof lut)) != cudaSuccess) return e;

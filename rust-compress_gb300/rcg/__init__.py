@@ -230,6 +230,8 @@ def _load():
         "rcg_search_requantize_device": (i32, [P, u32, u32, ctypes.POINTER(_Layout), ctypes.POINTER(_QTables), P,
                                                i32, ctypes.c_double, i32, i32, ctypes.POINTER(_Found), P, sz,
                                                ctypes.POINTER(_QTables)]),
+        "rcg_ssimulacra2_grad": (i32, [P, P, P, u32, u32, ctypes.POINTER(ctypes.c_double), P]),
+        "rcg_ssimulacra2_grad_device": (i32, [P, P, P, u32, u32, ctypes.POINTER(ctypes.c_double), P]),
         "rcg_plan": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, sz, ctypes.POINTER(_PlanResult)]),
         "rcg_plan_device": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, ctypes.POINTER(_PlanResult)]),
         "rcg_search_batch": (i32, [P, i32, P, P, P, P, P, i32, ctypes.POINTER(_Opts), i32, P, P, P, P]),
@@ -248,7 +250,7 @@ EXPORTED = (
     "rcg_ssimulacra2_device rcg_ssimulacra2_device_noalloc rcg_build_coefs rcg_reconstruct rcg_search rcg_search_device "
     "rcg_search_batch rcg_reconstruct_tables rcg_requantize rcg_search_requantize rcg_plan rcg_plan_device "
     "rcg_metric_score rcg_metric_score_device rcg_search_metric rcg_decode_coefs rcg_decode_coefs_device "
-    "rcg_search_requantize_device"
+    "rcg_search_requantize_device rcg_ssimulacra2_grad rcg_ssimulacra2_grad_device"
 ).split()
 
 
@@ -352,6 +354,20 @@ class Context:
         self._check(_lib.rcg_ssimulacra2_device(self._ptr, ctypes.c_void_p(ref_ptr), ctypes.c_void_p(dist_ptr),
                                                 width, height, channels, ctypes.byref(out)))
         return out.value
+
+    def ssimulacra2_grad(self, reference, distorted, score_only=False):
+        """(FP64 score, d score / d distorted) of an 8-bit RGB reference and a float RGB distorted image (values in
+        [0, 255], taken as continuous); the gradient as a float64 (h, w, 3) array (None with score_only)."""
+        a = np.ascontiguousarray(reference, dtype=np.uint8)
+        d = np.ascontiguousarray(distorted, dtype=np.float32)
+        if a.ndim != 3 or a.shape[2] != 3 or d.shape != a.shape:
+            raise ValueError("the gradient takes an RGB reference and an RGB float image of the same shape")
+        h, w = a.shape[:2]
+        g = None if score_only else np.zeros((h, w, 3), np.float64)
+        s = ctypes.c_double()
+        self._check(_lib.rcg_ssimulacra2_grad(self._ptr, a.ctypes.data, d.ctypes.data, w, h, ctypes.byref(s),
+                                              None if g is None else g.ctypes.data))
+        return s.value, g
 
     def metric(self, metric, reference, candidate):
         """score(reference, candidate, metric) (cli/src/pipeline.rs:130): 8-bit images with 1..=4 channels."""

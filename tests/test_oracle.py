@@ -519,3 +519,26 @@ def test_oracle_sequential_decoder_round_trips_and_fixtures(oracle):
                 oracle.decode_sequential(blob)
             except ValueError:
                 pass
+
+
+def test_oracle_fp64_gradient_matches_central_differences(oracle):
+    """The FP64 reverse-mode gradient of SSIMULACRA2 against FP64 central differences (h = 1e-3), and the
+    continuous-input forward against the FP64 scorer on integer samples."""
+    import rcg.synth as synth
+
+    w, h = 96, 80
+    ref = synth.image(w, h, 5)
+    coefs, qt, lay = oracle.build_coefs(ref, 60, 3, True)
+    dist = oracle.reconstruct(w, h, lay, qt, coefs)
+    r64, d64 = ref.astype(np.float64), dist.astype(np.float64)
+    assert abs(oracle.score64(r64, d64) - oracle.ssimulacra2(ref, dist, fp64=True)) < 1e-9
+    s, g = oracle.grad64(r64, d64)
+    rng = np.random.default_rng(0)
+    step = 1e-3
+    for _ in range(48):
+        y, x, c = int(rng.integers(0, h)), int(rng.integers(0, w)), int(rng.integers(0, 3))
+        dp, dm = d64.copy(), d64.copy()
+        dp[y, x, c] += step
+        dm[y, x, c] -= step
+        fd = (oracle.score64(r64, dp) - oracle.score64(r64, dm)) / (2 * step)
+        assert abs(fd - g[y, x, c]) <= 1e-9 + 1e-4 * abs(fd), (y, x, c, fd, g[y, x, c])
