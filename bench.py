@@ -258,6 +258,72 @@ def requantize_workload(ctx, img, timed, with_oracle=True, steps=5):
     return out
 
 
+def _pareto_bytes(curve, target):
+    """Bytes at `target` on the upper-left frontier of (bytes, score) points: the cheapest size that reaches the
+    score, interpolated linearly between frontier points."""
+    front = []
+    for b, s in sorted(curve):
+        if not front or s > front[-1][1]:
+            front.append((b, s))
+    if front and front[0][1] >= target:
+        return float(front[0][0])
+    for (b0, s0), (b1, s1) in zip(front, front[1:]):
+        if s0 < target <= s1:
+            return b0 + (target - s0) / (s1 - s0) * (b1 - b0)
+    return None
+
+
+def perceptual_workload(ctx, img, timed, steps=3):
+    """The perceptual trellis on the 12 MP workload, target 70, 4:2:0: the perceptual search (plain search ->
+    SSIMULACRA2 gradient at its result -> coefficient weights -> weighted search -> planned sizes) through the
+    public API with host buffers, and the file size at equal score: rate-score curves (planned bytes, score) over
+    qualities 50..95 for the plain trellis, the weighted trellis and a control with uniform weights of the same
+    strength (no gradient), each read off its Pareto frontier at scores 60..80."""
+    import numpy as np
+
+    import rcg
+
+    opts = rcg.EncodeOptions(90, rcg.Subsampling.S420, True)
+    popts = rcg.PerceptualOptions()
+    ctx.find_quality_perceptual(img, TARGET, 100, opts, popts)
+    times, r = timed(lambda: ctx.find_quality_perceptual(img, TARGET, 100, opts, popts), steps)
+    ms = sum(times) / len(times)
+    uniform = np.full_like(r.weights, np.float32(popts.strength))
+
+    def point(q, wts):
+        o = rcg.EncodeOptions(q, opts.subsampling, True)
+        ci = ctx.build_coefs(img, o) if wts is None else ctx.build_coefs_weighted(img, o, wts)
+        s = ctx.ssimulacra2(img, ctx.reconstruct(ci))
+        p = ctx.plan(ci)
+        return min(p.progressive_bytes, p.baseline_bytes), s
+
+    t0 = time.perf_counter()
+    curves = {name: [point(q, wts) for q in range(50, 96)]
+              for name, wts in (("plain", None), ("perceptual", r.weights), ("uniform_strength", uniform))}
+    curve_s = time.perf_counter() - t0
+    targets = [60.0, 65.0, 70.0, 75.0, 80.0]
+    at = {name: [_pareto_bytes(c, t) for t in targets] for name, c in curves.items()}
+
+    def change(name):
+        pct = [round(100 * (b / a - 1.0), 2) if a and b else None for a, b in zip(at["plain"], at[name])]
+        vals = [x for x in pct if x is not None]
+        return {"per_target_pct": pct, "mean_pct": round(float(np.mean(vals)), 2) if vals else None}
+
+    returned = r.perceptual_bytes if r.chose_perceptual else r.plain_bytes
+
+    return {"workload": "perceptual trellis: 4000x3000 seed 1 sigma 3, target 70, 4:2:0, default options "
+                        f"(strength {popts.strength}, gamma {popts.gamma}, radius {popts.radius})",
+            "ms_per_perceptual_search": ms, "searches_per_s": 1000.0 / ms,
+            "plain": {"quality": r.plain.quality, "score": r.plain.score, "bytes": r.plain_bytes},
+            "weighted": {"bytes": r.perceptual_bytes},
+            "returned": {"quality": r.found.quality, "score": r.found.score, "chose_perceptual": r.chose_perceptual,
+                         "bytes": returned, "bytes_vs_plain_pct": round(100 * (returned / r.plain_bytes - 1.0), 2)},
+            "equal_score": {"targets": targets, "plain_bytes": at["plain"],
+                            "perceptual_vs_plain": change("perceptual"),
+                            "uniform_strength_vs_plain": change("uniform_strength"),
+                            "qualities": "50..95", "seconds": round(curve_s, 1)}}
+
+
 def ssim_workload(ctx, img, timed, torch, dev, with_oracle=True, steps=5):
     """`--target-ssim` (jpeg/src/target.rs:24): the same 12 MP image, target SSIM 0.95, 4:2:0, trellis, host
     buffers; and SSIM alone on a device-resident 12 MP pair (the source vs its q50 round trip)."""
@@ -405,6 +471,7 @@ def main():
     ap.add_argument("--no-scorer", action="store_true", help="skip the scorer-alone measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the many-image batch measurement")
     ap.add_argument("--no-requant", action="store_true", help="skip the JPEG->JPEG search measurement")
+    ap.add_argument("--no-perceptual", action="store_true", help="skip the perceptual trellis measurement")
     ap.add_argument("--kernel-case", choices=["plan", "ssim", "ssim2"], default=None,
                     help="profiling aid: run only a few calls of one workload at --width x --height, print nothing")
     ap.add_argument("--width", type=int, default=W, help="smaller cases for profiling only; the bench line uses 4000")
@@ -541,6 +608,9 @@ def main():
     requant = None
     if rank == 0 and not args.no_requant:
         requant = requantize_workload(ctx, img, timed, with_oracle=not args.no_cpu_baseline)
+    perceptual = None
+    if rank == 0 and not args.no_perceptual:
+        perceptual = perceptual_workload(ctx, img, timed)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
@@ -579,6 +649,7 @@ def main():
             "write_best_plan": plan,
             "target_ssim": ssim_w,
             "jpeg_decode": decode,
+            "perceptual_trellis": perceptual,
         }
         print(json.dumps(out), flush=True)
     if dist:

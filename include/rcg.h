@@ -265,6 +265,59 @@ int rcg_search_batch(rcg_ctx* ctx, int n, const uint8_t* const* srcs, const uint
                      const rcg_encode_options* opts, int parallel, rcg_found* found, int16_t* const* coefs,
                      const size_t* coefs_len, uint8_t* const* qtables);
 
+/* ---- Perceptual trellis (opt-in; not a reference mode)
+ *
+ * The SSIMULACRA2 gradient of a decoded image, pulled back through the decoder's YCbCr->RGB conversion, chroma
+ * upsampling and orthonormal IDCT, gives d score / d coefficient; the perceptual weights derived from it multiply the
+ * trellis's distortion weight (jpeg/src/rdo.rs:41-43, (median / q)^1 per frequency) coefficient by coefficient. With
+ * the weights absent every entry point below is the reference's plain MSE trellis; the plain calls above never read
+ * weights. */
+typedef struct {
+  double strength; /* global scale of the weights (below 1: the trellis trades more distortion for rate) */
+  double gamma;    /* exponent on the block's normalised gradient sensitivity (0: uniform weights) */
+  double w_min;    /* clamp of the normalised, exponentiated sensitivity (before `strength`) */
+  double w_max;
+  int32_t radius;  /* sensitivity = RMS of the gradient energy over (2 radius + 1)^2 neighbouring blocks */
+  int32_t keep_smaller; /* rcg_search_perceptual: return the plain result when its planned size is smaller */
+} rcg_perceptual_options;
+
+/* The defaults: strength 0.35, gamma 0.5, w_min 0.25, w_max 4, radius 1, keep_smaller 1. */
+void rcg_perceptual_defaults(rcg_perceptual_options* opts);
+
+/* d SSIMULACRA2(reference, decoded) / d coefficient for the coefficient layout `layout` (64 zigzag entries per block,
+ * components in order; dequantized units: multiply by the quantization step for d score / d quantized value). Both
+ * images are 8-bit with `channels` (1 or 3, matching layout->ncomp); the gradient is taken at the decoded samples as
+ * f32 (FP64 adjoint), then pulled back linearly (roundings and clamps of the decoder dropped). Host buffers. */
+int rcg_coef_gradient(rcg_ctx* ctx, const uint8_t* reference, const uint8_t* decoded, uint32_t width, uint32_t height,
+                      int channels, const rcg_coef_layout* layout, double* score, double* grad, size_t grad_len);
+
+/* The perceptual trellis weights (f32, the coefficient layout of `layout`) from the gradient at `decoded`. */
+int rcg_perceptual_weights(rcg_ctx* ctx, const uint8_t* reference, const uint8_t* decoded, uint32_t width,
+                           uint32_t height, int channels, const rcg_coef_layout* layout,
+                           const rcg_perceptual_options* popts, double* score, float* weights, size_t weights_len);
+
+/* rcg_build_coefs with the trellis pass in the perceptual mode (`weights`: the layout's ncoefs entries). */
+int rcg_build_coefs_weighted(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
+                             const rcg_encode_options* opts, const float* weights, size_t weights_len, int16_t* coefs,
+                             size_t coefs_len, uint8_t* qtables);
+
+/* rcg_search with every candidate's trellis in the perceptual mode. The layout must not depend on the quality:
+ * an explicit subsampling (or Gray), trellis on. */
+int rcg_search_weighted(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
+                        double target, int max_quality, const rcg_encode_options* opts, const float* weights,
+                        size_t weights_len, rcg_found* found, int16_t* coefs, size_t coefs_len, uint8_t* qtables);
+
+/* The perceptual search: the plain search (`plain` receives its result), the weights from the gradient at the plain
+ * result's decoded image, then the weighted search. Both results are sized with write_best's plan (rcg_plan;
+ * `sizes` (nullable) receives {plain, perceptual} as min(progressive, baseline) bytes); `found`, `coefs` and
+ * `qtables` receive the weighted search's result, or the plain one when popts->keep_smaller is set and it is smaller
+ * (`*chose_perceptual`, nullable, says which). `weights` (nullable) receives the weights used. */
+int rcg_search_perceptual(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
+                          double target, int max_quality, const rcg_encode_options* opts,
+                          const rcg_perceptual_options* popts, rcg_found* plain, rcg_found* found, uint64_t* sizes,
+                          int* chose_perceptual, int16_t* coefs, size_t coefs_len, uint8_t* qtables, float* weights,
+                          size_t weights_len);
+
 #ifdef __cplusplus
 }
 #endif

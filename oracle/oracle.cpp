@@ -298,8 +298,12 @@ struct Rdo {
     return (float)zrl * len[0xF0] + len[((run % 16) << 4) | size] + (float)size;
   }
 
-  // jpeg/src/rdo.rs:54-119 (quantize_ac)
-  void quantize_ac(const float* a, int16_t* out) const {
+  // jpeg/src/rdo.rs:54-119 (quantize_ac). `pw` (nullable, 64 entries in zigzag order) is the perceptual mode's
+  // per-coefficient weight: the distortion weight of position k becomes w[k] * pw[k] (rounded to f32 first). With
+  // pw == nullptr this is the reference's plain MSE trellis.
+  void quantize_ac(const float* a, int16_t* out, const float* pw = nullptr) const {
+    float wk[64];
+    for (int k = 0; k < 64; k++) wk[k] = pw ? w[k] * pw[k] : w[k];
     struct Node {
       int pos;
       uint32_t v;
@@ -311,7 +315,7 @@ struct Rdo {
     zd[0] = 0.0f;
     for (int k = 1; k < 64; k++) {
       float e = a[k] * q[k];
-      zd[k] = zd[k - 1] + e * e * w[k];
+      zd[k] = zd[k - 1] + e * e * wk[k];
     }
     Node nodes[128];
     int nn = 0;
@@ -322,7 +326,7 @@ struct Rdo {
       uint32_t lo = v0 > 1 ? v0 - 1 : v0;
       for (uint32_t v = lo; v <= v0; v++) {
         float e = (m - (float)v) * q[i];
-        float dnz = e * e * w[i];
+        float dnz = e * e * wk[i];
         float best = zd[i - 1] + lambda * rate((uint32_t)(i - 1), v) + dnz;
         int prev = START;
         for (int ni = 0; ni < nn; ni++) {
@@ -400,7 +404,7 @@ static void fdct_divisors(const uint8_t* q, float* d) {
 
 // jpeg/src/encode.rs:185-219 (quantize_plane)
 static std::vector<int16_t> quantize_plane(const uint8_t* plane, int stride, int bw, int bh, const float* div,
-                                           const Rdo* rdo) {
+                                           const Rdo* rdo, const float* weights = nullptr) {
   std::vector<int16_t> out((size_t)bw * bh * 64, 0);
 #pragma omp parallel for schedule(dynamic)
   for (int by = 0; by < bh; by++) {
@@ -425,7 +429,7 @@ static std::vector<int16_t> quantize_plane(const uint8_t* plane, int stride, int
           a[k] = flat[f] * div[f];
         }
         dst[0] = (int16_t)clampi(round_f32(a[0]), -2047, 2047);
-        rdo->quantize_ac(a, dst);
+        rdo->quantize_ac(a, dst, weights ? weights + ((size_t)by * bw + bx) * 64 : nullptr);
       }
     }
   }
@@ -552,8 +556,10 @@ static void ac_code_lengths(const CoefImage& ci, uint8_t out[2][256]) {
 enum Subsampling { SUB_AUTO = 0, SUB_444 = 1, SUB_422 = 2, SUB_420 = 3 };
 
 // jpeg/src/encode.rs:426-539 (build_coefs). `channels` is 1 (Gray) or 3 (Rgb), 8-bit.
+// `weights` (nullable): the perceptual trellis's per-coefficient weights in the coefficient layout (components in
+// order, blocks row-major, 64 zigzag entries each); only the trellis pass reads them.
 static CoefImage build_coefs(const uint8_t* data, int w, int h, int channels, int quality, int subsampling,
-                             bool trellis) {
+                             bool trellis, const float* weights = nullptr) {
   bool gray = channels == 1;
   int hmax, vmax;
   if (gray) {
@@ -664,9 +670,12 @@ static CoefImage build_coefs(const uint8_t* data, int w, int h, int channels, in
     float divs[2][64];
     fdct_divisors(tables[0], divs[0]);
     fdct_divisors(tables[1], divs[1]);
+    size_t blk0 = 0;
     for (size_t i = 0; i < ci.comps.size(); i++) {
       PlaneRef& p = planes[i];
-      ci.comps[i].coefs = quantize_plane(p.p.data(), p.stride, p.bw, p.bh, divs[p.cls], rdos[p.cls]);
+      const float* pw = weights ? weights + blk0 * 64 : nullptr;
+      ci.comps[i].coefs = quantize_plane(p.p.data(), p.stride, p.bw, p.bh, divs[p.cls], rdos[p.cls], pw);
+      blk0 += (size_t)p.bw * p.bh;
     }
   }
   return ci;
@@ -1568,16 +1577,16 @@ static double score_coefs(const uint8_t* ref, int w, int h, int channels, const 
 
 static Found find_quality(const uint8_t* ref, int w, int h, int channels, double target, int max_quality,
                           int subsampling, bool trellis, std::vector<std::pair<int, double>>* trace,
-                          int metric = METRIC_SSIMULACRA2) {
+                          int metric = METRIC_SSIMULACRA2, const float* weights = nullptr) {
   int lo = 1, hi = std::max(max_quality, 1);
-  CoefImage top = build_coefs(ref, w, h, channels, hi, subsampling, trellis);
+  CoefImage top = build_coefs(ref, w, h, channels, hi, subsampling, trellis, weights);
   double top_score = score_coefs(ref, w, h, channels, top, metric);
   if (trace) trace->push_back({hi, top_score});
   Found best{hi, top_score, std::move(top)};
   if (top_score < target) return best;
   while (lo < hi) {
     int mid = lo + (hi - lo) / 2;
-    CoefImage ci = build_coefs(ref, w, h, channels, mid, subsampling, trellis);
+    CoefImage ci = build_coefs(ref, w, h, channels, mid, subsampling, trellis, weights);
     double s = score_coefs(ref, w, h, channels, ci, metric);
     if (trace) trace->push_back({mid, s});
     if (s >= target) {
@@ -2738,9 +2747,9 @@ int orc_coef_layout(int w, int h, int channels, int quality, int subsampling, in
 }
 
 int orc_build_coefs(const uint8_t* data, int w, int h, int channels, int quality, int subsampling, int trellis,
-                    int16_t* coefs_out, uint8_t* qtables_out) {
+                    int16_t* coefs_out, uint8_t* qtables_out, const float* weights) {
   if (w < 1 || h < 1 || (channels != 1 && channels != 3)) return 1;
-  orc::CoefImage ci = orc::build_coefs(data, w, h, channels, quality, subsampling, trellis != 0);
+  orc::CoefImage ci = orc::build_coefs(data, w, h, channels, quality, subsampling, trellis != 0, weights);
   orc::coef_to_flat(ci, coefs_out, qtables_out);
   return 0;
 }
@@ -2779,12 +2788,12 @@ int orc_ssimulacra2_fp64(const uint8_t* ref, const uint8_t* dist, int w, int h, 
 // every evaluated (quality, score) in order; *ntrace their count.
 int orc_search(const uint8_t* data, int w, int h, int channels, double target, int max_quality, int subsampling,
                int trellis, int* found_q, double* found_score, int16_t* coefs_out, uint8_t* qtables_out, int* trace_q,
-               double* trace_s, int* ntrace, int metric) {
+               double* trace_s, int* ntrace, int metric, const float* weights) {
   if (channels != 1 && channels != 3) return 1;
   if (metric == orc::METRIC_SSIMULACRA2 && (w < 8 || h < 8)) return 1;
   std::vector<std::pair<int, double>> tr;
-  orc::Found f =
-      orc::find_quality(data, w, h, channels, target, max_quality, subsampling, trellis != 0, &tr, metric);
+  orc::Found f = orc::find_quality(data, w, h, channels, target, max_quality, subsampling, trellis != 0, &tr, metric,
+                                   weights);
   *found_q = f.quality;
   *found_score = f.score;
   if (coefs_out) orc::coef_to_flat(f.coefs, coefs_out, qtables_out);

@@ -35,11 +35,11 @@ def lib():
         pi = ctypes.POINTER(ctypes.c_int)
         L.orc_ssimulacra2.argtypes = [P, P, i32, i32, i32, i32, pd, P, pi]
         L.orc_ssimulacra2_fp64.argtypes = [P, P, i32, i32, i32, i32, pd, P, pi]
-        L.orc_build_coefs.argtypes = [P, i32, i32, i32, i32, i32, i32, P, P]
+        L.orc_build_coefs.argtypes = [P, i32, i32, i32, i32, i32, i32, P, P, P]
         L.orc_coef_layout.argtypes = [i32, i32, i32, i32, i32, pi, P, P, P, P]
         L.orc_reconstruct.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, pi]
         L.orc_ac_code_lengths.argtypes = [i32, i32, i32, P, P, P, P, P, P, P]
-        L.orc_search.argtypes = [P, i32, i32, i32, ctypes.c_double, i32, i32, i32, pi, pd, P, P, P, P, pi, i32]
+        L.orc_search.argtypes = [P, i32, i32, i32, ctypes.c_double, i32, i32, i32, pi, pd, P, P, P, P, pi, i32, P]
         for name in ("orc_ssim", "orc_psnr"):
             getattr(L, name).argtypes = [P, P, i32, i32, i32]
             getattr(L, name).restype = ctypes.c_double
@@ -124,13 +124,24 @@ def layout(w, h, channels, quality, subsampling):
                 ncoefs=int(sum(bws[i] * bhs[i] for i in range(n)) * 64))
 
 
-def build_coefs(src, quality, subsampling, trellis=True):
+def _weights(weights, ncoefs):
+    """The perceptual trellis's per-coefficient weights (f32, coefficient layout) or None for the plain trellis."""
+    if weights is None:
+        return None, None
+    wt = np.ascontiguousarray(weights, dtype=np.float32)
+    if wt.size != ncoefs:
+        raise ValueError("weights do not match the coefficient layout")
+    return wt, wt.ctypes.data
+
+
+def build_coefs(src, quality, subsampling, trellis=True, weights=None):
     a, w, h, c, _ = _img(src)
     lay = layout(w, h, c, quality, subsampling)
     coefs = np.zeros(lay["ncoefs"], dtype=np.int16)
     qt = np.zeros((2, 64), dtype=np.uint8)
+    wt, wp = _weights(weights, lay["ncoefs"])
     rc = lib().orc_build_coefs(a.ctypes.data, w, h, c, quality, int(subsampling), 1 if trellis else 0,
-                               coefs.ctypes.data, qt.ctypes.data)
+                               coefs.ctypes.data, qt.ctypes.data, wp)
     if rc != 0:
         raise ValueError("bad input")
     return coefs, qt, lay
@@ -166,7 +177,9 @@ def ac_code_lengths(w, h, lay, qt, coefs):
 METRIC_SSIMULACRA2, METRIC_SSIM = 0, 1
 
 
-def search(src, target, max_quality=100, subsampling=0, trellis=True, metric=METRIC_SSIMULACRA2):
+def search(src, target, max_quality=100, subsampling=0, trellis=True, metric=METRIC_SSIMULACRA2, weights=None):
+    """find_quality_with; `weights` (explicit subsampling only) switches every candidate's trellis to the
+    perceptual mode."""
     a, w, h, c, _ = _img(src)
     q = ctypes.c_int()
     s = ctypes.c_double()
@@ -177,9 +190,12 @@ def search(src, target, max_quality=100, subsampling=0, trellis=True, metric=MET
     cap = max(layout(w, h, c, qq, subsampling)["ncoefs"] for qq in (1, 89, 90, 100))
     coefs = np.zeros(cap, dtype=np.int16)
     qt = np.zeros((2, 64), dtype=np.uint8)
+    if weights is not None and int(subsampling) == 0 and c == 3:
+        raise ValueError("perceptual weights need an explicit subsampling")
+    wt, wp = (None, None) if weights is None else _weights(weights, layout(w, h, c, 50, subsampling)["ncoefs"])
     rc = lib().orc_search(a.ctypes.data, w, h, c, float(target), int(max_quality), int(subsampling),
                           1 if trellis else 0, ctypes.byref(q), ctypes.byref(s), coefs.ctypes.data, qt.ctypes.data,
-                          tq.ctypes.data, ts.ctypes.data, ctypes.byref(nt), int(metric))
+                          tq.ctypes.data, ts.ctypes.data, ctypes.byref(nt), int(metric), wp)
     if rc != 0:
         raise ValueError("bad input")
     lay = layout(w, h, c, q.value, subsampling)
@@ -378,3 +394,107 @@ def grad64(ref, dist):
     s = lib().orc_grad64(r.ctypes.data, d.ctypes.data, w, h, g.ctypes.data)
     return s, g
 
+
+
+# ------------------------------------------------------------------------------------------------ perceptual trellis
+# The adjoint of the decoder's linear part, restated in numpy (f64). Forward: orthonormal 8x8 IDCT per block
+# (jpeg/src/dct.rs:67-119 with the multipliers of jpeg/src/decode.rs:1316-1321), triangle-filter chroma upsampling
+# (jpeg/src/decode.rs:1768-1828: 3/4 near + 1/4 far per axis, far index clamped), fixed-point YCbCr->RGB
+# (jpeg/src/decode.rs:1438-1441); roundings and clamps dropped. The weights are the perceptual mode's rule (no
+# reference counterpart): W[b][k] = strength * clamp((s_b / mean_c s)^gamma, w_min, w_max), s_b the RMS of the blocks'
+# gradient energies over a (2 radius + 1)^2 edge-replicated neighbourhood.
+
+ZIGZAG = np.array([0, 1, 8, 16, 9, 2, 3, 10, 17, 24, 32, 25, 18, 11, 4, 5, 12, 19, 26, 33, 40, 48, 41, 34, 27, 20,
+                   13, 6, 7, 14, 21, 28, 35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51, 58, 59, 52,
+                   45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63])  # jpeg/src/lib.rs:14-19
+DCT8 = np.array([[(np.sqrt(1 / 8) if u == 0 else 0.5) * np.cos((2 * x + 1) * u * np.pi / 16) for x in range(8)]
+                 for u in range(8)])
+# d(R, G, B) / d(Y, Cb, Cr) of jpeg/src/decode.rs:1438-1441 without rounding
+YCC_TO_RGB = np.array([[1.0, 0.0, 91881 / 65536], [1.0, -22554 / 65536, -46802 / 65536], [1.0, 116130 / 65536, 0.0]])
+
+
+def _upsample_matrix(n_full, n_c, f):
+    """[n_full, n_c] weights of one axis of the upsampler (identity for f == 1)."""
+    m = np.zeros((n_full, n_c))
+    if f == 1:
+        m[np.arange(n_full), np.arange(n_full)] = 1.0
+        return m
+    x = np.arange(n_full)
+    near = x // 2
+    far = np.where(x % 2 == 0, np.maximum(near - 1, 0), np.minimum(near + 1, n_c - 1))
+    np.add.at(m, (x, near), 0.75)
+    np.add.at(m, (x, far), 0.25)
+    return m
+
+
+def _comp_geometry(w, h, lay, c):
+    hmax, vmax = max(lay["h"]), max(lay["v"])
+    fx, fy = hmax // lay["h"][c], vmax // lay["v"][c]
+    cw, ch = (w * lay["h"][c] + hmax - 1) // hmax, (h * lay["v"][c] + vmax - 1) // vmax
+    return fx, fy, cw, ch
+
+
+def component_gradients(grad, w, h, lay):
+    """d score / d component sample per component (padded block grid, f64), from d score / d RGB (h, w, 3)."""
+    g = np.asarray(grad, dtype=np.float64)
+    if lay["ncomp"] == 1:
+        planes = [g.sum(2)]
+    else:
+        planes = [np.tensordot(g, YCC_TO_RGB[:, c], axes=([2], [0])) for c in range(3)]
+    out = []
+    for c in range(lay["ncomp"]):
+        fx, fy, cw, ch = _comp_geometry(w, h, lay, c)
+        ux, uy = _upsample_matrix(w, cw, fx), _upsample_matrix(h, ch, fy)
+        gc = uy.T @ planes[c] @ ux
+        P = np.zeros((lay["blocks_h"][c] * 8, lay["blocks_w"][c] * 8))
+        P[:ch, :cw] = gc
+        out.append(P)
+    return out
+
+
+def coef_gradient(grad, w, h, lay):
+    """d score / d coefficient (dequantized units), coefficient layout (64 zigzag entries per block), f64."""
+    res = []
+    for c, P in enumerate(component_gradients(grad, w, h, lay)):
+        bw, bh = lay["blocks_w"][c], lay["blocks_h"][c]
+        B = P.reshape(bh, 8, bw, 8).transpose(0, 2, 1, 3)
+        G = np.einsum("vy,abyx,ux->abvu", DCT8, B, DCT8).reshape(bh * bw, 64)
+        res.append(G[:, ZIGZAG].reshape(-1))
+    return np.concatenate(res)
+
+
+def decode_linear(coef_f, w, h, lay):
+    """The forward map whose adjoint coef_gradient is: dequantized coefficients (coefficient layout) -> RGB (h, w, 3)
+    (or Gray replicated), without level shift, roundings or clamps."""
+    comps, off = [], 0
+    for c in range(lay["ncomp"]):
+        bw, bh = lay["blocks_w"][c], lay["blocks_h"][c]
+        F = np.zeros((bh * bw, 64))
+        F[:, ZIGZAG] = coef_f[off * 64:(off + bw * bh) * 64].reshape(-1, 64)
+        off += bw * bh
+        B = np.einsum("vy,abvu,ux->abyx", DCT8, F.reshape(bh, bw, 8, 8), DCT8)
+        P = B.transpose(0, 2, 1, 3).reshape(bh * 8, bw * 8)
+        fx, fy, cw, ch = _comp_geometry(w, h, lay, c)
+        comps.append(_upsample_matrix(h, ch, fy) @ P[:ch, :cw] @ _upsample_matrix(w, cw, fx).T)
+    if lay["ncomp"] == 1:
+        return np.repeat(comps[0][:, :, None], 3, 2)
+    return np.stack([sum(YCC_TO_RGB[k, c] * comps[c] for c in range(3)) for k in range(3)], 2)
+
+
+def perceptual_weights(grad, w, h, lay, strength=0.35, gamma=0.5, w_min=0.25, w_max=4.0, radius=1):
+    """The perceptual trellis weights (f32, coefficient layout) from d score / d RGB."""
+    res = []
+    for c, P in enumerate(component_gradients(grad, w, h, lay)):
+        bw, bh = lay["blocks_w"][c], lay["blocks_h"][c]
+        e = (P.reshape(bh, 8, bw, 8) ** 2).sum((1, 3))
+        p = np.pad(e, radius, mode="edge")
+        acc = np.zeros_like(e)
+        for dy in range(2 * radius + 1):
+            for dx in range(2 * radius + 1):
+                acc += p[dy:dy + bh, dx:dx + bw]
+        s = np.sqrt(acc / (2 * radius + 1) ** 2).reshape(-1)
+        m = s.mean()
+        r = s / m if m > 0 else np.ones_like(s)
+        wv = (np.clip(r ** gamma, w_min, w_max) * strength).astype(np.float32)
+        res.append(np.repeat(wv, 64))
+    return np.concatenate(res)

@@ -35,6 +35,7 @@ UNITS = {
     "metrics.cu": [],
     "jpegdec.cu": [],
     "adjoint.cu": [],
+    "perceptual.cu": [],
 }
 
 

@@ -151,9 +151,10 @@ __global__ void k_vblur64_t(const double* __restrict__ g, int w, int h, double* 
   }
 }
 
-// The six map sums of one channel (:421-440): block partial sums, then one double atomic each.
+// The six map sums of one channel (:421-440): per-CTA partial sums (parts[block][6]); k_sum_parts adds them in a
+// fixed order, so the score and the gradient are the same bits on every run.
 __global__ void __launch_bounds__(256) k_maps64(const double* __restrict__ mom, const double* __restrict__ xa,
-                                                const double* __restrict__ xb, long long n, double* __restrict__ sums) {
+                                                const double* __restrict__ xb, long long n, double* __restrict__ parts) {
   __shared__ double red[6][8];
   double acc[6] = {0, 0, 0, 0, 0, 0};
   for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -182,8 +183,19 @@ __global__ void __launch_bounds__(256) k_maps64(const double* __restrict__ mom, 
   if (threadIdx.x < 6) {
     double v = 0.0;
     for (int wi = 0; wi < 8; wi++) v += red[threadIdx.x][wi];
-    atomicAdd(&sums[threadIdx.x], v);
+    parts[(size_t)blockIdx.x * 6 + threadIdx.x] = v;
   }
+}
+
+// sums[k] = the nparts partials of column k, one warp per column, lanes strided then a shuffle tree.
+__global__ void __launch_bounds__(192) k_sum_parts(const double* __restrict__ parts, int nparts,
+                                                   double* __restrict__ sums) {
+  const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double v = 0.0;
+  for (int i = lane; i < nparts; i += 32) v += parts[(size_t)i * 6 + k];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) sums[k] = v;
 }
 
 // Per sample of one channel: d score / d (m2, s22, s12) and the direct d score / d xb of the edge maps, given the
@@ -268,7 +280,9 @@ __global__ void k_grad_out64(const double* __restrict__ g_lin, const float* __re
     for (int c = 0; c < 3; c++) grad[i * 3 + c] = g_lin[c * n + i] * srgb64_deriv((double)dist[i * 3 + c]);
 }
 
-unsigned grid_of(long long n) { return (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 32)); }
+unsigned grid_of(long long n) {
+  return (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 32));
+}
 
 }  // namespace
 
@@ -327,15 +341,16 @@ int ssim2_grad_device(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, i
       RCG_LAUNCH(ctx, "adj_vblur", k_vblur64, grid_of(n), 256, 0, hb, sc[s].w, sc[s].h, mom + q * n);
     }
   };
-  cudaMemsetAsync(sums, 0, sizeof(double) * kMaxScales * 18, ctx->stream);
+  double* parts = (double*)workspace(ctx, "adj_parts", sizeof(double) * 6 * grid_of(n0));
+  if (!parts) return RCG_NO_MEMORY;
   for (int s = 0; s < ns; s++) {
     const long long n = sc[s].n;
     RCG_LAUNCH(ctx, "adj_xyb", k_xyb64, grid_of(n), 256, 0, pa + sc[s].off, n, xa);
     RCG_LAUNCH(ctx, "adj_xyb", k_xyb64, grid_of(n), 256, 0, pb + sc[s].off, n, xb);
     for (int c = 0; c < 3; c++) {
       moments(s, c);
-      RCG_LAUNCH(ctx, "adj_maps", k_maps64, grid_of(n), 256, 0, mom, xa + c * n, xb + c * n, n,
-                 sums + s * 18 + c * 6);
+      RCG_LAUNCH(ctx, "adj_maps", k_maps64, grid_of(n), 256, 0, mom, xa + c * n, xb + c * n, n, parts);
+      RCG_LAUNCH(ctx, "adj_sum_parts", k_sum_parts, 1, 192, 0, parts, (int)grid_of(n), sums + s * 18 + c * 6);
     }
   }
   double hs[kMaxScales * 18];

@@ -616,8 +616,11 @@ int rcg_metric_score_device(rcg_ctx* ctx, int metric, const uint8_t* d_reference
 
 // ---- encoder
 
-int rcg_build_coefs(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
-                    const rcg_encode_options* opts, int16_t* coefs, size_t coefs_len, uint8_t* qtables) {
+// build_coefs (jpeg/src/encode.rs:426-539); `weights` (host, nullable, ncoefs entries) runs the trellis pass in the
+// perceptual mode.
+static int build_coefs_impl(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
+                            const rcg_encode_options* opts, const float* weights, size_t weights_len, int16_t* coefs,
+                            size_t coefs_len, uint8_t* qtables) {
   if (!ctx) return RCG_INVALID;
   int rc;
   if ((rc = check_image(ctx, width, height, channels)) != RCG_OK) return rc;
@@ -631,16 +634,23 @@ int rcg_build_coefs(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t h
     delete st;
     return fail(ctx, RCG_INVALID, "coefficient buffer too short");
   }
+  if (weights && (long long)weights_len != ncoefs) {
+    delete st;
+    return fail(ctx, RCG_INVALID, "weights do not match the coefficient layout");
+  }
   cudaSetDevice(ctx->device);
   size_t bytes = (size_t)w * h * channels;
   uint8_t* d_src = (uint8_t*)workspace(ctx, "img_a", bytes);
   int16_t* d_coefs = (int16_t*)workspace(ctx, "coefs_single", (size_t)ncoefs * 2);
   StepDesc* d_st = (StepDesc*)workspace(ctx, "step_single", sizeof(StepDesc));
-  if (!d_src || !d_coefs || !d_st) {
+  float* d_w = weights ? (float*)workspace(ctx, "weights_single", (size_t)ncoefs * sizeof(float)) : nullptr;
+  if (!d_src || !d_coefs || !d_st || (weights && !d_w)) {
     delete st;
     return RCG_NO_MEMORY;
   }
   st->coefs = d_coefs;
+  st->pweights = d_w;
+  if (weights) cudaMemcpyAsync(d_w, weights, (size_t)ncoefs * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
   cudaMemcpyAsync(d_src, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
   cudaMemcpyAsync(d_st, st, sizeof(StepDesc), cudaMemcpyHostToDevice, ctx->stream);
   EncoderSetup es;
@@ -653,7 +663,7 @@ int rcg_build_coefs(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t h
   }
   quantize(ctx, d_st, es.caches, st->nblocks);
   rate_tables(ctx, d_st);
-  trellis(ctx, d_st, es.caches, st->nblocks);
+  trellis(ctx, d_st, es.caches, st->nblocks, weights != nullptr);
   cudaMemcpyAsync(coefs, d_coefs, (size_t)ncoefs * 2, cudaMemcpyDeviceToHost, ctx->stream);
   if (qtables) {
     std::memcpy(qtables, st->qt[0], 64);
@@ -662,6 +672,19 @@ int rcg_build_coefs(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t h
   cudaStreamSynchronize(ctx->stream);  // the host StepDesc must outlive the async upload
   delete st;
   return finish(ctx, "build_coefs");
+}
+
+int rcg_build_coefs(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
+                    const rcg_encode_options* opts, int16_t* coefs, size_t coefs_len, uint8_t* qtables) {
+  return build_coefs_impl(ctx, src, width, height, channels, opts, nullptr, 0, coefs, coefs_len, qtables);
+}
+
+int rcg_build_coefs_weighted(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
+                             const rcg_encode_options* opts, const float* weights, size_t weights_len, int16_t* coefs,
+                             size_t coefs_len, uint8_t* qtables) {
+  if (!ctx) return RCG_INVALID;
+  if (!weights) return fail(ctx, RCG_INVALID, "null weights");
+  return build_coefs_impl(ctx, src, width, height, channels, opts, weights, weights_len, coefs, coefs_len, qtables);
 }
 
 // ---- decoder
@@ -776,9 +799,12 @@ static void score_candidate(rcg_ctx* ctx, const SearchScorer& sc, StepDesc* d_st
   score_pyramids(ctx, sc.pd, sc.ref_pyr, sc.dist_pyr, sc.d_score, d_ss, d_st);
 }
 
+// d_weights (nullable): the perceptual trellis's weights in the coefficient layout of the (quality-independent)
+// subsampling; every candidate's trellis then runs in the weighted mode.
 static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, int metric, double target,
                        int max_q, int subsampling, int trellis_on, rcg_found* found, int16_t* d_coefs_out,
-                       size_t coefs_len, uint8_t* d_qt_out, int16_t* h_coefs_out, uint8_t* h_qt_out) {
+                       size_t coefs_len, uint8_t* d_qt_out, int16_t* h_coefs_out, uint8_t* h_qt_out,
+                       const float* d_weights = nullptr) {
   int rc;
   SearchScorer sc;
   SearchState* d_ss = (SearchState*)workspace(ctx, "search_state", sizeof(SearchState));
@@ -815,10 +841,10 @@ static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int cha
   hs.best_q = max_q;
   cudaMemcpyAsync(d_ss, &hs, sizeof hs, cudaMemcpyHostToDevice, ctx->stream);
   for (int s = 0; s < max_steps; s++) {
-    step_tables(ctx, d_ss, d_st, w, h, slots, es.max_coefs);
+    step_tables(ctx, d_ss, d_st, w, h, slots, es.max_coefs, d_weights);
     quantize(ctx, d_st, es.caches, es.max_blocks);
     rate_tables(ctx, d_st);
-    trellis(ctx, d_st, es.caches, es.max_blocks);
+    trellis(ctx, d_st, es.caches, es.max_blocks, d_weights != nullptr);
     dequant_idct(ctx, d_st, nullptr, planes, es.max_blocks);
     score_candidate(ctx, sc, d_st, planes, w, h, channels, d_ss);
   }
@@ -1228,6 +1254,248 @@ int rcg_ssimulacra2_grad(rcg_ctx* ctx, const uint8_t* reference, const float* di
     return rc;
   if (grad && (rc = copy_to_host(ctx, grad, d_grad, n * sizeof(double))) != RCG_OK) return rc;
   return finish(ctx, "ssimulacra2 gradient");
+}
+
+// ---- perceptual trellis
+
+void rcg_perceptual_defaults(rcg_perceptual_options* o) {
+  if (!o) return;
+  o->strength = 0.35;
+  o->gamma = 0.5;
+  o->w_min = 0.25;
+  o->w_max = 4.0;
+  o->radius = 1;
+  o->keep_smaller = 1;
+}
+
+static int check_popts(rcg_ctx* ctx, const rcg_perceptual_options* o, PerceptualParams* p) {
+  if (!o) return fail(ctx, RCG_INVALID, "null perceptual options");
+  const bool ok = std::isfinite(o->strength) && o->strength > 0.0 && std::isfinite(o->gamma) && o->gamma >= 0.0 &&
+                  std::isfinite(o->w_max) && o->w_min > 0.0 && o->w_max >= o->w_min && o->radius >= 0 &&
+                  o->radius <= 16;
+  if (!ok) return fail(ctx, RCG_INVALID, "perceptual options out of range");
+  *p = PerceptualParams{o->strength, o->gamma, o->w_min, o->w_max, o->radius};
+  return RCG_OK;
+}
+
+// The SSIMULACRA2 gradient at the decoded image d_dec against d_ref (both 8-bit with `channels`), pulled back to the
+// coefficient layout `lay`: coefficient gradient and/or weights (each nullable).
+static int perceptual_impl(rcg_ctx* ctx, const uint8_t* d_ref, const uint8_t* d_dec, int w, int h, int channels,
+                           const StepDesc* lay, const PerceptualParams& p, double* score, double* d_coef_grad,
+                           float* d_weights) {
+  const size_t npx = (size_t)w * h;
+  float* d_dist = (float*)workspace(ctx, "perc_dist", npx * 3 * sizeof(float));
+  double* d_grad = (double*)workspace(ctx, "perc_grad", npx * 3 * sizeof(double));
+  if (!d_dist || !d_grad) return RCG_NO_MEMORY;
+  const uint8_t* ref3 = d_ref;
+  if (channels == 1) {
+    uint8_t* r3 = (uint8_t*)workspace(ctx, "perc_ref3", npx * 3);
+    if (!r3) return RCG_NO_MEMORY;
+    expand_rgb(ctx, d_ref, 1, npx, r3, nullptr);
+    ref3 = r3;
+  }
+  expand_rgb(ctx, d_dec, channels, npx, nullptr, d_dist);
+  int rc = ssim2_grad_device(ctx, ref3, d_dist, w, h, score, d_grad);
+  if (rc != RCG_OK) return rc;
+  return perceptual_pullback(ctx, d_grad, w, h, lay, p, d_coef_grad, d_weights);
+}
+
+// Shared checks and uploads of rcg_coef_gradient / rcg_perceptual_weights; `*st` owned by the caller on success.
+static int pullback_inputs(rcg_ctx* ctx, const uint8_t* reference, const uint8_t* decoded, uint32_t width,
+                           uint32_t height, int channels, const rcg_coef_layout* layout, const void* out,
+                           size_t out_len, StepDesc** st_out, const uint8_t** d_ref, const uint8_t** d_dec) {
+  if (!reference || !decoded || !layout || !out) return fail(ctx, RCG_INVALID, "null pointer");
+  int rc;
+  if ((rc = check_image(ctx, width, height, channels)) != RCG_OK) return rc;
+  if (width < (uint32_t)kMinSide || height < (uint32_t)kMinSide)
+    return fail(ctx, RCG_UNSUPPORTED, "SSIMULACRA 2 needs at least 8x8 pixels");
+  if (layout->ncomp != channels) return fail(ctx, RCG_INVALID, "layout.ncomp does not match the channel count");
+  StepDesc* st = new StepDesc;
+  if ((rc = layout_step(ctx, st, (int)width, (int)height, layout)) != RCG_OK) {
+    delete st;
+    return rc;
+  }
+  if ((long long)out_len < st->nblocks * 64) {
+    delete st;
+    return fail(ctx, RCG_INVALID, "output buffer too short");
+  }
+  cudaSetDevice(ctx->device);
+  const size_t bytes = (size_t)width * height * channels;
+  uint8_t* a = (uint8_t*)workspace(ctx, "img_a", bytes);
+  uint8_t* b = (uint8_t*)workspace(ctx, "img_b", bytes);
+  if (!a || !b) {
+    delete st;
+    return RCG_NO_MEMORY;
+  }
+  if ((rc = copy_to_device(ctx, a, reference, bytes)) == RCG_OK) rc = copy_to_device(ctx, b, decoded, bytes);
+  if (rc != RCG_OK) {
+    delete st;
+    return rc;
+  }
+  *st_out = st;
+  *d_ref = a;
+  *d_dec = b;
+  return RCG_OK;
+}
+
+int rcg_coef_gradient(rcg_ctx* ctx, const uint8_t* reference, const uint8_t* decoded, uint32_t width, uint32_t height,
+                      int channels, const rcg_coef_layout* layout, double* score, double* grad, size_t grad_len) {
+  if (!ctx) return RCG_INVALID;
+  if (!score) return fail(ctx, RCG_INVALID, "null pointer");
+  StepDesc* st = nullptr;
+  const uint8_t *d_ref = nullptr, *d_dec = nullptr;
+  int rc = pullback_inputs(ctx, reference, decoded, width, height, channels, layout, grad, grad_len, &st, &d_ref,
+                           &d_dec);
+  if (rc != RCG_OK) return rc;
+  const size_t n = (size_t)st->nblocks * 64;
+  double* d_cg = (double*)workspace(ctx, "perc_coef_grad", n * sizeof(double));
+  if (!d_cg) rc = RCG_NO_MEMORY;
+  PerceptualParams p{1.0, 0.0, 1.0, 1.0, 0};
+  if (rc == RCG_OK) rc = perceptual_impl(ctx, d_ref, d_dec, (int)width, (int)height, channels, st, p, score, d_cg,
+                                         nullptr);
+  delete st;
+  if (rc == RCG_OK) rc = copy_to_host(ctx, grad, d_cg, n * sizeof(double));
+  return rc == RCG_OK ? finish(ctx, "coefficient gradient") : rc;
+}
+
+int rcg_perceptual_weights(rcg_ctx* ctx, const uint8_t* reference, const uint8_t* decoded, uint32_t width,
+                           uint32_t height, int channels, const rcg_coef_layout* layout,
+                           const rcg_perceptual_options* popts, double* score, float* weights, size_t weights_len) {
+  if (!ctx) return RCG_INVALID;
+  if (!score) return fail(ctx, RCG_INVALID, "null pointer");
+  PerceptualParams p;
+  int rc = check_popts(ctx, popts, &p);
+  if (rc != RCG_OK) return rc;
+  StepDesc* st = nullptr;
+  const uint8_t *d_ref = nullptr, *d_dec = nullptr;
+  rc = pullback_inputs(ctx, reference, decoded, width, height, channels, layout, weights, weights_len, &st, &d_ref,
+                       &d_dec);
+  if (rc != RCG_OK) return rc;
+  const size_t n = (size_t)st->nblocks * 64;
+  float* d_w = (float*)workspace(ctx, "perc_weights", n * sizeof(float));
+  if (!d_w) rc = RCG_NO_MEMORY;
+  if (rc == RCG_OK) rc = perceptual_impl(ctx, d_ref, d_dec, (int)width, (int)height, channels, st, p, score, nullptr,
+                                         d_w);
+  delete st;
+  if (rc == RCG_OK) rc = copy_to_host(ctx, weights, d_w, n * sizeof(float));
+  return rc == RCG_OK ? finish(ctx, "perceptual weights") : rc;
+}
+
+// Checks of the weighted searches: SSIMULACRA2 goal, quality-independent layout, trellis on. `ncoefs` receives the
+// layout's coefficient count.
+static int weighted_search_checks(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
+                                  double target, const rcg_encode_options* opts, const rcg_found* found,
+                                  long long* ncoefs) {
+  int rc;
+  if ((rc = check_image(ctx, width, height, channels)) != RCG_OK) return rc;
+  if ((rc = check_opts(ctx, opts, false)) != RCG_OK) return rc;
+  if (!src || !found) return fail(ctx, RCG_INVALID, "null pointer");
+  if ((rc = check_goal(ctx, RCG_METRIC_SSIMULACRA2, width, height, target)) != RCG_OK) return rc;
+  if (channels == 3 && opts->subsampling == RCG_SUB_AUTO)
+    return fail(ctx, RCG_UNSUPPORTED, "the perceptual trellis needs an explicit subsampling");
+  if (!opts->trellis) return fail(ctx, RCG_INVALID, "the perceptual mode weights the trellis: enable it");
+  rcg_coef_layout lay;
+  layout_of((int)width, (int)height, channels, 50, opts->subsampling, &lay);
+  *ncoefs = lay.ncoefs;
+  return RCG_OK;
+}
+
+int rcg_search_weighted(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
+                        double target, int max_quality, const rcg_encode_options* opts, const float* weights,
+                        size_t weights_len, rcg_found* found, int16_t* coefs, size_t coefs_len, uint8_t* qtables) {
+  if (!ctx) return RCG_INVALID;
+  long long ncoefs = 0;
+  int rc = weighted_search_checks(ctx, src, width, height, channels, target, opts, found, &ncoefs);
+  if (rc != RCG_OK) return rc;
+  if (!weights || (long long)weights_len != ncoefs)
+    return fail(ctx, RCG_INVALID, "weights do not match the coefficient layout");
+  const int max_q = std::max(1, std::min(max_quality, 100));
+  cudaSetDevice(ctx->device);
+  const size_t bytes = (size_t)width * height * channels;
+  uint8_t* d_src = (uint8_t*)workspace(ctx, "img_src", bytes);
+  float* d_w = (float*)workspace(ctx, "perc_weights", (size_t)ncoefs * sizeof(float));
+  if (!d_src || !d_w) return RCG_NO_MEMORY;
+  if ((rc = copy_to_device(ctx, d_src, src, bytes)) != RCG_OK) return rc;
+  if ((rc = copy_to_device(ctx, d_w, weights, (size_t)ncoefs * sizeof(float))) != RCG_OK) return rc;
+  return search_impl(ctx, d_src, (int)width, (int)height, channels, RCG_METRIC_SSIMULACRA2, target, max_q,
+                     opts->subsampling, opts->trellis, found, nullptr, coefs_len, nullptr, coefs, qtables, d_w);
+}
+
+// write_best's size of a search result (the smaller of the planned progressive script and baseline).
+static int planned_bytes(rcg_ctx* ctx, const StepDesc* lay, int w, int h, const int16_t* d_coefs, uint64_t* bytes) {
+  rcg_plan_result r;
+  int rc = plan_scans(ctx, lay, w, h, d_coefs, &r);
+  if (rc != RCG_OK) return rc;
+  *bytes = std::min(r.progressive_bytes, r.baseline_bytes);
+  return RCG_OK;
+}
+
+int rcg_search_perceptual(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
+                          double target, int max_quality, const rcg_encode_options* opts,
+                          const rcg_perceptual_options* popts, rcg_found* plain, rcg_found* found, uint64_t* sizes,
+                          int* chose_perceptual, int16_t* coefs, size_t coefs_len, uint8_t* qtables, float* weights,
+                          size_t weights_len) {
+  if (!ctx) return RCG_INVALID;
+  long long ncoefs = 0;
+  int rc = weighted_search_checks(ctx, src, width, height, channels, target, opts, found, &ncoefs);
+  if (rc != RCG_OK) return rc;
+  PerceptualParams p;
+  if ((rc = check_popts(ctx, popts, &p)) != RCG_OK) return rc;
+  if (!plain) return fail(ctx, RCG_INVALID, "null pointer");
+  if (weights && (long long)weights_len < ncoefs) return fail(ctx, RCG_INVALID, "weights buffer too short");
+  if (coefs && (long long)coefs_len < ncoefs) return fail(ctx, RCG_INVALID, "coefficient buffer too short");
+  const int w = (int)width, h = (int)height;
+  const int max_q = std::max(1, std::min(max_quality, 100));
+  cudaSetDevice(ctx->device);
+  const size_t npx = (size_t)w * h;
+  uint8_t* d_src = (uint8_t*)workspace(ctx, "img_src", npx * channels);
+  int16_t* d_plain = (int16_t*)workspace(ctx, "perc_plain_coefs", (size_t)ncoefs * 2);
+  int16_t* d_perc = (int16_t*)workspace(ctx, "perc_coefs", (size_t)ncoefs * 2);
+  float* d_w = (float*)workspace(ctx, "perc_weights", (size_t)ncoefs * sizeof(float));
+  uint8_t* d_dec = (uint8_t*)workspace(ctx, "perc_dec", npx * channels);
+  StepDesc* d_st = (StepDesc*)workspace(ctx, "perc_step", sizeof(StepDesc));
+  if (!d_src || !d_plain || !d_perc || !d_w || !d_dec || !d_st) return RCG_NO_MEMORY;
+  if ((rc = copy_to_device(ctx, d_src, src, npx * channels)) != RCG_OK) return rc;
+  // 1. the plain search
+  rc = search_impl(ctx, d_src, w, h, channels, RCG_METRIC_SSIMULACRA2, target, max_q, opts->subsampling,
+                   opts->trellis, plain, d_plain, (size_t)ncoefs, nullptr, nullptr, nullptr);
+  if (rc != RCG_OK) return rc;
+  // 2. its decoded image, and the weights from the gradient there
+  StepDesc* st = new StepDesc;
+  host_step_tables(st, plain->quality, opts->subsampling, channels, opts->trellis, w, h);
+  uint8_t* planes = (uint8_t*)workspace(ctx, "perc_planes", (size_t)plane_bytes(st));
+  if (!planes) {
+    delete st;
+    return RCG_NO_MEMORY;
+  }
+  cudaMemcpyAsync(d_st, st, sizeof(StepDesc), cudaMemcpyHostToDevice, ctx->stream);
+  dequant_idct(ctx, d_st, d_plain, planes, st->nblocks);
+  upsample_color(ctx, d_st, planes, w, h, d_dec, nullptr);
+  double gscore = 0.0;
+  rc = perceptual_impl(ctx, d_src, d_dec, w, h, channels, st, p, &gscore, nullptr, d_w);
+  cudaStreamSynchronize(ctx->stream);  // the host StepDesc must outlive its upload
+  // 3. the weighted search
+  rcg_found perc;
+  if (rc == RCG_OK)
+    rc = search_impl(ctx, d_src, w, h, channels, RCG_METRIC_SSIMULACRA2, target, max_q, opts->subsampling,
+                     opts->trellis, &perc, d_perc, (size_t)ncoefs, nullptr, nullptr, nullptr, d_w);
+  // 4. sizes; keep the smaller
+  uint64_t sz[2] = {0, 0};
+  if (rc == RCG_OK) rc = planned_bytes(ctx, st, w, h, d_plain, &sz[0]);
+  if (rc == RCG_OK) rc = planned_bytes(ctx, st, w, h, d_perc, &sz[1]);
+  delete st;
+  if (rc != RCG_OK) return rc;
+  const bool use_perc = !popts->keep_smaller || sz[1] <= sz[0];
+  *found = use_perc ? perc : *plain;
+  if (sizes) {
+    sizes[0] = sz[0];
+    sizes[1] = sz[1];
+  }
+  if (chose_perceptual) *chose_perceptual = use_perc ? 1 : 0;
+  if (coefs && (rc = copy_to_host(ctx, coefs, use_perc ? d_perc : d_plain, (size_t)ncoefs * 2)) != RCG_OK) return rc;
+  if (qtables) qtables_for(found->quality, qtables);
+  if (weights && (rc = copy_to_host(ctx, weights, d_w, (size_t)ncoefs * sizeof(float))) != RCG_OK) return rc;
+  return finish(ctx, "perceptual search");
 }
 
 }  // extern "C"

@@ -195,6 +195,8 @@ void fill_mult(StepDesc* st, const uint8_t* qtables, int ntables) {
 
 float mult_entry_host(const uint8_t* q, int n) { return mult_entry(q, n); }
 
+int zigzag_natural(int k) { return zigzag(k); }
+
 void qtables_for(int quality, uint8_t* out128) {
   for (int n = 0; n < 64; n++) out128[n] = out128[64 + n] = qtable_entry(quality, n);
 }
@@ -467,6 +469,9 @@ int rate_tables(rcg_ctx* ctx, StepDesc* d_step) {
 // both candidate values of a position scan the earlier nodes in one pass (neither sees the other: the reference
 // skips nodes at the same position, :86-88). zd[i-1] is carried as a running sum, and each node keeps zd at its
 // own position, so no 64-entry zd table is needed.
+// kWeighted: the perceptual mode. Each coefficient's distortion weight becomes rw[k] * pweights[block][k] (one f32
+// product, then the same squared-error product as the plain weight); the plain instantiation reads no weights.
+template <bool kWeighted>
 __global__ void __launch_bounds__(128) k_trellis(StepDesc* __restrict__ st, CacheSet cs) {
   __shared__ float lr[3][64 * 16];
   if (!st->active || !st->use_trellis) return;
@@ -486,6 +491,7 @@ __global__ void __launch_bounds__(128) k_trellis(StepDesc* __restrict__ st, Cach
   const float* rq = st->rq[c];
   const float* rw = st->rw[c];
   const float* lrc = lr[c];
+  const float* pw = kWeighted ? st->pweights + gb * 64 : nullptr;  // 16-byte aligned rows of 64 floats
 
   float ncost[128], nzd[128];
   unsigned char npos[128];
@@ -510,6 +516,18 @@ __global__ void __launch_bounds__(128) k_trellis(StepDesc* __restrict__ st, Cach
 #pragma unroll
       for (int j = 0; j < kChunk; j++) nxt[j] = load(c0 + kChunk + j);
     }
+    float wv[kChunk];
+    if constexpr (kWeighted) {
+      const float4* p4 = reinterpret_cast<const float4*>(pw + c0);
+#pragma unroll
+      for (int g = 0; g < kChunk / 4; g++) {
+        const float4 v = __ldg(p4 + g);
+        wv[4 * g] = v.x;
+        wv[4 * g + 1] = v.y;
+        wv[4 * g + 2] = v.z;
+        wv[4 * g + 3] = v.w;
+      }
+    }
 #pragma unroll
     for (int j = 0; j < kChunk; j++) {
       const int i = c0 + j;
@@ -518,7 +536,7 @@ __global__ void __launch_bounds__(128) k_trellis(StepDesc* __restrict__ st, Cach
         dc = clampi(round_f32(a), -2047, 2047);
         continue;
       }
-      float q = rq[i], w = rw[i];
+      float q = rq[i], w = kWeighted ? fmul(rw[i], wv[j]) : rw[i];
       if (a < 0.0f) negmask |= 1ull << i;
       float m = fabsf(a);
       unsigned v0 = (unsigned)fadd(m, 0.5f);
@@ -603,11 +621,14 @@ __global__ void __launch_bounds__(128) k_trellis(StepDesc* __restrict__ st, Cach
   }
 }
 
-int trellis(rcg_ctx* ctx, StepDesc* d_step, const float* const* d_caches, long long max_blocks) {
+int trellis(rcg_ctx* ctx, StepDesc* d_step, const float* const* d_caches, long long max_blocks, bool weighted) {
   CacheSet cs;
-  for (int i = 0; i < 9; i++) cs.p[i] = d_caches[i];
+  for (int i = 0; i < 9; i++) cs.p[i] = d_caches ? d_caches[i] : nullptr;
   int grid = (int)((max_blocks + 127) / 128);
-  RCG_LAUNCH(ctx, "trellis", k_trellis, grid, 128, 0, d_step, cs);
+  if (weighted)
+    RCG_LAUNCH(ctx, "trellis_weighted", k_trellis<true>, grid, 128, 0, d_step, cs);
+  else
+    RCG_LAUNCH(ctx, "trellis", k_trellis<false>, grid, 128, 0, d_step, cs);
   return RCG_OK;
 }
 
@@ -845,7 +866,8 @@ int upsample_color(rcg_ctx* ctx, StepDesc* d_step, const uint8_t* d_planes, int 
 // threads: one per (component, coefficient) entry; the Rdo median is the element of rank 31 among q[1..63] (ties
 // broken by index, which leaves the value unchanged), the same value the reference's sort yields.
 __global__ void __launch_bounds__(192) k_step_tables(const SearchState* __restrict__ ss, StepDesc* __restrict__ st,
-                                                     int w, int h, int16_t* slots, long long slot_stride) {
+                                                     int w, int h, int16_t* slots, long long slot_stride,
+                                                     const float* pweights) {
   __shared__ uint8_t qt[64];
   __shared__ float rq[64];
   __shared__ float median;
@@ -861,6 +883,7 @@ __global__ void __launch_bounds__(192) k_step_tables(const SearchState* __restri
     st->requant = 0;
     fill_layout(st, q, ss->subsampling, ss->channels, ss->trellis, w, h);
     st->coefs = slots + (long long)step * slot_stride;
+    st->pweights = pweights;
   }
   if (t < 64) qt[t] = qtable_entry(q, t);
   __syncthreads();
@@ -885,8 +908,9 @@ __global__ void __launch_bounds__(192) k_step_tables(const SearchState* __restri
 }
 
 int step_tables(rcg_ctx* ctx, SearchState* d_search, StepDesc* d_step, int w, int h, int16_t* d_coef_slots,
-                long long slot_stride) {
-  RCG_LAUNCH(ctx, "step_tables", k_step_tables, 1, 192, 0, d_search, d_step, w, h, d_coef_slots, slot_stride);
+                long long slot_stride, const float* d_pweights) {
+  RCG_LAUNCH(ctx, "step_tables", k_step_tables, 1, 192, 0, d_search, d_step, w, h, d_coef_slots, slot_stride,
+             d_pweights);
   return RCG_OK;
 }
 

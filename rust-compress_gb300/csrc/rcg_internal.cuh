@@ -82,6 +82,9 @@ struct StepDesc {
   uint8_t src_qt[3][64]; // the source table of each component (old; all ones where its slot is empty)
   float ratio[3][64];    // old / new per zigzag position
   int16_t* coefs;        // where this candidate's coefficients go
+  // Perceptual trellis (opt-in): per-coefficient distortion weights in the coefficient layout ([block][64], zigzag),
+  // read only by the weighted trellis instantiation.
+  const float* pweights;
 };
 
 // The device-side bisection (jpeg/src/target.rs:29-56).
@@ -235,7 +238,8 @@ int quantize(rcg_ctx* ctx, StepDesc* d_step, const float* const* d_caches, long 
 // Plain requantization of st->coef_src into st->coefs, with the AC histogram when the trellis pass follows.
 int requantize_plain(rcg_ctx* ctx, StepDesc* d_step, long long max_blocks);
 int rate_tables(rcg_ctx* ctx, StepDesc* d_step);
-int trellis(rcg_ctx* ctx, StepDesc* d_step, const float* const* d_caches, long long max_blocks);
+// weighted: the perceptual mode (d_step->pweights); otherwise the reference's plain trellis.
+int trellis(rcg_ctx* ctx, StepDesc* d_step, const float* const* d_caches, long long max_blocks, bool weighted = false);
 // d_coefs null: decode the candidate's own coefficients (d_step->coefs).
 int dequant_idct(rcg_ctx* ctx, StepDesc* d_step, const int16_t* d_coefs, uint8_t* d_planes, long long max_blocks);
 // Upsample + YCbCr->RGB (jpeg/src/decode.rs:1404-1444). Writes interleaved 8-bit pixels to d_rgb (nullable)
@@ -266,6 +270,8 @@ int ssim2_grad_device(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, i
 // component layout (ncomp, hmax, vmax, comp[]).
 int plan_scans(rcg_ctx* ctx, const StepDesc* lay, int w, int h, const int16_t* d_coefs, rcg_plan_result* res);
 
+// Natural (row * 8 + column) index of zigzag position k (jpeg/src/lib.rs:14-19), host side.
+int zigzag_natural(int k);
 // Dequantization multiplier of one entry (jpeg/src/decode.rs:1316-1321), host side.
 float mult_entry_host(const uint8_t* q, int n);
 // Dequantization multipliers from caller-given tables (ntables 1 or 2; natural order).
@@ -282,6 +288,20 @@ int step_tables_requant(rcg_ctx* ctx, SearchState* d_search, StepDesc* d_step, i
                         long long slot_stride);
 // Device-side: fill the step tables from the quality the search state holds.
 int step_tables(rcg_ctx* ctx, SearchState* d_search, StepDesc* d_step, int w, int h, int16_t* d_coef_slots,
-                long long slot_stride);
+                long long slot_stride, const float* d_pweights = nullptr);
+
+// ---- perceptual trellis weights (perceptual.cu)
+struct PerceptualParams {
+  double strength, gamma, w_min, w_max;
+  int radius;
+};
+// d SSIMULACRA2 / d coefficient of a decoded candidate: the pixel gradient (f64, [h][w][3]) pulled back through the
+// YCbCr->RGB conversion, the chroma upsampling and the orthonormal 8x8 IDCT, per coefficient in the coefficient
+// layout (zigzag, dequantized units; d_coef_grad nullable), plus the perceptual weights (d_weights nullable) for the
+// layout of `lay` (ncomp, hmax, vmax, comp[].bw/bh/h/v/blk0).
+int perceptual_pullback(rcg_ctx* ctx, const double* d_grad, int w, int h, const StepDesc* lay,
+                        const PerceptualParams& p, double* d_coef_grad, float* d_weights);
+// 8-bit Gray/RGB -> 8-bit RGB (d_rgb8) and/or f32 RGB (d_rgbf); either output nullable.
+int expand_rgb(rcg_ctx* ctx, const uint8_t* d_src, int channels, size_t npx, uint8_t* d_rgb8, float* d_rgbf);
 
 }  // namespace rcg

@@ -680,7 +680,7 @@ static cudaError_t scorer_constants(int device) {
   cudaError_t e;
   if ((e = cudaMemcpyToSymbol(c_gauss, kf, sizeof kf)) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(c_lut8s, lut, sizeof lut)) != cudaSuccess) return e;
-  if ((e = cudaMemcpyToSymbol(c_weights, W, sizeof W)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_weights, W, sizeof c_weights)) != cudaSuccess) return e;
   if (int ce = codec_upload_lut(lut)) return (cudaError_t)ce;
   if ((e = cudaFuncSetAttribute(k_ssim2_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem)) !=
       cudaSuccess)

@@ -101,6 +101,41 @@ class _PlanResult(ctypes.Structure):
                 ("ndistinct", ctypes.c_int32), ("distinct", _Scan * 48), ("distinct_bytes", ctypes.c_uint64 * 48)]
 
 
+class _PerceptualOpts(ctypes.Structure):
+    _fields_ = [("strength", ctypes.c_double), ("gamma", ctypes.c_double), ("w_min", ctypes.c_double),
+                ("w_max", ctypes.c_double), ("radius", ctypes.c_int32), ("keep_smaller", ctypes.c_int32)]
+
+
+@dataclass
+class PerceptualOptions:
+    """Options of the perceptual trellis (rcg_perceptual_options): W[b][k] = strength * clamp((s_b / mean s)^gamma,
+    w_min, w_max) with s_b the RMS coefficient-gradient energy over the (2 radius + 1)^2 blocks around block b."""
+
+    strength: float = 0.35
+    gamma: float = 0.5
+    w_min: float = 0.25
+    w_max: float = 4.0
+    radius: int = 1
+    keep_smaller: bool = True
+
+    def _c(self):
+        return _PerceptualOpts(float(self.strength), float(self.gamma), float(self.w_min), float(self.w_max),
+                               int(self.radius), 1 if self.keep_smaller else 0)
+
+
+@dataclass
+class PerceptualFound:
+    """rcg_search_perceptual: the plain search's result, the returned result (the weighted search's, or the plain
+    one when it plans smaller and keep_smaller is set), both planned sizes and the weights."""
+
+    plain: "Found"
+    found: "Found"
+    plain_bytes: int
+    perceptual_bytes: int
+    chose_perceptual: bool
+    weights: np.ndarray
+
+
 @dataclass
 class Plan:
     """write_best's decision (jpeg/src/encode.rs:543-565): the estimated sizes, whether the progressive script wins,
@@ -235,6 +270,17 @@ def _load():
         "rcg_plan": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, sz, ctypes.POINTER(_PlanResult)]),
         "rcg_plan_device": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, ctypes.POINTER(_PlanResult)]),
         "rcg_search_batch": (i32, [P, i32, P, P, P, P, P, i32, ctypes.POINTER(_Opts), i32, P, P, P, P]),
+        "rcg_perceptual_defaults": (None, [ctypes.POINTER(_PerceptualOpts)]),
+        "rcg_coef_gradient": (i32, [P, P, P, u32, u32, i32, ctypes.POINTER(_Layout),
+                                    ctypes.POINTER(ctypes.c_double), P, sz]),
+        "rcg_perceptual_weights": (i32, [P, P, P, u32, u32, i32, ctypes.POINTER(_Layout),
+                                         ctypes.POINTER(_PerceptualOpts), ctypes.POINTER(ctypes.c_double), P, sz]),
+        "rcg_build_coefs_weighted": (i32, [P, P, u32, u32, i32, ctypes.POINTER(_Opts), P, sz, P, sz, P]),
+        "rcg_search_weighted": (i32, [P, P, u32, u32, i32, ctypes.c_double, i32, ctypes.POINTER(_Opts), P, sz,
+                                      ctypes.POINTER(_Found), P, sz, P]),
+        "rcg_search_perceptual": (i32, [P, P, u32, u32, i32, ctypes.c_double, i32, ctypes.POINTER(_Opts),
+                                        ctypes.POINTER(_PerceptualOpts), ctypes.POINTER(_Found),
+                                        ctypes.POINTER(_Found), P, ctypes.POINTER(ctypes.c_int), P, sz, P, P, sz]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -250,7 +296,8 @@ EXPORTED = (
     "rcg_ssimulacra2_device rcg_ssimulacra2_device_noalloc rcg_build_coefs rcg_reconstruct rcg_search rcg_search_device "
     "rcg_search_batch rcg_reconstruct_tables rcg_requantize rcg_search_requantize rcg_plan rcg_plan_device "
     "rcg_metric_score rcg_metric_score_device rcg_search_metric rcg_decode_coefs rcg_decode_coefs_device "
-    "rcg_search_requantize_device rcg_ssimulacra2_grad rcg_ssimulacra2_grad_device"
+    "rcg_search_requantize_device rcg_ssimulacra2_grad rcg_ssimulacra2_grad_device rcg_perceptual_defaults "
+    "rcg_coef_gradient rcg_perceptual_weights rcg_build_coefs_weighted rcg_search_weighted rcg_search_perceptual"
 ).split()
 
 
@@ -419,6 +466,91 @@ class Context:
         self._check(_lib.rcg_build_coefs(self._ptr, a.ctypes.data, w, h, c, ctypes.byref(o), coefs.ctypes.data,
                                          coefs.size, qt.ctypes.data))
         return _coef_image(w, h, lay, coefs, qt)
+
+    def build_coefs_weighted(self, src, opts, weights):
+        """build_coefs with the trellis pass in the perceptual mode (`weights`: f32, the layout's ncoefs entries)."""
+        a, w, h, c, d = _image(src)
+        if d != 8 or c not in (1, 3):
+            raise RcgError(RCG_INVALID, "build_coefs takes 8-bit Gray or Rgb")
+        lay = self.coef_layout(w, h, c, opts)
+        wt = np.ascontiguousarray(weights, dtype=np.float32)
+        coefs = np.zeros(lay.ncoefs, dtype=np.int16)
+        qt = np.zeros((2, 64), dtype=np.uint8)
+        o = _opts(opts)
+        self._check(_lib.rcg_build_coefs_weighted(self._ptr, a.ctypes.data, w, h, c, ctypes.byref(o),
+                                                  wt.ctypes.data, wt.size, coefs.ctypes.data, coefs.size,
+                                                  qt.ctypes.data))
+        return _coef_image(w, h, lay, coefs, qt)
+
+    def _pullback_args(self, reference, decoded, layout):
+        a, w, h, c, d = _image(reference)
+        b, w2, h2, c2, d2 = _image(decoded)
+        if (w, h, c, d) != (w2, h2, c2, d2) or d != 8:
+            raise RcgError(RCG_INVALID, "reference and decoded must be 8-bit images of the same shape")
+        return a, b, w, h, c
+
+    def coef_gradient(self, reference, decoded, layout):
+        """(score, d score / d coefficient) of a decoded image for the coefficient layout `layout` (_Layout):
+        float64, 64 zigzag entries per block, dequantized units."""
+        a, b, w, h, c = self._pullback_args(reference, decoded, layout)
+        out = np.zeros(layout.ncoefs, dtype=np.float64)
+        s = ctypes.c_double()
+        self._check(_lib.rcg_coef_gradient(self._ptr, a.ctypes.data, b.ctypes.data, w, h, c, ctypes.byref(layout),
+                                           ctypes.byref(s), out.ctypes.data, out.size))
+        return s.value, out
+
+    def perceptual_weights(self, reference, decoded, layout, popts=None):
+        """(score, perceptual trellis weights) from the gradient at `decoded` for the layout `layout`."""
+        popts = popts or PerceptualOptions()
+        a, b, w, h, c = self._pullback_args(reference, decoded, layout)
+        out = np.zeros(layout.ncoefs, dtype=np.float32)
+        s = ctypes.c_double()
+        po = popts._c()
+        self._check(_lib.rcg_perceptual_weights(self._ptr, a.ctypes.data, b.ctypes.data, w, h, c,
+                                                ctypes.byref(layout), ctypes.byref(po), ctypes.byref(s),
+                                                out.ctypes.data, out.size))
+        return s.value, out
+
+    def find_quality_weighted(self, reference, target, weights, max_quality=100, opts=None):
+        """The --target-ssimulacra2 search with every candidate's trellis in the perceptual mode."""
+        opts = opts or EncodeOptions()
+        a, w, h, c, d = _image(reference)
+        lay = self.coef_layout(w, h, c, EncodeOptions(50, opts.subsampling, opts.trellis))
+        wt = np.ascontiguousarray(weights, dtype=np.float32)
+        coefs = np.zeros(lay.ncoefs, dtype=np.int16)
+        qt = np.zeros((2, 64), dtype=np.uint8)
+        f = _Found()
+        o = _opts(opts)
+        self._check(_lib.rcg_search_weighted(self._ptr, a.ctypes.data, w, h, c, float(target), int(max_quality),
+                                             ctypes.byref(o), wt.ctypes.data, wt.size, ctypes.byref(f),
+                                             coefs.ctypes.data, coefs.size, qt.ctypes.data))
+        trace = [(int(f.trace_q[i]), float(f.trace_score[i])) for i in range(f.nsteps)]
+        return Found(int(f.quality), float(f.score), _coef_image(w, h, lay, coefs, qt), trace)
+
+    def find_quality_perceptual(self, reference, target, max_quality=100, opts=None, popts=None):
+        """rcg_search_perceptual: plain search, gradient at its result, weighted search, planned sizes of both."""
+        opts = opts or EncodeOptions()
+        popts = popts or PerceptualOptions()
+        a, w, h, c, d = _image(reference)
+        lay = self.coef_layout(w, h, c, EncodeOptions(50, opts.subsampling, opts.trellis))
+        coefs = np.zeros(lay.ncoefs, dtype=np.int16)
+        wts = np.zeros(lay.ncoefs, dtype=np.float32)
+        qt = np.zeros((2, 64), dtype=np.uint8)
+        fp, ff = _Found(), _Found()
+        sizes = (ctypes.c_uint64 * 2)()
+        chose = ctypes.c_int()
+        o, po = _opts(opts), popts._c()
+        self._check(_lib.rcg_search_perceptual(self._ptr, a.ctypes.data, w, h, c, float(target), int(max_quality),
+                                               ctypes.byref(o), ctypes.byref(po), ctypes.byref(fp),
+                                               ctypes.byref(ff), sizes, ctypes.byref(chose), coefs.ctypes.data,
+                                               coefs.size, qt.ctypes.data, wts.ctypes.data, wts.size))
+
+        def found(f, ci):
+            return Found(int(f.quality), float(f.score), ci,
+                         [(int(f.trace_q[i]), float(f.trace_score[i])) for i in range(f.nsteps)])
+
+        return PerceptualFound(found(fp, None), found(ff, _coef_image(w, h, lay, coefs, qt)), int(sizes[0]),
+                               int(sizes[1]), bool(chose.value), wts)
 
     def reconstruct(self, ci):
         """jpeg/src/decode.rs:334: the pixels a viewer would show (Gray (h, w) or Rgb (h, w, 3) uint8)."""

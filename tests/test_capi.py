@@ -59,3 +59,14 @@ def test_context_creation_fails_cleanly_without_a_device():
     out = ctypes.c_void_p()
     rc = rcg.lib().rcg_ctx_create(0, ctypes.byref(out))
     assert rc != 0 and not out.value
+
+
+def test_perceptual_defaults_match_the_python_options():
+    import rcg
+
+    _lib()
+    o = rcg._PerceptualOpts()
+    rcg.lib().rcg_perceptual_defaults(ctypes.byref(o))
+    d = rcg.PerceptualOptions()
+    assert (o.strength, o.gamma, o.w_min, o.w_max, o.radius, bool(o.keep_smaller)) == \
+        (d.strength, d.gamma, d.w_min, d.w_max, d.radius, d.keep_smaller)

@@ -542,3 +542,79 @@ def test_oracle_fp64_gradient_matches_central_differences(oracle):
         dm[y, x, c] -= step
         fd = (oracle.score64(r64, dp) - oracle.score64(r64, dm)) / (2 * step)
         assert abs(fd - g[y, x, c]) <= 1e-9 + 1e-4 * abs(fd), (y, x, c, fd, g[y, x, c])
+
+
+def test_oracle_weighted_trellis(oracle):
+    """The perceptual mode in the oracle's trellis: all-ones weights are the plain trellis bit for bit; larger
+    weights keep more (or equal) nonzero coefficients, smaller ones fewer; weights are validated against the
+    layout."""
+    import rcg.synth as synth
+
+    img = synth.image(120, 88, 6, sensor_sigma=3.0)
+    for sub in (1, 2, 3):
+        plain, qt, lay = oracle.build_coefs(img, 70, sub, True)
+        ones = np.ones(lay["ncoefs"], dtype=np.float32)
+        same, _, _ = oracle.build_coefs(img, 70, sub, True, weights=ones)
+        assert np.array_equal(same, plain)
+        heavy, _, _ = oracle.build_coefs(img, 70, sub, True, weights=ones * 16)
+        light, _, _ = oracle.build_coefs(img, 70, sub, True, weights=ones / 16)
+        nz = lambda c: int(np.count_nonzero(c))
+        assert nz(light) < nz(plain) < nz(heavy)
+    with pytest.raises(ValueError):
+        oracle.build_coefs(img, 70, 3, True, weights=np.ones(5, dtype=np.float32))
+    # the search with all-ones weights is the plain search
+    small = synth.image(64, 48, 7)
+    a = oracle.search(small, 70.0, 100, 3, True)
+    b = oracle.search(small, 70.0, 100, 3, True, weights=np.ones(oracle.layout(64, 48, 3, 50, 3)["ncoefs"],
+                                                                 dtype=np.float32))
+    assert a[0] == b[0] and a[5] == b[5] and np.array_equal(a[2], b[2])
+
+
+def test_oracle_pullback_is_the_adjoint_of_the_decoder(oracle):
+    """coef_gradient is the exact adjoint of decode_linear (<g, L f> == <L^T g, f>), and decode_linear is the
+    oracle decoder (jpeg/src/decode.rs:334) without its roundings: within the accumulated rounding of the IDCT,
+    upsampling and colour steps on real coefficients, for every sampling layout and Gray."""
+    import rcg.synth as synth
+
+    rng = np.random.default_rng(1)
+    for w, h, c, sub, q in ((97, 61, 3, 3, 80), (64, 40, 3, 1, 85), (45, 33, 3, 2, 75), (40, 24, 1, 3, 80)):
+        lay = oracle.layout(w, h, c, q, sub)
+        f = rng.standard_normal(lay["ncoefs"])
+        g = rng.standard_normal((h, w, 3))
+        lhs = (g * oracle.decode_linear(f, w, h, lay)).sum()
+        rhs = (oracle.coef_gradient(g, w, h, lay) * f).sum()
+        assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+        img = synth.image(max(w, 8), max(h, 8), 5)[:h, :w]
+        if c == 1:
+            img = img[:, :, 1].copy()
+        coefs, qt, lay = oracle.build_coefs(img, q, sub, True)
+        dec = oracle.reconstruct(w, h, lay, qt, coefs).astype(np.float64)
+        deq, off = np.zeros(lay["ncoefs"]), 0
+        for ci in range(lay["ncomp"]):
+            n = lay["blocks_w"][ci] * lay["blocks_h"][ci]
+            t = qt[0 if ci == 0 else 1][oracle.ZIGZAG].astype(np.float64)
+            deq[off * 64:(off + n) * 64] = (coefs[off * 64:(off + n) * 64].reshape(n, 64) * t).reshape(-1)
+            off += n
+        lin = oracle.decode_linear(deq, w, h, lay) + 128.0  # level shift (chroma's cancels in the colour step)
+        if c == 1:
+            lin = lin[:, :, 0]
+        err = np.abs(np.clip(lin, 0, 255) - dec)
+        assert err.max() <= (0.5 if c == 1 else 2.5) and err.mean() < 0.6, (w, h, sub, err.max())
+
+
+def test_oracle_perceptual_weights_rule(oracle):
+    """A uniform gradient gives every block the clamp of ratio 1 (weight = strength); a gradient in one block
+    raises that block and its neighbours (radius 1) and lowers the rest, within the clamp."""
+    lay = oracle.layout(64, 48, 1, 50, 3)
+    g = np.ones((48, 64, 3))
+    wts = oracle.perceptual_weights(g, 64, 48, lay, strength=0.5)
+    assert np.all(wts == np.float32(0.5))
+    g = np.zeros((48, 64, 3))
+    g[16:24, 24:32, :] = 1.0  # block (2, 3) of the 6 x 8 grid
+    wts = oracle.perceptual_weights(g, 64, 48, lay, strength=1.0, gamma=1.0, w_min=0.25, w_max=4.0, radius=1)
+    per_block = wts.reshape(6, 8, 64)[:, :, 0]
+    assert np.all(per_block[1:4, 2:5] == per_block[2, 3]) and per_block[2, 3] > 1.0
+    assert np.all(per_block[0] == np.float32(0.25))
+    assert np.all(wts.reshape(-1, 64) == wts.reshape(-1, 64)[:, :1])
+    # zero gradient everywhere: ratio 1 by definition
+    assert np.all(oracle.perceptual_weights(np.zeros((48, 64, 3)), 64, 48, lay, strength=2.0) == 2.0)
