@@ -33,6 +33,10 @@ constexpr double kM20 = 0.2434226892454782, kM21 = 0.2047674442449682, kM22 = 1.
 constexpr double kC2 = 0.0009;
 
 __constant__ double c_k64[2 * kR + 1];  // normalized Gaussian taps (sigma 1.5)
+// The curve and its derivative at the 256 integer samples, computed on the host with the same expressions (an
+// 8-bit reference, and decoded candidates passed as whole-number samples, skip the f64 pow).
+__constant__ double c_lin8[256];
+__constant__ double c_dlin8[256];
 
 __device__ __forceinline__ double srgb64(double v) {
   return v <= 0.04045 ? v / 12.92 : pow((v + 0.055) / 1.055, 2.4);
@@ -44,15 +48,25 @@ __device__ __forceinline__ double srgb64_deriv(double v255) {
 
 __device__ __forceinline__ long long tid1() { return (long long)blockIdx.x * blockDim.x + threadIdx.x; }
 
+// Index of a whole-number sample in [0, 255], else -1.
+__device__ __forceinline__ int sample8(float v) {
+  return (v >= 0.0f && v <= 255.0f && v == rintf(v)) ? (int)v : -1;
+}
+
 // Linear planes [3][n] of the reference (8-bit samples) and of the distorted image (f32 samples), by the curve.
 __global__ void k_lin64(const uint8_t* __restrict__ ref, const float* __restrict__ dist, long long n,
                         double* __restrict__ la, double* __restrict__ lb) {
+  __shared__ double lut[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = c_lin8[i];
+  __syncthreads();
   for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x)
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       // both images through the same curve: identical inputs give identical planes (and the score 100)
-      la[c * n + i] = srgb64((double)ref[i * 3 + c] / 255.0);
-      lb[c * n + i] = srgb64((double)dist[i * 3 + c] / 255.0);
+      la[c * n + i] = lut[ref[i * 3 + c]];
+      const float v = dist[i * 3 + c];
+      const int k = sample8(v);
+      lb[c * n + i] = k >= 0 ? lut[k] : srgb64((double)v / 255.0);
     }
 }
 
@@ -275,9 +289,16 @@ __global__ void k_xyb_adj64(const double* __restrict__ lin, const double* __rest
 // Through the sRGB curve to the samples (interleaved RGB).
 __global__ void k_grad_out64(const double* __restrict__ g_lin, const float* __restrict__ dist, long long n,
                              double* __restrict__ grad) {
+  __shared__ double dlut[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) dlut[i] = c_dlin8[i];
+  __syncthreads();
   for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x)
 #pragma unroll
-    for (int c = 0; c < 3; c++) grad[i * 3 + c] = g_lin[c * n + i] * srgb64_deriv((double)dist[i * 3 + c]);
+    for (int c = 0; c < 3; c++) {
+      const float v = dist[i * 3 + c];
+      const int k = sample8(v);
+      grad[i * 3 + c] = g_lin[c * n + i] * (k >= 0 ? dlut[k] : srgb64_deriv((double)v));
+    }
 }
 
 unsigned grid_of(long long n) {
@@ -297,6 +318,14 @@ int ssim2_grad_device(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, i
   }
   for (int i = 0; i <= 2 * kR; i++) k[i] /= sum;
   cudaMemcpyToSymbolAsync(c_k64, k, sizeof k, 0, cudaMemcpyHostToDevice, ctx->stream);
+  double lin8[256], dlin8[256];  // pageable sources: the uploads have read them when the calls return
+  for (int i = 0; i < 256; i++) {
+    const double v = (double)i / 255.0;
+    lin8[i] = v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4);
+    dlin8[i] = v <= 0.04045 ? 1.0 / (12.92 * 255.0) : 2.4 * std::pow((v + 0.055) / 1.055, 1.4) / (1.055 * 255.0);
+  }
+  cudaMemcpyToSymbolAsync(c_lin8, lin8, sizeof lin8, 0, cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyToSymbolAsync(c_dlin8, dlin8, sizeof dlin8, 0, cudaMemcpyHostToDevice, ctx->stream);
   // pyramid of both images (linear, f64)
   struct Sc {
     int w, h;

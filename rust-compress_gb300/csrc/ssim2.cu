@@ -110,22 +110,26 @@ __device__ __forceinline__ int mirror_row(int yy, int h) {
   return yy;
 }
 
-// Row pitch 45 (>= 42): 8 horizontal-pass items per row read at a stride of 4 words, and 45 = 13 mod 32 puts the
-// four rows a warp covers in distinct bank classes, so those reads are conflict-free.
+// Row pitch 45 pairs (>= 42 columns): a horizontal-pass item reads 8-byte (a', d') pairs at a stride of 4 pairs,
+// and 2 * 45 = 26 mod 32 shifts each of the 4 rows a half-warp covers to its own bank class, so its 16 loads hit
+// 32 distinct banks.
 constexpr int kIW = 45;
 constexpr int kIH = kTileH + 2 * kRadius;  // 42
 constexpr int kHx = 4;                     // horizontal-pass outputs per item
+constexpr int kIHp = (kIH + 3) / 4 * 4;    // rows rounded up to the 4-row item groups
 constexpr size_t kTileSmem = (size_t)(6 * kIH * kIW + 5 * kIH * kTileW) * sizeof(float);
 
-// One CTA = one 32x32 output tile of one scale. Shared memory: XYB (offset) of both images for the tile plus its
-// 5-pixel halo, 3 channels each; then per channel the horizontally blurred five moments of the 42 halo rows.
+// One CTA = one 32x32 output tile of one scale. Shared memory: per channel the (a', d') pairs of the tile plus its
+// 5-pixel halo; then per channel the horizontally blurred five moments of the 42 halo rows. The blurs run the
+// moment pairs that share a tap weight ((a', d'), (a'^2, b'^2)) as packed two-lane f32 FMAs, each lane exactly
+// fmaf, so the results are those of scalar FMAs in the same order.
 __global__ void __launch_bounds__(kTileThreads, 3)
     k_ssim2_tiles(PyramidDesc pd, const float* __restrict__ ref, const float* __restrict__ dist,
                   double* __restrict__ partials, const StepDesc* __restrict__ st) {
   if (st && !st->active) return;
   extern __shared__ float smem[];
-  float* xs = smem;                      // [6][kIH][kIW]: ref X,Y,B then dist X,Y,B
-  float* hb = smem + 6 * kIH * kIW;      // [5][kIH][kTileW]
+  float2* xs = reinterpret_cast<float2*>(smem);  // [3][kIH][kIW] pairs (a', d') per channel
+  float* hb = smem + 6 * kIH * kIW;              // pair planes (m0, m1), (m2, m3) then m4, [kIH][kTileW] each
   __shared__ float s_red[kTileThreads / 32][kScoreSums];
 
   int blk = blockIdx.x;
@@ -191,7 +195,7 @@ __global__ void __launch_bounds__(kTileThreads, 3)
     }
     const int r = e / kCols, idx = r * kIW + (e - r * kCols);
 #pragma unroll
-    for (int k = 0; k < 6; k++) xs[k * kIH * kIW + idx] = v[k];
+    for (int k = 0; k < 3; k++) xs[k * kIH * kIW + idx] = make_float2(v[k], v[3 + k]);
 #pragma unroll
     for (int k = 0; k < 6; k++) cur[k] = nxt[k];
     cur_ok = nxt_ok;
@@ -218,58 +222,87 @@ __global__ void __launch_bounds__(kTileThreads, 3)
 #pragma unroll 1
   for (int ch = 0; ch < 3; ch++) {
     __syncthreads();  // xs complete (ch 0) / previous channel's vertical pass done with hb
-    const float* A = xs + ch * kIH * kIW;
-    const float* D = xs + (3 + ch) * kIH * kIW;
-    // Horizontal pass: kHx adjacent outputs per item; moments a', d', a'^2, b'^2 (b' = a' - d'), d'^2.
-    for (int item = tid; item < kIH * (kTileW / kHx); item += kTileThreads) {
-      int r = item / (kTileW / kHx), p = item - r * (kTileW / kHx);
-      const float* ar = A + r * kIW + kHx * p;
-      const float* dr = D + r * kIW + kHx * p;
-      float va[kHx + 2 * kRadius], vd[kHx + 2 * kRadius], vaa[kHx + 2 * kRadius], vbb[kHx + 2 * kRadius],
-          vdd[kHx + 2 * kRadius];
+    const float2* X = xs + ch * kIH * kIW;
+    // Horizontal pass: kHx adjacent outputs per item; moments a', d', a'^2, b'^2 (b' = a' - d'), d'^2. The pairs
+    // (a', d') and (a'^2, b'^2) share every tap weight and run as packed two-lane FMAs (per lane exactly fmaf).
+    // Items: each half-warp takes 4 rows x 4 items, so its 64-bit loads (row pitch 45 pairs = 26 banks mod 32)
+    // fall in distinct banks.
+    for (int item = tid; item < kIHp * (kTileW / kHx); item += kTileThreads) {
+      const int hw = item >> 4, j = item & 15;
+      const int r = (hw >> 1) * 4 + (j >> 2), p = (j & 3) + 4 * (hw & 1);
+      if (r >= kIH) continue;
+      const float2* xr = X + r * kIW + kHx * p;
+      float2 vad[kHx + 2 * kRadius], vsq[kHx + 2 * kRadius];
+      float vdd[kHx + 2 * kRadius];
 #pragma unroll
       for (int t = 0; t < kHx + 2 * kRadius; t++) {
-        float a = ar[t], d = dr[t], b = a - d;
-        va[t] = a;
-        vd[t] = d;
-        vaa[t] = a * a;
-        vbb[t] = b * b;
-        vdd[t] = d * d;
+        const float2 ad = xr[t];
+        const float2 ab = make_float2(ad.x, ad.x - ad.y);
+        vad[t] = ad;
+        vsq[t] = __fmul2_rn(ab, ab);
+        vdd[t] = ad.y * ad.y;
       }
-      float m[5][kHx];
+      float2 m01[kHx], m23[kHx];
+      float m4[kHx];
 #pragma unroll
       for (int o = 0; o < kHx; o++) {
-        float s1 = 0.f, sd = 0.f, s11 = 0.f, s22 = 0.f, sdd = 0.f;
+        float2 s01 = make_float2(0.f, 0.f), s23 = make_float2(0.f, 0.f);
+        float sdd = 0.f;
 #pragma unroll
         for (int t = 0; t < 2 * kRadius + 1; t++) {
           float k = c_gauss[t];
-          s1 = fmaf(k, va[o + t], s1);
-          sd = fmaf(k, vd[o + t], sd);
-          s11 = fmaf(k, vaa[o + t], s11);
-          s22 = fmaf(k, vbb[o + t], s22);
+          float2 kk = make_float2(k, k);
+          s01 = __ffma2_rn(kk, vad[o + t], s01);
+          s23 = __ffma2_rn(kk, vsq[o + t], s23);
           sdd = fmaf(k, vdd[o + t], sdd);
         }
-        m[0][o] = s1; m[1][o] = sd; m[2][o] = s11; m[3][o] = s22; m[4][o] = sdd;
+        m01[o] = s01;
+        m23[o] = s23;
+        m4[o] = sdd;
       }
-#pragma unroll
-      for (int q = 0; q < 5; q++)
-        *reinterpret_cast<float4*>(hb + (q * kIH + r) * kTileW + kHx * p) = make_float4(m[q][0], m[q][1], m[q][2],
-                                                                                        m[q][3]);
+      // hb: two planes of (moment 0, moment 1) and (moment 2, moment 3) pairs, then moment 4
+      float* h01 = hb + (r * kTileW + kHx * p) * 2;
+      float* h23 = hb + (kIH * kTileW + r * kTileW + kHx * p) * 2;
+      float* h4 = hb + 4 * kIH * kTileW + r * kTileW + kHx * p;
+      reinterpret_cast<float4*>(h01)[0] = make_float4(m01[0].x, m01[0].y, m01[1].x, m01[1].y);
+      reinterpret_cast<float4*>(h01)[1] = make_float4(m01[2].x, m01[2].y, m01[3].x, m01[3].y);
+      reinterpret_cast<float4*>(h23)[0] = make_float4(m23[0].x, m23[0].y, m23[1].x, m23[1].y);
+      reinterpret_cast<float4*>(h23)[1] = make_float4(m23[2].x, m23[2].y, m23[3].x, m23[3].y);
+      *reinterpret_cast<float4*>(h4) = make_float4(m4[0], m4[1], m4[2], m4[3]);
     }
     __syncthreads();
-    // Vertical pass + error maps: 4 output rows of one column per thread.
+    // Vertical pass + error maps: 4 output rows of one column per thread, the same pairs packed.
     float mu[5][4];
+    {
+      const float2* h01 = reinterpret_cast<const float2*>(hb);
+      const float2* h23 = reinterpret_cast<const float2*>(hb) + kIH * kTileW;
+      const float* h4 = hb + 4 * kIH * kTileW;
+      float2 v01[4 + 2 * kRadius], v23[4 + 2 * kRadius];
+      float v4[4 + 2 * kRadius];
 #pragma unroll
-    for (int q = 0; q < 5; q++) {
-      float v[4 + 2 * kRadius];
-#pragma unroll
-      for (int t = 0; t < 4 + 2 * kRadius; t++) v[t] = hb[(q * kIH + rg * 4 + t) * kTileW + col];
+      for (int t = 0; t < 4 + 2 * kRadius; t++) {
+        const int i = (rg * 4 + t) * kTileW + col;
+        v01[t] = h01[i];
+        v23[t] = h23[i];
+        v4[t] = h4[i];
+      }
 #pragma unroll
       for (int o = 0; o < 4; o++) {
-        float acc = 0.f;
+        float2 a01 = make_float2(0.f, 0.f), a23 = make_float2(0.f, 0.f);
+        float a4 = 0.f;
 #pragma unroll
-        for (int t = 0; t < 2 * kRadius + 1; t++) acc = fmaf(c_gauss[t], v[o + t], acc);
-        mu[q][o] = acc;
+        for (int t = 0; t < 2 * kRadius + 1; t++) {
+          float k = c_gauss[t];
+          float2 kk = make_float2(k, k);
+          a01 = __ffma2_rn(kk, v01[o + t], a01);
+          a23 = __ffma2_rn(kk, v23[o + t], a23);
+          a4 = fmaf(k, v4[o + t], a4);
+        }
+        mu[0][o] = a01.x;
+        mu[1][o] = a01.y;
+        mu[2][o] = a23.x;
+        mu[3][o] = a23.y;
+        mu[4][o] = a4;
       }
     }
     const float ca = oa[ch], cd = od[ch], cbv = ca - cd;
@@ -298,8 +331,8 @@ __global__ void __launch_bounds__(kTileThreads, 3)
         float num_s = den - vd;
         float d = fmaxf(__fdividef(fmaf(dmu * dmu, num_s, vd), den), 0.0f);
         // Edge maps (:431-433): d1 = (|r2| - |r1|) / (1 + |r1|) with r1 = a - mu1, r2 = b - mu2 = r1 - rd.
-        float a0 = A[(ry + kRadius) * kIW + col + kRadius];
-        float d0 = D[(ry + kRadius) * kIW + col + kRadius];
+        const float2 c0 = X[(ry + kRadius) * kIW + col + kRadius];
+        float a0 = c0.x, d0 = c0.y;
         float r1 = a0 - m1, rd = d0 - dmp;
         if (edge) {
           r1 = fmaf(ca, omk, r1);
