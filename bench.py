@@ -454,6 +454,9 @@ def kernel_case(name):
     if name == "plan":
         for _ in range(2):
             ctx.plan(ci)
+    elif name == "perceptual":
+        # one perceptual search (plain search, FP64 adjoint, pullback, weighted search, two plans)
+        ctx.find_quality_perceptual(img, TARGET, 100, rcg.EncodeOptions(90, rcg.Subsampling.S420, True))
     else:
         dist = ctx.reconstruct(ci)
         for _ in range(2):
@@ -472,7 +475,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the many-image batch measurement")
     ap.add_argument("--no-requant", action="store_true", help="skip the JPEG->JPEG search measurement")
     ap.add_argument("--no-perceptual", action="store_true", help="skip the perceptual trellis measurement")
-    ap.add_argument("--kernel-case", choices=["plan", "ssim", "ssim2"], default=None,
+    ap.add_argument("--kernel-case", choices=["plan", "ssim", "ssim2", "perceptual"], default=None,
                     help="profiling aid: run only a few calls of one workload at --width x --height, print nothing")
     ap.add_argument("--width", type=int, default=W, help="smaller cases for profiling only; the bench line uses 4000")
     ap.add_argument("--height", type=int, default=H)

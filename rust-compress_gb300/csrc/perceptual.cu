@@ -120,6 +120,10 @@ __global__ void __launch_bounds__(256) k_coef_grad(const double* __restrict__ g,
   for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
   if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = e;
   __syncthreads();
+  if (!coef_grad) {  // the weights need the energy alone (Parseval)
+    if (live && t == 0) energy[gb] = wsum[2 * grp] + wsum[2 * grp + 1];
+    return;
+  }
   // rows: tmp[y][u] = sum_x g[y][x] C[u][x]
   double r = 0.0;
 #pragma unroll
@@ -131,7 +135,7 @@ __global__ void __launch_bounds__(256) k_coef_grad(const double* __restrict__ g,
   double G = 0.0;
 #pragma unroll
   for (int y = 0; y < 8; y++) G += c_dct[ty * 8 + y] * tmp[grp][y * 8 + tx];
-  if (coef_grad) coef_grad[gb * 64 + c_izz[t]] = G;
+  coef_grad[gb * 64 + c_izz[t]] = G;
   if (t == 0) energy[gb] = wsum[2 * grp] + wsum[2 * grp + 1];
 }
 
@@ -172,17 +176,28 @@ __global__ void __launch_bounds__(1024) k_component_mean(PullDesc d, const doubl
   if (threadIdx.x == 0) mean[blockIdx.x] = part[0] / (double)nb;
 }
 
-// W[b][k] for all 64 k of a block: 16 threads per block, one float4 each.
+// W[b][k] for all 64 k of a block. One warp per 32 blocks: each lane evaluates its block's weight once, then the
+// warp writes the 32 blocks' 2048 floats as coalesced float4 rows (each value taken from its block's lane).
 __global__ void k_weights(PullDesc d, const double* __restrict__ sens, const double* __restrict__ mean,
                           PerceptualParams p, float* __restrict__ weights) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long gb = idx >> 4;
-  if (gb >= d.nblocks) return;
-  const double m = mean[comp_of_block(d, gb)];
-  const double r = m > 0.0 ? sens[gb] / m : 1.0;  // an all-zero gradient leaves every weight at clamp(1)
-  const double v = fmin(fmax(pow(r, p.gamma), p.w_min), p.w_max) * p.strength;
-  const float f = (float)v;
-  reinterpret_cast<float4*>(weights)[idx] = make_float4(f, f, f, f);
+  const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5 << 5;  // first block of the warp
+  const int lane = threadIdx.x & 31;
+  if (warp0 >= d.nblocks) return;
+  const long long gb = warp0 + lane;
+  float f = 0.0f;
+  if (gb < d.nblocks) {
+    const double m = mean[comp_of_block(d, gb)];
+    const double r = m > 0.0 ? sens[gb] / m : 1.0;  // an all-zero gradient leaves every weight at clamp(1)
+    f = (float)(fmin(fmax(pow(r, p.gamma), p.w_min), p.w_max) * p.strength);
+  }
+  float4* out = reinterpret_cast<float4*>(weights) + warp0 * 16;
+  const long long n4 = (d.nblocks - warp0) * 16;  // float4 entries left from this warp's first block
+#pragma unroll 4
+  for (int j = 0; j < 16; j++) {
+    const int q = j * 32 + lane;  // float4 index within the warp's 32 blocks
+    const float v = __shfl_sync(0xffffffffu, f, q >> 4);
+    if (q < n4) out[q] = make_float4(v, v, v, v);
+  }
 }
 
 // 8-bit Gray or RGB -> 8-bit RGB and/or f32 RGB (Gray replicated, as the scorer does: core/src/ssimulacra2.rs:192-203).
@@ -265,7 +280,7 @@ int perceptual_pullback(rcg_ctx* ctx, const double* d_grad, int w, int h, const 
   RCG_LAUNCH(ctx, "block_sensitivity", k_block_sensitivity, (unsigned)((nb + 255) / 256), 256, 0, d, energy,
              p.radius, sens);
   RCG_LAUNCH(ctx, "component_mean", k_component_mean, d.ncomp, 1024, 0, d, sens, mean);
-  RCG_LAUNCH(ctx, "weights", k_weights, (unsigned)((nb * 16 + 255) / 256), 256, 0, d, sens, mean, p, d_weights);
+  RCG_LAUNCH(ctx, "weights", k_weights, (unsigned)((nb + 255) / 256), 256, 0, d, sens, mean, p, d_weights);
   return RCG_OK;
 }
 
