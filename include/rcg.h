@@ -279,9 +279,10 @@ typedef struct {
   double w_max;
   int32_t radius;  /* sensitivity = RMS of the gradient energy over (2 radius + 1)^2 neighbouring blocks */
   int32_t keep_smaller; /* rcg_search_perceptual: return the plain result when its planned size is smaller */
+  int32_t gradient_fp64; /* 1: the weights come from the FP64 adjoint; 0: from the same pass in FP32 (faster) */
 } rcg_perceptual_options;
 
-/* The defaults: strength 0.35, gamma 0.5, w_min 0.25, w_max 4, radius 1, keep_smaller 1. */
+/* The defaults: strength 0.35, gamma 0.5, w_min 0.25, w_max 4, radius 1, keep_smaller 1, gradient_fp64 0. */
 void rcg_perceptual_defaults(rcg_perceptual_options* opts);
 
 /* d SSIMULACRA2(reference, decoded) / d coefficient for the coefficient layout `layout` (64 zigzag entries per block,

@@ -1,5 +1,5 @@
 // Reverse-mode derivative of SSIMULACRA2 (core/src/ssimulacra2.rs:171-512) with respect to the distorted image's
-// RGB samples, taken as continuous values in [0, 255], in FP64 on the GPU.
+// RGB samples, taken as continuous values in [0, 255], on the GPU.
 //
 // Forward: linear light by the sRGB curve itself (:172-175; the reference's 8-bit table samples it), the 2x2
 // pyramid, and per scale the XYB planes, the five blurred moments per channel and the six map sums. Backward, from
@@ -8,8 +8,11 @@
 // kinks); through the blurs (the zero-padded row blur is its own transpose, the mirrored column blur scatters
 // back); through XYB to linear light; plus the coarser scales' gradients spread back over their 2x2 blocks; and
 // finally through the sRGB curve. The blur intermediates are recomputed per scale in the backward pass, not kept
-// from the forward one. Plane kernels, one thread per sample, f64 throughout: this runs once per search, not per
-// candidate, so it trades speed for an exact match with the FP64 CPU gradient.
+// from the forward one. Plane kernels, one thread per sample, templated on the real type: FP64 (the checked
+// gradient: it matches the FP64 CPU gradient to rounding) and FP32 (the perceptual weights, where a few significant
+// digits suffice: the variances' cancellation error, ~1e-8, is small against the SSIM constant 9e-4 that bounds
+// every denominator, and GB300's FP32 rate is many times its FP64 rate). Sums of the maps are f64 across threads in
+// both; the final mapping runs on the host in f64.
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -32,11 +35,19 @@ constexpr double kM10 = 0.23, kM12 = 0.078, kM11 = 1.0 - kM12 - kM10;
 constexpr double kM20 = 0.2434226892454782, kM21 = 0.2047674442449682, kM22 = 1.0 - kM20 - kM21;
 constexpr double kC2 = 0.0009;
 
-__constant__ double c_k64[2 * kR + 1];  // normalized Gaussian taps (sigma 1.5)
+// normalized Gaussian taps (sigma 1.5) in both types
+__constant__ double c_k64[2 * kR + 1];
+__constant__ float c_k32[2 * kR + 1];
 // The curve and its derivative at the 256 integer samples, computed on the host with the same expressions (an
-// 8-bit reference, and decoded candidates passed as whole-number samples, skip the f64 pow).
+// 8-bit reference, and decoded candidates passed as whole-number samples, skip the pow).
 __constant__ double c_lin8[256];
 __constant__ double c_dlin8[256];
+
+template <typename T> __device__ __forceinline__ T tap(int t);
+template <> __device__ __forceinline__ double tap<double>(int t) { return c_k64[t]; }
+template <> __device__ __forceinline__ float tap<float>(int t) { return c_k32[t]; }
+__device__ __forceinline__ double cbrt_t(double x) { return cbrt(x); }
+__device__ __forceinline__ float cbrt_t(float x) { return cbrtf(x); }
 
 __device__ __forceinline__ double srgb64(double v) {
   return v <= 0.04045 ? v / 12.92 : pow((v + 0.055) / 1.055, 2.4);
@@ -54,10 +65,11 @@ __device__ __forceinline__ int sample8(float v) {
 }
 
 // Linear planes [3][n] of the reference (8-bit samples) and of the distorted image (f32 samples), by the curve.
-__global__ void k_lin64(const uint8_t* __restrict__ ref, const float* __restrict__ dist, long long n,
-                        double* __restrict__ la, double* __restrict__ lb) {
-  __shared__ double lut[256];
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = c_lin8[i];
+template <typename T>
+__global__ void k_lin(const uint8_t* __restrict__ ref, const float* __restrict__ dist, long long n,
+                      T* __restrict__ la, T* __restrict__ lb) {
+  __shared__ T lut[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = (T)c_lin8[i];
   __syncthreads();
   for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x)
 #pragma unroll
@@ -66,55 +78,60 @@ __global__ void k_lin64(const uint8_t* __restrict__ ref, const float* __restrict
       la[c * n + i] = lut[ref[i * 3 + c]];
       const float v = dist[i * 3 + c];
       const int k = sample8(v);
-      lb[c * n + i] = k >= 0 ? lut[k] : srgb64((double)v / 255.0);
+      lb[c * n + i] = k >= 0 ? lut[k] : (T)srgb64((double)v / 255.0);
     }
 }
 
 // 2x2 means (:225-247), fewer samples at odd edges; 3 channels.
-__global__ void k_down64(const double* __restrict__ src, int w, int h, double* __restrict__ dst, int ow, int oh) {
+template <typename T>
+__global__ void k_down(const T* __restrict__ src, int w, int h, T* __restrict__ dst, int ow, int oh) {
   const long long n = (long long)ow * oh;
   for (long long i = tid1(); i < 3 * n; i += (long long)gridDim.x * blockDim.x) {
     const int c = (int)(i / n);
     const long long o = i - c * n;
     const int oy = (int)(o / ow), ox = (int)(o % ow);
     const int x1 = min(2 * ox + 2, w), y1 = min(2 * oy + 2, h);
-    const double* p = src + (long long)c * w * h;
-    double s = 0.0;
+    const T* p = src + (long long)c * w * h;
+    T s = 0;
     for (int y = 2 * oy; y < y1; y++)
       for (int x = 2 * ox; x < x1; x++) s += p[(long long)y * w + x];
-    dst[i] = s / (double)((y1 - 2 * oy) * (x1 - 2 * ox));
+    dst[i] = s / (T)((y1 - 2 * oy) * (x1 - 2 * ox));
   }
 }
 
 // XYB (:249-258) of 3 linear planes.
-__global__ void k_xyb64(const double* __restrict__ lin, long long n, double* __restrict__ xyb) {
-  const double cb = cbrt(kBiasD);
+template <typename T>
+__global__ void k_xyb(const T* __restrict__ lin, long long n, T* __restrict__ xyb) {
+  const T M00 = (T)kM00, M01 = (T)kM01, M02 = (T)kM02, M10 = (T)kM10, M11 = (T)kM11, M12 = (T)kM12;
+  const T M20 = (T)kM20, M21 = (T)kM21, M22 = (T)kM22, bias = (T)kBiasD;
+  const T cb = cbrt_t(bias);
   for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
-    const double r = lin[i], g = lin[n + i], b = lin[2 * n + i];
-    const double m0 = cbrt(fmax(kM00 * r + kM01 * g + kM02 * b + kBiasD, 0.0)) - cb;
-    const double m1 = cbrt(fmax(kM10 * r + kM11 * g + kM12 * b + kBiasD, 0.0)) - cb;
-    const double m2 = cbrt(fmax(kM20 * r + kM21 * g + kM22 * b + kBiasD, 0.0)) - cb;
-    const double x = 0.5 * (m0 - m1), y = 0.5 * (m0 + m1);
-    xyb[i] = x * 14.0 + 0.42;
-    xyb[n + i] = y + 0.01;
-    xyb[2 * n + i] = (m2 - y) + 0.55;
+    const T r = lin[i], g = lin[n + i], b = lin[2 * n + i];
+    const T m0 = cbrt_t(fmax(M00 * r + M01 * g + M02 * b + bias, (T)0)) - cb;
+    const T m1 = cbrt_t(fmax(M10 * r + M11 * g + M12 * b + bias, (T)0)) - cb;
+    const T m2 = cbrt_t(fmax(M20 * r + M21 * g + M22 * b + bias, (T)0)) - cb;
+    const T x = (T)0.5 * (m0 - m1), y = (T)0.5 * (m0 + m1);
+    xyb[i] = x * (T)14.0 + (T)0.42;
+    xyb[n + i] = y + (T)0.01;
+    xyb[2 * n + i] = (m2 - y) + (T)0.55;
   }
 }
 
 // Row blur (zero outside) of the product `q` of one channel's XYB planes: 0 xa, 1 xb, 2 xa^2, 3 xb^2, 4 xa xb;
 // q = -1 blurs `src` itself (the adjoint's rows).
-__global__ void k_hblur64(const double* __restrict__ xa, const double* __restrict__ xb, const double* __restrict__ src,
-                          int q, int w, int h, double* __restrict__ dst) {
+template <typename T>
+__global__ void k_hblur(const T* __restrict__ xa, const T* __restrict__ xb, const T* __restrict__ src, int q, int w,
+                        int h, T* __restrict__ dst) {
   const long long n = (long long)w * h;
   for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
     const int y = (int)(i / w), x = (int)(i % w);
-    double s = 0.0;
+    T s = 0;
 #pragma unroll
     for (int t = 0; t <= 2 * kR; t++) {
       const int xx = x + t - kR;
       if (xx < 0 || xx >= w) continue;
       const long long j = (long long)y * w + xx;
-      double v;
+      T v;
       if (q < 0)
         v = src[j];
       else if (q == 0)
@@ -127,7 +144,7 @@ __global__ void k_hblur64(const double* __restrict__ xa, const double* __restric
         v = xb[j] * xb[j];
       else
         v = xa[j] * xb[j];
-      s += c_k64[t] * v;
+      s += tap<T>(t) * v;
     }
     dst[i] = s;
   }
@@ -136,49 +153,53 @@ __global__ void k_hblur64(const double* __restrict__ xa, const double* __restric
 __device__ __forceinline__ int mirror64(int yy, int h) { return yy < 0 ? -yy - 1 : (yy >= h ? 2 * h - 1 - yy : yy); }
 
 // Column blur with mirrored rows (:385-397).
-__global__ void k_vblur64(const double* __restrict__ src, int w, int h, double* __restrict__ dst) {
+template <typename T>
+__global__ void k_vblur(const T* __restrict__ src, int w, int h, T* __restrict__ dst) {
   const long long n = (long long)w * h;
   for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
     const int y = (int)(i / w), x = (int)(i % w);
-    double s = 0.0;
+    T s = 0;
 #pragma unroll
-    for (int t = 0; t <= 2 * kR; t++) s += c_k64[t] * src[(long long)mirror64(y + t - kR, h) * w + x];
+    for (int t = 0; t <= 2 * kR; t++) s += tap<T>(t) * src[(long long)mirror64(y + t - kR, h) * w + x];
     dst[i] = s;
   }
 }
 
-// Transpose of k_vblur64 as a gather: row y' receives tap t from the rows y whose mirrored source row is y', i.e.
+// Transpose of k_vblur as a gather: row y' receives tap t from the rows y whose mirrored source row is y', i.e.
 // from source index y' (y = y' - t + R), -y' - 1 (mirrored at the top) and 2h - 1 - y' (at the bottom).
-__global__ void k_vblur64_t(const double* __restrict__ g, int w, int h, double* __restrict__ dst) {
+template <typename T>
+__global__ void k_vblur_t(const T* __restrict__ g, int w, int h, T* __restrict__ dst) {
   const long long n = (long long)w * h;
   for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
     const int yp = (int)(i / w), x = (int)(i % w);
-    double s = 0.0;
+    T s = 0;
 #pragma unroll
     for (int t = 0; t <= 2 * kR; t++) {
       const int ys[3] = {yp - t + kR, -yp - 1 - t + kR, 2 * h - 1 - yp - t + kR};
 #pragma unroll
       for (int e = 0; e < 3; e++)
-        if (ys[e] >= 0 && ys[e] < h) s += c_k64[t] * g[(long long)ys[e] * w + x];
+        if (ys[e] >= 0 && ys[e] < h) s += tap<T>(t) * g[(long long)ys[e] * w + x];
     }
     dst[i] = s;
   }
 }
 
-// The six map sums of one channel (:421-440): per-CTA partial sums (parts[block][6]); k_sum_parts adds them in a
-// fixed order, so the score and the gradient are the same bits on every run.
-__global__ void __launch_bounds__(256) k_maps64(const double* __restrict__ mom, const double* __restrict__ xa,
-                                                const double* __restrict__ xb, long long n, double* __restrict__ parts) {
+// The six map sums of one channel (:421-440): per-thread sums in T, then f64 per-CTA partials (parts[block][6]);
+// k_sum_parts adds them in a fixed order, so the score and the gradient are the same bits on every run.
+template <typename T>
+__global__ void __launch_bounds__(256) k_maps(const T* __restrict__ mom, const T* __restrict__ xa,
+                                              const T* __restrict__ xb, long long n, double* __restrict__ parts) {
   __shared__ double red[6][8];
-  double acc[6] = {0, 0, 0, 0, 0, 0};
+  const T one = 1, c2 = (T)kC2;
+  T acc[6] = {0, 0, 0, 0, 0, 0};
   for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
-    const double m1 = mom[i], m2 = mom[n + i], s11 = mom[2 * n + i], s22 = mom[3 * n + i], s12 = mom[4 * n + i];
-    const double num_m = 1.0 - (m1 - m2) * (m1 - m2);
-    const double num_s = 2.0 * (s12 - m1 * m2) + kC2;
-    const double den_s = (s11 - m1 * m1) + (s22 - m2 * m2) + kC2;
-    const double d = fmax(1.0 - num_m * num_s / den_s, 0.0);
-    const double d1 = (1.0 + fabs(xb[i] - m2)) / (1.0 + fabs(xa[i] - m1)) - 1.0;
-    const double art = fmax(d1, 0.0), det = fmax(-d1, 0.0);
+    const T m1 = mom[i], m2 = mom[n + i], s11 = mom[2 * n + i], s22 = mom[3 * n + i], s12 = mom[4 * n + i];
+    const T num_m = one - (m1 - m2) * (m1 - m2);
+    const T num_s = (T)2 * (s12 - m1 * m2) + c2;
+    const T den_s = (s11 - m1 * m1) + (s22 - m2 * m2) + c2;
+    const T d = fmax(one - num_m * num_s / den_s, (T)0);
+    const T d1 = (one + fabs(xb[i] - m2)) / (one + fabs(xa[i] - m1)) - one;
+    const T art = fmax(d1, (T)0), det = fmax(-d1, (T)0);
     acc[0] += d;
     acc[1] += (d * d) * (d * d);
     acc[2] += art;
@@ -188,7 +209,7 @@ __global__ void __launch_bounds__(256) k_maps64(const double* __restrict__ mom, 
   }
 #pragma unroll
   for (int k = 0; k < 6; k++) {
-    double v = acc[k];
+    double v = (double)acc[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
@@ -219,30 +240,38 @@ struct NormCoef {
   double g1[3], g4[3];
 };
 
-__global__ void k_mapgrad64(const double* __restrict__ mom, const double* __restrict__ xa,
-                            const double* __restrict__ xb, long long n, NormCoef nc, double* __restrict__ g_m2,
-                            double* __restrict__ g_s22, double* __restrict__ g_s12, double* __restrict__ g_xb) {
+template <typename T>
+__global__ void k_mapgrad(const T* __restrict__ mom, const T* __restrict__ xa, const T* __restrict__ xb, long long n,
+                          NormCoef ncd, T* __restrict__ g_m2, T* __restrict__ g_s22, T* __restrict__ g_s12,
+                          T* __restrict__ g_xb) {
+  const T one = 1, two = 2, zero = 0, c2 = (T)kC2;
+  T g1[3], g4[3];
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    g1[m] = (T)ncd.g1[m];
+    g4[m] = (T)ncd.g4[m];
+  }
   for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
-    const double m1 = mom[i], m2 = mom[n + i], s11 = mom[2 * n + i], s22 = mom[3 * n + i], s12 = mom[4 * n + i];
-    const double num_m = 1.0 - (m1 - m2) * (m1 - m2);
-    const double num_s = 2.0 * (s12 - m1 * m2) + kC2;
-    const double den_s = (s11 - m1 * m1) + (s22 - m2 * m2) + kC2;
-    const double dv = 1.0 - num_m * num_s / den_s;
-    double gm2 = 0.0, gs22 = 0.0, gs12 = 0.0;
-    if (dv > 0.0) {
-      const double gd = nc.g1[0] + nc.g4[0] * dv * dv * dv;
-      const double g_num_m = -gd * num_s / den_s, g_num_s = -gd * num_m / den_s;
-      const double g_den = gd * num_m * num_s / (den_s * den_s);
-      gm2 = g_num_m * (2.0 * (m1 - m2)) + g_num_s * (-2.0 * m1) + g_den * (-2.0 * m2);
+    const T m1 = mom[i], m2 = mom[n + i], s11 = mom[2 * n + i], s22 = mom[3 * n + i], s12 = mom[4 * n + i];
+    const T num_m = one - (m1 - m2) * (m1 - m2);
+    const T num_s = two * (s12 - m1 * m2) + c2;
+    const T den_s = (s11 - m1 * m1) + (s22 - m2 * m2) + c2;
+    const T dv = one - num_m * num_s / den_s;
+    T gm2 = zero, gs22 = zero, gs12 = zero;
+    if (dv > zero) {
+      const T gd = g1[0] + g4[0] * dv * dv * dv;
+      const T g_num_m = -gd * num_s / den_s, g_num_s = -gd * num_m / den_s;
+      const T g_den = gd * num_m * num_s / (den_s * den_s);
+      gm2 = g_num_m * (two * (m1 - m2)) + g_num_s * (-two * m1) + g_den * (-two * m2);
       gs22 = g_den;
-      gs12 = 2.0 * g_num_s;
+      gs12 = two * g_num_s;
     }
-    const double a = xa[i], b = xb[i];
-    const double Nn = 1.0 + fabs(b - m2), Dn = 1.0 + fabs(a - m1);
-    const double d1 = Nn / Dn - 1.0;
-    const double gd1 = (d1 > 0.0 ? nc.g1[1] + nc.g4[1] * d1 * d1 * d1 : 0.0) -
-                       (d1 < 0.0 ? nc.g1[2] + nc.g4[2] * (-d1) * (-d1) * (-d1) : 0.0);
-    const double sb = b - m2 > 0.0 ? 1.0 : (b - m2 < 0.0 ? -1.0 : 0.0);
+    const T a = xa[i], b = xb[i];
+    const T Nn = one + fabs(b - m2), Dn = one + fabs(a - m1);
+    const T d1 = Nn / Dn - one;
+    const T gd1 = (d1 > zero ? g1[1] + g4[1] * d1 * d1 * d1 : zero) -
+                  (d1 < zero ? g1[2] + g4[2] * (-d1) * (-d1) * (-d1) : zero);
+    const T sb = b - m2 > zero ? one : (b - m2 < zero ? -one : zero);
     g_xb[i] = gd1 * sb / Dn;
     g_m2[i] = gm2 - gd1 * sb / Dn;
     g_s22[i] = gs22;
@@ -251,33 +280,37 @@ __global__ void k_mapgrad64(const double* __restrict__ mom, const double* __rest
 }
 
 // d score / d xb = direct + G^T(g_m2) + 2 xb G^T(g_s22) + xa G^T(g_s12) for one channel.
-__global__ void k_combine64(const double* __restrict__ t_m2, const double* __restrict__ t_s22,
-                            const double* __restrict__ t_s12, const double* __restrict__ xa,
-                            const double* __restrict__ xb, long long n, double* __restrict__ g_xb) {
+template <typename T>
+__global__ void k_combine(const T* __restrict__ t_m2, const T* __restrict__ t_s22, const T* __restrict__ t_s12,
+                          const T* __restrict__ xa, const T* __restrict__ xb, long long n, T* __restrict__ g_xb) {
   for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x)
-    g_xb[i] += t_m2[i] + 2.0 * xb[i] * t_s22[i] + xa[i] * t_s12[i];
+    g_xb[i] += t_m2[i] + (T)2 * xb[i] * t_s22[i] + xa[i] * t_s12[i];
 }
 
 // XYB adjoint to the linear planes of this scale, plus the coarser scale's gradient spread over its 2x2 blocks.
-__global__ void k_xyb_adj64(const double* __restrict__ lin, const double* __restrict__ g_xyb, int w, int h,
-                            const double* __restrict__ g_coarse, int cw, double* __restrict__ g_lin) {
+template <typename T>
+__global__ void k_xyb_adj(const T* __restrict__ lin, const T* __restrict__ g_xyb, int w, int h,
+                          const T* __restrict__ g_coarse, int cw, T* __restrict__ g_lin) {
+  const T M00 = (T)kM00, M01 = (T)kM01, M02 = (T)kM02, M10 = (T)kM10, M11 = (T)kM11, M12 = (T)kM12;
+  const T M20 = (T)kM20, M21 = (T)kM21, M22 = (T)kM22, bias = (T)kBiasD;
+  const T zero = 0, one = 1, three = 3, half = (T)0.5, seven = 7;
   const long long n = (long long)w * h, cn = (long long)cw * ((h + 1) / 2);
   for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
-    const double r = lin[i], g = lin[n + i], b = lin[2 * n + i];
-    const double u0 = kM00 * r + kM01 * g + kM02 * b + kBiasD, u1 = kM10 * r + kM11 * g + kM12 * b + kBiasD,
-                 u2 = kM20 * r + kM21 * g + kM22 * b + kBiasD;
-    const double d0 = u0 > 0.0 ? 1.0 / (3.0 * cbrt(u0) * cbrt(u0)) : 0.0;
-    const double d1 = u1 > 0.0 ? 1.0 / (3.0 * cbrt(u1) * cbrt(u1)) : 0.0;
-    const double d2 = u2 > 0.0 ? 1.0 / (3.0 * cbrt(u2) * cbrt(u2)) : 0.0;
-    const double gX = g_xyb[i], gY = g_xyb[n + i], gB = g_xyb[2 * n + i];
-    const double gu0 = (7.0 * gX + 0.5 * gY - 0.5 * gB) * d0, gu1 = (-7.0 * gX + 0.5 * gY - 0.5 * gB) * d1,
-                 gu2 = gB * d2;
-    double o[3] = {gu0 * kM00 + gu1 * kM10 + gu2 * kM20, gu0 * kM01 + gu1 * kM11 + gu2 * kM21,
-                   gu0 * kM02 + gu1 * kM12 + gu2 * kM22};
+    const T r = lin[i], g = lin[n + i], b = lin[2 * n + i];
+    const T u0 = M00 * r + M01 * g + M02 * b + bias, u1 = M10 * r + M11 * g + M12 * b + bias,
+            u2 = M20 * r + M21 * g + M22 * b + bias;
+    const T d0 = u0 > zero ? one / (three * cbrt_t(u0) * cbrt_t(u0)) : zero;
+    const T d1 = u1 > zero ? one / (three * cbrt_t(u1) * cbrt_t(u1)) : zero;
+    const T d2 = u2 > zero ? one / (three * cbrt_t(u2) * cbrt_t(u2)) : zero;
+    const T gX = g_xyb[i], gY = g_xyb[n + i], gB = g_xyb[2 * n + i];
+    const T gu0 = (seven * gX + half * gY - half * gB) * d0, gu1 = (-seven * gX + half * gY - half * gB) * d1,
+            gu2 = gB * d2;
+    T o[3] = {gu0 * M00 + gu1 * M10 + gu2 * M20, gu0 * M01 + gu1 * M11 + gu2 * M21,
+              gu0 * M02 + gu1 * M12 + gu2 * M22};
     if (g_coarse) {
       const int y = (int)(i / w), x = (int)(i % w), ox = x / 2, oy = y / 2;
       const int nx = min(2 * ox + 2, w) - 2 * ox, ny = min(2 * oy + 2, h) - 2 * oy;
-      const double inv = 1.0 / (double)(nx * ny);
+      const T inv = one / (T)(nx * ny);
 #pragma unroll
       for (int c = 0; c < 3; c++) o[c] += g_coarse[c * cn + (long long)oy * cw + ox] * inv;
     }
@@ -286,9 +319,10 @@ __global__ void k_xyb_adj64(const double* __restrict__ lin, const double* __rest
   }
 }
 
-// Through the sRGB curve to the samples (interleaved RGB).
-__global__ void k_grad_out64(const double* __restrict__ g_lin, const float* __restrict__ dist, long long n,
-                             double* __restrict__ grad) {
+// Through the sRGB curve to the samples (interleaved RGB), written as f64.
+template <typename T>
+__global__ void k_grad_out(const T* __restrict__ g_lin, const float* __restrict__ dist, long long n,
+                           double* __restrict__ grad) {
   __shared__ double dlut[256];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) dlut[i] = c_dlin8[i];
   __syncthreads();
@@ -297,7 +331,7 @@ __global__ void k_grad_out64(const double* __restrict__ g_lin, const float* __re
     for (int c = 0; c < 3; c++) {
       const float v = dist[i * 3 + c];
       const int k = sample8(v);
-      grad[i * 3 + c] = g_lin[c * n + i] * (k >= 0 ? dlut[k] : srgb64_deriv((double)v));
+      grad[i * 3 + c] = (double)g_lin[c * n + i] * (k >= 0 ? dlut[k] : srgb64_deriv((double)v));
     }
 }
 
@@ -305,10 +339,11 @@ unsigned grid_of(long long n) {
   return (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 32));
 }
 
-}  // namespace
-
-int ssim2_grad_device(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, int w, int h, double* score,
-                      double* d_grad) {
+// The whole pass in real type T; workspace buffers are named per type.
+template <typename T>
+int grad_impl(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, int w, int h, double* score, double* d_grad) {
+  const std::string pfx = sizeof(T) == 8 ? "adj64_" : "adj32_";
+  auto ws = [&](const char* name, size_t count) { return (T*)workspace(ctx, (pfx + name).c_str(), count * sizeof(T)); };
   // constants
   double k[2 * kR + 1], sum = 0.0;
   for (int i = 0; i <= 2 * kR; i++) {
@@ -316,9 +351,15 @@ int ssim2_grad_device(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, i
     k[i] = std::exp(-0.5 / (1.5 * 1.5) * x * x);
     sum += k[i];
   }
-  for (int i = 0; i <= 2 * kR; i++) k[i] /= sum;
+  float k32[2 * kR + 1];
+  for (int i = 0; i <= 2 * kR; i++) {
+    k[i] /= sum;
+    k32[i] = (float)k[i];
+  }
+  // pageable sources: each upload has read its source when the call returns
   cudaMemcpyToSymbolAsync(c_k64, k, sizeof k, 0, cudaMemcpyHostToDevice, ctx->stream);
-  double lin8[256], dlin8[256];  // pageable sources: the uploads have read them when the calls return
+  cudaMemcpyToSymbolAsync(c_k32, k32, sizeof k32, 0, cudaMemcpyHostToDevice, ctx->stream);
+  double lin8[256], dlin8[256];
   for (int i = 0; i < 256; i++) {
     const double v = (double)i / 255.0;
     lin8[i] = v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4);
@@ -326,7 +367,7 @@ int ssim2_grad_device(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, i
   }
   cudaMemcpyToSymbolAsync(c_lin8, lin8, sizeof lin8, 0, cudaMemcpyHostToDevice, ctx->stream);
   cudaMemcpyToSymbolAsync(c_dlin8, dlin8, sizeof dlin8, 0, cudaMemcpyHostToDevice, ctx->stream);
-  // pyramid of both images (linear, f64)
+  // pyramid of both images (linear)
   struct Sc {
     int w, h;
     long long n, off;
@@ -342,43 +383,42 @@ int ssim2_grad_device(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, i
   const int ns = (int)sc.size();
   if (ns == 0) return fail(ctx, RCG_INVALID, "SSIMULACRA 2 needs at least 8x8 pixels");
   const long long n0 = sc[0].n;
-  double* pa = (double*)workspace(ctx, "adj_pa", sizeof(double) * total);
-  double* pb = (double*)workspace(ctx, "adj_pb", sizeof(double) * total);
-  double* xa = (double*)workspace(ctx, "adj_xa", sizeof(double) * 3 * n0);
-  double* xb = (double*)workspace(ctx, "adj_xb", sizeof(double) * 3 * n0);
-  double* hb = (double*)workspace(ctx, "adj_hb", sizeof(double) * n0);
-  double* mom = (double*)workspace(ctx, "adj_mom", sizeof(double) * 5 * n0);
-  double* gq = (double*)workspace(ctx, "adj_gq", sizeof(double) * 3 * n0);   // g_m2, g_s22, g_s12
-  double* tq = (double*)workspace(ctx, "adj_tq", sizeof(double) * 3 * n0);   // their blur adjoints
-  double* gx = (double*)workspace(ctx, "adj_gx", sizeof(double) * 3 * n0);   // d score / d xb
-  double* gl = (double*)workspace(ctx, "adj_gl", sizeof(double) * total);     // d score / d linear, per scale
-  double* sums = (double*)workspace(ctx, "adj_sums", sizeof(double) * kMaxScales * 18);
-  if (!pa || !pb || !xa || !xb || !hb || !mom || !gq || !tq || !gx || !gl || !sums) return RCG_NO_MEMORY;
-  RCG_LAUNCH(ctx, "adj_lin", k_lin64, grid_of(n0), 256, 0, d_ref, d_dist, n0, pa, pb);
+  T* pa = ws("pa", total);
+  T* pb = ws("pb", total);
+  T* xa = ws("xa", 3 * n0);
+  T* xb = ws("xb", 3 * n0);
+  T* hb = ws("hb", n0);
+  T* mom = ws("mom", 5 * n0);
+  T* gq = ws("gq", 3 * n0);  // g_m2, g_s22, g_s12
+  T* tq = ws("tq", 3 * n0);  // their blur adjoints
+  T* gx = ws("gx", 3 * n0);  // d score / d xb
+  T* gl = ws("gl", total);   // d score / d linear, per scale
+  double* sums = (double*)workspace(ctx, (pfx + "sums").c_str(), sizeof(double) * kMaxScales * 18);
+  double* parts = (double*)workspace(ctx, (pfx + "parts").c_str(), sizeof(double) * 6 * grid_of(n0));
+  if (!pa || !pb || !xa || !xb || !hb || !mom || !gq || !tq || !gx || !gl || !sums || !parts) return RCG_NO_MEMORY;
+  RCG_LAUNCH(ctx, "adj_lin", k_lin<T>, grid_of(n0), 256, 0, d_ref, d_dist, n0, pa, pb);
   for (int s = 1; s < ns; s++) {
-    RCG_LAUNCH(ctx, "adj_down", k_down64, grid_of(3 * sc[s].n), 256, 0, pa + sc[s - 1].off, sc[s - 1].w, sc[s - 1].h,
-               pa + sc[s].off, sc[s].w, sc[s].h);
-    RCG_LAUNCH(ctx, "adj_down", k_down64, grid_of(3 * sc[s].n), 256, 0, pb + sc[s - 1].off, sc[s - 1].w, sc[s - 1].h,
-               pb + sc[s].off, sc[s].w, sc[s].h);
+    RCG_LAUNCH(ctx, "adj_down", k_down<T>, grid_of(3 * sc[s].n), 256, 0, pa + sc[s - 1].off, sc[s - 1].w,
+               sc[s - 1].h, pa + sc[s].off, sc[s].w, sc[s].h);
+    RCG_LAUNCH(ctx, "adj_down", k_down<T>, grid_of(3 * sc[s].n), 256, 0, pb + sc[s - 1].off, sc[s - 1].w,
+               sc[s - 1].h, pb + sc[s].off, sc[s].w, sc[s].h);
   }
   // forward: the moments and map sums of every scale
   auto moments = [&](int s, int c) {
     const long long n = sc[s].n;
     for (int q = 0; q < 5; q++) {
-      RCG_LAUNCH(ctx, "adj_hblur", k_hblur64, grid_of(n), 256, 0, xa + c * n, xb + c * n, (const double*)nullptr, q,
+      RCG_LAUNCH(ctx, "adj_hblur", k_hblur<T>, grid_of(n), 256, 0, xa + c * n, xb + c * n, (const T*)nullptr, q,
                  sc[s].w, sc[s].h, hb);
-      RCG_LAUNCH(ctx, "adj_vblur", k_vblur64, grid_of(n), 256, 0, hb, sc[s].w, sc[s].h, mom + q * n);
+      RCG_LAUNCH(ctx, "adj_vblur", k_vblur<T>, grid_of(n), 256, 0, hb, sc[s].w, sc[s].h, mom + q * n);
     }
   };
-  double* parts = (double*)workspace(ctx, "adj_parts", sizeof(double) * 6 * grid_of(n0));
-  if (!parts) return RCG_NO_MEMORY;
   for (int s = 0; s < ns; s++) {
     const long long n = sc[s].n;
-    RCG_LAUNCH(ctx, "adj_xyb", k_xyb64, grid_of(n), 256, 0, pa + sc[s].off, n, xa);
-    RCG_LAUNCH(ctx, "adj_xyb", k_xyb64, grid_of(n), 256, 0, pb + sc[s].off, n, xb);
+    RCG_LAUNCH(ctx, "adj_xyb", k_xyb<T>, grid_of(n), 256, 0, pa + sc[s].off, n, xa);
+    RCG_LAUNCH(ctx, "adj_xyb", k_xyb<T>, grid_of(n), 256, 0, pb + sc[s].off, n, xb);
     for (int c = 0; c < 3; c++) {
       moments(s, c);
-      RCG_LAUNCH(ctx, "adj_maps", k_maps64, grid_of(n), 256, 0, mom, xa + c * n, xb + c * n, n, parts);
+      RCG_LAUNCH(ctx, "adj_maps", k_maps<T>, grid_of(n), 256, 0, mom, xa + c * n, xb + c * n, n, parts);
       RCG_LAUNCH(ctx, "adj_sum_parts", k_sum_parts, 1, 192, 0, parts, (int)grid_of(n), sums + s * 18 + c * 6);
     }
   }
@@ -424,8 +464,8 @@ int ssim2_grad_device(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, i
   for (int s = ns - 1; s >= 0; s--) {
     const long long n = sc[s].n;
     const double count = (double)n;
-    RCG_LAUNCH(ctx, "adj_xyb", k_xyb64, grid_of(n), 256, 0, pa + sc[s].off, n, xa);
-    RCG_LAUNCH(ctx, "adj_xyb", k_xyb64, grid_of(n), 256, 0, pb + sc[s].off, n, xb);
+    RCG_LAUNCH(ctx, "adj_xyb", k_xyb<T>, grid_of(n), 256, 0, pa + sc[s].off, n, xa);
+    RCG_LAUNCH(ctx, "adj_xyb", k_xyb<T>, grid_of(n), 256, 0, pb + sc[s].off, n, xb);
     for (int c = 0; c < 3; c++) {
       NormCoef nc;
       for (int m = 0; m < 3; m++) {
@@ -434,21 +474,29 @@ int ssim2_grad_device(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, i
         nc.g4[m] = mean4 > 0.0 ? dsum * wst[s][c][2 * m + 1] * std::pow(mean4, -0.75) / count : 0.0;
       }
       moments(s, c);  // recomputed, not stored
-      RCG_LAUNCH(ctx, "adj_mapgrad", k_mapgrad64, grid_of(n), 256, 0, mom, xa + c * n, xb + c * n, n, nc, gq,
+      RCG_LAUNCH(ctx, "adj_mapgrad", k_mapgrad<T>, grid_of(n), 256, 0, mom, xa + c * n, xb + c * n, n, nc, gq,
                  gq + n, gq + 2 * n, gx + c * n);
       for (int j = 0; j < 3; j++) {
-        RCG_LAUNCH(ctx, "adj_vblur_t", k_vblur64_t, grid_of(n), 256, 0, gq + j * n, sc[s].w, sc[s].h, hb);
-        RCG_LAUNCH(ctx, "adj_hblur", k_hblur64, grid_of(n), 256, 0, (const double*)nullptr, (const double*)nullptr,
-                   hb, -1, sc[s].w, sc[s].h, tq + j * n);
+        RCG_LAUNCH(ctx, "adj_vblur_t", k_vblur_t<T>, grid_of(n), 256, 0, gq + j * n, sc[s].w, sc[s].h, hb);
+        RCG_LAUNCH(ctx, "adj_hblur", k_hblur<T>, grid_of(n), 256, 0, (const T*)nullptr, (const T*)nullptr, hb, -1,
+                   sc[s].w, sc[s].h, tq + j * n);
       }
-      RCG_LAUNCH(ctx, "adj_combine", k_combine64, grid_of(n), 256, 0, tq, tq + n, tq + 2 * n, xa + c * n, xb + c * n,
-                 n, gx + c * n);
+      RCG_LAUNCH(ctx, "adj_combine", k_combine<T>, grid_of(n), 256, 0, tq, tq + n, tq + 2 * n, xa + c * n,
+                 xb + c * n, n, gx + c * n);
     }
-    RCG_LAUNCH(ctx, "adj_xyb_adj", k_xyb_adj64, grid_of(n), 256, 0, pb + sc[s].off, gx, sc[s].w, sc[s].h,
+    RCG_LAUNCH(ctx, "adj_xyb_adj", k_xyb_adj<T>, grid_of(n), 256, 0, pb + sc[s].off, gx, sc[s].w, sc[s].h,
                s + 1 < ns ? gl + sc[s + 1].off : nullptr, s + 1 < ns ? sc[s + 1].w : 0, gl + sc[s].off);
   }
-  RCG_LAUNCH(ctx, "adj_out", k_grad_out64, grid_of(npx), 256, 0, gl + sc[0].off, d_dist, npx, d_grad);
+  RCG_LAUNCH(ctx, "adj_out", k_grad_out<T>, grid_of(npx), 256, 0, gl + sc[0].off, d_dist, npx, d_grad);
   return RCG_OK;
+}
+
+}  // namespace
+
+int ssim2_grad_device(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, int w, int h, double* score,
+                      double* d_grad, bool fp32) {
+  return fp32 ? grad_impl<float>(ctx, d_ref, d_dist, w, h, score, d_grad)
+              : grad_impl<double>(ctx, d_ref, d_dist, w, h, score, d_grad);
 }
 
 }  // namespace rcg

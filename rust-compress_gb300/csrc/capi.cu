@@ -1266,6 +1266,7 @@ void rcg_perceptual_defaults(rcg_perceptual_options* o) {
   o->w_max = 4.0;
   o->radius = 1;
   o->keep_smaller = 1;
+  o->gradient_fp64 = 0;
 }
 
 static int check_popts(rcg_ctx* ctx, const rcg_perceptual_options* o, PerceptualParams* p) {
@@ -1274,7 +1275,7 @@ static int check_popts(rcg_ctx* ctx, const rcg_perceptual_options* o, Perceptual
                   std::isfinite(o->w_max) && o->w_min > 0.0 && o->w_max >= o->w_min && o->radius >= 0 &&
                   o->radius <= 16;
   if (!ok) return fail(ctx, RCG_INVALID, "perceptual options out of range");
-  *p = PerceptualParams{o->strength, o->gamma, o->w_min, o->w_max, o->radius};
+  *p = PerceptualParams{o->strength, o->gamma, o->w_min, o->w_max, o->radius, o->gradient_fp64 != 0};
   return RCG_OK;
 }
 
@@ -1295,7 +1296,7 @@ static int perceptual_impl(rcg_ctx* ctx, const uint8_t* d_ref, const uint8_t* d_
     ref3 = r3;
   }
   expand_rgb(ctx, d_dec, channels, npx, nullptr, d_dist);
-  int rc = ssim2_grad_device(ctx, ref3, d_dist, w, h, score, d_grad);
+  int rc = ssim2_grad_device(ctx, ref3, d_dist, w, h, score, d_grad, !p.gradient_fp64);
   if (rc != RCG_OK) return rc;
   return perceptual_pullback(ctx, d_grad, w, h, lay, p, d_coef_grad, d_weights);
 }
@@ -1350,7 +1351,7 @@ int rcg_coef_gradient(rcg_ctx* ctx, const uint8_t* reference, const uint8_t* dec
   const size_t n = (size_t)st->nblocks * 64;
   double* d_cg = (double*)workspace(ctx, "perc_coef_grad", n * sizeof(double));
   if (!d_cg) rc = RCG_NO_MEMORY;
-  PerceptualParams p{1.0, 0.0, 1.0, 1.0, 0};
+  PerceptualParams p{1.0, 0.0, 1.0, 1.0, 0, true};  // the checked FP64 gradient
   if (rc == RCG_OK) rc = perceptual_impl(ctx, d_ref, d_dec, (int)width, (int)height, channels, st, p, score, d_cg,
                                          nullptr);
   delete st;

@@ -262,9 +262,10 @@ int jpeg_decode(rcg_ctx* ctx, const uint8_t* data, size_t len, rcg_jpeg_info* in
 
 // The scorer's 108 weights (core/src/ssimulacra2.rs:54-163), host side.
 const double* scorer_weights();
-// d SSIMULACRA2 / d distorted RGB samples (continuous, f32 in [0, 255]) in FP64; the reference image is 8-bit RGB.
+// d SSIMULACRA2 / d distorted RGB samples (continuous, f32 in [0, 255]); the reference image is 8-bit RGB. FP64
+// throughout (the checked gradient) or, with fp32, the same pass in f32 (the perceptual weights); both write f64.
 int ssim2_grad_device(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, int w, int h, double* score,
-                      double* d_grad);
+                      double* d_grad, bool fp32 = false);
 
 // write_best's plan (progressive candidates + baseline estimate) of coefficients on the device; `lay` carries the
 // component layout (ncomp, hmax, vmax, comp[]).
@@ -294,6 +295,7 @@ int step_tables(rcg_ctx* ctx, SearchState* d_search, StepDesc* d_step, int w, in
 struct PerceptualParams {
   double strength, gamma, w_min, w_max;
   int radius;
+  bool gradient_fp64;  // the FP64 adjoint (else the FP32 instantiation)
 };
 // d SSIMULACRA2 / d coefficient of a decoded candidate: the pixel gradient (f64, [h][w][3]) pulled back through the
 // YCbCr->RGB conversion, the chroma upsampling and the orthonormal 8x8 IDCT, per coefficient in the coefficient

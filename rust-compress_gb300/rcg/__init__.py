@@ -103,13 +103,15 @@ class _PlanResult(ctypes.Structure):
 
 class _PerceptualOpts(ctypes.Structure):
     _fields_ = [("strength", ctypes.c_double), ("gamma", ctypes.c_double), ("w_min", ctypes.c_double),
-                ("w_max", ctypes.c_double), ("radius", ctypes.c_int32), ("keep_smaller", ctypes.c_int32)]
+                ("w_max", ctypes.c_double), ("radius", ctypes.c_int32), ("keep_smaller", ctypes.c_int32),
+                ("gradient_fp64", ctypes.c_int32)]
 
 
 @dataclass
 class PerceptualOptions:
     """Options of the perceptual trellis (rcg_perceptual_options): W[b][k] = strength * clamp((s_b / mean s)^gamma,
-    w_min, w_max) with s_b the RMS coefficient-gradient energy over the (2 radius + 1)^2 blocks around block b."""
+    w_min, w_max) with s_b the RMS coefficient-gradient energy over the (2 radius + 1)^2 blocks around block b; the
+    gradient from the FP32 adjoint unless gradient_fp64."""
 
     strength: float = 0.35
     gamma: float = 0.5
@@ -117,10 +119,11 @@ class PerceptualOptions:
     w_max: float = 4.0
     radius: int = 1
     keep_smaller: bool = True
+    gradient_fp64: bool = False  # the FP64 adjoint instead of its FP32 instantiation
 
     def _c(self):
         return _PerceptualOpts(float(self.strength), float(self.gamma), float(self.w_min), float(self.w_max),
-                               int(self.radius), 1 if self.keep_smaller else 0)
+                               int(self.radius), 1 if self.keep_smaller else 0, 1 if self.gradient_fp64 else 0)
 
 
 @dataclass

@@ -68,5 +68,5 @@ def test_perceptual_defaults_match_the_python_options():
     o = rcg._PerceptualOpts()
     rcg.lib().rcg_perceptual_defaults(ctypes.byref(o))
     d = rcg.PerceptualOptions()
-    assert (o.strength, o.gamma, o.w_min, o.w_max, o.radius, bool(o.keep_smaller)) == \
-        (d.strength, d.gamma, d.w_min, d.w_max, d.radius, d.keep_smaller)
+    assert (o.strength, o.gamma, o.w_min, o.w_max, o.radius, bool(o.keep_smaller), bool(o.gradient_fp64)) == \
+        (d.strength, d.gamma, d.w_min, d.w_max, d.radius, d.keep_smaller, d.gradient_fp64)
