@@ -582,11 +582,11 @@ def main():
     alg_bytes = 6.0 * W * H  # two RGB8 images per score (full-resolution pixels)
     achieved = alg_bytes / (tile_ms / 1000.0) / 1e9
     # DRAM bytes of one launch at this workload size from an ncu capture of the same kernel (dram__bytes_read.sum +
-    # dram__bytes_write.sum: 384.0 MB + 5.5 MB); None for other sizes.
-    traffic = 389.48e6 if (W, H) == (4000, 3000) else None
+    # dram__bytes_write.sum: 384.0 MB + 5.7 MB); None for other sizes.
+    traffic = 389.63e6 if (W, H) == (4000, 3000) else None
     roof = {"kernel": "ssim2_tiles", "bound": "hbm", "achieved": achieved, "peak": hbm or 6800.0,
             "unit": "GB/s", "frac": achieved / (hbm or 6800.0), "traffic": traffic,
-            "traffic_source": "ncu capture of the same kernel and workload (384.0 MB read + 5.5 MB written)",
+            "traffic_source": "ncu capture of the same kernel and workload (384.0 MB read + 5.7 MB written)",
             "peak_source": "measured" if hbm else "fallback",
             "avg_launch_ms": tile_ms,
             "note": "the scorer is FP32-ALU bound (~1 kflop per full-resolution pixel), far below the HBM roof; "
