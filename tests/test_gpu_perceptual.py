@@ -161,3 +161,21 @@ def test_perceptual_errors(ctx):
         assert e.value.status == rcg.RCG_INVALID
     with pytest.raises(rcg.RcgError):
         ctx.coef_gradient(img, img[:, :, :1].copy(), lay)
+
+
+@pytest.mark.parametrize("c,sub", [(1, rcg.Subsampling.Auto), (3, rcg.Subsampling.S444), (3, rcg.Subsampling.S422)])
+def test_perceptual_search_other_layouts(ctx, oracle, c, sub):
+    """Gray (any subsampling: its layout never changes), 4:4:4 and 4:2:2: the weighted search follows the oracle's
+    weighted search with the same weights, and the returned result is the smaller planned one."""
+    img = synth.image(352, 264, 96, sensor_sigma=3.0)
+    if c == 1:
+        img = img[:, :, 2].copy()
+    opts = rcg.EncodeOptions(90, sub, True)
+    r = ctx.find_quality_perceptual(img, 65.0, 100, opts)
+    q, s, coefs, _, _, trace = oracle.search(img, 65.0, 100, int(sub), True, weights=r.weights)
+    weighted = ctx.find_quality_weighted(img, 65.0, r.weights, 100, opts)
+    assert [t[0] for t in weighted.trace] == [t[0] for t in trace]
+    assert weighted.quality == q and np.array_equal(weighted.coefs.flat(), coefs)
+    assert r.chose_perceptual == (r.perceptual_bytes <= r.plain_bytes)
+    assert r.found.quality == (weighted.quality if r.chose_perceptual else r.plain.quality)
+    assert r.found.score >= 65.0
