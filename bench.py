@@ -198,7 +198,7 @@ def scorer_alone(ctx, stream, timed, torch, dev, peaks, with_oracle=True, w=3840
     return out
 
 
-def batch_workload(ctx, torch, n=64, parallel=8, steps=2):
+def batch_workload(ctx, torch, n=64, parallel=8, steps=2, perceptual=True):
     """Many images of uneven sizes (seeds 2..2+n-1, log-uniform 640x480..6000x4000, aspect 4:3/3:2/16:9/1:1), each
     with its own target drawn uniformly from 55..85: plain searches one after another (rcg_search) against the
     concurrent rcg_search_batch. Host buffers (end to end through the C ABI); same results per image."""
@@ -219,11 +219,34 @@ def batch_workload(ctx, torch, n=64, parallel=8, steps=2):
     res_p = [ctx.find_quality_ssimulacra2(im, t, 100, opts) for im, t in zip(imgs, targets)]
     tp = time.perf_counter() - t0
     same = all(a.quality == b.quality and a.trace == b.trace for a, b in zip(res_b, res_p))
-    return {"workload": f"{n} images, log-uniform 640x480..6000x4000 ({mpx:.0f} MP in all), targets U(55,85), "
-                        "4:2:0, trellis", "images": n, "megapixels": mpx,
-            "plain_searches_per_s": n / tp, "batch_searches_per_s": n / tb, "batch_parallel": parallel,
-            "batch_vs_plain": tp / tb, "identical_results": same,
-            "mean_quality": sum(r.quality for r in res_b) / n}
+    out = {"workload": f"{n} images, log-uniform 640x480..6000x4000 ({mpx:.0f} MP in all), targets U(55,85), "
+                       "4:2:0, trellis", "images": n, "megapixels": mpx,
+           "plain_searches_per_s": n / tp, "batch_searches_per_s": n / tb, "batch_parallel": parallel,
+           "batch_vs_plain": tp / tb, "identical_results": same,
+           "mean_quality": sum(r.quality for r in res_b) / n}
+    if perceptual:
+        # The perceptual search on the same images and targets: planned file sizes of the plain result, of the
+        # weighted search's result, and of what the search returns (the smaller of the two); all meet the target.
+        t0 = time.perf_counter()
+        res_w = [ctx.find_quality_perceptual(im, t, 100, opts) for im, t in zip(imgs, targets)]
+        tw = time.perf_counter() - t0
+        plain_b = [r.plain_bytes for r in res_w]
+        weighted_b = [r.perceptual_bytes for r in res_w]
+        returned_b = [r.perceptual_bytes if r.chose_perceptual else r.plain_bytes for r in res_w]
+        mean = lambda v: sum(v) / len(v)
+        out["perceptual"] = {
+            "searches_per_s": n / tw,
+            "mean_plain_bytes": mean(plain_b), "mean_weighted_bytes": mean(weighted_b),
+            "mean_returned_bytes": mean(returned_b),
+            "returned_vs_plain_pct": round(100.0 * (mean(returned_b) / mean(plain_b) - 1.0), 2),
+            "weighted_vs_plain_pct": round(100.0 * (mean(weighted_b) / mean(plain_b) - 1.0), 2),
+            "images_weighted_smaller": sum(1 for a, b in zip(plain_b, weighted_b) if b < a),
+            "plain_same_as_batch": all(r.plain.quality == b.quality for r, b in zip(res_w, res_b)),
+            # the reference returns the max quality below the target when even that misses (jpeg/src/target.rs:36-39)
+            "returned_meets_target_when_plain_does": all(r.found.score >= t for r, t in zip(res_w, targets)
+                                                         if r.plain.score >= t),
+            "mean_returned_score_minus_plain": mean([r.found.score - r.plain.score for r in res_w])}
+    return out
 
 
 def requantize_workload(ctx, img, timed, with_oracle=True, steps=5):
@@ -288,7 +311,8 @@ def perceptual_workload(ctx, img, timed, steps=3):
     ctx.find_quality_perceptual(img, TARGET, 100, opts, popts)
     times, r = timed(lambda: ctx.find_quality_perceptual(img, TARGET, 100, opts, popts), steps)
     ms = sum(times) / len(times)
-    uniform = np.full_like(r.weights, np.float32(popts.strength))
+    strength = popts.strength_for(r.plain.quality)
+    uniform = np.full_like(r.weights, np.float32(strength))
 
     def point(q, wts):
         o = rcg.EncodeOptions(q, opts.subsampling, True)
@@ -312,7 +336,8 @@ def perceptual_workload(ctx, img, timed, steps=3):
     returned = r.perceptual_bytes if r.chose_perceptual else r.plain_bytes
 
     return {"workload": "perceptual trellis: 4000x3000 seed 1 sigma 3, target 70, 4:2:0, default options "
-                        f"(strength {popts.strength}, gamma {popts.gamma}, radius {popts.radius})",
+                        f"(strength {strength} for plain quality {r.plain.quality}, gamma {popts.gamma}, "
+                        f"radius {popts.radius}, FP32 adjoint)",
             "ms_per_perceptual_search": ms, "searches_per_s": 1000.0 / ms,
             "plain": {"quality": r.plain.quality, "score": r.plain.score, "bytes": r.plain_bytes},
             "weighted": {"bytes": r.perceptual_bytes},
@@ -594,7 +619,7 @@ def main():
                     "algorithmic bytes = 6 B per full-resolution pixel (two RGB8 images)"}
     batch = None
     if rank == 0 and not args.no_batch:
-        batch = batch_workload(ctx, torch)
+        batch = batch_workload(ctx, torch, perceptual=not args.no_perceptual)
     scorer = None
     if rank == 0 and not args.no_scorer:
         scorer = scorer_alone(ctx, stream, timed, torch, dev, peaks, with_oracle=not args.no_cpu_baseline)

@@ -280,10 +280,18 @@ typedef struct {
   int32_t radius;  /* sensitivity = RMS of the gradient energy over (2 radius + 1)^2 neighbouring blocks */
   int32_t keep_smaller; /* rcg_search_perceptual: return the plain result when its planned size is smaller */
   int32_t gradient_fp64; /* 1: the weights come from the FP64 adjoint; 0: from the same pass in FP32 (faster) */
+  int32_t strength_by_quality; /* rcg_search_perceptual: the strength follows the plain result's quality (see
+                                  rcg_perceptual_strength) instead of `strength` */
 } rcg_perceptual_options;
 
-/* The defaults: strength 0.35, gamma 0.5, w_min 0.25, w_max 4, radius 1, keep_smaller 1, gradient_fp64 0. */
+/* The defaults: strength 0.35, gamma 0.5, w_min 0.25, w_max 4, radius 1, keep_smaller 1, gradient_fp64 0,
+ * strength_by_quality 1. */
 void rcg_perceptual_defaults(rcg_perceptual_options* opts);
+
+/* The strength rcg_search_perceptual uses after a plain search found `quality`: `strength` unless
+ * strength_by_quality, else 0.35 below quality 70, 0.7 below 85 and 1.0 from 85 (a lower distortion weight pays at
+ * low qualities and costs at high ones; measured on seeded synthetic image sets). */
+double rcg_perceptual_strength(const rcg_perceptual_options* opts, int quality);
 
 /* d SSIMULACRA2(reference, decoded) / d coefficient for the coefficient layout `layout` (64 zigzag entries per block,
  * components in order; dequantized units: multiply by the quantization step for d score / d quantized value). Both

@@ -1267,6 +1267,13 @@ void rcg_perceptual_defaults(rcg_perceptual_options* o) {
   o->radius = 1;
   o->keep_smaller = 1;
   o->gradient_fp64 = 0;
+  o->strength_by_quality = 1;
+}
+
+double rcg_perceptual_strength(const rcg_perceptual_options* o, int quality) {
+  if (!o) return 0.0;
+  if (!o->strength_by_quality) return o->strength;
+  return quality < 70 ? 0.35 : (quality < 85 ? 0.7 : 1.0);
 }
 
 static int check_popts(rcg_ctx* ctx, const rcg_perceptual_options* o, PerceptualParams* p) {
@@ -1462,6 +1469,7 @@ int rcg_search_perceptual(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint
                    opts->trellis, plain, d_plain, (size_t)ncoefs, nullptr, nullptr, nullptr);
   if (rc != RCG_OK) return rc;
   // 2. its decoded image, and the weights from the gradient there
+  p.strength = rcg_perceptual_strength(popts, plain->quality);
   StepDesc* st = new StepDesc;
   host_step_tables(st, plain->quality, opts->subsampling, channels, opts->trellis, w, h);
   uint8_t* planes = (uint8_t*)workspace(ctx, "perc_planes", (size_t)plane_bytes(st));

@@ -104,7 +104,7 @@ class _PlanResult(ctypes.Structure):
 class _PerceptualOpts(ctypes.Structure):
     _fields_ = [("strength", ctypes.c_double), ("gamma", ctypes.c_double), ("w_min", ctypes.c_double),
                 ("w_max", ctypes.c_double), ("radius", ctypes.c_int32), ("keep_smaller", ctypes.c_int32),
-                ("gradient_fp64", ctypes.c_int32)]
+                ("gradient_fp64", ctypes.c_int32), ("strength_by_quality", ctypes.c_int32)]
 
 
 @dataclass
@@ -120,10 +120,17 @@ class PerceptualOptions:
     radius: int = 1
     keep_smaller: bool = True
     gradient_fp64: bool = False  # the FP64 adjoint instead of its FP32 instantiation
+    strength_by_quality: bool = True  # find_quality_perceptual: strength from the plain result's quality
 
     def _c(self):
         return _PerceptualOpts(float(self.strength), float(self.gamma), float(self.w_min), float(self.w_max),
-                               int(self.radius), 1 if self.keep_smaller else 0, 1 if self.gradient_fp64 else 0)
+                               int(self.radius), 1 if self.keep_smaller else 0, 1 if self.gradient_fp64 else 0,
+                               1 if self.strength_by_quality else 0)
+
+    def strength_for(self, quality):
+        """The strength find_quality_perceptual uses after a plain search found `quality`."""
+        o = self._c()
+        return float(_lib.rcg_perceptual_strength(ctypes.byref(o), int(quality)))
 
 
 @dataclass
@@ -274,6 +281,7 @@ def _load():
         "rcg_plan_device": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, ctypes.POINTER(_PlanResult)]),
         "rcg_search_batch": (i32, [P, i32, P, P, P, P, P, i32, ctypes.POINTER(_Opts), i32, P, P, P, P]),
         "rcg_perceptual_defaults": (None, [ctypes.POINTER(_PerceptualOpts)]),
+        "rcg_perceptual_strength": (ctypes.c_double, [ctypes.POINTER(_PerceptualOpts), i32]),
         "rcg_coef_gradient": (i32, [P, P, P, u32, u32, i32, ctypes.POINTER(_Layout),
                                     ctypes.POINTER(ctypes.c_double), P, sz]),
         "rcg_perceptual_weights": (i32, [P, P, P, u32, u32, i32, ctypes.POINTER(_Layout),
@@ -300,7 +308,8 @@ EXPORTED = (
     "rcg_search_batch rcg_reconstruct_tables rcg_requantize rcg_search_requantize rcg_plan rcg_plan_device "
     "rcg_metric_score rcg_metric_score_device rcg_search_metric rcg_decode_coefs rcg_decode_coefs_device "
     "rcg_search_requantize_device rcg_ssimulacra2_grad rcg_ssimulacra2_grad_device rcg_perceptual_defaults "
-    "rcg_coef_gradient rcg_perceptual_weights rcg_build_coefs_weighted rcg_search_weighted rcg_search_perceptual"
+    "rcg_coef_gradient rcg_perceptual_weights rcg_build_coefs_weighted rcg_search_weighted rcg_search_perceptual "
+    "rcg_perceptual_strength"
 ).split()
 
 

@@ -68,5 +68,9 @@ def test_perceptual_defaults_match_the_python_options():
     o = rcg._PerceptualOpts()
     rcg.lib().rcg_perceptual_defaults(ctypes.byref(o))
     d = rcg.PerceptualOptions()
-    assert (o.strength, o.gamma, o.w_min, o.w_max, o.radius, bool(o.keep_smaller), bool(o.gradient_fp64)) == \
-        (d.strength, d.gamma, d.w_min, d.w_max, d.radius, d.keep_smaller, d.gradient_fp64)
+    assert (o.strength, o.gamma, o.w_min, o.w_max, o.radius, bool(o.keep_smaller), bool(o.gradient_fp64),
+            bool(o.strength_by_quality)) == \
+        (d.strength, d.gamma, d.w_min, d.w_max, d.radius, d.keep_smaller, d.gradient_fp64, d.strength_by_quality)
+    # the strength schedule is host arithmetic: checkable without a GPU
+    assert [d.strength_for(q) for q in (1, 69, 70, 84, 85, 100)] == [0.35, 0.35, 0.7, 0.7, 1.0, 1.0]
+    assert rcg.PerceptualOptions(strength=0.5, strength_by_quality=False).strength_for(90) == 0.5

@@ -122,11 +122,15 @@ def test_perceptual_search(ctx):
     opts = rcg.EncodeOptions(90, rcg.Subsampling.S420, True)
     plain = ctx.find_quality_ssimulacra2(img, 70.0, 100, opts)
     for keep in (True, False):
-        r = ctx.find_quality_perceptual(img, 70.0, 100, opts, rcg.PerceptualOptions(keep_smaller=keep))
+        popts = rcg.PerceptualOptions(keep_smaller=keep)
+        r = ctx.find_quality_perceptual(img, 70.0, 100, opts, popts)
         assert (r.plain.quality, r.plain.score, r.plain.trace) == (plain.quality, plain.score, plain.trace)
-        # the weights come from the gradient at the plain result's decoded image
+        # the weights come from the gradient at the plain result's decoded image, with the strength the plain
+        # result's quality selects
+        strength = popts.strength_for(plain.quality)
+        assert strength == (0.35 if plain.quality < 70 else (0.7 if plain.quality < 85 else 1.0))
         lay = ctx.coef_layout(640, 480, 3, rcg.EncodeOptions(50, rcg.Subsampling.S420, True))
-        _, wts = ctx.perceptual_weights(img, ctx.reconstruct(plain.coefs), lay)
+        _, wts = ctx.perceptual_weights(img, ctx.reconstruct(plain.coefs), lay, rcg.PerceptualOptions(strength))
         assert np.array_equal(r.weights, wts)
         weighted = ctx.find_quality_weighted(img, 70.0, wts, 100, opts)
         p_plain, p_w = ctx.plan(plain.coefs), ctx.plan(weighted.coefs)
