@@ -117,68 +117,94 @@ __global__ void k_xyb(const T* __restrict__ lin, long long n, T* __restrict__ xy
   }
 }
 
-// Row blur (zero outside) of the product `q` of one channel's XYB planes: 0 xa, 1 xb, 2 xa^2, 3 xb^2, 4 xa xb;
-// q = -1 blurs `src` itself (the adjoint's rows).
+// Row blur (zero outside) of one plane: the backward pass's rows (the zero-padded row blur is its own transpose).
+// `planes` consecutive planes of n samples in one sweep.
 template <typename T>
-__global__ void k_hblur(const T* __restrict__ xa, const T* __restrict__ xb, const T* __restrict__ src, int q, int w,
-                        int h, T* __restrict__ dst) {
+__global__ void k_hblur(const T* __restrict__ src, int w, int h, int planes, T* __restrict__ dst) {
   const long long n = (long long)w * h;
-  for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int y = (int)(i / w), x = (int)(i % w);
+  for (long long i = tid1(); i < n * planes; i += (long long)gridDim.x * blockDim.x) {
+    const long long p = i / n, o = i - p * n;
+    const int y = (int)(o / w), x = (int)(o % w);
+    const T* sp = src + p * n;
     T s = 0;
 #pragma unroll
     for (int t = 0; t <= 2 * kR; t++) {
       const int xx = x + t - kR;
       if (xx < 0 || xx >= w) continue;
-      const long long j = (long long)y * w + xx;
-      T v;
-      if (q < 0)
-        v = src[j];
-      else if (q == 0)
-        v = xa[j];
-      else if (q == 1)
-        v = xb[j];
-      else if (q == 2)
-        v = xa[j] * xa[j];
-      else if (q == 3)
-        v = xb[j] * xb[j];
-      else
-        v = xa[j] * xb[j];
-      s += tap<T>(t) * v;
+      s += tap<T>(t) * sp[(long long)y * w + xx];
     }
     dst[i] = s;
   }
 }
 
-__device__ __forceinline__ int mirror64(int yy, int h) { return yy < 0 ? -yy - 1 : (yy >= h ? 2 * h - 1 - yy : yy); }
-
-// Column blur with mirrored rows (:385-397).
+// The five products of the forward pass blurred along rows in one sweep: dst + q * n for q = 0 xa, 1 xb, 2 xa^2,
+// 3 xb^2, 4 xa xb (each output summed over the taps in the same order as k_hblur).
 template <typename T>
-__global__ void k_vblur(const T* __restrict__ src, int w, int h, T* __restrict__ dst) {
+__global__ void k_hblur5(const T* __restrict__ xa, const T* __restrict__ xb, int w, int h, T* __restrict__ dst) {
   const long long n = (long long)w * h;
   for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
     const int y = (int)(i / w), x = (int)(i % w);
+    T s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0;
+#pragma unroll
+    for (int t = 0; t <= 2 * kR; t++) {
+      const int xx = x + t - kR;
+      if (xx < 0 || xx >= w) continue;
+      const long long j = (long long)y * w + xx;
+      const T a = xa[j], b = xb[j], k = tap<T>(t);
+      s0 += k * a;
+      s1 += k * b;
+      s2 += k * (a * a);
+      s3 += k * (b * b);
+      s4 += k * (a * b);
+    }
+    dst[i] = s0;
+    dst[n + i] = s1;
+    dst[2 * n + i] = s2;
+    dst[3 * n + i] = s3;
+    dst[4 * n + i] = s4;
+  }
+}
+
+__device__ __forceinline__ int mirror64(int yy, int h) { return yy < 0 ? -yy - 1 : (yy >= h ? 2 * h - 1 - yy : yy); }
+
+// Column blur with mirrored rows (:385-397) of `planes` consecutive planes of n samples in one sweep.
+template <typename T>
+__global__ void k_vblur_n(const T* __restrict__ src, int w, int h, int planes, T* __restrict__ dst) {
+  const long long n = (long long)w * h;
+  for (long long i = tid1(); i < n * planes; i += (long long)gridDim.x * blockDim.x) {
+    const long long p = i / n, o = i - p * n;
+    const int y = (int)(o / w), x = (int)(o % w);
+    const T* sp = src + p * n;
     T s = 0;
 #pragma unroll
-    for (int t = 0; t <= 2 * kR; t++) s += tap<T>(t) * src[(long long)mirror64(y + t - kR, h) * w + x];
+    for (int t = 0; t <= 2 * kR; t++) s += tap<T>(t) * sp[(long long)mirror64(y + t - kR, h) * w + x];
     dst[i] = s;
   }
 }
 
-// Transpose of k_vblur as a gather: row y' receives tap t from the rows y whose mirrored source row is y', i.e.
+// Transpose of the column blur as a gather: row y' receives tap t from the rows y whose mirrored source row is y', i.e.
 // from source index y' (y = y' - t + R), -y' - 1 (mirrored at the top) and 2h - 1 - y' (at the bottom).
+// `planes` consecutive planes of n samples in one sweep.
 template <typename T>
-__global__ void k_vblur_t(const T* __restrict__ g, int w, int h, T* __restrict__ dst) {
+__global__ void k_vblur_t(const T* __restrict__ gsrc, int w, int h, int planes, T* __restrict__ dst) {
   const long long n = (long long)w * h;
-  for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int yp = (int)(i / w), x = (int)(i % w);
+  for (long long i = tid1(); i < n * planes; i += (long long)gridDim.x * blockDim.x) {
+    const long long p = i / n, o = i - p * n;
+    const int yp = (int)(o / w), x = (int)(o % w);
+    const T* g = gsrc + p * n;
     T s = 0;
+    if (yp >= kR && yp < h - kR) {
+      // interior: only the direct source row is in range (the mirrored ones are not)
 #pragma unroll
-    for (int t = 0; t <= 2 * kR; t++) {
-      const int ys[3] = {yp - t + kR, -yp - 1 - t + kR, 2 * h - 1 - yp - t + kR};
+      for (int t = 0; t <= 2 * kR; t++) s += tap<T>(t) * g[(long long)(yp - t + kR) * w + x];
+    } else {
 #pragma unroll
-      for (int e = 0; e < 3; e++)
-        if (ys[e] >= 0 && ys[e] < h) s += tap<T>(t) * g[(long long)ys[e] * w + x];
+      for (int t = 0; t <= 2 * kR; t++) {
+        const int ys[3] = {yp - t + kR, -yp - 1 - t + kR, 2 * h - 1 - yp - t + kR};
+#pragma unroll
+        for (int e = 0; e < 3; e++)
+          if (ys[e] >= 0 && ys[e] < h) s += tap<T>(t) * g[(long long)ys[e] * w + x];
+      }
     }
     dst[i] = s;
   }
@@ -387,7 +413,7 @@ int grad_impl(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, int w, in
   T* pb = ws("pb", total);
   T* xa = ws("xa", 3 * n0);
   T* xb = ws("xb", 3 * n0);
-  T* hb = ws("hb", n0);
+  T* hb5 = ws("hb5", 5 * n0);  // row-blurred products (forward), column-blurred gradients (backward)
   T* mom = ws("mom", 5 * n0);
   T* gq = ws("gq", 3 * n0);  // g_m2, g_s22, g_s12
   T* tq = ws("tq", 3 * n0);  // their blur adjoints
@@ -395,7 +421,8 @@ int grad_impl(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, int w, in
   T* gl = ws("gl", total);   // d score / d linear, per scale
   double* sums = (double*)workspace(ctx, (pfx + "sums").c_str(), sizeof(double) * kMaxScales * 18);
   double* parts = (double*)workspace(ctx, (pfx + "parts").c_str(), sizeof(double) * 6 * grid_of(n0));
-  if (!pa || !pb || !xa || !xb || !hb || !mom || !gq || !tq || !gx || !gl || !sums || !parts) return RCG_NO_MEMORY;
+  if (!pa || !pb || !xa || !xb || !hb5 || !mom || !gq || !tq || !gx || !gl || !sums || !parts)
+    return RCG_NO_MEMORY;
   RCG_LAUNCH(ctx, "adj_lin", k_lin<T>, grid_of(n0), 256, 0, d_ref, d_dist, n0, pa, pb);
   for (int s = 1; s < ns; s++) {
     RCG_LAUNCH(ctx, "adj_down", k_down<T>, grid_of(3 * sc[s].n), 256, 0, pa + sc[s - 1].off, sc[s - 1].w,
@@ -406,11 +433,8 @@ int grad_impl(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, int w, in
   // forward: the moments and map sums of every scale
   auto moments = [&](int s, int c) {
     const long long n = sc[s].n;
-    for (int q = 0; q < 5; q++) {
-      RCG_LAUNCH(ctx, "adj_hblur", k_hblur<T>, grid_of(n), 256, 0, xa + c * n, xb + c * n, (const T*)nullptr, q,
-                 sc[s].w, sc[s].h, hb);
-      RCG_LAUNCH(ctx, "adj_vblur", k_vblur<T>, grid_of(n), 256, 0, hb, sc[s].w, sc[s].h, mom + q * n);
-    }
+    RCG_LAUNCH(ctx, "adj_hblur5", k_hblur5<T>, grid_of(n), 256, 0, xa + c * n, xb + c * n, sc[s].w, sc[s].h, hb5);
+    RCG_LAUNCH(ctx, "adj_vblur", k_vblur_n<T>, grid_of(5 * n), 256, 0, hb5, sc[s].w, sc[s].h, 5, mom);
   };
   for (int s = 0; s < ns; s++) {
     const long long n = sc[s].n;
@@ -476,11 +500,9 @@ int grad_impl(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, int w, in
       moments(s, c);  // recomputed, not stored
       RCG_LAUNCH(ctx, "adj_mapgrad", k_mapgrad<T>, grid_of(n), 256, 0, mom, xa + c * n, xb + c * n, n, nc, gq,
                  gq + n, gq + 2 * n, gx + c * n);
-      for (int j = 0; j < 3; j++) {
-        RCG_LAUNCH(ctx, "adj_vblur_t", k_vblur_t<T>, grid_of(n), 256, 0, gq + j * n, sc[s].w, sc[s].h, hb);
-        RCG_LAUNCH(ctx, "adj_hblur", k_hblur<T>, grid_of(n), 256, 0, (const T*)nullptr, (const T*)nullptr, hb, -1,
-                   sc[s].w, sc[s].h, tq + j * n);
-      }
+      // the three gradient planes through the transposed column blur, then the row blur (its own transpose)
+      RCG_LAUNCH(ctx, "adj_vblur_t", k_vblur_t<T>, grid_of(3 * n), 256, 0, gq, sc[s].w, sc[s].h, 3, hb5);
+      RCG_LAUNCH(ctx, "adj_hblur", k_hblur<T>, grid_of(3 * n), 256, 0, hb5, sc[s].w, sc[s].h, 3, tq);
       RCG_LAUNCH(ctx, "adj_combine", k_combine<T>, grid_of(n), 256, 0, tq, tq + n, tq + 2 * n, xa + c * n,
                  xb + c * n, n, gx + c * n);
     }
