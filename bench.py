@@ -198,6 +198,50 @@ def scorer_alone(ctx, stream, timed, torch, dev, peaks, with_oracle=True, w=3840
     return out
 
 
+def scorer_batch_workload(ctx, torch, dev, timed, n=64, steps=5):
+    """SSIMULACRA2 of many pairs of uneven sizes: the batch workload's images (seeds 2..2+n-1, log-uniform
+    640x480..6000x4000) against their q50 4:2:0 JPEG round trips (the bit-exact GPU codec). Device-resident pairs
+    (inputs far larger than L2); one rcg_ssimulacra2_batch_device call against n rcg_ssimulacra2_device calls."""
+    import rcg
+    import rcg.synth as synth
+
+    sizes = synth.log_uniform_sizes(2, n)
+    imgs = synth.images([(w, h, 2 + i, 0.0) for i, (w, h) in enumerate(sizes)])
+    o50 = rcg.EncodeOptions(50, rcg.Subsampling.S420, True)
+    d_r = [torch.from_numpy(im).to(dev) for im in imgs]
+    d_d = [torch.from_numpy(ctx.reconstruct(ctx.build_coefs(im, o50))).to(dev) for im in imgs]
+    del imgs
+    torch.cuda.synchronize()
+    ws, hs = [w for w, _ in sizes], [h for _, h in sizes]
+    rp, dp = [t.data_ptr() for t in d_r], [t.data_ptr() for t in d_d]
+
+    def batch():
+        return ctx.ssimulacra2_batch_device(rp, dp, ws, hs, [3] * n)
+
+    def one_by_one():
+        return [ctx.ssimulacra2_device(a, b, w, h, 3) for a, b, w, h in zip(rp, dp, ws, hs)]
+
+    for _ in range(3):
+        batch()
+        one_by_one()
+    tb, sb = timed(batch, steps)
+    tp, sp = timed(one_by_one, steps)
+    mpx = sum(w * h for w, h in sizes) / 1e6
+    ctx.set_profiling(True)
+    batch()
+    kb = {k: ctx.kernel_time(k)[1] for k in ("to_linear_batch", "pyramid_batch", "ssim2_tiles_batch",
+                                             "ssim2_reduce_batch")}
+    ctx.set_profiling(False)
+    del d_r, d_d
+    torch.cuda.empty_cache()
+    ms_b, ms_p = sum(tb) / len(tb), sum(tp) / len(tp)
+    return {"workload": f"{n} pairs, log-uniform 640x480..6000x4000 ({mpx:.0f} MP), distorted = q50 4:2:0 round trip",
+            "pairs": n, "megapixels": mpx, "batch_ms": ms_b, "one_by_one_ms": ms_p,
+            "batch_mpx_per_s": mpx / (ms_b / 1000.0), "one_by_one_mpx_per_s": mpx / (ms_p / 1000.0),
+            "batch_vs_one_by_one": ms_p / ms_b, "identical_scores": [float(x) for x in sb] == sp,
+            "batch_kernels_ms": kb, "launches_per_batch": 4}
+
+
 def batch_workload(ctx, torch, n=64, parallel=8, steps=2, perceptual=True):
     """Many images of uneven sizes (seeds 2..2+n-1, log-uniform 640x480..6000x4000, aspect 4:3/3:2/16:9/1:1), each
     with its own target drawn uniformly from 55..85: plain searches one after another (rcg_search) against the
@@ -471,6 +515,8 @@ def plan_workload(ctx, timed, d_coefs, lay, with_oracle=True, steps=10):
 
 def kernel_case(name):
     """A handful of launches of one workload on the W x H image (for ncu captures of a single kernel)."""
+    import numpy as np
+
     import rcg
     import rcg.synth as synth
 
@@ -480,6 +526,13 @@ def kernel_case(name):
     if name == "plan":
         for _ in range(2):
             ctx.plan(ci)
+    elif name == "ssim2_batch":
+        # the W x H pair plus three smaller crops of it, four times over, in one work-list call per repetition
+        dist = ctx.reconstruct(ci)
+        pairs = [(img, dist)] + [(np.ascontiguousarray(img[: H // k, : W // k]),
+                                  np.ascontiguousarray(dist[: H // k, : W // k])) for k in (2, 3, 5)]
+        for _ in range(2):
+            ctx.ssimulacra2_batch(pairs * 4)
     elif name == "perceptual":
         # one perceptual search (plain search, FP64 adjoint, pullback, weighted search, two plans)
         ctx.find_quality_perceptual(img, TARGET, 100, rcg.EncodeOptions(90, rcg.Subsampling.S420, True))
@@ -501,7 +554,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the many-image batch measurement")
     ap.add_argument("--no-requant", action="store_true", help="skip the JPEG->JPEG search measurement")
     ap.add_argument("--no-perceptual", action="store_true", help="skip the perceptual trellis measurement")
-    ap.add_argument("--kernel-case", choices=["plan", "ssim", "ssim2", "perceptual"], default=None,
+    ap.add_argument("--kernel-case", choices=["plan", "ssim", "ssim2", "ssim2_batch", "perceptual"], default=None,
                     help="profiling aid: run only a few calls of one workload at --width x --height, print nothing")
     ap.add_argument("--width", type=int, default=W, help="smaller cases for profiling only; the bench line uses 4000")
     ap.add_argument("--height", type=int, default=H)
@@ -621,8 +674,10 @@ def main():
     if rank == 0 and not args.no_batch:
         batch = batch_workload(ctx, torch, perceptual=not args.no_perceptual)
     scorer = None
+    scorer_batch = None
     if rank == 0 and not args.no_scorer:
         scorer = scorer_alone(ctx, stream, timed, torch, dev, peaks, with_oracle=not args.no_cpu_baseline)
+        scorer_batch = scorer_batch_workload(ctx, torch, dev, timed)
     plan = None
     if rank == 0:
         lay_found = ctx.coef_layout(W, H, 3, rcg.EncodeOptions(res[0], opts.subsampling, opts.trellis))
@@ -673,6 +728,7 @@ def main():
             "kernels_ms_per_search": {k: v["ms"] / 3 for k, v in prof.items() if v["launches"]},
             "scorer_mpx_per_s": (W * H / 1e6) / (tile_ms / 1000.0),
             "scorer_alone": scorer,
+            "scorer_batch": scorer_batch,
             "batch": batch,
             "requantize": requant,
             "write_best_plan": plan,

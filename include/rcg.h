@@ -128,6 +128,15 @@ uint64_t rcg_ctx_launch_count(const rcg_ctx* ctx);
 int rcg_ctx_set_profiling(rcg_ctx* ctx, int on);
 /* Accumulated event time of kernel `name` since profiling was switched on. Synchronizes the context. */
 int rcg_ctx_kernel_time(rcg_ctx* ctx, const char* name, uint64_t* launches, double* total_ms);
+/* CUDA graphs for the device searches' step loops (rcg_search*, rcg_search_requantize*): 1 on (the default), 0 off.
+ * The bisection is decided on the device, so a search's launches depend only on the image shape, the options and
+ * the context's buffers. The second search of a shape on a context is captured; later ones replay it, one graph
+ * launch per search. Results are the same either way. Graphs are not used while profiling is on, on the legacy
+ * default stream, or while the caller captures the context's stream. Replaces nothing in the reference (a rayon
+ * CPU loop has no launches to batch). Synchronizes the context. */
+int rcg_ctx_set_graphs(rcg_ctx* ctx, int on);
+/* Step loops captured into graphs, and graph launches, on this context so far. */
+int rcg_ctx_graph_stats(const rcg_ctx* ctx, uint64_t* captures, uint64_t* replays);
 
 /* Coefficient layout for an image and options. Replaces nothing in the reference: it sizes the caller-allocated
  * output buffers that a Rust `Vec<i16>` would otherwise grow (jpeg/src/encode.rs:440-517). */
@@ -142,6 +151,21 @@ int rcg_ssimulacra2(rcg_ctx* ctx, const uint8_t* reference, const uint8_t* disto
 /* The same on device buffers (8-bit Gray/Rgb only); no host<->device copies besides the 8-byte score. */
 int rcg_ssimulacra2_device(rcg_ctx* ctx, const uint8_t* d_reference, const uint8_t* d_distorted, uint32_t width,
                            uint32_t height, int channels, double* score);
+/* n calls of rc_core::ssimulacra2::ssimulacra2 (core/src/ssimulacra2.rs:471), one per pair, as a caller scoring many
+ * files or many candidates does (cli/tests/ssimulacra2.rs:12-31 loops over 54 fixture pairs of different sizes;
+ * cli/src/pipeline.rs:130-138 scores each candidate of each file). Pairs may differ in size and format
+ * (widths/heights/channels/depths per pair; depths NULL = all 8-bit). All pairs go through one launch per stage
+ * over a work-list of every pair's tiles; pairs that pass the same reference buffer with the same size and format
+ * share one conversion of it. scores[i] equals what rcg_ssimulacra2 gives for pair i. Errors as rcg_ssimulacra2,
+ * naming the first pair at fault; scores of every pair are written even when one of them is not finite (NaN there,
+ * RCG_INVALID returned). n = 0 does nothing. */
+int rcg_ssimulacra2_batch(rcg_ctx* ctx, int n, const uint8_t* const* references, const uint8_t* const* distorted,
+                          const uint32_t* widths, const uint32_t* heights, const int* channels, const int* depths,
+                          double* scores);
+/* The same with device images (arrays of device pointers, sizes and scores on the host). */
+int rcg_ssimulacra2_batch_device(rcg_ctx* ctx, int n, const uint8_t* const* d_references,
+                                 const uint8_t* const* d_distorted, const uint32_t* widths, const uint32_t* heights,
+                                 const int* channels, const int* depths, double* scores);
 
 /* SSIMULACRA 2 of two 8-bit Gray/Rgb images already on the device, for callers that cannot allocate device memory:
  * this call allocates nothing. No counterpart in the reference (which has no device memory at all); it exists for

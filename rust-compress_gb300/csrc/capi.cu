@@ -7,10 +7,13 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
 #include <string>
 #include <thread>
+#include <tuple>
+#include <vector>
 #include <atomic>
 #include <numeric>
 
@@ -48,7 +51,108 @@ void* workspace(rcg_ctx* ctx, const char* name, size_t bytes) {
   }
   cudaMemsetAsync(b.ptr, 0, sz, ctx->stream);
   b.bytes = sz;
+  ctx->ws_gen++;
   return b.ptr;
+}
+
+// ------------------------------------------------------------------------------------------------ step-loop graphs
+
+constexpr size_t kMaxGraphs = 4;  // per context; the least recently used one goes first
+
+void drop_graphs(rcg_ctx* ctx) {
+  for (auto& g : ctx->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  ctx->graphs.clear();
+  ctx->warm.clear();
+}
+
+int run_step_loop(rcg_ctx* ctx, const std::vector<long long>& key, const std::function<void()>& issue) {
+  bool can = ctx->use_graphs && !ctx->profiling && ctx->stream != nullptr && ctx->stream != cudaStreamLegacy &&
+             ctx->stream != cudaStreamPerThread;
+  if (can) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess) {
+      cudaGetLastError();
+      can = false;
+    } else if (cs != cudaStreamCaptureStatusNone) {
+      can = false;  // the caller is capturing our launches into its own graph
+    }
+  }
+  if (!can) {
+    issue();
+    return RCG_OK;
+  }
+  for (size_t i = 0; i < ctx->graphs.size();) {  // graphs of reallocated workspace point at freed memory
+    if (ctx->graphs[i].gen != ctx->ws_gen) {
+      cudaGraphExecDestroy(ctx->graphs[i].exec);
+      ctx->graphs.erase(ctx->graphs.begin() + (long)i);
+    } else {
+      i++;
+    }
+  }
+  for (auto& g : ctx->graphs) {
+    if (g.key != key) continue;
+    cudaError_t e = cudaGraphLaunch(g.exec, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "graph launch of a search loop");
+    g.last_use = ++ctx->graph_tick;
+    ctx->launches += g.launches;
+    ctx->graph_replays++;
+    return RCG_OK;
+  }
+  auto seen = std::find_if(ctx->warm.begin(), ctx->warm.end(), [&](const auto& w) { return w.first == key; });
+  if (seen == ctx->warm.end() || seen->second != ctx->ws_gen) {
+    // First sight of this key with these buffers: plain launches. A one-off shape (a batch of many sizes) never
+    // pays for a capture.
+    if (seen != ctx->warm.end()) ctx->warm.erase(seen);
+    issue();
+    if (ctx->warm.size() >= 2 * kMaxGraphs) ctx->warm.erase(ctx->warm.begin());
+    ctx->warm.emplace_back(key, ctx->ws_gen);
+    return RCG_OK;
+  }
+  ctx->warm.erase(seen);
+  const uint64_t gen0 = ctx->ws_gen, l0 = ctx->launches;
+  cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    issue();
+    return RCG_OK;
+  }
+  issue();
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(ctx->stream, &graph);
+  const uint64_t n = ctx->launches - l0;
+  ctx->launches = l0;
+  cudaGraphExec_t exec = nullptr;
+  if (e == cudaSuccess && ctx->ws_gen != gen0) e = cudaErrorStreamCaptureInvalidated;  // workspace moved meanwhile
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    if (exec) cudaGraphExecDestroy(exec);
+    issue();  // a capture runs nothing: issue the loop as plain launches instead
+    return RCG_OK;
+  }
+  if (ctx->graphs.size() >= kMaxGraphs) {
+    auto lru = std::min_element(ctx->graphs.begin(), ctx->graphs.end(),
+                                [](const rcg_ctx::StepGraph& a, const rcg_ctx::StepGraph& b) {
+                                  return a.last_use < b.last_use;
+                                });
+    cudaGraphExecDestroy(lru->exec);
+    ctx->graphs.erase(lru);
+  }
+  rcg_ctx::StepGraph g;
+  g.key = key;
+  g.gen = gen0;
+  g.exec = exec;
+  g.launches = n;
+  g.last_use = ++ctx->graph_tick;
+  ctx->graphs.push_back(g);
+  ctx->graph_captures++;
+  e = cudaGraphLaunch(exec, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "graph launch of a search loop");
+  ctx->launches += n;
+  ctx->graph_replays++;
+  return RCG_OK;
 }
 
 void launch_begin(rcg_ctx* ctx, const char* name, cudaEvent_t* a, cudaEvent_t* b) {
@@ -412,6 +516,7 @@ void rcg_ctx_destroy(rcg_ctx* ctx) {
   ctx->workers.clear();
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  drop_graphs(ctx);
   for (auto& kv : ctx->bufs)
     if (kv.second.ptr) cudaFree(kv.second.ptr);
   if (ctx->lut16) cudaFree(ctx->lut16);
@@ -450,6 +555,22 @@ int rcg_ctx_set_profiling(rcg_ctx* ctx, int on) {
   collect_times(ctx);
   ctx->profiling = on != 0;
   if (on) ctx->ktimes.clear();
+  return RCG_OK;
+}
+
+int rcg_ctx_set_graphs(rcg_ctx* ctx, int on) {
+  if (!ctx) return RCG_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->use_graphs = on != 0;
+  if (!on) drop_graphs(ctx);
+  return RCG_OK;
+}
+
+int rcg_ctx_graph_stats(const rcg_ctx* ctx, uint64_t* captures, uint64_t* replays) {
+  if (!ctx) return RCG_INVALID;
+  if (captures) *captures = ctx->graph_captures;
+  if (replays) *replays = ctx->graph_replays;
   return RCG_OK;
 }
 
@@ -521,6 +642,96 @@ int rcg_ssimulacra2_device(rcg_ctx* ctx, const uint8_t* d_reference, const uint8
     return fail(ctx, RCG_INVALID, "SSIMULACRA 2 needs at least 8x8 pixels");
   cudaSetDevice(ctx->device);
   return score_device_images(ctx, d_reference, d_distorted, (int)width, (int)height, channels, 8, score);
+}
+
+// ---- many pairs at once
+
+static int check_pairs(rcg_ctx* ctx, int n, const void* a, const void* b, const uint32_t* widths,
+                       const uint32_t* heights, const int* channels, const int* depths, const double* scores) {
+  if (n < 0 || n > 65535) return fail(ctx, RCG_INVALID, "a batch holds 0..=65535 pairs");
+  if (n > 0 && (!a || !b || !widths || !heights || !channels || !scores)) return fail(ctx, RCG_INVALID, "null pointer");
+  for (int i = 0; i < n; i++) {
+    const int depth = depths ? depths[i] : 8;
+    if (channels[i] < 1 || channels[i] > 4 || (depth != 8 && depth != 16))
+      return fail(ctx, RCG_INVALID, "pair " + std::to_string(i) + ": channels must be 1..4 and depth 8 or 16");
+    if (widths[i] < (uint32_t)kMinSide || heights[i] < (uint32_t)kMinSide)
+      return fail(ctx, RCG_INVALID, "pair " + std::to_string(i) + ": SSIMULACRA 2 needs at least 8x8 pixels");
+  }
+  return RCG_OK;
+}
+
+static int batch_scores_out(rcg_ctx* ctx, int n, const double* d_scores, double* scores) {
+  int rc = copy_to_host(ctx, scores, d_scores, (size_t)n * sizeof(double));
+  if (rc != RCG_OK) return rc;
+  if ((rc = finish(ctx, "ssimulacra2 batch")) != RCG_OK) return rc;
+  for (int i = 0; i < n; i++)
+    if (!std::isfinite(scores[i]))
+      return fail(ctx, RCG_INVALID, "pair " + std::to_string(i) + ": SSIMULACRA 2 produced a non-finite score");
+  return RCG_OK;
+}
+
+int rcg_ssimulacra2_batch_device(rcg_ctx* ctx, int n, const uint8_t* const* d_references,
+                                 const uint8_t* const* d_distorted, const uint32_t* widths, const uint32_t* heights,
+                                 const int* channels, const int* depths, double* scores) {
+  if (!ctx) return RCG_INVALID;
+  int rc = check_pairs(ctx, n, d_references, d_distorted, widths, heights, channels, depths, scores);
+  if (rc != RCG_OK || n == 0) return rc;
+  for (int i = 0; i < n; i++)
+    if (!d_references[i] || !d_distorted[i]) return fail(ctx, RCG_INVALID, "null pointer");
+  cudaSetDevice(ctx->device);
+  double* d_scores = nullptr;
+  if ((rc = score_batch(ctx, n, d_references, d_distorted, widths, heights, channels, depths, &d_scores)) != RCG_OK)
+    return rc;
+  return batch_scores_out(ctx, n, d_scores, scores);
+}
+
+int rcg_ssimulacra2_batch(rcg_ctx* ctx, int n, const uint8_t* const* references, const uint8_t* const* distorted,
+                          const uint32_t* widths, const uint32_t* heights, const int* channels, const int* depths,
+                          double* scores) {
+  if (!ctx) return RCG_INVALID;
+  int rc = check_pairs(ctx, n, references, distorted, widths, heights, channels, depths, scores);
+  if (rc != RCG_OK || n == 0) return rc;
+  for (int i = 0; i < n; i++)
+    if (!references[i] || !distorted[i]) return fail(ctx, RCG_INVALID, "null pointer");
+  cudaSetDevice(ctx->device);
+  // One device copy per distinct host image: pairs that pass the same reference buffer (several candidates of one
+  // image) upload it once and share its planes in the scorer.
+  auto bytes_of = [&](int i) {
+    return (size_t)widths[i] * heights[i] * channels[i] * ((depths ? depths[i] : 8) / 8);
+  };
+  std::map<std::tuple<const uint8_t*, uint32_t, uint32_t, int, int>, size_t> ref_off;
+  std::vector<size_t> roff((size_t)n), doff((size_t)n);
+  size_t total = 0;
+  auto take = [&](size_t b) {
+    size_t o = total;
+    total += (b + 255) / 256 * 256;
+    return o;
+  };
+  for (int i = 0; i < n; i++) {
+    auto key = std::make_tuple(references[i], widths[i], heights[i], channels[i], depths ? depths[i] : 8);
+    auto it = ref_off.find(key);
+    if (it == ref_off.end()) it = ref_off.emplace(key, take(bytes_of(i))).first;
+    roff[(size_t)i] = it->second;
+    doff[(size_t)i] = take(bytes_of(i));
+  }
+  uint8_t* d_imgs = (uint8_t*)workspace(ctx, "batch_imgs", total);
+  if (!d_imgs) return RCG_NO_MEMORY;
+  std::vector<const uint8_t*> d_ref((size_t)n), d_dist((size_t)n);
+  std::vector<char> sent(total / 256 + 1, 0);
+  for (int i = 0; i < n; i++) {
+    d_ref[(size_t)i] = d_imgs + roff[(size_t)i];
+    d_dist[(size_t)i] = d_imgs + doff[(size_t)i];
+    if (!sent[roff[(size_t)i] / 256]) {
+      sent[roff[(size_t)i] / 256] = 1;
+      if ((rc = copy_to_device(ctx, d_imgs + roff[(size_t)i], references[i], bytes_of(i))) != RCG_OK) return rc;
+    }
+    if ((rc = copy_to_device(ctx, d_imgs + doff[(size_t)i], distorted[i], bytes_of(i))) != RCG_OK) return rc;
+  }
+  double* d_scores = nullptr;
+  if ((rc = score_batch(ctx, n, d_ref.data(), d_dist.data(), widths, heights, channels, depths, &d_scores)) !=
+      RCG_OK)
+    return rc;
+  return batch_scores_out(ctx, n, d_scores, scores);
 }
 
 // ---- other metrics
@@ -772,18 +983,24 @@ struct SearchScorer {
   double* d_score = nullptr;
 };
 
+// Every buffer the per-candidate scoring uses is allocated here, before the step loop: the loop itself never
+// allocates (it may be captured as a graph, and a failed allocation inside it would go unnoticed).
 static int scorer_setup(rcg_ctx* ctx, int metric, int w, int h, int channels, SearchScorer* sc) {
   sc->metric = metric;
   sc->d_score = (double*)workspace(ctx, "score", sizeof(double));
   if (!sc->d_score) return RCG_NO_MEMORY;
   if (metric == RCG_METRIC_SSIM) {
     sc->cand_px = (uint8_t*)workspace(ctx, "cand_px", (size_t)w * h * channels);
-    return sc->cand_px ? RCG_OK : RCG_NO_MEMORY;
+    if (!sc->cand_px) return RCG_NO_MEMORY;
+    if (w >= 8 && h >= 8 && !workspace(ctx, "ssim_rows", sizeof(double) * (size_t)((h - 8) / 4 + 1)))
+      return RCG_NO_MEMORY;
+    return RCG_OK;
   }
   sc->pd = make_pyramid(w, h);
   sc->ref_pyr = (float*)workspace(ctx, "ref_pyr", (size_t)sc->pd.floats * sizeof(float));
   sc->dist_pyr = (float*)workspace(ctx, "dist_pyr", (size_t)sc->pd.floats * sizeof(float));
-  return sc->ref_pyr && sc->dist_pyr ? RCG_OK : RCG_NO_MEMORY;
+  if (!sc->ref_pyr || !sc->dist_pyr) return RCG_NO_MEMORY;
+  return score_workspace(ctx, sc->pd);
 }
 
 // Decoded planes of one candidate -> score -> one bisection step (all gated by the step's `active`).
@@ -840,14 +1057,20 @@ static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int cha
   hs.channels = channels;
   hs.best_q = max_q;
   cudaMemcpyAsync(d_ss, &hs, sizeof hs, cudaMemcpyHostToDevice, ctx->stream);
-  for (int s = 0; s < max_steps; s++) {
-    step_tables(ctx, d_ss, d_st, w, h, slots, es.max_coefs, d_weights);
-    quantize(ctx, d_st, es.caches, es.max_blocks);
-    rate_tables(ctx, d_st);
-    trellis(ctx, d_st, es.caches, es.max_blocks, d_weights != nullptr);
-    dequant_idct(ctx, d_st, nullptr, planes, es.max_blocks);
-    score_candidate(ctx, sc, d_st, planes, w, h, channels, d_ss);
-  }
+  // Every launch below takes pointers into this context's workspace and sizes that follow from the key.
+  const std::vector<long long> key = {1, (long long)(uintptr_t)d_src, w, h, channels, metric, subsampling, trellis_on,
+                                      max_steps, (long long)(uintptr_t)d_weights};
+  rc = run_step_loop(ctx, key, [&]() {
+    for (int s = 0; s < max_steps; s++) {
+      step_tables(ctx, d_ss, d_st, w, h, slots, es.max_coefs, d_weights);
+      quantize(ctx, d_st, es.caches, es.max_blocks);
+      rate_tables(ctx, d_st);
+      trellis(ctx, d_st, es.caches, es.max_blocks, d_weights != nullptr);
+      dequant_idct(ctx, d_st, nullptr, planes, es.max_blocks);
+      score_candidate(ctx, sc, d_st, planes, w, h, channels, d_ss);
+    }
+  });
+  if (rc != RCG_OK) return rc;
   cudaMemcpyAsync(&hs, d_ss, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream);
   if ((rc = finish(ctx, "search")) != RCG_OK) return rc;
   if (!hs.done) return fail(ctx, RCG_TIMEOUT, "bisection did not finish within the step budget");
@@ -1096,13 +1319,25 @@ static int search_requantize_impl(rcg_ctx* ctx, uint32_t width, uint32_t height,
   hs.best_q = max_q;
   cudaMemcpyAsync(d_ss, &hs, sizeof hs, cudaMemcpyHostToDevice, ctx->stream);
   const float* no_caches[9] = {nullptr};
-  for (int s = 0; s < max_steps; s++) {
-    step_tables_requant(ctx, d_ss, d_st, slots, nblocks * 64);
-    requantize_plain(ctx, d_st, nblocks);
-    rate_tables(ctx, d_st);
-    rcg::trellis(ctx, d_st, no_caches, nblocks);
-    dequant_idct(ctx, d_st, nullptr, planes, nblocks);
-    score_candidate(ctx, sc, d_st, planes, w, h, channels, d_ss);
+  std::vector<long long> key = {2, (long long)(uintptr_t)d_src, w, h, st->ncomp, metric, trellis, max_steps,
+                                st->hmax, st->vmax, nblocks};
+  for (int c = 0; c < st->ncomp; c++) {
+    const CompDesc& cd = st->comp[c];
+    key.insert(key.end(), {cd.bw, cd.bh, cd.h, cd.v, cd.blk0, cd.plane_off});
+  }
+  rc = run_step_loop(ctx, key, [&]() {
+    for (int s = 0; s < max_steps; s++) {
+      step_tables_requant(ctx, d_ss, d_st, slots, nblocks * 64);
+      requantize_plain(ctx, d_st, nblocks);
+      rate_tables(ctx, d_st);
+      rcg::trellis(ctx, d_st, no_caches, nblocks);
+      dequant_idct(ctx, d_st, nullptr, planes, nblocks);
+      score_candidate(ctx, sc, d_st, planes, w, h, channels, d_ss);
+    }
+  });
+  if (rc != RCG_OK) {
+    delete st;
+    return rc;
   }
   cudaMemcpyAsync(&hs, d_ss, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream);
   if ((rc = finish(ctx, "search_requantize")) != RCG_OK) {

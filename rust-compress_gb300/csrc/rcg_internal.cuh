@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <map>
 #include <string>
 #include <vector>
@@ -174,6 +175,22 @@ struct rcg_ctx {
   size_t pinned_in_bytes = 0;
   void* pinned_out = nullptr;
   size_t pinned_out_bytes = 0;
+  // Step loops of the device searches captured as CUDA graphs (capi.cu, run_step_loop). A loop's launches and their
+  // arguments follow from the image shape, the options and the workspace pointers, so the key holds the first two
+  // and ws_gen stands for the third: every workspace (re)allocation bumps it and makes older graphs stale.
+  struct StepGraph {
+    std::vector<long long> key;
+    uint64_t gen = 0;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t launches = 0;  // kernels per replay
+    uint64_t last_use = 0;
+  };
+  std::vector<StepGraph> graphs;
+  bool use_graphs = true;
+  uint64_t ws_gen = 0;
+  // Loops run as plain launches lately (key, ws_gen): captured when one comes again with the same ws_gen.
+  std::vector<std::pair<std::vector<long long>, uint64_t>> warm;
+  uint64_t graph_tick = 0, graph_captures = 0, graph_replays = 0;
 };
 
 namespace rcg {
@@ -195,6 +212,15 @@ int copy_to_host(rcg_ctx* ctx, void* dst, const void* src, size_t bytes);
 void launch_begin(rcg_ctx* ctx, const char* name, cudaEvent_t* a, cudaEvent_t* b);
 void launch_end(rcg_ctx* ctx, const char* name, cudaEvent_t a, cudaEvent_t b);
 void collect_times(rcg_ctx* ctx);
+
+// Issue a device search's step loop (`issue` launches every step's kernels on ctx->stream). With graphs on, the
+// first loop of a key runs as plain launches (it may allocate workspace), the next one with the same key is
+// captured and replayed, and later ones replay the stored graph: one graph launch per search instead of ~10
+// kernel launches per step. Plain launches whenever profiling is on, the stream is the legacy default stream, or
+// the caller is capturing the stream itself.
+int run_step_loop(rcg_ctx* ctx, const std::vector<long long>& key, const std::function<void()>& issue);
+// Release the context's stored graphs.
+void drop_graphs(rcg_ctx* ctx);
 
 #define RCG_LAUNCH(ctx, name, kernel, grid, block, smem, ...)                     \
   do {                                                                            \
@@ -224,6 +250,13 @@ int build_pyramid_gated(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, const
 // `search` is non-null the final kernel also advances the device-side bisection.
 int score_pyramids(rcg_ctx* ctx, const PyramidDesc& pd, const float* d_ref, const float* d_dist, double* d_score,
                    SearchState* search, StepDesc* step);
+// Allocate (or find) the scratch score_pyramids uses for a pyramid of this geometry.
+int score_workspace(rcg_ctx* ctx, const PyramidDesc& pd);
+// Score n device-resident pairs (checked sizes and formats; depths nullable = 8) with the work-list kernels;
+// *d_scores receives the device array of the n scores (NaN where a score is not finite), ready once the stream is.
+int score_batch(rcg_ctx* ctx, int n, const uint8_t* const* d_refs, const uint8_t* const* d_dists,
+                const uint32_t* widths, const uint32_t* heights, const int* channels, const int* depths,
+                double** d_scores);
 
 // ---- codec (codec.cu)
 // Colour conversion + edge padding (jpeg/src/encode.rs:463-477): full-resolution padded Y/Cb/Cr planes.

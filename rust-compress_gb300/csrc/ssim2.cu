@@ -27,7 +27,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
+#include <vector>
 
 #include "rcg_internal.cuh"
 
@@ -134,20 +137,15 @@ constexpr size_t kTileSmem = (size_t)(6 * kIH * kIW + 5 * kIH * kTileW) * sizeof
 // 5-pixel halo; then per channel the horizontally blurred five moments of the 42 halo rows. The blurs run the
 // moment pairs that share a tap weight ((a', d'), (a'^2, b'^2)) as packed two-lane f32 FMAs, each lane exactly
 // fmaf, so the results are those of scalar FMAs in the same order.
-__global__ void __launch_bounds__(kTileThreads, 3)
-    k_ssim2_tiles(PyramidDesc pd, const float* __restrict__ ref, const float* __restrict__ dist,
-                  double* __restrict__ partials, const StepDesc* __restrict__ st) {
-  if (st && !st->active) return;
+// Tile `local` of scale `sd` of a pyramid pair; the tile's 18 sums go to out[i * stride], i < 18.
+__device__ __forceinline__ void ssim2_tile(const ScaleDesc sd, const int local, const float* __restrict__ ref,
+                                           const float* __restrict__ dist, double* __restrict__ out,
+                                           const size_t stride) {
   extern __shared__ float smem[];
   float2* xs = reinterpret_cast<float2*>(smem);  // [3][kIH][kIW] pairs (a', d') per channel
   float* hb = smem + 6 * kIH * kIW;              // pair planes (m0, m1), (m2, m3) then m4, [kIH][kTileW] each
   __shared__ float s_red[kTileThreads / 32][kScoreSums];
 
-  int blk = blockIdx.x;
-  int s = 0;
-  while (s + 1 < pd.nscales && blk >= pd.s[s + 1].tile0) s++;
-  const ScaleDesc sd = pd.s[s];
-  const int local = blk - sd.tile0;
   const int tx = local % sd.tiles_x, ty = local / sd.tiles_x;
   const int x0 = tx * kTileW, y0 = ty * kTileH;
   const int w = sd.w, h = sd.h;
@@ -383,17 +381,27 @@ __global__ void __launch_bounds__(kTileThreads, 3)
   if (tid < kScoreSums) {
     double acc = 0.0;
     for (int wi = 0; wi < kTileThreads / 32; wi++) acc += (double)s_red[wi][tid];
-    partials[(size_t)tid * pd.total_tiles + blk] = acc;  // sum-major: the reduction reads each sum contiguously
+    out[(size_t)tid * stride] = acc;  // sum-major: the reduction reads each sum contiguously
   }
+}
+
+__global__ void __launch_bounds__(kTileThreads, 3)
+    k_ssim2_tiles(PyramidDesc pd, const float* __restrict__ ref, const float* __restrict__ dist,
+                  double* __restrict__ partials, const StepDesc* __restrict__ st) {
+  if (st && !st->active) return;
+  const int blk = blockIdx.x;
+  int s = 0;
+  while (s + 1 < pd.nscales && blk >= pd.s[s + 1].tile0) s++;
+  const ScaleDesc sd = pd.s[s];
+  ssim2_tile(sd, blk - sd.tile0, ref, dist, partials + blk, (size_t)pd.total_tiles);
 }
 
 // Deterministic reduction of the per-tile sums: CTA (scale, sum index); the last CTA to finish computes the score
 // (core/src/ssimulacra2.rs:457-511) and, in a search, advances the bisection (jpeg/src/target.rs:29-56).
-__global__ void __launch_bounds__(256) k_ssim2_reduce(PyramidDesc pd, const double* __restrict__ partials,
-                                                      double* __restrict__ scale_sums, unsigned* __restrict__ counter,
-                                                      double* __restrict__ score_out, SearchState* __restrict__ ss,
-                                                      const StepDesc* __restrict__ st) {
-  if (st && !st->active) return;
+// CTA (scale blockIdx.x, sum blockIdx.y) of one score; the last of its nscales x 18 CTAs maps the sums.
+__device__ __forceinline__ void reduce_scale_sum(const PyramidDesc& pd, const double* __restrict__ partials,
+                                                 double* __restrict__ scale_sums, unsigned* __restrict__ counter,
+                                                 double* __restrict__ score_out, SearchState* __restrict__ ss) {
   __shared__ double red[8];
   __shared__ bool last;
   const int s = blockIdx.x, i = blockIdx.y;
@@ -412,7 +420,7 @@ __global__ void __launch_bounds__(256) k_ssim2_reduce(PyramidDesc pd, const doub
     scale_sums[s * kScoreSums + i] = tot;
     __threadfence();
     unsigned prev = atomicAdd(counter, 1u);
-    last = prev == gridDim.x * gridDim.y - 1;
+    last = prev == (unsigned)(pd.nscales * kScoreSums) - 1;
   }
   __syncthreads();
   if (!last) return;
@@ -443,19 +451,25 @@ __global__ void __launch_bounds__(256) k_ssim2_reduce(PyramidDesc pd, const doub
   if (ss) search_record(ss, finite ? score : -1.7976931348623157e308);
 }
 
+__global__ void __launch_bounds__(256) k_ssim2_reduce(PyramidDesc pd, const double* __restrict__ partials,
+                                                      double* __restrict__ scale_sums, unsigned* __restrict__ counter,
+                                                      double* __restrict__ score_out, SearchState* __restrict__ ss,
+                                                      const StepDesc* __restrict__ st) {
+  if (st && !st->active) return;
+  reduce_scale_sum(pd, partials, scale_sums, counter, score_out, ss);
+}
+
 // ------------------------------------------------------------------------------------------------ planes, pyramid
 
 // Linear planes of an interleaved image (core/src/ssimulacra2.rs:177-221, with core/src/image.rs:143-190 for alpha:
 // 16-bit samples rounded to 8 bits, then composited onto mid-grey 128). Four consecutive pixels per thread (in
 // row-major order; the planes are contiguous [3][h][w]) so each thread moves enough bytes per request.
-__global__ void k_to_linear(const uint8_t* __restrict__ img, int w, int h, int channels, int depth,
-                            const float* __restrict__ lut16, float* __restrict__ out) {
-  // The table lives in shared memory: per-thread indices differ, which would serialize constant-memory reads.
-  __shared__ float lut8[256];
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) lut8[i] = c_lut8s[i];
-  __syncthreads();
+// CTA `cta` of an image's 4-pixel groups; lut8: the 8-bit table in shared memory.
+__device__ __forceinline__ void to_linear_groups(const uint8_t* __restrict__ img, int w, int h, int channels, int depth,
+                                                 const float* __restrict__ lut16, float* __restrict__ out,
+                                                 size_t cta, const float* lut8) {
   const size_t np = (size_t)w * h;
-  const size_t i0 = 4 * ((size_t)blockIdx.x * blockDim.x + threadIdx.x);
+  const size_t i0 = 4 * (cta * blockDim.x + threadIdx.x);
   if (i0 >= np) return;
   const int n = (int)min((size_t)4, np - i0);
   float v[3][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
@@ -527,6 +541,15 @@ __global__ void k_to_linear(const uint8_t* __restrict__ img, int w, int h, int c
   }
 }
 
+__global__ void k_to_linear(const uint8_t* __restrict__ img, int w, int h, int channels, int depth,
+                            const float* __restrict__ lut16, float* __restrict__ out) {
+  // The table lives in shared memory: per-thread indices differ, which would serialize constant-memory reads.
+  __shared__ float lut8[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) lut8[i] = c_lut8s[i];
+  __syncthreads();
+  to_linear_groups(img, w, h, channels, depth, lut16, out, blockIdx.x, lut8);
+}
+
 // Error-free transform: s + e == a + b exactly (Knuth's TwoSum).
 __device__ __forceinline__ float two_sum(float a, float b, float& e) {
   float s = __fadd_rn(a, b);
@@ -557,13 +580,12 @@ __device__ __forceinline__ float mean2x2(const float* p, int stride, int w, int 
 // nest exactly because each level halves the previous one, and odd edges occur only in the last tile of a row or
 // column, where mean2x2 clips to the level's size.
 constexpr int kPyrTile = 32;
-__global__ void __launch_bounds__(256) k_pyramid(PyramidDesc pd, float* __restrict__ pyr,
-                                                 const StepDesc* __restrict__ st) {
-  if (st && !st->active) return;
+// Scale-1 tile `blk` of a pyramid and every coarser tile below it.
+__device__ __forceinline__ void pyramid_tile(const PyramidDesc& pd, float* __restrict__ pyr, const int blk) {
   __shared__ float buf[2][3][kPyrTile][kPyrTile + 1];
   const ScaleDesc s0 = pd.s[0], s1 = pd.s[1];
   const int tiles_x = (s1.w + kPyrTile - 1) / kPyrTile;
-  const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  const int tx = blk % tiles_x, ty = blk / tiles_x;
   const size_t np0 = (size_t)s0.w * s0.h, np1 = (size_t)s1.w * s1.h;
   // scale 1 from global scale 0. Full 2x2 blocks (all but the last odd column/row) load their four samples at once
   // and sum them in mean2x2's order; partial blocks take the general path.
@@ -633,6 +655,101 @@ __global__ void __launch_bounds__(256) k_pyramid(PyramidDesc pd, float* __restri
     cur ^= 1;
     tile = half;
   }
+}
+
+__global__ void __launch_bounds__(256, 5) k_pyramid(const __grid_constant__ PyramidDesc pd, float* __restrict__ pyr,
+                                                 const StepDesc* __restrict__ st) {
+  if (st && !st->active) return;
+  pyramid_tile(pd, pyr, blockIdx.x);
+}
+
+// ------------------------------------------------------------------------------------------------ work-list scorer
+
+// Many (reference, distorted) pairs of any sizes scored together: one launch per stage over a work-list of every
+// pair's CTAs (linear planes, pyramid tiles, scorer tiles, reductions). Each stage's CTA finds its pair by a binary
+// search over the pairs' first-CTA indices; a pair with no CTAs in a stage has the same first index as the next
+// pair, and the search returns the last pair whose first index is <= the CTA's, so it is never chosen. Pairs that
+// name the same reference (same device pointer, size and format) share the first such pair's reference planes,
+// which are converted once.
+struct ScoreItem {
+  PyramidDesc pd;
+  const uint8_t* img[2];  // reference, distorted (interleaved samples)
+  float* pyr[2];          // their pyramids (pyr[0] may be an earlier pair's)
+  int channels, depth;
+  int own_ref;            // 1: this pair converts its reference; 0: it reuses an earlier pair's planes
+  int lin_ctas;           // to_linear CTAs per image
+  int pyr_ctas;           // pyramid CTAs per image
+  long long lin0, pyr0, tile0;  // first CTA / tile of this pair in each stage (own reference first, then distorted)
+  long long part;         // first double of this pair's [18][total_tiles] partial sums
+};
+
+template <typename Base>
+__device__ __forceinline__ int find_item(const ScoreItem* __restrict__ items, int n, long long x, Base base) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (base(items[mid]) <= x)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// Which image of the pair (0 reference, 1 distorted) and which CTA of it a stage's pair-local CTA index names.
+__device__ __forceinline__ int split_image(const ScoreItem& it, long long& local, int per_image) {
+  if (it.own_ref && local < per_image) return 0;
+  if (it.own_ref) local -= per_image;
+  return 1;
+}
+
+__global__ void __launch_bounds__(256) k_to_linear_batch(const ScoreItem* __restrict__ items, int n,
+                                                         const float* __restrict__ lut16) {
+  __shared__ float lut8[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) lut8[i] = c_lut8s[i];
+  __syncthreads();
+  const int i = find_item(items, n, blockIdx.x, [](const ScoreItem& it) { return it.lin0; });
+  const ScoreItem& it = items[i];
+  long long local = (long long)blockIdx.x - it.lin0;
+  const int which = split_image(it, local, it.lin_ctas);
+  to_linear_groups(it.img[which], it.pd.s[0].w, it.pd.s[0].h, it.channels, it.depth, lut16, it.pyr[which],
+                   (size_t)local, lut8);
+}
+
+__global__ void __launch_bounds__(256, 5) k_pyramid_batch(const ScoreItem* __restrict__ items, int n) {
+  const int i = find_item(items, n, blockIdx.x, [](const ScoreItem& it) { return it.pyr0; });
+  const ScoreItem& it = items[i];
+  long long local = (long long)blockIdx.x - it.pyr0;
+  const int which = split_image(it, local, it.pyr_ctas);
+  pyramid_tile(it.pd, it.pyr[which], (int)local);
+}
+
+// Persistent: each CTA walks the tile work-list with a stride of the grid; shared memory is reused tile after tile.
+__global__ void __launch_bounds__(kTileThreads, 3)
+    k_ssim2_tiles_batch(const ScoreItem* __restrict__ items, int n, long long total, double* __restrict__ partials) {
+  for (long long t = blockIdx.x; t < total; t += gridDim.x) {
+    const int i = find_item(items, n, t, [](const ScoreItem& it) { return it.tile0; });
+    const ScoreItem& it = items[i];
+    const int blk = (int)(t - it.tile0);
+    int s = 0;
+    while (s + 1 < it.pd.nscales && blk >= it.pd.s[s + 1].tile0) s++;
+    const ScaleDesc sd = it.pd.s[s];
+    ssim2_tile(sd, blk - sd.tile0, it.pyr[0], it.pyr[1], partials + it.part + blk, (size_t)it.pd.total_tiles);
+    __syncthreads();  // every thread is done with this tile's shared memory
+  }
+}
+
+// CTA (scale, sum, pair); scale_sums [n][kMaxScales][18], counters and scores [n].
+__global__ void __launch_bounds__(256) k_ssim2_reduce_batch(const ScoreItem* __restrict__ items,
+                                                            const double* __restrict__ partials,
+                                                            double* __restrict__ scale_sums,
+                                                            unsigned* __restrict__ counters,
+                                                            double* __restrict__ scores) {
+  const int p = blockIdx.z;
+  const ScoreItem& it = items[p];
+  if ((int)blockIdx.x >= it.pd.nscales) return;
+  reduce_scale_sum(it.pd, partials + it.part, scale_sums + (size_t)p * kMaxScales * kScoreSums, counters + p,
+                   scores + p, nullptr);
 }
 
 int to_linear(rcg_ctx* ctx, const uint8_t* d_img, int w, int h, int channels, int depth, float* d_pyr) {
@@ -733,6 +850,9 @@ static cudaError_t scorer_constants(int device) {
   if ((e = cudaFuncSetAttribute(k_ssim2_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem)) !=
       cudaSuccess)
     return e;
+  if ((e = cudaFuncSetAttribute(k_ssim2_tiles_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kTileSmem)) != cudaSuccess)
+    return e;
   if (device >= 0 && device < 64) g_scorer_ready[device] = true;
   return cudaSuccess;
 }
@@ -743,17 +863,126 @@ int scorer_init(rcg_ctx* ctx) {
   return RCG_OK;
 }
 
-int score_pyramids(rcg_ctx* ctx, const PyramidDesc& pd, const float* d_ref, const float* d_dist, double* d_score,
-                   SearchState* search, StepDesc* step) {
+int score_workspace(rcg_ctx* ctx, const PyramidDesc& pd) {
   double* partials = (double*)workspace(ctx, "score_partials", (size_t)pd.total_tiles * kScoreSums * sizeof(double));
   double* scale_sums = (double*)workspace(ctx, "score_scale_sums", kMaxScales * kScoreSums * sizeof(double));
   unsigned* counter = (unsigned*)workspace(ctx, "score_counter", 256);
-  if (!partials || !scale_sums || !counter) return RCG_NO_MEMORY;
+  return partials && scale_sums && counter ? RCG_OK : RCG_NO_MEMORY;
+}
+
+int score_pyramids(rcg_ctx* ctx, const PyramidDesc& pd, const float* d_ref, const float* d_dist, double* d_score,
+                   SearchState* search, StepDesc* step) {
+  if (score_workspace(ctx, pd) != RCG_OK) return RCG_NO_MEMORY;
+  double* partials = (double*)ctx->bufs["score_partials"].ptr;
+  double* scale_sums = (double*)ctx->bufs["score_scale_sums"].ptr;
+  unsigned* counter = (unsigned*)ctx->bufs["score_counter"].ptr;
   RCG_LAUNCH(ctx, "ssim2_tiles", k_ssim2_tiles, pd.total_tiles, kTileThreads, kTileSmem, pd, d_ref, d_dist, partials,
              step);
   dim3 rg(pd.nscales, kScoreSums);
   RCG_LAUNCH(ctx, "ssim2_reduce", k_ssim2_reduce, rg, 256, 0, pd, partials, scale_sums, counter, d_score, search,
              step);
+  return RCG_OK;
+}
+
+// Persistent grid of the work-list tile kernel: resident CTAs per SM x SMs, per device.
+static std::mutex g_batch_mu;
+static int g_batch_grid[64];
+
+static int tiles_batch_grid(int device) {
+  std::lock_guard<std::mutex> lk(g_batch_mu);
+  if (device >= 0 && device < 64 && g_batch_grid[device]) return g_batch_grid[device];
+  int per_sm = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ssim2_tiles_batch, kTileThreads, kTileSmem) !=
+          cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  const int g = std::max(1, per_sm) * std::max(1, sms);
+  if (device >= 0 && device < 64) g_batch_grid[device] = g;
+  return g;
+}
+
+int score_batch(rcg_ctx* ctx, int n, const uint8_t* const* d_refs, const uint8_t* const* d_dists,
+                const uint32_t* widths, const uint32_t* heights, const int* channels, const int* depths,
+                double** d_scores) {
+  std::vector<ScoreItem> items((size_t)n);
+  std::vector<long long> off_ref((size_t)n, -1), off_dist((size_t)n);
+  std::vector<int> ref_of((size_t)n);
+  std::map<std::tuple<const uint8_t*, uint32_t, uint32_t, int, int>, int> first_ref;
+  long long lin = 0, pyr = 0, tiles = 0, parts = 0, floats = 0;
+  int max_scales = 1;
+  bool need16 = false;
+  auto align64 = [](long long f) { return (f + 63) / 64 * 64; };  // 256-byte plane starts (vector stores)
+  for (int i = 0; i < n; i++) {
+    ScoreItem& it = items[(size_t)i];
+    std::memset(&it, 0, sizeof it);
+    const int w = (int)widths[i], h = (int)heights[i];
+    it.pd = make_pyramid(w, h);
+    it.img[0] = d_refs[i];
+    it.img[1] = d_dists[i];
+    it.channels = channels[i];
+    it.depth = depths ? depths[i] : 8;
+    auto key = std::make_tuple(d_refs[i], widths[i], heights[i], it.channels, it.depth);
+    auto found = first_ref.find(key);
+    it.own_ref = found == first_ref.end();
+    if (it.own_ref) {
+      first_ref.emplace(key, i);
+      ref_of[(size_t)i] = i;
+      off_ref[(size_t)i] = floats;
+      floats = align64(floats + it.pd.floats);
+    } else {
+      ref_of[(size_t)i] = found->second;
+    }
+    off_dist[(size_t)i] = floats;
+    floats = align64(floats + it.pd.floats);
+    const int copies = it.own_ref ? 2 : 1;
+    it.lin_ctas = (int)((((long long)w * h + 3) / 4 + 255) / 256);
+    it.pyr_ctas = it.pd.nscales >= 2 ? ((it.pd.s[1].w + kPyrTile - 1) / kPyrTile) *
+                                           ((it.pd.s[1].h + kPyrTile - 1) / kPyrTile)
+                                     : 0;
+    it.lin0 = lin;
+    lin += (long long)copies * it.lin_ctas;
+    it.pyr0 = pyr;
+    pyr += (long long)copies * it.pyr_ctas;
+    it.tile0 = tiles;
+    tiles += it.pd.total_tiles;
+    it.part = parts;
+    parts += (long long)kScoreSums * it.pd.total_tiles;
+    max_scales = std::max(max_scales, it.pd.nscales);
+    need16 |= it.depth == 16 && it.channels != 2 && it.channels != 4;
+  }
+  if (lin > INT32_MAX || pyr > INT32_MAX) return fail(ctx, RCG_INVALID, "batch too large for one launch");
+  float* pyr_base = (float*)workspace(ctx, "batch_pyr", (size_t)floats * sizeof(float));
+  double* partials = (double*)workspace(ctx, "batch_partials", (size_t)parts * sizeof(double));
+  double* sums = (double*)workspace(ctx, "batch_sums", (size_t)n * kMaxScales * kScoreSums * sizeof(double));
+  unsigned* counters = (unsigned*)workspace(ctx, "batch_counters", (size_t)n * sizeof(unsigned));
+  double* scores = (double*)workspace(ctx, "batch_scores", (size_t)n * sizeof(double));
+  ScoreItem* d_items = (ScoreItem*)workspace(ctx, "batch_items", (size_t)n * sizeof(ScoreItem));
+  const float* lut16 = need16 ? srgb_lut16_device(ctx) : nullptr;
+  if (!pyr_base || !partials || !sums || !counters || !scores || !d_items || (need16 && !lut16)) return RCG_NO_MEMORY;
+  for (int i = 0; i < n; i++) {
+    ScoreItem& it = items[(size_t)i];
+    it.pyr[0] = pyr_base + off_ref[(size_t)ref_of[(size_t)i]];
+    it.pyr[1] = pyr_base + off_dist[(size_t)i];
+  }
+  cudaError_t e = cudaMemcpyAsync(d_items, items.data(), (size_t)n * sizeof(ScoreItem), cudaMemcpyHostToDevice,
+                                  ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batch work-list upload");
+  const int grid = (int)std::min<long long>(tiles, std::max(1, tiles_batch_grid(ctx->device)));
+  // The launches take only the work-list's totals and this context's buffers: a later batch with the same totals
+  // replays them (its own pairs come in through the work-list uploaded above).
+  const std::vector<long long> key = {3, n, lin, pyr, tiles, max_scales, grid, (long long)(uintptr_t)lut16};
+  int rc = run_step_loop(ctx, key, [&]() {
+    RCG_LAUNCH(ctx, "to_linear_batch", k_to_linear_batch, (unsigned)lin, 256, 0, d_items, n, lut16);
+    if (pyr > 0) RCG_LAUNCH(ctx, "pyramid_batch", k_pyramid_batch, (unsigned)pyr, 256, 0, d_items, n);
+    RCG_LAUNCH(ctx, "ssim2_tiles_batch", k_ssim2_tiles_batch, grid, kTileThreads, kTileSmem, d_items, n, tiles,
+               partials);
+    RCG_LAUNCH(ctx, "ssim2_reduce_batch", k_ssim2_reduce_batch, dim3(max_scales, kScoreSums, n), 256, 0, d_items,
+               partials, sums, counters, scores);
+  });
+  if (rc != RCG_OK) return rc;
+  *d_scores = scores;
   return RCG_OK;
 }
 

@@ -246,6 +246,10 @@ def _load():
         "rcg_ctx_synchronize": (i32, [P]),
         "rcg_ctx_launch_count": (ctypes.c_uint64, [P]),
         "rcg_ctx_set_profiling": (i32, [P, i32]),
+        "rcg_ctx_set_graphs": (i32, [P, i32]),
+        "rcg_ssimulacra2_batch": (i32, [P, i32, P, P, P, P, P, P, P]),
+        "rcg_ssimulacra2_batch_device": (i32, [P, i32, P, P, P, P, P, P, P]),
+        "rcg_ctx_graph_stats": (i32, [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
         "rcg_ctx_kernel_time": (i32, [P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64),
                                       ctypes.POINTER(ctypes.c_double)]),
         "rcg_coef_layout_for": (i32, [u32, u32, i32, ctypes.POINTER(_Opts), ctypes.POINTER(_Layout)]),
@@ -309,7 +313,7 @@ EXPORTED = (
     "rcg_metric_score rcg_metric_score_device rcg_search_metric rcg_decode_coefs rcg_decode_coefs_device "
     "rcg_search_requantize_device rcg_ssimulacra2_grad rcg_ssimulacra2_grad_device rcg_perceptual_defaults "
     "rcg_coef_gradient rcg_perceptual_weights rcg_build_coefs_weighted rcg_search_weighted rcg_search_perceptual "
-    "rcg_perceptual_strength"
+    "rcg_perceptual_strength rcg_ctx_set_graphs rcg_ctx_graph_stats rcg_ssimulacra2_batch rcg_ssimulacra2_batch_device"
 ).split()
 
 
@@ -389,6 +393,17 @@ class Context:
     def set_profiling(self, on):
         self._check(_lib.rcg_ctx_set_profiling(self._ptr, 1 if on else 0))
 
+    def set_graphs(self, on):
+        """CUDA graphs for the searches' step loops (on by default); results are the same either way."""
+        self._check(_lib.rcg_ctx_set_graphs(self._ptr, 1 if on else 0))
+
+    def graph_stats(self):
+        """(step loops captured, graph launches) on this context so far."""
+        c = ctypes.c_uint64()
+        r = ctypes.c_uint64()
+        self._check(_lib.rcg_ctx_graph_stats(self._ptr, ctypes.byref(c), ctypes.byref(r)))
+        return int(c.value), int(r.value)
+
     def kernel_time(self, name):
         n = ctypes.c_uint64()
         ms = ctypes.c_double()
@@ -407,6 +422,45 @@ class Context:
         out = ctypes.c_double()
         self._check(_lib.rcg_ssimulacra2(self._ptr, a.ctypes.data, b.ctypes.data, w, h, c, d, ctypes.byref(out)))
         return out.value
+
+    def ssimulacra2_batch(self, pairs):
+        """Scores of many (reference, distorted) pairs of any sizes (rcg_ssimulacra2_batch); the same reference
+        object given for several pairs is uploaded and converted once. Returns a float64 array."""
+        n = len(pairs)
+        conv, keep = {}, []
+
+        def arr(img):
+            if id(img) not in conv:
+                conv[id(img)] = _image(img)
+                keep.append(img)
+            return conv[id(img)]
+
+        P = ctypes.c_void_p * max(n, 1)
+        refs, dists = P(), P()
+        ws, hs, cs, ds = (ctypes.c_uint32 * max(n, 1))(), (ctypes.c_uint32 * max(n, 1))(), \
+            (ctypes.c_int32 * max(n, 1))(), (ctypes.c_int32 * max(n, 1))()
+        for i, (ref, dist) in enumerate(pairs):
+            a, w, h, c, d = arr(ref)
+            b, w2, h2, c2, d2 = arr(dist)
+            if (w, h, c, d) != (w2, h2, c2, d2):
+                raise RcgError(RCG_INVALID, f"pair {i}: images differ in size or colour type")
+            refs[i], dists[i] = a.ctypes.data, b.ctypes.data
+            ws[i], hs[i], cs[i], ds[i] = w, h, c, d
+        out = np.zeros(max(n, 1), dtype=np.float64)
+        self._check(_lib.rcg_ssimulacra2_batch(self._ptr, n, refs, dists, ws, hs, cs, ds, out.ctypes.data))
+        return out[:n]
+
+    def ssimulacra2_batch_device(self, ref_ptrs, dist_ptrs, widths, heights, channels, depths=None):
+        """rcg_ssimulacra2_batch_device: device images, per-pair sizes; returns a float64 array of scores."""
+        n = len(ref_ptrs)
+        P = ctypes.c_void_p * max(n, 1)
+        U = ctypes.c_uint32 * max(n, 1)
+        I = ctypes.c_int32 * max(n, 1)
+        out = np.zeros(max(n, 1), dtype=np.float64)
+        dp = I(*depths) if depths is not None else None
+        self._check(_lib.rcg_ssimulacra2_batch_device(self._ptr, n, P(*ref_ptrs), P(*dist_ptrs), U(*widths),
+                                                      U(*heights), I(*channels), dp, out.ctypes.data))
+        return out[:n]
 
     def ssimulacra2_device(self, ref_ptr, dist_ptr, width, height, channels):
         out = ctypes.c_double()
