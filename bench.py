@@ -232,6 +232,10 @@ def scorer_batch_workload(ctx, torch, dev, timed, n=64, steps=5):
     kb = {k: ctx.kernel_time(k)[1] for k in ("to_linear_batch", "pyramid_batch", "ssim2_tiles_batch",
                                              "ssim2_reduce_batch")}
     ctx.set_profiling(False)
+    ctx.set_profiling(True)
+    one_by_one()
+    kp = {k: ctx.kernel_time(k)[1] for k in ("to_linear", "pyramid", "ssim2_tiles", "ssim2_reduce")}
+    ctx.set_profiling(False)
     del d_r, d_d
     torch.cuda.empty_cache()
     ms_b, ms_p = sum(tb) / len(tb), sum(tp) / len(tp)
@@ -239,7 +243,8 @@ def scorer_batch_workload(ctx, torch, dev, timed, n=64, steps=5):
             "pairs": n, "megapixels": mpx, "batch_ms": ms_b, "one_by_one_ms": ms_p,
             "batch_mpx_per_s": mpx / (ms_b / 1000.0), "one_by_one_mpx_per_s": mpx / (ms_p / 1000.0),
             "batch_vs_one_by_one": ms_p / ms_b, "identical_scores": [float(x) for x in sb] == sp,
-            "batch_kernels_ms": kb, "launches_per_batch": 4}
+            "batch_kernels_ms": kb, "one_by_one_kernels_ms": kp, "launches_per_batch": 4,
+            "launches_one_by_one": 6 * n}
 
 
 def batch_workload(ctx, torch, n=64, parallel=8, steps=2, perceptual=True):

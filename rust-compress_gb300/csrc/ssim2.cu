@@ -683,12 +683,21 @@ struct ScoreItem {
   long long part;         // first double of this pair's [18][total_tiles] partial sums
 };
 
-template <typename Base>
-__device__ __forceinline__ int find_item(const ScoreItem* __restrict__ items, int n, long long x, Base base) {
+// One scale of one pair in the tile work-list, with everything a tile needs resolved on the host.
+struct TileSeg {
+  const float* ref;   // channel 0 of this scale's planes
+  const float* dist;
+  double* out;        // partial sums of the segment's first tile; tile k, sum i at out[i * stride + k]
+  int w, h, tiles_x;
+  int stride;         // tiles of the pair (the sum-major stride of its partials)
+};
+
+// Last index whose first entry is <= x in an ascending array of first indices (n >= 1, first[0] = 0).
+__device__ __forceinline__ int find_first(const long long* __restrict__ first, int n, long long x) {
   int lo = 0, hi = n - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (base(items[mid]) <= x)
+    if (__ldg(first + mid) <= x)
       lo = mid;
     else
       hi = mid - 1;
@@ -703,12 +712,13 @@ __device__ __forceinline__ int split_image(const ScoreItem& it, long long& local
   return 1;
 }
 
-__global__ void __launch_bounds__(256) k_to_linear_batch(const ScoreItem* __restrict__ items, int n,
+__global__ void __launch_bounds__(256) k_to_linear_batch(const ScoreItem* __restrict__ items,
+                                                         const long long* __restrict__ lin0, int n,
                                                          const float* __restrict__ lut16) {
   __shared__ float lut8[256];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) lut8[i] = c_lut8s[i];
   __syncthreads();
-  const int i = find_item(items, n, blockIdx.x, [](const ScoreItem& it) { return it.lin0; });
+  const int i = find_first(lin0, n, blockIdx.x);
   const ScoreItem& it = items[i];
   long long local = (long long)blockIdx.x - it.lin0;
   const int which = split_image(it, local, it.lin_ctas);
@@ -716,27 +726,32 @@ __global__ void __launch_bounds__(256) k_to_linear_batch(const ScoreItem* __rest
                    (size_t)local, lut8);
 }
 
-__global__ void __launch_bounds__(256, 5) k_pyramid_batch(const ScoreItem* __restrict__ items, int n) {
-  const int i = find_item(items, n, blockIdx.x, [](const ScoreItem& it) { return it.pyr0; });
+__global__ void __launch_bounds__(256, 5) k_pyramid_batch(const ScoreItem* __restrict__ items,
+                                                          const long long* __restrict__ pyr0, int n) {
+  const int i = find_first(pyr0, n, blockIdx.x);
   const ScoreItem& it = items[i];
   long long local = (long long)blockIdx.x - it.pyr0;
   const int which = split_image(it, local, it.pyr_ctas);
   pyramid_tile(it.pd, it.pyr[which], (int)local);
 }
 
-// Persistent: each CTA walks the tile work-list with a stride of the grid; shared memory is reused tile after tile.
+// One CTA per tile of the work-list. A persistent form (a fixed grid of k CTAs per SM striding over the list, each
+// CTA reusing its shared memory tile after tile) measured slower on 64 pairs of mixed sizes: 22.7 / 25.4 / 38.9 ms
+// at k = 3 / 2 / 1 against 21.1 ms here, because the block scheduler hands tiles to whichever CTA slot frees first.
 __global__ void __launch_bounds__(kTileThreads, 3)
-    k_ssim2_tiles_batch(const ScoreItem* __restrict__ items, int n, long long total, double* __restrict__ partials) {
-  for (long long t = blockIdx.x; t < total; t += gridDim.x) {
-    const int i = find_item(items, n, t, [](const ScoreItem& it) { return it.tile0; });
-    const ScoreItem& it = items[i];
-    const int blk = (int)(t - it.tile0);
-    int s = 0;
-    while (s + 1 < it.pd.nscales && blk >= it.pd.s[s + 1].tile0) s++;
-    const ScaleDesc sd = it.pd.s[s];
-    ssim2_tile(sd, blk - sd.tile0, it.pyr[0], it.pyr[1], partials + it.part + blk, (size_t)it.pd.total_tiles);
-    __syncthreads();  // every thread is done with this tile's shared memory
-  }
+    k_ssim2_tiles_batch(const TileSeg* __restrict__ segs, const long long* __restrict__ seg0, int nseg) {
+  const long long t = blockIdx.x;
+  const int g = find_first(seg0, nseg, t);
+  const TileSeg sg = segs[g];
+  ScaleDesc sd;
+  sd.w = sg.w;
+  sd.h = sg.h;
+  sd.tiles_x = sg.tiles_x;
+  sd.tiles_y = 0;
+  sd.tile0 = 0;
+  sd.off = 0;
+  const int local = (int)(t - __ldg(seg0 + g));
+  ssim2_tile(sd, local, sg.ref, sg.dist, sg.out + local, (size_t)sg.stride);
 }
 
 // CTA (scale, sum, pair); scale_sums [n][kMaxScales][18], counters and scores [n].
@@ -884,25 +899,6 @@ int score_pyramids(rcg_ctx* ctx, const PyramidDesc& pd, const float* d_ref, cons
   return RCG_OK;
 }
 
-// Persistent grid of the work-list tile kernel: resident CTAs per SM x SMs, per device.
-static std::mutex g_batch_mu;
-static int g_batch_grid[64];
-
-static int tiles_batch_grid(int device) {
-  std::lock_guard<std::mutex> lk(g_batch_mu);
-  if (device >= 0 && device < 64 && g_batch_grid[device]) return g_batch_grid[device];
-  int per_sm = 0, sms = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ssim2_tiles_batch, kTileThreads, kTileSmem) !=
-          cudaSuccess ||
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
-    cudaGetLastError();
-    return 0;
-  }
-  const int g = std::max(1, per_sm) * std::max(1, sms);
-  if (device >= 0 && device < 64) g_batch_grid[device] = g;
-  return g;
-}
-
 int score_batch(rcg_ctx* ctx, int n, const uint8_t* const* d_refs, const uint8_t* const* d_dists,
                 const uint32_t* widths, const uint32_t* heights, const int* channels, const int* depths,
                 double** d_scores) {
@@ -952,32 +948,63 @@ int score_batch(rcg_ctx* ctx, int n, const uint8_t* const* d_refs, const uint8_t
     max_scales = std::max(max_scales, it.pd.nscales);
     need16 |= it.depth == 16 && it.channels != 2 && it.channels != 4;
   }
-  if (lin > INT32_MAX || pyr > INT32_MAX) return fail(ctx, RCG_INVALID, "batch too large for one launch");
+  if (lin > INT32_MAX || pyr > INT32_MAX || tiles > INT32_MAX)
+    return fail(ctx, RCG_INVALID, "batch too large for one launch");
   float* pyr_base = (float*)workspace(ctx, "batch_pyr", (size_t)floats * sizeof(float));
   double* partials = (double*)workspace(ctx, "batch_partials", (size_t)parts * sizeof(double));
   double* sums = (double*)workspace(ctx, "batch_sums", (size_t)n * kMaxScales * kScoreSums * sizeof(double));
   unsigned* counters = (unsigned*)workspace(ctx, "batch_counters", (size_t)n * sizeof(unsigned));
   double* scores = (double*)workspace(ctx, "batch_scores", (size_t)n * sizeof(double));
-  ScoreItem* d_items = (ScoreItem*)workspace(ctx, "batch_items", (size_t)n * sizeof(ScoreItem));
+  // The work-list in one upload: pairs, their first to_linear / pyramid CTAs, then the tile segments (one per
+  // pair and scale) and their first tiles.
+  int nseg = 0;
+  for (const ScoreItem& it : items) nseg += it.pd.nscales;
+  const size_t o_lin = (size_t)n * sizeof(ScoreItem), o_pyr = o_lin + (size_t)n * 8,
+               o_seg = o_pyr + (size_t)n * 8, o_seg0 = o_seg + (size_t)nseg * sizeof(TileSeg),
+               list_bytes = o_seg0 + (size_t)nseg * 8;
+  unsigned char* d_list = (unsigned char*)workspace(ctx, "batch_items", list_bytes);
   const float* lut16 = need16 ? srgb_lut16_device(ctx) : nullptr;
-  if (!pyr_base || !partials || !sums || !counters || !scores || !d_items || (need16 && !lut16)) return RCG_NO_MEMORY;
+  if (!pyr_base || !partials || !sums || !counters || !scores || !d_list || (need16 && !lut16)) return RCG_NO_MEMORY;
+  std::vector<unsigned char> list(list_bytes);
+  long long* lin0 = (long long*)(list.data() + o_lin);
+  long long* pyr0 = (long long*)(list.data() + o_pyr);
+  TileSeg* segs = (TileSeg*)(list.data() + o_seg);
+  long long* seg0 = (long long*)(list.data() + o_seg0);
+  int g = 0;
   for (int i = 0; i < n; i++) {
     ScoreItem& it = items[(size_t)i];
     it.pyr[0] = pyr_base + off_ref[(size_t)ref_of[(size_t)i]];
     it.pyr[1] = pyr_base + off_dist[(size_t)i];
+    lin0[i] = it.lin0;
+    pyr0[i] = it.pyr0;
+    for (int sc = 0; sc < it.pd.nscales; sc++, g++) {
+      const ScaleDesc& sd = it.pd.s[sc];
+      segs[g].ref = it.pyr[0] + sd.off;
+      segs[g].dist = it.pyr[1] + sd.off;
+      segs[g].out = partials + it.part + sd.tile0;
+      segs[g].w = sd.w;
+      segs[g].h = sd.h;
+      segs[g].tiles_x = sd.tiles_x;
+      segs[g].stride = it.pd.total_tiles;
+      seg0[g] = it.tile0 + sd.tile0;
+    }
   }
-  cudaError_t e = cudaMemcpyAsync(d_items, items.data(), (size_t)n * sizeof(ScoreItem), cudaMemcpyHostToDevice,
-                                  ctx->stream);
+  std::memcpy(list.data(), items.data(), o_lin);
+  cudaError_t e = cudaMemcpyAsync(d_list, list.data(), list_bytes, cudaMemcpyHostToDevice, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batch work-list upload");
-  const int grid = (int)std::min<long long>(tiles, std::max(1, tiles_batch_grid(ctx->device)));
+  const ScoreItem* d_items = (const ScoreItem*)d_list;
+  const long long* d_lin0 = (const long long*)(d_list + o_lin);
+  const long long* d_pyr0 = (const long long*)(d_list + o_pyr);
+  const TileSeg* d_segs = (const TileSeg*)(d_list + o_seg);
+  const long long* d_seg0 = (const long long*)(d_list + o_seg0);
   // The launches take only the work-list's totals and this context's buffers: a later batch with the same totals
   // replays them (its own pairs come in through the work-list uploaded above).
-  const std::vector<long long> key = {3, n, lin, pyr, tiles, max_scales, grid, (long long)(uintptr_t)lut16};
+  const std::vector<long long> key = {3, n, nseg, lin, pyr, tiles, max_scales, (long long)(uintptr_t)lut16};
   int rc = run_step_loop(ctx, key, [&]() {
-    RCG_LAUNCH(ctx, "to_linear_batch", k_to_linear_batch, (unsigned)lin, 256, 0, d_items, n, lut16);
-    if (pyr > 0) RCG_LAUNCH(ctx, "pyramid_batch", k_pyramid_batch, (unsigned)pyr, 256, 0, d_items, n);
-    RCG_LAUNCH(ctx, "ssim2_tiles_batch", k_ssim2_tiles_batch, grid, kTileThreads, kTileSmem, d_items, n, tiles,
-               partials);
+    RCG_LAUNCH(ctx, "to_linear_batch", k_to_linear_batch, (unsigned)lin, 256, 0, d_items, d_lin0, n, lut16);
+    if (pyr > 0) RCG_LAUNCH(ctx, "pyramid_batch", k_pyramid_batch, (unsigned)pyr, 256, 0, d_items, d_pyr0, n);
+    RCG_LAUNCH(ctx, "ssim2_tiles_batch", k_ssim2_tiles_batch, (unsigned)tiles, kTileThreads, kTileSmem, d_segs,
+               d_seg0, nseg);
     RCG_LAUNCH(ctx, "ssim2_reduce_batch", k_ssim2_reduce_batch, dim3(max_scales, kScoreSums, n), 256, 0, d_items,
                partials, sums, counters, scores);
   });
