@@ -929,7 +929,9 @@ __global__ void k_upsample_color(const StepDesc* __restrict__ st, const uint8_t*
 
 int upsample_color(rcg_ctx* ctx, StepDesc* d_step, const uint8_t* d_planes, int w, int h, uint8_t* d_rgb,
                    float* d_lin) {
-  dim3 grid(((w + 3) / 4 + 127) / 128, std::min(h, 65535));
+  // (h + 1) / 2 rows of CTAs: the 4:2:0 path writes two rows per chroma row, and the general path strides over the
+  // rows by the grid height, so every layout is covered (a grid of h rows would leave half of it idle for 4:2:0).
+  dim3 grid(((w + 3) / 4 + 127) / 128, std::min((h + 1) / 2, 65535));
   RCG_LAUNCH(ctx, "upsample_color", k_upsample_color, grid, 128, 0, d_step, d_planes, w, h, d_rgb, d_lin);
   return RCG_OK;
 }
