@@ -472,8 +472,8 @@ int rate_tables(rcg_ctx* ctx, StepDesc* d_step) {
 // own position, so no 64-entry zd table is needed.
 // kWeighted: the perceptual mode. Each coefficient's distortion weight becomes rw[k] * pweights[block][k] (one f32
 // product, then the same squared-error product as the plain weight); the plain instantiation reads no weights.
-template <bool kWeighted>
 // 6 CTAs per SM (80 registers, no spill) instead of 5.
+template <bool kWeighted>
 __global__ void __launch_bounds__(128, 6) k_trellis(StepDesc* __restrict__ st, CacheSet cs) {
   __shared__ float lr[3][64 * 16];
   if (!st->active || !st->use_trellis) return;
