@@ -224,8 +224,11 @@ def scorer_batch_workload(ctx, torch, dev, timed, n=64, steps=5):
     for _ in range(3):
         batch()
         one_by_one()
+    sampler = ClockSampler(dev.index or 0)
+    sampler.start()
     tb, sb = timed(batch, steps)
     tp, sp = timed(one_by_one, steps)
+    clocks = sampler.stop()
     mpx = sum(w * h for w, h in sizes) / 1e6
     ctx.set_profiling(True)
     batch()
@@ -244,7 +247,7 @@ def scorer_batch_workload(ctx, torch, dev, timed, n=64, steps=5):
             "batch_mpx_per_s": mpx / (ms_b / 1000.0), "one_by_one_mpx_per_s": mpx / (ms_p / 1000.0),
             "batch_vs_one_by_one": ms_p / ms_b, "identical_scores": [float(x) for x in sb] == sp,
             "batch_kernels_ms": kb, "one_by_one_kernels_ms": kp, "launches_per_batch": 4,
-            "launches_one_by_one": 6 * n}
+            "launches_one_by_one": 6 * n, "clocks": clocks}
 
 
 def batch_workload(ctx, torch, n=64, parallel=8, steps=2, perceptual=True):
