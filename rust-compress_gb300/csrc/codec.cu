@@ -475,23 +475,35 @@ int rate_tables(rcg_ctx* ctx, StepDesc* d_step) {
 // 6 CTAs per SM (80 registers, no spill) instead of 5.
 template <bool kWeighted>
 __global__ void __launch_bounds__(128, 6) k_trellis(StepDesc* __restrict__ st, CacheSet cs) {
+  // The per-position tables of every component and the lambda*rate tables of the components this CTA's blocks
+  // belong to (usually one), staged in shared memory: the DP reads them at every position.
   __shared__ float lr[3][64 * 16];
+  __shared__ float s_scale[3][64], s_rq[3][64], s_rw[3][64];
   if (!st->active || !st->use_trellis) return;
-  for (int i = threadIdx.x; i < 3 * 64 * 16; i += blockDim.x) (&lr[0][0])[i] = (&st->lr[0][0])[i];
+  const bool requant = st->requant != 0;
+  const long long blk0 = (long long)blockIdx.x * blockDim.x;
+  const int c_lo = comp_of(st, blk0), c_hi = comp_of(st, min(blk0 + (long long)blockDim.x, st->nblocks) - 1);
+  for (int i = threadIdx.x; i < (c_hi - c_lo + 1) * 64 * 16; i += blockDim.x)
+    (&lr[c_lo][0])[i] = (&st->lr[c_lo][0])[i];
+  for (int i = threadIdx.x; i < 3 * 64; i += blockDim.x) {
+    const int c = i / 64, k = i % 64;
+    s_scale[c][k] = requant ? st->ratio[c][k] : st->divz[c][k];
+    s_rq[c][k] = st->rq[c][k];
+    s_rw[c][k] = st->rw[c][k];
+  }
   __syncthreads();
-  const long long gb = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gb = blk0 + threadIdx.x;
   if (gb >= st->nblocks) return;
   const int c = comp_of(st, gb);
   const CompDesc& cd = st->comp[c];
   const long long nb = (long long)cd.bw * cd.bh;
   // Encoding: a[k] = flat[ZZ_T[k]] * div[ZZ_T[k]] from the FDCT cache (jpeg/src/encode.rs:207-211).
   // Requantization: a[k] = source[k] * ratio[k] (jpeg/src/encode.rs:162-166); the DC stays the plain value.
-  const bool requant = st->requant != 0;
   const float* cache = requant ? nullptr : cs.p[cd.cache] + (gb - cd.blk0);
   const int16_t* src = requant ? st->coef_src + gb * 64 : nullptr;
-  const float* scale = requant ? st->ratio[c] : st->divz[c];
-  const float* rq = st->rq[c];
-  const float* rw = st->rw[c];
+  const float* scale = s_scale[c];
+  const float* rq = s_rq[c];
+  const float* rw = s_rw[c];
   const float* lrc = lr[c];
   const float* pw = kWeighted ? st->pweights + gb * 64 : nullptr;  // 16-byte aligned rows of 64 floats
 
