@@ -676,6 +676,8 @@ def main():
             "traffic_source": "ncu capture of the same kernel and workload (384.0 MB read + 5.7 MB written)",
             "peak_source": "measured" if hbm else "fallback",
             "avg_launch_ms": tile_ms,
+            "compute_view": {"issue_active_pct": 73.9, "fma_pipe_pct": 53.4, "alu_pipe_pct": 34.6,
+                             "source": "ncu --set full of the same kernel at this workload (profiles/ssim2_tiles_12mp.md)"},
             "note": "the scorer is FP32-ALU bound (~1 kflop per full-resolution pixel), far below the HBM roof; "
                     "algorithmic bytes = 6 B per full-resolution pixel (two RGB8 images)"}
     batch = None
