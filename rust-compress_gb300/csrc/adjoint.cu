@@ -83,19 +83,21 @@ __global__ void k_lin(const uint8_t* __restrict__ ref, const float* __restrict__
 }
 
 // 2x2 means (:225-247), fewer samples at odd edges; 3 channels.
+// Grid (output columns, rows, channels): see grid_rows.
 template <typename T>
 __global__ void k_down(const T* __restrict__ src, int w, int h, T* __restrict__ dst, int ow, int oh) {
+  const int ox = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ox >= ow) return;
   const long long n = (long long)ow * oh;
-  for (long long i = tid1(); i < 3 * n; i += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(i / n);
-    const long long o = i - c * n;
-    const int oy = (int)(o / ow), ox = (int)(o % ow);
-    const int x1 = min(2 * ox + 2, w), y1 = min(2 * oy + 2, h);
-    const T* p = src + (long long)c * w * h;
+  const int c = blockIdx.z;
+  const T* p = src + (long long)c * w * h;
+  const int x1 = min(2 * ox + 2, w);
+  for (int oy = blockIdx.y; oy < oh; oy += gridDim.y) {
+    const int y1 = min(2 * oy + 2, h);
     T s = 0;
     for (int y = 2 * oy; y < y1; y++)
       for (int x = 2 * ox; x < x1; x++) s += p[(long long)y * w + x];
-    dst[i] = s / (T)((y1 - 2 * oy) * (x1 - 2 * ox));
+    dst[c * n + (long long)oy * ow + ox] = s / (T)((y1 - 2 * oy) * (x1 - 2 * ox));
   }
 }
 
@@ -117,23 +119,31 @@ __global__ void k_xyb(const T* __restrict__ lin, long long n, T* __restrict__ xy
   }
 }
 
+// The plane kernels below run on a (columns / 256, rows, planes) grid: a thread owns one column of one plane and
+// strides over the rows, so no sample index is divided back into (plane, row, column).
+dim3 grid_rows(int w, int h, int planes) {
+  return dim3((unsigned)((w + 255) / 256), (unsigned)std::min(h, 65535), (unsigned)planes);
+}
+
 // Row blur (zero outside) of one plane: the backward pass's rows (the zero-padded row blur is its own transpose).
-// `planes` consecutive planes of n samples in one sweep.
+// One plane per grid z.
 template <typename T>
-__global__ void k_hblur(const T* __restrict__ src, int w, int h, int planes, T* __restrict__ dst) {
+__global__ void k_hblur(const T* __restrict__ src, int w, int h, T* __restrict__ dst) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= w) return;
   const long long n = (long long)w * h;
-  for (long long i = tid1(); i < n * planes; i += (long long)gridDim.x * blockDim.x) {
-    const long long p = i / n, o = i - p * n;
-    const int y = (int)(o / w), x = (int)(o % w);
-    const T* sp = src + p * n;
+  const T* sp = src + blockIdx.z * n;
+  T* dp = dst + blockIdx.z * n;
+  for (int y = blockIdx.y; y < h; y += gridDim.y) {
+    const T* row = sp + (long long)y * w;
     T s = 0;
 #pragma unroll
     for (int t = 0; t <= 2 * kR; t++) {
       const int xx = x + t - kR;
       if (xx < 0 || xx >= w) continue;
-      s += tap<T>(t) * sp[(long long)y * w + xx];
+      s += tap<T>(t) * row[xx];
     }
-    dst[i] = s;
+    dp[(long long)y * w + x] = s;
   }
 }
 
@@ -141,9 +151,11 @@ __global__ void k_hblur(const T* __restrict__ src, int w, int h, int planes, T* 
 // 3 xb^2, 4 xa xb (each output summed over the taps in the same order as k_hblur).
 template <typename T>
 __global__ void k_hblur5(const T* __restrict__ xa, const T* __restrict__ xb, int w, int h, T* __restrict__ dst) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= w) return;
   const long long n = (long long)w * h;
-  for (long long i = tid1(); i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int y = (int)(i / w), x = (int)(i % w);
+  for (int y = blockIdx.y; y < h; y += gridDim.y) {
+    const long long i = (long long)y * w + x;
     T s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0;
 #pragma unroll
     for (int t = 0; t <= 2 * kR; t++) {
@@ -167,46 +179,82 @@ __global__ void k_hblur5(const T* __restrict__ xa, const T* __restrict__ xb, int
 
 __device__ __forceinline__ int mirror64(int yy, int h) { return yy < 0 ? -yy - 1 : (yy >= h ? 2 * h - 1 - yy : yy); }
 
-// Column blur with mirrored rows (:385-397) of `planes` consecutive planes of n samples in one sweep.
+// Rows per thread of the column blurs: a run of kRun outputs reads its kRun + 10 source rows once (in registers)
+// instead of 11 rows per output; every output still sums its taps in the same order.
+constexpr int kRun = 8;
+
+// Column blur with mirrored rows (:385-397), one plane per grid z, grid y over runs of kRun rows.
 template <typename T>
-__global__ void k_vblur_n(const T* __restrict__ src, int w, int h, int planes, T* __restrict__ dst) {
+__global__ void k_vblur_n(const T* __restrict__ src, int w, int h, T* __restrict__ dst) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= w) return;
   const long long n = (long long)w * h;
-  for (long long i = tid1(); i < n * planes; i += (long long)gridDim.x * blockDim.x) {
-    const long long p = i / n, o = i - p * n;
-    const int y = (int)(o / w), x = (int)(o % w);
-    const T* sp = src + p * n;
-    T s = 0;
+  const T* sp = src + blockIdx.z * n + x;
+  T* dp = dst + blockIdx.z * n + x;
+  const int runs = (h + kRun - 1) / kRun;
+  for (int r = blockIdx.y; r < runs; r += gridDim.y) {
+    const int y0 = r * kRun;
+    T v[kRun + 2 * kR];
 #pragma unroll
-    for (int t = 0; t <= 2 * kR; t++) s += tap<T>(t) * sp[(long long)mirror64(y + t - kR, h) * w + x];
-    dst[i] = s;
+    for (int k = 0; k < kRun + 2 * kR; k++) {
+      const int yy = y0 + k - kR;
+      v[k] = yy <= h - 1 + kR ? sp[(long long)mirror64(yy, h) * w] : (T)0;  // rows past a short last run: unused
+    }
+#pragma unroll
+    for (int o = 0; o < kRun; o++) {
+      if (y0 + o >= h) break;
+      T s = 0;
+#pragma unroll
+      for (int t = 0; t <= 2 * kR; t++) s += tap<T>(t) * v[o + t];
+      dp[(long long)(y0 + o) * w] = s;
+    }
   }
 }
 
 // Transpose of the column blur as a gather: row y' receives tap t from the rows y whose mirrored source row is y', i.e.
 // from source index y' (y = y' - t + R), -y' - 1 (mirrored at the top) and 2h - 1 - y' (at the bottom).
-// `planes` consecutive planes of n samples in one sweep.
+// One plane per grid z, grid y over runs of kRun rows; a run inside the interior reads its rows once.
 template <typename T>
-__global__ void k_vblur_t(const T* __restrict__ gsrc, int w, int h, int planes, T* __restrict__ dst) {
+__global__ void k_vblur_t(const T* __restrict__ gsrc, int w, int h, T* __restrict__ dst) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= w) return;
   const long long n = (long long)w * h;
-  for (long long i = tid1(); i < n * planes; i += (long long)gridDim.x * blockDim.x) {
-    const long long p = i / n, o = i - p * n;
-    const int yp = (int)(o / w), x = (int)(o % w);
-    const T* g = gsrc + p * n;
-    T s = 0;
-    if (yp >= kR && yp < h - kR) {
-      // interior: only the direct source row is in range (the mirrored ones are not)
+  const T* g = gsrc + blockIdx.z * n;
+  T* dp = dst + blockIdx.z * n;
+  const int runs = (h + kRun - 1) / kRun;
+  for (int r = blockIdx.y; r < runs; r += gridDim.y) {
+    const int y0 = r * kRun;
+    if (y0 >= kR && y0 + kRun - 1 < h - kR) {
+      // every output row of the run is interior: row yp takes tap t from source row yp - t + kR
+      T v[kRun + 2 * kR];
 #pragma unroll
-      for (int t = 0; t <= 2 * kR; t++) s += tap<T>(t) * g[(long long)(yp - t + kR) * w + x];
-    } else {
+      for (int k = 0; k < kRun + 2 * kR; k++) v[k] = g[(long long)(y0 - kR + k) * w + x];
 #pragma unroll
-      for (int t = 0; t <= 2 * kR; t++) {
-        const int ys[3] = {yp - t + kR, -yp - 1 - t + kR, 2 * h - 1 - yp - t + kR};
+      for (int o = 0; o < kRun; o++) {
+        T s = 0;
 #pragma unroll
-        for (int e = 0; e < 3; e++)
-          if (ys[e] >= 0 && ys[e] < h) s += tap<T>(t) * g[(long long)ys[e] * w + x];
+        for (int t = 0; t <= 2 * kR; t++) s += tap<T>(t) * v[o + 2 * kR - t];
+        dp[(long long)(y0 + o) * w + x] = s;
       }
+      continue;
     }
-    dst[i] = s;
+    for (int yp = y0; yp < min(y0 + kRun, h); yp++) {
+      T s = 0;
+      if (yp >= kR && yp < h - kR) {
+        // interior: only the direct source row is in range (the mirrored ones are not)
+#pragma unroll
+        for (int t = 0; t <= 2 * kR; t++) s += tap<T>(t) * g[(long long)(yp - t + kR) * w + x];
+      } else {
+#pragma unroll
+        for (int t = 0; t <= 2 * kR; t++) {
+          const int ys[3] = {yp - t + kR, -yp - 1 - t + kR, 2 * h - 1 - yp - t + kR};
+#pragma unroll
+          for (int e = 0; e < 3; e++)
+            if (ys[e] >= 0 && ys[e] < h) s += tap<T>(t) * g[(long long)ys[e] * w + x];
+        }
+      }
+      dp[(long long)yp * w + x] = s;
+    }
   }
 }
 
@@ -334,7 +382,8 @@ __global__ void k_xyb_adj(const T* __restrict__ lin, const T* __restrict__ g_xyb
     T o[3] = {gu0 * M00 + gu1 * M10 + gu2 * M20, gu0 * M01 + gu1 * M11 + gu2 * M21,
               gu0 * M02 + gu1 * M12 + gu2 * M22};
     if (g_coarse) {
-      const int y = (int)(i / w), x = (int)(i % w), ox = x / 2, oy = y / 2;
+      const unsigned ui = (unsigned)i;  // within one plane: fewer than 2^32 samples
+      const int y = (int)(ui / (unsigned)w), x = (int)(ui - (unsigned)y * (unsigned)w), ox = x / 2, oy = y / 2;
       const int nx = min(2 * ox + 2, w) - 2 * ox, ny = min(2 * oy + 2, h) - 2 * oy;
       const T inv = one / (T)(nx * ny);
 #pragma unroll
@@ -425,16 +474,18 @@ int grad_impl(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, int w, in
     return RCG_NO_MEMORY;
   RCG_LAUNCH(ctx, "adj_lin", k_lin<T>, grid_of(n0), 256, 0, d_ref, d_dist, n0, pa, pb);
   for (int s = 1; s < ns; s++) {
-    RCG_LAUNCH(ctx, "adj_down", k_down<T>, grid_of(3 * sc[s].n), 256, 0, pa + sc[s - 1].off, sc[s - 1].w,
+    RCG_LAUNCH(ctx, "adj_down", k_down<T>, grid_rows(sc[s].w, sc[s].h, 3), 256, 0, pa + sc[s - 1].off, sc[s - 1].w,
                sc[s - 1].h, pa + sc[s].off, sc[s].w, sc[s].h);
-    RCG_LAUNCH(ctx, "adj_down", k_down<T>, grid_of(3 * sc[s].n), 256, 0, pb + sc[s - 1].off, sc[s - 1].w,
+    RCG_LAUNCH(ctx, "adj_down", k_down<T>, grid_rows(sc[s].w, sc[s].h, 3), 256, 0, pb + sc[s - 1].off, sc[s - 1].w,
                sc[s - 1].h, pb + sc[s].off, sc[s].w, sc[s].h);
   }
   // forward: the moments and map sums of every scale
   auto moments = [&](int s, int c) {
     const long long n = sc[s].n;
-    RCG_LAUNCH(ctx, "adj_hblur5", k_hblur5<T>, grid_of(n), 256, 0, xa + c * n, xb + c * n, sc[s].w, sc[s].h, hb5);
-    RCG_LAUNCH(ctx, "adj_vblur", k_vblur_n<T>, grid_of(5 * n), 256, 0, hb5, sc[s].w, sc[s].h, 5, mom);
+    RCG_LAUNCH(ctx, "adj_hblur5", k_hblur5<T>, grid_rows(sc[s].w, sc[s].h, 1), 256, 0, xa + c * n, xb + c * n,
+               sc[s].w, sc[s].h, hb5);
+    RCG_LAUNCH(ctx, "adj_vblur", k_vblur_n<T>, grid_rows(sc[s].w, (sc[s].h + kRun - 1) / kRun, 5), 256, 0, hb5,
+               sc[s].w, sc[s].h, mom);
   };
   for (int s = 0; s < ns; s++) {
     const long long n = sc[s].n;
@@ -501,8 +552,9 @@ int grad_impl(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, int w, in
       RCG_LAUNCH(ctx, "adj_mapgrad", k_mapgrad<T>, grid_of(n), 256, 0, mom, xa + c * n, xb + c * n, n, nc, gq,
                  gq + n, gq + 2 * n, gx + c * n);
       // the three gradient planes through the transposed column blur, then the row blur (its own transpose)
-      RCG_LAUNCH(ctx, "adj_vblur_t", k_vblur_t<T>, grid_of(3 * n), 256, 0, gq, sc[s].w, sc[s].h, 3, hb5);
-      RCG_LAUNCH(ctx, "adj_hblur", k_hblur<T>, grid_of(3 * n), 256, 0, hb5, sc[s].w, sc[s].h, 3, tq);
+      RCG_LAUNCH(ctx, "adj_vblur_t", k_vblur_t<T>, grid_rows(sc[s].w, (sc[s].h + kRun - 1) / kRun, 3), 256, 0, gq,
+                 sc[s].w, sc[s].h, hb5);
+      RCG_LAUNCH(ctx, "adj_hblur", k_hblur<T>, grid_rows(sc[s].w, sc[s].h, 3), 256, 0, hb5, sc[s].w, sc[s].h, tq);
       RCG_LAUNCH(ctx, "adj_combine", k_combine<T>, grid_of(n), 256, 0, tq, tq + n, tq + 2 * n, xa + c * n,
                  xb + c * n, n, gx + c * n);
     }
