@@ -580,16 +580,19 @@ __device__ __forceinline__ float mean2x2(const float* p, int stride, int w, int 
 // nest exactly because each level halves the previous one, and odd edges occur only in the last tile of a row or
 // column, where mean2x2 clips to the level's size.
 constexpr int kPyrTile = 32;
-// Scale-1 tile `blk` of a pyramid and every coarser tile below it.
-__device__ __forceinline__ void pyramid_tile(const PyramidDesc& pd, float* __restrict__ pyr, const int blk) {
-  __shared__ float buf[2][3][kPyrTile][kPyrTile + 1];
-  const ScaleDesc s0 = pd.s[0], s1 = pd.s[1];
-  const int tiles_x = (s1.w + kPyrTile - 1) / kPyrTile;
-  const int tx = blk % tiles_x, ty = blk / tiles_x;
+constexpr int kPyrThreads = 256;  // every pyramid launch
+
+// Scale-1 tile (tx, ty) from scale 0 into `out` (shared) and dst1 (global). Full 2x2 blocks (all but the last odd
+// column/row) load their four samples at once and sum them in mean2x2's order; partial blocks take the general path.
+// Source and destination are separate restricted pointers, so the loads of later outputs may be issued before the
+// stores of earlier ones.
+__device__ __forceinline__ void scale1_tile(const float* __restrict__ src0, float* __restrict__ dst1,
+                                            const ScaleDesc& s0, const ScaleDesc& s1, int tx, int ty,
+                                            float (*out)[kPyrTile][kPyrTile + 1]) {
   const size_t np0 = (size_t)s0.w * s0.h, np1 = (size_t)s1.w * s1.h;
-  // scale 1 from global scale 0. Full 2x2 blocks (all but the last odd column/row) load their four samples at once
-  // and sum them in mean2x2's order; partial blocks take the general path.
-  for (int i = threadIdx.x; i < kPyrTile * kPyrTile; i += blockDim.x) {
+#pragma unroll
+  for (int k = 0; k < kPyrTile * kPyrTile / kPyrThreads; k++) {
+    const int i = threadIdx.x + k * kPyrThreads;
     int lx = i % kPyrTile, ly = i / kPyrTile;
     int ox = tx * kPyrTile + lx, oy = ty * kPyrTile + ly;
     if (ox < s1.w && oy < s1.h) {
@@ -599,7 +602,7 @@ __device__ __forceinline__ void pyramid_tile(const PyramidDesc& pd, float* __res
         float q[3][4];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-          const float* p = pyr + s0.off + c * np0 + (size_t)(2 * oy) * s0.w + 2 * ox;
+          const float* p = src0 + c * np0 + (size_t)(2 * oy) * s0.w + 2 * ox;
           q[c][0] = p[0];
           q[c][1] = p[1];
           q[c][2] = p[s0.w];
@@ -615,15 +618,24 @@ __device__ __forceinline__ void pyramid_tile(const PyramidDesc& pd, float* __res
         }
       } else {
 #pragma unroll
-        for (int c = 0; c < 3; c++) v[c] = mean2x2(pyr + s0.off + c * np0, s0.w, s0.w, s0.h, ox, oy);
+        for (int c = 0; c < 3; c++) v[c] = mean2x2(src0 + c * np0, s0.w, s0.w, s0.h, ox, oy);
       }
 #pragma unroll
       for (int c = 0; c < 3; c++) {
-        buf[0][c][ly][lx] = v[c];
-        pyr[s1.off + c * np1 + (size_t)oy * s1.w + ox] = v[c];
+        out[c][ly][lx] = v[c];
+        dst1[c * np1 + (size_t)oy * s1.w + ox] = v[c];
       }
     }
   }
+}
+
+// Scale-1 tile `blk` of a pyramid and every coarser tile below it.
+__device__ __forceinline__ void pyramid_tile(const PyramidDesc& pd, float* __restrict__ pyr, const int blk) {
+  __shared__ float buf[2][3][kPyrTile][kPyrTile + 1];
+  const ScaleDesc s0 = pd.s[0], s1 = pd.s[1];
+  const int tiles_x = (s1.w + kPyrTile - 1) / kPyrTile;
+  const int tx = blk % tiles_x, ty = blk / tiles_x;
+  scale1_tile(pyr + s0.off, pyr + s1.off, s0, s1, tx, ty, buf[0]);
   int cur = 0, tile = kPyrTile;
   for (int L = 2; L < pd.nscales; L++) {
     __syncthreads();
