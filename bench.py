@@ -250,6 +250,36 @@ def scorer_batch_workload(ctx, torch, dev, timed, n=64, steps=5):
             "launches_one_by_one": 6 * n, "clocks": clocks}
 
 
+def sweep_workload(ctx, img, steps=3):
+    """A rate-quality curve of the workload image (8 qualities, 4:2:0, trellis) through rcg_sweep_qualities (host
+    image in, scores out) against the same curve from build_coefs + reconstruct + ssimulacra2 per quality."""
+    import rcg
+
+    qs = [95, 90, 85, 80, 75, 70, 60, 50]
+    opts = rcg.EncodeOptions(90, rcg.Subsampling.S420, True)
+    ctx.sweep_qualities([img], qs, opts)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sw = ctx.sweep_qualities([img], qs, opts)[0]
+    t_sweep = (time.perf_counter() - t0) / steps
+
+    def singles():
+        out = []
+        for q in qs:
+            ci = ctx.build_coefs(img, rcg.EncodeOptions(q, opts.subsampling, opts.trellis))
+            out.append(ctx.ssimulacra2(img, ctx.reconstruct(ci)))
+        return out
+
+    singles()
+    t0 = time.perf_counter()
+    one = singles()
+    t_single = time.perf_counter() - t0
+    return {"workload": f"rate-quality curve of the {W}x{H} workload image, qualities {qs}, 4:2:0, trellis, host buffers",
+            "ms_per_curve": 1000.0 * t_sweep, "ms_per_curve_single_calls": 1000.0 * t_single,
+            "speedup": t_single / t_sweep, "identical_scores": [float(x) for x in sw] == one,
+            "scores": [round(float(x), 4) for x in sw]}
+
+
 def batch_workload(ctx, torch, n=64, parallel=8, steps=2, perceptual=True):
     """Many images of uneven sizes (seeds 2..2+n-1, log-uniform 640x480..6000x4000, aspect 4:3/3:2/16:9/1:1), each
     with its own target drawn uniformly from 55..85: plain searches one after another (rcg_search) against the
@@ -705,6 +735,9 @@ def main():
     perceptual = None
     if rank == 0 and not args.no_perceptual:
         perceptual = perceptual_workload(ctx, img, timed)
+    sweep = None
+    if rank == 0 and not args.no_scorer:
+        sweep = sweep_workload(ctx, img)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
@@ -739,6 +772,7 @@ def main():
             "scorer_mpx_per_s": (W * H / 1e6) / (tile_ms / 1000.0),
             "scorer_alone": scorer,
             "scorer_batch": scorer_batch,
+            "quality_sweep": sweep,
             "batch": batch,
             "requantize": requant,
             "write_best_plan": plan,

@@ -162,6 +162,16 @@ int rcg_ssimulacra2_device(rcg_ctx* ctx, const uint8_t* d_reference, const uint8
 int rcg_ssimulacra2_batch(rcg_ctx* ctx, int n, const uint8_t* const* references, const uint8_t* const* distorted,
                           const uint32_t* widths, const uint32_t* heights, const int* channels, const int* depths,
                           double* scores);
+/* A rate-quality curve: for each of n 8-bit Gray/Rgb host images and each of nq qualities (1..=100, any order), the
+ * SSIMULACRA2 score of the image against its candidate at that quality, scores[i * nq + k] =
+ * ssimulacra2(image_i, reconstruct(build_coefs(image_i, {qualities[k], opts->subsampling, opts->trellis}))), the
+ * value jpeg::target::find_quality_with would get for that quality (jpeg/src/target.rs:29-56 evaluates them one at a
+ * time; this has no single-call counterpart in the reference). Each image's FDCT is computed once; its candidates are
+ * decoded on the device and scored together by the work-list scorer, sharing one conversion of the image. Errors as
+ * rcg_search for the image (RCG_INVALID for sides < 8 or a non-finite score, naming the image). */
+int rcg_sweep_qualities(rcg_ctx* ctx, int n, const uint8_t* const* images, const uint32_t* widths,
+                        const uint32_t* heights, const int* channels, int nq, const int* qualities,
+                        const rcg_encode_options* opts, double* scores);
 /* The same with device images (arrays of device pointers, sizes and scores on the host). */
 int rcg_ssimulacra2_batch_device(rcg_ctx* ctx, int n, const uint8_t* const* d_references,
                                  const uint8_t* const* d_distorted, const uint32_t* widths, const uint32_t* heights,

@@ -734,6 +734,83 @@ int rcg_ssimulacra2_batch(rcg_ctx* ctx, int n, const uint8_t* const* references,
   return batch_scores_out(ctx, n, d_scores, scores);
 }
 
+// ---- rate-quality sweep
+
+// One image of rcg_sweep_qualities: every quality's candidate decoded to 8-bit pixels on the device, then all of
+// them scored by one work-list scorer call against the image (its planes converted once).
+static int sweep_image(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, int nq, const int* qualities,
+                       const rcg_encode_options* opts, double* scores) {
+  int rc;
+  EncoderSetup es;
+  if ((rc = setup_encoder(ctx, d_src, w, h, channels, opts->subsampling, &es)) != RCG_OK) return rc;
+  const size_t npx = (size_t)w * h * channels;
+  uint8_t* d_cand = (uint8_t*)workspace(ctx, "sweep_cands", npx * (size_t)nq);
+  int16_t* d_coefs = (int16_t*)workspace(ctx, "sweep_coefs", (size_t)es.max_coefs * 2);
+  uint8_t* d_planes = (uint8_t*)workspace(ctx, "sweep_planes", (size_t)es.max_plane_bytes);
+  StepDesc* d_sts = (StepDesc*)workspace(ctx, "sweep_steps", sizeof(StepDesc) * (size_t)nq);
+  if (!d_cand || !d_coefs || !d_planes || !d_sts) return RCG_NO_MEMORY;
+  // build_coefs' tables per quality (jpeg/src/encode.rs:426-539), one descriptor per candidate, uploaded at once.
+  std::vector<StepDesc> st((size_t)nq);
+  for (int k = 0; k < nq; k++) {
+    host_step_tables(&st[(size_t)k], qualities[k], opts->subsampling, channels, opts->trellis, w, h);
+    st[(size_t)k].coefs = d_coefs;
+  }
+  cudaError_t e = cudaMemcpyAsync(d_sts, st.data(), sizeof(StepDesc) * (size_t)nq, cudaMemcpyHostToDevice,
+                                  ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "sweep tables upload");
+  std::vector<const uint8_t*> refs((size_t)nq, d_src), dists((size_t)nq);
+  std::vector<uint32_t> ws((size_t)nq, (uint32_t)w), hs((size_t)nq, (uint32_t)h);
+  std::vector<int> cs((size_t)nq, channels);
+  for (int k = 0; k < nq; k++) {
+    StepDesc* d_st = d_sts + k;
+    quantize(ctx, d_st, es.caches, es.max_blocks);
+    rate_tables(ctx, d_st);
+    trellis(ctx, d_st, es.caches, es.max_blocks);
+    dequant_idct(ctx, d_st, nullptr, d_planes, es.max_blocks);  // reconstruct (jpeg/src/decode.rs:334-389)
+    dists[(size_t)k] = d_cand + npx * (size_t)k;
+    upsample_color(ctx, d_st, d_planes, w, h, d_cand + npx * (size_t)k, nullptr);
+  }
+  double* d_scores = nullptr;
+  if ((rc = score_batch(ctx, nq, refs.data(), dists.data(), ws.data(), hs.data(), cs.data(), nullptr, &d_scores)) !=
+      RCG_OK)
+    return rc;
+  if ((rc = copy_to_host(ctx, scores, d_scores, sizeof(double) * (size_t)nq)) != RCG_OK) return rc;
+  return finish(ctx, "sweep");  // the host descriptors above must outlive their upload
+}
+
+int rcg_sweep_qualities(rcg_ctx* ctx, int n, const uint8_t* const* images, const uint32_t* widths,
+                        const uint32_t* heights, const int* channels, int nq, const int* qualities,
+                        const rcg_encode_options* opts, double* scores) {
+  if (!ctx) return RCG_INVALID;
+  if (n < 0 || nq < 1 || nq > 100) return fail(ctx, RCG_INVALID, "a sweep takes n >= 0 images and 1..=100 qualities");
+  if (n == 0) return RCG_OK;
+  if (!images || !widths || !heights || !channels || !qualities || !scores) return fail(ctx, RCG_INVALID, "null pointer");
+  int rc = check_opts(ctx, opts, false);
+  if (rc != RCG_OK) return rc;
+  for (int k = 0; k < nq; k++)
+    if (qualities[k] < 1 || qualities[k] > 100) return fail(ctx, RCG_INVALID, "qualities are 1..=100");
+  for (int i = 0; i < n; i++) {
+    if (!images[i]) return fail(ctx, RCG_INVALID, "null pointer");
+    if ((rc = check_image(ctx, widths[i], heights[i], channels[i])) != RCG_OK) return rc;
+    if (widths[i] < (uint32_t)kMinSide || heights[i] < (uint32_t)kMinSide)
+      return fail(ctx, RCG_INVALID, "image " + std::to_string(i) + ": SSIMULACRA 2 needs at least 8x8 pixels");
+  }
+  cudaSetDevice(ctx->device);
+  for (int i = 0; i < n; i++) {
+    const size_t bytes = (size_t)widths[i] * heights[i] * channels[i];
+    uint8_t* d_src = (uint8_t*)workspace(ctx, "img_src", bytes);
+    if (!d_src) return RCG_NO_MEMORY;
+    if ((rc = copy_to_device(ctx, d_src, images[i], bytes)) != RCG_OK) return rc;
+    if ((rc = sweep_image(ctx, d_src, (int)widths[i], (int)heights[i], channels[i], nq, qualities, opts,
+                          scores + (size_t)i * nq)) != RCG_OK)
+      return rc;
+    for (int k = 0; k < nq; k++)
+      if (!std::isfinite(scores[(size_t)i * nq + k]))
+        return fail(ctx, RCG_INVALID, "image " + std::to_string(i) + ": SSIMULACRA 2 produced a non-finite score");
+  }
+  return RCG_OK;
+}
+
 // ---- other metrics
 
 static int metric_on_device(rcg_ctx* ctx, int metric, const uint8_t* d_a, const uint8_t* d_b, int w, int h, int ch,

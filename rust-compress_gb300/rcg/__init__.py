@@ -249,6 +249,7 @@ def _load():
         "rcg_ctx_set_graphs": (i32, [P, i32]),
         "rcg_ssimulacra2_batch": (i32, [P, i32, P, P, P, P, P, P, P]),
         "rcg_ssimulacra2_batch_device": (i32, [P, i32, P, P, P, P, P, P, P]),
+        "rcg_sweep_qualities": (i32, [P, i32, P, P, P, P, i32, P, ctypes.POINTER(_Opts), P]),
         "rcg_ctx_graph_stats": (i32, [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
         "rcg_ctx_kernel_time": (i32, [P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64),
                                       ctypes.POINTER(ctypes.c_double)]),
@@ -313,7 +314,8 @@ EXPORTED = (
     "rcg_metric_score rcg_metric_score_device rcg_search_metric rcg_decode_coefs rcg_decode_coefs_device "
     "rcg_search_requantize_device rcg_ssimulacra2_grad rcg_ssimulacra2_grad_device rcg_perceptual_defaults "
     "rcg_coef_gradient rcg_perceptual_weights rcg_build_coefs_weighted rcg_search_weighted rcg_search_perceptual "
-    "rcg_perceptual_strength rcg_ctx_set_graphs rcg_ctx_graph_stats rcg_ssimulacra2_batch rcg_ssimulacra2_batch_device"
+    "rcg_perceptual_strength rcg_ctx_set_graphs rcg_ctx_graph_stats rcg_ssimulacra2_batch rcg_ssimulacra2_batch_device "
+    "rcg_sweep_qualities"
 ).split()
 
 
@@ -448,6 +450,29 @@ class Context:
             ws[i], hs[i], cs[i], ds[i] = w, h, c, d
         out = np.zeros(max(n, 1), dtype=np.float64)
         self._check(_lib.rcg_ssimulacra2_batch(self._ptr, n, refs, dists, ws, hs, cs, ds, out.ctypes.data))
+        return out[:n]
+
+    def sweep_qualities(self, images, qualities, opts=None):
+        """rcg_sweep_qualities: a (len(images), len(qualities)) float64 array of the SSIMULACRA2 score of each image
+        against its candidate at each quality (build_coefs at that quality, reconstruct, ssimulacra2)."""
+        opts = opts or EncodeOptions()
+        n, nq = len(images), len(qualities)
+        arrs = []
+        for im in images:
+            a, w, h, c, d = _image(im)
+            if d != 8 or c not in (1, 3):
+                raise RcgError(RCG_INVALID, "the sweep takes 8-bit Gray or Rgb")
+            arrs.append((a, w, h, c))
+        P = ctypes.c_void_p * max(n, 1)
+        U = ctypes.c_uint32 * max(n, 1)
+        I = ctypes.c_int32 * max(n, 1)
+        q = (ctypes.c_int32 * nq)(*[int(x) for x in qualities])
+        out = np.zeros((max(n, 1), nq), dtype=np.float64)
+        o = _opts(opts)
+        self._check(_lib.rcg_sweep_qualities(self._ptr, n, P(*[a.ctypes.data for a, _, _, _ in arrs]),
+                                             U(*[w for _, w, _, _ in arrs]), U(*[h for _, _, h, _ in arrs]),
+                                             I(*[c for _, _, _, c in arrs]), nq, q, ctypes.byref(o),
+                                             out.ctypes.data))
         return out[:n]
 
     def ssimulacra2_batch_device(self, ref_ptrs, dist_ptrs, widths, heights, channels, depths=None):
