@@ -274,10 +274,33 @@ def sweep_workload(ctx, img, steps=3):
     t0 = time.perf_counter()
     one = singles()
     t_single = time.perf_counter() - t0
-    return {"workload": f"rate-quality curve of the {W}x{H} workload image, qualities {qs}, 4:2:0, trellis, host buffers",
-            "ms_per_curve": 1000.0 * t_sweep, "ms_per_curve_single_calls": 1000.0 * t_single,
-            "speedup": t_single / t_sweep, "identical_scores": [float(x) for x in sw] == one,
-            "scores": [round(float(x), 4) for x in sw]}
+    out = {"workload": f"rate-quality curve of the {W}x{H} workload image, qualities {qs}, 4:2:0, trellis, host buffers",
+           "ms_per_curve": 1000.0 * t_sweep, "ms_per_curve_single_calls": 1000.0 * t_single,
+           "speedup": t_single / t_sweep, "identical_scores": [float(x) for x in sw] == one,
+           "scores": [round(float(x), 4) for x in sw]}
+    # The batch workload's 64 images x the same 8 qualities: one call (images grouped, each group's 512 pairs
+    # scored by one work-list launch) against one call per image.
+    import rcg.synth as synth
+
+    sizes = synth.log_uniform_sizes(2, 64)
+    imgs = synth.images([(w, h, 2 + i, 0.0) for i, (w, h) in enumerate(sizes)])
+    ctx.sweep_qualities(imgs[:2], qs, opts)
+    t0 = time.perf_counter()
+    allq = ctx.sweep_qualities(imgs, qs, opts)
+    t_all = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    per = [ctx.sweep_qualities([im], qs, opts)[0] for im in imgs]
+    t_per = time.perf_counter() - t0
+    mpx = sum(w * h for w, h in sizes) / 1e6
+    out["image_set"] = {"workload": f"64 images (log-uniform 640x480..6000x4000, {mpx:.0f} MP) x {len(qs)} qualities",
+                        "candidates": 64 * len(qs), "ms_one_call": 1000.0 * t_all, "ms_one_call_per_image": 1000.0 * t_per,
+                        "candidates_per_s": 64 * len(qs) / t_all, "candidate_mpx_per_s": mpx * len(qs) / t_all,
+                        "identical_scores": all(np_equal(a, b) for a, b in zip(allq, per))}
+    return out
+
+
+def np_equal(a, b):
+    return len(a) == len(b) and all(float(x) == float(y) for x, y in zip(a, b))
 
 
 def batch_workload(ctx, torch, n=64, parallel=8, steps=2, perceptual=True):

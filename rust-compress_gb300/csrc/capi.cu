@@ -736,46 +736,87 @@ int rcg_ssimulacra2_batch(rcg_ctx* ctx, int n, const uint8_t* const* references,
 
 // ---- rate-quality sweep
 
-// One image of rcg_sweep_qualities: every quality's candidate decoded to 8-bit pixels on the device, then all of
-// them scored by one work-list scorer call against the image (its planes converted once).
-static int sweep_image(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, int nq, const int* qualities,
+// Device bytes one image of a sweep holds until its group is scored: the image and its candidates (8-bit), and both
+// sides' linear pyramids in the scorer (3 channels, 4/3 for the coarser scales, 4-byte floats: 16 B per pixel).
+static size_t sweep_bytes(uint32_t w, uint32_t h, int channels, int nq) {
+  const size_t px = (size_t)w * h;
+  return (px * channels + 16 * px) * (size_t)(nq + 1);
+}
+constexpr size_t kSweepGroupBytes = 8ull << 30;  // images per group: as many as fit this estimate
+
+static size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+
+// A group of images of rcg_sweep_qualities: every image's candidates at every quality encoded and decoded to 8-bit
+// pixels on the device, then all of the group's pairs scored by one work-list scorer call (each image converted once
+// as the reference of its candidates).
+static int sweep_group(rcg_ctx* ctx, int n, const uint8_t* const* images, const uint32_t* widths,
+                       const uint32_t* heights, const int* channels, int nq, const int* qualities,
                        const rcg_encode_options* opts, double* scores) {
   int rc;
-  EncoderSetup es;
-  if ((rc = setup_encoder(ctx, d_src, w, h, channels, opts->subsampling, &es)) != RCG_OK) return rc;
-  const size_t npx = (size_t)w * h * channels;
-  uint8_t* d_cand = (uint8_t*)workspace(ctx, "sweep_cands", npx * (size_t)nq);
-  int16_t* d_coefs = (int16_t*)workspace(ctx, "sweep_coefs", (size_t)es.max_coefs * 2);
-  uint8_t* d_planes = (uint8_t*)workspace(ctx, "sweep_planes", (size_t)es.max_plane_bytes);
-  StepDesc* d_sts = (StepDesc*)workspace(ctx, "sweep_steps", sizeof(StepDesc) * (size_t)nq);
-  if (!d_cand || !d_coefs || !d_planes || !d_sts) return RCG_NO_MEMORY;
-  // build_coefs' tables per quality (jpeg/src/encode.rs:426-539), one descriptor per candidate, uploaded at once.
-  std::vector<StepDesc> st((size_t)nq);
-  for (int k = 0; k < nq; k++) {
-    host_step_tables(&st[(size_t)k], qualities[k], opts->subsampling, channels, opts->trellis, w, h);
-    st[(size_t)k].coefs = d_coefs;
+  std::vector<size_t> img_off((size_t)n), cand_off((size_t)n), img_bytes((size_t)n);
+  size_t tot_img = 0, tot_cand = 0;
+  for (int i = 0; i < n; i++) {
+    img_bytes[(size_t)i] = (size_t)widths[i] * heights[i] * channels[i];
+    img_off[(size_t)i] = tot_img;
+    tot_img += align256(img_bytes[(size_t)i]);
+    cand_off[(size_t)i] = tot_cand;
+    tot_cand += align256(img_bytes[(size_t)i]) * (size_t)nq;
   }
-  cudaError_t e = cudaMemcpyAsync(d_sts, st.data(), sizeof(StepDesc) * (size_t)nq, cudaMemcpyHostToDevice,
+  // build_coefs' tables per (image, quality) (jpeg/src/encode.rs:426-539), one descriptor per candidate.
+  std::vector<StepDesc> st((size_t)n * nq);
+  long long max_coefs = 0, max_planes = 0;
+  for (int i = 0; i < n; i++)
+    for (int k = 0; k < nq; k++) {
+      StepDesc& d = st[(size_t)i * nq + k];
+      host_step_tables(&d, qualities[k], opts->subsampling, channels[i], opts->trellis, (int)widths[i],
+                       (int)heights[i]);
+      max_coefs = std::max(max_coefs, d.nblocks * 64);
+      max_planes = std::max(max_planes, plane_bytes(&d));
+    }
+  uint8_t* d_imgs = (uint8_t*)workspace(ctx, "sweep_imgs", tot_img);
+  uint8_t* d_cand = (uint8_t*)workspace(ctx, "sweep_cands", tot_cand);
+  int16_t* d_coefs = (int16_t*)workspace(ctx, "sweep_coefs", (size_t)max_coefs * 2);
+  uint8_t* d_planes = (uint8_t*)workspace(ctx, "sweep_planes", (size_t)max_planes);
+  StepDesc* d_sts = (StepDesc*)workspace(ctx, "sweep_steps", sizeof(StepDesc) * st.size());
+  if (!d_imgs || !d_cand || !d_coefs || !d_planes || !d_sts) return RCG_NO_MEMORY;
+  for (StepDesc& d : st) d.coefs = d_coefs;  // one candidate at a time, in stream order
+  // Host copies first: a pageable copy waits for the stream, so they go before any kernel of the group.
+  for (int i = 0; i < n; i++)
+    if ((rc = copy_to_device(ctx, d_imgs + img_off[(size_t)i], images[i], img_bytes[(size_t)i])) != RCG_OK) return rc;
+  cudaError_t e = cudaMemcpyAsync(d_sts, st.data(), sizeof(StepDesc) * st.size(), cudaMemcpyHostToDevice,
                                   ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "sweep tables upload");
-  std::vector<const uint8_t*> refs((size_t)nq, d_src), dists((size_t)nq);
-  std::vector<uint32_t> ws((size_t)nq, (uint32_t)w), hs((size_t)nq, (uint32_t)h);
-  std::vector<int> cs((size_t)nq, channels);
-  for (int k = 0; k < nq; k++) {
-    StepDesc* d_st = d_sts + k;
-    quantize(ctx, d_st, es.caches, es.max_blocks);
-    rate_tables(ctx, d_st);
-    trellis(ctx, d_st, es.caches, es.max_blocks);
-    dequant_idct(ctx, d_st, nullptr, d_planes, es.max_blocks);  // reconstruct (jpeg/src/decode.rs:334-389)
-    dists[(size_t)k] = d_cand + npx * (size_t)k;
-    upsample_color(ctx, d_st, d_planes, w, h, d_cand + npx * (size_t)k, nullptr);
+  std::vector<const uint8_t*> refs(st.size()), dists(st.size());
+  std::vector<uint32_t> ws(st.size()), hs(st.size());
+  std::vector<int> cs(st.size());
+  for (int i = 0; i < n; i++) {
+    const uint8_t* d_src = d_imgs + img_off[(size_t)i];
+    EncoderSetup es;
+    if ((rc = setup_encoder(ctx, d_src, (int)widths[i], (int)heights[i], channels[i], opts->subsampling, &es)) !=
+        RCG_OK)
+      return rc;
+    for (int k = 0; k < nq; k++) {
+      const size_t j = (size_t)i * nq + k;
+      StepDesc* d_st = d_sts + j;
+      quantize(ctx, d_st, es.caches, es.max_blocks);
+      rate_tables(ctx, d_st);
+      trellis(ctx, d_st, es.caches, es.max_blocks);
+      dequant_idct(ctx, d_st, nullptr, d_planes, es.max_blocks);  // reconstruct (jpeg/src/decode.rs:334-389)
+      uint8_t* out = d_cand + cand_off[(size_t)i] + align256(img_bytes[(size_t)i]) * (size_t)k;
+      upsample_color(ctx, d_st, d_planes, (int)widths[i], (int)heights[i], out, nullptr);
+      refs[j] = d_src;
+      dists[j] = out;
+      ws[j] = widths[i];
+      hs[j] = heights[i];
+      cs[j] = channels[i];
+    }
   }
   double* d_scores = nullptr;
-  if ((rc = score_batch(ctx, nq, refs.data(), dists.data(), ws.data(), hs.data(), cs.data(), nullptr, &d_scores)) !=
-      RCG_OK)
+  if ((rc = score_batch(ctx, (int)st.size(), refs.data(), dists.data(), ws.data(), hs.data(), cs.data(), nullptr,
+                        &d_scores)) != RCG_OK)
     return rc;
-  if ((rc = copy_to_host(ctx, scores, d_scores, sizeof(double) * (size_t)nq)) != RCG_OK) return rc;
-  return finish(ctx, "sweep");  // the host descriptors above must outlive their upload
+  if ((rc = copy_to_host(ctx, scores, d_scores, sizeof(double) * st.size())) != RCG_OK) return rc;
+  return finish(ctx, "sweep");
 }
 
 int rcg_sweep_qualities(rcg_ctx* ctx, int n, const uint8_t* const* images, const uint32_t* widths,
@@ -796,18 +837,21 @@ int rcg_sweep_qualities(rcg_ctx* ctx, int n, const uint8_t* const* images, const
       return fail(ctx, RCG_INVALID, "image " + std::to_string(i) + ": SSIMULACRA 2 needs at least 8x8 pixels");
   }
   cudaSetDevice(ctx->device);
-  for (int i = 0; i < n; i++) {
-    const size_t bytes = (size_t)widths[i] * heights[i] * channels[i];
-    uint8_t* d_src = (uint8_t*)workspace(ctx, "img_src", bytes);
-    if (!d_src) return RCG_NO_MEMORY;
-    if ((rc = copy_to_device(ctx, d_src, images[i], bytes)) != RCG_OK) return rc;
-    if ((rc = sweep_image(ctx, d_src, (int)widths[i], (int)heights[i], channels[i], nq, qualities, opts,
-                          scores + (size_t)i * nq)) != RCG_OK)
+  for (int i0 = 0; i0 < n;) {
+    int i1 = i0 + 1;
+    size_t bytes = sweep_bytes(widths[i0], heights[i0], channels[i0], nq);
+    while (i1 < n && (size_t)(i1 - i0 + 1) * nq <= 65535 &&
+           bytes + sweep_bytes(widths[i1], heights[i1], channels[i1], nq) <= kSweepGroupBytes)
+      bytes += sweep_bytes(widths[i1], heights[i1], channels[i1], nq), i1++;
+    if ((rc = sweep_group(ctx, i1 - i0, images + i0, widths + i0, heights + i0, channels + i0, nq, qualities, opts,
+                          scores + (size_t)i0 * nq)) != RCG_OK)
       return rc;
+    i0 = i1;
+  }
+  for (int i = 0; i < n; i++)
     for (int k = 0; k < nq; k++)
       if (!std::isfinite(scores[(size_t)i * nq + k]))
         return fail(ctx, RCG_INVALID, "image " + std::to_string(i) + ": SSIMULACRA 2 produced a non-finite score");
-  }
   return RCG_OK;
 }
 
