@@ -123,3 +123,21 @@ def test_perceptual_search_replays_both_loops():
             assert np.array_equal(got.weights, want.weights)
         captures, replays = g.graph_stats()
         assert captures == 2 and replays >= 4
+
+
+def test_graphs_on_a_caller_stream():
+    """Captured and replayed on a stream the caller owns (the context's stream set to it), same results."""
+    torch = pytest.importorskip("torch")
+    img = synth.image(256, 160, 47)
+    opts = rcg.EncodeOptions(90, rcg.Subsampling.S420, True)
+    with rcg.Context(0) as plain, rcg.Context(0) as g:
+        plain.set_graphs(False)
+        want = plain.find_quality_ssimulacra2(img, 72.0, 100, opts)
+        s = torch.cuda.Stream()
+        g.set_stream(s.cuda_stream)
+        for _ in range(3):
+            _same(g.find_quality_ssimulacra2(img, 72.0, 100, opts), want)
+        assert g.graph_stats() == (1, 2)
+        g.set_stream(0)  # back to the context's own stream: the stored graph replays there too
+        _same(g.find_quality_ssimulacra2(img, 72.0, 100, opts), want)
+        assert g.graph_stats() == (1, 3)
