@@ -135,7 +135,7 @@ int rcg_ctx_kernel_time(rcg_ctx* ctx, const char* name, uint64_t* launches, doub
  * default stream, or while the caller captures the context's stream. Replaces nothing in the reference (a rayon
  * CPU loop has no launches to batch). Synchronizes the context. */
 int rcg_ctx_set_graphs(rcg_ctx* ctx, int on);
-/* Step loops captured into graphs, and graph launches, on this context so far. */
+/* Step loops captured into graphs, and graph launches, on this context so far (no reference counterpart). */
 int rcg_ctx_graph_stats(const rcg_ctx* ctx, uint64_t* captures, uint64_t* replays);
 
 /* Coefficient layout for an image and options. Replaces nothing in the reference: it sizes the caller-allocated
