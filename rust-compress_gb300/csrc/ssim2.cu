@@ -364,18 +364,35 @@ __device__ __forceinline__ void ssim2_tile(const ScaleDesc sd, const int local, 
       }
     }
   }
-  // Warp sums (f32, 32 threads x 4 pixels), then the 8 warps in f64 in a fixed order.
+  // Warp sums (f32, 32 threads x 4 pixels), then the 8 warps in f64 in a fixed order. Sums 0..15 by a reduce-scatter
+  // butterfly: at each exchange (lane distance 16, 8, 4, 2) a lane keeps half of the values it carries and adds its
+  // partner's copy of that half, then distance 1 adds the pair; lane l ends with sum l >> 1. The additions are those
+  // of a full butterfly per sum, so every sum has the same bits, in 16 shuffles instead of 80. Sums 16 and 17 by full
+  // butterflies.
+  const int lane = tid & 31, warp = tid >> 5;
+  {
+    float a[16];
 #pragma unroll
-  for (int i = 0; i < kScoreSums; i++) {
+    for (int i = 0; i < 16; i++) a[i] = sums[i];
+#pragma unroll
+    for (int m = 8, off = 16; m >= 1; m >>= 1, off >>= 1) {
+      const bool upper = (lane & off) != 0;
+#pragma unroll
+      for (int i = 0; i < m; i++) {
+        const float keep = upper ? a[i + m] : a[i];
+        const float send = upper ? a[i] : a[i + m];
+        a[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+      }
+    }
+    a[0] += __shfl_xor_sync(0xffffffffu, a[0], 1);
+    if ((lane & 1) == 0) s_red[warp][lane >> 1] = a[0];
+  }
+#pragma unroll
+  for (int i = 16; i < kScoreSums; i++) {
     float v = sums[i];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    sums[i] = v;
-  }
-  const int lane = tid & 31, warp = tid >> 5;
-  if (lane == 0) {
-#pragma unroll
-    for (int i = 0; i < kScoreSums; i++) s_red[warp][i] = sums[i];
+    if (lane == 0) s_red[warp][i] = v;
   }
   __syncthreads();
   if (tid < kScoreSums) {
