@@ -783,7 +783,8 @@ def main():
             "metric": METRIC, "value": value, "unit": "searches/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": steps_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8/int16/f32 (integer+f32 codec, f32 scorer)", "data": "synthetic",
-            "config": dict(WORKLOAD, parallelism=f"replicas x{world}"),
+            "config": dict(WORKLOAD),
+            "replicas": world,
             "e2e": {"value": e2e_value, "unit": "searches/s", "h2d_bytes_per_step": W * H * 3,
                     "d2h_bytes_per_step": int(f.coefs.flat().nbytes) + 128 + 312},
             "gpu_launches": launches,

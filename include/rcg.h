@@ -118,10 +118,21 @@ int rcg_ctx_create(int device, rcg_ctx** out);
 void rcg_ctx_destroy(rcg_ctx* ctx);
 /* Message of the last failed call on this context ("" if none). Valid until the next call on it. */
 const char* rcg_last_error(const rcg_ctx* ctx);
-/* Run the context's work on a caller stream (a cudaStream_t; NULL restores the context's own stream). */
+/* Run the context's work on a caller stream (a cudaStream_t; NULL restores the context's own stream). The switch
+ * is ordered on the device: later work on the new stream waits for everything queued on the old one (an event
+ * recorded on the old stream, waited on by the new one), because both use the same context buffers. The host is
+ * not blocked. When either stream is being captured into a graph, that ordering is the capturing caller's. */
 int rcg_ctx_set_stream(rcg_ctx* ctx, void* stream);
 void* rcg_ctx_stream(const rcg_ctx* ctx);
 int rcg_ctx_synchronize(rcg_ctx* ctx);
+/* Near-tie band of the SSIMULACRA2 searches (rcg_search*, rcg_search_requantize*, the weighted and perceptual
+ * searches): jpeg/src/target.rs:48 accepts a candidate on score >= target, and the fast f32 scorer is within about
+ * 1e-6 of the reference, so a candidate whose fast score lies within `band` of the target is decided on its
+ * reference-order FP64 score (rcg_ssimulacra2_exact) instead, and that score is the one reported. Default 1e-3;
+ * 0 decides every candidate on the fast score; INFINITY decides every candidate on the exact score. */
+int rcg_ctx_set_tie_band(rcg_ctx* ctx, double band);
+/* Candidates this context has decided on the exact score so far. */
+uint64_t rcg_ctx_tie_rescores(const rcg_ctx* ctx);
 /* Kernels this context has launched so far (each kernel launch counts once). */
 uint64_t rcg_ctx_launch_count(const rcg_ctx* ctx);
 /* Per-kernel timing with CUDA events around every launch, for profiling: 1 on, 0 off. Off by default. */
@@ -151,6 +162,14 @@ int rcg_ssimulacra2(rcg_ctx* ctx, const uint8_t* reference, const uint8_t* disto
 /* The same on device buffers (8-bit Gray/Rgb only); no host<->device copies besides the 8-byte score. */
 int rcg_ssimulacra2_device(rcg_ctx* ctx, const uint8_t* d_reference, const uint8_t* d_distorted, uint32_t width,
                            uint32_t height, int channels, double* score);
+/* rc_core::ssimulacra2::ssimulacra2 (core/src/ssimulacra2.rs:471) in the reference's own arithmetic and order on the
+ * GPU: f32 linear planes and pyramid (2x2 means summed in f64), f64 XYB, blurs and maps, and the per-96-row-stripe
+ * sums added in the reference's order (:339-466), no FMA contraction. Equal to the reference's score up to the last
+ * bits of cbrt/pow (the reference calls the platform libm). Much slower than rcg_ssimulacra2 (FP64 plus serial stripe
+ * sums: tens of milliseconds at 12 MP); the searches use it to decide near ties (rcg_ctx_set_tie_band). Same
+ * arguments and errors as rcg_ssimulacra2. */
+int rcg_ssimulacra2_exact(rcg_ctx* ctx, const uint8_t* reference, const uint8_t* distorted, uint32_t width,
+                          uint32_t height, int channels, int depth, double* score);
 /* n calls of rc_core::ssimulacra2::ssimulacra2 (core/src/ssimulacra2.rs:471), one per pair, as a caller scoring many
  * files or many candidates does (cli/tests/ssimulacra2.rs:12-31 loops over 54 fixture pairs of different sizes;
  * cli/src/pipeline.rs:130-138 scores each candidate of each file). Pairs may differ in size and format
@@ -182,13 +201,15 @@ int rcg_ssimulacra2_batch_device(rcg_ctx* ctx, int n, const uint8_t* const* d_re
  * hosts that own every device allocation themselves -- a framework whose caching allocator holds a fixed device
  * budget, or a latency-critical loop where cudaMalloc/cudaFree would synchronize the whole device -- and so cannot let
  * a library call cudaMalloc. It needs no rcg_ctx. Scratch lives in one fixed device array compiled into the library
- * (about 10 MB, held on every GPU that loads the library until the process exits), so images are limited to
+ * (about 10 MB). CUDA loads a module's device arrays onto a device when the module is first used there, so the array
+ * is reserved on every device where any scorer call (allocating or not) has run, until the process exits; images are limited to
  * width*height <= 262144 pixels (e.g. 512x512); larger ones return RCG_INVALID, as do sides < 8 and channels other than
  * 1 or 3. The score (f64; NaN if it is not finite) is written to the device pointer `d_score`; the work is queued on
  * `stream` (a cudaStream_t, NULL for the legacy default stream) of the current device and the call returns without
  * waiting. The first call on a device sets up that device (looks up the scratch address and uploads constant tables),
  * so make it before any stream capture. Every call on a device shares the one scratch array: calls whose work overlaps
- * on the GPU (different streams, or other host threads) race and corrupt each other's results; serialize them. */
+ * on the GPU (different streams, or other host threads) race and corrupt each other's results; serialize them. The
+ * set-up is kept for the life of the process: calls after a cudaDeviceReset of that device are not supported. */
 int rcg_ssimulacra2_device_noalloc(const uint8_t* d_reference, const uint8_t* d_distorted, uint32_t width,
                                    uint32_t height, int channels, double* d_score, void* stream);
 

@@ -1,8 +1,8 @@
 """Build librcg.so (the CUDA library behind include/rcg.h) in-tree for sm_103a.
 
 Each translation unit is compiled by its own nvcc process in parallel, then linked with the static CUDA runtime.
-codec.cu is compiled with -fmad=false: the encoder and decoder reproduce the reference's f32 arithmetic bit for
-bit and must never contract a*b+c into an FMA. Host code gets -ffp-contract=off for the same reason (the host
+codec.cu and exact.cu are compiled with -fmad=false: the encoder and decoder reproduce the reference's f32
+arithmetic bit for bit, and the exact scorer its f64 arithmetic, so neither may contract a*b+c into an FMA. Host code gets -ffp-contract=off for the same reason (the host
 computes the per-quality tables that the device also computes).
 
 Usage: python rust-compress_gb300/build.py [--verbose] [--ptxas-info]
@@ -29,6 +29,7 @@ COMMON = ARCH + [
 ]
 UNITS = {
     "codec.cu": ["-fmad=false"],
+    "exact.cu": ["-fmad=false"],
     "ssim2.cu": [],
     "capi.cu": [],
     "plan.cu": [],

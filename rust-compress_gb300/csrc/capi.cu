@@ -33,7 +33,7 @@ int cuda_fail(rcg_ctx* ctx, cudaError_t e, const char* what) {
   return e == cudaErrorMemoryAllocation ? RCG_NO_MEMORY : RCG_CUDA_ERROR;
 }
 
-void* workspace(rcg_ctx* ctx, const char* name, size_t bytes) {
+void* workspace(rcg_ctx* ctx, const char* name, size_t bytes, bool in_graphs) {
   DeviceBuffer& b = ctx->bufs[name];
   if (b.ptr && b.bytes >= bytes) return b.ptr;
   if (b.ptr) {
@@ -51,7 +51,7 @@ void* workspace(rcg_ctx* ctx, const char* name, size_t bytes) {
   }
   cudaMemsetAsync(b.ptr, 0, sz, ctx->stream);
   b.bytes = sz;
-  ctx->ws_gen++;
+  if (in_graphs) ctx->ws_gen++;
   return b.ptr;
 }
 
@@ -527,6 +527,7 @@ void rcg_ctx_destroy(rcg_ctx* ctx) {
     cudaEventDestroy(p.b);
   }
   for (auto e : ctx->event_pool) cudaEventDestroy(e);
+  if (ctx->switch_event) cudaEventDestroy(ctx->switch_event);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
 }
@@ -535,7 +536,28 @@ const char* rcg_last_error(const rcg_ctx* ctx) { return ctx ? ctx->last_error.c_
 
 int rcg_ctx_set_stream(rcg_ctx* ctx, void* stream) {
   if (!ctx) return RCG_INVALID;
-  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+  cudaStream_t next = stream ? (cudaStream_t)stream : ctx->own_stream;
+  if (next == ctx->stream) return RCG_OK;
+  // The context's workspace and stored graphs move to the new stream with it: work still queued on the old stream
+  // must finish before the new stream touches the same buffers. An event recorded on the old stream and waited on
+  // by the new one orders them without blocking the host. A stream under capture is left to the capturing caller
+  // (an event of a capture cannot be waited on outside it).
+  cudaSetDevice(ctx->device);
+  cudaStreamCaptureStatus a = cudaStreamCaptureStatusNone, b = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(ctx->stream, &a) != cudaSuccess || cudaStreamIsCapturing(next, &b) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, RCG_CUDA_ERROR, "stream switch: cannot query the streams");
+  }
+  if (a == cudaStreamCaptureStatusNone && b == cudaStreamCaptureStatusNone) {
+    if (!ctx->switch_event) {
+      cudaError_t e = cudaEventCreateWithFlags(&ctx->switch_event, cudaEventDisableTiming);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "stream switch event");
+    }
+    cudaError_t e = cudaEventRecord(ctx->switch_event, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(next, ctx->switch_event, 0);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "stream switch ordering");
+  }
+  ctx->stream = next;
   return RCG_OK;
 }
 
@@ -591,6 +613,15 @@ int rcg_coef_layout_for(uint32_t width, uint32_t height, int channels, const rcg
   return RCG_OK;
 }
 
+int rcg_ctx_set_tie_band(rcg_ctx* ctx, double band) {
+  if (!ctx) return RCG_INVALID;
+  if (!(band >= 0.0)) return fail(ctx, RCG_INVALID, "the tie band must be >= 0");
+  ctx->tie_band = band;
+  return RCG_OK;
+}
+
+uint64_t rcg_ctx_tie_rescores(const rcg_ctx* ctx) { return ctx ? ctx->tie_rescores : 0; }
+
 // ---- scorer
 
 static int score_device_images(rcg_ctx* ctx, const uint8_t* d_ref, const uint8_t* d_dist, int w, int h, int channels,
@@ -631,6 +662,36 @@ int rcg_ssimulacra2(rcg_ctx* ctx, const uint8_t* reference, const uint8_t* disto
   if ((rc = copy_to_device(ctx, d_a, reference, bytes)) != RCG_OK) return rc;
   if ((rc = copy_to_device(ctx, d_b, distorted, bytes)) != RCG_OK) return rc;
   return score_device_images(ctx, d_a, d_b, (int)width, (int)height, channels, depth, score);
+}
+
+int rcg_ssimulacra2_exact(rcg_ctx* ctx, const uint8_t* reference, const uint8_t* distorted, uint32_t width,
+                          uint32_t height, int channels, int depth, double* score) {
+  if (!ctx) return RCG_INVALID;
+  if (!reference || !distorted || !score) return fail(ctx, RCG_INVALID, "null pointer");
+  if (channels < 1 || channels > 4 || (depth != 8 && depth != 16))
+    return fail(ctx, RCG_INVALID, "channels must be 1..4 and depth 8 or 16");
+  if (width < (uint32_t)kMinSide || height < (uint32_t)kMinSide)
+    return fail(ctx, RCG_INVALID, "SSIMULACRA 2 needs at least 8x8 pixels");
+  cudaSetDevice(ctx->device);
+  const int w = (int)width, h = (int)height;
+  const size_t bytes = (size_t)width * height * channels * (depth / 8), np = (size_t)3 * width * height;
+  uint8_t* d_a = (uint8_t*)workspace(ctx, "img_a", bytes);
+  uint8_t* d_b = (uint8_t*)workspace(ctx, "img_b", bytes);
+  float* lin = (float*)workspace(ctx, "x_lin", 2 * np * sizeof(float), false);
+  double* d_score = (double*)workspace(ctx, "x_score", sizeof(double), false);
+  if (!d_a || !d_b || !lin || !d_score) return RCG_NO_MEMORY;
+  int rc;
+  if ((rc = copy_to_device(ctx, d_a, reference, bytes)) != RCG_OK) return rc;
+  if ((rc = copy_to_device(ctx, d_b, distorted, bytes)) != RCG_OK) return rc;
+  if ((rc = to_linear(ctx, d_a, w, h, channels, depth, lin)) != RCG_OK) return rc;
+  if ((rc = to_linear(ctx, d_b, w, h, channels, depth, lin + np)) != RCG_OK) return rc;
+  if ((rc = exact_score(ctx, lin, lin + np, w, h, d_score)) != RCG_OK) return rc;
+  double s = 0.0;
+  cudaMemcpyAsync(&s, d_score, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if ((rc = finish(ctx, "ssimulacra2_exact")) != RCG_OK) return rc;
+  if (!std::isfinite(s)) return fail(ctx, RCG_INVALID, "SSIMULACRA 2 produced a non-finite score");
+  *score = s;
+  return RCG_OK;
 }
 
 int rcg_ssimulacra2_device(rcg_ctx* ctx, const uint8_t* d_reference, const uint8_t* d_distorted, uint32_t width,
@@ -1137,6 +1198,29 @@ static void score_candidate(rcg_ctx* ctx, const SearchScorer& sc, StepDesc* d_st
   score_pyramids(ctx, sc.pd, sc.ref_pyr, sc.dist_pyr, sc.d_score, d_ss, d_st);
 }
 
+// Near ties. jpeg/src/target.rs:48 accepts a candidate on s >= target; the fast scorer is within about 1e-6 of the
+// reference, so a candidate scored within ctx->tie_band of the target paused the device bisection (search_record,
+// done = 2) with its decoded linear planes still at scale 0 of the candidate pyramid (every later step was
+// inactive). Here it is rescored in the reference's f64 arithmetic and order on the GPU (exact_score), the bisection
+// records that score and goes on, and the remaining steps run as plain launches; repeated while a later candidate
+// pauses again. `issue_step` issues one bisection step's kernels.
+static int settle_ties(rcg_ctx* ctx, const SearchScorer& sc, SearchState* d_ss, SearchState* hs, int max_steps,
+                       int w, int h, const std::function<void()>& issue_step) {
+  while (hs->done == 2) {
+    if (sc.metric != RCG_METRIC_SSIMULACRA2) return fail(ctx, RCG_INVALID, "paused search without a rescorer");
+    double* d_exact = (double*)workspace(ctx, "x_score", sizeof(double), false);
+    if (!d_exact) return RCG_NO_MEMORY;
+    int rc = exact_score(ctx, sc.ref_pyr, sc.dist_pyr, w, h, d_exact);
+    if (rc != RCG_OK) return rc;
+    search_resume(ctx, d_ss, d_exact);
+    ctx->tie_rescores++;
+    for (int s = hs->step + 1; s < max_steps; s++) issue_step();
+    cudaMemcpyAsync(hs, d_ss, sizeof *hs, cudaMemcpyDeviceToHost, ctx->stream);
+    if ((rc = finish(ctx, "search after a near tie")) != RCG_OK) return rc;
+  }
+  return RCG_OK;
+}
+
 // d_weights (nullable): the perceptual trellis's weights in the coefficient layout of the (quality-independent)
 // subsampling; every candidate's trellis then runs in the weighted mode.
 static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, int metric, double target,
@@ -1177,23 +1261,26 @@ static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int cha
   hs.trellis = trellis_on;
   hs.channels = channels;
   hs.best_q = max_q;
+  hs.tie_band = metric == RCG_METRIC_SSIMULACRA2 ? ctx->tie_band : 0.0;
   cudaMemcpyAsync(d_ss, &hs, sizeof hs, cudaMemcpyHostToDevice, ctx->stream);
   // Every launch below takes pointers into this context's workspace and sizes that follow from the key.
   const std::vector<long long> key = {1, (long long)(uintptr_t)d_src, w, h, channels, metric, subsampling, trellis_on,
                                       max_steps, (long long)(uintptr_t)d_weights};
+  auto issue_step = [&]() {
+    step_tables(ctx, d_ss, d_st, w, h, slots, es.max_coefs, d_weights);
+    quantize(ctx, d_st, es.caches, es.max_blocks);
+    rate_tables(ctx, d_st);
+    trellis(ctx, d_st, es.caches, es.max_blocks, d_weights != nullptr);
+    dequant_idct(ctx, d_st, nullptr, planes, es.max_blocks);
+    score_candidate(ctx, sc, d_st, planes, w, h, channels, d_ss);
+  };
   rc = run_step_loop(ctx, key, [&]() {
-    for (int s = 0; s < max_steps; s++) {
-      step_tables(ctx, d_ss, d_st, w, h, slots, es.max_coefs, d_weights);
-      quantize(ctx, d_st, es.caches, es.max_blocks);
-      rate_tables(ctx, d_st);
-      trellis(ctx, d_st, es.caches, es.max_blocks, d_weights != nullptr);
-      dequant_idct(ctx, d_st, nullptr, planes, es.max_blocks);
-      score_candidate(ctx, sc, d_st, planes, w, h, channels, d_ss);
-    }
+    for (int s = 0; s < max_steps; s++) issue_step();
   });
   if (rc != RCG_OK) return rc;
   cudaMemcpyAsync(&hs, d_ss, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream);
   if ((rc = finish(ctx, "search")) != RCG_OK) return rc;
+  if ((rc = settle_ties(ctx, sc, d_ss, &hs, max_steps, w, h, issue_step)) != RCG_OK) return rc;
   if (!hs.done) return fail(ctx, RCG_TIMEOUT, "bisection did not finish within the step budget");
   found->quality = hs.best_q;
   found->score = hs.best_score;
@@ -1298,6 +1385,12 @@ int rcg_search_batch(rcg_ctx* ctx, int n, const uint8_t* const* srcs, const uint
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
     return (uint64_t)widths[a] * heights[a] > (uint64_t)widths[b] * heights[b];
   });
+  // The workers decide near ties like the caller's context, and their rescores count toward it.
+  std::vector<uint64_t> ties0;
+  for (int t = 0; t < p; t++) {
+    ctx->workers[t]->tie_band = ctx->tie_band;
+    ties0.push_back(ctx->workers[t]->tie_rescores);
+  }
   std::atomic<int> next(0);
   std::vector<int> status(n, RCG_OK);
   std::vector<std::string> messages(n);
@@ -1315,6 +1408,7 @@ int rcg_search_batch(rcg_ctx* ctx, int n, const uint8_t* const* srcs, const uint
   for (int t = 1; t < p; t++) threads.emplace_back(work, ctx->workers[t]);
   work(ctx->workers[0]);
   for (auto& th : threads) th.join();
+  for (int t = 0; t < p; t++) ctx->tie_rescores += ctx->workers[t]->tie_rescores - ties0[t];
   for (int i = 0; i < n; i++)
     if (status[i] != RCG_OK) return fail(ctx, status[i], "image " + std::to_string(i) + ": " + messages[i]);
   ctx->last_error.clear();
@@ -1438,6 +1532,7 @@ static int search_requantize_impl(rcg_ctx* ctx, uint32_t width, uint32_t height,
   hs.trellis = trellis;
   hs.channels = channels;
   hs.best_q = max_q;
+  hs.tie_band = metric == RCG_METRIC_SSIMULACRA2 ? ctx->tie_band : 0.0;
   cudaMemcpyAsync(d_ss, &hs, sizeof hs, cudaMemcpyHostToDevice, ctx->stream);
   const float* no_caches[9] = {nullptr};
   std::vector<long long> key = {2, (long long)(uintptr_t)d_src, w, h, st->ncomp, metric, trellis, max_steps,
@@ -1446,22 +1541,24 @@ static int search_requantize_impl(rcg_ctx* ctx, uint32_t width, uint32_t height,
     const CompDesc& cd = st->comp[c];
     key.insert(key.end(), {cd.bw, cd.bh, cd.h, cd.v, cd.blk0, cd.plane_off});
   }
+  auto issue_step = [&]() {
+    step_tables_requant(ctx, d_ss, d_st, slots, nblocks * 64);
+    requantize_plain(ctx, d_st, nblocks);
+    rate_tables(ctx, d_st);
+    rcg::trellis(ctx, d_st, no_caches, nblocks);
+    dequant_idct(ctx, d_st, nullptr, planes, nblocks);
+    score_candidate(ctx, sc, d_st, planes, w, h, channels, d_ss);
+  };
   rc = run_step_loop(ctx, key, [&]() {
-    for (int s = 0; s < max_steps; s++) {
-      step_tables_requant(ctx, d_ss, d_st, slots, nblocks * 64);
-      requantize_plain(ctx, d_st, nblocks);
-      rate_tables(ctx, d_st);
-      rcg::trellis(ctx, d_st, no_caches, nblocks);
-      dequant_idct(ctx, d_st, nullptr, planes, nblocks);
-      score_candidate(ctx, sc, d_st, planes, w, h, channels, d_ss);
-    }
+    for (int s = 0; s < max_steps; s++) issue_step();
   });
   if (rc != RCG_OK) {
     delete st;
     return rc;
   }
   cudaMemcpyAsync(&hs, d_ss, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream);
-  if ((rc = finish(ctx, "search_requantize")) != RCG_OK) {
+  if ((rc = finish(ctx, "search_requantize")) != RCG_OK ||
+      (rc = settle_ties(ctx, sc, d_ss, &hs, max_steps, w, h, issue_step)) != RCG_OK) {
     delete st;
     return rc;
   }

@@ -104,16 +104,25 @@ struct SearchState {
   int qs[kMaxSteps];
   double scores[kMaxSteps];
   int status;            // nonzero: a device-side check failed
+  // Near ties: a candidate whose score lies within tie_band of the target pauses the search (done = 2) so that the
+  // host can decide it on the reference-order FP64 score (exact.cu); 0 disables the pause.
+  double tie_band;
 };
 
 // One bisection step of jpeg/src/target.rs:35-53 on the device, after candidate `ss->step` scored `sv`: the first
 // candidate (max quality) ends the search when it misses the target; later ones move hi (accepted, s >= target) or
 // lo; the next quality is lo + (hi - lo) / 2 until lo == hi.
-__device__ __forceinline__ void search_record(SearchState* ss, double sv) {
+// A candidate scored within tie_band of the target (by the fast f32 scorer) pauses instead: done = 2, the step and
+// its score kept, nothing decided; search_resume later records the candidate's exact score with the pause disabled.
+__device__ __forceinline__ void search_record(SearchState* ss, double sv, bool may_pause = true) {
   if (ss->done) return;
   const int step = ss->step;
   const int q = ss->qs[step];
   ss->scores[step] = sv;
+  if (may_pause && ss->tie_band > 0.0 && fabs(sv - ss->target) <= ss->tie_band) {
+    ss->done = 2;
+    return;
+  }
   if (step == 0) {
     ss->best_q = q;
     ss->best_score = sv;
@@ -155,6 +164,7 @@ struct rcg_ctx {
   int device = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  cudaEvent_t switch_event = nullptr;  // orders a stream switch after the old stream's queued work
   std::string last_error;
   uint64_t launches = 0;
   bool profiling = false;
@@ -191,6 +201,10 @@ struct rcg_ctx {
   // Loops run as plain launches lately (key, ws_gen): captured when one comes again with the same ws_gen.
   std::vector<std::pair<std::vector<long long>, uint64_t>> warm;
   uint64_t graph_tick = 0, graph_captures = 0, graph_replays = 0;
+  // Near-tie rescoring of the SSIMULACRA2 searches (exact.cu): band around the target, and how many candidates were
+  // decided on the reference-order FP64 score so far.
+  double tie_band = 1e-3;
+  uint64_t tie_rescores = 0;
 };
 
 namespace rcg {
@@ -199,8 +213,10 @@ namespace rcg {
 int fail(rcg_ctx* ctx, int status, const std::string& msg);
 int cuda_fail(rcg_ctx* ctx, cudaError_t e, const char* what);
 
-// Grow-only named device workspace. Returns nullptr (and sets the error) on allocation failure.
-void* workspace(rcg_ctx* ctx, const char* name, size_t bytes);
+// Grow-only named device workspace. Returns nullptr (and sets the error) on allocation failure. A (re)allocation
+// retires the context's stored graphs unless `in_graphs` is false: buffers that no captured step loop uses (the exact
+// scorer's) move without making the graphs stale.
+void* workspace(rcg_ctx* ctx, const char* name, size_t bytes, bool in_graphs = true);
 
 // Host<->device copies of caller buffers: the driver's path for single calls; on batch worker contexts direct DMA when
 // the caller's memory is pinned, else through the context's pinned staging buffer. copy_to_device is asynchronous on the context stream (the source may be reused as soon as it
@@ -250,6 +266,11 @@ int build_pyramid_gated(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, const
 // `search` is non-null the final kernel also advances the device-side bisection.
 int score_pyramids(rcg_ctx* ctx, const PyramidDesc& pd, const float* d_ref, const float* d_dist, double* d_score,
                    SearchState* search, StepDesc* step);
+// The reference-order FP64 score (exact.cu) of two images given as scale-0 linear planes ([3][h][w] f32, as
+// to_linear writes them): to d_score (NaN for the reference's non-finite Err), queued on the context stream.
+int exact_score(rcg_ctx* ctx, const float* d_ref0, const float* d_dist0, int w, int h, double* d_score);
+// Record the exact score of a paused search's candidate (search_record without the pause) and let it go on.
+int search_resume(rcg_ctx* ctx, SearchState* d_ss, const double* d_score);
 // Allocate (or find) the scratch score_pyramids uses for a pyramid of this geometry.
 int score_workspace(rcg_ctx* ctx, const PyramidDesc& pd);
 // Score n device-resident pairs (checked sizes and formats; depths nullable = 8) with the work-list kernels;

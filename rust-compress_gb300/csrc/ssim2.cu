@@ -1049,8 +1049,10 @@ int score_batch(rcg_ctx* ctx, int n, const uint8_t* const* d_refs, const uint8_t
 namespace rcg {
 
 // Fixed scratch of rcg_ssimulacra2_device_noalloc: both images' linear pyramids, the per-tile partial sums, the
-// per-scale sums and the reduction's completion counter. Sized for images of at most kNoAllocMaxPixels pixels; every
-// GPU that loads this library holds it (about 10 MB) until the process exits.
+// per-scale sums and the reduction's completion counter. Sized for images of at most kNoAllocMaxPixels pixels. CUDA
+// places a module's device arrays on a device when the module is first used there, so every device where any scorer
+// call has run holds it (about 10 MB) until the process exits. The per-device set-up below is cached for the life of
+// the process; a cudaDeviceReset invalidates it and is not supported.
 constexpr long long kNoAllocMaxPixels = 512LL * 512LL;
 constexpr long long kNoAllocPyrFloats = 1200000;  // one image: 3 channels x every scale, with margin
 constexpr int kNoAllocMaxTiles = 4096;

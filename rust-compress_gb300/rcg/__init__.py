@@ -10,8 +10,9 @@ Names and argument meaning follow rust-compress:
 Errors surface as RcgError carrying the C status (Invalid / Unsupported like rc_core::error::Error).
 
 Images are numpy uint8 arrays: (h, w, 3) for Rgb, (h, w) or (h, w, 1) for Gray; the scorer also takes
-(h, w, 2|4) with alpha and uint16 arrays (16-bit samples). The library is loaded from this directory; there is no
-fallback: if librcg.so is missing or cannot be loaded, importing the bindings raises.
+(h, w, 2|4) with alpha and uint16 arrays (16-bit samples). The library is loaded from this directory on first use
+(creating a Context, or lib()), so importing the package or rcg.synth maps no GPU code; there is no fallback: if
+librcg.so is missing or cannot be loaded, that first use raises.
 """
 
 import ctypes
@@ -256,6 +257,9 @@ def _load():
         "rcg_coef_layout_for": (i32, [u32, u32, i32, ctypes.POINTER(_Opts), ctypes.POINTER(_Layout)]),
         "rcg_ssimulacra2": (i32, [P, P, P, u32, u32, i32, i32, ctypes.POINTER(ctypes.c_double)]),
         "rcg_ssimulacra2_device": (i32, [P, P, P, u32, u32, i32, ctypes.POINTER(ctypes.c_double)]),
+        "rcg_ssimulacra2_exact": (i32, [P, P, P, u32, u32, i32, i32, ctypes.POINTER(ctypes.c_double)]),
+        "rcg_ctx_set_tie_band": (i32, [P, ctypes.c_double]),
+        "rcg_ctx_tie_rescores": (ctypes.c_uint64, [P]),
         "rcg_ssimulacra2_device_noalloc": (i32, [P, P, u32, u32, i32, P, P]),
         "rcg_build_coefs": (i32, [P, P, u32, u32, i32, ctypes.POINTER(_Opts), P, sz, P]),
         "rcg_reconstruct": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, P, P, sz]),
@@ -305,7 +309,21 @@ def _load():
     return lib
 
 
-_lib = _load()
+class _LazyLib:
+    """librcg.so, loaded (and its signatures declared) on the first attribute access."""
+
+    _real = None
+
+    def get(self):
+        if _LazyLib._real is None:
+            _LazyLib._real = _load()
+        return _LazyLib._real
+
+    def __getattr__(self, name):
+        return getattr(self.get(), name)
+
+
+_lib = _LazyLib()
 EXPORTED = (
     "rcg_ctx_create rcg_ctx_destroy rcg_last_error rcg_ctx_set_stream rcg_ctx_stream rcg_ctx_synchronize "
     "rcg_ctx_launch_count rcg_ctx_set_profiling rcg_ctx_kernel_time rcg_coef_layout_for rcg_ssimulacra2 "
@@ -315,12 +333,13 @@ EXPORTED = (
     "rcg_search_requantize_device rcg_ssimulacra2_grad rcg_ssimulacra2_grad_device rcg_perceptual_defaults "
     "rcg_coef_gradient rcg_perceptual_weights rcg_build_coefs_weighted rcg_search_weighted rcg_search_perceptual "
     "rcg_perceptual_strength rcg_ctx_set_graphs rcg_ctx_graph_stats rcg_ssimulacra2_batch rcg_ssimulacra2_batch_device "
-    "rcg_sweep_qualities"
+    "rcg_sweep_qualities rcg_ssimulacra2_exact rcg_ctx_set_tie_band rcg_ctx_tie_rescores"
 ).split()
 
 
 def lib():
-    return _lib
+    """The loaded librcg.so (loads it on first call; raises if it is missing)."""
+    return _lib.get()
 
 
 def _opts(o):
@@ -406,6 +425,15 @@ class Context:
         self._check(_lib.rcg_ctx_graph_stats(self._ptr, ctypes.byref(c), ctypes.byref(r)))
         return int(c.value), int(r.value)
 
+    def set_tie_band(self, band):
+        """Near-tie band of the SSIMULACRA2 searches: candidates whose fast score lies within `band` of the target
+        are decided on their reference-order FP64 score (default 1e-3; 0 never, math.inf always)."""
+        self._check(_lib.rcg_ctx_set_tie_band(self._ptr, float(band)))
+
+    def tie_rescores(self):
+        """Candidates this context has decided on the reference-order FP64 score so far."""
+        return int(_lib.rcg_ctx_tie_rescores(self._ptr))
+
     def kernel_time(self, name):
         n = ctypes.c_uint64()
         ms = ctypes.c_double()
@@ -423,6 +451,20 @@ class Context:
             raise RcgError(RCG_INVALID, "images differ in colour type")
         out = ctypes.c_double()
         self._check(_lib.rcg_ssimulacra2(self._ptr, a.ctypes.data, b.ctypes.data, w, h, c, d, ctypes.byref(out)))
+        return out.value
+
+    def ssimulacra2_exact(self, reference, distorted):
+        """The same score in the reference's own f64 arithmetic and order (rcg_ssimulacra2_exact): equal to
+        core/src/ssimulacra2.rs:471's result up to the last bits of cbrt/pow; much slower than ssimulacra2."""
+        a, w, h, c, d = _image(reference)
+        b, w2, h2, c2, d2 = _image(distorted)
+        if (w, h) != (w2, h2):
+            raise RcgError(RCG_INVALID, "images differ in size")
+        if (c, d) != (c2, d2):
+            raise RcgError(RCG_INVALID, "images differ in colour type")
+        out = ctypes.c_double()
+        self._check(_lib.rcg_ssimulacra2_exact(self._ptr, a.ctypes.data, b.ctypes.data, w, h, c, d,
+                                               ctypes.byref(out)))
         return out.value
 
     def ssimulacra2_batch(self, pairs):

@@ -141,3 +141,31 @@ def test_graphs_on_a_caller_stream():
         g.set_stream(0)  # back to the context's own stream: the stored graph replays there too
         _same(g.find_quality_ssimulacra2(img, 72.0, 100, opts), want)
         assert g.graph_stats() == (1, 3)
+
+
+def test_stream_switch_orders_work_queued_on_the_old_stream():
+    """A stream switch orders the new stream after everything queued on the old one: an upload of the image queued
+    on the old stream behind a long spin must land before a device search issued on the new stream reads it."""
+    torch = pytest.importorskip("torch")
+    w, h = 320, 240
+    img = synth.image(w, h, 48)
+    opts = rcg.EncodeOptions(90, rcg.Subsampling.S420, True)
+    with rcg.Context(0) as plain, rcg.Context(0) as g:
+        want = plain.find_quality_ssimulacra2(img, 72.0, 100, opts)
+        lay = g.coef_layout(w, h, 3, rcg.EncodeOptions(100, rcg.Subsampling.S420, True))
+        s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+        dev = torch.zeros(img.size, dtype=torch.uint8, device="cuda")
+        coefs = torch.zeros(lay.ncoefs, dtype=torch.int16, device="cuda")
+        host = torch.from_numpy(img.reshape(-1).copy()).pin_memory()
+        torch.cuda.synchronize()
+        for a, b in ((s1, s2), (s2, s1)):
+            dev.zero_()
+            torch.cuda.synchronize()
+            g.set_stream(a.cuda_stream)
+            with torch.cuda.stream(a):
+                torch.cuda._sleep(100_000_000)  # tens of milliseconds of spinning ahead of the upload
+                dev.copy_(host, non_blocking=True)
+            g.set_stream(b.cuda_stream)
+            q, s, trace = g.search_device(dev.data_ptr(), w, h, 3, 72.0, 100, opts, coefs.data_ptr(), lay.ncoefs)
+            assert (q, s, trace) == (want.quality, want.score, want.trace)
+        g.set_stream(0)

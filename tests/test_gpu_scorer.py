@@ -90,17 +90,19 @@ def test_awkward_sizes_match_the_oracle(ctx, oracle, w, h):
 
 
 def test_large_pair_vs_oracle_and_fp64(ctx, oracle):
-    """A 4K-class pair (the scorer workload's shape, reduced to keep the oracle fast): error vs both oracles."""
+    """The scorer workload itself: a 3840x2160 pair (synthetic seed 0 against its q50 4:2:0 round trip through the
+    reference's JPEG path), with the error against the reference-exact oracle and the FP64 oracle printed."""
     import rcg.synth as synth
 
-    w, h = 1920, 1080
+    w, h = 3840, 2160
     ref = synth.image(w, h, 0)
     coefs, qt, lay = oracle.build_coefs(ref, 50, 3, True)
     dist = oracle.reconstruct(w, h, lay, qt, coefs)
     got = ctx.ssimulacra2(ref, dist)
     want = oracle.ssimulacra2(ref, dist)
     want64 = oracle.ssimulacra2(ref, dist, fp64=True)
-    print(f"gpu {got:.9f} oracle {want:.9f} fp64 {want64:.9f}")
+    print(f"gpu {got:.9f} oracle {want:.9f} fp64 {want64:.9f}: |gpu - oracle| {abs(got - want):.2e}, "
+          f"|gpu - fp64| {abs(got - want64):.2e}")
     assert abs(got - want) <= TOL_ORACLE
     assert abs(got - want64) <= TOL_ORACLE
 

@@ -1,9 +1,10 @@
 """The device-driven --target-ssimulacra2 search against the oracle's find_quality_with.
 
-Per step the GPU and the oracle encode the same coefficients (bit-exact) and score them within 1e-3; the bisection
-then takes the same path unless a score lands within that tolerance of the target, which these cases avoid and the
-test reports. The chosen coefficients must be bit-exact with the oracle's, and the bitstream written from them
-(the oracle's write_best, standing in for the Rust host's entropy coder) byte-identical.
+Per step the GPU and the oracle encode the same coefficients (bit-exact) and score them within 1e-3; a candidate
+whose fast score lands within 1e-3 of the target is decided on its reference-order FP64 score (within 1e-9 of the
+oracle's), so the bisection takes the oracle's path in every case. The chosen coefficients must be bit-exact with the
+oracle's, and the bitstream written from them (the oracle's write_best, standing in for the Rust host's entropy
+coder) byte-identical.
 """
 
 import hashlib
@@ -21,9 +22,6 @@ def _compare(ctx, oracle, img, target, sub, trellis=True, max_q=100):
     h, w = img.shape[:2]
     f = ctx.find_quality_ssimulacra2(img, target, max_q, rcg.EncodeOptions(90, sub, trellis))
     q, s, coefs, qt, lay, trace = oracle.search(img, target, max_q, int(sub), trellis)
-    near = [abs(ts - target) < 1e-3 for _, ts in trace]
-    if any(near):
-        pytest.skip("a candidate scored within the score tolerance of the target")
     assert [t[0] for t in f.trace] == [t[0] for t in trace], (f.trace, trace)
     for (gq, gs), (oq, os_) in zip(f.trace, trace):
         assert abs(gs - os_) <= 1e-3, (gq, gs, os_)
