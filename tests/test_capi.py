@@ -74,3 +74,28 @@ def test_perceptual_defaults_match_the_python_options():
     # the strength schedule is host arithmetic: checkable without a GPU
     assert [d.strength_for(q) for q in (1, 69, 70, 84, 85, 100)] == [0.35, 0.35, 0.7, 0.7, 1.0, 1.0]
     assert rcg.PerceptualOptions(strength=0.5, strength_by_quality=False).strength_for(90) == 0.5
+
+
+def _rust_externs():
+    src = open(os.path.join(ROOT, "rust-compress_gb300", "rcg-sys", "src", "lib.rs")).read()
+    block = src[src.index('extern "C" {'):]
+    out = {}
+    for m in re.finditer(r"pub fn (rcg_[a-z0-9_]+)\((.*?)\)", block, flags=re.S):
+        args = [a for a in m.group(2).split(",") if a.strip()]
+        out[m.group(1)] = len(args)
+    return out
+
+
+def _c_arities():
+    src = open(os.path.join(ROOT, "include", "rcg.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return {m.group(1): len([a for a in m.group(2).split(",") if a.strip()])
+            for m in re.finditer(r"\b(rcg_[a-z0-9_]+)\s*\(([^;]*?)\)\s*;", src, flags=re.S)}
+
+
+def test_rust_binding_matches_the_header():
+    """rcg-sys (the uncompiled Rust FFI crate a maintainer adds to rust-compress) declares every header function
+    with the same number of parameters."""
+    rust, c = _rust_externs(), _c_arities()
+    assert set(rust) == set(c), (set(c) - set(rust), set(rust) - set(c))
+    assert {k: v for k, v in rust.items() if c[k] != v} == {}

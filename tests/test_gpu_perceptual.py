@@ -117,6 +117,28 @@ def test_weighted_search_matches_the_oracle(ctx, oracle):
     assert np.array_equal(f.coefs.flat(), coefs)
 
 
+def test_weighted_search_at_the_workload_size(ctx, oracle):
+    """The perceptual trellis at the size it is specified for: 4000x3000 (seed 1, sensor noise sigma 3), target 70,
+    4:2:0, the weights of the perceptual search's own schedule at the plain result; the weighted search visits the
+    oracle's qualities and returns its coefficients bit for bit."""
+    img = synth.image(4000, 3000, 1, 3.0)
+    sub = rcg.Subsampling.S420
+    opts = rcg.EncodeOptions(90, sub, True)
+    plain = ctx.find_quality_ssimulacra2(img, 70.0, 100, opts)
+    dec = ctx.reconstruct(plain.coefs)
+    lay = ctx.coef_layout(4000, 3000, 3, rcg.EncodeOptions(50, sub, True))
+    popts = rcg.PerceptualOptions()
+    popts.strength = popts.strength_for(plain.quality)
+    _, wts = ctx.perceptual_weights(img, dec, lay, popts)
+    f = ctx.find_quality_weighted(img, 70.0, wts, 100, opts)
+    q, s, coefs, qt, olay, trace = oracle.search(img, 70.0, 100, int(sub), True, weights=wts)
+    assert [t[0] for t in f.trace] == [t[0] for t in trace], (f.trace, trace)
+    for (_, x), (_, y) in zip(f.trace, trace):
+        assert abs(x - y) <= 1e-3
+    assert f.quality == q
+    assert np.array_equal(f.coefs.flat(), coefs)
+
+
 def test_perceptual_search(ctx):
     img = synth.image(640, 480, 94, sensor_sigma=3.0)
     opts = rcg.EncodeOptions(90, rcg.Subsampling.S420, True)

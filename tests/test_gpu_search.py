@@ -115,3 +115,23 @@ def test_batch_reports_the_failing_image(ctx):
     with pytest.raises(rcg.RcgError) as e:
         ctx.search_batch(imgs, [60.0, 60.0, 60.0], 100, rcg.EncodeOptions(90, rcg.Subsampling.S420, True), 2)
     assert e.value.status == rcg.RCG_UNSUPPORTED and "image 1" in e.value.message
+
+
+def test_batch_at_the_large_end_of_the_image_set(ctx, oracle):
+    """The four largest images of the 64-image set (seeds 2..65, log-uniform 640x480..6000x4000, targets U(55,85))
+    through rcg_search_batch, each against the oracle's search: same path, coefficients and file."""
+    sizes = synth.log_uniform_sizes(2, 64)
+    targets = [55.0 + 30.0 * u for u in synth.uniforms(2, 40, 64)]
+    largest = sorted(range(64), key=lambda i: sizes[i][0] * sizes[i][1])[-4:]
+    imgs = [synth.image(sizes[i][0], sizes[i][1], 2 + i) for i in largest]
+    tgts = [targets[i] for i in largest]
+    opts = rcg.EncodeOptions(90, rcg.Subsampling.S420, True)
+    res = ctx.search_batch(imgs, tgts, 100, opts, parallel=4)
+    for img, t, r in zip(imgs, tgts, res):
+        h, w = img.shape[:2]
+        q, s, coefs, qt, lay, trace = oracle.search(img, t, 100, 3, True)
+        assert [x[0] for x in r.trace] == [x[0] for x in trace], (w, h, r.trace, trace)
+        assert r.quality == q and np.array_equal(r.coefs.flat(), coefs), (w, h)
+        a, _ = oracle.write_best(w, h, lay, r.coefs.qtables, r.coefs.flat())
+        b, _ = oracle.write_best(w, h, lay, qt, coefs)
+        assert hashlib.sha256(a).hexdigest() == hashlib.sha256(b).hexdigest()
