@@ -133,6 +133,16 @@ int rcg_ctx_synchronize(rcg_ctx* ctx);
 int rcg_ctx_set_tie_band(rcg_ctx* ctx, double band);
 /* Candidates this context has decided on the exact score so far. */
 uint64_t rcg_ctx_tie_rescores(const rcg_ctx* ctx);
+/* The fast scorer's CTA shape. No counterpart option in the reference; its own shape parameter is the 96-row stripe
+ * of core/src/ssimulacra2.rs:33. Each CTA walks a band 32 columns wide and `chunks` x 32 rows tall, computing the XYB
+ * of the rows it shares between chunks once. 0 (the default) autotunes: the first image of each size class (scale-0
+ * tiles in half-octave steps) on a device times the candidates 1, 2, 4 and 8 and the fastest is kept for the
+ * process; images under about 1 MP always use 1 (plain 32x32 tiles). A fixed 1..64 applies to every image this
+ * context scores. Scores move by about 1e-9 between shapes; for one shape they are the same bits every call. */
+int rcg_ctx_set_band_chunks(rcg_ctx* ctx, int chunks);
+/* The chunks per band this context uses for a width x height image (autotuning its size class first if needed);
+ * 0 for sizes the scorer rejects. */
+int rcg_ctx_band_chunks(rcg_ctx* ctx, uint32_t width, uint32_t height);
 /* Kernels this context has launched so far (each kernel launch counts once). */
 uint64_t rcg_ctx_launch_count(const rcg_ctx* ctx);
 /* Per-kernel timing with CUDA events around every launch, for profiling: 1 on, 0 off. Off by default. */

@@ -622,6 +622,19 @@ int rcg_ctx_set_tie_band(rcg_ctx* ctx, double band) {
 
 uint64_t rcg_ctx_tie_rescores(const rcg_ctx* ctx) { return ctx ? ctx->tie_rescores : 0; }
 
+int rcg_ctx_set_band_chunks(rcg_ctx* ctx, int chunks) {
+  if (!ctx) return RCG_INVALID;
+  if (chunks < 0 || chunks > 64) return fail(ctx, RCG_INVALID, "band chunks must be 0 (autotune) or 1..64");
+  ctx->band_chunks = chunks;
+  return RCG_OK;
+}
+
+int rcg_ctx_band_chunks(rcg_ctx* ctx, uint32_t width, uint32_t height) {
+  if (!ctx || width < (uint32_t)kMinSide || height < (uint32_t)kMinSide) return 0;
+  cudaSetDevice(ctx->device);
+  return band_chunks(ctx, make_pyramid((int)width, (int)height));
+}
+
 // ---- scorer
 
 static int score_device_images(rcg_ctx* ctx, const uint8_t* d_ref, const uint8_t* d_dist, int w, int h, int channels,

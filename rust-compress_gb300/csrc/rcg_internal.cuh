@@ -31,8 +31,9 @@ constexpr int kTileThreads = 256;
 // One scale of the scorer's pyramid: planes are channel-planar f32, [3][h][w], at `off` (floats) in a pyramid buffer.
 struct ScaleDesc {
   int w, h;
-  int tiles_x, tiles_y;
+  int tiles_x, tiles_y;  // CTAs across and down (32-column bands of nch chunks of 32 rows; nch = 1: 32x32 tiles)
   int tile0;        // first CTA of this scale in the multi-scale launch
+  int nch;          // 32-row chunks per CTA (ssim2.cu, ssim2_band)
   long long off;    // float offset of channel 0 of this scale
 };
 
@@ -205,6 +206,8 @@ struct rcg_ctx {
   // decided on the reference-order FP64 score so far.
   double tie_band = 1e-3;
   uint64_t tie_rescores = 0;
+  // Scorer bands: 0 autotunes the chunks per band per size class (ssim2.cu, band_chunks); >= 1 fixes them.
+  int band_chunks = 0;
 };
 
 namespace rcg {
@@ -271,6 +274,14 @@ int score_pyramids(rcg_ctx* ctx, const PyramidDesc& pd, const float* d_ref, cons
 int exact_score(rcg_ctx* ctx, const float* d_ref0, const float* d_dist0, int w, int h, double* d_score);
 // Record the exact score of a paused search's candidate (search_record without the pause) and let it go on.
 int search_resume(rcg_ctx* ctx, SearchState* d_ss, const double* d_score);
+// The scorer's CTA layout for a pyramid: 32-column bands of `nch0` chunks of 32 rows at the scales with at least
+// `min_tiles` tiles, 32x32 tiles elsewhere (nch0 = 1: tiles everywhere).
+PyramidDesc banded(const PyramidDesc& pd, int nch0, int min_tiles);
+// The layout a context scores this pyramid with (its fixed chunks at every scale, or the tuned ones).
+PyramidDesc plan_bands(rcg_ctx* ctx, const PyramidDesc& pd);
+// Chunks per band for a pyramid of this geometry: the context's fixed choice, or the process-wide autotuned one for
+// its size class (tuned on first use by timing the candidates; small images always take 1).
+int band_chunks(rcg_ctx* ctx, const PyramidDesc& pd);
 // Allocate (or find) the scratch score_pyramids uses for a pyramid of this geometry.
 int score_workspace(rcg_ctx* ctx, const PyramidDesc& pd);
 // Score n device-resident pairs (checked sizes and formats; depths nullable = 8) with the work-list kernels;

@@ -133,36 +133,45 @@ constexpr int kHx = 4;                     // horizontal-pass outputs per item
 constexpr int kIHp = (kIH + 3) / 4 * 4;    // rows rounded up to the 4-row item groups
 constexpr size_t kTileSmem = (size_t)(6 * kIH * kIW + 5 * kIH * kTileW) * sizeof(float);
 
-// One CTA = one 32x32 output tile of one scale. Shared memory: per channel the (a', d') pairs of the tile plus its
-// 5-pixel halo; then per channel the horizontally blurred five moments of the 42 halo rows. The blurs run the
-// moment pairs that share a tap weight ((a', d'), (a'^2, b'^2)) as packed two-lane f32 FMAs, each lane exactly
-// fmaf, so the results are those of scalar FMAs in the same order.
-// Tile `local` of scale `sd` of a pyramid pair; the tile's 18 sums go to out[i * stride], i < 18.
-__device__ __forceinline__ void ssim2_tile(const ScaleDesc sd, const int local, const float* __restrict__ ref,
+// One CTA = one band of 32 output columns and nch chunks of 32 output rows of one scale, walked top to bottom.
+// Shared memory: per channel the (a', d') pairs of the chunk plus its 5-pixel halo (42 x 42); then per channel the
+// horizontally blurred five moments of the 42 halo rows. Between chunks the 10 halo rows that the next chunk shares
+// with this one (its top halo and first output rows) move to the top of the buffer instead of being converted to XYB
+// again, so a band pays the vertical halo's XYB once: 42 x (32 nch + 10) conversions for 32 x 32 nch outputs where
+// nch separate tiles pay 42 x 42 x nch. The blurs run the moment pairs that share a tap weight ((a', d'),
+// (a'^2, b'^2)) as packed two-lane f32 FMAs, each lane exactly fmaf, so the results are those of scalar FMAs in the
+// same order.
+// Offsets: every chunk takes the XYB and XYB difference at its own centre, as a 32 x 32 tile does; the carried rows
+// are re-offset by the change (one f32 subtraction each). With nch = 1 the band is exactly the single tile.
+// Band `local` of scale `sd` (sd.tiles_x bands across; sd.nch chunks each) of a pyramid pair; the band's 18 sums go to
+// out[i * stride], i < 18.
+__device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, const float* __restrict__ ref,
                                            const float* __restrict__ dist, double* __restrict__ out,
                                            const size_t stride) {
   extern __shared__ float smem[];
   float2* xs = reinterpret_cast<float2*>(smem);  // [3][kIH][kIW] pairs (a', d') per channel
   float* hb = smem + 6 * kIH * kIW;              // pair planes (m0, m1), (m2, m3) then m4, [kIH][kTileW] each
   __shared__ float s_red[kTileThreads / 32][kScoreSums];
+  __shared__ float s_oa[3], s_od[3], s_noa[3], s_nod[3];
 
   const int tx = local % sd.tiles_x, ty = local / sd.tiles_x;
-  const int x0 = tx * kTileW, y0 = ty * kTileH;
+  const int nch = sd.nch;
+  const int x0 = tx * kTileW, ybeg = ty * kTileH * nch;
   const int w = sd.w, h = sd.h;
   const size_t np = (size_t)w * h;
   const float* ra = ref + sd.off;
   const float* rb = dist + sd.off;
   const float cb_bias = cbrt_fast((float)kBias);
   const int tid = threadIdx.x;
-
-  // XYB of the tile and its halo; the six plane values of the next pixel are loaded before the current one is
-  // converted, so the global loads overlap the arithmetic.
   constexpr int kCols = kTileW + 2 * kRadius;  // 42 real columns of the kIW-pitched rows
-  auto load6 = [&](int e, float* v) -> bool {
-    int r = e / kCols, c = e - r * kCols;
+  constexpr int kCarry = 2 * kRadius;          // rows a chunk hands to the next
+
+  // The six plane values of halo pixel e of the chunk at y0 (rows from r0 on), with the mirror rule for rows.
+  auto load6 = [&](int e, int y0, int r0, float* v) -> bool {
+    int r = r0 + e / kCols, c = e - (r - r0) * kCols;
     int gy = mirror_row(y0 - kRadius + r, h);
     int gx = x0 - kRadius + c;
-    if (e < kIH * kCols && gy >= 0 && gx >= 0 && gx < w) {
+    if (r < kIH && gy >= 0 && gx >= 0 && gx < w) {
       size_t i = (size_t)gy * w + gx;
       v[0] = __ldg(ra + i);
       v[1] = __ldg(ra + np + i);
@@ -174,45 +183,20 @@ __device__ __forceinline__ void ssim2_tile(const ScaleDesc sd, const int local, 
     }
     return false;
   };
-  // The first pixel's loads go out before the tile offsets are settled (they do not depend on them).
-  float cur[6], nxt[6];
-  bool cur_ok = load6(tid, cur);
-
-  // Per-tile offsets: the reference's XYB and the XYB difference at the tile centre. Stored values are
-  // a' = a - oa and d' = (a - b) - od inside the image and 0 outside (the zero border). Every moment the maps need
-  // is recovered exactly from the blurred primed values and the in-image tap sum K of the column (K = 1 away from
-  // the left/right edges, where the offsets cancel outright).
-  __shared__ float s_oa[3], s_od[3];
-  if (tid == 0) {
+  // Per-chunk offsets: the reference's XYB and the XYB difference at the centre of the chunk at y0. Stored values
+  // are a' = a - oa and d' = (a - b) - od inside the image and 0 outside (the zero border). Every moment the maps
+  // need is recovered exactly from the blurred primed values and the in-image tap sum K of the column (K = 1 away
+  // from the left/right edges, where the offsets cancel outright).
+  auto centre = [&](int y0, float* oa_out, float* od_out) {
     int cx = min(x0 + kTileW / 2, w - 1), cy = min(y0 + kTileH / 2, h - 1);
     size_t i = (size_t)cy * w + cx;
     const float z[3] = {0.f, 0.f, 0.f};
     Pix c = pix(ra[i], ra[np + i], ra[2 * np + i], rb[i], rb[np + i], rb[2 * np + i], z, z, cb_bias);
     for (int k = 0; k < 3; k++) {
-      s_oa[k] = c.a[k];
-      s_od[k] = c.d[k];
+      oa_out[k] = c.a[k];
+      od_out[k] = c.d[k];
     }
-  }
-  __syncthreads();
-  float oa[3] = {s_oa[0], s_oa[1], s_oa[2]}, od[3] = {s_od[0], s_od[1], s_od[2]};
-
-  // two halo pixels per trip: the measured best unroll (1.9% faster than none, and 7 is slower)
-#pragma unroll 2
-  for (int e = tid; e < kIH * kCols; e += kTileThreads) {
-    bool nxt_ok = load6(e + kTileThreads, nxt);
-    float v[6] = {0, 0, 0, 0, 0, 0};
-    if (cur_ok) {
-      Pix p = pix(cur[0], cur[1], cur[2], cur[3], cur[4], cur[5], oa, od, cb_bias);
-      v[0] = p.a[0]; v[1] = p.a[1]; v[2] = p.a[2];
-      v[3] = p.d[0]; v[4] = p.d[1]; v[5] = p.d[2];
-    }
-    const int r = e / kCols, idx = r * kIW + (e - r * kCols);
-#pragma unroll
-    for (int k = 0; k < 3; k++) xs[k * kIH * kIW + idx] = make_float2(v[k], v[3 + k]);
-#pragma unroll
-    for (int k = 0; k < 6; k++) cur[k] = nxt[k];
-    cur_ok = nxt_ok;
-  }
+  };
 
   float sums[kScoreSums];
 #pragma unroll
@@ -232,135 +216,216 @@ __device__ __forceinline__ void ssim2_tile(const ScaleDesc sd, const int local, 
     }
   }
   const float omk = 1.0f - K;
+
 #pragma unroll 1
-  for (int ch = 0; ch < 3; ch++) {
-    __syncthreads();  // xs complete (ch 0) / previous channel's vertical pass done with hb
-    const float2* X = xs + ch * kIH * kIW;
-    // Horizontal pass: kHx adjacent outputs per item; moments a', d', a'^2, b'^2 (b' = a' - d'), d'^2. The pairs
-    // (a', d') and (a'^2, b'^2) share every tap weight and run as packed two-lane FMAs (per lane exactly fmaf).
-    // Items: each half-warp takes 4 rows x 4 items, so its 64-bit loads (row pitch 45 pairs = 26 banks mod 32)
-    // fall in distinct banks.
-    for (int item = tid; item < kIHp * (kTileW / kHx); item += kTileThreads) {
-      const int hw = item >> 4, j = item & 15;
-      const int r = (hw >> 1) * 4 + (j >> 2), p = (j & 3) + 4 * (hw & 1);
-      if (r >= kIH) continue;
-      const float2* xr = X + r * kIW + kHx * p;
-      float2 vad[kHx + 2 * kRadius], vsq[kHx + 2 * kRadius];
-      float vdd[kHx + 2 * kRadius];
+  for (int chunk = 0; chunk < nch; chunk++) {
+    const int y0 = ybeg + chunk * kTileH;
+    if (y0 >= h) break;
+    // Rows of the halo buffer converted in this chunk: all 42 in the first, the 32 below the carried ones after.
+    const int r0 = chunk == 0 ? 0 : kCarry;
+    float cur[6], nxt[6];
+    bool cur_ok;
+    if (chunk == 0) {
+      // The first pixel's loads go out before the offsets are settled (they do not depend on them).
+      cur_ok = load6(tid, y0, r0, cur);
+      if (tid == 0) centre(y0, s_oa, s_od);
+      __syncthreads();
+    } else {
+      __syncthreads();  // the previous chunk's passes are done with xs and hb; s_noa/s_nod are visible
+      cur_ok = load6(tid, y0, r0, cur);
+      // Carried rows: rows 32..41 of the previous chunk become rows 0..9, re-offset from the previous chunk's
+      // offsets to this one's (s_noa/s_nod, computed during the previous chunk).
+      float da[3], dd[3];
 #pragma unroll
-      for (int t = 0; t < kHx + 2 * kRadius; t++) {
-        const float2 ad = xr[t];
-        const float2 ab = make_float2(ad.x, ad.x - ad.y);
-        vad[t] = ad;
-        vsq[t] = __fmul2_rn(ab, ab);
-        vdd[t] = ad.y * ad.y;
+      for (int k = 0; k < 3; k++) {
+        da[k] = s_noa[k] - s_oa[k];
+        dd[k] = s_nod[k] - s_od[k];
       }
-      float2 m01[kHx], m23[kHx];
-      float m4[kHx];
+      constexpr int kCarried = kCarry * kCols * 3, kPer = (kCarried + kTileThreads - 1) / kTileThreads;
+      float2 keep[kPer];
 #pragma unroll
-      for (int o = 0; o < kHx; o++) {
-        float2 s01 = make_float2(0.f, 0.f), s23 = make_float2(0.f, 0.f);
-        float sdd = 0.f;
-#pragma unroll
-        for (int t = 0; t < 2 * kRadius + 1; t++) {
-          float k = c_gauss[t];
-          float2 kk = make_float2(k, k);
-          s01 = __ffma2_rn(kk, vad[o + t], s01);
-          s23 = __ffma2_rn(kk, vsq[o + t], s23);
-          sdd = fmaf(k, vdd[o + t], sdd);
+      for (int j = 0; j < kPer; j++) {
+        const int e = tid + j * kTileThreads;
+        if (e < kCarried) {
+          const int k = e / (kCarry * kCols), rem = e - k * (kCarry * kCols);
+          const int r = rem / kCols, c = rem - r * kCols;
+          float2 v = xs[k * kIH * kIW + (r + kTileH) * kIW + c];
+          // inside the image the stored values move with the offsets; outside they stay 0 (the zero border)
+          const int gy = mirror_row(y0 - kRadius + r, h), gxx = x0 - kRadius + c;
+          if (gy >= 0 && gxx >= 0 && gxx < w) v = make_float2(v.x - da[k], v.y - dd[k]);
+          keep[j] = v;
         }
-        m01[o] = s01;
-        m23[o] = s23;
-        m4[o] = sdd;
       }
-      // hb: two planes of (moment 0, moment 1) and (moment 2, moment 3) pairs, then moment 4
-      float* h01 = hb + (r * kTileW + kHx * p) * 2;
-      float* h23 = hb + (kIH * kTileW + r * kTileW + kHx * p) * 2;
-      float* h4 = hb + 4 * kIH * kTileW + r * kTileW + kHx * p;
-      reinterpret_cast<float4*>(h01)[0] = make_float4(m01[0].x, m01[0].y, m01[1].x, m01[1].y);
-      reinterpret_cast<float4*>(h01)[1] = make_float4(m01[2].x, m01[2].y, m01[3].x, m01[3].y);
-      reinterpret_cast<float4*>(h23)[0] = make_float4(m23[0].x, m23[0].y, m23[1].x, m23[1].y);
-      reinterpret_cast<float4*>(h23)[1] = make_float4(m23[2].x, m23[2].y, m23[3].x, m23[3].y);
-      *reinterpret_cast<float4*>(h4) = make_float4(m4[0], m4[1], m4[2], m4[3]);
-    }
-    __syncthreads();
-    // Vertical pass + error maps: 4 output rows of one column per thread, the same pairs packed.
-    float mu[5][4];
-    {
-      const float2* h01 = reinterpret_cast<const float2*>(hb);
-      const float2* h23 = reinterpret_cast<const float2*>(hb) + kIH * kTileW;
-      const float* h4 = hb + 4 * kIH * kTileW;
-      float2 v01[4 + 2 * kRadius], v23[4 + 2 * kRadius];
-      float v4[4 + 2 * kRadius];
+      __syncthreads();  // every carried value is read before rows 32..41 are overwritten
 #pragma unroll
-      for (int t = 0; t < 4 + 2 * kRadius; t++) {
-        const int i = (rg * 4 + t) * kTileW + col;
-        v01[t] = h01[i];
-        v23[t] = h23[i];
-        v4[t] = h4[i];
+      for (int j = 0; j < kPer; j++) {
+        const int e = tid + j * kTileThreads;
+        if (e < kCarried) {
+          const int k = e / (kCarry * kCols), rem = e - k * (kCarry * kCols);
+          const int r = rem / kCols, c = rem - r * kCols;
+          xs[k * kIH * kIW + r * kIW + c] = keep[j];
+        }
       }
+      if (tid < 3) {
+        s_oa[tid] = s_noa[tid];
+        s_od[tid] = s_nod[tid];
+      }
+      __syncthreads();
+    }
+    float oa[3] = {s_oa[0], s_oa[1], s_oa[2]}, od[3] = {s_od[0], s_od[1], s_od[2]};
+
+    // XYB of the chunk's new rows; the six plane values of the next pixel are loaded before the current one is
+    // converted, so the global loads overlap the arithmetic. Two halo pixels per trip: the measured best unroll.
+    const int nconv = (kIH - r0) * kCols;
+#pragma unroll 2
+    for (int e = tid; e < nconv; e += kTileThreads) {
+      bool nxt_ok = load6(e + kTileThreads, y0, r0, nxt);
+      float v[6] = {0, 0, 0, 0, 0, 0};
+      if (cur_ok) {
+        Pix p = pix(cur[0], cur[1], cur[2], cur[3], cur[4], cur[5], oa, od, cb_bias);
+        v[0] = p.a[0]; v[1] = p.a[1]; v[2] = p.a[2];
+        v[3] = p.d[0]; v[4] = p.d[1]; v[5] = p.d[2];
+      }
+      const int r = r0 + e / kCols, idx = r * kIW + (e - (r - r0) * kCols);
+#pragma unroll
+      for (int k = 0; k < 3; k++) xs[k * kIH * kIW + idx] = make_float2(v[k], v[3 + k]);
+#pragma unroll
+      for (int k = 0; k < 6; k++) cur[k] = nxt[k];
+      cur_ok = nxt_ok;
+    }
+    // The next chunk's offsets, while the other threads finish their conversions.
+    if (tid == 0 && chunk + 1 < nch && y0 + kTileH < h) centre(y0 + kTileH, s_noa, s_nod);
+
+#pragma unroll 1
+    for (int ch = 0; ch < 3; ch++) {
+      __syncthreads();  // xs complete (ch 0) / previous channel's vertical pass done with hb
+      const float2* X = xs + ch * kIH * kIW;
+      // Horizontal pass: kHx adjacent outputs per item; moments a', d', a'^2, b'^2 (b' = a' - d'), d'^2. The pairs
+      // (a', d') and (a'^2, b'^2) share every tap weight and run as packed two-lane FMAs (per lane exactly fmaf).
+      // Items: each half-warp takes 4 rows x 4 items, so its 64-bit loads (row pitch 45 pairs = 26 banks mod 32)
+      // fall in distinct banks.
+      for (int item = tid; item < kIHp * (kTileW / kHx); item += kTileThreads) {
+        const int hw = item >> 4, j = item & 15;
+        const int r = (hw >> 1) * 4 + (j >> 2), p = (j & 3) + 4 * (hw & 1);
+        if (r >= kIH) continue;
+        const float2* xr = X + r * kIW + kHx * p;
+        float2 vad[kHx + 2 * kRadius], vsq[kHx + 2 * kRadius];
+        float vdd[kHx + 2 * kRadius];
+#pragma unroll
+        for (int t = 0; t < kHx + 2 * kRadius; t++) {
+          const float2 ad = xr[t];
+          const float2 ab = make_float2(ad.x, ad.x - ad.y);
+          vad[t] = ad;
+          vsq[t] = __fmul2_rn(ab, ab);
+          vdd[t] = ad.y * ad.y;
+        }
+        float2 m01[kHx], m23[kHx];
+        float m4[kHx];
+#pragma unroll
+        for (int o = 0; o < kHx; o++) {
+          float2 s01 = make_float2(0.f, 0.f), s23 = make_float2(0.f, 0.f);
+          float sdd = 0.f;
+#pragma unroll
+          for (int t = 0; t < 2 * kRadius + 1; t++) {
+            float k = c_gauss[t];
+            float2 kk = make_float2(k, k);
+            s01 = __ffma2_rn(kk, vad[o + t], s01);
+            s23 = __ffma2_rn(kk, vsq[o + t], s23);
+            sdd = fmaf(k, vdd[o + t], sdd);
+          }
+          m01[o] = s01;
+          m23[o] = s23;
+          m4[o] = sdd;
+        }
+        // hb: two planes of (moment 0, moment 1) and (moment 2, moment 3) pairs, then moment 4
+        float* h01 = hb + (r * kTileW + kHx * p) * 2;
+        float* h23 = hb + (kIH * kTileW + r * kTileW + kHx * p) * 2;
+        float* h4 = hb + 4 * kIH * kTileW + r * kTileW + kHx * p;
+        reinterpret_cast<float4*>(h01)[0] = make_float4(m01[0].x, m01[0].y, m01[1].x, m01[1].y);
+        reinterpret_cast<float4*>(h01)[1] = make_float4(m01[2].x, m01[2].y, m01[3].x, m01[3].y);
+        reinterpret_cast<float4*>(h23)[0] = make_float4(m23[0].x, m23[0].y, m23[1].x, m23[1].y);
+        reinterpret_cast<float4*>(h23)[1] = make_float4(m23[2].x, m23[2].y, m23[3].x, m23[3].y);
+        *reinterpret_cast<float4*>(h4) = make_float4(m4[0], m4[1], m4[2], m4[3]);
+      }
+      __syncthreads();
+      // Vertical pass + error maps: 4 output rows of one column per thread, the same pairs packed.
+      float mu[5][4];
+      {
+        const float2* h01 = reinterpret_cast<const float2*>(hb);
+        const float2* h23 = reinterpret_cast<const float2*>(hb) + kIH * kTileW;
+        const float* h4 = hb + 4 * kIH * kTileW;
+        float2 v01[4 + 2 * kRadius], v23[4 + 2 * kRadius];
+        float v4[4 + 2 * kRadius];
+#pragma unroll
+        for (int t = 0; t < 4 + 2 * kRadius; t++) {
+          const int i = (rg * 4 + t) * kTileW + col;
+          v01[t] = h01[i];
+          v23[t] = h23[i];
+          v4[t] = h4[i];
+        }
+#pragma unroll
+        for (int o = 0; o < 4; o++) {
+          float2 a01 = make_float2(0.f, 0.f), a23 = make_float2(0.f, 0.f);
+          float a4 = 0.f;
+#pragma unroll
+          for (int t = 0; t < 2 * kRadius + 1; t++) {
+            float k = c_gauss[t];
+            float2 kk = make_float2(k, k);
+            a01 = __ffma2_rn(kk, v01[o + t], a01);
+            a23 = __ffma2_rn(kk, v23[o + t], a23);
+            a4 = fmaf(k, v4[o + t], a4);
+          }
+          mu[0][o] = a01.x;
+          mu[1][o] = a01.y;
+          mu[2][o] = a23.x;
+          mu[3][o] = a23.y;
+          mu[4][o] = a4;
+        }
+      }
+      const float ca = s_oa[ch], cd = s_od[ch], cbv = ca - cd;
 #pragma unroll
       for (int o = 0; o < 4; o++) {
-        float2 a01 = make_float2(0.f, 0.f), a23 = make_float2(0.f, 0.f);
-        float a4 = 0.f;
-#pragma unroll
-        for (int t = 0; t < 2 * kRadius + 1; t++) {
-          float k = c_gauss[t];
-          float2 kk = make_float2(k, k);
-          a01 = __ffma2_rn(kk, v01[o + t], a01);
-          a23 = __ffma2_rn(kk, v23[o + t], a23);
-          a4 = fmaf(k, v4[o + t], a4);
+        int ry = rg * 4 + o;
+        int gy = y0 + ry;
+        if (gx < w && gy < h) {
+          // Blurred primed moments -> sigma_1^2, sigma_2^2, sigma_(a-b)^2, mu1 - mu2 (exactly, given K).
+          float m1 = mu[0][o], dmp = mu[1][o], m2 = m1 - dmp;
+          float v1 = fmaf(-m1, m1, mu[2][o]);
+          float v2 = fmaf(-m2, m2, mu[3][o]);
+          float vd = fmaf(-dmp, dmp, mu[4][o]);
+          float dmu;
+          if (edge) {
+            v1 = fmaf(omk * ca, fmaf(ca, K, 2.0f * m1), v1);
+            v2 = fmaf(omk * cbv, fmaf(cbv, K, 2.0f * m2), v2);
+            vd = fmaf(omk * cd, fmaf(cd, K, 2.0f * dmp), vd);
+            dmu = fmaf(cd, K, dmp);
+          } else {
+            dmu = dmp + cd;
+          }
+          // SSIM error (core/src/ssimulacra2.rs:427-430) as (sigma_(a-b)^2 + dmu^2 num_s) / denom_s, which equals
+          // 1 - (1 - dmu^2) num_s / denom_s since num_s = denom_s - sigma_(a-b)^2.
+          float den = (v1 + v2) + 0.0009f;
+          float num_s = den - vd;
+          float d = fmaxf(__fdividef(fmaf(dmu * dmu, num_s, vd), den), 0.0f);
+          // Edge maps (:431-433): d1 = (|r2| - |r1|) / (1 + |r1|) with r1 = a - mu1, r2 = b - mu2 = r1 - rd.
+          const float2 c0 = X[(ry + kRadius) * kIW + col + kRadius];
+          float a0 = c0.x, d0 = c0.y;
+          float r1 = a0 - m1, rd = d0 - dmp;
+          if (edge) {
+            r1 = fmaf(ca, omk, r1);
+            rd = fmaf(cd, omk, rd);
+          }
+          float t = fabsf(r1 - rd) + fabsf(r1);
+          float d1 = t > 0.0f ? __fdividef(-rd * (2.0f * r1 - rd), t * (1.0f + fabsf(r1))) : 0.0f;
+          float art = fmaxf(d1, 0.0f), det = fmaxf(-d1, 0.0f);
+          float d2 = d * d, a2 = art * art, e2 = det * det;
+          sums[ch * 6 + 0] += d;
+          sums[ch * 6 + 1] += d2 * d2;
+          sums[ch * 6 + 2] += art;
+          sums[ch * 6 + 3] += a2 * a2;
+          sums[ch * 6 + 4] += det;
+          sums[ch * 6 + 5] += e2 * e2;
         }
-        mu[0][o] = a01.x;
-        mu[1][o] = a01.y;
-        mu[2][o] = a23.x;
-        mu[3][o] = a23.y;
-        mu[4][o] = a4;
-      }
-    }
-    const float ca = oa[ch], cd = od[ch], cbv = ca - cd;
-#pragma unroll
-    for (int o = 0; o < 4; o++) {
-      int ry = rg * 4 + o;
-      int gy = y0 + ry;
-      if (gx < w && gy < h) {
-        // Blurred primed moments -> sigma_1^2, sigma_2^2, sigma_(a-b)^2, mu1 - mu2 (exactly, given K).
-        float m1 = mu[0][o], dmp = mu[1][o], m2 = m1 - dmp;
-        float v1 = fmaf(-m1, m1, mu[2][o]);
-        float v2 = fmaf(-m2, m2, mu[3][o]);
-        float vd = fmaf(-dmp, dmp, mu[4][o]);
-        float dmu;
-        if (edge) {
-          v1 = fmaf(omk * ca, fmaf(ca, K, 2.0f * m1), v1);
-          v2 = fmaf(omk * cbv, fmaf(cbv, K, 2.0f * m2), v2);
-          vd = fmaf(omk * cd, fmaf(cd, K, 2.0f * dmp), vd);
-          dmu = fmaf(cd, K, dmp);
-        } else {
-          dmu = dmp + cd;
-        }
-        // SSIM error (core/src/ssimulacra2.rs:427-430) as (sigma_(a-b)^2 + dmu^2 num_s) / denom_s, which equals
-        // 1 - (1 - dmu^2) num_s / denom_s since num_s = denom_s - sigma_(a-b)^2.
-        float den = (v1 + v2) + 0.0009f;
-        float num_s = den - vd;
-        float d = fmaxf(__fdividef(fmaf(dmu * dmu, num_s, vd), den), 0.0f);
-        // Edge maps (:431-433): d1 = (|r2| - |r1|) / (1 + |r1|) with r1 = a - mu1, r2 = b - mu2 = r1 - rd.
-        const float2 c0 = X[(ry + kRadius) * kIW + col + kRadius];
-        float a0 = c0.x, d0 = c0.y;
-        float r1 = a0 - m1, rd = d0 - dmp;
-        if (edge) {
-          r1 = fmaf(ca, omk, r1);
-          rd = fmaf(cd, omk, rd);
-        }
-        float t = fabsf(r1 - rd) + fabsf(r1);
-        float d1 = t > 0.0f ? __fdividef(-rd * (2.0f * r1 - rd), t * (1.0f + fabsf(r1))) : 0.0f;
-        float art = fmaxf(d1, 0.0f), det = fmaxf(-d1, 0.0f);
-        float d2 = d * d, a2 = art * art, e2 = det * det;
-        sums[ch * 6 + 0] += d;
-        sums[ch * 6 + 1] += d2 * d2;
-        sums[ch * 6 + 2] += art;
-        sums[ch * 6 + 3] += a2 * a2;
-        sums[ch * 6 + 4] += det;
-        sums[ch * 6 + 5] += e2 * e2;
       }
     }
   }
@@ -410,7 +475,7 @@ __global__ void __launch_bounds__(kTileThreads, 3)
   int s = 0;
   while (s + 1 < pd.nscales && blk >= pd.s[s + 1].tile0) s++;
   const ScaleDesc sd = pd.s[s];
-  ssim2_tile(sd, blk - sd.tile0, ref, dist, partials + blk, (size_t)pd.total_tiles);
+  ssim2_band(sd, blk - sd.tile0, ref, dist, partials + blk, (size_t)pd.total_tiles);
 }
 
 // Deterministic reduction of the per-tile sums: CTA (scale, sum index); the last CTA to finish computes the score
@@ -716,9 +781,10 @@ struct ScoreItem {
 struct TileSeg {
   const float* ref;   // channel 0 of this scale's planes
   const float* dist;
-  double* out;        // partial sums of the segment's first tile; tile k, sum i at out[i * stride + k]
+  double* out;        // partial sums of the segment's first band; band k, sum i at out[i * stride + k]
   int w, h, tiles_x;
-  int stride;         // tiles of the pair (the sum-major stride of its partials)
+  int nch;            // chunks per band
+  int stride;         // bands of the pair (the sum-major stride of its partials)
 };
 
 // Last index whose first entry is <= x in an ascending array of first indices (n >= 1, first[0] = 0).
@@ -778,9 +844,10 @@ __global__ void __launch_bounds__(kTileThreads, 3)
   sd.tiles_x = sg.tiles_x;
   sd.tiles_y = 0;
   sd.tile0 = 0;
+  sd.nch = sg.nch;
   sd.off = 0;
   const int local = (int)(t - __ldg(seg0 + g));
-  ssim2_tile(sd, local, sg.ref, sg.dist, sg.out + local, (size_t)sg.stride);
+  ssim2_band(sd, local, sg.ref, sg.dist, sg.out + local, (size_t)sg.stride);
 }
 
 // CTA (scale, sum, pair); scale_sums [n][kMaxScales][18], counters and scores [n].
@@ -832,6 +899,7 @@ PyramidDesc make_pyramid(int w, int h) {
     sd.tiles_x = (w + kTileW - 1) / kTileW;
     sd.tiles_y = (h + kTileH - 1) / kTileH;
     sd.tile0 = tiles;
+    sd.nch = 1;
     sd.off = off;
     tiles += sd.tiles_x * sd.tiles_y;
     off += 3LL * w * h;
@@ -907,6 +975,111 @@ int scorer_init(rcg_ctx* ctx) {
   return RCG_OK;
 }
 
+// ------------------------------------------------------------------------------------------------ band autotuner
+
+// Bands pay off where a scale has enough tiles to keep every SM busy with long CTAs; smaller scales (and whole
+// images below kBandMinTiles0 scale-0 tiles, which are never tuned) keep 32x32 tiles.
+constexpr int kBandMinTiles = 3 * 152;
+constexpr int kBandMinTiles0 = 1024;
+constexpr int kBandCandidates[] = {1, 2, 4, 8};
+
+PyramidDesc banded(const PyramidDesc& pd, int nch0, int min_tiles) {
+  PyramidDesc b = pd;
+  int total = 0;
+  for (int s = 0; s < pd.nscales; s++) {
+    ScaleDesc& sd = b.s[s];
+    const int tiles = pd.s[s].tiles_x * pd.s[s].tiles_y;
+    const int n = (nch0 > 1 && tiles >= min_tiles) ? std::min(nch0, pd.s[s].tiles_y) : 1;
+    sd.nch = n;
+    sd.tiles_y = (pd.s[s].tiles_y + n - 1) / n;
+    sd.tile0 = total;
+    total += sd.tiles_x * sd.tiles_y;
+  }
+  b.total_tiles = total;
+  return b;
+}
+
+// Deterministic stand-in content for the tuning runs (linear values in [0, 1), the second image a perturbed copy);
+// the kernel's time does not depend on the values.
+__global__ void k_tune_fill(float* __restrict__ p, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    uint32_t x = (uint32_t)(i % (n / 2)) * 2654435761u;
+    x ^= x >> 15;
+    float v = (float)(x & 0xFFFFFF) * (1.0f / 16777216.0f);
+    p[i] = i < n / 2 ? v : fminf(1.0f, v * 0.98f + 0.01f);
+  }
+}
+
+static std::mutex g_band_mu;
+static std::map<std::pair<int, int>, int> g_band_choice;  // (device, size class) -> chunks per band
+
+// Size class: scale-0 tiles in half-octave steps.
+static int band_class(const PyramidDesc& pd) {
+  const double t = (double)pd.s[0].tiles_x * pd.s[0].tiles_y;
+  return (int)std::floor(2.0 * std::log2(std::max(1.0, t)));
+}
+
+// Time k_ssim2_tiles for each candidate on a stand-in pair of this geometry (own allocation, freed after); the
+// fastest by the best of three launches wins.
+static int tune_bands(rcg_ctx* ctx, const PyramidDesc& pd) {
+  float* pyr = nullptr;
+  double* part = nullptr;
+  const long long n = 2 * pd.floats;
+  if (cudaMalloc(&pyr, (size_t)n * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&part, (size_t)pd.total_tiles * kScoreSums * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    if (pyr) cudaFree(pyr);
+    return 1;  // no room to tune: tiles
+  }
+  k_tune_fill<<<4 * 152, 256, 0, ctx->stream>>>(pyr, n);
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  int best = 1;
+  float best_ms = 1e30f;
+  for (int nch0 : kBandCandidates) {
+    const PyramidDesc pb = banded(pd, nch0, kBandMinTiles);
+    float t = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+      cudaEventRecord(a, ctx->stream);
+      k_ssim2_tiles<<<pb.total_tiles, kTileThreads, kTileSmem, ctx->stream>>>(pb, pyr, pyr + pd.floats, part,
+                                                                              nullptr);
+      cudaEventRecord(b, ctx->stream);
+      cudaEventSynchronize(b);
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, a, b);
+      if (rep > 0) t = std::min(t, ms);  // the first launch warms up
+    }
+    if (t < best_ms * 0.99f) {  // a longer band must win by more than noise
+      best_ms = t;
+      best = nch0;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(pyr);
+  cudaFree(part);
+  cudaGetLastError();
+  return best;
+}
+
+PyramidDesc plan_bands(rcg_ctx* ctx, const PyramidDesc& pd) {
+  // A fixed choice applies at every scale; a tuned one only where a scale has tiles enough to fill the GPU.
+  return banded(pd, band_chunks(ctx, pd), ctx->band_chunks > 0 ? 0 : kBandMinTiles);
+}
+
+int band_chunks(rcg_ctx* ctx, const PyramidDesc& pd) {
+  if (ctx->band_chunks > 0) return ctx->band_chunks;
+  if (pd.nscales == 0 || pd.s[0].tiles_x * pd.s[0].tiles_y < kBandMinTiles0) return 1;
+  const auto key = std::make_pair(ctx->device, band_class(pd));
+  std::lock_guard<std::mutex> lk(g_band_mu);
+  auto it = g_band_choice.find(key);
+  if (it != g_band_choice.end()) return it->second;
+  const int best = tune_bands(ctx, pd);
+  g_band_choice[key] = best;
+  return best;
+}
+
 int score_workspace(rcg_ctx* ctx, const PyramidDesc& pd) {
   double* partials = (double*)workspace(ctx, "score_partials", (size_t)pd.total_tiles * kScoreSums * sizeof(double));
   double* scale_sums = (double*)workspace(ctx, "score_scale_sums", kMaxScales * kScoreSums * sizeof(double));
@@ -920,10 +1093,11 @@ int score_pyramids(rcg_ctx* ctx, const PyramidDesc& pd, const float* d_ref, cons
   double* partials = (double*)ctx->bufs["score_partials"].ptr;
   double* scale_sums = (double*)ctx->bufs["score_scale_sums"].ptr;
   unsigned* counter = (unsigned*)ctx->bufs["score_counter"].ptr;
-  RCG_LAUNCH(ctx, "ssim2_tiles", k_ssim2_tiles, pd.total_tiles, kTileThreads, kTileSmem, pd, d_ref, d_dist, partials,
+  const PyramidDesc pb = plan_bands(ctx, pd);
+  RCG_LAUNCH(ctx, "ssim2_tiles", k_ssim2_tiles, pb.total_tiles, kTileThreads, kTileSmem, pb, d_ref, d_dist, partials,
              step);
-  dim3 rg(pd.nscales, kScoreSums);
-  RCG_LAUNCH(ctx, "ssim2_reduce", k_ssim2_reduce, rg, 256, 0, pd, partials, scale_sums, counter, d_score, search,
+  dim3 rg(pb.nscales, kScoreSums);
+  RCG_LAUNCH(ctx, "ssim2_reduce", k_ssim2_reduce, rg, 256, 0, pb, partials, scale_sums, counter, d_score, search,
              step);
   return RCG_OK;
 }
@@ -944,6 +1118,7 @@ int score_batch(rcg_ctx* ctx, int n, const uint8_t* const* d_refs, const uint8_t
     std::memset(&it, 0, sizeof it);
     const int w = (int)widths[i], h = (int)heights[i];
     it.pd = make_pyramid(w, h);
+    it.pd = plan_bands(ctx, it.pd);
     it.img[0] = d_refs[i];
     it.img[1] = d_dists[i];
     it.channels = channels[i];
@@ -1014,6 +1189,7 @@ int score_batch(rcg_ctx* ctx, int n, const uint8_t* const* d_refs, const uint8_t
       segs[g].w = sd.w;
       segs[g].h = sd.h;
       segs[g].tiles_x = sd.tiles_x;
+      segs[g].nch = sd.nch;
       segs[g].stride = it.pd.total_tiles;
       seg0[g] = it.tile0 + sd.tile0;
     }

@@ -260,6 +260,8 @@ def _load():
         "rcg_ssimulacra2_exact": (i32, [P, P, P, u32, u32, i32, i32, ctypes.POINTER(ctypes.c_double)]),
         "rcg_ctx_set_tie_band": (i32, [P, ctypes.c_double]),
         "rcg_ctx_tie_rescores": (ctypes.c_uint64, [P]),
+        "rcg_ctx_set_band_chunks": (i32, [P, i32]),
+        "rcg_ctx_band_chunks": (i32, [P, u32, u32]),
         "rcg_ssimulacra2_device_noalloc": (i32, [P, P, u32, u32, i32, P, P]),
         "rcg_build_coefs": (i32, [P, P, u32, u32, i32, ctypes.POINTER(_Opts), P, sz, P]),
         "rcg_reconstruct": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, P, P, sz]),
@@ -333,7 +335,8 @@ EXPORTED = (
     "rcg_search_requantize_device rcg_ssimulacra2_grad rcg_ssimulacra2_grad_device rcg_perceptual_defaults "
     "rcg_coef_gradient rcg_perceptual_weights rcg_build_coefs_weighted rcg_search_weighted rcg_search_perceptual "
     "rcg_perceptual_strength rcg_ctx_set_graphs rcg_ctx_graph_stats rcg_ssimulacra2_batch rcg_ssimulacra2_batch_device "
-    "rcg_sweep_qualities rcg_ssimulacra2_exact rcg_ctx_set_tie_band rcg_ctx_tie_rescores"
+    "rcg_sweep_qualities rcg_ssimulacra2_exact rcg_ctx_set_tie_band rcg_ctx_tie_rescores "
+    "rcg_ctx_set_band_chunks rcg_ctx_band_chunks"
 ).split()
 
 
@@ -433,6 +436,14 @@ class Context:
     def tie_rescores(self):
         """Candidates this context has decided on the reference-order FP64 score so far."""
         return int(_lib.rcg_ctx_tie_rescores(self._ptr))
+
+    def set_band_chunks(self, chunks):
+        """The fast scorer's band height in 32-row chunks: 0 autotunes per size class (default), 1..64 fixes it."""
+        self._check(_lib.rcg_ctx_set_band_chunks(self._ptr, int(chunks)))
+
+    def band_chunks(self, width, height):
+        """Chunks per band used for a width x height image (autotuning its size class if needed)."""
+        return int(_lib.rcg_ctx_band_chunks(self._ptr, int(width), int(height)))
 
     def kernel_time(self, name):
         n = ctypes.c_uint64()
