@@ -2382,6 +2382,94 @@ static int decode_sequential(BitReader& br, const HuffDec& dc, const HuffDec& ac
   return 0;
 }
 
+// jpeg/src/decode.rs:1509-1517 (decode_dc_first)
+static int decode_dc_first(BitReader& br, const HuffDec& dc, int16_t* blk, int32_t* pred, uint32_t al) {
+  int t;
+  if (huff_decode(dc, br, &t)) return 1;
+  if (t > 16) return 1;
+  *pred = (int32_t)((uint32_t)*pred + (uint32_t)extend_bits(br.bits((uint32_t)t), (uint32_t)t));
+  blk[0] = (int16_t)(int32_t)((uint32_t)*pred << al);
+  return 0;
+}
+
+struct ProgParams {
+  int ss, se;
+  uint32_t ah, al;
+};
+
+// jpeg/src/decode.rs:1519-1547 (decode_ac_first)
+static int decode_ac_first(BitReader& br, const HuffDec& ac, int16_t* blk, uint32_t* eobrun, const ProgParams& p) {
+  if (*eobrun > 0) {
+    (*eobrun)--;
+    return 0;
+  }
+  int k = p.ss;
+  while (k <= p.se) {
+    int rs;
+    if (huff_decode(ac, br, &rs)) return 1;
+    int r = rs >> 4, sz = rs & 15;
+    if (sz == 0) {
+      if (r < 15) {
+        *eobrun = (1u << r) - 1;
+        if (r > 0) *eobrun += br.bits((uint32_t)r);
+        break;
+      }
+      k += 16;
+      continue;
+    }
+    k += r;
+    if (k > 63) return 1;
+    blk[k] = (int16_t)(int32_t)((uint32_t)extend_bits(br.bits((uint32_t)sz), (uint32_t)sz) << p.al);
+    k++;
+  }
+  return 0;
+}
+
+// jpeg/src/decode.rs:1549-1601 (decode_ac_refine)
+static int decode_ac_refine(BitReader& br, const HuffDec& ac, int16_t* blk, uint32_t* eobrun, const ProgParams& p) {
+  const int16_t p1 = (int16_t)(1 << p.al), m1 = (int16_t)(-1 * (1 << p.al));
+  int k = p.ss;
+  if (*eobrun == 0) {
+    while (k <= p.se) {
+      int rs;
+      if (huff_decode(ac, br, &rs)) return 1;
+      int r = rs >> 4, sz = rs & 15;
+      int16_t value = 0;
+      if (sz != 0) {
+        value = br.bits(1) ? p1 : m1;
+      } else if (r != 15) {
+        *eobrun = 1u << r;
+        if (r > 0) *eobrun += br.bits((uint32_t)r);
+        break;
+      }
+      while (k <= p.se) {
+        int16_t& c = blk[k];
+        if (c != 0) {
+          if (br.bits(1) && (c & p1) == 0) c = (int16_t)(c + (c >= 0 ? p1 : m1));
+        } else {
+          r--;
+          if (r < 0) break;
+        }
+        k++;
+      }
+      if (value != 0) {
+        if (k > 63) return 1;
+        blk[k] = value;
+      }
+      k++;
+    }
+  }
+  if (*eobrun > 0) {
+    while (k <= p.se) {
+      int16_t& c = blk[k];
+      if (c != 0 && br.bits(1) && (c & p1) == 0) c = (int16_t)(c + (c >= 0 ? p1 : m1));
+      k++;
+    }
+    (*eobrun)--;
+  }
+  return 0;
+}
+
 struct ParsedComp {
   uint8_t id = 0;
   int h = 1, v = 1, tq = 0, blocks_w = 0, blocks_h = 0, real_bw = 0, real_bh = 0;
@@ -2391,9 +2479,9 @@ struct ParsedComp {
 };
 
 // jpeg::decode::parse(data)?.into_coefs() (jpeg/src/decode.rs:397-445, :540-570, :622-697, :906-1103, :1230-1309)
-// for sequential Huffman frames. Returns 0, 1 (invalid) or 2 (unsupported: other frame kinds, 12-bit, RGB-coded,
-// 16-bit tables, four components).
-static int parse_sequential(const uint8_t* d, size_t len, CoefImage& out) {
+// for sequential and progressive Huffman frames (SOF0, SOF1, SOF2). Returns 0, 1 (invalid) or 2 (unsupported: other
+// frame kinds, 12-bit, RGB-coded, 16-bit tables, four components).
+static int parse_huffman(const uint8_t* d, size_t len, CoefImage& out) {
   if (len < 4 || d[0] != 0xFF || d[1] != 0xD8) return 1;
   size_t pos = 2;
   bool has_qt[4] = {false, false, false, false};
@@ -2405,6 +2493,7 @@ static int parse_sequential(const uint8_t* d, size_t len, CoefImage& out) {
   size_t ri = 0;
   int scans = 0;
   int adobe = -1;
+  bool progressive = false;
   auto be16 = [&](size_t at, size_t* v) -> bool {
     if (at + 2 > len) return false;
     *v = ((size_t)d[at] << 8) | d[at + 1];
@@ -2454,8 +2543,9 @@ static int parse_sequential(const uint8_t* d, size_t len, CoefImage& out) {
         b += 17 + total;
         bl -= 17 + total;
       }
-    } else if (m == 0xC0 || m == 0xC1) {
+    } else if (m == 0xC0 || m == 0xC1 || m == 0xC2) {
       if (!comps.empty()) return 2;  // a second frame: hierarchical
+      progressive = m == 0xC2;
       if (bl < 6) return 1;
       if (b[0] != 8) return b[0] == 12 ? 2 : 2;
       height = (b[1] << 8) | b[2];
@@ -2490,8 +2580,8 @@ static int parse_sequential(const uint8_t* d, size_t len, CoefImage& out) {
         c.real_bh = (chh + 7) / 8;
         c.coefs.assign((size_t)c.blocks_w * c.blocks_h * 64, 0);
       }
-    } else if ((m >= 0xC2 && m <= 0xCF && m != 0xC4 && m != 0xC8 && m != 0xCC) || m == 0xDE || m == 0xDF) {
-      return 2;  // progressive, lossless, hierarchical or arithmetic frames
+    } else if ((m >= 0xC3 && m <= 0xCF && m != 0xC4 && m != 0xC8 && m != 0xCC) || m == 0xDE || m == 0xDF) {
+      return 2;  // lossless, hierarchical or arithmetic frames
     } else if (m == 0xDD) {
       if (bl < 2) return 1;
       ri = ((size_t)b[0] << 8) | b[1];
@@ -2518,17 +2608,29 @@ static int parse_sequential(const uint8_t* d, size_t len, CoefImage& out) {
         dci[i] = (t >> 4) & 3;
         aci[i] = (t & 15) & 3;
       }
+      // scan parameters (:1084-1096)
+      const uint8_t* tp = b + 1 + 2 * ns;
+      ProgParams pp{0, 63, 0, 0};
+      if (progressive) {
+        pp = ProgParams{tp[0], tp[1], (uint32_t)(tp[2] >> 4), (uint32_t)(tp[2] & 15)};
+        if (pp.ss > pp.se || pp.se > 63 || pp.al > 13 || (pp.ss == 0 && pp.se != 0) || (pp.ss > 0 && ns != 1))
+          return 1;
+      }
+      // tables the scan needs (:1240-1248)
+      const bool need_dc = !progressive || (pp.ss == 0 && pp.ah == 0);
+      const bool need_ac = !progressive || pp.ss > 0;
       for (int i = 0; i < ns; i++) {
         ParsedComp& c = comps[idx[i]];
         if (!c.has_snap && has_qt[c.tq]) {
           std::memcpy(c.snap, qt[c.tq], sizeof c.snap);
           c.has_snap = true;
         }
-        if (!has_dc[dci[i]] || !has_ac[aci[i]]) return 1;
+        if ((need_dc && !has_dc[dci[i]]) || (need_ac && !has_ac[aci[i]])) return 1;
       }
-      // decode_scan (:1230-1309), sequential Huffman
+      // decode_scan (:1230-1309), Huffman
       BitReader br{d, len, pos};
       int32_t pred[4] = {0, 0, 0, 0};
+      uint32_t eobrun = 0;
       bool inter = ns > 1;
       size_t mx_n = inter ? (size_t)mcus_x : (size_t)comps[idx[0]].real_bw;
       size_t my_n = inter ? (size_t)mcus_y : (size_t)comps[idx[0]].real_bh;
@@ -2537,6 +2639,7 @@ static int parse_sequential(const uint8_t* d, size_t len, CoefImage& out) {
         if (ri > 0 && mcu > 0 && mcu % ri == 0) {
           br.restart();
           for (int i = 0; i < 4; i++) pred[i] = 0;
+          eobrun = 0;
         }
         size_t mx = mcu % mx_n, my = mcu / mx_n;
         for (int si = 0; si < ns; si++) {
@@ -2546,7 +2649,19 @@ static int parse_sequential(const uint8_t* d, size_t len, CoefImage& out) {
             for (int bx = 0; bx < bh; bx++) {
               size_t col = mx * bh + bx, row = my * bv + by;
               int16_t* blk = &c.coefs[(row * c.blocks_w + col) * 64];
-              if (decode_sequential(br, dct[dci[si]], act[aci[si]], blk, &pred[si])) return 1;
+              int bad;
+              if (!progressive)
+                bad = decode_sequential(br, dct[dci[si]], act[aci[si]], blk, &pred[si]);
+              else if (pp.ss == 0 && pp.ah == 0)
+                bad = decode_dc_first(br, dct[dci[si]], blk, &pred[si], pp.al);
+              else if (pp.ss == 0) {
+                blk[0] = (int16_t)(blk[0] | (int16_t)(br.bits(1) << pp.al));
+                bad = 0;
+              } else if (pp.ah == 0)
+                bad = decode_ac_first(br, act[aci[si]], blk, &eobrun, pp);
+              else
+                bad = decode_ac_refine(br, act[aci[si]], blk, &eobrun, pp);
+              if (bad) return 1;
             }
         }
       }
@@ -2913,12 +3028,27 @@ long orc_write_best(int w, int h, int ncomp, const int* hs, const int* vs, const
   return (long)bytes.size();
 }
 
-// parse(data)?.into_coefs() for sequential Huffman JPEGs. Query with coefs_out == NULL: fills w, h, ncomp, layout,
-// ids. Returns 0, 1 (invalid), 2 (unsupported).
+// progressive::emit (jpeg/src/progressive.rs:397-403) of candidate script `index` of scripts(ncomp)
+// (jpeg/src/progressive.rs:242-295) for a flat CoefImage; returns the byte count (out may be NULL), -1 for a bad
+// index. Test input for the progressive decoders.
+long orc_emit_script(int w, int h, int ncomp, const int* hs, const int* vs, const int* bws, const int* bhs,
+                     const uint8_t* qtables, const int16_t* coefs, int index, uint8_t* out, long cap) {
+  orc::CoefImage ci = orc::coef_from_flat(w, h, ncomp, hs, vs, bws, bhs, qtables, coefs);
+  std::vector<std::vector<orc::Scan>> cands = orc::scripts(ncomp);
+  if (index < 0 || index >= (int)cands.size()) return -1;
+  std::vector<uint8_t> bytes = orc::emit_progressive(ci, cands[(size_t)index]);
+  if (out) std::memcpy(out, bytes.data(), std::min<size_t>(bytes.size(), (size_t)cap));
+  return (long)bytes.size();
+}
+
+int orc_script_count(int ncomp) { return (int)orc::scripts(ncomp).size(); }
+
+// parse(data)?.into_coefs() for sequential and progressive Huffman JPEGs. Query with coefs_out == NULL: fills w, h,
+// ncomp, layout, ids. Returns 0, 1 (invalid), 2 (unsupported).
 int orc_decode_sequential(const uint8_t* data, long len, int* w, int* h, int* ncomp, int* hs, int* vs, int* bws,
                           int* bhs, uint8_t* ids, int16_t* coefs_out, int* tq, uint8_t* qtables4, uint8_t* has_q) {
   orc::CoefImage ci;
-  int rc = orc::parse_sequential(data, (size_t)len, ci);
+  int rc = orc::parse_huffman(data, (size_t)len, ci);
   if (rc) return rc;
   *w = ci.width;
   *h = ci.height;

@@ -61,6 +61,10 @@ def lib():
         L.orc_decode_sequential.argtypes = [P, ctypes.c_long, pi, pi, pi, P, P, P, P, P, P, P, P, P]
         L.orc_write_jpeg_variant.argtypes = [i32, i32, i32, P, P, P, P, P, P, P, P, i32, i32, P, ctypes.c_long]
         L.orc_write_jpeg_variant.restype = ctypes.c_long
+        L.orc_emit_script.argtypes = [i32, i32, i32, P, P, P, P, P, P, i32, P, ctypes.c_long]
+        L.orc_emit_script.restype = ctypes.c_long
+        L.orc_script_count.argtypes = [i32]
+        L.orc_script_count.restype = i32
         L.orc_plan.argtypes = [i32, i32, i32, P, P, P, P, P, pu64, pu64, pi, P, pi, P, P]
         L.orc_round_f32.argtypes = [ctypes.c_float]
         L.orc_round_f32.restype = ctypes.c_int32
@@ -347,8 +351,8 @@ def ms_ssim(a, b, per_scale=False):
 
 
 def decode_sequential(data):
-    """parse(data)?.into_coefs() for sequential Huffman JPEGs: (GeneralCoefs, ids) or raises ValueError with
-    "invalid" / "unsupported"."""
+    """parse(data)?.into_coefs() for sequential and progressive Huffman JPEGs: (GeneralCoefs, ids) or raises
+    ValueError with "invalid" / "unsupported". (The name predates progressive support; decode_huffman is the same.)"""
     data = np.frombuffer(bytes(data), np.uint8)
     w, h, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     hs, vs, bws, bhs = (np.zeros(4, np.int32) for _ in range(4))
@@ -367,6 +371,29 @@ def decode_sequential(data):
     has = np.zeros(4, np.uint8)
     lib().orc_decode_sequential(*args(coefs.ctypes.data, tq.ctypes.data, q4.ctypes.data, has.ctypes.data))
     return GeneralCoefs(w.value, h.value, lay, tq[:k], q4, has, coefs), bytes(ids[:k])
+
+
+decode_huffman = decode_sequential
+
+
+def script_count(ncomp):
+    """Candidate progressive scripts (jpeg/src/progressive.rs:242-295) for ncomp components."""
+    return int(lib().orc_script_count(int(ncomp)))
+
+
+def emit_script(w, h, lay, qt, coefs, index):
+    """The progressive JPEG of a flat CoefImage written with candidate script `index` (progressive::emit)."""
+    n, hs, vs, bws, bhs = _lay_arrays(lay)
+    qt = np.ascontiguousarray(qt, dtype=np.uint8)
+    coefs = np.ascontiguousarray(coefs, dtype=np.int16)
+    size = lib().orc_emit_script(w, h, n, hs.ctypes.data, vs.ctypes.data, bws.ctypes.data, bhs.ctypes.data,
+                                 qt.ctypes.data, coefs.ctypes.data, int(index), None, 0)
+    if size < 0:
+        raise ValueError("bad script index")
+    out = np.zeros(size, np.uint8)
+    lib().orc_emit_script(w, h, n, hs.ctypes.data, vs.ctypes.data, bws.ctypes.data, bhs.ctypes.data,
+                          qt.ctypes.data, coefs.ctypes.data, int(index), out.ctypes.data, size)
+    return out.tobytes()
 
 
 def write_jpeg_variant(g, restart_interval=0, per_component=False):

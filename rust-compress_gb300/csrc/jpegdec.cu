@@ -1,6 +1,6 @@
-// Entropy decoding of sequential Huffman JPEGs on the GPU: jpeg::decode::parse(data)?.into_coefs()
-// (jpeg/src/decode.rs:397-445, :540-570) for SOF0/SOF1 8-bit frames with 1 or 3 components, any sampling, restart
-// intervals and any number of scans.
+// Entropy decoding of Huffman JPEGs on the GPU: jpeg::decode::parse(data)?.into_coefs()
+// (jpeg/src/decode.rs:397-445, :540-570) for SOF0/SOF1 (sequential) and SOF2 (progressive) 8-bit frames with 1 or 3
+// components, any sampling, restart intervals and any number of scans.
 //
 // The host walks the markers (decode.rs:622-697: DQT, DHT, SOF, DRI, SOS, APP14), builds each scan's Huffman tables
 // as they stand when the scan starts, removes the 0xFF00 stuffing and cuts each scan into its restart segments,
@@ -98,7 +98,16 @@ struct Segment {
   int nspan;          // spans
 };
 
+// Scan kinds (jpeg/src/decode.rs:1275-1300): sequential, and the four progressive ones. The first three decode by
+// self-synchronization; a DC refinement scan is one raw bit per block; an AC refinement scan reads one correction
+// bit per coefficient that earlier scans made nonzero, so where its bits fall depends on every block's history and
+// one thread decodes each restart segment in order.
+enum ScanKind { kSeq = 0, kDcFirst = 1, kDcRefine = 2, kAcFirst = 3, kAcRefine = 4 };
+
 struct ScanDesc {
+  int kind;                   // ScanKind
+  int ss, se, ah, al;         // spectral band and successive approximation (sequential: 0, 63, 0, 0)
+  int k0;                     // coefficient index at a block's start (ss for AC scans, else 0)
   int ns;                     // components in the scan
   int bmcu;                   // blocks per MCU (1 for a single-component scan)
   int mcus_x;                 // MCUs per row
@@ -244,11 +253,16 @@ __device__ __forceinline__ int decode_run(const Tables& tb, const ScanDesc& sd, 
   // One symbol per iteration with a single code path for DC and AC symbols (the lanes of a warp decode different
   // streams; branches would serialize them). decode_sequential (decode.rs:1482-1506) in select form: a DC symbol is
   // a size t <= 16 and t extra bits; an AC symbol (run, size) is EOB (size 0, run < 15), ZRL (size 0, run 15: k += 16)
-  // or a coefficient at k + run (error past 63); the block ends when k reaches 64 or at EOB.
+  // or a coefficient at k + run (error past 63); the block ends when k reaches 64 or at EOB. The progressive first
+  // scans are the same loop: decode_dc_first (:1509-1517) is a DC symbol per block, its value shifted left by al;
+  // decode_ac_first (:1519-1547) runs k from ss, ends the block past se, shifts values by al, and an EOB symbol
+  // there is an end-of-band run: 2^run - 1 + (run extra bits) further blocks read no bits at all.
+  const bool dc_only = sd.kind == kDcFirst, ac_first = sd.kind == kAcFirst;
+  const int kend = ac_first ? sd.se : 63, shift = sd.al;
   long long blocks = cnt.blocks;
   while (blocks < max_blocks && r.bit < stop_bit) {
     const int si = sd.mcu_si[u];
-    const bool dc = k == 0;
+    const bool dc = dc_only || (!ac_first && k == 0);
     const int sym = huff_decode(dc ? tb.dc[sd.dc[si]] : tb.ac[sd.ac[si]], r);
     const int run = dc ? 0 : (sym >> 4);
     const int sz = dc ? sym : (sym & 15);
@@ -257,6 +271,8 @@ __device__ __forceinline__ int decode_run(const Tables& tb, const ScanDesc& sd, 
       break;
     }
     const int v = extend_bits(r.bits(sz), sz);
+    // end-of-band run of an AC first scan (sz == 0 here, so no value bits were read)
+    const long long skip = (ac_first && sz == 0 && run < 15) ? (long long)((1u << run) - 1u + r.bits(run)) : 0;
     const uint32_t ud = dc ? (uint32_t)v : 0u;  // selects instead of indexing by si: the sums stay in registers
     d0 += si == 0 ? ud : 0u;
     d1 += si == 1 ? ud : 0u;
@@ -264,16 +280,16 @@ __device__ __forceinline__ int decode_run(const Tables& tb, const ScanDesc& sd, 
     d3 += si == 3 ? ud : 0u;
     if (WRITE) {
       if (dc)
-        blk[0] = (int16_t)(si == 0 ? p0 + d0 : si == 1 ? p1 + d1 : si == 2 ? p2 + d2 : p3 + d3);
+        blk[0] = (int16_t)((si == 0 ? p0 + d0 : si == 1 ? p1 + d1 : si == 2 ? p2 + d2 : p3 + d3) << shift);
       else if (sz > 0)
-        blk[k + run] = (int16_t)v;
+        blk[k + run] = (int16_t)((uint32_t)v << shift);
     }
-    const int nk = dc ? 1 : (sz == 0 ? (run == 15 ? k + 16 : 64) : k + run + 1);
-    const bool end = nk >= 64;
-    k = end ? 0 : nk;
+    const int nk = dc ? (dc_only ? 64 : 1) : (sz == 0 ? (run == 15 ? k + 16 : 64) : k + run + 1);
+    const bool end = nk > kend;
+    k = end ? sd.k0 : nk;
     if (end) {
       u = u + 1 == sd.bmcu ? 0 : u + 1;
-      blocks++;
+      blocks += 1 + skip;
       if (WRITE && blocks < max_blocks) blk = block_ptr(block_base + blocks);
     }
   }
@@ -360,7 +376,7 @@ __global__ void __launch_bounds__(kDecThreads) k_seq_sync(const ScanDesc* __rest
   if (t >= sd.nspan) return;
   const SubRef ref = find_sub(segs, sd.nseg, t, true);
   const Segment& sg = segs[ref.seg];
-  if (ref.local == 0) nxt[t] = SubState{0, 0, 0};
+  if (ref.local == 0) nxt[t] = SubState{0, 0, sd.k0};
   const int f0 = ref.local * kSpanSubs, f1 = min(f0 + kSpanSubs, sg.nsub);
   SubState st = cur[t];
   piece_state[sg.sub0 + f0] = st;
@@ -370,7 +386,7 @@ __global__ void __launch_bounds__(kDecThreads) k_seq_sync(const ScanDesc* __rest
     SubCount cnt{};
     const long long stop = (long long)(f + 1) * kSubBits;
     if (decode_run<false>(tb, sd, r, st, stop, LLONG_MAX, cnt, 0, nullptr, nullptr)) {
-      st = SubState{stop, 0, 0};  // desynchronized: any guess will do
+      st = SubState{stop, 0, sd.k0};  // desynchronized: any guess will do
       r.init(data, sg.byte0, sg.nbytes, stop, win, w_lo, w_hi);
     }
     counts[sg.sub0 + f] = cnt;
@@ -392,7 +408,7 @@ __global__ void k_seq_chain(const ScanDesc* __restrict__ sdp, const Tables* __re
   load_tables(tb, tg);
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < sd.nseg; s += gridDim.x * blockDim.x) {
     const Segment& sg = segs[s];
-    SubState st{0, 0, 0};
+    SubState st{0, 0, sd.k0};
     Reader r;
     r.init(data, sg.byte0, sg.nbytes, 0);
     for (int i = 0; i + 1 < sg.nsub; i++) {
@@ -400,7 +416,7 @@ __global__ void k_seq_chain(const ScanDesc* __restrict__ sdp, const Tables* __re
       SubCount cnt{};
       const long long stop = (long long)(i + 1) * kSubBits;
       if (decode_run<false>(tb, sd, r, st, stop, LLONG_MAX, cnt, 0, nullptr, nullptr)) {
-        st = SubState{stop, 0, 0};
+        st = SubState{stop, 0, sd.k0};
         r.init(data, sg.byte0, sg.nbytes, stop);
       }
       counts[sg.sub0 + i] = cnt;
@@ -524,6 +540,108 @@ __global__ void __launch_bounds__(kDecThreads) k_seq_write(const ScanDesc* __res
     atomicCAS(error, 0, 1);
 }
 
+// The visiting-order block b of a scan -> its coefficients.
+__device__ __forceinline__ int16_t* scan_block(const ScanDesc& sd, int16_t* out, long long b) {
+  const long long mcu = b / sd.bmcu;
+  const int uu = (int)(b - mcu * sd.bmcu);
+  const int si = sd.mcu_si[uu];
+  const CompDesc& c = sd.fc[sd.comp[si]];
+  const long long my = mcu / sd.mcus_x, mx = mcu - my * sd.mcus_x;
+  const long long row = my * (sd.bmcu == 1 ? 1 : c.v) + sd.mcu_dy[uu];
+  const long long col = mx * (sd.bmcu == 1 ? 1 : c.h) + sd.mcu_dx[uu];
+  return out + (c.blk0 + row * c.bw + col) * 64;
+}
+
+// DC refinement (decode.rs:1283-1286): block j of a segment reads bit j of the segment (zero past its end) into bit al
+// of its DC. One thread per block of the scan.
+__global__ void __launch_bounds__(256) k_dc_refine(const ScanDesc* __restrict__ sdp, const Segment* __restrict__ segs,
+                                                   const uint8_t* __restrict__ data, long long nblocks,
+                                                   int16_t* __restrict__ out) {
+  const ScanDesc& sd = *sdp;
+  const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nblocks) return;
+  int lo = 0, hi = sd.nseg - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (segs[mid].block0 <= b)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const Segment& sg = segs[lo];
+  const long long j = b - sg.block0;
+  const int bit = (j >> 3) < sg.nbytes ? (data[sg.byte0 + (j >> 3)] >> (7 - (int)(j & 7))) & 1 : 0;
+  int16_t* blk = scan_block(sd, out, b);
+  blk[0] = (int16_t)(blk[0] | (int16_t)(bit << sd.al));
+}
+
+// AC refinement (decode.rs:1549-1601, decode_ac_refine), one thread per restart segment, its blocks in order: the
+// bits a block reads depend on which of its coefficients earlier scans made nonzero.
+__global__ void k_ac_refine(const ScanDesc* __restrict__ sdp, const Tables* __restrict__ tg,
+                            const Segment* __restrict__ segs, const uint8_t* __restrict__ data,
+                            int16_t* __restrict__ out, int* __restrict__ error) {
+  __shared__ __align__(16) Tables tb;
+  __shared__ ScanDesc sd;
+  if (threadIdx.x == 0) sd = *sdp;
+  load_tables(tb, tg);
+  const int16_t p1 = (int16_t)(1 << sd.al), m1 = (int16_t)(-(1 << sd.al));
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < sd.nseg; s += gridDim.x * blockDim.x) {
+    const Segment& sg = segs[s];
+    const DevHuff& ac = tb.ac[sd.ac[0]];
+    Reader r;
+    r.init(data, sg.byte0, sg.nbytes, 0);
+    uint32_t eobrun = 0;
+    for (long long b = 0; b < sg.nblocks; b++) {
+      int16_t* blk = scan_block(sd, out, sg.block0 + b);
+      int k = sd.ss;
+      if (eobrun == 0) {
+        while (k <= sd.se) {
+          const int rs = huff_decode(ac, r);
+          if (rs < 0) {
+            atomicCAS(error, 0, 1);
+            return;
+          }
+          int run = rs >> 4;
+          const int sz = rs & 15;
+          int16_t value = 0;
+          if (sz != 0) {
+            value = r.bits(1) ? p1 : m1;
+          } else if (run != 15) {
+            eobrun = 1u << run;
+            if (run > 0) eobrun += r.bits(run);
+            break;
+          }
+          // skip over already-nonzero coefficients (refining them) and `run` zero ones
+          while (k <= sd.se) {
+            const int16_t c = blk[k];
+            if (c != 0) {
+              if (r.bits(1) && (c & p1) == 0) blk[k] = (int16_t)(c + (c >= 0 ? p1 : m1));
+            } else {
+              if (--run < 0) break;
+            }
+            k++;
+          }
+          if (value != 0) {
+            if (k > 63) {
+              atomicCAS(error, 0, 1);
+              return;
+            }
+            blk[k] = value;
+          }
+          k++;
+        }
+      }
+      if (eobrun > 0) {
+        for (; k <= sd.se; k++) {
+          const int16_t c = blk[k];
+          if (c != 0 && r.bits(1) && (c & p1) == 0) blk[k] = (int16_t)(c + (c >= 0 ? p1 : m1));
+        }
+        eobrun--;
+      }
+    }
+  }
+}
+
 struct HostComp {
   uint8_t id;
   int h, v, tq, bw, bh, real_bw, real_bh;
@@ -540,6 +658,7 @@ struct HostScan {
 
 struct Parsed {
   int width = 0, height = 0;
+  bool progressive = false;
   std::vector<HostComp> comps;
   std::vector<HostScan> scans;
   uint8_t qt8[4][64];
@@ -566,7 +685,7 @@ size_t destuff(const uint8_t* d, size_t len, size_t pos, std::vector<uint8_t>& o
 
 int fail_parse(rcg_ctx* ctx, int status, const char* msg) { return fail(ctx, status, msg); }
 
-// The host part of parse() (decode.rs:622-697, :906-1103) for sequential Huffman frames.
+// The host part of parse() (decode.rs:622-697, :906-1103) for sequential and progressive Huffman frames.
 int parse_jpeg(rcg_ctx* ctx, const uint8_t* d, size_t len, Parsed& P) {
   if (len < 4 || d[0] != 0xFF || d[1] != 0xD8) return fail_parse(ctx, RCG_INVALID, "not a JPEG file");
   size_t pos = 2;
@@ -619,8 +738,9 @@ int parse_jpeg(rcg_ctx* ctx, const uint8_t* d, size_t len, Parsed& P) {
         b += 17 + total;
         bl -= 17 + total;
       }
-    } else if (m == 0xC0 || m == 0xC1) {
+    } else if (m == 0xC0 || m == 0xC1 || m == 0xC2) {
       if (!P.comps.empty()) return fail_parse(ctx, RCG_INVALID, "multiple SOF markers");
+      P.progressive = m == 0xC2;
       if (bl < 6) return fail_parse(ctx, RCG_INVALID, "bad SOF");
       if (b[0] != 8) return fail_parse(ctx, RCG_UNSUPPORTED, "only 8-bit JPEGs are decoded on the GPU");
       P.height = (b[1] << 8) | b[2];
@@ -655,9 +775,8 @@ int parse_jpeg(rcg_ctx* ctx, const uint8_t* d, size_t len, Parsed& P) {
         c.real_bw = ((P.width * c.h + hmax - 1) / hmax + 7) / 8;
         c.real_bh = ((P.height * c.v + vmax - 1) / vmax + 7) / 8;
       }
-    } else if ((m >= 0xC2 && m <= 0xCF && m != 0xC4 && m != 0xC8 && m != 0xCC) || m == 0xDE || m == 0xDF) {
-      return fail_parse(ctx, RCG_UNSUPPORTED,
-                        "progressive, lossless, hierarchical and arithmetic JPEGs are decoded on the host");
+    } else if ((m >= 0xC3 && m <= 0xCF && m != 0xC4 && m != 0xC8 && m != 0xCC) || m == 0xDE || m == 0xDF) {
+      return fail_parse(ctx, RCG_UNSUPPORTED, "lossless, hierarchical and arithmetic JPEGs are decoded on the host");
     } else if (m == 0xDD) {
       if (bl < 2) return fail_parse(ctx, RCG_INVALID, "bad DRI");
       ri = ((size_t)b[0] << 8) | b[1];
@@ -689,16 +808,36 @@ int parse_jpeg(rcg_ctx* ctx, const uint8_t* d, size_t len, Parsed& P) {
         sc.sd.dc[i] = (t >> 4) & 3;
         sc.sd.ac[i] = (t & 15) & 3;
       }
+      // Scan parameters (decode.rs:1084-1096): the spectral band and successive approximation of a progressive scan.
+      const uint8_t* tp = b + 1 + 2 * ns;
+      sc.sd.ss = 0;
+      sc.sd.se = 63;
+      if (P.progressive) {
+        sc.sd.ss = tp[0];
+        sc.sd.se = tp[1];
+        sc.sd.ah = tp[2] >> 4;
+        sc.sd.al = tp[2] & 15;
+        if (sc.sd.ss > sc.sd.se || sc.sd.se > 63 || sc.sd.al > 13 || (sc.sd.ss == 0 && sc.sd.se != 0) ||
+            (sc.sd.ss > 0 && ns != 1))
+          return fail_parse(ctx, RCG_INVALID, "bad progressive scan parameters");
+        sc.sd.kind = sc.sd.ss == 0 ? (sc.sd.ah == 0 ? kDcFirst : kDcRefine) : (sc.sd.ah == 0 ? kAcFirst : kAcRefine);
+      } else {
+        sc.sd.kind = kSeq;
+      }
+      sc.sd.k0 = sc.sd.ss;
+      // The tables the scan decodes with (decode.rs:1240-1248).
+      const bool need_dc = sc.sd.kind == kSeq || sc.sd.kind == kDcFirst;
+      const bool need_ac = sc.sd.kind == kSeq || sc.sd.ss > 0;
       for (int i = 0; i < ns; i++) {
         HostComp& c = P.comps[sc.sd.comp[i]];
         if (!c.snap && has_qt[c.tq]) {
           std::memcpy(c.snapq, qt[c.tq], sizeof c.snapq);
           c.snap = true;
         }
-        if (!has_dc[sc.sd.dc[i]] || !has_ac[sc.sd.ac[i]])
+        if ((need_dc && !has_dc[sc.sd.dc[i]]) || (need_ac && !has_ac[sc.sd.ac[i]]))
           return fail_parse(ctx, RCG_INVALID, "scan uses undefined huffman table");
-        sc.tables.dc[sc.sd.dc[i]] = dct[sc.sd.dc[i]];
-        sc.tables.ac[sc.sd.ac[i]] = act[sc.sd.ac[i]];
+        if (has_dc[sc.sd.dc[i]]) sc.tables.dc[sc.sd.dc[i]] = dct[sc.sd.dc[i]];
+        if (has_ac[sc.sd.ac[i]]) sc.tables.ac[sc.sd.ac[i]] = act[sc.sd.ac[i]];
       }
       // MCU pattern and geometry (decode.rs:1251-1258, :1270-1275)
       const bool inter = ns > 1;
@@ -851,10 +990,24 @@ int jpeg_decode(rcg_ctx* ctx, const uint8_t* data, size_t len, rcg_jpeg_info* in
     cudaMemcpyAsync(d_segs, sc.segs.data(), sizeof(Segment) * sc.segs.size(), cudaMemcpyHostToDevice, ctx->stream);
     cudaMemcpyAsync(d_sd, &sc.sd, sizeof(ScanDesc), cudaMemcpyHostToDevice, ctx->stream);
     cudaMemcpyAsync(d_tab, &sc.tables, sizeof(Tables), cudaMemcpyHostToDevice, ctx->stream);
-    // Initial guesses: every span starts at its first bit, first block of the MCU, at a DC.
+    if (sc.sd.kind == kDcRefine) {
+      long long nb = 0;
+      for (const Segment& g : sc.segs) nb = std::max(nb, g.block0 + g.nblocks);
+      if (nb > 0)
+        RCG_LAUNCH(ctx, "dc_refine", k_dc_refine, (unsigned)((nb + 255) / 256), 256, 0, d_sd, d_segs, d_bytes, nb,
+                   d_out);
+      continue;
+    }
+    if (sc.sd.kind == kAcRefine) {
+      RCG_LAUNCH(ctx, "ac_refine", k_ac_refine, (unsigned)((sc.sd.nseg + 31) / 32), 32, 0, d_sd, d_tab, d_segs,
+                 d_bytes, d_out, d_err);
+      continue;
+    }
+    // Initial guesses: every span starts at its first bit, first block of the MCU, at a block's first coefficient.
     std::vector<SubState> init((size_t)nspan);
     for (const Segment& g : sc.segs)
-      for (int i = 0; i < g.nspan; i++) init[g.span0 + i] = SubState{(long long)i * kSpanSubs * kSubBits, 0, 0};
+      for (int i = 0; i < g.nspan; i++)
+        init[g.span0 + i] = SubState{(long long)i * kSpanSubs * kSubBits, 0, sc.sd.k0};
     cudaMemcpyAsync(d_s0, init.data(), sizeof(SubState) * (size_t)nspan, cudaMemcpyHostToDevice, ctx->stream);
     cudaMemsetAsync(d_cnt, 0, sizeof(SubCount) * (size_t)nsub, ctx->stream);
     const unsigned grid_span = (unsigned)((nspan + kDecThreads - 1) / kDecThreads);

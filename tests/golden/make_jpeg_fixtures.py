@@ -1,9 +1,10 @@
-"""Collect the reference's sequential-Huffman JPEG fixtures as decoder test inputs (tests/golden/jpeg_fixtures.npz).
+"""Collect the reference's Huffman JPEG fixtures as decoder test inputs (tests/golden/jpeg_fixtures.npz).
 
-Reads rust-compress's fixtures/ directory (the path is the first argument), keeps the files the oracle's sequential
+Reads rust-compress's fixtures/ directory (the path is the first argument), keeps the files the oracle's Huffman
 decoder accepts (the reference's own test images written by libjpeg/libjpeg-turbo: baseline, optimized tables,
-gray, 4:4:4 and 4:2:0, ICC-tagged, and the Huffman twins of the arithmetic-coding fixtures), and stores each file's
-bytes with the SHA-256 of the coefficients the oracle decodes from it.
+gray, 4:4:4 and 4:2:0, ICC-tagged, progressive with successive approximation (rgb8_prog.jpg), and the sequential
+Huffman twins of the arithmetic-coding fixtures), and stores each file's bytes with the SHA-256 of the
+coefficients the oracle decodes from it.
 
     python tests/golden/make_jpeg_fixtures.py /path/to/rust-compress/fixtures
 """

@@ -1,10 +1,11 @@
-"""GPU entropy decoding of sequential Huffman JPEGs against the oracle's parse().into_coefs() restatement.
+"""GPU entropy decoding of Huffman JPEGs against the oracle's parse().into_coefs() restatement.
 
 Integer work: the coefficients, the table assignment, the component ids and the error behaviour must match the
 oracle exactly, for every sampling layout, gray, odd sizes, restart intervals (every MCU, and irregular ones),
 one scan per component, a 12 MP file (tens of thousands of self-synchronizing subsequences), the reference's own
-sequential fixture files (tests/golden/jpeg_fixtures.npz), corrupt and truncated files; other frame kinds answer
-RCG_UNSUPPORTED.
+fixture files (tests/golden/jpeg_fixtures.npz, rgb8_prog.jpg among them), progressive files of every candidate
+script of the restated progressive writer (DC and AC first scans, DC and AC refinement), corrupt and truncated files;
+other frame kinds answer RCG_UNSUPPORTED.
 """
 
 import hashlib
@@ -110,20 +111,65 @@ def test_decode_corrupt_and_truncated(ctx, oracle):
 
 
 def test_decode_unsupported_kinds(ctx, oracle):
-    found = False
-    for w, h in ((300, 200), (640, 480), (1024, 768)):
-        g = _encoded(oracle, synth.image(w, h, 74, sensor_sigma=3.0), 75, rcg.Subsampling.S420)
-        data, progressive = oracle.write_best_general(g)
-        if progressive:  # write_best chose a progressive script: SOF2
-            found = True
-            with pytest.raises(rcg.RcgError) as e:
-                ctx.decode_coefs(data)
-            assert e.value.status == rcg.RCG_UNSUPPORTED
-            break
-    assert found
+    g = _encoded(oracle, synth.image(64, 48, 74), 75, rcg.Subsampling.S420)
+    data = bytearray(oracle.write_jpeg_variant(g, 0, False))
+    sof = data.find(b"\xff\xc0")
+    for marker in (0xC3, 0xC9, 0xCA):  # lossless, arithmetic sequential, arithmetic progressive frames
+        data[sof + 1] = marker
+        with pytest.raises(rcg.RcgError) as e:
+            ctx.decode_coefs(bytes(data))
+        assert e.value.status == rcg.RCG_UNSUPPORTED
     with pytest.raises(rcg.RcgError) as e:
         ctx.decode_coefs(b"not a jpeg")
     assert e.value.status == rcg.RCG_INVALID
+
+
+@pytest.mark.parametrize("w,h,sub,gray,step", [(200, 152, 3, False, 1), (120, 90, 2, False, 7), (97, 65, 1, False, 7),
+                                               (33, 17, 3, False, 11), (64, 48, 0, True, 1)])
+def test_decode_progressive_scripts(ctx, oracle, w, h, sub, gray, step):
+    """Every `step`-th candidate script of the restated progressive writer (jpeg/src/progressive.rs:242-295): DC first
+    with and without a refinement, luma and chroma spectral splits, successive approximation down to al 0."""
+    img = synth.image(max(w, 16), max(h, 16), 75, sensor_sigma=2.0)[:h, :w].copy()
+    if gray:
+        img = np.ascontiguousarray(img[:, :, 0])
+    coefs, qt, lay = oracle.build_coefs(img, 80, sub, True)
+    for i in range(0, oracle.script_count(lay["ncomp"]), step):
+        _check(ctx, oracle, oracle.emit_script(w, h, lay, qt, coefs, i))
+
+
+def test_decode_progressive_12mp(ctx, oracle):
+    """A 12 MP progressive file with successive approximation in every band (the writer's last script: DC al 1, luma
+    al 2 split at 8, chroma al 1 split at 5: refinement scans for all three components)."""
+    import time
+
+    img = synth.image(4000, 3000, 76, sensor_sigma=3.0)
+    coefs, qt, lay = oracle.build_coefs(img, 80, 3, True)
+    n = oracle.script_count(3)
+    data = oracle.emit_script(4000, 3000, lay, qt, coefs, n - 1)
+    g, ids = oracle.decode_huffman(data)
+    ctx.decode_coefs(data)  # warm-up
+    t0 = time.perf_counter()
+    ci = ctx.decode_coefs(data)
+    dt = time.perf_counter() - t0
+    _same(ci, g, ids)
+    print(f"12 MP progressive, {len(data)} bytes: {dt * 1e3:.1f} ms")
+
+
+def test_decode_corrupt_progressive(ctx, oracle):
+    from test_oracle import _fixtures
+
+    rng = np.random.default_rng(12)
+    prog = [d for name, d, _ in _fixtures() if name == "rgb8_prog.jpg"]
+    img = synth.image(96, 80, 77)
+    coefs, qt, lay = oracle.build_coefs(img, 70, 3, True)
+    prog.append(oracle.emit_script(96, 80, lay, qt, coefs, oracle.script_count(3) - 1))
+    for data in prog:
+        for _ in range(60):
+            m = bytearray(data)
+            for i in rng.integers(2, len(m), 3):
+                m[i] = int(rng.integers(0, 256))
+            _check(ctx, oracle, bytes(m))
+            _check(ctx, oracle, bytes(m[: int(rng.integers(0, len(m) + 1))]))
 
 
 def test_decoded_source_feeds_the_requantize_search(ctx, oracle):

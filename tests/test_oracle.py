@@ -482,8 +482,9 @@ def _fixtures():
 
 def test_oracle_sequential_decoder_round_trips_and_fixtures(oracle):
     """parse().into_coefs() restated: the restated writer's baseline files (with restart intervals and per-component
-    scans too) decode to the coefficients written, and the reference's sequential fixture files decode to pinned
-    coefficients that survive a baseline re-encode unchanged (jpeg/tests/jpeg_decode.rs:95-110)."""
+    scans too) decode to the coefficients written, and the reference's Huffman fixture files (sequential and
+    progressive) decode to pinned coefficients that survive a baseline re-encode unchanged
+    (jpeg/tests/jpeg_decode.rs:95-110)."""
     import hashlib
 
     import rcg.synth as synth
@@ -502,6 +503,7 @@ def test_oracle_sequential_decoder_round_trips_and_fixtures(oracle):
     assert np.array_equal(d.coefs, g.coefs)
     fx = _fixtures()
     assert len(fx) >= 10
+    assert any(name == "rgb8_prog.jpg" for name, _, _ in fx)  # libjpeg's progressive script with refinement scans
     for name, data, sha in fx:
         d, ids = oracle.decode_sequential(data)
         assert hashlib.sha256(d.coefs.tobytes()).hexdigest() == sha, name
@@ -519,6 +521,45 @@ def test_oracle_sequential_decoder_round_trips_and_fixtures(oracle):
                 oracle.decode_sequential(blob)
             except ValueError:
                 pass
+
+
+def _coded_coefs(w, h, lay, coefs):
+    """The coefficients a progressive file carries: single-component AC scans code only the blocks that overlap the
+    image (jpeg/src/decode.rs:1255-1257), so the AC of the MCU-padding blocks reads back as 0."""
+    out = np.array(coefs, copy=True)
+    n = lay["ncomp"]
+    hmax, vmax = max(lay["h"][:n]), max(lay["v"][:n])
+    off = 0
+    for c in range(n):
+        bw, bh = int(lay["blocks_w"][c]), int(lay["blocks_h"][c])
+        rbw = ((w * lay["h"][c] + hmax - 1) // hmax + 7) // 8
+        rbh = ((h * lay["v"][c] + vmax - 1) // vmax + 7) // 8
+        blk = out[off: off + bw * bh * 64].reshape(bh, bw, 64)
+        blk[:, rbw:, 1:] = 0
+        blk[rbh:, :, 1:] = 0
+        off += bw * bh * 64
+    return out
+
+
+def test_oracle_progressive_decoder_round_trips(oracle):
+    """decode_dc_first / dc refinement / decode_ac_first / decode_ac_refine (jpeg/src/decode.rs:1509-1601) restated:
+    every candidate script of the restated progressive writer (jpeg/src/progressive.rs:242-295: spectral splits and
+    successive approximation of DC, luma and chroma) decodes back to the coefficients written, for 4:2:0, 4:2:2,
+    4:4:4 and gray, odd sizes with MCU padding included."""
+    import rcg.synth as synth
+
+    for w, h, sub, gray in ((200, 152, 3, False), (120, 90, 2, False), (97, 65, 1, False), (33, 17, 3, False),
+                            (64, 48, 0, True)):
+        img = synth.image(max(w, 16), max(h, 16), 7)[:h, :w].copy()
+        if gray:
+            img = np.ascontiguousarray(img[:, :, 0])
+        coefs, qt, lay = oracle.build_coefs(img, 70, sub, True)
+        want = _coded_coefs(w, h, lay, coefs)
+        n = oracle.script_count(lay["ncomp"])
+        assert n == (24 if gray else 144)
+        for i in range(n):
+            d, _ = oracle.decode_huffman(oracle.emit_script(w, h, lay, qt, coefs, i))
+            assert np.array_equal(d.coefs, want), (w, h, sub, i)
 
 
 def test_oracle_fp64_gradient_matches_central_differences(oracle):
