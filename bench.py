@@ -320,14 +320,24 @@ def batch_workload(ctx, torch, n=64, parallel=8, steps=2, perceptual=True):
     for _ in range(steps):
         res_b = ctx.search_batch(imgs, targets, 100, opts, parallel)
     tb = (time.perf_counter() - t0) / steps
+    # The lockstep batch: every step of every image in one work-list launch per stage (first call: plain launches,
+    # second: capture, then replays).
+    for _ in range(2):
+        ctx.search_batch(imgs, targets, 100, opts, lockstep=True)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        res_l = ctx.search_batch(imgs, targets, 100, opts, lockstep=True)
+    tl = (time.perf_counter() - t0) / steps
     t0 = time.perf_counter()
     res_p = [ctx.find_quality_ssimulacra2(im, t, 100, opts) for im, t in zip(imgs, targets)]
     tp = time.perf_counter() - t0
     same = all(a.quality == b.quality and a.trace == b.trace for a, b in zip(res_b, res_p))
+    same_l = all(a.quality == b.quality and a.trace == b.trace for a, b in zip(res_l, res_p))
     out = {"workload": f"{n} images, log-uniform 640x480..6000x4000 ({mpx:.0f} MP in all), targets U(55,85), "
                        "4:2:0, trellis", "images": n, "megapixels": mpx,
            "plain_searches_per_s": n / tp, "batch_searches_per_s": n / tb, "batch_parallel": parallel,
            "batch_vs_plain": tp / tb, "identical_results": same,
+           "lockstep_searches_per_s": n / tl, "lockstep_vs_batch": tb / tl, "lockstep_identical": same_l,
            "mean_quality": sum(r.quality for r in res_b) / n}
     if perceptual:
         # The perceptual search on the same images and targets: planned file sizes of the plain result, of the

@@ -330,6 +330,20 @@ int rcg_search_batch(rcg_ctx* ctx, int n, const uint8_t* const* srcs, const uint
                      const rcg_encode_options* opts, int parallel, rcg_found* found, int16_t* const* coefs,
                      const size_t* coefs_len, uint8_t* const* qtables);
 
+/* The same many searches in lockstep: every bisection step of every image is one launch per stage over a work-list
+ * of all the images' CTAs (step tables, quantization, rate tables, trellis, dequantization + IDCT, upsampling,
+ * pyramid, scorer tiles, reductions), the step loop captured as one CUDA graph per batch composition (the images'
+ * sizes) and replayed for later batches of the same composition. Each image's set-up (upload, colour planes, FDCTs,
+ * the reference pyramid) runs on its own stream first. Results are exactly those of rcg_search on each image (the
+ * same kernels per image), near ties included; arguments as rcg_search_batch without `parallel`. All images' buffers
+ * are resident at once (about 70 bytes per pixel). Like rcg_search_batch, no single reference function corresponds to
+ * it: the cli runs find_quality_with per file (jpeg/src/target.rs:29-56) across rayon workers (cli/src/main.rs:57-60).
+ */
+int rcg_search_batch_lockstep(rcg_ctx* ctx, int n, const uint8_t* const* srcs, const uint32_t* widths,
+                              const uint32_t* heights, const int* channels, const double* targets, int max_quality,
+                              const rcg_encode_options* opts, rcg_found* found, int16_t* const* coefs,
+                              const size_t* coefs_len, uint8_t* const* qtables);
+
 /* ---- Perceptual trellis (opt-in; not a reference mode)
  *
  * The SSIMULACRA2 gradient of a decoded image, pulled back through the decoder's YCbCr->RGB conversion, chroma

@@ -514,6 +514,8 @@ void rcg_ctx_destroy(rcg_ctx* ctx) {
   if (!ctx) return;
   for (rcg_ctx* wk : ctx->workers) rcg_ctx_destroy(wk);
   ctx->workers.clear();
+  for (rcg_ctx* sub : ctx->lock_subs) rcg_ctx_destroy(sub);
+  ctx->lock_subs.clear();
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   drop_graphs(ctx);
@@ -1234,34 +1236,46 @@ static int settle_ties(rcg_ctx* ctx, const SearchScorer& sc, SearchState* d_ss, 
   return RCG_OK;
 }
 
-// d_weights (nullable): the perceptual trellis's weights in the coefficient layout of the (quality-independent)
-// subsampling; every candidate's trellis then runs in the weighted mode.
-static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, int metric, double target,
-                       int max_q, int subsampling, int trellis_on, rcg_found* found, int16_t* d_coefs_out,
-                       size_t coefs_len, uint8_t* d_qt_out, int16_t* h_coefs_out, uint8_t* h_qt_out,
-                       const float* d_weights = nullptr) {
-  int rc;
+// One device search from set-up to collection: its buffers (in the context's workspace), the encoder's set-up and
+// the scorer.
+struct SearchRun {
+  int w = 0, h = 0, channels = 0, metric = 0, subsampling = 0, max_steps = 0;
   SearchScorer sc;
-  SearchState* d_ss = (SearchState*)workspace(ctx, "search_state", sizeof(SearchState));
-  StepDesc* d_st = (StepDesc*)workspace(ctx, "step_search", sizeof(StepDesc));
-  if (!d_ss || !d_st) return RCG_NO_MEMORY;
+  EncoderSetup es;
+  SearchState* d_ss = nullptr;
+  StepDesc* d_st = nullptr;
+  int16_t* slots = nullptr;
+  uint8_t* planes = nullptr;
+};
+
+// Everything before the step loop, queued on the context's stream: the buffers, the quality-independent work (the
+// reference image's linear pyramid for SSIMULACRA2, colour planes, FDCTs) and the initial bisection state.
+static int search_prepare(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, int metric, double target,
+                          int max_q, int subsampling, int trellis_on, SearchRun* run) {
+  int rc;
+  run->w = w;
+  run->h = h;
+  run->channels = channels;
+  run->metric = metric;
+  run->subsampling = subsampling;
+  SearchScorer& sc = run->sc;
+  run->d_ss = (SearchState*)workspace(ctx, "search_state", sizeof(SearchState));
+  run->d_st = (StepDesc*)workspace(ctx, "step_search", sizeof(StepDesc));
+  if (!run->d_ss || !run->d_st) return RCG_NO_MEMORY;
   if ((rc = scorer_setup(ctx, metric, w, h, channels, &sc)) != RCG_OK) return rc;
-  // Quality-independent work, once per search: the reference image's linear pyramid (SSIMULACRA2; SSIM reads the
-  // source pixels as they are), colour planes, FDCTs.
   if (metric == RCG_METRIC_SSIM) {
     sc.ref_px = d_src;
   } else {
     if ((rc = to_linear(ctx, d_src, w, h, channels, 8, sc.ref_pyr)) != RCG_OK) return rc;
     build_pyramid(ctx, sc.pd, sc.ref_pyr);
   }
-  EncoderSetup es;
-  if ((rc = setup_encoder(ctx, d_src, w, h, channels, subsampling, &es)) != RCG_OK) return rc;
+  if ((rc = setup_encoder(ctx, d_src, w, h, channels, subsampling, &run->es)) != RCG_OK) return rc;
   int max_steps = 1;
   for (int span = max_q; span > 1; span = (span + 1) / 2) max_steps++;
-  max_steps = std::min(max_steps, kMaxSteps);
-  int16_t* slots = (int16_t*)workspace(ctx, "coef_slots", (size_t)es.max_coefs * 2 * max_steps);
-  uint8_t* planes = (uint8_t*)workspace(ctx, "dec_planes", (size_t)es.max_plane_bytes);
-  if (!slots || !planes) return RCG_NO_MEMORY;
+  run->max_steps = std::min(max_steps, kMaxSteps);
+  run->slots = (int16_t*)workspace(ctx, "coef_slots", (size_t)run->es.max_coefs * 2 * run->max_steps);
+  run->planes = (uint8_t*)workspace(ctx, "dec_planes", (size_t)run->es.max_plane_bytes);
+  if (!run->slots || !run->planes) return RCG_NO_MEMORY;
   SearchState hs;
   std::memset(&hs, 0, sizeof hs);
   hs.lo = 1;
@@ -1275,25 +1289,17 @@ static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int cha
   hs.channels = channels;
   hs.best_q = max_q;
   hs.tie_band = metric == RCG_METRIC_SSIMULACRA2 ? ctx->tie_band : 0.0;
-  cudaMemcpyAsync(d_ss, &hs, sizeof hs, cudaMemcpyHostToDevice, ctx->stream);
-  // Every launch below takes pointers into this context's workspace and sizes that follow from the key.
-  const std::vector<long long> key = {1, (long long)(uintptr_t)d_src, w, h, channels, metric, subsampling, trellis_on,
-                                      max_steps, (long long)(uintptr_t)d_weights};
-  auto issue_step = [&]() {
-    step_tables(ctx, d_ss, d_st, w, h, slots, es.max_coefs, d_weights);
-    quantize(ctx, d_st, es.caches, es.max_blocks);
-    rate_tables(ctx, d_st);
-    trellis(ctx, d_st, es.caches, es.max_blocks, d_weights != nullptr);
-    dequant_idct(ctx, d_st, nullptr, planes, es.max_blocks);
-    score_candidate(ctx, sc, d_st, planes, w, h, channels, d_ss);
-  };
-  rc = run_step_loop(ctx, key, [&]() {
-    for (int s = 0; s < max_steps; s++) issue_step();
-  });
-  if (rc != RCG_OK) return rc;
-  cudaMemcpyAsync(&hs, d_ss, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream);
-  if ((rc = finish(ctx, "search")) != RCG_OK) return rc;
-  if ((rc = settle_ties(ctx, sc, d_ss, &hs, max_steps, w, h, issue_step)) != RCG_OK) return rc;
+  // A copy from pageable memory returns once the source is staged, so `hs` may go out of scope.
+  cudaError_t e = cudaMemcpyAsync(run->d_ss, &hs, sizeof hs, cudaMemcpyHostToDevice, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "search state upload");
+  return RCG_OK;
+}
+
+// The result of a finished search: Found, and the chosen coefficients and tables to device or host buffers.
+static int search_collect(rcg_ctx* ctx, const SearchRun& run, const SearchState& hs, rcg_found* found,
+                          int16_t* d_coefs_out, size_t coefs_len, uint8_t* d_qt_out, int16_t* h_coefs_out,
+                          uint8_t* h_qt_out) {
+  int rc;
   if (!hs.done) return fail(ctx, RCG_TIMEOUT, "bisection did not finish within the step budget");
   found->quality = hs.best_q;
   found->score = hs.best_score;
@@ -1304,8 +1310,8 @@ static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int cha
     found->nsteps = s + 1;
   }
   rcg_coef_layout lay;
-  layout_of(w, h, channels, hs.best_q, subsampling, &lay);
-  const int16_t* best = slots + (size_t)hs.best_step * es.max_coefs;
+  layout_of(run.w, run.h, run.channels, hs.best_q, run.subsampling, &lay);
+  const int16_t* best = run.slots + (size_t)hs.best_step * run.es.max_coefs;
   if (d_coefs_out || h_coefs_out) {
     if ((long long)coefs_len < lay.ncoefs) return fail(ctx, RCG_INVALID, "coefficient buffer too short");
     if (d_coefs_out) {
@@ -1319,6 +1325,41 @@ static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int cha
   if (h_qt_out) std::memcpy(h_qt_out, qt, 128);
   if (d_qt_out) cudaMemcpyAsync(d_qt_out, qt, 128, cudaMemcpyHostToDevice, ctx->stream);
   return finish(ctx, "search output");
+}
+
+// d_weights (nullable): the perceptual trellis's weights in the coefficient layout of the (quality-independent)
+// subsampling; every candidate's trellis then runs in the weighted mode.
+static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, int metric, double target,
+                       int max_q, int subsampling, int trellis_on, rcg_found* found, int16_t* d_coefs_out,
+                       size_t coefs_len, uint8_t* d_qt_out, int16_t* h_coefs_out, uint8_t* h_qt_out,
+                       const float* d_weights = nullptr) {
+  SearchRun run;
+  int rc = search_prepare(ctx, d_src, w, h, channels, metric, target, max_q, subsampling, trellis_on, &run);
+  if (rc != RCG_OK) return rc;
+  const EncoderSetup& es = run.es;
+  const SearchScorer& sc = run.sc;
+  SearchState* d_ss = run.d_ss;
+  StepDesc* d_st = run.d_st;
+  // Every launch below takes pointers into this context's workspace and sizes that follow from the key.
+  const std::vector<long long> key = {1, (long long)(uintptr_t)d_src, w, h, channels, metric, subsampling, trellis_on,
+                                      run.max_steps, (long long)(uintptr_t)d_weights};
+  auto issue_step = [&]() {
+    step_tables(ctx, d_ss, d_st, w, h, run.slots, es.max_coefs, d_weights);
+    quantize(ctx, d_st, es.caches, es.max_blocks);
+    rate_tables(ctx, d_st);
+    trellis(ctx, d_st, es.caches, es.max_blocks, d_weights != nullptr);
+    dequant_idct(ctx, d_st, nullptr, run.planes, es.max_blocks);
+    score_candidate(ctx, sc, d_st, run.planes, w, h, channels, d_ss);
+  };
+  rc = run_step_loop(ctx, key, [&]() {
+    for (int s = 0; s < run.max_steps; s++) issue_step();
+  });
+  if (rc != RCG_OK) return rc;
+  SearchState hs;
+  cudaMemcpyAsync(&hs, d_ss, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream);
+  if ((rc = finish(ctx, "search")) != RCG_OK) return rc;
+  if ((rc = settle_ties(ctx, sc, d_ss, &hs, run.max_steps, w, h, issue_step)) != RCG_OK) return rc;
+  return search_collect(ctx, run, hs, found, d_coefs_out, coefs_len, d_qt_out, h_coefs_out, h_qt_out);
 }
 
 // The goal checks of find_jpeg_quality (cli/src/pipeline.rs:211-218).
@@ -1424,6 +1465,166 @@ int rcg_search_batch(rcg_ctx* ctx, int n, const uint8_t* const* srcs, const uint
   for (int t = 0; t < p; t++) ctx->tie_rescores += ctx->workers[t]->tie_rescores - ties0[t];
   for (int i = 0; i < n; i++)
     if (status[i] != RCG_OK) return fail(ctx, status[i], "image " + std::to_string(i) + ": " + messages[i]);
+  ctx->last_error.clear();
+  return RCG_OK;
+}
+
+constexpr int kLockThreads = 8;  // host threads of a lockstep batch's per-image set-up and collection
+
+int rcg_search_batch_lockstep(rcg_ctx* ctx, int n, const uint8_t* const* srcs, const uint32_t* widths,
+                              const uint32_t* heights, const int* channels, const double* targets, int max_quality,
+                              const rcg_encode_options* opts, rcg_found* found, int16_t* const* coefs,
+                              const size_t* coefs_len, uint8_t* const* qtables) {
+  if (!ctx) return RCG_INVALID;
+  if (n < 0 || (n > 0 && (!srcs || !widths || !heights || !channels || !targets || !found)))
+    return fail(ctx, RCG_INVALID, "null pointer");
+  if (n == 0) return RCG_OK;
+  int rc = check_opts(ctx, opts, false);
+  if (rc != RCG_OK) return rc;
+  for (int i = 0; i < n; i++) {
+    if (!srcs[i]) return fail(ctx, RCG_INVALID, "image " + std::to_string(i) + ": null pointer");
+    if ((rc = check_image(ctx, widths[i], heights[i], channels[i])) != RCG_OK ||
+        (rc = check_goal(ctx, RCG_METRIC_SSIMULACRA2, widths[i], heights[i], targets[i])) != RCG_OK)
+      return fail(ctx, rc, "image " + std::to_string(i) + ": " + ctx->last_error);
+  }
+  const int max_q = std::max(1, std::min(max_quality, 100));
+  cudaSetDevice(ctx->device);
+  while ((int)ctx->lock_subs.size() < n) {
+    rcg_ctx* sub = nullptr;
+    int crc = rcg_ctx_create(ctx->device, &sub);
+    if (crc != RCG_OK) return fail(ctx, crc, "cannot create a batch image context");
+    sub->stage_copies = true;
+    ctx->lock_subs.push_back(sub);
+  }
+  // Per image, on its own context's stream (the images' set-ups overlap one another): upload, colour planes, FDCTs,
+  // the reference's pyramid, the initial bisection state. Host threads share the images, so the staging copies of
+  // the uploads run in parallel. Then the caller's stream waits for all of them.
+  std::vector<SearchRun> runs((size_t)n);
+  std::vector<int> status((size_t)n, RCG_OK);
+  const int nthreads = std::max(1, std::min(n, kLockThreads));
+  auto for_images = [&](const std::function<void(int)>& fn) {
+    std::atomic<int> next(0);
+    auto work = [&]() {
+      cudaSetDevice(ctx->device);
+      for (int i = next.fetch_add(1); i < n; i = next.fetch_add(1)) fn(i);
+    };
+    std::vector<std::thread> threads;
+    for (int t = 1; t < nthreads; t++) threads.emplace_back(work);
+    work();
+    for (auto& th : threads) th.join();
+  };
+  for_images([&](int i) {
+    rcg_ctx* sub = ctx->lock_subs[(size_t)i];
+    sub->tie_band = ctx->tie_band;
+    sub->band_chunks = ctx->band_chunks;
+    const size_t bytes = (size_t)widths[i] * heights[i] * channels[i];
+    uint8_t* d_src = (uint8_t*)workspace(sub, "img_src", bytes);
+    int r = d_src ? RCG_OK : RCG_NO_MEMORY;
+    if (r == RCG_OK) r = copy_to_device(sub, d_src, srcs[i], bytes);
+    if (r == RCG_OK)
+      r = search_prepare(sub, d_src, (int)widths[i], (int)heights[i], channels[i], RCG_METRIC_SSIMULACRA2,
+                         targets[i], max_q, opts->subsampling, opts->trellis, &runs[(size_t)i]);
+    if (r == RCG_OK && !sub->switch_event &&
+        cudaEventCreateWithFlags(&sub->switch_event, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      r = fail(sub, RCG_CUDA_ERROR, "batch event");
+    }
+    if (r == RCG_OK) cudaEventRecord(sub->switch_event, sub->stream);
+    status[(size_t)i] = r;
+  });
+  for (int i = 0; i < n; i++) {
+    if (status[(size_t)i] != RCG_OK)
+      return fail(ctx, status[(size_t)i], "image " + std::to_string(i) + ": " + ctx->lock_subs[(size_t)i]->last_error);
+    cudaStreamWaitEvent(ctx->stream, ctx->lock_subs[(size_t)i]->switch_event, 0);
+  }
+  // The work-lists: per image its StepDesc, search state, buffers and first CTA in each stage's grid.
+  std::vector<LockItem> items((size_t)n);
+  long long q_total = 0, u_total = 0, p_total = 0, t_total = 0;
+  int max_scales = 1, max_steps = 1;
+  for (int i = 0; i < n; i++) {
+    const SearchRun& r = runs[(size_t)i];
+    rcg_ctx* sub = ctx->lock_subs[(size_t)i];
+    LockItem& it = items[(size_t)i];
+    std::memset(&it, 0, sizeof it);
+    it.ss = r.d_ss;
+    it.st = r.d_st;
+    for (int k = 0; k < 9; k++) it.caches[k] = r.es.caches[k];
+    it.slots = r.slots;
+    it.slot_stride = r.es.max_coefs;
+    it.planes = r.planes;
+    it.w = r.w;
+    it.h = r.h;
+    it.ref_pyr = r.sc.ref_pyr;
+    it.dist_pyr = r.sc.dist_pyr;
+    it.partials = (double*)sub->bufs["score_partials"].ptr;
+    it.scale_sums = (double*)sub->bufs["score_scale_sums"].ptr;
+    it.counter = (unsigned*)sub->bufs["score_counter"].ptr;
+    it.score = r.sc.d_score;
+    it.pd = plan_bands(ctx, r.sc.pd);
+    it.q0 = q_total;
+    q_total += (r.es.max_blocks + 127) / 128;
+    it.ux = ((r.w + 3) / 4 + 127) / 128;
+    it.uy = std::min((r.h + 1) / 2, 65535);
+    it.u0 = u_total;
+    u_total += (long long)it.ux * it.uy;
+    it.p0 = p_total;
+    if (it.pd.nscales >= 2)
+      p_total += (long long)((it.pd.s[1].w + 31) / 32) * ((it.pd.s[1].h + 31) / 32);
+    it.t0 = t_total;
+    t_total += it.pd.total_tiles;
+    max_scales = std::max(max_scales, it.pd.nscales);
+    max_steps = std::max(max_steps, r.max_steps);
+  }
+  if (q_total > INT32_MAX || u_total > INT32_MAX || p_total > INT32_MAX || t_total > INT32_MAX)
+    return fail(ctx, RCG_INVALID, "batch too large for one launch");
+  LockItem* d_items = (LockItem*)workspace(ctx, "lock_items", sizeof(LockItem) * (size_t)n);
+  double* d_exact = (double*)workspace(ctx, "x_score", sizeof(double), false);
+  if (!d_items || !d_exact) return RCG_NO_MEMORY;
+  cudaMemcpyAsync(d_items, items.data(), sizeof(LockItem) * (size_t)n, cudaMemcpyHostToDevice, ctx->stream);
+  auto issue_step = [&]() {
+    lock_step_codec(ctx, d_items, n, q_total, u_total);
+    lock_step_score(ctx, d_items, n, p_total, t_total, max_scales);
+  };
+  // The grids follow from the totals; the images' buffers come in through the work-list uploaded above.
+  const std::vector<long long> key = {5, n, max_steps, q_total, u_total, p_total, t_total, max_scales};
+  rc = run_step_loop(ctx, key, [&]() {
+    for (int s = 0; s < max_steps; s++) issue_step();
+  });
+  if (rc != RCG_OK) return rc;
+  std::vector<SearchState> hs((size_t)n);
+  auto read_states = [&]() -> int {
+    for (int i = 0; i < n; i++)
+      cudaMemcpyAsync(&hs[(size_t)i], runs[(size_t)i].d_ss, sizeof(SearchState), cudaMemcpyDeviceToHost, ctx->stream);
+    return finish(ctx, "lockstep batch");
+  };
+  if ((rc = read_states()) != RCG_OK) return rc;
+  // Near ties (settle_ties): every paused image's candidate is rescored in the reference's arithmetic and resumed,
+  // then the remaining steps run for all images (the finished ones skip).
+  for (;;) {
+    int from = max_steps;
+    for (int i = 0; i < n; i++) {
+      if (hs[(size_t)i].done != 2) continue;
+      const SearchRun& r = runs[(size_t)i];
+      if ((rc = exact_score(ctx, r.sc.ref_pyr, r.sc.dist_pyr, r.w, r.h, d_exact)) != RCG_OK) return rc;
+      search_resume(ctx, r.d_ss, d_exact);
+      ctx->tie_rescores++;
+      from = std::min(from, hs[(size_t)i].step + 1);
+    }
+    if (from == max_steps) break;
+    for (int s = from; s < max_steps; s++) issue_step();
+    if ((rc = read_states()) != RCG_OK) return rc;
+  }
+  // Results, each through its image's context (the step loop is complete: the states were read after it), in
+  // parallel like the set-up.
+  for_images([&](int i) {
+    rcg_ctx* sub = ctx->lock_subs[(size_t)i];
+    status[(size_t)i] = search_collect(sub, runs[(size_t)i], hs[(size_t)i], &found[i], nullptr,
+                                       coefs_len ? coefs_len[i] : 0, nullptr, coefs ? coefs[i] : nullptr,
+                                       qtables ? qtables[i] : nullptr);
+  });
+  for (int i = 0; i < n; i++)
+    if (status[(size_t)i] != RCG_OK)
+      return fail(ctx, status[(size_t)i], "image " + std::to_string(i) + ": " + ctx->lock_subs[(size_t)i]->last_error);
   ctx->last_error.clear();
   return RCG_OK;
 }

@@ -355,7 +355,7 @@ __device__ __forceinline__ int bitlen(unsigned v) { return 32 - __clz(v); }
 // 221-228, :343-374: (run<<4)|size symbols, ZRL 0xF0, EOB 0x00; luma = component 0, chroma = components 1-2);
 // otherwise they are the candidate's output.
 // At most 128 registers: 4 CTAs per SM instead of 3 (34 -> 30 us per 12 MP candidate, small spill).
-__global__ void __launch_bounds__(128, 4) k_quantize(StepDesc* __restrict__ st, CacheSet cs) {
+__device__ __forceinline__ void quantize_body(StepDesc* __restrict__ st, const CacheSet& cs, long long bx) {
   __shared__ unsigned int sh[2][256];
   if (!st->active) return;
   const bool hist = st->use_trellis != 0;
@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(128, 4) k_quantize(StepDesc* __restrict__ st, 
     for (int i = threadIdx.x; i < 512; i += blockDim.x) (&sh[0][0])[i] = 0;
     __syncthreads();
   }
-  const long long gb = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gb = bx * blockDim.x + threadIdx.x;
   if (gb < st->nblocks) {
     int c = comp_of(st, gb);
     const CompDesc& cd = st->comp[c];
@@ -414,6 +414,10 @@ __global__ void __launch_bounds__(128, 4) k_quantize(StepDesc* __restrict__ st, 
   }
 }
 
+__global__ void __launch_bounds__(128, 4) k_quantize(StepDesc* __restrict__ st, CacheSet cs) {
+  quantize_body(st, cs, blockIdx.x);
+}
+
 int quantize(rcg_ctx* ctx, StepDesc* d_step, const float* const* d_caches, long long max_blocks) {
   CacheSet cs;
   for (int i = 0; i < 9; i++) cs.p[i] = d_caches[i];
@@ -427,13 +431,13 @@ int quantize(rcg_ctx* ctx, StepDesc* d_step, const float* const* d_caches, long 
 // Code lengths of the measured AC statistics (huff_lengths: build_lengths over the 256 symbols plus optimal_table's
 // dummy), then optimal_table's sizes (jpeg/src/encode.rs:245-262), Rdo's code-length table (jpeg/src/rdo.rs:36-39)
 // and the lambda*rate table (jpeg/src/rdo.rs:47-52). One CTA per component.
-__global__ void __launch_bounds__(288) k_rate_tables(StepDesc* __restrict__ st) {
+__device__ __forceinline__ void rate_tables_body(StepDesc* __restrict__ st, const int comp) {
   __shared__ unsigned freq[kHuffSyms];
   __shared__ unsigned char lens[kHuffSyms];
   __shared__ HuffScratch scratch;
   __shared__ float len[256];
   if (!st->active || !st->use_trellis) return;
-  const int comp = blockIdx.x;  // the rate model is per class, lambda per component
+  // the rate model is per class, lambda per component
   if (comp >= st->ncomp) return;
   const int cls = comp < 1 ? comp : 1;
   const int t = threadIdx.x;
@@ -458,6 +462,8 @@ __global__ void __launch_bounds__(288) k_rate_tables(StepDesc* __restrict__ st) 
   if (t == 0) st->eob[comp] = fmul(lambda, len[0]);
 }
 
+__global__ void __launch_bounds__(288) k_rate_tables(StepDesc* __restrict__ st) { rate_tables_body(st, blockIdx.x); }
+
 int rate_tables(rcg_ctx* ctx, StepDesc* d_step) {
   RCG_LAUNCH(ctx, "rate_tables", k_rate_tables, 3, 288, 0, d_step);
   return RCG_OK;
@@ -474,14 +480,14 @@ int rate_tables(rcg_ctx* ctx, StepDesc* d_step) {
 // product, then the same squared-error product as the plain weight); the plain instantiation reads no weights.
 // 6 CTAs per SM (80 registers, no spill) instead of 5.
 template <bool kWeighted>
-__global__ void __launch_bounds__(128, 6) k_trellis(StepDesc* __restrict__ st, CacheSet cs) {
+__device__ __forceinline__ void trellis_body(StepDesc* __restrict__ st, const CacheSet& cs, long long bx) {
   // The per-position tables of every component and the lambda*rate tables of the components this CTA's blocks
   // belong to (usually one), staged in shared memory: the DP reads them at every position.
   __shared__ float lr[3][64 * 16];
   __shared__ float s_scale[3][64], s_rq[3][64], s_rw[3][64];
   if (!st->active || !st->use_trellis) return;
   const bool requant = st->requant != 0;
-  const long long blk0 = (long long)blockIdx.x * blockDim.x;
+  const long long blk0 = bx * blockDim.x;
   const int c_lo = comp_of(st, blk0), c_hi = comp_of(st, min(blk0 + (long long)blockDim.x, st->nblocks) - 1);
   for (int i = threadIdx.x; i < (c_hi - c_lo + 1) * 64 * 16; i += blockDim.x)
     (&lr[c_lo][0])[i] = (&st->lr[c_lo][0])[i];
@@ -635,6 +641,11 @@ __global__ void __launch_bounds__(128, 6) k_trellis(StepDesc* __restrict__ st, C
   }
 }
 
+template <bool kWeighted>
+__global__ void __launch_bounds__(128, 6) k_trellis(StepDesc* __restrict__ st, CacheSet cs) {
+  trellis_body<kWeighted>(st, cs, blockIdx.x);
+}
+
 int trellis(rcg_ctx* ctx, StepDesc* d_step, const float* const* d_caches, long long max_blocks, bool weighted) {
   CacheSet cs;
   for (int i = 0; i < 9; i++) cs.p[i] = d_caches ? d_caches[i] : nullptr;
@@ -680,10 +691,10 @@ __device__ __forceinline__ void idct_pass(float (&d)[64]) {
 
 // idct_planes (jpeg/src/decode.rs:1310-1343): dequantize into natural order, IDCT (jpeg/src/dct.rs:111-123),
 // round_f32 + 128 clamped to 0..255. One thread per block.
-__global__ void __launch_bounds__(128) k_dequant_idct(const StepDesc* __restrict__ st,
-                                                     const int16_t* __restrict__ coefs, uint8_t* __restrict__ planes) {
+__device__ __forceinline__ void dequant_idct_body(const StepDesc* __restrict__ st, const int16_t* __restrict__ coefs,
+                                                  uint8_t* __restrict__ planes, long long cta) {
   if (!st->active) return;
-  long long gb = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long gb = cta * blockDim.x + threadIdx.x;
   if (gb >= st->nblocks) return;
   int c = comp_of(st, gb);
   const CompDesc& cd = st->comp[c];
@@ -724,6 +735,11 @@ __global__ void __launch_bounds__(128) k_dequant_idct(const StepDesc* __restrict
     }
     *reinterpret_cast<uint2*>(dst + (size_t)y * stride) = make_uint2(lo, hi);
   }
+}
+
+__global__ void __launch_bounds__(128) k_dequant_idct(const StepDesc* __restrict__ st,
+                                                     const int16_t* __restrict__ coefs, uint8_t* __restrict__ planes) {
+  dequant_idct_body(st, coefs, planes, blockIdx.x);
 }
 
 int dequant_idct(rcg_ctx* ctx, StepDesc* d_step, const int16_t* d_coefs, uint8_t* d_planes, long long max_blocks) {
@@ -833,8 +849,10 @@ __device__ __forceinline__ void upsample_420(const StepDesc* __restrict__ st, co
 // planes the scorer starts from (core/src/ssimulacra2.rs:192-203: Gray is replicated to three channels).
 // 10 CTAs per SM (48 registers) instead of 7: the kernel waits on loads, so more warps hide more of it
 // (51 -> 47 us per 12 MP candidate).
-__global__ void __launch_bounds__(128, 10) k_upsample_color(const StepDesc* __restrict__ st, const uint8_t* __restrict__ planes, int w, int h,
-                                 uint8_t* __restrict__ rgb, float* __restrict__ lin) {
+__device__ __forceinline__ void upsample_color_body(const StepDesc* __restrict__ st,
+                                                    const uint8_t* __restrict__ planes, int w, int h,
+                                                    uint8_t* __restrict__ rgb, float* __restrict__ lin,
+                                                    const unsigned bx, const unsigned by, const unsigned gy) {
   if (!st->active) return;
   const int ncomp = st->ncomp, hmax = st->hmax, vmax = st->vmax;
   const CompDesc c0 = st->comp[0];
@@ -842,21 +860,21 @@ __global__ void __launch_bounds__(128, 10) k_upsample_color(const StepDesc* __re
   const bool fast420 = !rgb && lin && ncomp == 3 && hmax == 2 && vmax == 2 && c0.h == 2 && c0.v == 2 &&
                        st->comp[1].h == 1 && st->comp[1].v == 1 && st->comp[2].h == 1 && st->comp[2].v == 1 &&
                        w % 4 == 0;
-  if (fast420 && (int)blockIdx.y >= (h + 1) / 2) return;
+  if (fast420 && (int)by >= (h + 1) / 2) return;
   // The sRGB table lives in shared memory: per-thread indices differ, which would serialize constant-memory reads.
   __shared__ float lut[256];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = c_lut8[i];
   __syncthreads();
   // Four consecutive pixels of one row per thread, so each thread moves enough bytes per request.
-  const int x0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int x0 = 4 * (bx * blockDim.x + threadIdx.x);
   if (x0 >= w) return;
   if (fast420) {
-    for (int j = blockIdx.y; j < (h + 1) / 2; j += gridDim.y) upsample_420(st, planes, w, h, lin, lut, x0, j);
+    for (int j = by; j < (h + 1) / 2; j += gy) upsample_420(st, planes, w, h, lin, lut, x0, j);
     return;
   }
   const size_t np = (size_t)w * h;
   const bool vec_out = (w % 4 == 0) && (np % 4 == 0) && (x0 + 4 <= w);
-  for (int y = blockIdx.y; y < h; y += gridDim.y) {
+  for (int y = by; y < h; y += gy) {
     int yv[4], cbv[4], crv[4];
     // Luma: full resolution when it carries the maximum sampling factors (always, for this encoder's layouts).
     if (c0.h == hmax && c0.v == vmax) {
@@ -943,6 +961,12 @@ __global__ void __launch_bounds__(128, 10) k_upsample_color(const StepDesc* __re
   }
 }
 
+__global__ void __launch_bounds__(128, 10) k_upsample_color(const StepDesc* __restrict__ st,
+                                                             const uint8_t* __restrict__ planes, int w, int h,
+                                                             uint8_t* __restrict__ rgb, float* __restrict__ lin) {
+  upsample_color_body(st, planes, w, h, rgb, lin, blockIdx.x, blockIdx.y, gridDim.y);
+}
+
 int upsample_color(rcg_ctx* ctx, StepDesc* d_step, const uint8_t* d_planes, int w, int h, uint8_t* d_rgb,
                    float* d_lin) {
   // (h + 1) / 2 rows of CTAs: the 4:2:0 path writes two rows per chroma row, and the general path strides over the
@@ -957,9 +981,9 @@ int upsample_color(rcg_ctx* ctx, StepDesc* d_step, const uint8_t* d_planes, int 
 // First kernel of every search step: the bisection state names the quality; fill the candidate's tables. 192
 // threads: one per (component, coefficient) entry; the Rdo median is the element of rank 31 among q[1..63] (ties
 // broken by index, which leaves the value unchanged), the same value the reference's sort yields.
-__global__ void __launch_bounds__(192) k_step_tables(const SearchState* __restrict__ ss, StepDesc* __restrict__ st,
-                                                     int w, int h, int16_t* slots, long long slot_stride,
-                                                     const float* pweights) {
+__device__ __forceinline__ void step_tables_body(const SearchState* __restrict__ ss, StepDesc* __restrict__ st,
+                                                 int w, int h, int16_t* slots, long long slot_stride,
+                                                 const float* pweights) {
   __shared__ uint8_t qt[64];
   __shared__ float rq[64];
   __shared__ float median;
@@ -999,11 +1023,72 @@ __global__ void __launch_bounds__(192) k_step_tables(const SearchState* __restri
   if (k == 0) st->lambda[c] = fmul(fmul(0.02f, median), median);  // TRELLIS_KAPPA (jpeg/src/encode.rs:42)
 }
 
+__global__ void __launch_bounds__(192) k_step_tables(const SearchState* __restrict__ ss, StepDesc* __restrict__ st,
+                                                     int w, int h, int16_t* slots, long long slot_stride,
+                                                     const float* pweights) {
+  step_tables_body(ss, st, w, h, slots, slot_stride, pweights);
+}
+
 int step_tables(rcg_ctx* ctx, SearchState* d_search, StepDesc* d_step, int w, int h, int16_t* d_coef_slots,
                 long long slot_stride, const float* d_pweights) {
   RCG_LAUNCH(ctx, "step_tables", k_step_tables, 1, 192, 0, d_search, d_step, w, h, d_coef_slots, slot_stride,
              d_pweights);
   return RCG_OK;
+}
+
+// ------------------------------------------------------------------------------------------------ lockstep batch
+
+// One bisection step of every image of a lockstep batch: the same kernel bodies as one search, each launch over a
+// work-list of every image's CTAs (an image whose search has finished skips through its StepDesc's `active`).
+__global__ void __launch_bounds__(192) k_step_tables_lock(const LockItem* __restrict__ items) {
+  const LockItem& it = items[blockIdx.x];
+  step_tables_body(it.ss, it.st, it.w, it.h, it.slots, it.slot_stride, nullptr);
+}
+
+__device__ __forceinline__ CacheSet lock_caches(const LockItem& it) {
+  CacheSet cs;
+#pragma unroll
+  for (int i = 0; i < 9; i++) cs.p[i] = it.caches[i];
+  return cs;
+}
+
+__global__ void __launch_bounds__(128, 4) k_quantize_lock(const LockItem* __restrict__ items, int n) {
+  const int i = lock_find<&LockItem::q0>(items, n, blockIdx.x);
+  const LockItem& it = items[i];
+  quantize_body(it.st, lock_caches(it), (long long)blockIdx.x - it.q0);
+}
+
+__global__ void __launch_bounds__(288) k_rate_tables_lock(const LockItem* __restrict__ items) {
+  rate_tables_body(items[blockIdx.y].st, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(128, 6) k_trellis_lock(const LockItem* __restrict__ items, int n) {
+  const int i = lock_find<&LockItem::q0>(items, n, blockIdx.x);
+  const LockItem& it = items[i];
+  trellis_body<false>(it.st, lock_caches(it), (long long)blockIdx.x - it.q0);
+}
+
+__global__ void __launch_bounds__(128) k_dequant_idct_lock(const LockItem* __restrict__ items, int n) {
+  const int i = lock_find<&LockItem::q0>(items, n, blockIdx.x);
+  const LockItem& it = items[i];
+  dequant_idct_body(it.st, nullptr, it.planes, (long long)blockIdx.x - it.q0);
+}
+
+__global__ void __launch_bounds__(128, 10) k_upsample_color_lock(const LockItem* __restrict__ items, int n) {
+  const int i = lock_find<&LockItem::u0>(items, n, blockIdx.x);
+  const LockItem& it = items[i];
+  const long long local = (long long)blockIdx.x - it.u0;
+  const unsigned bx = (unsigned)(local % it.ux), by = (unsigned)(local / it.ux);
+  upsample_color_body(it.st, it.planes, it.w, it.h, nullptr, it.dist_pyr, bx, by, (unsigned)it.uy);
+}
+
+void lock_step_codec(rcg_ctx* ctx, const LockItem* d_items, int n, long long q_total, long long u_total) {
+  RCG_LAUNCH(ctx, "step_tables_lock", k_step_tables_lock, n, 192, 0, d_items);
+  RCG_LAUNCH(ctx, "quantize_lock", k_quantize_lock, (unsigned)q_total, 128, 0, d_items, n);
+  RCG_LAUNCH(ctx, "rate_tables_lock", k_rate_tables_lock, dim3(3, n), 288, 0, d_items);
+  RCG_LAUNCH(ctx, "trellis_lock", k_trellis_lock, (unsigned)q_total, 128, 0, d_items, n);
+  RCG_LAUNCH(ctx, "dequant_idct_lock", k_dequant_idct_lock, (unsigned)q_total, 128, 0, d_items, n);
+  RCG_LAUNCH(ctx, "upsample_color_lock", k_upsample_color_lock, (unsigned)u_total, 128, 0, d_items, n);
 }
 
 int codec_upload_lut(const float* lut8) {

@@ -147,6 +147,44 @@ __device__ __forceinline__ void search_record(SearchState* ss, double sv, bool m
   }
 }
 
+// One image of a lockstep batch of searches (capi.cu, rcg_search_batch_lockstep): every bisection step of every
+// image runs as one work-list launch per stage, each CTA finding its image by the first-CTA offsets below.
+struct LockItem {
+  SearchState* ss;
+  StepDesc* st;
+  const float* caches[9];  // FDCT caches of the sampling layouts (as CacheSet)
+  int16_t* slots;          // coefficient slots, one per step
+  long long slot_stride;
+  uint8_t* planes;         // decoded component planes
+  int w, h;
+  float* ref_pyr;          // the reference's linear pyramid
+  float* dist_pyr;         // the candidate's (scale 0 written by the upsampling)
+  double* partials;        // scorer scratch: per-CTA sums, per-scale sums, completion counter, score
+  double* scale_sums;
+  unsigned* counter;
+  double* score;
+  PyramidDesc pd;          // the scorer's CTA layout (bands)
+  long long q0;            // first CTA in the block grids (quantize, trellis, dequantize: 128 blocks a CTA)
+  long long u0;            // first CTA in the upsampling grid (ux x uy CTAs)
+  int ux, uy;
+  long long p0;            // first CTA in the pyramid grid
+  long long t0;            // first CTA in the scorer's grid (pd.total_tiles)
+};
+
+// Last item whose first CTA (field `f` of LockItem) is <= x (n >= 1, the first item's offset 0).
+template <long long LockItem::*f>
+__device__ __forceinline__ int lock_find(const LockItem* __restrict__ items, int n, long long x) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (items[mid].*f <= x)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
 // ------------------------------------------------------------------------------------------------ context
 
 struct KernelTimes {
@@ -179,6 +217,7 @@ struct rcg_ctx {
   std::map<std::string, rcg::DeviceBuffer> bufs;
   float* lut16 = nullptr;  // 65536-entry sRGB->linear table for 16-bit samples (allocated on first use)
   std::vector<rcg_ctx*> workers;  // sub-contexts of rcg_search_batch (own streams and workspaces)
+  std::vector<rcg_ctx*> lock_subs;  // per-image sub-contexts of rcg_search_batch_lockstep (buffers, set-up streams)
   // Pinned host staging for host-buffer calls (grow-only): pageable copies go through the driver's own staging and
   // serialize across threads; these let a worker thread do its memcpy in parallel with other workers' GPU work.
   bool stage_copies = false;  // set on batch worker contexts
@@ -289,6 +328,11 @@ int score_workspace(rcg_ctx* ctx, const PyramidDesc& pd);
 int score_batch(rcg_ctx* ctx, int n, const uint8_t* const* d_refs, const uint8_t* const* d_dists,
                 const uint32_t* widths, const uint32_t* heights, const int* channels, const int* depths,
                 double** d_scores);
+
+// ---- lockstep batch (work-list launches over the LockItems of a batch; totals are the grids' CTA counts)
+void lock_step_codec(rcg_ctx* ctx, const LockItem* d_items, int n, long long q_total, long long u_total);
+void lock_step_score(rcg_ctx* ctx, const LockItem* d_items, int n, long long p_total, long long t_total,
+                     int max_scales);
 
 // ---- codec (codec.cu)
 // Colour conversion + edge padding (jpeg/src/encode.rs:463-477): full-resolution padded Y/Cb/Cr planes.

@@ -863,6 +863,42 @@ __global__ void __launch_bounds__(256) k_ssim2_reduce_batch(const ScoreItem* __r
                    scores + p, nullptr);
 }
 
+// ------------------------------------------------------------------------------------------------ lockstep batch
+
+// The scoring half of one bisection step of every image of a lockstep batch (capi.cu): the candidate pyramids, the
+// tiles and the reductions, each one launch over a work-list of every image's CTAs; an image whose search has
+// finished skips through its StepDesc's `active`.
+__global__ void __launch_bounds__(256, 5) k_pyramid_lock(const LockItem* __restrict__ items, int n) {
+  const int i = lock_find<&LockItem::p0>(items, n, blockIdx.x);
+  const LockItem& it = items[i];
+  if (!it.st->active) return;
+  pyramid_tile(it.pd, it.dist_pyr, (int)((long long)blockIdx.x - it.p0));
+}
+
+__global__ void __launch_bounds__(kTileThreads, 3) k_ssim2_tiles_lock(const LockItem* __restrict__ items, int n) {
+  const int i = lock_find<&LockItem::t0>(items, n, blockIdx.x);
+  const LockItem& it = items[i];
+  if (!it.st->active) return;
+  const int blk = (int)((long long)blockIdx.x - it.t0);
+  int s = 0;
+  while (s + 1 < it.pd.nscales && blk >= it.pd.s[s + 1].tile0) s++;
+  const ScaleDesc sd = it.pd.s[s];
+  ssim2_band(sd, blk - sd.tile0, it.ref_pyr, it.dist_pyr, it.partials + blk, (size_t)it.pd.total_tiles);
+}
+
+__global__ void __launch_bounds__(256) k_ssim2_reduce_lock(const LockItem* __restrict__ items) {
+  const LockItem& it = items[blockIdx.z];
+  if (!it.st->active || (int)blockIdx.x >= it.pd.nscales) return;
+  reduce_scale_sum(it.pd, it.partials, it.scale_sums, it.counter, it.score, it.ss);
+}
+
+void lock_step_score(rcg_ctx* ctx, const LockItem* d_items, int n, long long p_total, long long t_total,
+                     int max_scales) {
+  if (p_total > 0) RCG_LAUNCH(ctx, "pyramid_lock", k_pyramid_lock, (unsigned)p_total, 256, 0, d_items, n);
+  RCG_LAUNCH(ctx, "ssim2_tiles_lock", k_ssim2_tiles_lock, (unsigned)t_total, kTileThreads, kTileSmem, d_items, n);
+  RCG_LAUNCH(ctx, "ssim2_reduce_lock", k_ssim2_reduce_lock, dim3(max_scales, kScoreSums, n), 256, 0, d_items);
+}
+
 int to_linear(rcg_ctx* ctx, const uint8_t* d_img, int w, int h, int channels, int depth, float* d_pyr) {
   const float* lut16 = nullptr;
   if (depth == 16 && channels != 2 && channels != 4) {
@@ -963,6 +999,9 @@ static cudaError_t scorer_constants(int device) {
       cudaSuccess)
     return e;
   if ((e = cudaFuncSetAttribute(k_ssim2_tiles_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kTileSmem)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_ssim2_tiles_lock, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kTileSmem)) != cudaSuccess)
     return e;
   if (device >= 0 && device < 64) g_scorer_ready[device] = true;

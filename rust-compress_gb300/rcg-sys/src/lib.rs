@@ -209,6 +209,10 @@ extern "C" {
         heights: *const u32, channels: *const c_int, targets: *const f64, max_quality: c_int,
         opts: *const RcgEncodeOptions, parallel: c_int, found: *mut RcgFound, coefs: *const *mut i16,
         coefs_len: *const usize, qtables: *const *mut u8) -> c_int;
+    pub fn rcg_search_batch_lockstep(ctx: *mut RcgCtx, n: c_int, srcs: *const *const u8, widths: *const u32,
+        heights: *const u32, channels: *const c_int, targets: *const f64, max_quality: c_int,
+        opts: *const RcgEncodeOptions, found: *mut RcgFound, coefs: *const *mut i16, coefs_len: *const usize,
+        qtables: *const *mut u8) -> c_int;
     pub fn rcg_perceptual_defaults(opts: *mut RcgPerceptualOptions);
     pub fn rcg_perceptual_strength(opts: *const RcgPerceptualOptions, quality: c_int) -> f64;
     pub fn rcg_coef_gradient(ctx: *mut RcgCtx, reference: *const u8, decoded: *const u8, width: u32, height: u32,

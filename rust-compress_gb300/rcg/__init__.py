@@ -291,6 +291,7 @@ def _load():
         "rcg_plan": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, sz, ctypes.POINTER(_PlanResult)]),
         "rcg_plan_device": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, ctypes.POINTER(_PlanResult)]),
         "rcg_search_batch": (i32, [P, i32, P, P, P, P, P, i32, ctypes.POINTER(_Opts), i32, P, P, P, P]),
+        "rcg_search_batch_lockstep": (i32, [P, i32, P, P, P, P, P, i32, ctypes.POINTER(_Opts), P, P, P, P]),
         "rcg_perceptual_defaults": (None, [ctypes.POINTER(_PerceptualOpts)]),
         "rcg_perceptual_strength": (ctypes.c_double, [ctypes.POINTER(_PerceptualOpts), i32]),
         "rcg_coef_gradient": (i32, [P, P, P, u32, u32, i32, ctypes.POINTER(_Layout),
@@ -336,7 +337,7 @@ EXPORTED = (
     "rcg_coef_gradient rcg_perceptual_weights rcg_build_coefs_weighted rcg_search_weighted rcg_search_perceptual "
     "rcg_perceptual_strength rcg_ctx_set_graphs rcg_ctx_graph_stats rcg_ssimulacra2_batch rcg_ssimulacra2_batch_device "
     "rcg_sweep_qualities rcg_ssimulacra2_exact rcg_ctx_set_tie_band rcg_ctx_tie_rescores "
-    "rcg_ctx_set_band_chunks rcg_ctx_band_chunks"
+    "rcg_ctx_set_band_chunks rcg_ctx_band_chunks rcg_search_batch_lockstep"
 ).split()
 
 
@@ -835,8 +836,10 @@ class Context:
         trace = [(int(f.trace_q[i]), float(f.trace_score[i])) for i in range(f.nsteps)]
         return Found(int(f.quality), float(f.score), ci, trace)
 
-    def search_batch(self, images, targets, max_quality=100, opts=None, parallel=0):
-        """Independent searches over many images at once (rcg_search_batch); same results as one search each."""
+    def search_batch(self, images, targets, max_quality=100, opts=None, parallel=0, lockstep=False):
+        """Independent searches over many images at once (rcg_search_batch on `parallel` worker streams, or with
+        lockstep rcg_search_batch_lockstep: every step of every image in one work-list launch per stage); same
+        results as one search each."""
         opts = opts or EncodeOptions()
         n = len(images)
         arrs = [_image(im) for im in images]
@@ -860,8 +863,12 @@ class Context:
         clen = (ctypes.c_size_t * n)(*caps)
         qptr = (ctypes.c_void_p * n)(*[x.ctypes.data for x in qts])
         o = _opts(opts)
-        self._check(_lib.rcg_search_batch(self._ptr, n, srcs, ws, hs, cs, ts, int(max_quality), ctypes.byref(o),
-                                          int(parallel), found, cptr, clen, qptr))
+        if lockstep:
+            self._check(_lib.rcg_search_batch_lockstep(self._ptr, n, srcs, ws, hs, cs, ts, int(max_quality),
+                                                       ctypes.byref(o), found, cptr, clen, qptr))
+        else:
+            self._check(_lib.rcg_search_batch(self._ptr, n, srcs, ws, hs, cs, ts, int(max_quality), ctypes.byref(o),
+                                              int(parallel), found, cptr, clen, qptr))
         out = []
         for i, (a, w, h, c, _) in enumerate(arrs):
             f = found[i]

@@ -135,3 +135,40 @@ def test_batch_at_the_large_end_of_the_image_set(ctx, oracle):
         a, _ = oracle.write_best(w, h, lay, r.coefs.qtables, r.coefs.flat())
         b, _ = oracle.write_best(w, h, lay, qt, coefs)
         assert hashlib.sha256(a).hexdigest() == hashlib.sha256(b).hexdigest()
+
+
+def test_lockstep_batch_matches_individual_searches(ctx):
+    """rcg_search_batch_lockstep (every step of every image in one work-list launch per stage) gives exactly each
+    image's own search result: sizes from tiny to 2 MP, gray, a target the max quality misses, Auto subsampling."""
+    sizes = [(96, 80), (300, 200), (1600, 1200), (17, 33), (1000, 700), (64, 64), (333, 111), (8, 8)]
+    imgs = [synth.image(max(w, 16), max(h, 16), 30 + i, sensor_sigma=2.0)[:h, :w].copy()
+            for i, (w, h) in enumerate(sizes)]
+    imgs[5] = np.ascontiguousarray(imgs[5][:, :, 0])
+    targets = [60.0, 70.0, 80.0, 65.0, 99.5, 55.0, 72.0, 50.0]
+    for sub in (rcg.Subsampling.S420, rcg.Subsampling.Auto):
+        opts = rcg.EncodeOptions(90, sub, True)
+        want = [ctx.find_quality_ssimulacra2(im, t, 100, opts) for im, t in zip(imgs, targets)]
+        for _ in range(3):  # plain launches, then the captured graph, then its replay
+            res = ctx.search_batch(imgs, targets, 100, opts, lockstep=True)
+            for r, f in zip(res, want):
+                assert r.quality == f.quality and r.trace == f.trace, (r.trace, f.trace)
+                assert np.array_equal(r.coefs.flat(), f.coefs.flat())
+
+
+def test_lockstep_batch_near_tie(ctx, oracle):
+    """A target 1e-9 above a candidate's oracle score: the lockstep batch pauses that image, decides it on the exact
+    score and finishes it on the oracle's path while the other images run on."""
+    a = synth.image(512, 512, 0)
+    b = synth.image(320, 240, 4, sensor_sigma=2.0)
+    _, _, _, _, _, trace = oracle.search(a, 70.0, 100, 3, True)
+    assert len(trace) >= 3
+    t = trace[2][1] + 1e-9
+    opts = rcg.EncodeOptions(90, rcg.Subsampling.S420, True)
+    n0 = ctx.tie_rescores()
+    res = ctx.search_batch([a, b], [t, 70.0], 100, opts, lockstep=True)
+    assert ctx.tie_rescores() > n0
+    q, s, coefs, qt, lay, otrace = oracle.search(a, t, 100, 3, True)
+    assert [x[0] for x in res[0].trace] == [x[0] for x in otrace]
+    assert res[0].quality == q and np.array_equal(res[0].coefs.flat(), coefs)
+    f = ctx.find_quality_ssimulacra2(b, 70.0, 100, opts)
+    assert res[1].trace == f.trace and np.array_equal(res[1].coefs.flat(), f.coefs.flat())
