@@ -54,6 +54,22 @@ def _env_rank():
     return replicas.env_rank()
 
 
+def _tile_capture():
+    """Per-launch figures of the scorer's tile kernel on the 12 MP workload, from the committed summary of its ncu
+    capture (profiles/, metric,value rows); None if absent."""
+    path = os.path.join(ROOT, "profiles", "ssim2_tiles_12mp.csv")
+    if not os.path.exists(path):
+        return None
+    out = {}
+    for ln in open(path):
+        k, _, v = ln.strip().partition(",")
+        if k and v and k != "metric":
+            out[k] = float(v)
+    need = ("dram_read_bytes", "dram_write_bytes", "issue_active_pct", "fma_pipe_pct", "alu_pipe_pct", "ffma",
+            "ffma2", "fadd", "fadd2", "fmul", "fmul2")
+    return out if all(k in out for k in need) else None
+
+
 def _peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -585,33 +601,47 @@ def plan_workload(ctx, timed, d_coefs, lay, with_oracle=True, steps=10):
 
 
 def kernel_case(name):
-    """A handful of launches of one workload on the W x H image (for ncu captures of a single kernel)."""
+    """A handful of launches of one workload on the W x H image (for ncu captures of a single kernel). The workload
+    runs once untimed (first-use work: the scorer's band tuning, workspace), then again inside an NVTX range named
+    "profiled", which `ncu --nvtx --nvtx-include profiled/` selects. Step loops run as plain launches."""
     import numpy as np
+    import torch
 
     import rcg
     import rcg.synth as synth
 
     ctx = rcg.Context(0)
+    ctx.set_graphs(False)
     img = synth.image(W, H, SEED, SIGMA)
     ci = ctx.build_coefs(img, rcg.EncodeOptions(70, rcg.Subsampling.S420, True))
-    if name == "plan":
-        for _ in range(2):
-            ctx.plan(ci)
-    elif name == "ssim2_batch":
-        # the W x H pair plus three smaller crops of it, four times over, in one work-list call per repetition
-        dist = ctx.reconstruct(ci)
-        pairs = [(img, dist)] + [(np.ascontiguousarray(img[: H // k, : W // k]),
-                                  np.ascontiguousarray(dist[: H // k, : W // k])) for k in (2, 3, 5)]
-        for _ in range(2):
-            ctx.ssimulacra2_batch(pairs * 4)
-    elif name == "perceptual":
-        # one perceptual search (plain search, FP64 adjoint, pullback, weighted search, two plans)
-        ctx.find_quality_perceptual(img, TARGET, 100, rcg.EncodeOptions(90, rcg.Subsampling.S420, True))
-    else:
-        dist = ctx.reconstruct(ci)
-        for _ in range(2):
-            ctx.ssim(img, dist) if name == "ssim" else ctx.ssimulacra2(img, dist)
-    ctx.synchronize()
+    opts = rcg.EncodeOptions(90, rcg.Subsampling.S420, True)
+    dist = ctx.reconstruct(ci)
+    pairs = [(img, dist)] + [(np.ascontiguousarray(img[: H // k, : W // k]),
+                              np.ascontiguousarray(dist[: H // k, : W // k])) for k in (2, 3, 5)]
+
+    def run(reps):
+        for _ in range(reps):
+            if name == "plan":
+                ctx.plan(ci)
+            elif name == "ssim2_batch":
+                # the W x H pair plus three smaller crops of it, four times over, in one work-list call
+                ctx.ssimulacra2_batch(pairs * 4)
+            elif name == "perceptual":
+                # one perceptual search (plain search, adjoint, pullback, weighted search, two plans)
+                ctx.find_quality_perceptual(img, TARGET, 100, opts)
+            elif name == "search":
+                # one search of the workload: every kernel of the timed step, once per candidate
+                ctx.find_quality_ssimulacra2(img, TARGET, 100, opts)
+            elif name == "ssim":
+                ctx.ssim(img, dist)
+            else:
+                ctx.ssimulacra2(img, dist)
+        ctx.synchronize()
+
+    run(1)
+    torch.cuda.nvtx.range_push("profiled")
+    run(1 if name in ("perceptual", "search") else 2)
+    torch.cuda.nvtx.range_pop()
 
 
 def main():
@@ -625,7 +655,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the many-image batch measurement")
     ap.add_argument("--no-requant", action="store_true", help="skip the JPEG->JPEG search measurement")
     ap.add_argument("--no-perceptual", action="store_true", help="skip the perceptual trellis measurement")
-    ap.add_argument("--kernel-case", choices=["plan", "ssim", "ssim2", "ssim2_batch", "perceptual"], default=None,
+    ap.add_argument("--kernel-case", choices=["plan", "ssim", "ssim2", "ssim2_batch", "perceptual", "search"],
+                    default=None,
                     help="profiling aid: run only a few calls of one workload at --width x --height, print nothing")
     ap.add_argument("--width", type=int, default=W, help="smaller cases for profiling only; the bench line uses 4000")
     ap.add_argument("--height", type=int, default=H)
@@ -731,18 +762,33 @@ def main():
     tile_ms = tiles["ms"] / max(1, tiles["launches"])
     alg_bytes = 6.0 * W * H  # two RGB8 images per score (full-resolution pixels)
     achieved = alg_bytes / (tile_ms / 1000.0) / 1e9
-    # DRAM bytes of one launch at this workload size from an ncu capture of the same kernel (dram__bytes_read.sum +
-    # dram__bytes_write.sum: 384.0 MB + 5.7 MB); None for other sizes.
-    traffic = 389.63e6 if (W, H) == (4000, 3000) else None
+    # DRAM bytes and the compute view of one launch at this workload size, from the committed summary of an ncu
+    # capture of the same kernel and workload (None for other sizes or without the summary).
+    cap = _tile_capture() if (W, H) == (4000, 3000) else None
     roof = {"kernel": "ssim2_tiles", "bound": "hbm", "achieved": achieved, "peak": hbm or 6800.0,
-            "unit": "GB/s", "frac": achieved / (hbm or 6800.0), "traffic": traffic,
-            "traffic_source": "ncu capture of the same kernel and workload (384.0 MB read + 5.7 MB written)",
+            "unit": "GB/s", "frac": achieved / (hbm or 6800.0),
+            "traffic": cap["dram_read_bytes"] + cap["dram_write_bytes"] if cap else None,
             "peak_source": "measured" if hbm else "fallback",
             "avg_launch_ms": tile_ms,
-            "compute_view": {"issue_active_pct": 73.9, "fma_pipe_pct": 53.4, "alu_pipe_pct": 34.6,
-                             "source": "ncu --set full of the same kernel at this workload (profiles/ssim2_tiles_12mp.md)"},
-            "note": "the scorer is FP32-ALU bound (~1 kflop per full-resolution pixel), far below the HBM roof; "
-                    "algorithmic bytes = 6 B per full-resolution pixel (two RGB8 images)"}
+            "note": "the scorer is FP32-ALU bound, far below the HBM roof; algorithmic bytes = 6 B per "
+                    "full-resolution pixel (two RGB8 images)"}
+    if cap:
+        roof["traffic_source"] = (f"ncu capture of the same kernel and workload: {cap['dram_read_bytes'] / 1e6:.1f} MB "
+                                  f"read + {cap['dram_write_bytes'] / 1e6:.1f} MB written per launch")
+        # FP32 roof: flops per launch counted by the capture (FFMA 2, FFMA2 4, FADD/FMUL 1, FADD2/FMUL2 2 per thread
+        # instruction) over the event-timed launch, against 152 SMs x 128 FP32 lanes x 2 flops x the median SM clock
+        # seen while the bench ran.
+        flops = (2 * cap["ffma"] + 4 * cap["ffma2"] + cap["fadd"] + 2 * cap["fadd2"] + cap["fmul"] +
+                 2 * cap["fmul2"])
+        mhz = (clocks or {}).get("sm_mhz") or 2070.0
+        peak_fp32 = 152 * 128 * 2 * mhz * 1e6 / 1e12
+        roof["compute_view"] = {
+            "issue_active_pct": cap["issue_active_pct"], "fma_pipe_pct": cap["fma_pipe_pct"],
+            "alu_pipe_pct": cap["alu_pipe_pct"], "fp32_gflop_per_launch": flops / 1e9,
+            "fp32_tflops": flops / (tile_ms / 1000.0) / 1e12, "fp32_peak_tflops": peak_fp32,
+            "fp32_frac": flops / (tile_ms / 1000.0) / 1e12 / peak_fp32,
+            "fp32_peak_formula": "152 SMs x 128 lanes x 2 flops x median SM clock",
+            "source": "ncu --set full of the same kernel and workload (committed summary)"}
     batch = None
     if rank == 0 and not args.no_batch:
         batch = batch_workload(ctx, torch, perceptual=not args.no_perceptual)
