@@ -377,6 +377,24 @@ def batch_workload(ctx, torch, n=64, parallel=8, steps=2, perceptual=True):
             "returned_meets_target_when_plain_does": all(r.found.score >= t for r, t in zip(res_w, targets)
                                                          if r.plain.score >= t),
             "mean_returned_score_minus_plain": mean([r.found.score - r.plain.score for r in res_w])}
+        # The single-search form: a four-candidate plain probe, the gradient at its best candidate, one weighted
+        # search; its planned sizes against the plain results' above.
+        t0 = time.perf_counter()
+        res_f = [ctx.find_quality_perceptual_fast(im, t, 100, opts)[1] for im, t in zip(imgs, targets)]
+        tf = time.perf_counter() - t0
+
+        def planned(f):
+            p = ctx.plan(f.coefs)
+            return min(p.progressive_bytes, p.baseline_bytes)
+
+        fast_b = [planned(f) for f in res_f]
+        out["perceptual_fast"] = {
+            "searches_per_s": n / tf, "vs_plain_searches_per_s": (n / tf) / out["plain_searches_per_s"],
+            "mean_bytes": mean(fast_b),
+            "vs_plain_pct": round(100.0 * (mean(fast_b) / mean(plain_b) - 1.0), 2),
+            "images_smaller_than_plain": sum(1 for a, b in zip(plain_b, fast_b) if b < a),
+            "meets_target_when_plain_does": all(f.score >= t for f, r, t in zip(res_f, res_w, targets)
+                                                if r.plain.score >= t)}
     return out
 
 
@@ -465,11 +483,19 @@ def perceptual_workload(ctx, img, timed, steps=3):
         return {"per_target_pct": pct, "mean_pct": round(float(np.mean(vals)), 2) if vals else None}
 
     returned = r.perceptual_bytes if r.chose_perceptual else r.plain_bytes
+    # the single-search form on the same image
+    ctx.find_quality_perceptual_fast(img, TARGET, 100, opts, popts)
+    times_f, rf = timed(lambda: ctx.find_quality_perceptual_fast(img, TARGET, 100, opts, popts), steps)
+    ms_f = sum(times_f) / len(times_f)
+    pf = ctx.plan(rf[1].coefs)
 
     return {"workload": "perceptual trellis: 4000x3000 seed 1 sigma 3, target 70, 4:2:0, default options "
                         f"(strength {strength} for plain quality {r.plain.quality}, gamma {popts.gamma}, "
                         f"radius {popts.radius}, FP32 adjoint)",
             "ms_per_perceptual_search": ms, "searches_per_s": 1000.0 / ms,
+            "fast": {"ms_per_search": ms_f, "searches_per_s": 1000.0 / ms_f, "probe_quality": rf[0].quality,
+                     "quality": rf[1].quality, "score": rf[1].score,
+                     "bytes": min(pf.progressive_bytes, pf.baseline_bytes)},
             "plain": {"quality": r.plain.quality, "score": r.plain.score, "bytes": r.plain_bytes},
             "weighted": {"bytes": r.perceptual_bytes},
             "returned": {"quality": r.found.quality, "score": r.found.score, "chose_perceptual": r.chose_perceptual,

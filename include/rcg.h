@@ -277,11 +277,13 @@ int rcg_search_metric(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t
                       double target, int max_quality, const rcg_encode_options* opts, rcg_found* found,
                       int16_t* coefs, size_t coefs_len, uint8_t* qtables);
 
-/* jpeg::decode::parse(data)?.into_coefs() (jpeg/src/decode.rs:397, :540) for sequential Huffman JPEGs (SOF0/SOF1,
- * 8-bit, 1 or 3 components, any sampling, restart intervals, any number of scans): markers on the host, the
- * entropy-coded data decoded on the GPU. Progressive, arithmetic, lossless, hierarchical, 12-bit, RGB-coded and
- * 4-component files answer RCG_UNSUPPORTED (decode them on the host). With coefs == NULL only the header is parsed
- * (info, layout, tables: size the buffer from layout.ncoefs). Metadata segments are not returned. */
+/* jpeg::decode::parse(data)?.into_coefs() (jpeg/src/decode.rs:397, :540) for Huffman JPEGs, sequential (SOF0/SOF1)
+ * and progressive (SOF2), 8-bit, 1 or 3 components, any sampling, restart intervals, any number of scans: markers on
+ * the host, the entropy-coded data decoded on the GPU (sequential, DC-first and AC-first scans by self-synchronizing
+ * spans in parallel, DC refinement one bit per block, AC refinement one thread per restart segment). Arithmetic,
+ * lossless, hierarchical, 12-bit, RGB-coded and 4-component files answer RCG_UNSUPPORTED (decode them on the host).
+ * With coefs == NULL only the header is parsed (info, layout, tables: size the buffer from layout.ncoefs). Metadata
+ * segments are not returned. */
 int rcg_decode_coefs(rcg_ctx* ctx, const uint8_t* jpeg, size_t len, rcg_jpeg_info* info, rcg_coef_layout* layout,
                      rcg_qtables* tables, int16_t* coefs, size_t coefs_len);
 /* As rcg_decode_coefs with the coefficients written to device memory. */
@@ -405,6 +407,18 @@ int rcg_search_perceptual(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint
                           const rcg_perceptual_options* popts, rcg_found* plain, rcg_found* found, uint64_t* sizes,
                           int* chose_perceptual, int16_t* coefs, size_t coefs_len, uint8_t* qtables, float* weights,
                           size_t weights_len);
+
+/* The perceptual search in one full search: the plain bisection's first four candidates only (the maximum quality,
+ * then three bisection steps; `probe`, nullable, receives their trace and, as quality and score, the one scoring closest
+ * to the target), the weights from the gradient at that candidate's decoded image (strength by its quality when
+ * popts->strength_by_quality), then the weighted search, whose result `found`, `coefs` and `qtables` receive. No plain search to compare with and no
+ * plans: the result is the weighted search's whatever its size (popts->keep_smaller does not apply). 12 candidates
+ * against rcg_search_perceptual's 16. */
+int rcg_search_perceptual_fast(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
+                               double target, int max_quality, const rcg_encode_options* opts,
+                               const rcg_perceptual_options* popts, rcg_found* probe, rcg_found* found,
+                               int16_t* coefs, size_t coefs_len, uint8_t* qtables, float* weights,
+                               size_t weights_len);
 
 #ifdef __cplusplus
 }

@@ -1298,9 +1298,9 @@ static int search_prepare(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int 
 // The result of a finished search: Found, and the chosen coefficients and tables to device or host buffers.
 static int search_collect(rcg_ctx* ctx, const SearchRun& run, const SearchState& hs, rcg_found* found,
                           int16_t* d_coefs_out, size_t coefs_len, uint8_t* d_qt_out, int16_t* h_coefs_out,
-                          uint8_t* h_qt_out) {
+                          uint8_t* h_qt_out, bool partial = false) {
   int rc;
-  if (!hs.done) return fail(ctx, RCG_TIMEOUT, "bisection did not finish within the step budget");
+  if (!hs.done && !partial) return fail(ctx, RCG_TIMEOUT, "bisection did not finish within the step budget");
   found->quality = hs.best_q;
   found->score = hs.best_score;
   found->nsteps = 0;
@@ -1332,7 +1332,7 @@ static int search_collect(rcg_ctx* ctx, const SearchRun& run, const SearchState&
 static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int channels, int metric, double target,
                        int max_q, int subsampling, int trellis_on, rcg_found* found, int16_t* d_coefs_out,
                        size_t coefs_len, uint8_t* d_qt_out, int16_t* h_coefs_out, uint8_t* h_qt_out,
-                       const float* d_weights = nullptr) {
+                       const float* d_weights = nullptr, int step_limit = 0) {
   SearchRun run;
   int rc = search_prepare(ctx, d_src, w, h, channels, metric, target, max_q, subsampling, trellis_on, &run);
   if (rc != RCG_OK) return rc;
@@ -1341,8 +1341,10 @@ static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int cha
   SearchState* d_ss = run.d_ss;
   StepDesc* d_st = run.d_st;
   // Every launch below takes pointers into this context's workspace and sizes that follow from the key.
+  // step_limit > 0: only the first steps of the bisection (a probe); the result is the best candidate so far.
+  const int nsteps = step_limit > 0 ? std::min(step_limit, run.max_steps) : run.max_steps;
   const std::vector<long long> key = {1, (long long)(uintptr_t)d_src, w, h, channels, metric, subsampling, trellis_on,
-                                      run.max_steps, (long long)(uintptr_t)d_weights};
+                                      nsteps, (long long)(uintptr_t)d_weights};
   auto issue_step = [&]() {
     step_tables(ctx, d_ss, d_st, w, h, run.slots, es.max_coefs, d_weights);
     quantize(ctx, d_st, es.caches, es.max_blocks);
@@ -1352,13 +1354,26 @@ static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int cha
     score_candidate(ctx, sc, d_st, run.planes, w, h, channels, d_ss);
   };
   rc = run_step_loop(ctx, key, [&]() {
-    for (int s = 0; s < run.max_steps; s++) issue_step();
+    for (int s = 0; s < nsteps; s++) issue_step();
   });
   if (rc != RCG_OK) return rc;
   SearchState hs;
   cudaMemcpyAsync(&hs, d_ss, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream);
   if ((rc = finish(ctx, "search")) != RCG_OK) return rc;
-  if ((rc = settle_ties(ctx, sc, d_ss, &hs, run.max_steps, w, h, issue_step)) != RCG_OK) return rc;
+  if ((rc = settle_ties(ctx, sc, d_ss, &hs, nsteps, w, h, issue_step)) != RCG_OK) return rc;
+  if (nsteps < run.max_steps && !hs.done) {
+    // A probe: the evaluated candidates only (not the next one the bisection has chosen), and as its result the
+    // candidate whose score is closest to the target, from either side.
+    SearchState pr = hs;
+    pr.step = hs.step - 1;
+    int pick = 0;
+    for (int s = 1; s <= pr.step; s++)
+      if (std::fabs(hs.scores[s] - target) < std::fabs(hs.scores[pick] - target)) pick = s;
+    pr.best_step = pick;
+    pr.best_q = hs.qs[pick];
+    pr.best_score = hs.scores[pick];
+    return search_collect(ctx, run, pr, found, d_coefs_out, coefs_len, d_qt_out, h_coefs_out, h_qt_out, true);
+  }
   return search_collect(ctx, run, hs, found, d_coefs_out, coefs_len, d_qt_out, h_coefs_out, h_qt_out);
 }
 
@@ -2105,6 +2120,11 @@ static int planned_bytes(rcg_ctx* ctx, const StepDesc* lay, int w, int h, const 
   return RCG_OK;
 }
 
+// Candidates of the fast form's probe: the maximum quality and three bisection steps. Measured on the 64-image set
+// (planned bytes of the weighted result against the plain search's): 3 -> -0.20%, 4 -> -0.74%, 5 -> -0.82%, the full
+// plain search -1.32%.
+constexpr int kPerceptualProbeSteps = 4;
+
 int rcg_search_perceptual(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
                           double target, int max_quality, const rcg_encode_options* opts,
                           const rcg_perceptual_options* popts, rcg_found* plain, rcg_found* found, uint64_t* sizes,
@@ -2172,6 +2192,66 @@ int rcg_search_perceptual(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint
   if (qtables) qtables_for(found->quality, qtables);
   if (weights && (rc = copy_to_host(ctx, weights, d_w, (size_t)ncoefs * sizeof(float))) != RCG_OK) return rc;
   return finish(ctx, "perceptual search");
+}
+
+int rcg_search_perceptual_fast(rcg_ctx* ctx, const uint8_t* src, uint32_t width, uint32_t height, int channels,
+                               double target, int max_quality, const rcg_encode_options* opts,
+                               const rcg_perceptual_options* popts, rcg_found* probe, rcg_found* found,
+                               int16_t* coefs, size_t coefs_len, uint8_t* qtables, float* weights,
+                               size_t weights_len) {
+  if (!ctx) return RCG_INVALID;
+  long long ncoefs = 0;
+  int rc = weighted_search_checks(ctx, src, width, height, channels, target, opts, found, &ncoefs);
+  if (rc != RCG_OK) return rc;
+  PerceptualParams p;
+  if ((rc = check_popts(ctx, popts, &p)) != RCG_OK) return rc;
+  if (weights && (long long)weights_len < ncoefs) return fail(ctx, RCG_INVALID, "weights buffer too short");
+  if (coefs && (long long)coefs_len < ncoefs) return fail(ctx, RCG_INVALID, "coefficient buffer too short");
+  const int w = (int)width, h = (int)height;
+  const int max_q = std::max(1, std::min(max_quality, 100));
+  cudaSetDevice(ctx->device);
+  const size_t npx = (size_t)w * h;
+  uint8_t* d_src = (uint8_t*)workspace(ctx, "img_src", npx * channels);
+  int16_t* d_probe = (int16_t*)workspace(ctx, "perc_plain_coefs", (size_t)ncoefs * 2);
+  int16_t* d_perc = (int16_t*)workspace(ctx, "perc_coefs", (size_t)ncoefs * 2);
+  float* d_w = (float*)workspace(ctx, "perc_weights", (size_t)ncoefs * sizeof(float));
+  uint8_t* d_dec = (uint8_t*)workspace(ctx, "perc_dec", npx * channels);
+  StepDesc* d_st = (StepDesc*)workspace(ctx, "perc_step", sizeof(StepDesc));
+  if (!d_src || !d_probe || !d_perc || !d_w || !d_dec || !d_st) return RCG_NO_MEMORY;
+  if ((rc = copy_to_device(ctx, d_src, src, npx * channels)) != RCG_OK) return rc;
+  // 1. the plain bisection's first kPerceptualProbeSteps candidates; the one scoring closest to the target stands in
+  //    for the result (which lies within the 6 qualities the bisection has left after four steps from 1..100)
+  rcg_found pr;
+  rc = search_impl(ctx, d_src, w, h, channels, RCG_METRIC_SSIMULACRA2, target, max_q, opts->subsampling,
+                   opts->trellis, &pr, d_probe, (size_t)ncoefs, nullptr, nullptr, nullptr, nullptr,
+                   kPerceptualProbeSteps);
+  if (rc != RCG_OK) return rc;
+  if (probe) *probe = pr;
+  // 2. the gradient at that candidate's decode, the weights with the strength its quality selects
+  p.strength = rcg_perceptual_strength(popts, pr.quality);
+  StepDesc* st = new StepDesc;
+  host_step_tables(st, pr.quality, opts->subsampling, channels, opts->trellis, w, h);
+  uint8_t* planes = (uint8_t*)workspace(ctx, "perc_planes", (size_t)plane_bytes(st));
+  if (!planes) {
+    delete st;
+    return RCG_NO_MEMORY;
+  }
+  cudaMemcpyAsync(d_st, st, sizeof(StepDesc), cudaMemcpyHostToDevice, ctx->stream);
+  dequant_idct(ctx, d_st, d_probe, planes, st->nblocks);
+  upsample_color(ctx, d_st, planes, w, h, d_dec, nullptr);
+  double gscore = 0.0;
+  rc = perceptual_impl(ctx, d_src, d_dec, w, h, channels, st, p, &gscore, nullptr, d_w);
+  cudaStreamSynchronize(ctx->stream);  // the host StepDesc must outlive its upload
+  delete st;
+  if (rc != RCG_OK) return rc;
+  // 3. one weighted search
+  rc = search_impl(ctx, d_src, w, h, channels, RCG_METRIC_SSIMULACRA2, target, max_q, opts->subsampling,
+                   opts->trellis, found, d_perc, (size_t)ncoefs, nullptr, nullptr, nullptr, d_w);
+  if (rc != RCG_OK) return rc;
+  if (coefs && (rc = copy_to_host(ctx, coefs, d_perc, (size_t)ncoefs * 2)) != RCG_OK) return rc;
+  if (qtables) qtables_for(found->quality, qtables);
+  if (weights && (rc = copy_to_host(ctx, weights, d_w, (size_t)ncoefs * sizeof(float))) != RCG_OK) return rc;
+  return finish(ctx, "fast perceptual search");
 }
 
 }  // extern "C"

@@ -575,69 +575,130 @@ __global__ void __launch_bounds__(256) k_dc_refine(const ScanDesc* __restrict__ 
   blk[0] = (int16_t)(blk[0] | (int16_t)(bit << sd.al));
 }
 
+// Reads n (0..64) bits MSB first into the low bits of a 64-bit value.
+__device__ __forceinline__ uint64_t read_bits64(Reader& r, int n) {
+  uint64_t v = 0;
+  while (n > 0) {
+    const int k = n > 24 ? 24 : n;
+    v = (v << k) | r.bits(k);
+    n -= k;
+  }
+  return v;
+}
+
+// Correction bits (decode.rs:1571-1575, :1590-1595) for the already-nonzero coefficients at the set positions of
+// `corr`, in ascending order, one bit each: a set bit with the al bit of the magnitude still clear moves the
+// coefficient away from zero by 2^al.
+__device__ __forceinline__ void refine_corrections(Reader& r, int16_t* c, uint64_t corr, int16_t p1, int16_t m1) {
+  int nb = __popcll(corr);
+  while (nb > 0) {
+    const int take = nb > 32 ? 32 : nb;
+    const uint64_t bits = read_bits64(r, take);
+    for (int j = take - 1; j >= 0; j--) {
+      const int pos = __ffsll((long long)corr) - 1;
+      corr &= corr - 1;
+      const int16_t v = c[pos];
+      if (((bits >> j) & 1) && (v & p1) == 0) c[pos] = (int16_t)(v + (v >= 0 ? p1 : m1));
+    }
+    nb -= take;
+  }
+}
+
 // AC refinement (decode.rs:1549-1601, decode_ac_refine), one thread per restart segment, its blocks in order: the
-// bits a block reads depend on which of its coefficients earlier scans made nonzero.
-__global__ void k_ac_refine(const ScanDesc* __restrict__ sdp, const Tables* __restrict__ tg,
-                            const Segment* __restrict__ segs, const uint8_t* __restrict__ data,
-                            int16_t* __restrict__ out, int* __restrict__ error) {
+// bits a block reads depend on which of its coefficients earlier scans made nonzero. Each block's 64 coefficients
+// come in once (eight 16-byte loads, the next block's issued before this one is decoded) to a per-thread row of
+// shared memory with a 64-bit mask of the nonzero ones; a run of zero-history coefficients and the correction bits
+// of the nonzero ones inside it are then one mask operation and one multi-bit read each, instead of a step per
+// coefficient. Same bits read, same values as the reference's loop.
+constexpr int kRefineThreads = 32;
+
+__global__ void __launch_bounds__(kRefineThreads) k_ac_refine(const ScanDesc* __restrict__ sdp,
+                                                              const Tables* __restrict__ tg,
+                                                              const Segment* __restrict__ segs,
+                                                              const uint8_t* __restrict__ data,
+                                                              int16_t* __restrict__ out, int* __restrict__ error) {
   __shared__ __align__(16) Tables tb;
   __shared__ ScanDesc sd;
+  __shared__ __align__(16) int16_t rows[kRefineThreads][64];
   if (threadIdx.x == 0) sd = *sdp;
   load_tables(tb, tg);
   const int16_t p1 = (int16_t)(1 << sd.al), m1 = (int16_t)(-(1 << sd.al));
+  const int ss = sd.ss, se = sd.se;
+  const uint64_t band = (se >= 63 ? ~0ull : ((1ull << (se + 1)) - 1)) & ~((1ull << ss) - 1);
+  int16_t* c = rows[threadIdx.x];
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < sd.nseg; s += gridDim.x * blockDim.x) {
     const Segment& sg = segs[s];
     const DevHuff& ac = tb.ac[sd.ac[0]];
     Reader r;
     r.init(data, sg.byte0, sg.nbytes, 0);
     uint32_t eobrun = 0;
+    int4 nxt[8];
+    if (sg.nblocks > 0) {
+      const int4* src = reinterpret_cast<const int4*>(scan_block(sd, out, sg.block0));
+#pragma unroll
+      for (int g = 0; g < 8; g++) nxt[g] = src[g];
+    }
     for (long long b = 0; b < sg.nblocks; b++) {
       int16_t* blk = scan_block(sd, out, sg.block0 + b);
-      int k = sd.ss;
+      int4* crow = reinterpret_cast<int4*>(c);
+      uint64_t mask = 0;
+#pragma unroll
+      for (int g = 0; g < 8; g++) {
+        crow[g] = nxt[g];
+        const uint32_t wv[4] = {(uint32_t)nxt[g].x, (uint32_t)nxt[g].y, (uint32_t)nxt[g].z, (uint32_t)nxt[g].w};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          if (wv[q] & 0xFFFFu) mask |= 1ull << (g * 8 + 2 * q);
+          if (wv[q] >> 16) mask |= 1ull << (g * 8 + 2 * q + 1);
+        }
+      }
+      if (b + 1 < sg.nblocks) {
+        const int4* src = reinterpret_cast<const int4*>(scan_block(sd, out, sg.block0 + b + 1));
+#pragma unroll
+        for (int g = 0; g < 8; g++) nxt[g] = src[g];
+      }
+      const uint64_t hist = mask & band;  // coefficients earlier scans made nonzero, inside the band
+      int k = ss;
       if (eobrun == 0) {
-        while (k <= sd.se) {
+        while (k <= se) {
           const int rs = huff_decode(ac, r);
           if (rs < 0) {
             atomicCAS(error, 0, 1);
             return;
           }
-          int run = rs >> 4;
-          const int sz = rs & 15;
+          const int run = rs >> 4, sz = rs & 15;
           int16_t value = 0;
           if (sz != 0) {
             value = r.bits(1) ? p1 : m1;
           } else if (run != 15) {
-            eobrun = 1u << run;
-            if (run > 0) eobrun += r.bits(run);
+            eobrun = (1u << run) + (run > 0 ? r.bits(run) : 0u);
             break;
           }
-          // skip over already-nonzero coefficients (refining them) and `run` zero ones
-          while (k <= sd.se) {
-            const int16_t c = blk[k];
-            if (c != 0) {
-              if (r.bits(1) && (c & p1) == 0) blk[k] = (int16_t)(c + (c >= 0 ? p1 : m1));
-            } else {
-              if (--run < 0) break;
-            }
-            k++;
-          }
+          // Skip `run` zero-history coefficients (and refine the nonzero ones among them): stop at the next
+          // zero-history one after them, or past the band.
+          uint64_t zeros = ~mask & band & (~0ull << k);
+          for (int i = 0; i < run && zeros; i++) zeros &= zeros - 1;
+          const int t = zeros ? __ffsll((long long)zeros) - 1 : se + 1;
+          const uint64_t below = t >= 64 ? ~0ull : ((1ull << t) - 1);
+          refine_corrections(r, c, hist & below & (~0ull << k), p1, m1);
+          k = t;
           if (value != 0) {
             if (k > 63) {
               atomicCAS(error, 0, 1);
               return;
             }
-            blk[k] = value;
+            c[k] = value;
           }
           k++;
         }
       }
       if (eobrun > 0) {
-        for (; k <= sd.se; k++) {
-          const int16_t c = blk[k];
-          if (c != 0 && r.bits(1) && (c & p1) == 0) blk[k] = (int16_t)(c + (c >= 0 ? p1 : m1));
-        }
+        if (k <= se) refine_corrections(r, c, hist & (~0ull << k), p1, m1);
         eobrun--;
       }
+      int4* dst = reinterpret_cast<int4*>(blk);
+#pragma unroll
+      for (int g = 0; g < 8; g++) dst[g] = crow[g];
     }
   }
 }
@@ -961,7 +1022,10 @@ int jpeg_decode(rcg_ctx* ctx, const uint8_t* data, size_t len, rcg_jpeg_info* in
   if (!coefs) return RCG_OK;
   if ((long long)coefs_len < nblocks * 64) return fail(ctx, RCG_INVALID, "coefficient buffer too short");
   cudaSetDevice(ctx->device);
-  int16_t* d_out = coefs_on_device ? coefs : (int16_t*)workspace(ctx, "dec_coefs", (size_t)nblocks * 128);
+  // The kernels move whole blocks with 16-byte accesses: a caller buffer that is not 16-byte aligned gets the
+  // coefficients through the context's own buffer and one device copy.
+  const bool direct = coefs_on_device && ((uintptr_t)coefs & 15) == 0;
+  int16_t* d_out = direct ? coefs : (int16_t*)workspace(ctx, "dec_coefs", (size_t)nblocks * 128);
   int* d_err = (int*)workspace(ctx, "dec_error", sizeof(int) * 4);
   ScanDesc* d_sd = (ScanDesc*)workspace(ctx, "dec_scan", sizeof(ScanDesc));
   Tables* d_tab = (Tables*)workspace(ctx, "dec_tables", sizeof(Tables));
@@ -999,8 +1063,8 @@ int jpeg_decode(rcg_ctx* ctx, const uint8_t* data, size_t len, rcg_jpeg_info* in
       continue;
     }
     if (sc.sd.kind == kAcRefine) {
-      RCG_LAUNCH(ctx, "ac_refine", k_ac_refine, (unsigned)((sc.sd.nseg + 31) / 32), 32, 0, d_sd, d_tab, d_segs,
-                 d_bytes, d_out, d_err);
+      RCG_LAUNCH(ctx, "ac_refine", k_ac_refine, (unsigned)((sc.sd.nseg + kRefineThreads - 1) / kRefineThreads),
+                 kRefineThreads, 0, d_sd, d_tab, d_segs, d_bytes, d_out, d_err);
       continue;
     }
     // Initial guesses: every span starts at its first bit, first block of the MCU, at a block's first coefficient.
@@ -1055,6 +1119,10 @@ int jpeg_decode(rcg_ctx* ctx, const uint8_t* data, size_t len, rcg_jpeg_info* in
   if (h_err) return fail(ctx, RCG_INVALID, h_err == 1 ? "bad JPEG entropy-coded data" : "JPEG decode lost its place");
   if (info) info->sync_rounds = fell_back ? -1 : rounds_max;
   if (!coefs_on_device) return copy_to_host(ctx, coefs, d_out, (size_t)nblocks * 128);
+  if (!direct) {
+    e = cudaMemcpyAsync(coefs, d_out, (size_t)nblocks * 128, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "JPEG decode output copy");
+  }
   return RCG_OK;
 }
 

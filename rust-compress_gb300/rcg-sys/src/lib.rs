@@ -230,4 +230,8 @@ extern "C" {
         target: f64, max_quality: c_int, opts: *const RcgEncodeOptions, popts: *const RcgPerceptualOptions,
         plain: *mut RcgFound, found: *mut RcgFound, sizes: *mut u64, chose_perceptual: *mut c_int, coefs: *mut i16,
         coefs_len: usize, qtables: *mut u8, weights: *mut f32, weights_len: usize) -> c_int;
+    pub fn rcg_search_perceptual_fast(ctx: *mut RcgCtx, src: *const u8, width: u32, height: u32, channels: c_int,
+        target: f64, max_quality: c_int, opts: *const RcgEncodeOptions, popts: *const RcgPerceptualOptions,
+        probe: *mut RcgFound, found: *mut RcgFound, coefs: *mut i16, coefs_len: usize, qtables: *mut u8,
+        weights: *mut f32, weights_len: usize) -> c_int;
 }

@@ -304,6 +304,9 @@ def _load():
         "rcg_search_perceptual": (i32, [P, P, u32, u32, i32, ctypes.c_double, i32, ctypes.POINTER(_Opts),
                                         ctypes.POINTER(_PerceptualOpts), ctypes.POINTER(_Found),
                                         ctypes.POINTER(_Found), P, ctypes.POINTER(ctypes.c_int), P, sz, P, P, sz]),
+        "rcg_search_perceptual_fast": (i32, [P, P, u32, u32, i32, ctypes.c_double, i32, ctypes.POINTER(_Opts),
+                                             ctypes.POINTER(_PerceptualOpts), ctypes.POINTER(_Found),
+                                             ctypes.POINTER(_Found), P, sz, P, P, sz]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -337,7 +340,7 @@ EXPORTED = (
     "rcg_coef_gradient rcg_perceptual_weights rcg_build_coefs_weighted rcg_search_weighted rcg_search_perceptual "
     "rcg_perceptual_strength rcg_ctx_set_graphs rcg_ctx_graph_stats rcg_ssimulacra2_batch rcg_ssimulacra2_batch_device "
     "rcg_sweep_qualities rcg_ssimulacra2_exact rcg_ctx_set_tie_band rcg_ctx_tie_rescores "
-    "rcg_ctx_set_band_chunks rcg_ctx_band_chunks rcg_search_batch_lockstep"
+    "rcg_ctx_set_band_chunks rcg_ctx_band_chunks rcg_search_batch_lockstep rcg_search_perceptual_fast"
 ).split()
 
 
@@ -696,6 +699,29 @@ class Context:
 
         return PerceptualFound(found(fp, None), found(ff, _coef_image(w, h, lay, coefs, qt)), int(sizes[0]),
                                int(sizes[1]), bool(chose.value), wts)
+
+    def find_quality_perceptual_fast(self, reference, target, max_quality=100, opts=None, popts=None):
+        """rcg_search_perceptual_fast: a four-candidate plain probe, the gradient at its best candidate, one
+        weighted search. Returns (probe Found without coefficients, weighted Found, weights)."""
+        opts = opts or EncodeOptions()
+        popts = popts or PerceptualOptions()
+        a, w, h, c, d = _image(reference)
+        lay = self.coef_layout(w, h, c, EncodeOptions(50, opts.subsampling, opts.trellis))
+        coefs = np.zeros(lay.ncoefs, dtype=np.int16)
+        wts = np.zeros(lay.ncoefs, dtype=np.float32)
+        qt = np.zeros((2, 64), dtype=np.uint8)
+        fp, ff = _Found(), _Found()
+        o, po = _opts(opts), popts._c()
+        self._check(_lib.rcg_search_perceptual_fast(self._ptr, a.ctypes.data, w, h, c, float(target),
+                                                    int(max_quality), ctypes.byref(o), ctypes.byref(po),
+                                                    ctypes.byref(fp), ctypes.byref(ff), coefs.ctypes.data, coefs.size,
+                                                    qt.ctypes.data, wts.ctypes.data, wts.size))
+
+        def found(f, ci):
+            return Found(int(f.quality), float(f.score), ci,
+                         [(int(f.trace_q[i]), float(f.trace_score[i])) for i in range(f.nsteps)])
+
+        return found(fp, None), found(ff, _coef_image(w, h, lay, coefs, qt)), wts
 
     def reconstruct(self, ci):
         """jpeg/src/decode.rs:334: the pixels a viewer would show (Gray (h, w) or Rgb (h, w, 3) uint8)."""

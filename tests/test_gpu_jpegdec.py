@@ -213,3 +213,21 @@ def test_device_resident_jpeg_to_jpeg_chain(ctx, oracle):
     torch.cuda.synchronize()
     assert np.array_equal(out.cpu().numpy(), f.coefs.flat())
     assert ctx.plan_device(w, h, lay, out.data_ptr()) == ctx.plan(f.coefs)
+
+
+def test_decode_progressive_to_device_any_alignment(ctx, oracle):
+    """rcg_decode_coefs_device into aligned and unaligned device buffers gives the oracle's coefficients."""
+    import torch
+
+    img = synth.image(200, 150, 78, sensor_sigma=2.0)
+    coefs, qt, lay = oracle.build_coefs(img, 80, 3, True)
+    data = oracle.emit_script(200, 150, lay, qt, coefs, oracle.script_count(3) - 1)
+    g, _ = oracle.decode_huffman(data)
+    n = g.coefs.size
+    buf = torch.zeros(n + 8, dtype=torch.int16, device="cuda")
+    for off in (0, 1, 3):  # int16 offsets: 0, 2 and 6 bytes past a 256-byte boundary
+        buf.zero_()
+        ctx.decode_coefs_device(data, buf.data_ptr() + 2 * off, n)
+        torch.cuda.synchronize()
+        got = buf[off: off + n].cpu().numpy()
+        assert np.array_equal(got, g.coefs), off

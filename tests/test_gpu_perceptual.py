@@ -205,3 +205,30 @@ def test_perceptual_search_other_layouts(ctx, oracle, c, sub):
     assert r.chose_perceptual == (r.perceptual_bytes <= r.plain_bytes)
     assert r.found.quality == (weighted.quality if r.chose_perceptual else r.plain.quality)
     assert r.found.score >= 65.0
+
+
+def test_fast_perceptual_search(ctx, oracle):
+    """rcg_search_perceptual_fast: its probe is the plain bisection's first four candidates, its weights those of
+    the gradient at the probe candidate scoring closest to the target, and its result the weighted search with those
+    weights (and the oracle's weighted search)."""
+    img = synth.image(640, 480, 95, sensor_sigma=3.0)
+    sub = rcg.Subsampling.S420
+    opts = rcg.EncodeOptions(90, sub, True)
+    popts = rcg.PerceptualOptions()
+    probe, res, wts = ctx.find_quality_perceptual_fast(img, 70.0, 100, opts, popts)
+    plain = ctx.find_quality_ssimulacra2(img, 70.0, 100, opts)
+    assert probe.trace == plain.trace[:4]
+    closest = min(probe.trace, key=lambda qs: abs(qs[1] - 70.0))
+    assert (probe.quality, probe.score) == closest
+    ci = ctx.build_coefs(img, rcg.EncodeOptions(probe.quality, sub, True))
+    lay = ctx.coef_layout(640, 480, 3, rcg.EncodeOptions(50, sub, True))
+    po = rcg.PerceptualOptions()
+    po.strength = popts.strength_for(probe.quality)
+    _, want_w = ctx.perceptual_weights(img, ctx.reconstruct(ci), lay, po)
+    assert np.array_equal(wts, want_w)
+    f = ctx.find_quality_weighted(img, 70.0, wts, 100, opts)
+    assert (res.quality, res.trace) == (f.quality, f.trace)
+    assert np.array_equal(res.coefs.flat(), f.coefs.flat())
+    q, s, coefs, qt, olay, trace = oracle.search(img, 70.0, 100, int(sub), True, weights=wts)
+    assert res.quality == q and np.array_equal(res.coefs.flat(), coefs)
+    assert res.score >= 70.0 or res.quality == 100
