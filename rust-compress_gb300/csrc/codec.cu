@@ -478,7 +478,11 @@ int rate_tables(rcg_ctx* ctx, StepDesc* d_step) {
 // own position, so no 64-entry zd table is needed.
 // kWeighted: the perceptual mode. Each coefficient's distortion weight becomes rw[k] * pweights[block][k] (one f32
 // product, then the same squared-error product as the plain weight); the plain instantiation reads no weights.
-// 6 CTAs per SM (80 registers, no spill) instead of 5.
+// 8 CTAs per SM (64 registers; the weighted instantiation spills 8 bytes and is still faster, 20.9 against 24.1 us
+// per candidate of a 3 MP perceptual search). The DP is latency-bound (one block's positions are serial); measured per
+// 12 MP candidate: 16-coefficient chunks at 6 CTAs per SM 75.6 us, 8-coefficient chunks at 8 CTAs 72.1 us. A rolled
+// DP loop over cp.async-staged shared-memory coefficients, (cost, zd) node pairs and an unrolled node scan were all
+// slower or no faster (80-92, 74.2 and 72.3-76.6 us).
 template <bool kWeighted>
 __device__ __forceinline__ void trellis_body(StepDesc* __restrict__ st, const CacheSet& cs, long long bx) {
   // The per-position tables of every component and the lambda*rate tables of the components this CTA's blocks
@@ -522,8 +526,8 @@ __device__ __forceinline__ void trellis_body(StepDesc* __restrict__ st, const Ca
   int dc = 0;
   float zprev = 0.0f;  // zd[i-1]
 
-  // The coefficients arrive 16 at a time: the next chunk's loads are in flight while this chunk's DP steps run.
-  constexpr int kChunk = 16;
+  // The coefficients arrive 8 at a time: the next chunk's loads are in flight while this chunk's DP steps run.
+  constexpr int kChunk = 8;
   auto load = [&](int k) -> float {
     return requant ? (float)__ldg(src + k) : __ldg(cache + (long long)k * nb);
   };
@@ -642,7 +646,7 @@ __device__ __forceinline__ void trellis_body(StepDesc* __restrict__ st, const Ca
 }
 
 template <bool kWeighted>
-__global__ void __launch_bounds__(128, 6) k_trellis(StepDesc* __restrict__ st, CacheSet cs) {
+__global__ void __launch_bounds__(128, 8) k_trellis(StepDesc* __restrict__ st, CacheSet cs) {
   trellis_body<kWeighted>(st, cs, blockIdx.x);
 }
 
@@ -1062,7 +1066,7 @@ __global__ void __launch_bounds__(288) k_rate_tables_lock(const LockItem* __rest
   rate_tables_body(items[blockIdx.y].st, blockIdx.x);
 }
 
-__global__ void __launch_bounds__(128, 6) k_trellis_lock(const LockItem* __restrict__ items, int n) {
+__global__ void __launch_bounds__(128, 8) k_trellis_lock(const LockItem* __restrict__ items, int n) {
   const int i = lock_find<&LockItem::q0>(items, n, blockIdx.x);
   const LockItem& it = items[i];
   trellis_body<false>(it.st, lock_caches(it), (long long)blockIdx.x - it.q0);
