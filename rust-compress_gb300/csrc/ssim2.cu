@@ -18,8 +18,9 @@
 //     that equal the reference's expressions algebraically but keep full relative precision for similar images;
 //   * cube roots: 2^(log2(x) / 3) from the hardware's approximate log2 and exp2 (relative error a few 1e-7; the
 //     differences between the two images never go through them, only through the identity below);
-//   * sums: f32 over the 4 pixels of a thread, f32 across a warp, f64 from there on, in a fixed order
-//     (bit-reproducible from run to run, as the reference's test :630 requires).
+//   * sums: f32 over the 4 pixels of a thread (in registers, then added to the thread's running sums of its band),
+//     f32 across a warp, f64 from there on, in a fixed order (bit-reproducible from run to run, as the reference's
+//     test :630 requires).
 // Identical images give exactly 100: every difference term is exactly 0, so every map value is exactly 0.
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -201,6 +202,11 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
   float sums[kScoreSums];
 #pragma unroll
   for (int i = 0; i < kScoreSums; i++) sums[i] = 0.0f;
+  // The blur's six distinct taps as (k, k) pairs, held in registers for the packed FMAs (the taps are symmetric:
+  // tap t and tap 2 kRadius - t are the same f32 value).
+  float2 g2[kRadius + 1];
+#pragma unroll
+  for (int t = 0; t <= kRadius; t++) g2[t] = make_float2(c_gauss[t], c_gauss[t]);
 
   const int col = tid & 31, rg = tid >> 5;  // vertical pass: column, group of 4 output rows
   const int gx = x0 + col;
@@ -327,11 +333,10 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
           float sdd = 0.f;
 #pragma unroll
           for (int t = 0; t < 2 * kRadius + 1; t++) {
-            float k = c_gauss[t];
-            float2 kk = make_float2(k, k);
+            const float2 kk = g2[t <= kRadius ? t : 2 * kRadius - t];
             s01 = __ffma2_rn(kk, vad[o + t], s01);
             s23 = __ffma2_rn(kk, vsq[o + t], s23);
-            sdd = fmaf(k, vdd[o + t], sdd);
+            sdd = fmaf(kk.x, vdd[o + t], sdd);
           }
           m01[o] = s01;
           m23[o] = s23;
@@ -369,11 +374,10 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
           float a4 = 0.f;
 #pragma unroll
           for (int t = 0; t < 2 * kRadius + 1; t++) {
-            float k = c_gauss[t];
-            float2 kk = make_float2(k, k);
+            const float2 kk = g2[t <= kRadius ? t : 2 * kRadius - t];
             a01 = __ffma2_rn(kk, v01[o + t], a01);
             a23 = __ffma2_rn(kk, v23[o + t], a23);
-            a4 = fmaf(k, v4[o + t], a4);
+            a4 = fmaf(kk.x, v4[o + t], a4);
           }
           mu[0][o] = a01.x;
           mu[1][o] = a01.y;
@@ -383,6 +387,7 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
         }
       }
       const float ca = s_oa[ch], cd = s_od[ch], cbv = ca - cd;
+      float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
       for (int o = 0; o < 4; o++) {
         int ry = rg * 4 + o;
@@ -419,14 +424,16 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
           float d1 = t > 0.0f ? __fdividef(-rd * (2.0f * r1 - rd), t * (1.0f + fabsf(r1))) : 0.0f;
           float art = fmaxf(d1, 0.0f), det = fmaxf(-d1, 0.0f);
           float d2 = d * d, a2 = art * art, e2 = det * det;
-          sums[ch * 6 + 0] += d;
-          sums[ch * 6 + 1] += d2 * d2;
-          sums[ch * 6 + 2] += art;
-          sums[ch * 6 + 3] += a2 * a2;
-          sums[ch * 6 + 4] += det;
-          sums[ch * 6 + 5] += e2 * e2;
+          acc[0] += d;
+          acc[1] += d2 * d2;
+          acc[2] += art;
+          acc[3] += a2 * a2;
+          acc[4] += det;
+          acc[5] += e2 * e2;
         }
       }
+#pragma unroll
+      for (int i = 0; i < 6; i++) sums[ch * 6 + i] += acc[i];
     }
   }
   // Warp sums (f32, 32 threads x 4 pixels), then the 8 warps in f64 in a fixed order. Sums 0..15 by a reduce-scatter
@@ -508,7 +515,8 @@ __device__ __forceinline__ void reduce_scale_sum(const PyramidDesc& pd, const do
   if (!last) return;
   __threadfence();
   // The last CTA maps the per-scale sums to the score. Term t follows the reference's weight order: channel, scale,
-  // norm (mean, 4-norm), then (ssim, artifact, detail) (core/src/ssimulacra2.rs:491-506); one thread per term.
+  // norm (mean, 4-norm), then (ssim, artifact, detail) (core/src/ssimulacra2.rs:491-506); one thread per term, then
+  // the terms summed by a fixed pairwise tree (18.4 against 20.5 us per launch for the serial sum).
   __shared__ double terms[3 * kMaxScales * 6];
   const volatile double* vs = scale_sums;
   const int ns = pd.nscales, nterms = 3 * ns * 6, t = threadIdx.x;
@@ -520,10 +528,14 @@ __device__ __forceinline__ void reduce_scale_sum(const PyramidDesc& pd, const do
     terms[t] = c_weights[t] * fabs(v);
   }
   __syncthreads();
+  // Fixed-order pairwise sum of the terms (deterministic; the same tree on every call).
+  for (int span = 1; span < nterms; span *= 2) {
+    if (t % (2 * span) == 0 && t + span < nterms) terms[t] += terms[t + span];
+    __syncthreads();
+  }
   if (t != 0) return;
   *counter = 0;
-  double ssim = 0.0;
-  for (int i = 0; i < nterms; i++) ssim += terms[i];
+  double ssim = terms[0];
   ssim *= 0.9562382616834844;
   ssim = 2.326765642916932 * ssim - 0.020884521182843837 * ssim * ssim + 6.248496625763138e-05 * ssim * ssim * ssim;
   double score = ssim > 0.0 ? 100.0 - 10.0 * pow(ssim, 0.6276336467831387) : 100.0;
@@ -664,48 +676,70 @@ __device__ __forceinline__ float mean2x2(const float* p, int stride, int w, int 
 constexpr int kPyrTile = 32;
 constexpr int kPyrThreads = 256;  // every pyramid launch
 
-// Scale-1 tile (tx, ty) from scale 0 into `out` (shared) and dst1 (global). Full 2x2 blocks (all but the last odd
-// column/row) load their four samples at once and sum them in mean2x2's order; partial blocks take the general path.
-// Source and destination are separate restricted pointers, so the loads of later outputs may be issued before the
-// stores of earlier ones.
+// Scale-1 tile (tx, ty) from scale 0 into `out` (shared) and dst1 (global). Each thread takes pairs of adjacent
+// outputs, whose 2x4 source samples per channel are two aligned 16-byte loads when the scale-0 rows are (width a
+// multiple of 4, planes 16-byte aligned; the usual case); each output sums its four samples in mean2x2's order.
+// Partial blocks (the last odd column or row) and unaligned planes take the general path. Source and destination
+// are separate restricted pointers, so the loads of later outputs may be issued before the stores of earlier ones.
+__device__ __forceinline__ float quad_mean(float q0, float q1, float q2, float q3) {
+  float e0, e1, e2;
+  float t = two_sum(q0, q1, e0);  // 0 + q0 is exact, so this matches mean2x2's first steps
+  t = two_sum(t, q2, e1);
+  t = two_sum(t, q3, e2);
+  return __fadd_rn(t, (e0 + e1) + e2) * 0.25f;
+}
+
 __device__ __forceinline__ void scale1_tile(const float* __restrict__ src0, float* __restrict__ dst1,
                                             const ScaleDesc& s0, const ScaleDesc& s1, int tx, int ty,
                                             float (*out)[kPyrTile][kPyrTile + 1]) {
   const size_t np0 = (size_t)s0.w * s0.h, np1 = (size_t)s1.w * s1.h;
+  const bool vec = (s0.w & 3) == 0 && ((uintptr_t)src0 & 15) == 0;
 #pragma unroll
-  for (int k = 0; k < kPyrTile * kPyrTile / kPyrThreads; k++) {
+  for (int k = 0; k < kPyrTile * kPyrTile / (2 * kPyrThreads); k++) {
     const int i = threadIdx.x + k * kPyrThreads;
-    int lx = i % kPyrTile, ly = i / kPyrTile;
-    int ox = tx * kPyrTile + lx, oy = ty * kPyrTile + ly;
-    if (ox < s1.w && oy < s1.h) {
-      const bool full = 2 * ox + 1 < s0.w && 2 * oy + 1 < s0.h;
-      float v[3];
-      if (full) {
-        float q[3][4];
+    const int lx = 2 * (i % (kPyrTile / 2)), ly = i / (kPyrTile / 2);
+    const int ox = tx * kPyrTile + lx, oy = ty * kPyrTile + ly;
+    if (ox >= s1.w || oy >= s1.h) continue;
+    float v[2][3];
+    const bool two = ox + 1 < s1.w;
+    if (vec && 2 * ox + 3 < s0.w && 2 * oy + 1 < s0.h) {
+      float4 r0[3], r1[3];
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-          const float* p = src0 + c * np0 + (size_t)(2 * oy) * s0.w + 2 * ox;
-          q[c][0] = p[0];
-          q[c][1] = p[1];
-          q[c][2] = p[s0.w];
-          q[c][3] = p[s0.w + 1];
-        }
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          float e0, e1, e2;
-          float t = two_sum(q[c][0], q[c][1], e0);  // 0 + q0 is exact, so this matches mean2x2's first steps
-          t = two_sum(t, q[c][2], e1);
-          t = two_sum(t, q[c][3], e2);
-          v[c] = __fadd_rn(t, (e0 + e1) + e2) * 0.25f;
-        }
-      } else {
-#pragma unroll
-        for (int c = 0; c < 3; c++) v[c] = mean2x2(src0 + c * np0, s0.w, s0.w, s0.h, ox, oy);
+      for (int c = 0; c < 3; c++) {
+        const float4* p = reinterpret_cast<const float4*>(src0 + c * np0 + (size_t)(2 * oy) * s0.w + 2 * ox);
+        r0[c] = p[0];
+        r1[c] = p[s0.w / 4];
       }
 #pragma unroll
       for (int c = 0; c < 3; c++) {
-        out[c][ly][lx] = v[c];
-        dst1[c * np1 + (size_t)oy * s1.w + ox] = v[c];
+        v[0][c] = quad_mean(r0[c].x, r0[c].y, r1[c].x, r1[c].y);
+        v[1][c] = quad_mean(r0[c].z, r0[c].w, r1[c].z, r1[c].w);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        const int x = ox + j;
+        if (j == 1 && !two) break;
+        const bool full = 2 * x + 1 < s0.w && 2 * oy + 1 < s0.h;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          if (full) {
+            const float* p = src0 + c * np0 + (size_t)(2 * oy) * s0.w + 2 * x;
+            v[j][c] = quad_mean(p[0], p[1], p[s0.w], p[s0.w + 1]);
+          } else {
+            v[j][c] = mean2x2(src0 + c * np0, s0.w, s0.w, s0.h, x, oy);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      out[c][ly][lx] = v[0][c];
+      float* d = dst1 + c * np1 + (size_t)oy * s1.w + ox;
+      d[0] = v[0][c];
+      if (two) {
+        out[c][ly][lx + 1] = v[1][c];
+        d[1] = v[1][c];
       }
     }
   }
@@ -985,6 +1019,7 @@ static cudaError_t scorer_constants(int device) {
     k[i] = std::exp(-0.5 / (1.5 * 1.5) * x * x);
     sum += k[i];
   }
+  // Taps i and 2 kRadius - i have the same x * x, hence the same f32 value: the tile kernel holds six distinct taps.
   float kf[2 * kRadius + 1];
   for (int i = 0; i < 2 * kRadius + 1; i++) kf[i] = (float)(k[i] / sum);
   float lut[256];
