@@ -627,7 +627,15 @@ uint64_t rcg_ctx_tie_rescores(const rcg_ctx* ctx) { return ctx ? ctx->tie_rescor
 int rcg_ctx_set_band_chunks(rcg_ctx* ctx, int chunks) {
   if (!ctx) return RCG_INVALID;
   if (chunks < 0 || chunks > 64) return fail(ctx, RCG_INVALID, "band chunks must be 0 (autotune) or 1..64");
+  if (chunks != ctx->band_chunks) drop_graphs(ctx);  // captured step loops hold the old band layout
   ctx->band_chunks = chunks;
+  return RCG_OK;
+}
+
+int rcg_ctx_set_ref_cache(rcg_ctx* ctx, int on) {
+  if (!ctx) return RCG_INVALID;
+  if ((on != 0) != ctx->ref_cache) drop_graphs(ctx);  // captured step loops hold the old scorer launches
+  ctx->ref_cache = on != 0;
   return RCG_OK;
 }
 
@@ -1175,6 +1183,7 @@ struct SearchScorer {
   PyramidDesc pd;
   float* ref_pyr = nullptr;
   float* dist_pyr = nullptr;
+  float2* ref_moments = nullptr;  // the reference's blurred a', a'^2 per pyramid pixel (null: the cache is off)
   const uint8_t* ref_px = nullptr;
   uint8_t* cand_px = nullptr;
   double* d_score = nullptr;
@@ -1197,12 +1206,18 @@ static int scorer_setup(rcg_ctx* ctx, int metric, int w, int h, int channels, Se
   sc->ref_pyr = (float*)workspace(ctx, "ref_pyr", (size_t)sc->pd.floats * sizeof(float));
   sc->dist_pyr = (float*)workspace(ctx, "dist_pyr", (size_t)sc->pd.floats * sizeof(float));
   if (!sc->ref_pyr || !sc->dist_pyr) return RCG_NO_MEMORY;
+  if (ctx->ref_cache) {
+    // Sized for the band layout the scorer will run (the same plan_bands call score_pyramids makes).
+    sc->ref_moments = (float2*)workspace(ctx, "ref_moments", ref_moment_bytes(plan_bands(ctx, sc->pd)));
+    if (!sc->ref_moments) return RCG_NO_MEMORY;
+  }
   return score_workspace(ctx, sc->pd);
 }
 
-// Decoded planes of one candidate -> score -> one bisection step (all gated by the step's `active`).
+// Decoded planes of one candidate -> score -> one bisection step (all gated by the step's `active`). Step `s` of the
+// loop: the first candidate of a search (s = 0, always active) stores the reference moments, later ones read them.
 static void score_candidate(rcg_ctx* ctx, const SearchScorer& sc, StepDesc* d_st, const uint8_t* planes, int w,
-                            int h, int channels, SearchState* d_ss) {
+                            int h, int channels, SearchState* d_ss, int s) {
   if (sc.metric == RCG_METRIC_SSIM) {
     upsample_color(ctx, d_st, planes, w, h, sc.cand_px, nullptr);
     ssim_score(ctx, sc.ref_px, sc.cand_px, w, h, channels, sc.d_score, d_ss, d_st);
@@ -1210,7 +1225,8 @@ static void score_candidate(rcg_ctx* ctx, const SearchScorer& sc, StepDesc* d_st
   }
   upsample_color(ctx, d_st, planes, w, h, nullptr, sc.dist_pyr);
   build_pyramid_gated(ctx, sc.pd, sc.dist_pyr, d_st);
-  score_pyramids(ctx, sc.pd, sc.ref_pyr, sc.dist_pyr, sc.d_score, d_ss, d_st);
+  score_pyramids(ctx, sc.pd, sc.ref_pyr, sc.dist_pyr, sc.d_score, d_ss, d_st, sc.ref_moments,
+                 s == 0 ? kRefWrite : kRefRead);
 }
 
 // Near ties. jpeg/src/target.rs:48 accepts a candidate on s >= target; the fast scorer is within about 1e-6 of the
@@ -1218,9 +1234,9 @@ static void score_candidate(rcg_ctx* ctx, const SearchScorer& sc, StepDesc* d_st
 // done = 2) with its decoded linear planes still at scale 0 of the candidate pyramid (every later step was
 // inactive). Here it is rescored in the reference's f64 arithmetic and order on the GPU (exact_score), the bisection
 // records that score and goes on, and the remaining steps run as plain launches; repeated while a later candidate
-// pauses again. `issue_step` issues one bisection step's kernels.
+// pauses again. `issue_step(s)` issues step s's kernels.
 static int settle_ties(rcg_ctx* ctx, const SearchScorer& sc, SearchState* d_ss, SearchState* hs, int max_steps,
-                       int w, int h, const std::function<void()>& issue_step) {
+                       int w, int h, const std::function<void(int)>& issue_step) {
   while (hs->done == 2) {
     if (sc.metric != RCG_METRIC_SSIMULACRA2) return fail(ctx, RCG_INVALID, "paused search without a rescorer");
     double* d_exact = (double*)workspace(ctx, "x_score", sizeof(double), false);
@@ -1229,7 +1245,7 @@ static int settle_ties(rcg_ctx* ctx, const SearchScorer& sc, SearchState* d_ss, 
     if (rc != RCG_OK) return rc;
     search_resume(ctx, d_ss, d_exact);
     ctx->tie_rescores++;
-    for (int s = hs->step + 1; s < max_steps; s++) issue_step();
+    for (int s = hs->step + 1; s < max_steps; s++) issue_step(s);
     cudaMemcpyAsync(hs, d_ss, sizeof *hs, cudaMemcpyDeviceToHost, ctx->stream);
     if ((rc = finish(ctx, "search after a near tie")) != RCG_OK) return rc;
   }
@@ -1345,16 +1361,16 @@ static int search_impl(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int cha
   const int nsteps = step_limit > 0 ? std::min(step_limit, run.max_steps) : run.max_steps;
   const std::vector<long long> key = {1, (long long)(uintptr_t)d_src, w, h, channels, metric, subsampling, trellis_on,
                                       nsteps, (long long)(uintptr_t)d_weights};
-  auto issue_step = [&]() {
+  auto issue_step = [&](int s) {
     step_tables(ctx, d_ss, d_st, w, h, run.slots, es.max_coefs, d_weights);
     quantize(ctx, d_st, es.caches, es.max_blocks);
     rate_tables(ctx, d_st);
     trellis(ctx, d_st, es.caches, es.max_blocks, d_weights != nullptr);
     dequant_idct(ctx, d_st, nullptr, run.planes, es.max_blocks);
-    score_candidate(ctx, sc, d_st, run.planes, w, h, channels, d_ss);
+    score_candidate(ctx, sc, d_st, run.planes, w, h, channels, d_ss, s);
   };
   rc = run_step_loop(ctx, key, [&]() {
-    for (int s = 0; s < nsteps; s++) issue_step();
+    for (int s = 0; s < nsteps; s++) issue_step(s);
   });
   if (rc != RCG_OK) return rc;
   SearchState hs;
@@ -1532,6 +1548,7 @@ int rcg_search_batch_lockstep(rcg_ctx* ctx, int n, const uint8_t* const* srcs, c
     rcg_ctx* sub = ctx->lock_subs[(size_t)i];
     sub->tie_band = ctx->tie_band;
     sub->band_chunks = ctx->band_chunks;
+    sub->ref_cache = false;  // the work-list tile kernel computes every moment (no store to allocate)
     const size_t bytes = (size_t)widths[i] * heights[i] * channels[i];
     uint8_t* d_src = (uint8_t*)workspace(sub, "img_src", bytes);
     int r = d_src ? RCG_OK : RCG_NO_MEMORY;
@@ -1770,16 +1787,16 @@ static int search_requantize_impl(rcg_ctx* ctx, uint32_t width, uint32_t height,
     const CompDesc& cd = st->comp[c];
     key.insert(key.end(), {cd.bw, cd.bh, cd.h, cd.v, cd.blk0, cd.plane_off});
   }
-  auto issue_step = [&]() {
+  auto issue_step = [&](int s) {
     step_tables_requant(ctx, d_ss, d_st, slots, nblocks * 64);
     requantize_plain(ctx, d_st, nblocks);
     rate_tables(ctx, d_st);
     rcg::trellis(ctx, d_st, no_caches, nblocks);
     dequant_idct(ctx, d_st, nullptr, planes, nblocks);
-    score_candidate(ctx, sc, d_st, planes, w, h, channels, d_ss);
+    score_candidate(ctx, sc, d_st, planes, w, h, channels, d_ss, s);
   };
   rc = run_step_loop(ctx, key, [&]() {
-    for (int s = 0; s < max_steps; s++) issue_step();
+    for (int s = 0; s < max_steps; s++) issue_step(s);
   });
   if (rc != RCG_OK) {
     delete st;

@@ -34,6 +34,7 @@ struct ScaleDesc {
   int tiles_x, tiles_y;  // CTAs across and down (32-column bands of nch chunks of 32 rows; nch = 1: 32x32 tiles)
   int tile0;        // first CTA of this scale in the multi-scale launch
   int nch;          // 32-row chunks per CTA (ssim2.cu, ssim2_band)
+  int chunk0;       // first 32x32 chunk of this scale (CTA-major, nch per CTA) in chunk-indexed buffers
   long long off;    // float offset of channel 0 of this scale
 };
 
@@ -42,6 +43,7 @@ struct PyramidDesc {
   int total_tiles;
   ScaleDesc s[kMaxScales];
   long long floats;  // total floats of one image's pyramid
+  int total_chunks;  // chunks of every CTA of every scale (total_tiles x nch, per scale)
 };
 
 // One JPEG component of the current candidate, as the device kernels see it.
@@ -247,6 +249,8 @@ struct rcg_ctx {
   uint64_t tie_rescores = 0;
   // Scorer bands: 0 autotunes the chunks per band per size class (ssim2.cu, band_chunks); >= 1 fixes them.
   int band_chunks = 0;
+  // The searches' reference moments (kRefWrite at the first candidate, kRefRead after): on by default.
+  bool ref_cache = true;
 };
 
 namespace rcg {
@@ -304,10 +308,17 @@ int to_linear(rcg_ctx* ctx, const uint8_t* d_img, int w, int h, int channels, in
 int build_pyramid(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr);
 // The same, skipped on the device when the search step is inactive.
 int build_pyramid_gated(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, const StepDesc* st);
+// Reference moments of the tile kernel: kRefNone computes every blurred moment; kRefWrite also stores the
+// reference-only ones (blur a', blur a'^2) for later candidates against the same reference; kRefRead reads them
+// instead of blurring them. Same scores in every mode. The store is chunk-major: per 32x32 chunk of the banded
+// layout the scorer runs (plan_bands), kRefChunk float2 as [channel][row][column], ref_moment_bytes() in all.
+constexpr int kRefChunk = 3 * kTileH * kTileW;
+constexpr int kRefNone = 0, kRefWrite = 1, kRefRead = 2;
 // Score: per-tile sums of every scale, then the final mapping. `d_score` receives the score (f64); when
-// `search` is non-null the final kernel also advances the device-side bisection.
+// `search` is non-null the final kernel also advances the device-side bisection. `refm`/`ref_mode`: the reference
+// moments (nullptr / kRefNone: none).
 int score_pyramids(rcg_ctx* ctx, const PyramidDesc& pd, const float* d_ref, const float* d_dist, double* d_score,
-                   SearchState* search, StepDesc* step);
+                   SearchState* search, StepDesc* step, float2* refm = nullptr, int ref_mode = kRefNone);
 // The reference-order FP64 score (exact.cu) of two images given as scale-0 linear planes ([3][h][w] f32, as
 // to_linear writes them): to d_score (NaN for the reference's non-finite Err), queued on the context stream.
 int exact_score(rcg_ctx* ctx, const float* d_ref0, const float* d_dist0, int w, int h, double* d_score);
@@ -321,6 +332,10 @@ PyramidDesc plan_bands(rcg_ctx* ctx, const PyramidDesc& pd);
 // Chunks per band for a pyramid of this geometry: the context's fixed choice, or the process-wide autotuned one for
 // its size class (tuned on first use by timing the candidates; small images always take 1).
 int band_chunks(rcg_ctx* ctx, const PyramidDesc& pd);
+// Bytes of the reference-moment store for a banded layout.
+inline size_t ref_moment_bytes(const PyramidDesc& banded_pd) {
+  return (size_t)banded_pd.total_chunks * kRefChunk * 8;
+}
 // Allocate (or find) the scratch score_pyramids uses for a pyramid of this geometry.
 int score_workspace(rcg_ctx* ctx, const PyramidDesc& pd);
 // Score n device-resident pairs (checked sizes and formats; depths nullable = 8) with the work-list kernels;

@@ -146,9 +146,22 @@ constexpr size_t kTileSmem = (size_t)(6 * kIH * kIW + 5 * kIH * kTileW) * sizeof
 // are re-offset by the change (one f32 subtraction each). With nch = 1 the band is exactly the single tile.
 // Band `local` of scale `sd` (sd.tiles_x bands across; sd.nch chunks each) of a pyramid pair; the band's 18 sums go to
 // out[i * stride], i < 18.
+// Reference moments (kRef). The offsets a chunk subtracts come from the reference alone (its XYB at the chunk
+// centre), so the blurred a' and a'^2 of every output pixel depend on the reference and the band layout only. A
+// search scores every candidate against one reference: its first candidate runs kRef = kRefWrite, which also stores
+// (blur a', blur a'^2) per output pixel and channel; the later ones run kRef = kRefRead, which blur only (d', b'^2)
+// as a packed pair and d'^2, and read the other two. Each blurred moment is the same chain of per-lane fmaf in every
+// mode, so the scores are bit-identical to kRefNone. The store keeps each chunk's 3 x 32 x 32 pairs contiguous
+// (24 KB, [channel][row][column]); a reading CTA asks for the whole block in L2 with one bulk prefetch per channel
+// as the chunk starts and reads it in its vertical pass. Measured per 12 MP score: 651.5 us without the store,
+// 680.0 us writing it, 608.9 us reading it (603 us with the two moments left out altogether); with the store
+// indexed like the pyramid planes and no bulk prefetch the read mode took 645 us, and staging each channel's block
+// in shared memory with cp.async 629 us.
+
+template <int kRef>
 __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, const float* __restrict__ ref,
                                            const float* __restrict__ dist, double* __restrict__ out,
-                                           const size_t stride) {
+                                           const size_t stride, float2* __restrict__ refm) {
   extern __shared__ float smem[];
   float2* xs = reinterpret_cast<float2*>(smem);  // [3][kIH][kIW] pairs (a', d') per channel
   float* hb = smem + 6 * kIH * kIW;              // pair planes (m0, m1), (m2, m3) then m4, [kIH][kTileW] each
@@ -279,6 +292,17 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
       __syncthreads();
     }
     float oa[3] = {s_oa[0], s_oa[1], s_oa[2]}, od[3] = {s_od[0], s_od[1], s_od[2]};
+    // This chunk's block of reference moments (kRefChunk float2).
+    float2* rchunk = nullptr;
+    if constexpr (kRef != kRefNone) rchunk = refm + (size_t)(sd.chunk0 + local * nch + chunk) * kRefChunk;
+    if constexpr (kRef == kRefRead) {
+      // Into L2 while this chunk's XYB and horizontal passes run: 8 KB per channel (16-byte aligned, as the bulk
+      // prefetch requires: blocks are 24 KB apart from an aligned base).
+      if (tid < 3) {
+        const float2* p = rchunk + tid * kTileH * kTileW;
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(kTileH * kTileW * 8) : "memory");
+      }
+    }
 
     // XYB of the chunk's new rows; the six plane values of the next pixel are loaded before the current one is
     // converted, so the global loads overlap the arithmetic. Two halo pixels per trip: the measured best unroll.
@@ -315,6 +339,39 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
         const int r = (hw >> 1) * 4 + (j >> 2), p = (j & 3) + 4 * (hw & 1);
         if (r >= kIH) continue;
         const float2* xr = X + r * kIW + kHx * p;
+        if constexpr (kRef == kRefRead) {
+          // (d', b'^2) pairs and d'^2; the first plane of hb holds (blur d', blur b'^2).
+          float2 vdb[kHx + 2 * kRadius];
+          float vdd[kHx + 2 * kRadius];
+#pragma unroll
+          for (int t = 0; t < kHx + 2 * kRadius; t++) {
+            const float2 ad = xr[t];
+            const float bb = __fsub_rn(ad.x, ad.y);
+            vdb[t] = make_float2(ad.y, __fmul_rn(bb, bb));
+            vdd[t] = __fmul_rn(ad.y, ad.y);
+          }
+          float2 m13[kHx];
+          float m4[kHx];
+#pragma unroll
+          for (int o = 0; o < kHx; o++) {
+            float2 s13 = make_float2(0.f, 0.f);
+            float sdd = 0.f;
+#pragma unroll
+            for (int t = 0; t < 2 * kRadius + 1; t++) {
+              const float2 kk = g2[t <= kRadius ? t : 2 * kRadius - t];
+              s13 = __ffma2_rn(kk, vdb[o + t], s13);
+              sdd = fmaf(kk.x, vdd[o + t], sdd);
+            }
+            m13[o] = s13;
+            m4[o] = sdd;
+          }
+          float* h13 = hb + (r * kTileW + kHx * p) * 2;
+          float* h4 = hb + 4 * kIH * kTileW + r * kTileW + kHx * p;
+          reinterpret_cast<float4*>(h13)[0] = make_float4(m13[0].x, m13[0].y, m13[1].x, m13[1].y);
+          reinterpret_cast<float4*>(h13)[1] = make_float4(m13[2].x, m13[2].y, m13[3].x, m13[3].y);
+          *reinterpret_cast<float4*>(h4) = make_float4(m4[0], m4[1], m4[2], m4[3]);
+          continue;
+        }
         float2 vad[kHx + 2 * kRadius], vsq[kHx + 2 * kRadius];
         float vdd[kHx + 2 * kRadius];
 #pragma unroll
@@ -355,7 +412,42 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
       __syncthreads();
       // Vertical pass + error maps: 4 output rows of one column per thread, the same pairs packed.
       float mu[5][4];
-      {
+      float2* rrow = nullptr;  // this thread's row 0 in the chunk's block
+      if constexpr (kRef != kRefNone) rrow = rchunk + (ch * kTileH + rg * 4) * kTileW + col;
+      if constexpr (kRef == kRefRead) {
+        // The reference moments first (their loads overlap the blur), then (blur d', blur b'^2) and blur d'^2.
+#pragma unroll
+        for (int o = 0; o < 4; o++) {
+          float2 rm = make_float2(0.f, 0.f);
+          if (gx < w && y0 + rg * 4 + o < h) rm = __ldg(rrow + o * kTileW);
+          mu[0][o] = rm.x;
+          mu[2][o] = rm.y;
+        }
+        const float2* h13 = reinterpret_cast<const float2*>(hb);
+        const float* h4 = hb + 4 * kIH * kTileW;
+        float2 v13[4 + 2 * kRadius];
+        float v4[4 + 2 * kRadius];
+#pragma unroll
+        for (int t = 0; t < 4 + 2 * kRadius; t++) {
+          const int i = (rg * 4 + t) * kTileW + col;
+          v13[t] = h13[i];
+          v4[t] = h4[i];
+        }
+#pragma unroll
+        for (int o = 0; o < 4; o++) {
+          float2 a13 = make_float2(0.f, 0.f);
+          float a4 = 0.f;
+#pragma unroll
+          for (int t = 0; t < 2 * kRadius + 1; t++) {
+            const float2 kk = g2[t <= kRadius ? t : 2 * kRadius - t];
+            a13 = __ffma2_rn(kk, v13[o + t], a13);
+            a4 = fmaf(kk.x, v4[o + t], a4);
+          }
+          mu[1][o] = a13.x;
+          mu[3][o] = a13.y;
+          mu[4][o] = a4;
+        }
+      } else {
         const float2* h01 = reinterpret_cast<const float2*>(hb);
         const float2* h23 = reinterpret_cast<const float2*>(hb) + kIH * kTileW;
         const float* h4 = hb + 4 * kIH * kTileW;
@@ -384,6 +476,9 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
           mu[2][o] = a23.x;
           mu[3][o] = a23.y;
           mu[4][o] = a4;
+          if constexpr (kRef == kRefWrite) {
+            if (gx < w && y0 + rg * 4 + o < h) rrow[o * kTileW] = make_float2(a01.x, a23.x);
+          }
         }
       }
       const float ca = s_oa[ch], cd = s_od[ch], cbv = ca - cd;
@@ -474,15 +569,16 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
   }
 }
 
+template <int kRef>
 __global__ void __launch_bounds__(kTileThreads, 3)
     k_ssim2_tiles(PyramidDesc pd, const float* __restrict__ ref, const float* __restrict__ dist,
-                  double* __restrict__ partials, const StepDesc* __restrict__ st) {
+                  double* __restrict__ partials, const StepDesc* __restrict__ st, float2* __restrict__ refm) {
   if (st && !st->active) return;
   const int blk = blockIdx.x;
   int s = 0;
   while (s + 1 < pd.nscales && blk >= pd.s[s + 1].tile0) s++;
   const ScaleDesc sd = pd.s[s];
-  ssim2_band(sd, blk - sd.tile0, ref, dist, partials + blk, (size_t)pd.total_tiles);
+  ssim2_band<kRef>(sd, blk - sd.tile0, ref, dist, partials + blk, (size_t)pd.total_tiles, refm);
 }
 
 // Deterministic reduction of the per-tile sums: CTA (scale, sum index); the last CTA to finish computes the score
@@ -881,7 +977,7 @@ __global__ void __launch_bounds__(kTileThreads, 3)
   sd.nch = sg.nch;
   sd.off = 0;
   const int local = (int)(t - __ldg(seg0 + g));
-  ssim2_band(sd, local, sg.ref, sg.dist, sg.out + local, (size_t)sg.stride);
+  ssim2_band<kRefNone>(sd, local, sg.ref, sg.dist, sg.out + local, (size_t)sg.stride, nullptr);
 }
 
 // CTA (scale, sum, pair); scale_sums [n][kMaxScales][18], counters and scores [n].
@@ -917,7 +1013,8 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_ssim2_tiles_lock(const Lock
   int s = 0;
   while (s + 1 < it.pd.nscales && blk >= it.pd.s[s + 1].tile0) s++;
   const ScaleDesc sd = it.pd.s[s];
-  ssim2_band(sd, blk - sd.tile0, it.ref_pyr, it.dist_pyr, it.partials + blk, (size_t)it.pd.total_tiles);
+  ssim2_band<kRefNone>(sd, blk - sd.tile0, it.ref_pyr, it.dist_pyr, it.partials + blk, (size_t)it.pd.total_tiles,
+                       nullptr);
 }
 
 __global__ void __launch_bounds__(256) k_ssim2_reduce_lock(const LockItem* __restrict__ items) {
@@ -970,6 +1067,7 @@ PyramidDesc make_pyramid(int w, int h) {
     sd.tiles_y = (h + kTileH - 1) / kTileH;
     sd.tile0 = tiles;
     sd.nch = 1;
+    sd.chunk0 = tiles;
     sd.off = off;
     tiles += sd.tiles_x * sd.tiles_y;
     off += 3LL * w * h;
@@ -978,6 +1076,7 @@ PyramidDesc make_pyramid(int w, int h) {
     h = (h + 1) / 2;
   }
   pd.total_tiles = tiles;
+  pd.total_chunks = tiles;
   pd.floats = off;
   return pd;
 }
@@ -1030,8 +1129,12 @@ static cudaError_t scorer_constants(int device) {
   if ((e = cudaMemcpyToSymbol(c_lut8s, lut, sizeof lut)) != cudaSuccess) return e;
   if ((e = cudaMemcpyToSymbol(c_weights, W, sizeof c_weights)) != cudaSuccess) return e;
   if (int ce = codec_upload_lut(lut)) return (cudaError_t)ce;
-  if ((e = cudaFuncSetAttribute(k_ssim2_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem)) !=
-      cudaSuccess)
+  if ((e = cudaFuncSetAttribute(k_ssim2_tiles<kRefNone>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kTileSmem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_ssim2_tiles<kRefWrite>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kTileSmem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_ssim2_tiles<kRefRead>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kTileSmem)) != cudaSuccess)
     return e;
   if ((e = cudaFuncSetAttribute(k_ssim2_tiles_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kTileSmem)) != cudaSuccess)
@@ -1059,7 +1162,7 @@ constexpr int kBandCandidates[] = {1, 2, 4, 8};
 
 PyramidDesc banded(const PyramidDesc& pd, int nch0, int min_tiles) {
   PyramidDesc b = pd;
-  int total = 0;
+  int total = 0, chunks = 0;
   for (int s = 0; s < pd.nscales; s++) {
     ScaleDesc& sd = b.s[s];
     const int tiles = pd.s[s].tiles_x * pd.s[s].tiles_y;
@@ -1067,9 +1170,12 @@ PyramidDesc banded(const PyramidDesc& pd, int nch0, int min_tiles) {
     sd.nch = n;
     sd.tiles_y = (pd.s[s].tiles_y + n - 1) / n;
     sd.tile0 = total;
+    sd.chunk0 = chunks;
     total += sd.tiles_x * sd.tiles_y;
+    chunks += sd.tiles_x * sd.tiles_y * n;
   }
   b.total_tiles = total;
+  b.total_chunks = chunks;
   return b;
 }
 
@@ -1116,8 +1222,8 @@ static int tune_bands(rcg_ctx* ctx, const PyramidDesc& pd) {
     float t = 1e30f;
     for (int rep = 0; rep < 4; rep++) {
       cudaEventRecord(a, ctx->stream);
-      k_ssim2_tiles<<<pb.total_tiles, kTileThreads, kTileSmem, ctx->stream>>>(pb, pyr, pyr + pd.floats, part,
-                                                                              nullptr);
+      k_ssim2_tiles<kRefNone><<<pb.total_tiles, kTileThreads, kTileSmem, ctx->stream>>>(pb, pyr, pyr + pd.floats,
+                                                                                        part, nullptr, nullptr);
       cudaEventRecord(b, ctx->stream);
       cudaEventSynchronize(b);
       float ms = 0.0f;
@@ -1162,14 +1268,21 @@ int score_workspace(rcg_ctx* ctx, const PyramidDesc& pd) {
 }
 
 int score_pyramids(rcg_ctx* ctx, const PyramidDesc& pd, const float* d_ref, const float* d_dist, double* d_score,
-                   SearchState* search, StepDesc* step) {
+                   SearchState* search, StepDesc* step, float2* refm, int ref_mode) {
   if (score_workspace(ctx, pd) != RCG_OK) return RCG_NO_MEMORY;
   double* partials = (double*)ctx->bufs["score_partials"].ptr;
   double* scale_sums = (double*)ctx->bufs["score_scale_sums"].ptr;
   unsigned* counter = (unsigned*)ctx->bufs["score_counter"].ptr;
   const PyramidDesc pb = plan_bands(ctx, pd);
-  RCG_LAUNCH(ctx, "ssim2_tiles", k_ssim2_tiles, pb.total_tiles, kTileThreads, kTileSmem, pb, d_ref, d_dist, partials,
-             step);
+  if (!refm || ref_mode == kRefNone)
+    RCG_LAUNCH(ctx, "ssim2_tiles", k_ssim2_tiles<kRefNone>, pb.total_tiles, kTileThreads, kTileSmem, pb, d_ref, d_dist,
+               partials, step, nullptr);
+  else if (ref_mode == kRefWrite)
+    RCG_LAUNCH(ctx, "ssim2_tiles_store", k_ssim2_tiles<kRefWrite>, pb.total_tiles, kTileThreads, kTileSmem, pb, d_ref,
+               d_dist, partials, step, refm);
+  else
+    RCG_LAUNCH(ctx, "ssim2_tiles_cached", k_ssim2_tiles<kRefRead>, pb.total_tiles, kTileThreads, kTileSmem, pb, d_ref,
+               d_dist, partials, step, refm);
   dim3 rg(pb.nscales, kScoreSums);
   RCG_LAUNCH(ctx, "ssim2_reduce", k_ssim2_reduce, rg, 256, 0, pb, partials, scale_sums, counter, d_score, search,
              step);
@@ -1378,7 +1491,8 @@ extern "C" int rcg_ssimulacra2_device_noalloc(const uint8_t* d_reference, const 
     k_pyramid<<<pg, 256, 0, s>>>(pd, pyr_ref, nullptr);
     k_pyramid<<<pg, 256, 0, s>>>(pd, pyr_dist, nullptr);
   }
-  k_ssim2_tiles<<<pd.total_tiles, kTileThreads, kTileSmem, s>>>(pd, pyr_ref, pyr_dist, partials, nullptr);
+  k_ssim2_tiles<kRefNone><<<pd.total_tiles, kTileThreads, kTileSmem, s>>>(pd, pyr_ref, pyr_dist, partials, nullptr,
+                                                                        nullptr);
   k_ssim2_reduce<<<dim3(pd.nscales, kScoreSums), 256, 0, s>>>(pd, partials, sums, counter, d_score, nullptr,
                                                               nullptr);
   cudaError_t e = cudaGetLastError();

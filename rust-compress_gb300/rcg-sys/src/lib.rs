@@ -138,6 +138,7 @@ extern "C" {
     pub fn rcg_ctx_tie_rescores(ctx: *const RcgCtx) -> u64;
     pub fn rcg_ctx_set_band_chunks(ctx: *mut RcgCtx, chunks: c_int) -> c_int;
     pub fn rcg_ctx_band_chunks(ctx: *mut RcgCtx, width: u32, height: u32) -> c_int;
+    pub fn rcg_ctx_set_ref_cache(ctx: *mut RcgCtx, on: c_int) -> c_int;
     pub fn rcg_ctx_launch_count(ctx: *const RcgCtx) -> u64;
     pub fn rcg_ctx_set_profiling(ctx: *mut RcgCtx, on: c_int) -> c_int;
     pub fn rcg_ctx_kernel_time(ctx: *mut RcgCtx, name: *const c_char, launches: *mut u64,

@@ -262,6 +262,7 @@ def _load():
         "rcg_ctx_tie_rescores": (ctypes.c_uint64, [P]),
         "rcg_ctx_set_band_chunks": (i32, [P, i32]),
         "rcg_ctx_band_chunks": (i32, [P, u32, u32]),
+        "rcg_ctx_set_ref_cache": (i32, [P, i32]),
         "rcg_ssimulacra2_device_noalloc": (i32, [P, P, u32, u32, i32, P, P]),
         "rcg_build_coefs": (i32, [P, P, u32, u32, i32, ctypes.POINTER(_Opts), P, sz, P]),
         "rcg_reconstruct": (i32, [P, u32, u32, ctypes.POINTER(_Layout), P, P, P, sz]),
@@ -340,7 +341,8 @@ EXPORTED = (
     "rcg_coef_gradient rcg_perceptual_weights rcg_build_coefs_weighted rcg_search_weighted rcg_search_perceptual "
     "rcg_perceptual_strength rcg_ctx_set_graphs rcg_ctx_graph_stats rcg_ssimulacra2_batch rcg_ssimulacra2_batch_device "
     "rcg_sweep_qualities rcg_ssimulacra2_exact rcg_ctx_set_tie_band rcg_ctx_tie_rescores "
-    "rcg_ctx_set_band_chunks rcg_ctx_band_chunks rcg_search_batch_lockstep rcg_search_perceptual_fast"
+    "rcg_ctx_set_band_chunks rcg_ctx_band_chunks rcg_search_batch_lockstep rcg_search_perceptual_fast "
+    "rcg_ctx_set_ref_cache"
 ).split()
 
 
@@ -444,6 +446,10 @@ class Context:
     def set_band_chunks(self, chunks):
         """The fast scorer's band height in 32-row chunks: 0 autotunes per size class (default), 1..64 fixes it."""
         self._check(_lib.rcg_ctx_set_band_chunks(self._ptr, int(chunks)))
+
+    def set_ref_cache(self, on):
+        """The SSIMULACRA2 searches' stored reference moments (default on; the same scores either way)."""
+        self._check(_lib.rcg_ctx_set_ref_cache(self._ptr, 1 if on else 0))
 
     def band_chunks(self, width, height):
         """Chunks per band used for a width x height image (autotuning its size class if needed)."""
