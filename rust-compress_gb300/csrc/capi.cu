@@ -1596,12 +1596,11 @@ int rcg_search_batch_lockstep(rcg_ctx* ctx, int n, const uint8_t* const* srcs, c
     it.q0 = q_total;
     q_total += (r.es.max_blocks + 127) / 128;
     it.ux = ((r.w + 3) / 4 + 127) / 128;
-    it.uy = std::min((r.h + 1) / 2, 65535);
+    it.uy = std::min(((r.h + 1) / 2 + 3) / 4, 65535);  // four chroma rows per CTA, as upsample_color
     it.u0 = u_total;
     u_total += (long long)it.ux * it.uy;
     it.p0 = p_total;
-    if (it.pd.nscales >= 2)
-      p_total += (long long)((it.pd.s[1].w + 31) / 32) * ((it.pd.s[1].h + 31) / 32);
+    p_total += pyramid_ctas(it.pd);
     it.t0 = t_total;
     t_total += it.pd.total_tiles;
     max_scales = std::max(max_scales, it.pd.nscales);

@@ -973,9 +973,10 @@ __global__ void __launch_bounds__(128, 10) k_upsample_color(const StepDesc* __re
 
 int upsample_color(rcg_ctx* ctx, StepDesc* d_step, const uint8_t* d_planes, int w, int h, uint8_t* d_rgb,
                    float* d_lin) {
-  // (h + 1) / 2 rows of CTAs: the 4:2:0 path writes two rows per chroma row, and the general path strides over the
-  // rows by the grid height, so every layout is covered (a grid of h rows would leave half of it idle for 4:2:0).
-  dim3 grid(((w + 3) / 4 + 127) / 128, std::min((h + 1) / 2, 65535));
+  // (h + 1) / 8 rows of CTAs: the 4:2:0 path writes two rows per chroma row and each CTA takes four chroma rows (its
+  // shared-memory table filled once for 8 output rows: 46.5 -> 40.7 us per 12 MP candidate against one chroma row
+  // per CTA); the general path strides over the rows by the grid height, so every layout is covered.
+  dim3 grid(((w + 3) / 4 + 127) / 128, std::min(((h + 1) / 2 + 3) / 4, 65535));
   RCG_LAUNCH(ctx, "upsample_color", k_upsample_color, grid, 128, 0, d_step, d_planes, w, h, d_rgb, d_lin);
   return RCG_OK;
 }

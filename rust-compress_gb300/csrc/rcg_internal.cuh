@@ -308,6 +308,8 @@ int to_linear(rcg_ctx* ctx, const uint8_t* d_img, int w, int h, int channels, in
 int build_pyramid(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr);
 // The same, skipped on the device when the search step is inactive.
 int build_pyramid_gated(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, const StepDesc* st);
+// CTAs of one pyramid launch (k_pyramid and the work-list forms): one per scale-1 tile, 0 for a single scale.
+int pyramid_ctas(const PyramidDesc& pd);
 // Reference moments of the tile kernel: kRefNone computes every blurred moment; kRefWrite also stores the
 // reference-only ones (blur a', blur a'^2) for later candidates against the same reference; kRefRead reads them
 // instead of blurring them. Same scores in every mode. The store is chunk-major: per 32x32 chunk of the banded

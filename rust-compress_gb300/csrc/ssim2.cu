@@ -765,12 +765,19 @@ __device__ __forceinline__ float mean2x2(const float* p, int stride, int w, int 
   return __fadd_rn(s, err) * (1.0f / (float)((y1 - y0) * (x1 - x0)));
 }
 
-// Every coarser scale of a pyramid from scale 0 in one launch. One CTA owns a 32x32 tile of scale 1 (a 64x64 block
-// of scale 0) and the 16x16, 8x8, 4x4, 2x2 tiles of scales 2-5 below it, kept in shared memory between levels: tiles
-// nest exactly because each level halves the previous one, and odd edges occur only in the last tile of a row or
-// column, where mean2x2 clips to the level's size.
-constexpr int kPyrTile = 32;
+// Every coarser scale of a pyramid from scale 0 in one launch. One CTA owns a kPyrTW x kPyrTH tile of scale 1 (a
+// block of scale 0 twice as wide and tall) and the tiles of scales 2-5 below it, each half the one above, kept in
+// shared memory between levels: tiles nest exactly because each level halves the previous one, and odd edges occur
+// only in the last tile of a row or column, where mean2x2 clips to the level's size. The scale-5 tile is
+// kPyrTW/16 x kPyrTH/16.
+constexpr int kPyrTW = 32, kPyrTH = 32;
 constexpr int kPyrThreads = 256;  // every pyramid launch
+static_assert(kPyrTH % 16 == 0 && kPyrTW % 32 == 0 && kPyrTW * kPyrTH % (2 * kPyrThreads) == 0, "pyramid tile");
+
+int pyramid_ctas(const PyramidDesc& pd) {
+  if (pd.nscales < 2) return 0;
+  return ((pd.s[1].w + kPyrTW - 1) / kPyrTW) * ((pd.s[1].h + kPyrTH - 1) / kPyrTH);
+}
 
 // Scale-1 tile (tx, ty) from scale 0 into `out` (shared) and dst1 (global). Each thread takes pairs of adjacent
 // outputs, whose 2x4 source samples per channel are two aligned 16-byte loads when the scale-0 rows are (width a
@@ -787,14 +794,14 @@ __device__ __forceinline__ float quad_mean(float q0, float q1, float q2, float q
 
 __device__ __forceinline__ void scale1_tile(const float* __restrict__ src0, float* __restrict__ dst1,
                                             const ScaleDesc& s0, const ScaleDesc& s1, int tx, int ty,
-                                            float (*out)[kPyrTile][kPyrTile + 1]) {
+                                            float (*out)[kPyrTH][kPyrTW + 1]) {
   const size_t np0 = (size_t)s0.w * s0.h, np1 = (size_t)s1.w * s1.h;
   const bool vec = (s0.w & 3) == 0 && ((uintptr_t)src0 & 15) == 0;
 #pragma unroll
-  for (int k = 0; k < kPyrTile * kPyrTile / (2 * kPyrThreads); k++) {
+  for (int k = 0; k < kPyrTW * kPyrTH / (2 * kPyrThreads); k++) {
     const int i = threadIdx.x + k * kPyrThreads;
-    const int lx = 2 * (i % (kPyrTile / 2)), ly = i / (kPyrTile / 2);
-    const int ox = tx * kPyrTile + lx, oy = ty * kPyrTile + ly;
+    const int lx = 2 * (i % (kPyrTW / 2)), ly = i / (kPyrTW / 2);
+    const int ox = tx * kPyrTW + lx, oy = ty * kPyrTH + ly;
     if (ox >= s1.w || oy >= s1.h) continue;
     float v[2][3];
     const bool two = ox + 1 < s1.w;
@@ -843,21 +850,21 @@ __device__ __forceinline__ void scale1_tile(const float* __restrict__ src0, floa
 
 // Scale-1 tile `blk` of a pyramid and every coarser tile below it.
 __device__ __forceinline__ void pyramid_tile(const PyramidDesc& pd, float* __restrict__ pyr, const int blk) {
-  __shared__ float buf[2][3][kPyrTile][kPyrTile + 1];
+  __shared__ float buf[2][3][kPyrTH][kPyrTW + 1];
   const ScaleDesc s0 = pd.s[0], s1 = pd.s[1];
-  const int tiles_x = (s1.w + kPyrTile - 1) / kPyrTile;
+  const int tiles_x = (s1.w + kPyrTW - 1) / kPyrTW;
   const int tx = blk % tiles_x, ty = blk / tiles_x;
   scale1_tile(pyr + s0.off, pyr + s1.off, s0, s1, tx, ty, buf[0]);
-  int cur = 0, tile = kPyrTile;
+  int cur = 0, tw = kPyrTW, th = kPyrTH;
   for (int L = 2; L < pd.nscales; L++) {
     __syncthreads();
     const ScaleDesc a = pd.s[L - 1], b = pd.s[L];
     const size_t npb = (size_t)b.w * b.h;
-    const int half = tile / 2;
-    const int ax0 = tx * tile, ay0 = ty * tile;  // tile origin at level L-1
-    for (int i = threadIdx.x; i < half * half; i += blockDim.x) {
-      int lx = i % half, ly = i / half;
-      int ox = tx * half + lx, oy = ty * half + ly;
+    const int hw = tw / 2, hh = th / 2;
+    const int ax0 = tx * tw, ay0 = ty * th;  // tile origin at level L-1
+    for (int i = threadIdx.x; i < hw * hh; i += blockDim.x) {
+      int lx = i % hw, ly = i / hw;
+      int ox = tx * hw + lx, oy = ty * hh + ly;
       if (ox < b.w && oy < b.h) {
         // the 2x2 source block lies in this CTA's level L-1 tile; clip to level L-1's size like mean2x2
         int x1 = min(ox * 2 + 2, a.w) - ax0, y1 = min(oy * 2 + 2, a.h) - ay0;
@@ -877,7 +884,8 @@ __device__ __forceinline__ void pyramid_tile(const PyramidDesc& pd, float* __res
       }
     }
     cur ^= 1;
-    tile = half;
+    tw = hw;
+    th = hh;
   }
 }
 
@@ -1044,8 +1052,7 @@ int to_linear(rcg_ctx* ctx, const uint8_t* d_img, int w, int h, int channels, in
 
 int build_pyramid_gated(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, const StepDesc* st) {
   if (pd.nscales < 2) return RCG_OK;
-  const int grid = ((pd.s[1].w + kPyrTile - 1) / kPyrTile) * ((pd.s[1].h + kPyrTile - 1) / kPyrTile);
-  RCG_LAUNCH(ctx, "pyramid", k_pyramid, grid, 256, 0, pd, d_pyr, st);
+  RCG_LAUNCH(ctx, "pyramid", k_pyramid, pyramid_ctas(pd), kPyrThreads, 0, pd, d_pyr, st);
   return RCG_OK;
 }
 
@@ -1325,9 +1332,7 @@ int score_batch(rcg_ctx* ctx, int n, const uint8_t* const* d_refs, const uint8_t
     floats = align64(floats + it.pd.floats);
     const int copies = it.own_ref ? 2 : 1;
     it.lin_ctas = (int)((((long long)w * h + 3) / 4 + 255) / 256);
-    it.pyr_ctas = it.pd.nscales >= 2 ? ((it.pd.s[1].w + kPyrTile - 1) / kPyrTile) *
-                                           ((it.pd.s[1].h + kPyrTile - 1) / kPyrTile)
-                                     : 0;
+    it.pyr_ctas = pyramid_ctas(it.pd);
     it.lin0 = lin;
     lin += (long long)copies * it.lin_ctas;
     it.pyr0 = pyr;
@@ -1487,9 +1492,9 @@ extern "C" int rcg_ssimulacra2_device_noalloc(const uint8_t* d_reference, const 
   k_to_linear<<<lg, 256, 0, s>>>(d_reference, w, h, channels, 8, nullptr, pyr_ref);
   k_to_linear<<<lg, 256, 0, s>>>(d_distorted, w, h, channels, 8, nullptr, pyr_dist);
   if (pd.nscales > 1) {
-    const int pg = ((pd.s[1].w + kPyrTile - 1) / kPyrTile) * ((pd.s[1].h + kPyrTile - 1) / kPyrTile);
-    k_pyramid<<<pg, 256, 0, s>>>(pd, pyr_ref, nullptr);
-    k_pyramid<<<pg, 256, 0, s>>>(pd, pyr_dist, nullptr);
+    const int pg = pyramid_ctas(pd);
+    k_pyramid<<<pg, kPyrThreads, 0, s>>>(pd, pyr_ref, nullptr);
+    k_pyramid<<<pg, kPyrThreads, 0, s>>>(pd, pyr_dist, nullptr);
   }
   k_ssim2_tiles<kRefNone><<<pd.total_tiles, kTileThreads, kTileSmem, s>>>(pd, pyr_ref, pyr_dist, partials, nullptr,
                                                                         nullptr);
