@@ -482,7 +482,12 @@ int rate_tables(rcg_ctx* ctx, StepDesc* d_step) {
 // per candidate of a 3 MP perceptual search). The DP is latency-bound (one block's positions are serial); measured per
 // 12 MP candidate: 16-coefficient chunks at 6 CTAs per SM 75.6 us, 8-coefficient chunks at 8 CTAs 72.1 us. A rolled
 // DP loop over cp.async-staged shared-memory coefficients, (cost, zd) node pairs and an unrolled node scan were all
-// slower or no faster (80-92, 74.2 and 72.3-76.6 us).
+// slower or no faster (80-92, 74.2 and 72.3-76.6 us). So was a work-list: at the qualities a search visits most
+// blocks have no position with a candidate (72% at q74, 96% at q62, yet only 3% of 32-block warps are all such
+// blocks), so the quantize kernel wrote those blocks' results (DC only) and listed the rest for the trellis: the
+// trellis went 70 -> 61 us but the quantize kernel 29 -> 40 us (the extra test per coefficient and the writes it
+// took over); listing the blocks in buckets by their count of candidates, heaviest first, scattered each warp's
+// blocks and cost 78 + 41 us.
 template <bool kWeighted>
 __device__ __forceinline__ void trellis_body(StepDesc* __restrict__ st, const CacheSet& cs, long long bx) {
   // The per-position tables of every component and the lambda*rate tables of the components this CTA's blocks
