@@ -1548,7 +1548,7 @@ int rcg_search_batch_lockstep(rcg_ctx* ctx, int n, const uint8_t* const* srcs, c
     rcg_ctx* sub = ctx->lock_subs[(size_t)i];
     sub->tie_band = ctx->tie_band;
     sub->band_chunks = ctx->band_chunks;
-    sub->ref_cache = false;  // the work-list tile kernel computes every moment (no store to allocate)
+    sub->ref_cache = ctx->ref_cache;
     const size_t bytes = (size_t)widths[i] * heights[i] * channels[i];
     uint8_t* d_src = (uint8_t*)workspace(sub, "img_src", bytes);
     int r = d_src ? RCG_OK : RCG_NO_MEMORY;
@@ -1587,6 +1587,7 @@ int rcg_search_batch_lockstep(rcg_ctx* ctx, int n, const uint8_t* const* srcs, c
     it.w = r.w;
     it.h = r.h;
     it.ref_pyr = r.sc.ref_pyr;
+    it.refm = r.sc.ref_moments;
     it.dist_pyr = r.sc.dist_pyr;
     it.partials = (double*)sub->bufs["score_partials"].ptr;
     it.scale_sums = (double*)sub->bufs["score_scale_sums"].ptr;
@@ -1612,14 +1613,15 @@ int rcg_search_batch_lockstep(rcg_ctx* ctx, int n, const uint8_t* const* srcs, c
   double* d_exact = (double*)workspace(ctx, "x_score", sizeof(double), false);
   if (!d_items || !d_exact) return RCG_NO_MEMORY;
   cudaMemcpyAsync(d_items, items.data(), sizeof(LockItem) * (size_t)n, cudaMemcpyHostToDevice, ctx->stream);
-  auto issue_step = [&]() {
+  auto issue_step = [&](int s) {
     lock_step_codec(ctx, d_items, n, q_total, u_total);
-    lock_step_score(ctx, d_items, n, p_total, t_total, max_scales);
+    lock_step_score(ctx, d_items, n, p_total, t_total, max_scales,
+                    ctx->ref_cache ? (s == 0 ? kRefWrite : kRefRead) : kRefNone);
   };
   // The grids follow from the totals; the images' buffers come in through the work-list uploaded above.
   const std::vector<long long> key = {5, n, max_steps, q_total, u_total, p_total, t_total, max_scales};
   rc = run_step_loop(ctx, key, [&]() {
-    for (int s = 0; s < max_steps; s++) issue_step();
+    for (int s = 0; s < max_steps; s++) issue_step(s);
   });
   if (rc != RCG_OK) return rc;
   std::vector<SearchState> hs((size_t)n);
@@ -1642,7 +1644,7 @@ int rcg_search_batch_lockstep(rcg_ctx* ctx, int n, const uint8_t* const* srcs, c
       from = std::min(from, hs[(size_t)i].step + 1);
     }
     if (from == max_steps) break;
-    for (int s = from; s < max_steps; s++) issue_step();
+    for (int s = from; s < max_steps; s++) issue_step(s);
     if ((rc = read_states()) != RCG_OK) return rc;
   }
   // Results, each through its image's context (the step loop is complete: the states were read after it), in

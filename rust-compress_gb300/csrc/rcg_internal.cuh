@@ -166,6 +166,7 @@ struct LockItem {
   unsigned* counter;
   double* score;
   PyramidDesc pd;          // the scorer's CTA layout (bands)
+  float2* refm;            // the reference moments (null: the store is off)
   long long q0;            // first CTA in the block grids (quantize, trellis, dequantize: 128 blocks a CTA)
   long long u0;            // first CTA in the upsampling grid (ux x uy CTAs)
   int ux, uy;
@@ -349,7 +350,7 @@ int score_batch(rcg_ctx* ctx, int n, const uint8_t* const* d_refs, const uint8_t
 // ---- lockstep batch (work-list launches over the LockItems of a batch; totals are the grids' CTA counts)
 void lock_step_codec(rcg_ctx* ctx, const LockItem* d_items, int n, long long q_total, long long u_total);
 void lock_step_score(rcg_ctx* ctx, const LockItem* d_items, int n, long long p_total, long long t_total,
-                     int max_scales);
+                     int max_scales, int ref_mode = kRefNone);
 
 // ---- codec (codec.cu)
 // Colour conversion + edge padding (jpeg/src/encode.rs:463-477): full-resolution padded Y/Cb/Cr planes.

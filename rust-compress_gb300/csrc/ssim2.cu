@@ -1013,6 +1013,7 @@ __global__ void __launch_bounds__(256, 5) k_pyramid_lock(const LockItem* __restr
   pyramid_tile(it.pd, it.dist_pyr, (int)((long long)blockIdx.x - it.p0));
 }
 
+template <int kRef>
 __global__ void __launch_bounds__(kTileThreads, 3) k_ssim2_tiles_lock(const LockItem* __restrict__ items, int n) {
   const int i = lock_find<&LockItem::t0>(items, n, blockIdx.x);
   const LockItem& it = items[i];
@@ -1021,8 +1022,8 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_ssim2_tiles_lock(const Lock
   int s = 0;
   while (s + 1 < it.pd.nscales && blk >= it.pd.s[s + 1].tile0) s++;
   const ScaleDesc sd = it.pd.s[s];
-  ssim2_band<kRefNone>(sd, blk - sd.tile0, it.ref_pyr, it.dist_pyr, it.partials + blk, (size_t)it.pd.total_tiles,
-                       nullptr);
+  ssim2_band<kRef>(sd, blk - sd.tile0, it.ref_pyr, it.dist_pyr, it.partials + blk, (size_t)it.pd.total_tiles,
+                   it.refm);
 }
 
 __global__ void __launch_bounds__(256) k_ssim2_reduce_lock(const LockItem* __restrict__ items) {
@@ -1032,9 +1033,18 @@ __global__ void __launch_bounds__(256) k_ssim2_reduce_lock(const LockItem* __res
 }
 
 void lock_step_score(rcg_ctx* ctx, const LockItem* d_items, int n, long long p_total, long long t_total,
-                     int max_scales) {
+                     int max_scales, int ref_mode) {
   if (p_total > 0) RCG_LAUNCH(ctx, "pyramid_lock", k_pyramid_lock, (unsigned)p_total, 256, 0, d_items, n);
-  RCG_LAUNCH(ctx, "ssim2_tiles_lock", k_ssim2_tiles_lock, (unsigned)t_total, kTileThreads, kTileSmem, d_items, n);
+  // Every image of the batch is at the same step: the first stores its reference moments, the later ones read them.
+  if (ref_mode == kRefWrite)
+    RCG_LAUNCH(ctx, "ssim2_tiles_lock", k_ssim2_tiles_lock<kRefWrite>, (unsigned)t_total, kTileThreads, kTileSmem,
+               d_items, n);
+  else if (ref_mode == kRefRead)
+    RCG_LAUNCH(ctx, "ssim2_tiles_lock", k_ssim2_tiles_lock<kRefRead>, (unsigned)t_total, kTileThreads, kTileSmem,
+               d_items, n);
+  else
+    RCG_LAUNCH(ctx, "ssim2_tiles_lock", k_ssim2_tiles_lock<kRefNone>, (unsigned)t_total, kTileThreads, kTileSmem,
+               d_items, n);
   RCG_LAUNCH(ctx, "ssim2_reduce_lock", k_ssim2_reduce_lock, dim3(max_scales, kScoreSums, n), 256, 0, d_items);
 }
 
@@ -1146,7 +1156,11 @@ static cudaError_t scorer_constants(int device) {
   if ((e = cudaFuncSetAttribute(k_ssim2_tiles_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kTileSmem)) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(k_ssim2_tiles_lock, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if ((e = cudaFuncSetAttribute(k_ssim2_tiles_lock<kRefNone>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kTileSmem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_ssim2_tiles_lock<kRefWrite>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kTileSmem)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_ssim2_tiles_lock<kRefRead>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kTileSmem)) != cudaSuccess)
     return e;
   if (device >= 0 && device < 64) g_scorer_ready[device] = true;

@@ -90,6 +90,12 @@ def test_cache_in_batch_and_perceptual_searches():
         rb = off.search_batch(imgs, targets, 100, OPTS, 2)
         for a, b in zip(ra, rb):
             _same(a, b)
+        for _ in range(3):  # the lockstep batch: plain launches, capture, replay
+            la = on.search_batch(imgs, targets, 100, OPTS, lockstep=True)
+            lb = off.search_batch(imgs, targets, 100, OPTS, lockstep=True)
+            for a, b, c in zip(la, lb, ra):
+                _same(a, b)
+                _same(a, c)
         pa, fa, wa = on.find_quality_perceptual_fast(imgs[2], 70.0, 100, OPTS)
         pb, fb, wb = off.find_quality_perceptual_fast(imgs[2], 70.0, 100, OPTS)
         _same(pa, pb)
