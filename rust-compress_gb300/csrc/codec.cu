@@ -487,13 +487,17 @@ int rate_tables(rcg_ctx* ctx, StepDesc* d_step) {
 // blocks), so the quantize kernel wrote those blocks' results (DC only) and listed the rest for the trellis: the
 // trellis went 70 -> 61 us but the quantize kernel 29 -> 40 us (the extra test per coefficient and the writes it
 // took over); listing the blocks in buckets by their count of candidates, heaviest first, scattered each warp's
-// blocks and cost 78 + 41 us.
+// blocks and cost 78 + 41 us. Sorting each CTA's blocks by that count, heaviest first, after a counting pass (the
+// DC-only blocks written there) gave the same 70.6 us: the cost is the per-position work every lane runs, not the
+// lanes that wait for a heavy neighbour. Cutting that work did help: each position's scale, step and weight are one
+// 16-byte shared-memory entry, and a node keeps its value with its sign instead of a 64-bit sign mask updated at
+// every position: 70.7 -> 66.8 us, the same coefficients.
 template <bool kWeighted>
 __device__ __forceinline__ void trellis_body(StepDesc* __restrict__ st, const CacheSet& cs, long long bx) {
   // The per-position tables of every component and the lambda*rate tables of the components this CTA's blocks
   // belong to (usually one), staged in shared memory: the DP reads them at every position.
   __shared__ float lr[3][64 * 16];
-  __shared__ float s_scale[3][64], s_rq[3][64], s_rw[3][64];
+  __shared__ float4 s_tab[3][64];  // per position: (scale, step, weight, -)
   if (!st->active || !st->use_trellis) return;
   const bool requant = st->requant != 0;
   const long long blk0 = bx * blockDim.x;
@@ -502,9 +506,7 @@ __device__ __forceinline__ void trellis_body(StepDesc* __restrict__ st, const Ca
     (&lr[c_lo][0])[i] = (&st->lr[c_lo][0])[i];
   for (int i = threadIdx.x; i < 3 * 64; i += blockDim.x) {
     const int c = i / 64, k = i % 64;
-    s_scale[c][k] = requant ? st->ratio[c][k] : st->divz[c][k];
-    s_rq[c][k] = st->rq[c][k];
-    s_rw[c][k] = st->rw[c][k];
+    s_tab[c][k] = make_float4(requant ? st->ratio[c][k] : st->divz[c][k], st->rq[c][k], st->rw[c][k], 0.0f);
   }
   __syncthreads();
   const long long gb = blk0 + threadIdx.x;
@@ -516,9 +518,7 @@ __device__ __forceinline__ void trellis_body(StepDesc* __restrict__ st, const Ca
   // Requantization: a[k] = source[k] * ratio[k] (jpeg/src/encode.rs:162-166); the DC stays the plain value.
   const float* cache = requant ? nullptr : cs.p[cd.cache] + (gb - cd.blk0);
   const int16_t* src = requant ? st->coef_src + gb * 64 : nullptr;
-  const float* scale = s_scale[c];
-  const float* rq = s_rq[c];
-  const float* rw = s_rw[c];
+  const float4* tab = s_tab[c];
   const float* lrc = lr[c];
   const float* pw = kWeighted ? st->pweights + gb * 64 : nullptr;  // 16-byte aligned rows of 64 floats
 
@@ -527,7 +527,6 @@ __device__ __forceinline__ void trellis_body(StepDesc* __restrict__ st, const Ca
   short nv[128];
   signed char nprev[128];
   int nn = 0;
-  unsigned long long negmask = 0;
   int dc = 0;
   float zprev = 0.0f;  // zd[i-1]
 
@@ -560,13 +559,14 @@ __device__ __forceinline__ void trellis_body(StepDesc* __restrict__ st, const Ca
 #pragma unroll
     for (int j = 0; j < kChunk; j++) {
       const int i = c0 + j;
-      float a = fmul(cur[j], scale[i]);
+      const float4 tb = tab[i];
+      float a = fmul(cur[j], tb.x);
       if (i == 0) {
         dc = clampi(round_f32(a), -2047, 2047);
         continue;
       }
-      float q = rq[i], w = kWeighted ? fmul(rw[i], wv[j]) : rw[i];
-      if (a < 0.0f) negmask |= 1ull << i;
+      float q = tb.y, w = kWeighted ? fmul(tb.z, wv[j]) : tb.z;
+      const bool neg = a < 0.0f;  // a node keeps its value with this sign
       float m = fabsf(a);
       unsigned v0 = (unsigned)fadd(m, 0.5f);
       int pushed = 0;
@@ -598,14 +598,14 @@ __device__ __forceinline__ void trellis_body(StepDesc* __restrict__ st, const Ca
         }
         ncost[nn] = best_lo;
         npos[nn] = (unsigned char)i;
-        nv[nn] = (short)lo;
+        nv[nn] = (short)(neg ? -(int)lo : (int)lo);
         nprev[nn] = (signed char)prev_lo;
         nn++;
         pushed = 1;
         if (two) {
           ncost[nn] = best_hi;
           npos[nn] = (unsigned char)i;
-          nv[nn] = (short)v0;
+          nv[nn] = (short)(neg ? -(int)v0 : (int)v0);
           nprev[nn] = (signed char)prev_hi;
           nn++;
           pushed = 2;
@@ -645,7 +645,7 @@ __device__ __forceinline__ void trellis_body(StepDesc* __restrict__ st, const Ca
   while (node >= 0) {
     int p = npos[node];
     short v = nv[node];
-    out[p] = ((negmask >> p) & 1) ? (int16_t)(-v) : (int16_t)v;
+    out[p] = (int16_t)v;
     node = nprev[node];
   }
 }
