@@ -491,7 +491,9 @@ int rate_tables(rcg_ctx* ctx, StepDesc* d_step) {
 // DC-only blocks written there) gave the same 70.6 us: the cost is the per-position work every lane runs, not the
 // lanes that wait for a heavy neighbour. Cutting that work did help: each position's scale, step and weight are one
 // 16-byte shared-memory entry, and a node keeps its value with its sign instead of a 64-bit sign mask updated at
-// every position: 70.7 -> 66.8 us, the same coefficients.
+// every position: 70.7 -> 66.8 us, the same coefficients. The pass then waits on its coefficient loads, yet deeper
+// prefetches measured slower: two chunks ahead 68.5 us, 16-position chunks 71.2 us (7 CTAs per SM), two or three
+// chunks staged ahead in shared memory by 4-byte cp.async copies 79-81 us.
 template <bool kWeighted>
 __device__ __forceinline__ void trellis_body(StepDesc* __restrict__ st, const CacheSet& cs, long long bx) {
   // The per-position tables of every component and the lambda*rate tables of the components this CTA's blocks
