@@ -1,6 +1,6 @@
 """SSIMULACRA2 on the GPU (through the C ABI) against the reference's golden vectors and the CPU oracle.
 
-Tolerances: the benchmark spec's bound is 1e-3 absolute against the reference's scorer (the oracle); the golden pairs also
+Tolerances: the fast scorer's bound is 1e-3 absolute against the reference's scorer (the oracle); the golden pairs also
 keep the reference's own 1e-4 against py-ssimulacra2 (cli/tests/ssimulacra2.rs:8). Identical images must give exactly
 100 and repeated calls must agree bit for bit (core/src/ssimulacra2.rs:542, :630).
 """

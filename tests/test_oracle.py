@@ -11,7 +11,7 @@ import math
 import numpy as np
 import pytest
 
-# cli/tests/ssimulacra2.rs:8 allows 1e-4; the restatement reproduces the reference's ~7e-6 (README.md:118).
+# cli/tests/ssimulacra2.rs:8 allows 1e-4; the restatement reproduces the ~7e-6 the reference reports for its own scorer.
 GOLDEN_TOL = 1e-5
 
 
