@@ -848,12 +848,118 @@ __device__ __forceinline__ void scale1_tile(const float* __restrict__ src0, floa
   }
 }
 
+// Every output of every level of tile (tx, ty) is a full 2x2 mean (no clipped block at an odd edge).
+__device__ __forceinline__ bool pyramid_interior(const PyramidDesc& pd, int tx, int ty) {
+  int tw = kPyrTW, th = kPyrTH;
+  for (int L = 1; L < pd.nscales; L++) {
+    if (2 * (tx + 1) * tw > pd.s[L - 1].w || 2 * (ty + 1) * th > pd.s[L - 1].h) return false;
+    tw /= 2;
+    th /= 2;
+  }
+  return true;
+}
+
+// Tile (tx, ty) when it is interior and scale 0 takes 16-byte row loads: each thread owns a 2x2 block of scale 1 (its
+// 4x4 scale-0 source as 16-byte loads) and so one scale-2 sample, computed in registers; the four scale-2 samples of
+// a scale-3 sample sit in one warp (a warp holds two scale-2 rows) and meet by shuffles; scales 4 and 5 (16 and 4
+// samples) go through shared memory. Every sample is quad_mean of its four sources in mean2x2's order, as the general
+// path computes it for full blocks, so the planes are the same bits.
+__device__ __forceinline__ void pyramid_tile_interior(const PyramidDesc& pd, float* __restrict__ pyr, int tx, int ty) {
+  static_assert(kPyrTW == 32 && kPyrTH == 32 && kPyrThreads == 256, "thread layout of the interior path");
+  __shared__ float l3[3][8][8], l4[3][4][4];
+  const ScaleDesc s0 = pd.s[0], s1 = pd.s[1];
+  const size_t np0 = (size_t)s0.w * s0.h, np1 = (size_t)s1.w * s1.h;
+  const float* src0 = pyr + s0.off;
+  const int t = threadIdx.x, bx = t % 16, by = t / 16;
+  const int ox = tx * 32 + 2 * bx, oy = ty * 32 + 2 * by;  // scale-1 origin of the thread's 2x2 block
+  float v1[2][2][3];  // [row][column][channel]
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    float4 a0[3], a1[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float4* p = reinterpret_cast<const float4*>(src0 + c * np0 + (size_t)(2 * (oy + r)) * s0.w + 2 * ox);
+      a0[c] = p[0];
+      a1[c] = p[s0.w / 4];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      v1[r][0][c] = quad_mean(a0[c].x, a0[c].y, a1[c].x, a1[c].y);
+      v1[r][1][c] = quad_mean(a0[c].z, a0[c].w, a1[c].z, a1[c].w);
+    }
+  }
+  float* dst1 = pyr + s1.off;
+#pragma unroll
+  for (int r = 0; r < 2; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      float* d = dst1 + c * np1 + (size_t)(oy + r) * s1.w + ox;
+      d[0] = v1[r][0][c];
+      d[1] = v1[r][1][c];
+    }
+  if (pd.nscales < 3) return;
+  const ScaleDesc s2 = pd.s[2];
+  const size_t np2 = (size_t)s2.w * s2.h;
+  float v2[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    v2[c] = quad_mean(v1[0][0][c], v1[0][1][c], v1[1][0][c], v1[1][1][c]);
+    pyr[s2.off + c * np2 + (size_t)(ty * 16 + by) * s2.w + tx * 16 + bx] = v2[c];
+  }
+  if (pd.nscales < 4) return;
+  // Scale 3: lane = 16 * (row parity) + column; the sample at (column pair, warp) takes lanes l, l+1, l+16, l+17.
+  const ScaleDesc s3 = pd.s[3];
+  const size_t np3 = (size_t)s3.w * s3.h;
+  const int lane = t & 31, warp = t >> 5;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const float q1 = __shfl_down_sync(0xffffffffu, v2[c], 1);
+    const float q2 = __shfl_down_sync(0xffffffffu, v2[c], 16);
+    const float q3 = __shfl_down_sync(0xffffffffu, v2[c], 17);
+    if (lane < 16 && (lane & 1) == 0) {
+      const float v3 = quad_mean(v2[c], q1, q2, q3);
+      const int X = lane / 2, Y = warp;
+      pyr[s3.off + c * np3 + (size_t)(ty * 8 + Y) * s3.w + tx * 8 + X] = v3;
+      l3[c][Y][X] = v3;
+    }
+  }
+  if (pd.nscales < 5) return;
+  __syncthreads();
+  const ScaleDesc s4 = pd.s[4];
+  const size_t np4 = (size_t)s4.w * s4.h;
+  if (t < 16) {
+    const int X = t % 4, Y = t / 4;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float v4 = quad_mean(l3[c][2 * Y][2 * X], l3[c][2 * Y][2 * X + 1], l3[c][2 * Y + 1][2 * X],
+                                 l3[c][2 * Y + 1][2 * X + 1]);
+      pyr[s4.off + c * np4 + (size_t)(ty * 4 + Y) * s4.w + tx * 4 + X] = v4;
+      l4[c][Y][X] = v4;
+    }
+  }
+  if (pd.nscales < 6 || t >= 32) return;
+  __syncwarp();
+  const ScaleDesc s5 = pd.s[5];
+  const size_t np5 = (size_t)s5.w * s5.h;
+  if (t < 4) {
+    const int X = t % 2, Y = t / 2;
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+      pyr[s5.off + c * np5 + (size_t)(ty * 2 + Y) * s5.w + tx * 2 + X] =
+          quad_mean(l4[c][2 * Y][2 * X], l4[c][2 * Y][2 * X + 1], l4[c][2 * Y + 1][2 * X], l4[c][2 * Y + 1][2 * X + 1]);
+  }
+}
+
 // Scale-1 tile `blk` of a pyramid and every coarser tile below it.
 __device__ __forceinline__ void pyramid_tile(const PyramidDesc& pd, float* __restrict__ pyr, const int blk) {
   __shared__ float buf[2][3][kPyrTH][kPyrTW + 1];
   const ScaleDesc s0 = pd.s[0], s1 = pd.s[1];
   const int tiles_x = (s1.w + kPyrTW - 1) / kPyrTW;
   const int tx = blk % tiles_x, ty = blk / tiles_x;
+  if ((s0.w & 3) == 0 && ((uintptr_t)(pyr + s0.off) & 15) == 0 && pyramid_interior(pd, tx, ty)) {
+    pyramid_tile_interior(pd, pyr, tx, ty);
+    return;
+  }
   scale1_tile(pyr + s0.off, pyr + s1.off, s0, s1, tx, ty, buf[0]);
   int cur = 0, tw = kPyrTW, th = kPyrTH;
   for (int L = 2; L < pd.nscales; L++) {
@@ -1006,7 +1112,7 @@ __global__ void __launch_bounds__(256) k_ssim2_reduce_batch(const ScoreItem* __r
 // The scoring half of one bisection step of every image of a lockstep batch (capi.cu): the candidate pyramids, the
 // tiles and the reductions, each one launch over a work-list of every image's CTAs; an image whose search has
 // finished skips through its StepDesc's `active`.
-__global__ void __launch_bounds__(256, 5) k_pyramid_lock(const LockItem* __restrict__ items, int n) {
+__global__ void __launch_bounds__(256, 4) k_pyramid_lock(const LockItem* __restrict__ items, int n) {
   const int i = lock_find<&LockItem::p0>(items, n, blockIdx.x);
   const LockItem& it = items[i];
   if (!it.st->active) return;
