@@ -48,10 +48,11 @@ __device__ __forceinline__ int comp_of_block(const PullDesc& d, long long gb) {
 
 // Full-resolution samples feeding component sample `i` along one axis, with their weights: near = X / 2 (3/4),
 // far = X - 1 / X + 1 in component samples, clamped to [0, n_c - 1] (1/4). Candidates X in [2i - 1, 2i + 2].
-__device__ __forceinline__ int up_taps(int i, int f, int n_full, int n_c, int* xs, double* ws) {
+template <typename T>
+__device__ __forceinline__ int up_taps(int i, int f, int n_full, int n_c, int* xs, T* ws) {
   if (f == 1) {
     xs[0] = i;
-    ws[0] = 1.0;
+    ws[0] = T(1);
     return 1;
   }
   int n = 0;
@@ -59,7 +60,7 @@ __device__ __forceinline__ int up_taps(int i, int f, int n_full, int n_c, int* x
     if (X < 0 || X >= n_full) continue;
     const int near = X >> 1;
     const int far = (X & 1) == 0 ? max(near - 1, 0) : min(near + 1, n_c - 1);
-    const double wt = (near == i ? 0.75 : 0.0) + (far == i ? 0.25 : 0.0);
+    const T wt = (near == i ? T(0.75) : T(0)) + (far == i ? T(0.25) : T(0));
     if (wt != 0.0) {
       xs[n] = X;
       ws[n] = wt;
@@ -70,7 +71,11 @@ __device__ __forceinline__ int up_taps(int i, int f, int n_full, int n_c, int* x
 }
 
 // Four blocks per CTA, one thread per sample: component gradient -> smem -> row and column DCT -> coefficient
-// gradient (zigzag) and the block's gradient energy.
+// gradient (zigzag) and the block's gradient energy. T is the arithmetic of the gather (the upsampling and colour
+// transposes): double for the checked coefficient gradient and for weights from the FP64 adjoint; float for the
+// weights from the FP32 adjoint, whose gradient is already a few 1e-4 from the FP64 one (the FP64 gather took
+// 1.2 ms at 12 MP on this part's FP64 rate). Only the energy is kept with float (coef_grad must be null).
+template <typename T>
 __global__ void __launch_bounds__(256) k_coef_grad(const double* __restrict__ g, PullDesc d,
                                                    double* __restrict__ coef_grad, double* __restrict__ energy) {
   __shared__ double gs[4][64];
@@ -87,30 +92,32 @@ __global__ void __launch_bounds__(256) k_coef_grad(const double* __restrict__ g,
     const long long b = gb - pc.blk0;
     const int cy = (int)(b / pc.bw) * 8 + ty, cx = (int)(b % pc.bw) * 8 + tx;
     if (cx < pc.cw && cy < pc.ch) {
-      double aR, aG, aB;
+      T aR, aG, aB;
       if (d.ncomp == 1 || c == 0) {
-        aR = aG = aB = 1.0;
+        aR = aG = aB = T(1);
       } else if (c == 1) {
-        aR = 0.0;
-        aG = -22554.0 / 65536.0;
-        aB = 116130.0 / 65536.0;
+        aR = T(0);
+        aG = T(-22554.0 / 65536.0);
+        aB = T(116130.0 / 65536.0);
       } else {
-        aR = 91881.0 / 65536.0;
-        aG = -46802.0 / 65536.0;
-        aB = 0.0;
+        aR = T(91881.0 / 65536.0);
+        aG = T(-46802.0 / 65536.0);
+        aB = T(0);
       }
       int xs[4], ys[4];
-      double wx[4], wy[4];
-      const int nx = up_taps(cx, pc.fx, d.w, pc.cw, xs, wx);
-      const int ny = up_taps(cy, pc.fy, d.h, pc.ch, ys, wy);
+      T wx[4], wy[4];
+      const int nx = up_taps<T>(cx, pc.fx, d.w, pc.cw, xs, wx);
+      const int ny = up_taps<T>(cy, pc.fy, d.h, pc.ch, ys, wy);
+      T acc = T(0);
       for (int j = 0; j < ny; j++) {
-        double row = 0.0;
+        T row = T(0);
         for (int i = 0; i < nx; i++) {
           const double* p = g + ((size_t)ys[j] * d.w + xs[i]) * 3;
-          row += wx[i] * (aR * p[0] + aG * p[1] + aB * p[2]);
+          row += wx[i] * (aR * T(p[0]) + aG * T(p[1]) + aB * T(p[2]));
         }
-        gc += wy[j] * row;
+        acc += wy[j] * row;
       }
+      gc = (double)acc;
     }
   }
   gs[grp][t] = gc;
@@ -275,7 +282,11 @@ int perceptual_pullback(rcg_ctx* ctx, const double* d_grad, int w, int h, const 
   double* sens = (double*)workspace(ctx, "perc_sens", (size_t)nb * sizeof(double));
   double* mean = (double*)workspace(ctx, "perc_mean", 3 * sizeof(double));
   if (!energy || !sens || !mean) return RCG_NO_MEMORY;
-  RCG_LAUNCH(ctx, "coef_grad", k_coef_grad, (unsigned)((nb + 3) / 4), 256, 0, d_grad, d, d_coef_grad, energy);
+  if (!d_coef_grad && !p.gradient_fp64)
+    RCG_LAUNCH(ctx, "coef_grad", k_coef_grad<float>, (unsigned)((nb + 3) / 4), 256, 0, d_grad, d, d_coef_grad, energy);
+  else
+    RCG_LAUNCH(ctx, "coef_grad", k_coef_grad<double>, (unsigned)((nb + 3) / 4), 256, 0, d_grad, d, d_coef_grad,
+               energy);
   if (!d_weights) return RCG_OK;
   RCG_LAUNCH(ctx, "block_sensitivity", k_block_sensitivity, (unsigned)((nb + 255) / 256), 256, 0, d, energy,
              p.radius, sens);
