@@ -452,7 +452,8 @@ def _pareto_bytes(curve, target):
 def perceptual_workload(ctx, img, timed, steps=3):
     """The perceptual trellis on the 12 MP workload, target 70, 4:2:0: the perceptual search (plain search ->
     SSIMULACRA2 gradient at its result -> coefficient weights -> weighted search -> planned sizes) through the
-    public API with host buffers, and the file size at equal score: rate-score curves (planned bytes, score) over
+    public API with host buffers (a reusable coefficient buffer, no weights copied back), and the file size at equal
+    score: rate-score curves (planned bytes, score) over
     qualities 50..95 for the plain trellis, the weighted trellis and a control with uniform weights of the same
     strength (no gradient), each read off its Pareto frontier at scores 60..80."""
     import numpy as np
@@ -461,8 +462,13 @@ def perceptual_workload(ctx, img, timed, steps=3):
 
     opts = rcg.EncodeOptions(90, rcg.Subsampling.S420, True)
     popts = rcg.PerceptualOptions()
-    ctx.find_quality_perceptual(img, TARGET, 100, opts, popts)
-    times, r = timed(lambda: ctx.find_quality_perceptual(img, TARGET, 100, opts, popts), steps)
+    # Timed as a host that keeps one output buffer per worker and wants the encoded result only (no weights copied
+    # back: the C ABI's weights argument is nullable); one more call returns the weights for the curves below.
+    coefs_out = np.zeros(ctx.coef_capacity(W, H, 3, opts), dtype=np.int16)
+    ctx.find_quality_perceptual(img, TARGET, 100, opts, popts, out=coefs_out, want_weights=False)
+    times, _ = timed(lambda: ctx.find_quality_perceptual(img, TARGET, 100, opts, popts, out=coefs_out,
+                                                         want_weights=False), steps)
+    r = ctx.find_quality_perceptual(img, TARGET, 100, opts, popts)
     ms = sum(times) / len(times)
     strength = popts.strength_for(r.plain.quality)
     uniform = np.full_like(r.weights, np.float32(strength))
@@ -487,9 +493,12 @@ def perceptual_workload(ctx, img, timed, steps=3):
         return {"per_target_pct": pct, "mean_pct": round(float(np.mean(vals)), 2) if vals else None}
 
     returned = r.perceptual_bytes if r.chose_perceptual else r.plain_bytes
-    # the single-search form on the same image
-    ctx.find_quality_perceptual_fast(img, TARGET, 100, opts, popts)
-    times_f, rf = timed(lambda: ctx.find_quality_perceptual_fast(img, TARGET, 100, opts, popts), steps)
+    # the single-search form on the same image, timed the same way
+    def fast():
+        return ctx.find_quality_perceptual_fast(img, TARGET, 100, opts, popts, out=coefs_out, want_weights=False)
+
+    fast()
+    times_f, rf = timed(fast, steps)
     ms_f = sum(times_f) / len(times_f)
     pf = ctx.plan(rf[1].coefs)
 
@@ -659,6 +668,9 @@ def kernel_case(name):
             elif name == "perceptual":
                 # one perceptual search (plain search, adjoint, pullback, weighted search, two plans)
                 ctx.find_quality_perceptual(img, TARGET, 100, opts)
+            elif name == "perceptual_fast":
+                # one fast perceptual search (four-candidate probe, adjoint, pullback, weighted search)
+                ctx.find_quality_perceptual_fast(img, TARGET, 100, opts)
             elif name == "search":
                 # one search of the workload: every kernel of the timed step, once per candidate
                 ctx.find_quality_ssimulacra2(img, TARGET, 100, opts)
@@ -670,7 +682,7 @@ def kernel_case(name):
 
     run(1)
     torch.cuda.nvtx.range_push("profiled")
-    run(1 if name in ("perceptual", "search") else 2)
+    run(1 if name in ("perceptual", "perceptual_fast", "search") else 2)
     torch.cuda.nvtx.range_pop()
 
 
@@ -685,7 +697,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the many-image batch measurement")
     ap.add_argument("--no-requant", action="store_true", help="skip the JPEG->JPEG search measurement")
     ap.add_argument("--no-perceptual", action="store_true", help="skip the perceptual trellis measurement")
-    ap.add_argument("--kernel-case", choices=["plan", "ssim", "ssim2", "ssim2_batch", "perceptual", "search"],
+    ap.add_argument("--kernel-case", choices=["plan", "ssim", "ssim2", "ssim2_batch", "perceptual", "perceptual_fast",
+                                              "search"],
                     default=None,
                     help="profiling aid: run only a few calls of one workload at --width x --height, print nothing")
     ap.add_argument("--width", type=int, default=W, help="smaller cases for profiling only; the bench line uses 4000")

@@ -355,6 +355,15 @@ def _opts(o):
     return _Opts(int(o.quality), int(o.subsampling), 1 if o.trellis else 0)
 
 
+def _out_buffer(arr, dtype, n):
+    """A caller's reusable output array (checked) or a new one of n entries."""
+    if arr is None:
+        return np.zeros(n, dtype=dtype)
+    if arr.dtype != dtype or arr.size < n or not arr.flags.c_contiguous:
+        raise ValueError(f"the buffer must be a contiguous {np.dtype(dtype).name} array of at least {n} entries")
+    return arr
+
+
 def _image(img):
     """(data, w, h, channels, depth) of an image array, C-contiguous."""
     a = np.ascontiguousarray(img)
@@ -681,14 +690,16 @@ class Context:
         trace = [(int(f.trace_q[i]), float(f.trace_score[i])) for i in range(f.nsteps)]
         return Found(int(f.quality), float(f.score), _coef_image(w, h, lay, coefs, qt), trace)
 
-    def find_quality_perceptual(self, reference, target, max_quality=100, opts=None, popts=None):
-        """rcg_search_perceptual: plain search, gradient at its result, weighted search, planned sizes of both."""
+    def find_quality_perceptual(self, reference, target, max_quality=100, opts=None, popts=None, out=None,
+                                weights_out=None, want_weights=True):
+        """rcg_search_perceptual: plain search, gradient at its result, weighted search, planned sizes of both.
+        `out`, `weights_out` and `want_weights` as in find_quality_perceptual_fast."""
         opts = opts or EncodeOptions()
         popts = popts or PerceptualOptions()
         a, w, h, c, d = _image(reference)
         lay = self.coef_layout(w, h, c, EncodeOptions(50, opts.subsampling, opts.trellis))
-        coefs = np.zeros(lay.ncoefs, dtype=np.int16)
-        wts = np.zeros(lay.ncoefs, dtype=np.float32)
+        coefs = _out_buffer(out, np.int16, lay.ncoefs)
+        wts = _out_buffer(weights_out, np.float32, lay.ncoefs) if want_weights else None
         qt = np.zeros((2, 64), dtype=np.uint8)
         fp, ff = _Found(), _Found()
         sizes = (ctypes.c_uint64 * 2)()
@@ -697,37 +708,47 @@ class Context:
         self._check(_lib.rcg_search_perceptual(self._ptr, a.ctypes.data, w, h, c, float(target), int(max_quality),
                                                ctypes.byref(o), ctypes.byref(po), ctypes.byref(fp),
                                                ctypes.byref(ff), sizes, ctypes.byref(chose), coefs.ctypes.data,
-                                               coefs.size, qt.ctypes.data, wts.ctypes.data, wts.size))
+                                               coefs.size, qt.ctypes.data, wts.ctypes.data if wts is not None else None,
+                                               wts.size if wts is not None else 0))
 
         def found(f, ci):
             return Found(int(f.quality), float(f.score), ci,
                          [(int(f.trace_q[i]), float(f.trace_score[i])) for i in range(f.nsteps)])
 
-        return PerceptualFound(found(fp, None), found(ff, _coef_image(w, h, lay, coefs, qt)), int(sizes[0]),
-                               int(sizes[1]), bool(chose.value), wts)
+        return PerceptualFound(found(fp, None), found(ff, _coef_image(w, h, lay, coefs[: lay.ncoefs], qt)),
+                               int(sizes[0]), int(sizes[1]), bool(chose.value),
+                               wts[: lay.ncoefs] if wts is not None else None)
 
-    def find_quality_perceptual_fast(self, reference, target, max_quality=100, opts=None, popts=None):
+    def find_quality_perceptual_fast(self, reference, target, max_quality=100, opts=None, popts=None, out=None,
+                                     weights_out=None, want_weights=True):
         """rcg_search_perceptual_fast: a four-candidate plain probe, the gradient at its best candidate, one
-        weighted search. Returns (probe Found without coefficients, weighted Found, weights)."""
+        weighted search. Returns (probe Found without coefficients, weighted Found, weights).
+
+        `out` / `weights_out` (optional): reusable int16 / float32 arrays of at least coef_capacity() entries that
+        receive the coefficients / weights (the returned Found and weights are views of them); want_weights=False
+        passes no weights buffer (the library then copies none back) and returns None for them."""
         opts = opts or EncodeOptions()
         popts = popts or PerceptualOptions()
         a, w, h, c, d = _image(reference)
         lay = self.coef_layout(w, h, c, EncodeOptions(50, opts.subsampling, opts.trellis))
-        coefs = np.zeros(lay.ncoefs, dtype=np.int16)
-        wts = np.zeros(lay.ncoefs, dtype=np.float32)
+
+        coefs = _out_buffer(out, np.int16, lay.ncoefs)
+        wts = _out_buffer(weights_out, np.float32, lay.ncoefs) if want_weights else None
         qt = np.zeros((2, 64), dtype=np.uint8)
         fp, ff = _Found(), _Found()
         o, po = _opts(opts), popts._c()
         self._check(_lib.rcg_search_perceptual_fast(self._ptr, a.ctypes.data, w, h, c, float(target),
                                                     int(max_quality), ctypes.byref(o), ctypes.byref(po),
                                                     ctypes.byref(fp), ctypes.byref(ff), coefs.ctypes.data, coefs.size,
-                                                    qt.ctypes.data, wts.ctypes.data, wts.size))
+                                                    qt.ctypes.data, wts.ctypes.data if wts is not None else None,
+                                                    wts.size if wts is not None else 0))
 
         def found(f, ci):
             return Found(int(f.quality), float(f.score), ci,
                          [(int(f.trace_q[i]), float(f.trace_score[i])) for i in range(f.nsteps)])
 
-        return found(fp, None), found(ff, _coef_image(w, h, lay, coefs, qt)), wts
+        return (found(fp, None), found(ff, _coef_image(w, h, lay, coefs[: lay.ncoefs], qt)),
+                wts[: lay.ncoefs] if wts is not None else None)
 
     def reconstruct(self, ci):
         """jpeg/src/decode.rs:334: the pixels a viewer would show (Gray (h, w) or Rgb (h, w, 3) uint8)."""
