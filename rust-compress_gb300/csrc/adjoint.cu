@@ -125,55 +125,114 @@ dim3 grid_rows(int w, int h, int planes) {
   return dim3((unsigned)((w + 255) / 256), (unsigned)std::min(h, 65535), (unsigned)planes);
 }
 
+// Outputs per thread of the row blurs: a run of kHRun consecutive outputs reads its kHRun + 10 source samples once
+// (in registers) instead of 11 per output; every output still sums its in-range taps in the same order.
+constexpr int kHRun = 4;
+
+// The row blurs' grid: (column runs / 256, rows, planes).
+dim3 grid_row_runs(int w, int h, int planes) {
+  return dim3((unsigned)(((w + kHRun - 1) / kHRun + 255) / 256), (unsigned)std::min(h, 65535), (unsigned)planes);
+}
+
 // Row blur (zero outside) of one plane: the backward pass's rows (the zero-padded row blur is its own transpose).
 // One plane per grid z.
 template <typename T>
 __global__ void k_hblur(const T* __restrict__ src, int w, int h, T* __restrict__ dst) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= w) return;
+  const int x0 = (blockIdx.x * blockDim.x + threadIdx.x) * kHRun;
+  if (x0 >= w) return;
   const long long n = (long long)w * h;
   const T* sp = src + blockIdx.z * n;
   T* dp = dst + blockIdx.z * n;
   for (int y = blockIdx.y; y < h; y += gridDim.y) {
     const T* row = sp + (long long)y * w;
-    T s = 0;
+    T v[kHRun + 2 * kR];
 #pragma unroll
-    for (int t = 0; t <= 2 * kR; t++) {
-      const int xx = x + t - kR;
-      if (xx < 0 || xx >= w) continue;
-      s += tap<T>(t) * row[xx];
+    for (int k = 0; k < kHRun + 2 * kR; k++) {
+      const int xx = x0 + k - kR;
+      v[k] = xx >= 0 && xx < w ? row[xx] : (T)0;
     }
-    dp[(long long)y * w + x] = s;
+#pragma unroll
+    for (int o = 0; o < kHRun; o++) {
+      const int x = x0 + o;
+      if (x >= w) break;
+      T s = 0;
+#pragma unroll
+      for (int t = 0; t <= 2 * kR; t++) {
+        const int xx = x + t - kR;
+        if (xx < 0 || xx >= w) continue;
+        s += tap<T>(t) * v[o + t];
+      }
+      dp[(long long)y * w + x] = s;
+    }
   }
+}
+
+// A thread's run of kHRun outputs in each of the five planes: one 16-byte store per plane (two for double) when the
+// run lies in the row and the planes are 4-sample aligned, else one store per output.
+template <typename T>
+__device__ __forceinline__ void store_run5(T* __restrict__ dst, long long n, long long rowi, int x0, int w,
+                                           const T (&out)[5][kHRun]) {
+  static_assert(kHRun == 4, "vector stores of four samples");
+  const long long i = rowi + x0;
+  if (x0 + kHRun <= w && (w & 3) == 0 && ((uintptr_t)dst & 31) == 0) {
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+      if constexpr (sizeof(T) == 4) {
+        *reinterpret_cast<float4*>(dst + q * n + i) = make_float4(out[q][0], out[q][1], out[q][2], out[q][3]);
+      } else {
+        reinterpret_cast<double2*>(dst + q * n + i)[0] = make_double2(out[q][0], out[q][1]);
+        reinterpret_cast<double2*>(dst + q * n + i)[1] = make_double2(out[q][2], out[q][3]);
+      }
+    }
+    return;
+  }
+#pragma unroll
+  for (int o = 0; o < kHRun; o++)
+    if (x0 + o < w)
+#pragma unroll
+      for (int q = 0; q < 5; q++) dst[q * n + i + o] = out[q][o];
 }
 
 // The five products of the forward pass blurred along rows in one sweep: dst + q * n for q = 0 xa, 1 xb, 2 xa^2,
 // 3 xb^2, 4 xa xb (each output summed over the taps in the same order as k_hblur).
 template <typename T>
 __global__ void k_hblur5(const T* __restrict__ xa, const T* __restrict__ xb, int w, int h, T* __restrict__ dst) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= w) return;
+  const int x0 = (blockIdx.x * blockDim.x + threadIdx.x) * kHRun;
+  if (x0 >= w) return;
   const long long n = (long long)w * h;
   for (int y = blockIdx.y; y < h; y += gridDim.y) {
-    const long long i = (long long)y * w + x;
-    T s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0;
+    const long long rowi = (long long)y * w;
+    T va[kHRun + 2 * kR], vb[kHRun + 2 * kR];
 #pragma unroll
-    for (int t = 0; t <= 2 * kR; t++) {
-      const int xx = x + t - kR;
-      if (xx < 0 || xx >= w) continue;
-      const long long j = (long long)y * w + xx;
-      const T a = xa[j], b = xb[j], k = tap<T>(t);
-      s0 += k * a;
-      s1 += k * b;
-      s2 += k * (a * a);
-      s3 += k * (b * b);
-      s4 += k * (a * b);
+    for (int k = 0; k < kHRun + 2 * kR; k++) {
+      const int xx = x0 + k - kR;
+      const bool in = xx >= 0 && xx < w;
+      va[k] = in ? xa[rowi + xx] : (T)0;
+      vb[k] = in ? xb[rowi + xx] : (T)0;
     }
-    dst[i] = s0;
-    dst[n + i] = s1;
-    dst[2 * n + i] = s2;
-    dst[3 * n + i] = s3;
-    dst[4 * n + i] = s4;
+    T out[5][kHRun];
+#pragma unroll
+    for (int o = 0; o < kHRun; o++) {
+      const int x = x0 + o;
+      T s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0;
+#pragma unroll
+      for (int t = 0; t <= 2 * kR; t++) {
+        const int xx = x + t - kR;
+        if (xx < 0 || xx >= w) continue;
+        const T a = va[o + t], b = vb[o + t], k = tap<T>(t);
+        s0 += k * a;
+        s1 += k * b;
+        s2 += k * (a * a);
+        s3 += k * (b * b);
+        s4 += k * (a * b);
+      }
+      out[0][o] = s0;
+      out[1][o] = s1;
+      out[2][o] = s2;
+      out[3][o] = s3;
+      out[4][o] = s4;
+    }
+    store_run5(dst, n, rowi, x0, w, out);
   }
 }
 
@@ -482,7 +541,7 @@ int grad_impl(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, int w, in
   // forward: the moments and map sums of every scale
   auto moments = [&](int s, int c) {
     const long long n = sc[s].n;
-    RCG_LAUNCH(ctx, "adj_hblur5", k_hblur5<T>, grid_rows(sc[s].w, sc[s].h, 1), 256, 0, xa + c * n, xb + c * n,
+    RCG_LAUNCH(ctx, "adj_hblur5", k_hblur5<T>, grid_row_runs(sc[s].w, sc[s].h, 1), 256, 0, xa + c * n, xb + c * n,
                sc[s].w, sc[s].h, hb5);
     RCG_LAUNCH(ctx, "adj_vblur", k_vblur_n<T>, grid_rows(sc[s].w, (sc[s].h + kRun - 1) / kRun, 5), 256, 0, hb5,
                sc[s].w, sc[s].h, mom);
@@ -554,7 +613,7 @@ int grad_impl(rcg_ctx* ctx, const uint8_t* d_ref, const float* d_dist, int w, in
       // the three gradient planes through the transposed column blur, then the row blur (its own transpose)
       RCG_LAUNCH(ctx, "adj_vblur_t", k_vblur_t<T>, grid_rows(sc[s].w, (sc[s].h + kRun - 1) / kRun, 3), 256, 0, gq,
                  sc[s].w, sc[s].h, hb5);
-      RCG_LAUNCH(ctx, "adj_hblur", k_hblur<T>, grid_rows(sc[s].w, sc[s].h, 3), 256, 0, hb5, sc[s].w, sc[s].h, tq);
+      RCG_LAUNCH(ctx, "adj_hblur", k_hblur<T>, grid_row_runs(sc[s].w, sc[s].h, 3), 256, 0, hb5, sc[s].w, sc[s].h, tq);
       RCG_LAUNCH(ctx, "adj_combine", k_combine<T>, grid_of(n), 256, 0, tq, tq + n, tq + 2 * n, xa + c * n,
                  xb + c * n, n, gx + c * n);
     }
