@@ -341,12 +341,14 @@ __global__ void __launch_bounds__(256) k_maps(const T* __restrict__ mom, const T
     acc[4] += det;
     acc[5] += (det * det) * (det * det);
   }
+  // Warp sums in T (the FP32 pass keeps its shuffles off this part's narrow FP64 pipe, which otherwise took half
+  // of each launch), then f64 across the warps and CTAs in a fixed order.
 #pragma unroll
   for (int k = 0; k < 6; k++) {
-    double v = (double)acc[k];
+    T v = acc[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
+    if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = (double)v;
   }
   __syncthreads();
   if (threadIdx.x < 6) {
