@@ -147,8 +147,8 @@ int rcg_ctx_band_chunks(rcg_ctx* ctx, uint32_t width, uint32_t height);
  * recomputes everything per candidate (core/src/ssimulacra2.rs:339-452 from jpeg/src/target.rs:29-56). The
  * scorer's blurred reference-only moments depend on the reference image alone, so a search's first candidate stores
  * them (24 KB per 32x32 chunk of the scorer's layout: about 2x the reference's f32 pyramid, 388 MB at 12 MP, in the
- * context's workspace) and the later candidates read them instead of blurring them: 609 against 652 us per 12 MP
- * candidate score, 680 for the first. Scores are the same bits either way. Off: nothing is stored or allocated. */
+ * context's workspace) and the later candidates read them instead of blurring them: 547 against 585 us per 12 MP
+ * candidate score, 613 for the first. Scores are the same bits either way. Off: nothing is stored or allocated. */
 int rcg_ctx_set_ref_cache(rcg_ctx* ctx, int on);
 /* Kernels this context has launched so far (each kernel launch counts once). */
 uint64_t rcg_ctx_launch_count(const rcg_ctx* ctx);

@@ -47,13 +47,24 @@ constexpr double kM12 = 0.078, kM10 = 0.23, kM11 = 1.0 - kM12 - kM10;
 constexpr double kM20 = 0.2434226892454782, kM21 = 0.2047674442449682, kM22 = 1.0 - kM20 - kM21;
 constexpr double kBias = 0.0037930732552754493;
 
-// Cube root of x > 0 as 2^(log2(x) / 3) with the hardware's approximate log2 and exp2 (a few ulp).
+// Cube root of x > 0 as 2^(log2(x) / 3) with the hardware's approximate log2 and exp2 (a few ulp). The flush-to-zero
+// forms: every argument here is at least the opsin bias (0.0038) and every result at least its cube root, so no
+// subnormal can occur, and the forms without .ftz only add a range check and rescaling around each operation
+// (measured: the tile kernel 608 -> 556 us per 12 MP score with these and the division below).
 __device__ __forceinline__ float cbrt_fast(float x) {
   float l, y;
-  asm("lg2.approx.f32 %0, %1;" : "=f"(l) : "f"(x));
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(l) : "f"(x));
   l *= (1.0f / 3.0f);
-  asm("ex2.approx.f32 %0, %1;" : "=f"(y) : "f"(l));
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(l));
   return y;
+}
+
+// a / b as a * approximate(1 / b) (2 ulp), flush-to-zero form; the divisors below are normal and well inside the
+// range where the reciprocal is defined.
+__device__ __forceinline__ float fdiv_ftz(float a, float b) {
+  float r;
+  asm("div.approx.ftz.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
 }
 
 // x^2 + x*y + y^2: cbrt(u) - cbrt(v) = (u - v) / D(cbrt(u), cbrt(v)).
@@ -61,7 +72,7 @@ __device__ __forceinline__ float dsq(float x, float y) { return fmaf(x, x, fmaf(
 
 // q_a/D_a - q_b/D_b without cancellation: (dq*D_b - q_b*dD) / (D_a*D_b), dq = q_a - q_b and dD = D_a - D_b given.
 __device__ __forceinline__ float qdiff(float qb, float dq, float Da, float Db, float dD) {
-  return __fdividef(fmaf(dq, Db, -qb * dD), Da * Db);
+  return fdiv_ftz(fmaf(dq, Db, -qb * dD), Da * Db);
 }
 
 // One pixel of the tile: the reference image's XYB minus the tile offsets (`a`, core/src/ssimulacra2.rs:249-258)
@@ -97,13 +108,13 @@ __device__ __forceinline__ Pix pix(float ra, float ga, float ba, float rb, float
   float D01b = dsq(cb[0], cb[1]), D20b = dsq(cb[2], cb[0]), D21b = dsq(cb[2], cb[1]);
   Pix o;
   float ya = 0.5f * (ca[0] + ca[1]);
-  o.a[0] = fmaf(7.0f, __fdividef(q01a, D01a), 0.42f - oa[0]);
+  o.a[0] = fmaf(7.0f, fdiv_ftz(q01a, D01a), 0.42f - oa[0]);
   o.a[1] = (ya - cbrt_bias) + (0.01f - oa[1]);
-  o.a[2] = 0.5f * (__fdividef(q20a, D20a) + __fdividef(q21a, D21a)) + (0.55f - oa[2]);
+  o.a[2] = 0.5f * (fdiv_ftz(q20a, D20a) + fdiv_ftz(q21a, D21a)) + (0.55f - oa[2]);
   float dr = ra - rb, dg = ga - gb, db = ba - bb;
-  float dc0 = __fdividef(fmaf(M00, dr, fmaf(M01, dg, M02 * db)), dsq(ca[0], cb[0]));
-  float dc1 = __fdividef(fmaf(M10, dr, fmaf(M11, dg, M12 * db)), dsq(ca[1], cb[1]));
-  float dc2 = __fdividef(fmaf(M20, dr, fmaf(M21, dg, M22 * db)), dsq(ca[2], cb[2]));
+  float dc0 = fdiv_ftz(fmaf(M00, dr, fmaf(M01, dg, M02 * db)), dsq(ca[0], cb[0]));
+  float dc1 = fdiv_ftz(fmaf(M10, dr, fmaf(M11, dg, M12 * db)), dsq(ca[1], cb[1]));
+  float dc2 = fdiv_ftz(fmaf(M20, dr, fmaf(M21, dg, M22 * db)), dsq(ca[2], cb[2]));
   // D(x, y) of image a minus of image b: dx (xa + xb) + dx ya + xb dy + dy (ya + yb)
   float dD01 = fmaf(dc0, ca[0] + cb[0], fmaf(dc0, ca[1], fmaf(cb[0], dc1, dc1 * (ca[1] + cb[1]))));
   float dD20 = fmaf(dc2, ca[2] + cb[2], fmaf(dc2, ca[0], fmaf(cb[2], dc0, dc0 * (ca[0] + cb[0]))));
@@ -140,7 +151,7 @@ constexpr size_t kTileSmem = (size_t)(6 * kIH * kIW + 5 * kIH * kTileW) * sizeof
 // with this one (its top halo and first output rows) move to the top of the buffer instead of being converted to XYB
 // again, so a band pays the vertical halo's XYB once: 42 x (32 nch + 10) conversions for 32 x 32 nch outputs where
 // nch separate tiles pay 42 x 42 x nch. The blurs run the moment pairs that share a tap weight ((a', d'),
-// (a'^2, b'^2)) as packed two-lane f32 FMAs, each lane exactly fmaf, so the results are those of scalar FMAs in the
+// (a'^2, d'^2)) as packed two-lane f32 FMAs, each lane exactly fmaf, so the results are those of scalar FMAs in the
 // same order.
 // Offsets: every chunk takes the XYB and XYB difference at its own centre, as a 32 x 32 tile does; the carried rows
 // are re-offset by the change (one f32 subtraction each). With nch = 1 the band is exactly the single tile.
@@ -149,14 +160,14 @@ constexpr size_t kTileSmem = (size_t)(6 * kIH * kIW + 5 * kIH * kTileW) * sizeof
 // Reference moments (kRef). The offsets a chunk subtracts come from the reference alone (its XYB at the chunk
 // centre), so the blurred a' and a'^2 of every output pixel depend on the reference and the band layout only. A
 // search scores every candidate against one reference: its first candidate runs kRef = kRefWrite, which also stores
-// (blur a', blur a'^2) per output pixel and channel; the later ones run kRef = kRefRead, which blur only (d', b'^2)
-// as a packed pair and d'^2, and read the other two. Each blurred moment is the same chain of per-lane fmaf in every
+// (blur a', blur a'^2) per output pixel and channel; the later ones run kRef = kRefRead, which blur only (b'^2, d'^2)
+// as a packed pair and d', and read the other two. Each blurred moment is the same chain of per-lane fmaf in every
 // mode, so the scores are bit-identical to kRefNone. The store keeps each chunk's 3 x 32 x 32 pairs contiguous
 // (24 KB, [channel][row][column]); a reading CTA asks for the whole block in L2 with one bulk prefetch per channel
-// as the chunk starts and reads it in its vertical pass. Measured per 12 MP score: 651.5 us without the store,
-// 680.0 us writing it, 608.9 us reading it (603 us with the two moments left out altogether); with the store
-// indexed like the pyramid planes and no bulk prefetch the read mode took 645 us, and staging each channel's block
-// in shared memory with cp.async 629 us.
+// as the chunk starts and reads it in its vertical pass. Measured per 12 MP score: 584.7 us without the store,
+// 612.7 us writing it, 547.0 us reading it (before the flush-to-zero forms and packed squares: 651.5 / 680.0 /
+// 608.9, and 603 us with the two moments left out altogether); with the store indexed like the pyramid planes and
+// no bulk prefetch the read mode took 645 us, and staging each channel's block in shared memory with cp.async 629.
 
 template <int kRef>
 __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, const float* __restrict__ ref,
@@ -271,7 +282,11 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
           float2 v = xs[k * kIH * kIW + (r + kTileH) * kIW + c];
           // inside the image the stored values move with the offsets; outside they stay 0 (the zero border)
           const int gy = mirror_row(y0 - kRadius + r, h), gxx = x0 - kRadius + c;
-          if (gy >= 0 && gxx >= 0 && gxx < w) v = make_float2(v.x - da[k], v.y - dd[k]);
+          if (gy >= 0 && gxx >= 0 && gxx < w) {
+            const float dak = k == 0 ? da[0] : (k == 1 ? da[1] : da[2]);
+            const float ddk = k == 0 ? dd[0] : (k == 1 ? dd[1] : dd[2]);
+            v = make_float2(v.x - dak, v.y - ddk);
+          }
           keep[j] = v;
         }
       }
@@ -331,7 +346,8 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
       __syncthreads();  // xs complete (ch 0) / previous channel's vertical pass done with hb
       const float2* X = xs + ch * kIH * kIW;
       // Horizontal pass: kHx adjacent outputs per item; moments a', d', a'^2, b'^2 (b' = a' - d'), d'^2. The pairs
-      // (a', d') and (a'^2, b'^2) share every tap weight and run as packed two-lane FMAs (per lane exactly fmaf).
+      // (a', d') and (a'^2, d'^2) share every tap weight and run as packed two-lane FMAs (per lane exactly fmaf);
+      // the squares of a loaded (a', d') pair are one packed multiply.
       // Items: each half-warp takes 4 rows x 4 items, so its 64-bit loads (row pitch 45 pairs = 26 banks mod 32)
       // fall in distinct banks.
       for (int item = tid; item < kIHp * (kTileW / kHx); item += kTileThreads) {
@@ -340,30 +356,31 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
         if (r >= kIH) continue;
         const float2* xr = X + r * kIW + kHx * p;
         if constexpr (kRef == kRefRead) {
-          // (d', b'^2) pairs and d'^2; the first plane of hb holds (blur d', blur b'^2).
-          float2 vdb[kHx + 2 * kRadius];
-          float vdd[kHx + 2 * kRadius];
+          // (b'^2, d'^2) pairs and d'; the first plane of hb holds (blur b'^2, blur d'^2). b' replaces a' in its
+          // pair, so one packed multiply squares both.
+          float2 vsq[kHx + 2 * kRadius];
+          float vd[kHx + 2 * kRadius];
 #pragma unroll
           for (int t = 0; t < kHx + 2 * kRadius; t++) {
-            const float2 ad = xr[t];
-            const float bb = __fsub_rn(ad.x, ad.y);
-            vdb[t] = make_float2(ad.y, __fmul_rn(bb, bb));
-            vdd[t] = __fmul_rn(ad.y, ad.y);
+            float2 bd = xr[t];
+            vd[t] = bd.y;
+            bd.x = __fsub_rn(bd.x, bd.y);
+            vsq[t] = __fmul2_rn(bd, bd);
           }
           float2 m13[kHx];
           float m4[kHx];
 #pragma unroll
           for (int o = 0; o < kHx; o++) {
             float2 s13 = make_float2(0.f, 0.f);
-            float sdd = 0.f;
+            float sd = 0.f;
 #pragma unroll
             for (int t = 0; t < 2 * kRadius + 1; t++) {
               const float2 kk = g2[t <= kRadius ? t : 2 * kRadius - t];
-              s13 = __ffma2_rn(kk, vdb[o + t], s13);
-              sdd = fmaf(kk.x, vdd[o + t], sdd);
+              s13 = __ffma2_rn(kk, vsq[o + t], s13);
+              sd = fmaf(kk.x, vd[o + t], sd);
             }
             m13[o] = s13;
-            m4[o] = sdd;
+            m4[o] = sd;
           }
           float* h13 = hb + (r * kTileW + kHx * p) * 2;
           float* h4 = hb + 4 * kIH * kTileW + r * kTileW + kHx * p;
@@ -372,34 +389,35 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
           *reinterpret_cast<float4*>(h4) = make_float4(m4[0], m4[1], m4[2], m4[3]);
           continue;
         }
+        // Pairs (a', d') and (a'^2, d'^2) (one packed multiply of the loaded pair), b'^2 alone.
         float2 vad[kHx + 2 * kRadius], vsq[kHx + 2 * kRadius];
-        float vdd[kHx + 2 * kRadius];
+        float vbb[kHx + 2 * kRadius];
 #pragma unroll
         for (int t = 0; t < kHx + 2 * kRadius; t++) {
           const float2 ad = xr[t];
-          const float2 ab = make_float2(ad.x, ad.x - ad.y);
+          const float bb = __fsub_rn(ad.x, ad.y);
           vad[t] = ad;
-          vsq[t] = __fmul2_rn(ab, ab);
-          vdd[t] = ad.y * ad.y;
+          vsq[t] = __fmul2_rn(ad, ad);
+          vbb[t] = __fmul_rn(bb, bb);
         }
         float2 m01[kHx], m23[kHx];
         float m4[kHx];
 #pragma unroll
         for (int o = 0; o < kHx; o++) {
-          float2 s01 = make_float2(0.f, 0.f), s23 = make_float2(0.f, 0.f);
-          float sdd = 0.f;
+          float2 s01 = make_float2(0.f, 0.f), s24 = make_float2(0.f, 0.f);
+          float sbb = 0.f;
 #pragma unroll
           for (int t = 0; t < 2 * kRadius + 1; t++) {
             const float2 kk = g2[t <= kRadius ? t : 2 * kRadius - t];
             s01 = __ffma2_rn(kk, vad[o + t], s01);
-            s23 = __ffma2_rn(kk, vsq[o + t], s23);
-            sdd = fmaf(kk.x, vdd[o + t], sdd);
+            s24 = __ffma2_rn(kk, vsq[o + t], s24);
+            sbb = fmaf(kk.x, vbb[o + t], sbb);
           }
           m01[o] = s01;
-          m23[o] = s23;
-          m4[o] = sdd;
+          m23[o] = s24;
+          m4[o] = sbb;
         }
-        // hb: two planes of (moment 0, moment 1) and (moment 2, moment 3) pairs, then moment 4
+        // hb: two planes of (moment 0, moment 1) and (moment 2, moment 4) pairs, then moment 3
         float* h01 = hb + (r * kTileW + kHx * p) * 2;
         float* h23 = hb + (kIH * kTileW + r * kTileW + kHx * p) * 2;
         float* h4 = hb + 4 * kIH * kTileW + r * kTileW + kHx * p;
@@ -415,7 +433,7 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
       float2* rrow = nullptr;  // this thread's row 0 in the chunk's block
       if constexpr (kRef != kRefNone) rrow = rchunk + (ch * kTileH + rg * 4) * kTileW + col;
       if constexpr (kRef == kRefRead) {
-        // The reference moments first (their loads overlap the blur), then (blur d', blur b'^2) and blur d'^2.
+        // The reference moments first (their loads overlap the blur), then (blur b'^2, blur d'^2) and blur d'.
 #pragma unroll
         for (int o = 0; o < 4; o++) {
           float2 rm = make_float2(0.f, 0.f);
@@ -443,9 +461,9 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
             a13 = __ffma2_rn(kk, v13[o + t], a13);
             a4 = fmaf(kk.x, v4[o + t], a4);
           }
-          mu[1][o] = a13.x;
-          mu[3][o] = a13.y;
-          mu[4][o] = a4;
+          mu[3][o] = a13.x;
+          mu[4][o] = a13.y;
+          mu[1][o] = a4;
         }
       } else {
         const float2* h01 = reinterpret_cast<const float2*>(hb);
@@ -474,8 +492,8 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
           mu[0][o] = a01.x;
           mu[1][o] = a01.y;
           mu[2][o] = a23.x;
-          mu[3][o] = a23.y;
-          mu[4][o] = a4;
+          mu[4][o] = a23.y;
+          mu[3][o] = a4;
           if constexpr (kRef == kRefWrite) {
             if (gx < w && y0 + rg * 4 + o < h) rrow[o * kTileW] = make_float2(a01.x, a23.x);
           }
@@ -506,7 +524,7 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
           // 1 - (1 - dmu^2) num_s / denom_s since num_s = denom_s - sigma_(a-b)^2.
           float den = (v1 + v2) + 0.0009f;
           float num_s = den - vd;
-          float d = fmaxf(__fdividef(fmaf(dmu * dmu, num_s, vd), den), 0.0f);
+          float d = fmaxf(fdiv_ftz(fmaf(dmu * dmu, num_s, vd), den), 0.0f);
           // Edge maps (:431-433): d1 = (|r2| - |r1|) / (1 + |r1|) with r1 = a - mu1, r2 = b - mu2 = r1 - rd.
           const float2 c0 = X[(ry + kRadius) * kIW + col + kRadius];
           float a0 = c0.x, d0 = c0.y;
@@ -515,8 +533,10 @@ __device__ __forceinline__ void ssim2_band(const ScaleDesc sd, const int local, 
             r1 = fmaf(ca, omk, r1);
             rd = fmaf(cd, omk, rd);
           }
+          // t is 0 (then so is the numerator) or far above the subnormal range: the residuals are differences of
+          // f32 values of order 1e-3..1 and their blurs, so the flush-to-zero division sees a normal divisor.
           float t = fabsf(r1 - rd) + fabsf(r1);
-          float d1 = t > 0.0f ? __fdividef(-rd * (2.0f * r1 - rd), t * (1.0f + fabsf(r1))) : 0.0f;
+          float d1 = t > 0.0f ? fdiv_ftz(-rd * (2.0f * r1 - rd), t * (1.0f + fabsf(r1))) : 0.0f;
           float art = fmaxf(d1, 0.0f), det = fmaxf(-d1, 0.0f);
           float d2 = d * d, a2 = art * art, e2 = det * det;
           acc[0] += d;
