@@ -795,7 +795,8 @@ def main():
         step_device()
     prof = {}
     for k in ("ssim2_tiles_cached", "ssim2_tiles_store", "ssim2_tiles", "trellis", "quantize", "dequant_idct",
-              "upsample_color", "pyramid", "ssim2_reduce", "rate_tables", "step_tables", "fdct_cache", "color_pad",
+              "upsample_color", "pyramid", "upsample_pyramid", "ssim2_reduce", "rate_tables", "step_tables",
+              "fdct_cache", "color_pad",
               "chroma_down", "to_linear"):
         n, ms = ctx.kernel_time(k)
         prof[k] = {"launches": n, "ms": ms}

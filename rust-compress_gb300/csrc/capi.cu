@@ -1187,7 +1187,15 @@ struct SearchScorer {
   const uint8_t* ref_px = nullptr;
   uint8_t* cand_px = nullptr;
   double* d_score = nullptr;
+  bool fuse420 = false;  // every candidate has the 4:2:0 layout of upsample_pyramid (set by the search's setup)
 };
+
+// Whether a host-side layout is the 4:2:0 case of upsample_pyramid.
+static bool layout_fast420(const StepDesc* st, int w) {
+  const CompDesc& c0 = st->comp[0];
+  return st->ncomp == 3 && st->hmax == 2 && st->vmax == 2 && c0.h == 2 && c0.v == 2 && st->comp[1].h == 1 &&
+         st->comp[1].v == 1 && st->comp[2].h == 1 && st->comp[2].v == 1 && w % 4 == 0;
+}
 
 // Every buffer the per-candidate scoring uses is allocated here, before the step loop: the loop itself never
 // allocates (it may be captured as a graph, and a failed allocation inside it would go unnoticed).
@@ -1223,8 +1231,12 @@ static void score_candidate(rcg_ctx* ctx, const SearchScorer& sc, StepDesc* d_st
     ssim_score(ctx, sc.ref_px, sc.cand_px, w, h, channels, sc.d_score, d_ss, d_st);
     return;
   }
-  upsample_color(ctx, d_st, planes, w, h, nullptr, sc.dist_pyr);
-  build_pyramid_gated(ctx, sc.pd, sc.dist_pyr, d_st);
+  if (sc.fuse420) {
+    upsample_pyramid(ctx, d_st, planes, w, h, sc.pd, sc.dist_pyr);
+  } else {
+    upsample_color(ctx, d_st, planes, w, h, nullptr, sc.dist_pyr);
+    build_pyramid_gated(ctx, sc.pd, sc.dist_pyr, d_st);
+  }
   score_pyramids(ctx, sc.pd, sc.ref_pyr, sc.dist_pyr, sc.d_score, d_ss, d_st, sc.ref_moments,
                  s == 0 ? kRefWrite : kRefRead);
 }
@@ -1285,6 +1297,9 @@ static int search_prepare(rcg_ctx* ctx, const uint8_t* d_src, int w, int h, int 
     if ((rc = to_linear(ctx, d_src, w, h, channels, 8, sc.ref_pyr)) != RCG_OK) return rc;
     build_pyramid(ctx, sc.pd, sc.ref_pyr);
   }
+  // Every candidate of an explicit 4:2:0 colour search has the fused layout (the sampling factors of
+  // jpeg/src/encode.rs:428-439 do not depend on the quality then).
+  sc.fuse420 = metric == RCG_METRIC_SSIMULACRA2 && channels != 1 && subsampling == RCG_SUB_420 && w % 4 == 0;
   if ((rc = setup_encoder(ctx, d_src, w, h, channels, subsampling, &run->es)) != RCG_OK) return rc;
   int max_steps = 1;
   for (int span = max_q; span > 1; span = (span + 1) / 2) max_steps++;
@@ -1763,8 +1778,12 @@ static int search_requantize_impl(rcg_ctx* ctx, uint32_t width, uint32_t height,
   st->requant = 1;
   cudaMemcpyAsync(d_st, st, sizeof(StepDesc), cudaMemcpyHostToDevice, ctx->stream);
   dequant_idct(ctx, d_st, d_src, planes, nblocks);
+  // A requantized candidate keeps the source's block layout.
+  sc.fuse420 = metric == RCG_METRIC_SSIMULACRA2 && layout_fast420(st, w);
   if (metric == RCG_METRIC_SSIM) {
     upsample_color(ctx, d_st, planes, w, h, ref_px, nullptr);
+  } else if (sc.fuse420) {
+    upsample_pyramid(ctx, d_st, planes, w, h, sc.pd, sc.ref_pyr);
   } else {
     upsample_color(ctx, d_st, planes, w, h, nullptr, sc.ref_pyr);
     build_pyramid(ctx, sc.pd, sc.ref_pyr);

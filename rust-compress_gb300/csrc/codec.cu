@@ -20,6 +20,7 @@
 
 #include "rcg_internal.cuh"
 #include "huffman.cuh"
+#include "upsample420.cuh"
 
 namespace rcg {
 
@@ -790,68 +791,24 @@ __device__ __forceinline__ int up_sample(const uint8_t* p, int stride, int cw, i
   return px(x / fx, y / fy);
 }
 
-// The search's common case: 3 components at 4:2:0 with luma at full resolution, linear planes only, w % 4 == 0.
-// One thread = 4 columns x 2 rows (output rows 2j, 2j+1 of chroma row j): both rows share the near chroma row j, so three chroma rows per
-// component feed 8 pixels. Each chroma row's 4 columns (i-1 .. i+2, i = x0/2) come from two aligned 32-bit loads
-// and a funnel shift wherever no clamping applies and both words lie inside the row; the edges take the clamped
-// byte path. Same arithmetic as k_upsample_color (jpeg/src/decode.rs:1806-1818, :1438-1441).
+// The search's common case (upsample420.cuh): one thread = 4 columns x 2 rows (output rows 2j, 2j+1 of chroma row
+// j), stored as one 16-byte write per row and plane. Same arithmetic as the general path below
+// (jpeg/src/decode.rs:1806-1818, :1438-1441).
 __device__ __forceinline__ void upsample_420(const StepDesc* __restrict__ st, const uint8_t* __restrict__ planes,
                                              int w, int h, float* __restrict__ lin, const float* lut, int x0,
                                              int j) {
-  const CompDesc c0 = st->comp[0];
-  const int cstride = st->comp[1].bw * 8;
-  const int cw = (w + 1) / 2, ch = (h + 1) / 2;
-  const int i = x0 / 2;
+  float l[2][3][4];
+  upsample_420_rows(st, planes, w, h, lut, x0, j, l);
   const size_t np = (size_t)w * h;
-  // four chroma samples of one row, columns i-1 .. i+2 clamped to [0, cw-1], packed little-endian
-  auto row4 = [&](const uint8_t* r) -> uint32_t {
-    const int a = (i - 1) & ~3;
-    if (i >= 1 && i + 2 <= cw - 1 && a + 8 <= cstride) {
-      const uint32_t* q = reinterpret_cast<const uint32_t*>(r + a);  // rows start 8-byte aligned
-      return __funnelshift_r(q[0], q[1], 8 * ((i - 1) & 3));
-    }
-    uint32_t v = 0;
-#pragma unroll
-    for (int d = 0; d < 4; d++) v |= (uint32_t)r[min(max(i - 1 + d, 0), cw - 1)] << (8 * d);
-    return v;
-  };
-  const int jm = max(j - 1, 0), jp = min(j + 1, ch - 1);
-  int up[2][2][4];  // [component][row parity][column]
-#pragma unroll
-  for (int c = 0; c < 2; c++) {
-    const uint8_t* p = planes + st->comp[1 + c].plane_off;
-    const uint32_t rn = row4(p + (size_t)j * cstride), rm = row4(p + (size_t)jm * cstride),
-                   rp = row4(p + (size_t)jp * cstride);
-#pragma unroll
-    for (int par = 0; par < 2; par++) {
-      const uint32_t rf = par == 0 ? rm : rp;  // far row: j-1 for the even output row, j+1 for the odd one
-      int vert[4];
-#pragma unroll
-      for (int d = 0; d < 4; d++) vert[d] = 3 * (int)((rn >> (8 * d)) & 0xFF) + (int)((rf >> (8 * d)) & 0xFF);
-      up[c][par][0] = (3 * vert[1] + vert[0] + 8) >> 4;
-      up[c][par][1] = (3 * vert[1] + vert[2] + 7) >> 4;
-      up[c][par][2] = (3 * vert[2] + vert[1] + 8) >> 4;
-      up[c][par][3] = (3 * vert[2] + vert[3] + 7) >> 4;
-    }
-  }
 #pragma unroll
   for (int par = 0; par < 2; par++) {
     const int y = 2 * j + par;
     if (y >= h) break;
-    const uint32_t q = *reinterpret_cast<const uint32_t*>(planes + c0.plane_off + (size_t)y * (c0.bw * 8) + x0);
-    float l[3][4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const int yv = (q >> (8 * k)) & 0xFF;
-      const int cb = up[0][par][k] - 128, cr = up[1][par][k] - 128;
-      l[0][k] = lut[clampi(yv + ((91881 * cr + 32768) >> 16), 0, 255)];
-      l[1][k] = lut[clampi(yv - ((22554 * cb + 46802 * cr + 32768) >> 16), 0, 255)];
-      l[2][k] = lut[clampi(yv + ((116130 * cb + 32768) >> 16), 0, 255)];
-    }
     const size_t o = (size_t)y * w + x0;
 #pragma unroll
     for (int c = 0; c < 3; c++)
-      *reinterpret_cast<float4*>(lin + c * np + o) = make_float4(l[c][0], l[c][1], l[c][2], l[c][3]);
+      *reinterpret_cast<float4*>(lin + c * np + o) = make_float4(l[par][c][0], l[par][c][1], l[par][c][2],
+                                                                 l[par][c][3]);
   }
 }
 
@@ -868,9 +825,7 @@ __device__ __forceinline__ void upsample_color_body(const StepDesc* __restrict__
   const int ncomp = st->ncomp, hmax = st->hmax, vmax = st->vmax;
   const CompDesc c0 = st->comp[0];
   // 4:2:0 linear planes for the scorer: the two-row path, over chroma rows (half the grid's rows)
-  const bool fast420 = !rgb && lin && ncomp == 3 && hmax == 2 && vmax == 2 && c0.h == 2 && c0.v == 2 &&
-                       st->comp[1].h == 1 && st->comp[1].v == 1 && st->comp[2].h == 1 && st->comp[2].v == 1 &&
-                       w % 4 == 0;
+  const bool fast420 = !rgb && lin && layout_is_fast420(st, w);
   if (fast420 && (int)by >= (h + 1) / 2) return;
   // The sRGB table lives in shared memory: per-thread indices differ, which would serialize constant-memory reads.
   __shared__ float lut[256];

@@ -311,6 +311,10 @@ int build_pyramid(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr);
 int build_pyramid_gated(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, const StepDesc* st);
 // CTAs of one pyramid launch (k_pyramid and the work-list forms): one per scale-1 tile, 0 for a single scale.
 int pyramid_ctas(const PyramidDesc& pd);
+// upsample_color's linear planes and build_pyramid_gated in one launch, for a step whose layout is the 4:2:0 case of
+// upsample420.cuh (the caller's promise: 3 components, luma 2x2 and chroma 1x1 sampling, w % 4 == 0).
+int upsample_pyramid(rcg_ctx* ctx, StepDesc* d_step, const uint8_t* d_planes, int w, int h, const PyramidDesc& pd,
+                     float* d_pyr);
 // Reference moments of the tile kernel: kRefNone computes every blurred moment; kRefWrite also stores the
 // reference-only ones (blur a', blur a'^2) for later candidates against the same reference; kRefRead reads them
 // instead of blurring them. Same scores in every mode. The store is chunk-major: per 32x32 chunk of the banded

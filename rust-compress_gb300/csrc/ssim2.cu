@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "rcg_internal.cuh"
+#include "upsample420.cuh"
 
 namespace rcg {
 
@@ -789,13 +790,27 @@ __device__ __forceinline__ float two_sum(float a, float b, float& e) {
 // (core/src/ssimulacra2.rs:223-247) computes it: the reference sums in f64, which is exact for these inputs, then
 // rounds once to f32; the compensated sum here (TwoSum) rounds the same exact sum once, so the planes agree with the
 // reference's except in rare double-rounding cases.
+// kFresh: the plane was written earlier in the same kernel (the fused upsample + pyramid), so loads go through L2
+// (ld.global.cg) and never through the read-only data path, which need not see this kernel's own writes.
+template <bool kFresh>
+__device__ __forceinline__ float ldp(const float* p) {
+  if constexpr (kFresh) return __ldcg(p);
+  else return *p;
+}
+template <bool kFresh>
+__device__ __forceinline__ float4 ldp4(const float4* p) {
+  if constexpr (kFresh) return __ldcg(p);
+  else return *p;
+}
+
+template <bool kFresh = false>
 __device__ __forceinline__ float mean2x2(const float* p, int stride, int w, int h, int ox, int oy) {
   int x0 = ox * 2, x1 = min(ox * 2 + 2, w), y0 = oy * 2, y1 = min(oy * 2 + 2, h);
   float s = 0.0f, err = 0.0f;
   for (int y = y0; y < y1; y++)
     for (int x = x0; x < x1; x++) {
       float e;
-      s = two_sum(s, p[(size_t)y * stride + x], e);
+      s = two_sum(s, ldp<kFresh>(p + (size_t)y * stride + x), e);
       err += e;
     }
   // count is 1, 2 or 4: the scaling is exact.
@@ -829,6 +844,7 @@ __device__ __forceinline__ float quad_mean(float q0, float q1, float q2, float q
   return __fadd_rn(t, (e0 + e1) + e2) * 0.25f;
 }
 
+template <bool kFresh>
 __device__ __forceinline__ void scale1_tile(const float* __restrict__ src0, float* __restrict__ dst1,
                                             const ScaleDesc& s0, const ScaleDesc& s1, int tx, int ty,
                                             float (*out)[kPyrTH][kPyrTW + 1]) {
@@ -847,8 +863,8 @@ __device__ __forceinline__ void scale1_tile(const float* __restrict__ src0, floa
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         const float4* p = reinterpret_cast<const float4*>(src0 + c * np0 + (size_t)(2 * oy) * s0.w + 2 * ox);
-        r0[c] = p[0];
-        r1[c] = p[s0.w / 4];
+        r0[c] = ldp4<kFresh>(p);
+        r1[c] = ldp4<kFresh>(p + s0.w / 4);
       }
 #pragma unroll
       for (int c = 0; c < 3; c++) {
@@ -865,9 +881,9 @@ __device__ __forceinline__ void scale1_tile(const float* __restrict__ src0, floa
         for (int c = 0; c < 3; c++) {
           if (full) {
             const float* p = src0 + c * np0 + (size_t)(2 * oy) * s0.w + 2 * x;
-            v[j][c] = quad_mean(p[0], p[1], p[s0.w], p[s0.w + 1]);
+            v[j][c] = quad_mean(ldp<kFresh>(p), ldp<kFresh>(p + 1), ldp<kFresh>(p + s0.w), ldp<kFresh>(p + s0.w + 1));
           } else {
-            v[j][c] = mean2x2(src0 + c * np0, s0.w, s0.w, s0.h, x, oy);
+            v[j][c] = mean2x2<kFresh>(src0 + c * np0, s0.w, s0.w, s0.h, x, oy);
           }
         }
       }
@@ -901,30 +917,16 @@ __device__ __forceinline__ bool pyramid_interior(const PyramidDesc& pd, int tx, 
 // a scale-3 sample sit in one warp (a warp holds two scale-2 rows) and meet by shuffles; scales 4 and 5 (16 and 4
 // samples) go through shared memory. Every sample is quad_mean of its four sources in mean2x2's order, as the general
 // path computes it for full blocks, so the planes are the same bits.
-__device__ __forceinline__ void pyramid_tile_interior(const PyramidDesc& pd, float* __restrict__ pyr, int tx, int ty) {
+// Scales 1-5 of interior tile (tx, ty) from the thread's 2x2 block of scale 1 (v1[row][column][channel], at
+// scale-1 origin (tx * 32 + 2 (t % 16), ty * 32 + 2 (t / 16))).
+__device__ __forceinline__ void pyramid_levels_interior(const PyramidDesc& pd, float* __restrict__ pyr, int tx,
+                                                        int ty, const float (&v1)[2][2][3]) {
   static_assert(kPyrTW == 32 && kPyrTH == 32 && kPyrThreads == 256, "thread layout of the interior path");
   __shared__ float l3[3][8][8], l4[3][4][4];
-  const ScaleDesc s0 = pd.s[0], s1 = pd.s[1];
-  const size_t np0 = (size_t)s0.w * s0.h, np1 = (size_t)s1.w * s1.h;
-  const float* src0 = pyr + s0.off;
+  const ScaleDesc s1 = pd.s[1];
+  const size_t np1 = (size_t)s1.w * s1.h;
   const int t = threadIdx.x, bx = t % 16, by = t / 16;
   const int ox = tx * 32 + 2 * bx, oy = ty * 32 + 2 * by;  // scale-1 origin of the thread's 2x2 block
-  float v1[2][2][3];  // [row][column][channel]
-#pragma unroll
-  for (int r = 0; r < 2; r++) {
-    float4 a0[3], a1[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const float4* p = reinterpret_cast<const float4*>(src0 + c * np0 + (size_t)(2 * (oy + r)) * s0.w + 2 * ox);
-      a0[c] = p[0];
-      a1[c] = p[s0.w / 4];
-    }
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      v1[r][0][c] = quad_mean(a0[c].x, a0[c].y, a1[c].x, a1[c].y);
-      v1[r][1][c] = quad_mean(a0[c].z, a0[c].w, a1[c].z, a1[c].w);
-    }
-  }
   float* dst1 = pyr + s1.off;
 #pragma unroll
   for (int r = 0; r < 2; r++)
@@ -987,17 +989,43 @@ __device__ __forceinline__ void pyramid_tile_interior(const PyramidDesc& pd, flo
   }
 }
 
-// Scale-1 tile `blk` of a pyramid and every coarser tile below it.
-__device__ __forceinline__ void pyramid_tile(const PyramidDesc& pd, float* __restrict__ pyr, const int blk) {
+// Interior tile (tx, ty) from scale 0 in memory: each thread's 4x4 source block as 16-byte row loads.
+__device__ __forceinline__ void pyramid_tile_interior(const PyramidDesc& pd, float* __restrict__ pyr, int tx, int ty) {
+  const ScaleDesc s0 = pd.s[0];
+  const size_t np0 = (size_t)s0.w * s0.h;
+  const float* src0 = pyr + s0.off;
+  const int t = threadIdx.x, bx = t % 16, by = t / 16;
+  const int ox = tx * 32 + 2 * bx, oy = ty * 32 + 2 * by;
+  float v1[2][2][3];  // [row][column][channel]
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    float4 a0[3], a1[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float4* p = reinterpret_cast<const float4*>(src0 + c * np0 + (size_t)(2 * (oy + r)) * s0.w + 2 * ox);
+      a0[c] = p[0];
+      a1[c] = p[s0.w / 4];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      v1[r][0][c] = quad_mean(a0[c].x, a0[c].y, a1[c].x, a1[c].y);
+      v1[r][1][c] = quad_mean(a0[c].z, a0[c].w, a1[c].z, a1[c].w);
+    }
+  }
+  pyramid_levels_interior(pd, pyr, tx, ty, v1);
+}
+
+__device__ __forceinline__ bool pyramid_fast_tile(const PyramidDesc& pd, const float* pyr, int tx, int ty) {
+  return (pd.s[0].w & 3) == 0 && ((uintptr_t)(pyr + pd.s[0].off) & 15) == 0 && pyramid_interior(pd, tx, ty);
+}
+
+// Tile (tx, ty) by the general path: scale 1 from scale 0 in memory, then each coarser level from the one above in
+// shared memory.
+template <bool kFresh>
+__device__ __forceinline__ void pyramid_tile_general(const PyramidDesc& pd, float* __restrict__ pyr, int tx, int ty) {
   __shared__ float buf[2][3][kPyrTH][kPyrTW + 1];
   const ScaleDesc s0 = pd.s[0], s1 = pd.s[1];
-  const int tiles_x = (s1.w + kPyrTW - 1) / kPyrTW;
-  const int tx = blk % tiles_x, ty = blk / tiles_x;
-  if ((s0.w & 3) == 0 && ((uintptr_t)(pyr + s0.off) & 15) == 0 && pyramid_interior(pd, tx, ty)) {
-    pyramid_tile_interior(pd, pyr, tx, ty);
-    return;
-  }
-  scale1_tile(pyr + s0.off, pyr + s1.off, s0, s1, tx, ty, buf[0]);
+  scale1_tile<kFresh>(pyr + s0.off, pyr + s1.off, s0, s1, tx, ty, buf[0]);
   int cur = 0, tw = kPyrTW, th = kPyrTH;
   for (int L = 2; L < pd.nscales; L++) {
     __syncthreads();
@@ -1032,10 +1060,72 @@ __device__ __forceinline__ void pyramid_tile(const PyramidDesc& pd, float* __res
   }
 }
 
+// Scale-1 tile `blk` of a pyramid and every coarser tile below it.
+__device__ __forceinline__ void pyramid_tile(const PyramidDesc& pd, float* __restrict__ pyr, const int blk) {
+  const int tiles_x = (pd.s[1].w + kPyrTW - 1) / kPyrTW;
+  const int tx = blk % tiles_x, ty = blk / tiles_x;
+  if (pyramid_fast_tile(pd, pyr, tx, ty)) pyramid_tile_interior(pd, pyr, tx, ty);
+  else pyramid_tile_general<false>(pd, pyr, tx, ty);
+}
+
 __global__ void __launch_bounds__(256, 5) k_pyramid(const __grid_constant__ PyramidDesc pd, float* __restrict__ pyr,
                                                  const StepDesc* __restrict__ st) {
   if (st && !st->active) return;
   pyramid_tile(pd, pyr, blockIdx.x);
+}
+
+// A search candidate's linear planes and pyramid in one pass, for the 4:2:0 layouts of upsample420.cuh. CTA = pyramid
+// tile (tx, ty): its threads upsample the tile's 64 x 64 block of scale 0 (thread t the 4 x 4 block at columns
+// tx * 64 + 4 (t % 16), rows ty * 64 + 4 (t / 16)), write it as scale 0 for the scorer, and, on an interior tile,
+// build scale 1 from the same registers: that 4 x 4 block is exactly the source of the thread's 2 x 2 block of scale
+// 1 in the pyramid's interior path, so scale 0 is never read back (the separate kernels wrote 144 MB at 12 MP and read
+// it back from DRAM). Edge tiles read their block back through L2 after a barrier and take the general path. The
+// planes are the same bits as the decoder's upsampling kernel followed by k_pyramid.
+__global__ void __launch_bounds__(kPyrThreads, 4) k_upsample_pyramid(const StepDesc* __restrict__ st,
+                                                                    const uint8_t* __restrict__ planes, int w, int h,
+                                                                    const __grid_constant__ PyramidDesc pd,
+                                                                    float* __restrict__ pyr) {
+  if (!st->active) return;
+  __shared__ float lut[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = c_lut8s[i];
+  __syncthreads();
+  const int tiles_x = (pd.s[1].w + kPyrTW - 1) / kPyrTW;
+  const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  const int t = threadIdx.x, bx = t % 16, by = t / 16;
+  const int x0 = tx * 2 * kPyrTW + 4 * bx, j0 = ty * kPyrTH + 2 * by;  // columns x0.., chroma rows j0, j0 + 1
+  const size_t np0 = (size_t)w * h;
+  float* lin = pyr + pd.s[0].off;
+  const bool fast = pyramid_fast_tile(pd, pyr, tx, ty);
+  float v1[2][2][3];  // the interior path's scale-1 block: [row][column][channel]
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    const int j = j0 + r;
+    if (x0 >= w || 2 * j >= h) break;
+    float l[2][3][4];  // [row parity][channel][column]
+    upsample_420_rows(st, planes, w, h, lut, x0, j, l);
+#pragma unroll
+    for (int par = 0; par < 2; par++) {
+      const int y = 2 * j + par;
+      if (y >= h) break;
+#pragma unroll
+      for (int c = 0; c < 3; c++)
+        *reinterpret_cast<float4*>(lin + c * np0 + (size_t)y * w + x0) =
+            make_float4(l[par][c][0], l[par][c][1], l[par][c][2], l[par][c][3]);
+    }
+    if (fast) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        v1[r][0][c] = quad_mean(l[0][c][0], l[0][c][1], l[1][c][0], l[1][c][1]);
+        v1[r][1][c] = quad_mean(l[0][c][2], l[0][c][3], l[1][c][2], l[1][c][3]);
+      }
+    }
+  }
+  if (fast) {
+    pyramid_levels_interior(pd, pyr, tx, ty, v1);
+    return;
+  }
+  __syncthreads();  // the tile's scale 0 is written; a block's global writes are visible to it after the barrier
+  pyramid_tile_general<true>(pd, pyr, tx, ty);
 }
 
 // ------------------------------------------------------------------------------------------------ work-list scorer
@@ -1211,6 +1301,14 @@ int build_pyramid_gated(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr, const
 
 int build_pyramid(rcg_ctx* ctx, const PyramidDesc& pd, float* d_pyr) {
   return build_pyramid_gated(ctx, pd, d_pyr, nullptr);
+}
+
+int upsample_pyramid(rcg_ctx* ctx, StepDesc* d_step, const uint8_t* d_planes, int w, int h, const PyramidDesc& pd,
+                     float* d_pyr) {
+  if (pd.nscales < 2) return upsample_color(ctx, d_step, d_planes, w, h, nullptr, d_pyr + pd.s[0].off);
+  RCG_LAUNCH(ctx, "upsample_pyramid", k_upsample_pyramid, pyramid_ctas(pd), kPyrThreads, 0, d_step, d_planes, w, h,
+             pd, d_pyr);
+  return RCG_OK;
 }
 
 PyramidDesc make_pyramid(int w, int h) {
