@@ -1080,7 +1080,9 @@ __global__ void __launch_bounds__(256, 5) k_pyramid(const __grid_constant__ Pyra
 // build scale 1 from the same registers: that 4 x 4 block is exactly the source of the thread's 2 x 2 block of scale
 // 1 in the pyramid's interior path, so scale 0 is never read back (the separate kernels wrote 144 MB at 12 MP and read
 // it back from DRAM). Edge tiles read their block back through L2 after a barrier and take the general path. The
-// planes are the same bits as the decoder's upsampling kernel followed by k_pyramid.
+// planes are the same bits as the decoder's upsampling kernel followed by k_pyramid. Measured per 12 MP candidate:
+// 63.6 us converting the block as two 2-row halves, 61.0 us with all of its loads issued first (upsample_420_quad),
+// against 40.7 + 41.9 us for the two kernels; 72 us at 3 or 5 CTAs per SM.
 __global__ void __launch_bounds__(kPyrThreads, 4) k_upsample_pyramid(const StepDesc* __restrict__ st,
                                                                     const uint8_t* __restrict__ planes, int w, int h,
                                                                     const __grid_constant__ PyramidDesc pd,
@@ -1097,27 +1099,26 @@ __global__ void __launch_bounds__(kPyrThreads, 4) k_upsample_pyramid(const StepD
   float* lin = pyr + pd.s[0].off;
   const bool fast = pyramid_fast_tile(pd, pyr, tx, ty);
   float v1[2][2][3];  // the interior path's scale-1 block: [row][column][channel]
+  if (x0 < w && 2 * j0 < h) {
+    float l[4][3][4];  // [row][channel][column]
+    upsample_420_quad(st, planes, w, h, lut, x0, j0, l);
 #pragma unroll
-  for (int r = 0; r < 2; r++) {
-    const int j = j0 + r;
-    if (x0 >= w || 2 * j >= h) break;
-    float l[2][3][4];  // [row parity][channel][column]
-    upsample_420_rows(st, planes, w, h, lut, x0, j, l);
-#pragma unroll
-    for (int par = 0; par < 2; par++) {
-      const int y = 2 * j + par;
+    for (int r = 0; r < 4; r++) {
+      const int y = 2 * j0 + r;
       if (y >= h) break;
 #pragma unroll
       for (int c = 0; c < 3; c++)
         *reinterpret_cast<float4*>(lin + c * np0 + (size_t)y * w + x0) =
-            make_float4(l[par][c][0], l[par][c][1], l[par][c][2], l[par][c][3]);
+            make_float4(l[r][c][0], l[r][c][1], l[r][c][2], l[r][c][3]);
     }
     if (fast) {
 #pragma unroll
-      for (int c = 0; c < 3; c++) {
-        v1[r][0][c] = quad_mean(l[0][c][0], l[0][c][1], l[1][c][0], l[1][c][1]);
-        v1[r][1][c] = quad_mean(l[0][c][2], l[0][c][3], l[1][c][2], l[1][c][3]);
-      }
+      for (int r = 0; r < 2; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          v1[r][0][c] = quad_mean(l[2 * r][c][0], l[2 * r][c][1], l[2 * r + 1][c][0], l[2 * r + 1][c][1]);
+          v1[r][1][c] = quad_mean(l[2 * r][c][2], l[2 * r][c][3], l[2 * r + 1][c][2], l[2 * r + 1][c][3]);
+        }
     }
   }
   if (fast) {
