@@ -87,10 +87,11 @@ def test_repeated_searches_agree(ctx):
     assert a.trace == b.trace and np.array_equal(a.coefs.flat(), b.coefs.flat())
 
 
-@pytest.mark.parametrize("w,h", [(8, 8), (9, 13), (17, 33), (64, 48), (257, 9)])
+@pytest.mark.parametrize("w,h", [(8, 8), (9, 13), (17, 33), (64, 48), (257, 9), (64, 33), (132, 67)])
 def test_search_tiny_and_awkward_sizes(ctx, oracle, w, h):
     """Every column of these images is near the zero left/right border at some scale: the split scorer's border
-    corrections and the per-scale tiling are exercised on each candidate."""
+    corrections and the per-scale tiling are exercised on each candidate. Widths that are a multiple of 4 take the
+    fused upsampling + pyramid kernel (odd heights: a last chroma row with one output row; edge tiles)."""
     img = synth.image(max(w, 16), max(h, 16), 9, sensor_sigma=4.0)[:h, :w].copy()
     _compare(ctx, oracle, img, 60.0, rcg.Subsampling.S420)
 
